@@ -1,0 +1,105 @@
+/*
+ * mat_gpu.h - C ABI of libmatgpu, the GB300 (sm_103a) implementation of
+ * Mat's dense-factorization hot path: packed GEMM, blocked partial-pivoting
+ * LU (PLU), Cholesky (LLT), blocked Householder QR and the Solve calls on top
+ * of them, plus a mixed-precision (split-BF16 + iterative refinement) solve
+ * and reverse-mode (adjoint) kernels.
+ *
+ * Conventions (all entry points):
+ *   - Matrices are column-major with an explicit leading dimension, exactly
+ *     like Mat's MAT<T> / __BlockMat<T> (Mat-8.3.1/Base/__Matrix.h:141-146,
+ *     Mat-8.3.1/Base/__Block.h:3-34): element (r,c) lives at data[r + c*ld].
+ *   - Every matrix / vector pointer is a DEVICE pointer unless the parameter
+ *     name starts with "host_".  Work is enqueued on the handle's stream; the
+ *     call returns after enqueueing unless documented otherwise (calls that
+ *     report an `info` or a `report` synchronise the stream).
+ *   - Sizes are `int`, as in Mat.  Every call returns an mg_status_t; Mat
+ *     itself has no error channel (singular/non-SPD inputs fail silently,
+ *     Mat-8.3.1/LU/__PLU.h:68-71, Mat-8.3.1/LU/__LLT.h:7).
+ *   - There is no CPU fallback: without a CUDA device every compute call
+ *     returns MG_ERR_CUDA.
+ */
+#ifndef MAT_GPU_H
+#define MAT_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mg_status {
+    MG_OK = 0,
+    MG_ERR_ARG = 1,          /* bad size / null pointer / bad leading dimension   */
+    MG_ERR_CUDA = 2,         /* CUDA runtime error (no device, launch failure ...) */
+    MG_ERR_ALLOC = 3,        /* device or pinned-host allocation failed            */
+    MG_SINGULAR = 4,         /* exact zero pivot met; info = 1-based column        */
+    MG_NOT_SPD = 5,          /* non-positive Cholesky pivot; info = 1-based column */
+    MG_IR_STALLED = 6,       /* refinement did not reach the requested tolerance   */
+    MG_FALLBACK_USED = 7,    /* mixed solve fell back to GMRES-IR or the FP64 path */
+    MG_TIMEOUT = 8,          /* a bounded device-side wait gave up                 */
+    MG_ERR_UNSUPPORTED = 9   /* option not supported on this device                */
+} mg_status_t;
+
+typedef struct mg_handle_s* mg_handle_t;
+
+/* ---------------------------------------------------------------- handles */
+
+/* Creates a handle bound to the current CUDA device.  `cuda_stream` is a
+ * cudaStream_t (NULL = the legacy default stream). */
+mg_status_t mg_handle_create(mg_handle_t* out, void* cuda_stream);
+mg_status_t mg_handle_destroy(mg_handle_t h);
+mg_status_t mg_set_stream(mg_handle_t h, void* cuda_stream);
+mg_status_t mg_synchronize(mg_handle_t h);
+const char* mg_status_string(mg_status_t s);
+/* Last error text recorded on this handle (empty string if none). */
+const char* mg_get_last_error(mg_handle_t h);
+/* Number of this library's kernel launches enqueued through `h` so far. */
+uint64_t mg_launch_count(mg_handle_t h);
+
+/* ------------------------------------------------------ memory utilities
+ * For callers (C, cgo, JNI, ctypes) that do not link the CUDA runtime. */
+mg_status_t mg_device_malloc(void** out, size_t bytes);
+mg_status_t mg_device_free(void* p);
+mg_status_t mg_host_malloc_pinned(void** out, size_t bytes);
+mg_status_t mg_host_free_pinned(void* p);
+/* Asynchronous copies on the handle's stream (kind: 0 = H2D, 1 = D2H, 2 = D2D). */
+mg_status_t mg_memcpy(mg_handle_t h, void* dst, const void* src, size_t bytes, int kind);
+
+/* ------------------------------------------------------ seeded generators
+ * Counter-based, bit-identical on the host and on the device (no libm, no
+ * fused operations).  Element (r,c) of a rows x cols matrix draws stream
+ * index r*cols + c when `rowmajor_stream` != 0 (the "row-major fill" of the
+ * benchmark configurations), else r + c*rows.  Mat's own generator is
+ * time-seeded (Mat-5.1/_extra/__Random.h:2-27) and cannot be reproduced. */
+void mg_host_fill_uniform(double* host_A, int rows, int cols, int ld, uint64_t seed,
+                          double lo, double hi, int rowmajor_stream);
+void mg_host_fill_normal(double* host_A, int rows, int cols, int ld, uint64_t seed,
+                         int rowmajor_stream);
+mg_status_t mg_fill_uniform(mg_handle_t h, double* A, int rows, int cols, int ld,
+                            uint64_t seed, double lo, double hi, int rowmajor_stream);
+mg_status_t mg_fill_normal(mg_handle_t h, double* A, int rows, int cols, int ld,
+                           uint64_t seed, int rowmajor_stream);
+
+/* ------------------------------------------------------------------ GEMM
+ * C = alpha * op(A) * op(B) + beta * C, op(X) = X (trans = 0) or X^T (1).
+ * With alpha = 1, beta = 0, transA = transB = 0 this is Mat's
+ * `operator*(const MAT<t1>&, const MAT<t2>&)` for double
+ * (Mat-8.3.1/Mul/Mul.h:204-235 -> __mulAB_2, Mul.h:155-202, which zeroes C
+ * first, Mul.h:167).  With alpha = -1, beta = 1 it is the subtracting
+ * trailing update __mulAB_packed_n (Mul.h:240-263).  When beta == 0, C is
+ * not read (NaNs in C do not propagate). */
+mg_status_t mg_dgemm(mg_handle_t h, int transA, int transB, int m, int n, int k,
+                     double alpha, const double* A, int lda, const double* B, int ldb,
+                     double beta, double* C, int ldc);
+
+/* Measures the FP64 peaks of this GPU with dependent-free FMA / DMMA loops
+ * (TFLOP/s, counting an FMA as 2 flops).  Synchronises. */
+mg_status_t mg_measure_fp64_peaks(mg_handle_t h, double* dfma_tflops, double* dmma_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MAT_GPU_H */

@@ -1,0 +1,127 @@
+"""Python mirror of Mat's API for the GPU hot path, over the C ABI.
+
+Matrices are torch float64 CUDA tensors viewed column-major: a logical
+m x n matrix has strides (1, ld), exactly Mat's MAT<T> layout
+(Mat-8.3.1/Base/__Matrix.h:141-146).  ``colmajor(m, n)`` makes one and
+``as_colmajor(t)`` converts any tensor.  Every call goes through
+libmatgpu.so; nothing here computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from ._lib import MatGpuError, load
+
+_F64 = torch.float64
+
+
+def colmajor(m: int, n: int, dtype=_F64, device="cuda") -> torch.Tensor:
+    """An uninitialised m x n column-major matrix (ld = m)."""
+    return torch.empty((n, m), dtype=dtype, device=device).t()
+
+
+def as_colmajor(t: torch.Tensor, dtype=_F64, device="cuda") -> torch.Tensor:
+    """Copy of ``t`` (logical 2-D) in column-major layout on ``device``."""
+    t = t.to(device=device, dtype=dtype)
+    return t.t().contiguous().t()
+
+
+def ld_of(t: torch.Tensor) -> int:
+    if t.dim() != 2:
+        raise ValueError("expected a 2-D matrix")
+    if t.shape[0] > 1 and t.stride(0) != 1:
+        raise ValueError("matrix must be column-major (stride(0) == 1); use as_colmajor()")
+    if t.shape[1] <= 1:
+        return max(1, t.shape[0])
+    return t.stride(1)
+
+
+def _ptr(t: torch.Tensor | None) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+class Handle:
+    """Owns an mg_handle_t bound to a CUDA stream (default: torch's current stream)."""
+
+    def __init__(self, stream: torch.cuda.Stream | None = None):
+        self.lib = load()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        self._stream = s
+        h = C.c_void_p()
+        self.check(self.lib.mg_handle_create(C.byref(h), C.c_void_p(s.cuda_stream)), "mg_handle_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mg_handle_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> torch.cuda.Stream:
+        return self._stream
+
+    def check(self, status: int, what: str = ""):
+        if status != 0:
+            msg = ""
+            if getattr(self, "h", None):
+                msg = (self.lib.mg_get_last_error(self.h) or b"").decode(errors="replace")
+            raise MatGpuError(status, f"{what}: {msg}" if what else msg)
+
+    def launch_count(self) -> int:
+        return int(self.lib.mg_launch_count(self.h))
+
+    # ------------------------------------------------------------ generators
+    def fill_uniform(self, A: torch.Tensor, seed: int, lo=-1.0, hi=1.0, rowmajor_stream=True):
+        self.check(self.lib.mg_fill_uniform(self.h, _ptr(A), A.shape[0], A.shape[1], ld_of(A), seed,
+                                            lo, hi, int(rowmajor_stream)), "mg_fill_uniform")
+        return A
+
+    def fill_normal(self, A: torch.Tensor, seed: int, rowmajor_stream=True):
+        self.check(self.lib.mg_fill_normal(self.h, _ptr(A), A.shape[0], A.shape[1], ld_of(A), seed,
+                                           int(rowmajor_stream)), "mg_fill_normal")
+        return A
+
+    # ------------------------------------------------------------------ GEMM
+    def dgemm(self, A, B, C_=None, alpha=1.0, beta=0.0, transA=False, transB=False):
+        """C = alpha op(A) op(B) + beta C (Mat's operator* when alpha=1, beta=0)."""
+        m = A.shape[1] if transA else A.shape[0]
+        k = A.shape[0] if transA else A.shape[1]
+        n = B.shape[0] if transB else B.shape[1]
+        kb = B.shape[1] if transB else B.shape[0]
+        if k != kb:
+            raise ValueError(f"inner dimensions differ: {k} vs {kb}")
+        if C_ is None:
+            C_ = colmajor(m, n, device=A.device)
+            beta = 0.0
+        self.check(self.lib.mg_dgemm(self.h, int(transA), int(transB), m, n, k, alpha, _ptr(A), ld_of(A),
+                                     _ptr(B), ld_of(B), beta, _ptr(C_), ld_of(C_)), "mg_dgemm")
+        return C_
+
+    def measure_fp64_peaks(self) -> tuple[float, float]:
+        a, b = C.c_double(), C.c_double()
+        self.check(self.lib.mg_measure_fp64_peaks(self.h, C.byref(a), C.byref(b)), "mg_measure_fp64_peaks")
+        return a.value, b.value
+
+
+def host_fill_uniform(rows: int, cols: int, seed: int, lo=-1.0, hi=1.0, rowmajor_stream=True):
+    """Seeded uniform matrix on the host (numpy, column-major), bit-identical to fill_uniform."""
+    import numpy as np
+    a = np.empty((rows, cols), dtype=np.float64, order="F")
+    load().mg_host_fill_uniform(a.ctypes.data, rows, cols, max(rows, 1), seed, lo, hi, int(rowmajor_stream))
+    return a
+
+
+def host_fill_normal(rows: int, cols: int, seed: int, rowmajor_stream=True):
+    """Seeded N(0,1) matrix on the host (numpy, column-major), bit-identical to fill_normal."""
+    import numpy as np
+    a = np.empty((rows, cols), dtype=np.float64, order="F")
+    load().mg_host_fill_normal(a.ctypes.data, rows, cols, max(rows, 1), seed, int(rowmajor_stream))
+    return a

@@ -1,0 +1,155 @@
+// Handle, workspace and memory utilities of the C ABI.
+#include <cstdarg>
+#include <cstdlib>
+
+#include "mg_internal.cuh"
+
+namespace mg {
+
+mg_status_t fail(mg_handle_t h, mg_status_t s, const char* fmt, ...) {
+    if (h) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(h->last_error, sizeof(h->last_error), fmt, ap);
+        va_end(ap);
+    }
+    return s;
+}
+
+mg_status_t cuda_fail(mg_handle_t h, cudaError_t e, const char* what) {
+    return fail(h, MG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+mg_status_t ensure_ws(mg_handle_t h, size_t bytes) {
+    if (bytes <= h->ws_bytes) return MG_OK;
+    bytes = align_up(bytes + (bytes >> 3), 1 << 20);
+    if (h->ws) {
+        MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+        MG_CHECK_CUDA(h, cudaFree(h->ws));
+        h->ws = nullptr;
+        h->ws_bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&h->ws, bytes);
+    if (e != cudaSuccess) {
+        h->ws = nullptr;
+        return fail(h, MG_ERR_ALLOC, "workspace cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    h->ws_bytes = bytes;
+    return MG_OK;
+}
+
+mg_status_t ensure_hws(mg_handle_t h, size_t bytes) {
+    if (bytes <= h->hws_bytes) return MG_OK;
+    bytes = align_up(bytes, 4096);
+    if (h->hws) {
+        MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+        cudaFreeHost(h->hws);
+        h->hws = nullptr;
+        h->hws_bytes = 0;
+    }
+    cudaError_t e = cudaMallocHost(&h->hws, bytes);
+    if (e != cudaSuccess) {
+        h->hws = nullptr;
+        return fail(h, MG_ERR_ALLOC, "pinned workspace (%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    h->hws_bytes = bytes;
+    return MG_OK;
+}
+
+mg_status_t post_launch(mg_handle_t h, const char* name) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(h, MG_ERR_CUDA, "launch of %s: %s", name, cudaGetErrorString(e));
+    h->launches++;
+    return MG_OK;
+}
+
+}  // namespace mg
+
+extern "C" {
+
+mg_status_t mg_handle_create(mg_handle_t* out, void* cuda_stream) {
+    if (!out) return MG_ERR_ARG;
+    *out = nullptr;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return MG_ERR_CUDA;
+    mg_handle_t h = new (std::nothrow) mg_handle_s();
+    if (!h) return MG_ERR_ALLOC;
+    h->stream = (cudaStream_t)cuda_stream;
+    h->device = dev;
+    if (cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&h->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+            cudaSuccess) {
+        delete h;
+        return MG_ERR_CUDA;
+    }
+    *out = h;
+    return MG_OK;
+}
+
+mg_status_t mg_handle_destroy(mg_handle_t h) {
+    if (!h) return MG_ERR_ARG;
+    if (h->ws || h->hws) cudaStreamSynchronize(h->stream);
+    if (h->ws) cudaFree(h->ws);
+    if (h->hws) cudaFreeHost(h->hws);
+    delete h;
+    return MG_OK;
+}
+
+mg_status_t mg_set_stream(mg_handle_t h, void* cuda_stream) {
+    if (!h) return MG_ERR_ARG;
+    h->stream = (cudaStream_t)cuda_stream;
+    return MG_OK;
+}
+
+mg_status_t mg_synchronize(mg_handle_t h) {
+    if (!h) return MG_ERR_ARG;
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    return MG_OK;
+}
+
+const char* mg_status_string(mg_status_t s) {
+    switch (s) {
+        case MG_OK: return "MG_OK";
+        case MG_ERR_ARG: return "MG_ERR_ARG";
+        case MG_ERR_CUDA: return "MG_ERR_CUDA";
+        case MG_ERR_ALLOC: return "MG_ERR_ALLOC";
+        case MG_SINGULAR: return "MG_SINGULAR";
+        case MG_NOT_SPD: return "MG_NOT_SPD";
+        case MG_IR_STALLED: return "MG_IR_STALLED";
+        case MG_FALLBACK_USED: return "MG_FALLBACK_USED";
+        case MG_TIMEOUT: return "MG_TIMEOUT";
+        case MG_ERR_UNSUPPORTED: return "MG_ERR_UNSUPPORTED";
+    }
+    return "MG_UNKNOWN";
+}
+
+const char* mg_get_last_error(mg_handle_t h) { return h ? h->last_error : ""; }
+
+uint64_t mg_launch_count(mg_handle_t h) { return h ? h->launches : 0; }
+
+mg_status_t mg_device_malloc(void** out, size_t bytes) {
+    if (!out) return MG_ERR_ARG;
+    return cudaMalloc(out, bytes) == cudaSuccess ? MG_OK : MG_ERR_ALLOC;
+}
+
+mg_status_t mg_device_free(void* p) { return cudaFree(p) == cudaSuccess ? MG_OK : MG_ERR_CUDA; }
+
+mg_status_t mg_host_malloc_pinned(void** out, size_t bytes) {
+    if (!out) return MG_ERR_ARG;
+    return cudaMallocHost(out, bytes) == cudaSuccess ? MG_OK : MG_ERR_ALLOC;
+}
+
+mg_status_t mg_host_free_pinned(void* p) { return cudaFreeHost(p) == cudaSuccess ? MG_OK : MG_ERR_CUDA; }
+
+mg_status_t mg_memcpy(mg_handle_t h, void* dst, const void* src, size_t bytes, int kind) {
+    if (!h || (bytes && (!dst || !src))) return MG_ERR_ARG;
+    cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice
+                     : kind == 1 ? cudaMemcpyDeviceToHost
+                                 : cudaMemcpyDeviceToDevice;
+    if (bytes == 0) return MG_OK;
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(dst, src, bytes, k, h->stream));
+    return MG_OK;
+}
+
+}  // extern "C"

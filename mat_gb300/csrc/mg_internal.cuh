@@ -1,0 +1,65 @@
+// Internal definitions shared by the libmatgpu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/mat_gpu.h"
+
+struct mg_handle_s {
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    int num_sms = 0;
+    int max_smem_optin = 0;
+    // Device workspace, grown on demand (cudaMalloc) and reused across calls.
+    void* ws = nullptr;
+    size_t ws_bytes = 0;
+    // Pinned host workspace (status words read back by info-reporting calls).
+    void* hws = nullptr;
+    size_t hws_bytes = 0;
+    uint64_t launches = 0;
+    char last_error[512] = {0};
+};
+
+namespace mg {
+
+// Records a message on the handle and returns the status.
+mg_status_t fail(mg_handle_t h, mg_status_t s, const char* fmt, ...);
+
+// Translates a CUDA error into MG_ERR_CUDA with a message.
+mg_status_t cuda_fail(mg_handle_t h, cudaError_t e, const char* what);
+
+// Grows the device workspace to at least `bytes` (synchronises when it grows).
+mg_status_t ensure_ws(mg_handle_t h, size_t bytes);
+mg_status_t ensure_hws(mg_handle_t h, size_t bytes);
+
+// Checks the last launch on the handle's stream; counts it.
+mg_status_t post_launch(mg_handle_t h, const char* name);
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Internal GEMM launcher (no argument checking), used by the factorizations.
+// Computes C = alpha*op(A)*op(B) + beta*C.  `tri` = 0 full, 1 = only tiles
+// that intersect the lower triangle of C (row >= col - tile), used by the
+// Cholesky trailing update.
+mg_status_t dgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, int k,
+                         double alpha, const double* A, int lda, const double* B, int ldb,
+                         double beta, double* C, int ldc, int tri);
+
+}  // namespace mg
+
+#define MG_CHECK_CUDA(h, call)                                   \
+    do {                                                         \
+        cudaError_t _e = (call);                                 \
+        if (_e != cudaSuccess) return mg::cuda_fail(h, _e, #call); \
+    } while (0)
+
+#define MG_TRY(call)                                  \
+    do {                                              \
+        mg_status_t _s = (call);                      \
+        if (_s != MG_OK) return _s;                   \
+    } while (0)

@@ -1,0 +1,106 @@
+"""ctypes wrappers of the oracle libraries (test infrastructure only).
+
+`Oracle(lib)` wraps either the restatement (liboracle.so, prefix orc_) or the
+reference build (_ref/libmatref.so, prefix ref_) behind one numpy API; both
+take and return column-major float64 arrays."""
+from __future__ import annotations
+
+import ctypes as C
+from functools import lru_cache
+
+import numpy as np
+
+from . import build as _build
+
+_P = C.c_void_p
+
+
+def _f(a):
+    a = np.asfortranarray(a, dtype=np.float64)
+    return a
+
+
+def _p(a):
+    return a.ctypes.data_as(_P)
+
+
+class Oracle:
+    def __init__(self, path, prefix):
+        self.lib = C.CDLL(str(path))
+        self.prefix = prefix
+        self.is_ref = prefix == "ref_"
+        if not self.is_ref:
+            self.lib.orc_det.restype = C.c_double
+            for n in ("orc_dgetrf", "orc_plu", "orc_solve", "orc_llt"):
+                getattr(self.lib, n).restype = C.c_int
+        else:
+            self.lib.ref_det.restype = C.c_double
+
+    def _fn(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    def set_threads(self, n: int):
+        if not self.is_ref:
+            self.lib.orc_set_threads(int(n))
+
+    def dgemm(self, A, B):
+        A, B = _f(A), _f(B)
+        m, k = A.shape
+        n = B.shape[1]
+        Cm = np.zeros((m, n), order="F")
+        if self.is_ref:
+            self.lib.ref_dgemm(m, n, k, _p(A), _p(B), _p(Cm))
+        else:
+            self.lib.orc_dgemm(m, n, k, _p(A), max(m, 1), _p(B), max(k, 1), _p(Cm), max(m, 1))
+        return Cm
+
+    def plu(self, A):
+        """Mat PLU(A, pos, L, U): returns (pos, L, U) with A[pos] == L @ U."""
+        A = _f(A)
+        m, n = A.shape
+        pos = np.zeros(m, dtype=np.int32)
+        L = np.zeros((m, m), order="F")
+        U = np.zeros((m, n), order="F")
+        self._fn("plu")(m, n, _p(A), _p(pos), _p(L), _p(U))
+        return pos, L, U
+
+    def solve(self, A, B):
+        A, B = _f(A), _f(B)
+        n, nrhs = B.shape
+        X = np.zeros((n, nrhs), order="F")
+        self._fn("solve")(n, nrhs, _p(A), _p(B), _p(X))
+        return X
+
+    def llt(self, A):
+        A = _f(A)
+        n = A.shape[0]
+        L = np.zeros((n, n), order="F")
+        self._fn("llt")(n, _p(A), _p(L))
+        return L
+
+    def qr(self, A):
+        A = _f(A)
+        m, n = A.shape
+        Q = np.zeros((m, m), order="F")
+        R = np.zeros((m, n), order="F")
+        self._fn("qr")(m, n, _p(A), _p(Q), _p(R))
+        return Q, R
+
+    def det(self, A):
+        A = _f(A)
+        return float(self._fn("det")(A.shape[0], _p(A)))
+
+
+@lru_cache(maxsize=None)
+def restatement() -> Oracle:
+    return Oracle(_build.build_oracle(), "orc_")
+
+
+@lru_cache(maxsize=None)
+def reference() -> Oracle | None:
+    lib = _build.build_ref()
+    return Oracle(lib, "ref_") if lib else None
+
+
+def dgemm(A, B):
+    return restatement().dgemm(A, B)

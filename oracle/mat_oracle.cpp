@@ -1,0 +1,587 @@
+// ORACLE — test infrastructure only.  A CPU restatement of Mat-8.3.1's
+// algorithms for the GPU hot path (GEMM, blocked PLU, Solve_direct, blocked
+// LLT, blocked Householder QR, Det), written from the reference's behaviour,
+// with each routine citing the reference file:line it follows.  Only the
+// tests, the smoke check and the benchmark's CPU-baseline leg may load it.
+//
+// Numerics follow Mat's AVX-512 double build: every multiply-add is a fused
+// fma in the same per-element order (sequential over k for the GEMM
+// updates, Mat-8.3.1/Mul/__micro_kernel_packed_double.h:43-84; fmadd for
+// __mixed, Calculate/__AVX512_double.h:81-93), reciprocals where Mat
+// multiplies by 1/x, and the same first-index-of-max pivot rule
+// (LU/__PLU.h:67-77).  Parity with the reference itself is checked by the
+// CPU tests against oracle/_ref (the reference compiled from its headers)
+// and against the committed golden fixtures.
+//
+// All matrices are column-major with an explicit leading dimension.
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+#include <cstring>
+#include <functional>
+#include <thread>
+#include <vector>
+
+namespace {
+
+int g_threads = 1;
+
+// Block sizes of Mat's AVX-512 configuration (Mat-8.3.1/Mat.h:57-81).
+constexpr int BS_LU = 60;
+constexpr int BS_LLT = 48;
+constexpr int BS_QR = 48;
+
+inline double& at(double* A, int lda, int r, int c) { return A[r + (size_t)c * lda]; }
+
+// Runs fn(lo, hi) over [0, n) split into contiguous chunks across threads.
+void parallel_cols(int n, const std::function<void(int, int)>& fn) {
+    const int t = std::max(1, std::min(g_threads, n));
+    if (t == 1) {
+        fn(0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    const int chunk = (n + t - 1) / t;
+    for (int i = 0; i < t; ++i) {
+        const int lo = i * chunk, hi = std::min(n, lo + chunk);
+        if (lo < hi) th.emplace_back(fn, lo, hi);
+    }
+    for (auto& x : th) x.join();
+}
+
+// C(m x n) (+|-)= A(m x k) * B(k x n): per element a sequential fused chain
+// over p = 0..k-1 (Mat's micro-kernels load C and fmadd / fnmadd into it,
+// Mul/__micro_kernel_packed_double.h:14-110 and :301-398).
+void gemm_acc(int m, int n, int k, const double* A, int lda, const double* B, int ldb, double* C, int ldc,
+              bool subtract) {
+    if (m <= 0 || n <= 0 || k <= 0) return;
+    parallel_cols(n, [&](int j0, int j1) {
+        constexpr int MB = 256;
+        for (int i0 = 0; i0 < m; i0 += MB) {
+            const int i1 = std::min(m, i0 + MB);
+            for (int j = j0; j < j1; ++j) {
+                double* c = C + (size_t)j * ldc;
+                for (int p = 0; p < k; ++p) {
+                    const double b = subtract ? -B[p + (size_t)j * ldb] : B[p + (size_t)j * ldb];
+                    const double* a = A + (size_t)p * lda;
+                    for (int i = i0; i < i1; ++i) c[i] = std::fma(a[i], b, c[i]);
+                }
+            }
+        }
+    });
+}
+
+// C -= A * B^T with B given as rows (Mat's __times_A_BT_LLT, LU/__LLT.h:59-91).
+void gemm_abt_sub(int m, int n, int k, const double* A, int lda, const double* B, int ldb, double* C, int ldc) {
+    if (m <= 0 || n <= 0 || k <= 0) return;
+    parallel_cols(n, [&](int j0, int j1) {
+        for (int j = j0; j < j1; ++j) {
+            double* c = C + (size_t)j * ldc;
+            for (int p = 0; p < k; ++p) {
+                const double b = -B[j + (size_t)p * ldb];
+                const double* a = A + (size_t)p * lda;
+                for (int i = 0; i < m; ++i) c[i] = std::fma(a[i], b, c[i]);
+            }
+        }
+    });
+}
+
+// Mat's AVX-512 dot product (Calculate/__AVX512_double.h:110-133): four
+// 8-lane fused accumulators over 32-element strides, then the full 8-blocks
+// into the first, a lane-wise (a0+a1)+(a2+a3), a masked fused tail and a
+// 8 -> 4 -> 2 -> 1 horizontal reduction.
+double dot_mat(const double* a, const double* b, int len) {
+    double acc[4][8] = {{0}};
+    const int nb = len / 8;
+    int i = 0;
+    for (; i <= nb - 4; i += 4)
+        for (int q = 0; q < 4; ++q)
+            for (int l = 0; l < 8; ++l) acc[q][l] = std::fma(a[(i + q) * 8 + l], b[(i + q) * 8 + l], acc[q][l]);
+    for (; i < nb; ++i)
+        for (int l = 0; l < 8; ++l) acc[0][l] = std::fma(a[i * 8 + l], b[i * 8 + l], acc[0][l]);
+    double s[8];
+    for (int l = 0; l < 8; ++l) s[l] = (acc[0][l] + acc[1][l]) + (acc[2][l] + acc[3][l]);
+    const int rem = len - nb * 8;
+    for (int l = 0; l < rem; ++l) s[l] = std::fma(a[nb * 8 + l], b[nb * 8 + l], s[l]);
+    double h4[4], h2[2];
+    for (int l = 0; l < 4; ++l) h4[l] = s[l] + s[l + 4];
+    for (int l = 0; l < 2; ++l) h2[l] = h4[l] + h4[l + 2];
+    return h2[0] + h2[1];
+}
+
+// ---------------------------------------------------------------- TRSM
+// X(k x n) := L^{-1} X, L unit lower k x k (Mat's AVX-512 __Solve_direct_LX,
+// LU/__Base.h:95-208): 8-column blocks by four partial sums, the ragged
+// columns by column-oriented fused updates.
+void trsm_lx(int k, int n, const double* L, int ldl, double* X, int ldx) {
+    int c = 0;
+    for (; c + 8 <= n; c += 8) {
+        for (int i = 0; i < k; ++i) {
+            for (int r = 0; r < 8; ++r) {
+                double* xc = X + (size_t)(c + r) * ldx;
+                double s0 = xc[i], s1 = 0, s2 = 0, s3 = 0;
+                int j = 0;
+                for (; j + 4 <= i; j += 4) {
+                    s0 = std::fma(-L[i + (size_t)(j + 0) * ldl], xc[j + 0], s0);
+                    s1 = std::fma(-L[i + (size_t)(j + 1) * ldl], xc[j + 1], s1);
+                    s2 = std::fma(-L[i + (size_t)(j + 2) * ldl], xc[j + 2], s2);
+                    s3 = std::fma(-L[i + (size_t)(j + 3) * ldl], xc[j + 3], s3);
+                }
+                for (; j < i; ++j) s0 = std::fma(-L[i + (size_t)j * ldl], xc[j], s0);
+                xc[i] = s0 + (s1 + (s2 + s3));
+            }
+        }
+    }
+    for (; c < n; ++c) {
+        double* x = X + (size_t)c * ldx;
+        for (int i = 1; i < k; ++i) {
+            const double a = x[i - 1];
+            if (a == 0.0) continue;
+            const double* li = L + (size_t)(i - 1) * ldl;
+            for (int r = i; r < k; ++r) x[r] = std::fma(li[r], -a, x[r]);
+        }
+    }
+}
+
+// X(k x n) := U^{-1} X, U upper k x k (generic __Solve_direct_UX, LU/__Base.h:51-92).
+void trsm_ux(int k, int n, const double* U, int ldu, double* X, int ldx) {
+    for (int c = 0; c < n; ++c) {
+        double* x = X + (size_t)c * ldx;
+        for (int i = k - 1; i >= 0; --i) {
+            x[i] /= U[i + (size_t)i * ldu];
+            const double xi = x[i];
+            const double* ui = U + (size_t)i * ldu;
+            for (int r = 0; r < i; ++r) x[r] = std::fma(ui[r], -xi, x[r]);
+        }
+    }
+}
+
+// ----------------------------------------------------------------- PLU
+// Panel LU with partial pivoting on columns [r0, r0+bs) (Mat's __PLU2_piv,
+// LU/__PLU.h:54-90; with r0 = 0 and bs = all columns it is __PLU2,
+// :22-51).  Left-looking column updates, first index attaining max |a|,
+// row swaps over columns [0, r0+bs), multiplication by the reciprocal.
+// Returns the panel column at which a zero column stopped it (Mat's
+// `break`), or -1.
+int plu_panel(double* A, int lda, int m, int r0, int bs, int* pos, int* piv) {
+    for (int i = 0; i < bs; ++i) piv[i] = i;
+    for (int c = 0; c < bs; ++c) {
+        const int gc = r0 + c;
+        double* col = A + (size_t)gc * lda;
+        for (int i = 0; i < c; ++i) {
+            const int gi = r0 + i;
+            const double q = -col[gi];
+            const double* li = A + (size_t)gi * lda;
+            for (int r = gi + 1; r < m; ++r) col[r] = std::fma(li[r], q, col[r]);
+        }
+        double maxv = 0.0;
+        for (int r = gc; r < m; ++r) maxv = std::max(maxv, std::fabs(col[r]));
+        if (maxv == 0.0) {
+            piv[c] = c;
+            return c;
+        }
+        int j = gc;
+        for (int r = gc; r < m; ++r)
+            if (std::fabs(col[r]) == maxv) {
+                j = r;
+                break;
+            }
+        piv[c] = j - r0;
+        if (j != gc) {
+            for (int cc = 0; cc < r0 + bs; ++cc) std::swap(at(A, lda, gc, cc), at(A, lda, j, cc));
+            std::swap(pos[gc], pos[j]);
+        }
+        const double inv = 1.0 / col[gc];
+        for (int r = gc + 1; r < m; ++r) col[r] = col[r] * inv;
+    }
+    return -1;
+}
+
+// Applies a panel's interchanges to columns [c0, c1) (Mat's __laswp_trailing, LU/__PLU.h:3-19).
+void laswp(double* A, int lda, int r0, int kcount, int c0, int c1, const int* piv) {
+    for (int c = c0; c < c1; ++c) {
+        double* col = A + (size_t)c * lda;
+        for (int k = 0; k < kcount; ++k) {
+            const int i = r0 + k, j = r0 + piv[k];
+            if (i != j) std::swap(col[i], col[j]);
+        }
+    }
+}
+
+// In-place blocked right-looking PLU (Mat's PLU / __PLU, LU/__PLU.h:93-190).
+// Returns 0, or 1 + the first column at which a zero pivot column was met.
+int plu_inplace(int m, int n, double* A, int lda, int* pos) {
+    for (int i = 0; i < m; ++i) pos[i] = i;
+    const int s = std::min(m, n);
+    int info = 0;
+    std::vector<int> piv(std::max(BS_LU, n) + 1);
+    if (s <= BS_LU * 1.5) {
+        // __PLU2 over all columns (LU/__PLU.h:22-51): swaps every column.
+        for (int c = 0; c < n && c < m; ++c) {
+            double* col = A + (size_t)c * lda;
+            for (int i = 0; i < c; ++i) {
+                const double q = -col[i];
+                const double* li = A + (size_t)i * lda;
+                for (int r = i + 1; r < m; ++r) col[r] = std::fma(li[r], q, col[r]);
+            }
+            double maxv = 0.0;
+            for (int r = c; r < m; ++r) maxv = std::max(maxv, std::fabs(col[r]));
+            if (maxv == 0.0) {
+                info = c + 1;
+                break;
+            }
+            int j = c;
+            for (int r = c; r < m; ++r)
+                if (std::fabs(col[r]) == maxv) {
+                    j = r;
+                    break;
+                }
+            if (j != c) {
+                for (int cc = 0; cc < n; ++cc) std::swap(at(A, lda, c, cc), at(A, lda, j, cc));
+                std::swap(pos[c], pos[j]);
+            }
+            const double inv = 1.0 / col[c];
+            for (int r = c + 1; r < m; ++r) col[r] = col[r] * inv;
+        }
+        return info;
+    }
+    int r = 0;
+    for (; r + BS_LU <= s; r += BS_LU) {
+        const int brk = plu_panel(A, lda, m, r, BS_LU, pos, piv.data());
+        if (brk >= 0 && !info) info = r + brk + 1;
+        laswp(A, lda, r, BS_LU, r + BS_LU, n, piv.data());
+        if (r + BS_LU < s) {
+            const int nt = n - (r + BS_LU);
+            double* A12 = A + r + (size_t)(r + BS_LU) * lda;
+            trsm_lx(BS_LU, nt, A + r + (size_t)r * lda, lda, A12, lda);
+            gemm_acc(m - (r + BS_LU), nt, BS_LU, A + (r + BS_LU) + (size_t)r * lda, lda, A12, lda,
+                     A + (r + BS_LU) + (size_t)(r + BS_LU) * lda, lda, true);
+        }
+    }
+    if (r < s) {
+        const int rem = s - r;
+        const int brk = plu_panel(A, lda, m, r, rem, pos, piv.data());
+        if (brk >= 0 && !info) info = r + brk + 1;
+    }
+    return info;
+}
+
+// ----------------------------------------------------------------- LLT
+// Unblocked Cholesky of a k x k block (Mat's __LLT2, LU/__LLT.h:3-13).
+void llt2(double* L, int ldl, int k) {
+    for (int j = 0; j < k; ++j) {
+        const double t = 1.0 / std::sqrt(at(L, ldl, j, j));
+        double* cj = L + (size_t)j * ldl;
+        for (int r = j; r < k; ++r) cj[r] = cj[r] * t;
+        for (int i = j + 1; i < k; ++i) {
+            const double q = -at(L, ldl, i, j);
+            double* ci = L + (size_t)i * ldl;
+            for (int r = i; r < k; ++r) ci[r] = std::fma(cj[r], q, ci[r]);
+        }
+    }
+}
+
+// X(rows x k) := X * L^{-T} (Mat's __Solve_direct_XLT, LU/__LLT.h:30-40).
+void trsm_xlt(int rows, int k, const double* L, int ldl, double* X, int ldx) {
+    for (int j = 0; j < k; ++j) {
+        double* x = X + (size_t)j * ldx;
+        const double t = 1.0 / L[j + (size_t)j * ldl];
+        for (int r = 0; r < rows; ++r) x[r] = x[r] * t;
+        for (int kk = j + 1; kk < k; ++kk) {
+            const double q = -L[kk + (size_t)j * ldl];
+            double* xk = X + (size_t)kk * ldx;
+            for (int r = 0; r < rows; ++r) xk[r] = std::fma(x[r], q, xk[r]);
+        }
+    }
+}
+
+// Blocked right-looking Cholesky (Mat's LLT / __LLT, LU/__LLT.h:94-150, 212-246).
+// Reads the lower triangle of A into L, factors, zeroes the strict upper part.
+int llt(int n, double* L, int ldl) {
+    if (n <= 2 * BS_LLT) {
+        llt2(L, ldl, n);
+    } else {
+        for (int j = 0; j < n; j += BS_LLT) {
+            const int nb = std::min(BS_LLT, n - j);
+            llt2(L + j + (size_t)j * ldl, ldl, nb);
+            if (j + BS_LLT < n) {
+                for (int i = j + BS_LLT; i < n; i += BS_LLT) {
+                    const int mb = std::min(BS_LLT, n - i);
+                    trsm_xlt(mb, BS_LLT, L + j + (size_t)j * ldl, ldl, L + i + (size_t)j * ldl, ldl);
+                }
+                // C(k.., i..i+m) -= L(k.., j..j+BS) * L(i..i+m, j..j+BS)^T for k >= i
+                for (int i = j + BS_LLT; i < n; i += BS_LLT) {
+                    const int mb = std::min(BS_LLT, n - i);
+                    gemm_abt_sub(n - i, mb, BS_LLT, L + i + (size_t)j * ldl, ldl, L + i + (size_t)j * ldl, ldl,
+                                 L + i + (size_t)i * ldl, ldl);
+                }
+            }
+        }
+    }
+    for (int i = 0; i < n; ++i)
+        for (int r = 0; r < i; ++r) at(L, ldl, r, i) = 0.0;
+    for (int i = 0; i < n; ++i)
+        if (!(at(L, ldl, i, i) > 0.0)) return i + 1;
+    return 0;
+}
+
+// ------------------------------------------------------------------ QR
+// Householder panel (Mat's __QR_HouseHolder_Blocked2, QR/__Householder_Blocked.h:63-84):
+// LAPACK-style v (v0 = 1 implicit, stored below the diagonal), tau = (x0+cr)/cr,
+// R_rr = -cr with cr = sign(x0) ||x||.
+void qr_panel(double* R, int ldr, int h, int b, double* tau, std::vector<double>& v) {
+    v.resize(h);
+    for (int r = 0; r < b; ++r) {
+        double* w = R + r + (size_t)r * ldr;
+        const int len = h - r;
+        double cr = std::sqrt(dot_mat(w, w, len));
+        if (cr == 0.0) {
+            tau[r] = 0.0;
+            continue;
+        }
+        if (w[0] < 0.0) cr = -cr;
+        const double w0 = w[0] + cr;
+        const double hr = 1.0 / w0;
+        w[0] = -cr;
+        for (int i = 1; i < len; ++i) w[i] = w[i] * hr;
+        v[0] = 1.0;
+        for (int i = 1; i < len; ++i) v[i] = w[i];
+        tau[r] = w0 / cr;
+        for (int c = r + 1; c < b; ++c) {
+            double* col = R + r + (size_t)c * ldr;
+            const double d = col[0] + dot_mat(v.data() + 1, col + 1, len - 1);
+            const double q = -d * tau[r];
+            for (int i = 0; i < len; ++i) col[i] = std::fma(v[i], q, col[i]);
+        }
+    }
+}
+
+// Upper-triangular T of the compact WY form (Mat's CalculateT, :87-103).
+void qr_T(const double* V, int ldv, int h, int k, const double* tau, double* T /* k x k, ld k */) {
+    std::vector<double> s(k), w(k);
+    std::fill(T, T + (size_t)k * k, 0.0);
+    T[0] = tau[0];
+    for (int i = 1; i < k; ++i) {
+        for (int l = 0; l < i; ++l) {
+            const double* vl = V + (size_t)l * ldv;
+            const double* vi = V + (size_t)i * ldv;
+            s[l] = vl[i] + dot_mat(vl + i + 1, vi + i + 1, h - i - 1);
+        }
+        for (int r = 0; r < i; ++r) w[r] = 0.0;
+        for (int c = 0; c < i; ++c)
+            for (int r = 0; r <= c; ++r) w[r] = std::fma(T[r + (size_t)c * k], s[c], w[r]);
+        for (int r = 0; r < i; ++r) T[r + (size_t)i * k] = w[r] * -tau[i];
+        T[i + (size_t)i * k] = tau[i];
+    }
+}
+
+// Unit-lower V (h x k) expanded into a dense copy (implicit ones, zeros above).
+std::vector<double> expand_v(const double* V, int ldv, int h, int k) {
+    std::vector<double> Vd((size_t)h * k, 0.0);
+    for (int c = 0; c < k; ++c)
+        for (int r = c; r < h; ++r) Vd[r + (size_t)c * h] = r == c ? 1.0 : V[r + (size_t)c * ldv];
+    return Vd;
+}
+
+// R(h x nc) := (I - V op(T) V^T) R; op(T) = T^T for the factorization
+// (…_Mul, :144-212) and T for building Q (CalculateQ, :248-333).
+void apply_block_reflector(const std::vector<double>& Vd, int h, int k, const double* T, bool transT, double* R,
+                           int ldr, int nc) {
+    if (nc <= 0) return;
+    // W = V^T R  (k x nc)
+    std::vector<double> W((size_t)k * nc, 0.0), W2((size_t)k * nc, 0.0);
+    parallel_cols(nc, [&](int j0, int j1) {
+        for (int j = j0; j < j1; ++j)
+            for (int i = 0; i < k; ++i) {
+                double acc = 0.0;
+                const double* vi = Vd.data() + (size_t)i * h;
+                const double* rj = R + (size_t)j * ldr;
+                for (int p = i; p < h; ++p) acc = std::fma(vi[p], rj[p], acc);
+                W[i + (size_t)j * k] = acc;
+            }
+    });
+    // W2 = op(T) W
+    for (int j = 0; j < nc; ++j)
+        for (int i = 0; i < k; ++i) {
+            double acc = 0.0;
+            if (transT)
+                for (int p = 0; p <= i; ++p) acc = std::fma(T[p + (size_t)i * k], W[p + (size_t)j * k], acc);
+            else
+                for (int p = i; p < k; ++p) acc = std::fma(T[i + (size_t)p * k], W[p + (size_t)j * k], acc);
+            W2[i + (size_t)j * k] = acc;
+        }
+    // R -= V W2
+    gemm_acc(h, nc, k, Vd.data(), h, W2.data(), k, R, ldr, true);
+}
+
+// Unblocked Householder QR (Mat's __QR_HouseHolder + __HouseHolder_Q1,
+// QR/__HouseHolder.h:179-208, 48-79), used when min(m,n) <= 2*BS_QR.
+void qr_unblocked(int m, int n, double* R, double* Q) {
+    const int k = std::min(m, n);
+    std::vector<std::vector<double>> ws(k);
+    for (int r = 0; r < k; ++r) {
+        std::vector<double>& w = ws[r];
+        w.assign(R + r + (size_t)r * m, R + m + (size_t)r * m);
+        const int len = m - r;
+        double cr = std::sqrt(dot_mat(w.data(), w.data(), len));
+        if (cr == 0.0) {
+            w.assign(len, 0.0);
+            continue;
+        }
+        if (w[0] < 0.0) cr = -cr;
+        w[0] += cr;
+        const double hr = 1.0 / std::sqrt(cr * w[0]);
+        for (int i = 0; i < len; ++i) w[i] = w[i] * hr;
+        for (int c = r; c < n; ++c) {
+            double* col = R + r + (size_t)c * m;
+            const double d = -dot_mat(w.data(), col, len);
+            for (int i = 0; i < len; ++i) col[i] = std::fma(w[i], d, col[i]);
+        }
+    }
+    // Q = H_0 H_1 ... H_{k-1} applied to I, accumulated backwards (H = I - w w^T).
+    std::fill(Q, Q + (size_t)m * m, 0.0);
+    for (int i = 0; i < m; ++i) Q[i + (size_t)i * m] = 1.0;
+    for (int r = k - 1; r >= 0; --r) {
+        const std::vector<double>& w = ws[r];
+        const int len = m - r;
+        for (int c = r; c < m; ++c) {
+            double* col = Q + r + (size_t)c * m;
+            const double d = -dot_mat(w.data(), col, len);
+            for (int i = 0; i < len; ++i) col[i] = std::fma(w[i], d, col[i]);
+        }
+    }
+    for (int j = 0; j < n; ++j)
+        for (int r = j + 1; r < m; ++r) R[r + (size_t)j * m] = 0.0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void orc_set_threads(int n) { g_threads = std::max(1, n); }
+
+// Mat operator* (Mul/Mul.h:204-235): C = A B, C zeroed first (Mul.h:167).
+void orc_dgemm(int m, int n, int k, const double* A, int lda, const double* B, int ldb, double* C, int ldc) {
+    for (int j = 0; j < n; ++j) std::memset(C + (size_t)j * ldc, 0, sizeof(double) * (size_t)std::max(m, 0));
+    gemm_acc(m, n, k, A, lda, B, ldb, C, ldc, false);
+}
+
+// In-place Mat PLU: A := L\U (unit L below the diagonal), pos as Mat returns it.
+int orc_dgetrf(int m, int n, double* A, int lda, int* pos) { return plu_inplace(m, n, A, lda, pos); }
+
+// PLU(A, pos, L, U) (LU/__PLU.h:152-190): L m x m unit lower, U m x n upper.
+int orc_plu(int m, int n, const double* A, int* pos, double* L, double* U) {
+    std::memcpy(U, A, sizeof(double) * (size_t)m * n);
+    const int info = plu_inplace(m, n, U, m, pos);
+    std::fill(L, L + (size_t)m * m, 0.0);
+    const int s = std::min(m, n);
+    for (int c = 0; c < s; ++c) {
+        at(L, m, c, c) = 1.0;
+        for (int r = c + 1; r < m; ++r) {
+            at(L, m, r, c) = at(U, m, r, c);
+            at(U, m, r, c) = 0.0;
+        }
+    }
+    return info;
+}
+
+// Solve_direct(A, B) (LU/__Solve_direct.h:70-220).  For <= 4 right-hand
+// sides, Mat's narrow path: in-place PLU, permute, scalar forward and back
+// substitution (:112-139).  Wider: blocked substitution by the same TRSMs.
+int orc_solve(int n, int nrhs, const double* A, const double* B, double* X) {
+    std::vector<double> a(A, A + (size_t)n * n);
+    std::vector<int> pos(n);
+    const int info = plu_inplace(n, n, a.data(), n, pos.data());
+    for (int j = 0; j < nrhs; ++j)
+        for (int i = 0; i < n; ++i) X[i + (size_t)j * n] = B[pos[i] + (size_t)j * n];
+    if (nrhs <= 4) {
+        for (int j = 0; j < nrhs; ++j) {
+            double* x = X + (size_t)j * n;
+            for (int k = 0; k < n - 1; ++k) {
+                const double q = -x[k];
+                const double* lk = a.data() + (size_t)k * n;
+                for (int r = k + 1; r < n; ++r) x[r] = std::fma(lk[r], q, x[r]);
+            }
+            for (int r = n - 1; r > 0; --r) {
+                x[r] /= a[r + (size_t)r * n];
+                const double q = -x[r];
+                const double* ur = a.data() + (size_t)r * n;
+                for (int i = 0; i < r; ++i) x[i] = std::fma(ur[i], q, x[i]);
+            }
+            if (n > 0) x[0] /= a[0];
+        }
+    } else {
+        trsm_lx(n, nrhs, a.data(), n, X, n);
+        trsm_ux(n, nrhs, a.data(), n, X, n);
+    }
+    return info;
+}
+
+// LLT(A, L) (LU/__LLT.h:212-246): lower triangle of A in, L out (upper zeroed).
+int orc_llt(int n, const double* A, double* L) {
+    std::fill(L, L + (size_t)n * n, 0.0);
+    for (int c = 0; c < n; ++c)
+        for (int r = c; r < n; ++r) at(L, n, r, c) = A[r + (size_t)c * n];
+    return llt(n, L, n);
+}
+
+// QR(A, Q, R, QR_Householder) (QR/QR.h:8-25): Q m x m, R m x n.
+void orc_qr(int m, int n, const double* A, double* Q, double* R) {
+    std::memcpy(R, A, sizeof(double) * (size_t)m * n);
+    const int k = std::min(m, n);
+    if (k <= 2 * BS_QR) {
+        qr_unblocked(m, n, R, Q);
+        return;
+    }
+    // Factorization (:215-245).
+    std::vector<double> tau(k), v;
+    std::vector<std::vector<double>> Ts;
+    for (int j = 0; j < k; j += BS_QR) {
+        const int b = std::min(BS_QR, k - j);
+        const int h = m - j;
+        double* P = R + j + (size_t)j * m;
+        qr_panel(P, m, h, b, tau.data() + j, v);
+        std::vector<double> T((size_t)b * b);
+        qr_T(P, m, h, b, tau.data() + j, T.data());
+        if (j + b < n) apply_block_reflector(expand_v(P, m, h, b), h, b, T.data(), true, P + (size_t)b * m, m,
+                                             n - j - b);
+        Ts.push_back(std::move(T));
+    }
+    // Full m x m Q, accumulated backwards (:248-333).
+    std::fill(Q, Q + (size_t)m * m, 0.0);
+    for (int i = 0; i < m; ++i) Q[i + (size_t)i * m] = 1.0;
+    const int last = ((k - 1) / BS_QR) * BS_QR;
+    for (int j = last, t = (int)Ts.size() - 1; j >= 0; j -= BS_QR, --t) {
+        const int b = std::min(BS_QR, k - j);
+        const int h = m - j;
+        apply_block_reflector(expand_v(R + j + (size_t)j * m, m, h, b), h, b, Ts[t].data(), false,
+                              Q + j, m, m);
+    }
+    for (int j = 0; j < n; ++j)
+        for (int r = j + 1; r < m; ++r) R[r + (size_t)j * m] = 0.0;
+}
+
+// Det(A) (LU/__Det.h:30-101): sign of the interchanges times the product of U's diagonal.
+double orc_det(int n, const double* A) {
+    std::vector<double> a(A, A + (size_t)n * n);
+    std::vector<int> pos(n);
+    plu_inplace(n, n, a.data(), n, pos.data());
+    // parity of the permutation pos
+    std::vector<char> seen(n, 0);
+    int swaps = 0;
+    for (int i = 0; i < n; ++i) {
+        if (seen[i]) continue;
+        int len = 0;
+        for (int j = i; !seen[j]; j = pos[j]) {
+            seen[j] = 1;
+            ++len;
+        }
+        swaps += len - 1;
+    }
+    double ret = (swaps & 1) ? -1.0 : 1.0;
+    for (int i = 0; i < n; ++i) ret = ret * a[i + (size_t)i * n];
+    return ret;
+}
+
+}  // extern "C"
