@@ -94,6 +94,45 @@ mg_status_t mg_dgemm(mg_handle_t h, int transA, int transB, int m, int n, int k,
                      double alpha, const double* A, int lda, const double* B, int ldb,
                      double beta, double* C, int ldc);
 
+/* ------------------------------------------------------------------- LU
+ * In-place LU with partial pivoting, Mat's PLU (Mat-8.3.1/LU/__PLU.h:152-190,
+ * blocked as __PLU, :93-149, block size 60): on return A holds the unit-lower
+ * L strictly below the diagonal and U on and above it, and pos[0..m) (device)
+ * is Mat's permutation: row i of L*U is row pos[i] of the input
+ * (PLU_getP, :193-197, builds P with P(pos[i], i) = 1).  The pivot is the
+ * first row holding the largest |a| of the column (:67-77).  m >= n is the
+ * reference-parity domain; for m < n the trailing columns are eliminated
+ * LAPACK-style (Mat leaves them un-updated after the last panel).  Returns
+ * MG_SINGULAR with *info = first exactly-zero pivot column (1-based); Mat
+ * has no such report and stops that panel instead.  Synchronises. */
+mg_status_t mg_dgetrf(mg_handle_t h, int m, int n, double* A, int lda, int* pos, int* info);
+
+/* X := A^{-1} B from mg_dgetrf's factors and pos (n x n), B and X distinct.
+ * Substitution order of Mat's narrow solve (Solve_direct_narrow,
+ * Mat-8.3.1/LU/__Solve_direct.h:112-139) for every right-hand side. */
+mg_status_t mg_dgetrs(mg_handle_t h, int n, int nrhs, const double* LU, int lda, const int* pos,
+                      const double* B, int ldb, double* X, int ldx);
+
+/* Mat's Solve_direct(A, B) (Mat-8.3.1/LU/__Solve_direct.h:146-220): A is
+ * not modified (factored in a workspace copy), X = A^{-1} B.  Synchronises. */
+mg_status_t mg_dgesv(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B, int ldb,
+                     double* X, int ldx, int* info);
+
+/* ------------------------------------------------- split-precision GEMM
+ * C = alpha * A * B + beta * C for fp32 column-major operands on the
+ * tcgen05 BF16 tensor cores: A and B are split into `nterms` bf16 terms
+ * (A = A0 + A1 + A2, A0 = bf16(A), A1 = bf16(A - A0), ...) and the products
+ * of total order < nterms are accumulated in fp32 (nterms = 3: six products,
+ * about fp32 accuracy; 2: three products; 1: plain bf16).  No counterpart in
+ * Mat (Mat has no mixed precision); it is the trailing update of the mixed
+ * LU and the split GEMM of the M=N=K=16384 benchmark configuration.
+ * Uses handle workspace of nterms*(m+n)*k*2 bytes (k rounded up to 32). */
+mg_status_t mg_sgemm_bf16x(mg_handle_t h, int nterms, int m, int n, int k, float alpha,
+                           const float* A, int lda, const float* B, int ldb, float beta,
+                           float* C, int ldc);
+/* Device error word of the last split GEMM (MG_TIMEOUT if a bounded wait gave up). */
+mg_status_t mg_bf16x_check_error(mg_handle_t h, int* device_err_flag);
+
 /* Measures the FP64 peaks of this GPU with dependent-free FMA / DMMA loops
  * (TFLOP/s, counting an FMA as 2 flops).  Synchronises. */
 mg_status_t mg_measure_fp64_peaks(mg_handle_t h, double* dfma_tflops, double* dmma_tflops);

@@ -105,6 +105,55 @@ class Handle:
                                      _ptr(B), ld_of(B), beta, _ptr(C_), ld_of(C_)), "mg_dgemm")
         return C_
 
+    def sgemm_bf16x(self, A, B, C_=None, alpha=1.0, beta=0.0, nterms=3):
+        """fp32 C = alpha A B + beta C on the BF16 tensor cores with `nterms` split terms."""
+        m, k = A.shape
+        n = B.shape[1]
+        if C_ is None:
+            C_ = colmajor(m, n, dtype=torch.float32, device=A.device)
+            beta = 0.0
+        self.check(self.lib.mg_sgemm_bf16x(self.h, nterms, m, n, k, alpha, _ptr(A), ld_of(A), _ptr(B), ld_of(B),
+                                           beta, _ptr(C_), ld_of(C_)), "mg_sgemm_bf16x")
+        flag = C.c_int(0)
+        self.check(self.lib.mg_bf16x_check_error(self.h, C.byref(flag)), "mg_bf16x_check_error")
+        if flag.value:
+            raise MatGpuError(flag.value, "split GEMM: a bounded device wait timed out")
+        return C_
+
+    # -------------------------------------------------------------------- LU
+    def dgetrf(self, A: torch.Tensor, pos: torch.Tensor | None = None, check=True):
+        """In-place Mat PLU of A (m x n, column-major). Returns (pos, info)."""
+        m, n = A.shape
+        if pos is None:
+            pos = torch.empty(m, dtype=torch.int32, device=A.device)
+        info = C.c_int(0)
+        st = self.lib.mg_dgetrf(self.h, m, n, _ptr(A), ld_of(A), _ptr(pos), C.byref(info))
+        if check and st not in (0, 4):
+            self.check(st, "mg_dgetrf")
+        return pos, info.value
+
+    def dgetrs(self, LU: torch.Tensor, pos: torch.Tensor, B: torch.Tensor, X: torch.Tensor | None = None):
+        n = LU.shape[0]
+        nrhs = B.shape[1]
+        if X is None:
+            X = colmajor(n, nrhs, device=B.device)
+        self.check(self.lib.mg_dgetrs(self.h, n, nrhs, _ptr(LU), ld_of(LU), _ptr(pos), _ptr(B), ld_of(B),
+                                      _ptr(X), ld_of(X)), "mg_dgetrs")
+        return X
+
+    def dgesv(self, A: torch.Tensor, B: torch.Tensor, X: torch.Tensor | None = None):
+        """Mat Solve_direct(A, B): X = A^-1 B, A untouched. Returns (X, info)."""
+        n = A.shape[0]
+        nrhs = B.shape[1]
+        if X is None:
+            X = colmajor(n, nrhs, device=B.device)
+        info = C.c_int(0)
+        st = self.lib.mg_dgesv(self.h, n, nrhs, _ptr(A), ld_of(A), _ptr(B), ld_of(B), _ptr(X), ld_of(X),
+                               C.byref(info))
+        if st not in (0, 4):
+            self.check(st, "mg_dgesv")
+        return X, info.value
+
     def measure_fp64_peaks(self) -> tuple[float, float]:
         a, b = C.c_double(), C.c_double()
         self.check(self.lib.mg_measure_fp64_peaks(self.h, C.byref(a), C.byref(b)), "mg_measure_fp64_peaks")

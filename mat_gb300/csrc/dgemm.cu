@@ -94,8 +94,15 @@ __device__ __forceinline__ void load_stage(double* sA, double* sB, const double*
     }
 }
 
+// MODE selects how the accumulators meet C (Mat's micro-kernels load C and
+// fuse every product into it, Mul/__micro_kernel_packed_double.h:14-110,
+// :301-398, so the in-place modes keep that per-element chain):
+//   0: acc = 0,  C = alpha*acc            (beta == 0; operator*)
+//   1: acc = C,  acc -= A*B, C = acc      (alpha == -1, beta == 1; __mulAB_packed_n)
+//   2: acc = C,  acc += A*B, C = acc      (alpha == 1, beta == 1)
+//   3: acc = 0,  C = alpha*acc + beta*C   (general)
 // TRI = 1: only tiles containing elements with row >= col are computed.
-template <int TA, int TB, int BETA0, int TRI>
+template <int TA, int TB, int MODE, int TRI>
 __global__ void __launch_bounds__(THREADS, 1)
     dgemm_kernel(int M, int N, int K, double alpha, const double* __restrict__ A, int lda,
                  const double* __restrict__ B, int ldb, double beta, double* __restrict__ C, int ldc) {
@@ -115,7 +122,15 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
         for (int j = 0; j < 4; ++j)
 #pragma unroll
-            for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.0;
+            for (int r = 0; r < 4; ++r) {
+                double v = 0.0;
+                if (MODE == 1 || MODE == 2) {
+                    const int row = bm + wm + 16 * i + g + (r >= 2 ? 8 : 0);
+                    const int col = bn + wn + 8 * j + 2 * t + (r & 1);
+                    if (row < M && col < N) v = C[row + (size_t)col * ldc];
+                }
+                acc[i][j][r] = v;
+            }
 
     const int ktiles = (K + BK - 1) / BK;
 #pragma unroll
@@ -148,6 +163,10 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int i = 0; i < 4; ++i) {
                 a[i][0] = sA[(ks + t) * SA + wm + 16 * i + g];
                 a[i][1] = sA[(ks + t) * SA + wm + 16 * i + g + 8];
+                if (MODE == 1) {
+                    a[i][0] = -a[i][0];
+                    a[i][1] = -a[i][1];
+                }
             }
 #pragma unroll
             for (int j = 0; j < 4; ++j) b[j] = sB[(wn + 8 * j + g) * SB + ks + t];
@@ -170,18 +189,22 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const int col = bn + wn + 8 * j + 2 * t + (r & 1);
                 if (row < M && col < N) {
                     double* cp = C + row + (size_t)col * ldc;
-                    const double v = alpha * acc[i][j][r];
-                    *cp = BETA0 ? v : fma(beta, *cp, v);
+                    if (MODE == 1 || MODE == 2) {
+                        *cp = acc[i][j][r];
+                    } else {
+                        const double v = alpha * acc[i][j][r];
+                        *cp = MODE == 0 ? v : fma(beta, *cp, v);
+                    }
                 }
             }
         }
     }
 }
 
-template <int TA, int TB, int BETA0, int TRI>
+template <int TA, int TB, int MODE, int TRI>
 cudaError_t launch_t(cudaStream_t st, int M, int N, int K, double alpha, const double* A, int lda,
                      const double* B, int ldb, double beta, double* C, int ldc) {
-    auto kern = dgemm_kernel<TA, TB, BETA0, TRI>;
+    auto kern = dgemm_kernel<TA, TB, MODE, TRI>;
     static bool configured = false;  // per instantiation
     if (!configured) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
@@ -217,15 +240,21 @@ mg_status_t dgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, in
         scale_kernel<<<h->num_sms * 4, 256, 0, st>>>(m, n, beta, C, ldc);
         return post_launch(h, "scale_kernel");
     }
-    const bool b0 = beta == 0.0;
+    const int mode = beta == 0.0                    ? 0
+                     : (alpha == -1.0 && beta == 1.0) ? 1
+                     : (alpha == 1.0 && beta == 1.0)  ? 2
+                                                      : 3;
     cudaError_t e;
-#define MG_DISPATCH(TA, TB)                                                                                 \
-    if (b0)                                                                                                 \
-        e = tri ? launch_t<TA, TB, 1, 1>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc)                  \
-                : launch_t<TA, TB, 1, 0>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);                 \
-    else                                                                                                    \
-        e = tri ? launch_t<TA, TB, 0, 1>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc)                  \
-                : launch_t<TA, TB, 0, 0>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+#define MG_MODE(TA, TB, MODE)                                                                \
+    e = tri ? launch_t<TA, TB, MODE, 1>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc)    \
+            : launch_t<TA, TB, MODE, 0>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+#define MG_DISPATCH(TA, TB)          \
+    switch (mode) {                  \
+        case 0: MG_MODE(TA, TB, 0) break; \
+        case 1: MG_MODE(TA, TB, 1) break; \
+        case 2: MG_MODE(TA, TB, 2) break; \
+        default: MG_MODE(TA, TB, 3) break; \
+    }
     if (!transA && !transB) {
         MG_DISPATCH(0, 0)
     } else if (transA && !transB) {
@@ -235,6 +264,7 @@ mg_status_t dgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, in
     } else {
         MG_DISPATCH(1, 1)
     }
+#undef MG_MODE
 #undef MG_DISPATCH
     if (e != cudaSuccess) return cuda_fail(h, e, "dgemm_kernel launch");
     h->launches++;

@@ -1,0 +1,427 @@
+// Split-BF16 GEMM on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// C (fp32, column-major) = alpha * sum_{(i,j) in S} A_i * B_j^T + beta * C
+// where A = A_0 + A_1 + A_2 and B = B_0 + B_1 + B_2 are fp32 operands split
+// into bf16 terms (A_0 = bf16(A), A_1 = bf16(A - A_0), ...).  With three terms
+// and the six products of total order <= 2 the product carries ~24 bits, the
+// accuracy of an fp32 GEMM; two terms / three products give ~16 bits; one
+// term is a plain bf16 GEMM.  Accumulation is fp32 in tensor memory.
+//
+// This is the mixed-precision replacement for the trailing-matrix updates of
+// Mat's blocked factorizations (__mulAB_packed_n, Mat-8.3.1/Mul/Mul.h:240-263)
+// and the split-precision product of the benchmark configuration
+// M=N=K=16384; Mat itself has no mixed-precision path.
+//
+// Kernel: persistent, one CTA per SM, warp-specialised:
+//   warp 0      TMA producer: per k-block of 32 it loads every term of the
+//               128-row A tile and the 256-row B tile (64-byte swizzle) into
+//               one pipeline stage; one mbarrier per stage counts the bytes.
+//   warp 1      allocates 512 TMEM columns (two 128x256 fp32 accumulators)
+//               and one elected lane issues tcgen05.mma (M=128, N=256, K=16),
+//               committing each stage back to the producer and each finished
+//               tile to the epilogue.
+//   warps 2-5   epilogue: tcgen05.ld the accumulator (each warp its 32 TMEM
+//               lanes = 32 rows), apply alpha/beta, store C coalesced by
+//               column.  Two accumulators let tile t+1's MMAs run under tile
+//               t's epilogue.
+// Every mbarrier wait is bounded; on a timeout the kernel records MG_TIMEOUT,
+// drains its own outstanding copies/MMAs and frees TMEM before returning.
+#include <cuda_bf16.h>
+
+#include "mg_internal.cuh"
+#include "tc_common.cuh"
+
+namespace {
+
+constexpr int BM = 128, BN = 256, BK = 32;  // BK * 2 B = 64 B = one swizzle row
+constexpr int THREADS = 192;
+constexpr int TMEM_COLS = 512;
+
+template <int NP>
+struct Cfg {
+    static constexpr int A_TILE = BM * BK * 2;                 // bytes per A term tile
+    static constexpr int B_TILE = BN * BK * 2;                 // bytes per B term tile
+    static constexpr int STAGE = NP * (A_TILE + B_TILE);
+    static constexpr int STAGES = NP == 3 ? 3 : NP == 2 ? 4 : 8;
+    static constexpr int NPROD = NP == 3 ? 6 : NP == 2 ? 3 : 1;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE + 1024 /*align*/ + 256 /*barriers*/;
+};
+
+// Products (A term, B term), smallest first.
+__device__ __constant__ int kProdA[6] = {2, 1, 0, 1, 0, 0};
+__device__ __constant__ int kProdB[6] = {0, 1, 2, 0, 1, 0};
+__device__ __forceinline__ int prod_a(int np, int p) { return np == 3 ? kProdA[p] : np == 2 ? (p == 0 ? 1 : 0) : 0; }
+__device__ __forceinline__ int prod_b(int np, int p) { return np == 3 ? kProdB[p] : np == 2 ? (p == 1 ? 1 : 0) : 0; }
+
+__device__ __forceinline__ void tile_coords(int t, int num_m, int num_n, int& mb, int& nb) {
+    // grouped raster: 16 m-blocks per group, n fastest inside the group
+    constexpr int GM = 16;
+    const int per_group = GM * num_n;
+    const int g = t / per_group;
+    const int first_m = g * GM;
+    const int gsize = min(GM, num_m - first_m);
+    const int r = t - g * per_group;
+    mb = first_m + r % gsize;
+    nb = r / gsize;
+}
+
+template <int NP>
+__global__ void __launch_bounds__(THREADS, 1)
+    bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                      float* __restrict__ C, int ldc, int M, int N, int Kp, float alpha, float beta,
+                      int* __restrict__ err) {
+    using CF = Cfg<NP>;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* bars = (uint64_t*)(smem + (size_t)CF::STAGES * CF::STAGE);
+    uint64_t* full = bars;
+    uint64_t* empty = bars + CF::STAGES;
+    uint64_t* acc_full = bars + 2 * CF::STAGES;
+    uint64_t* acc_empty = acc_full + 2;
+    uint64_t* mma_done = acc_empty + 2;
+    uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
+    __shared__ int s_abort;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int num_m = (M + BM - 1) / BM, num_n = (N + BN - 1) / BN;
+    const int total = num_m * num_n;
+    const int kblocks = Kp / BK;
+
+    if (threadIdx.x == 0) {
+        s_abort = 0;
+        for (int s = 0; s < CF::STAGES; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&acc_full[b], 1);
+            tc::mbar_init(&acc_empty[b], 128);
+        }
+        tc::mbar_init(mma_done, 1);
+        tc::fence_barrier_init();
+        tc::prefetch_tmap(&tmA);
+        tc::prefetch_tmap(&tmB);
+    }
+    if (warp == 1) {
+        tc::tmem_alloc(tmem_slot, TMEM_COLS);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---------------------------------------------------------------- producer
+            int stage = 0;
+            uint32_t phase = 0;
+            bool issued[CF::STAGES];
+            uint32_t last_phase[CF::STAGES];
+            for (int s = 0; s < CF::STAGES; ++s) issued[s] = false, last_phase[s] = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
+                int mb, nb;
+                tile_coords(t, num_m, num_n, mb, nb);
+                for (int kb = 0; kb < kblocks; ++kb) {
+                    if (!tc::mbar_wait(&empty[stage], phase ^ 1)) {
+                        ok = false;
+                        break;
+                    }
+                    if (*(volatile int*)&s_abort) {
+                        ok = false;
+                        break;
+                    }
+                    unsigned char* st = smem + (size_t)stage * CF::STAGE;
+                    tc::mbar_arrive_expect_tx(&full[stage], CF::STAGE);
+                    for (int p = 0; p < NP; ++p) {
+                        tc::tma_load_3d(st + p * CF::A_TILE, &tmA, &full[stage], kb * BK, mb * BM, p);
+                        tc::tma_load_3d(st + NP * CF::A_TILE + p * CF::B_TILE, &tmB, &full[stage], kb * BK,
+                                        nb * BN, p);
+                    }
+                    issued[stage] = true;
+                    last_phase[stage] = phase;
+                    if (++stage == CF::STAGES) stage = 0, phase ^= 1;
+                }
+            }
+            if (!ok) {
+                atomicExch(err, 8);
+                s_abort = 1;
+            }
+            // drain: every copy this thread issued has landed before exit
+            for (int s = 0; s < CF::STAGES; ++s)
+                if (issued[s]) tc::mbar_wait(&full[s], last_phase[s]);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ------------------------------------------------------------ MMA issuer
+            constexpr uint32_t idesc = tc::idesc_bf16_f32(BM, BN);
+            int stage = 0;
+            uint32_t phase = 0;
+            int it = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < total && ok; t += gridDim.x, ++it) {
+                const int buf = it & 1;
+                if (!tc::mbar_wait(&acc_empty[buf], ((it >> 1) & 1) ^ 1)) {
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t d = tmem_base + (uint32_t)(buf * BN);
+                for (int kb = 0; kb < kblocks; ++kb) {
+                    if (!tc::mbar_wait(&full[stage], phase) || *(volatile int*)&s_abort) {
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    const uint32_t st = tc::smem_u32(smem + (size_t)stage * CF::STAGE);
+#pragma unroll
+                    for (int p = 0; p < CF::NPROD; ++p) {
+                        const uint32_t a0 = st + prod_a(NP, p) * CF::A_TILE;
+                        const uint32_t b0 = st + NP * CF::A_TILE + prod_b(NP, p) * CF::B_TILE;
+#pragma unroll
+                        for (int kk = 0; kk < BK / 16; ++kk) {
+                            // advance 16 bf16 = 32 B inside the 64-byte swizzled row
+                            const uint64_t ad = tc::smem_desc_sw64(a0 + kk * 32);
+                            const uint64_t bd = tc::smem_desc_sw64(b0 + kk * 32);
+                            tc::mma_bf16(d, ad, bd, idesc, (kb | p | kk) != 0);
+                        }
+                    }
+                    tc::mma_commit(&empty[stage]);
+                    if (++stage == CF::STAGES) stage = 0, phase ^= 1;
+                }
+                if (!ok) break;
+                tc::mma_commit(&acc_full[buf]);
+            }
+            if (!ok) {
+                atomicExch(err, 8);
+                s_abort = 1;
+            }
+            // all MMAs of this thread complete before TMEM is released
+            tc::mma_commit(mma_done);
+            tc::mbar_wait(mma_done, 0);
+        }
+    } else {
+        // ------------------------------------------------------------------ epilogue
+        const int q = warp & 3;  // TMEM lane quarter this warp may access
+        const int row_in_tile = q * 32 + lane;
+        int it = 0;
+        for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
+            const int buf = it & 1;
+            if (!tc::mbar_wait(&acc_full[buf], (it >> 1) & 1) || *(volatile int*)&s_abort) {
+                atomicExch(err, 8);
+                s_abort = 1;
+                break;
+            }
+            tc::tc_fence_after();
+            int mb, nb;
+            tile_coords(t, num_m, num_n, mb, nb);
+            const int row = mb * BM + row_in_tile;
+            const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN);
+#pragma unroll 1
+            for (int ch = 0; ch < BN / 32; ++ch) {
+                uint32_t r[32];
+                tc::tmem_ld_32x32b_x32(taddr + ch * 32, r);
+                tc::tmem_ld_wait();
+                const int col0 = nb * BN + ch * 32;
+                if (row < M) {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const int col = col0 + j;
+                        if (col < N) {
+                            float* cp = C + (size_t)row + (size_t)col * ldc;
+                            const float v = alpha * __uint_as_float(r[j]);
+                            *cp = beta == 0.f ? v : fmaf(beta, *cp, v);
+                        }
+                    }
+                }
+            }
+            tc::tc_fence_before();
+            tc::mbar_arrive(&acc_empty[buf]);
+        }
+    }
+
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc(tmem_base, TMEM_COLS);
+    }
+}
+
+// ------------------------------------------------------------------ splitting
+__device__ __forceinline__ void split3(float x, __nv_bfloat16& h0, __nv_bfloat16& h1, __nv_bfloat16& h2) {
+    h0 = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(h0);
+    h1 = __float2bfloat16_rn(r1);
+    const float r2 = r1 - __bfloat162float(h1);
+    h2 = __float2bfloat16_rn(r2);
+}
+
+// A (rows x K, column-major, ld) -> parts[p][row][k] (row stride Kp, zero
+// padded for k >= K): a 32x32 tiled transpose through shared memory.
+template <typename TIN>
+__global__ void split_rows_kernel(const TIN* __restrict__ A, int lda, int rows, int K, int Kp, int np,
+                                  __nv_bfloat16* __restrict__ out, size_t part_stride) {
+    __shared__ float tile[32][33];
+    const int k0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+    for (int j = ty; j < 32; j += 8) {
+        const int k = k0 + j, r = r0 + tx;
+        tile[j][tx] = (k < K && r < rows) ? (float)A[(size_t)r + (size_t)k * lda] : 0.f;
+    }
+    __syncthreads();
+    for (int j = ty; j < 32; j += 8) {
+        const int r = r0 + j, k = k0 + tx;
+        if (r < rows && k < Kp) {
+            __nv_bfloat16 h0, h1, h2;
+            split3(tile[tx][j], h0, h1, h2);
+            const size_t o = (size_t)r * Kp + k;
+            out[o] = h0;
+            if (np > 1) out[part_stride + o] = h1;
+            if (np > 2) out[2 * part_stride + o] = h2;
+        }
+    }
+}
+
+// B (K x cols, column-major, ld) -> parts[p][col][k]: column c of B is row c.
+template <typename TIN>
+__global__ void split_cols_kernel(const TIN* __restrict__ B, int ldb, int K, int cols, int Kp, int np,
+                                  __nv_bfloat16* __restrict__ out, size_t part_stride) {
+    const size_t total = (size_t)cols * Kp;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int c = (int)(e / Kp), k = (int)(e % Kp);
+        const float x = k < K ? (float)B[(size_t)k + (size_t)c * ldb] : 0.f;
+        __nv_bfloat16 h0, h1, h2;
+        split3(x, h0, h1, h2);
+        out[e] = h0;
+        if (np > 1) out[part_stride + e] = h1;
+        if (np > 2) out[2 * part_stride + e] = h2;
+    }
+}
+
+// --------------------------------------------------------------- tensor maps
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn get_encode() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
+// 3-D map over parts[np][rows][Kp] bf16 with box {BK, box_rows, 1}, 64-byte swizzle.
+bool make_map(CUtensorMap* map, const void* base, int rows, int Kp, int np, size_t part_stride, int box_rows) {
+    EncodeTiledFn enc = get_encode();
+    if (!enc) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)np};
+    cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)part_stride * 2};
+    cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int NP>
+mg_status_t launch_gemm_np(mg_handle_t h, const CUtensorMap& ma, const CUtensorMap& mb, float* C, int ldc, int M,
+                           int N, int Kp, float alpha, float beta, int* err) {
+    auto kern = bf16x_gemm_kernel<NP>;
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<NP>::SMEM));
+    const int tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+    const int grid = tiles < h->num_sms ? tiles : h->num_sms;
+    kern<<<grid, THREADS, Cfg<NP>::SMEM, h->stream>>>(ma, mb, C, ldc, M, N, Kp, alpha, beta, err);
+    return mg::post_launch(h, "bf16x_gemm_kernel");
+}
+
+}  // namespace
+
+namespace mg {
+
+size_t bf16x_split_bytes(int rows, int K, int np) {
+    const int Kp = (K + BK - 1) / BK * BK;
+    return align_up((size_t)np * rows * Kp * 2, 1024);
+}
+
+// Splits an fp32/fp64 operand into np bf16 terms.  a_side: rows x K column-
+// major (transposed into K-major rows); else K x cols column-major.
+template <typename TIN>
+mg_status_t bf16x_split(mg_handle_t h, bool a_side, const TIN* X, int ldx, int rows_or_cols, int K, int np,
+                        void* out) {
+    const int Kp = (K + BK - 1) / BK * BK;
+    const size_t ps = (size_t)rows_or_cols * Kp;
+    if (a_side) {
+        dim3 grid((Kp + 31) / 32, (rows_or_cols + 31) / 32);
+        split_rows_kernel<TIN><<<grid, dim3(32, 8), 0, h->stream>>>(X, ldx, rows_or_cols, K, Kp, np,
+                                                                     (__nv_bfloat16*)out, ps);
+        return post_launch(h, "split_rows_kernel");
+    }
+    size_t blocks = (ps + 255) / 256;
+    if (blocks > (size_t)h->num_sms * 16) blocks = (size_t)h->num_sms * 16;
+    split_cols_kernel<TIN><<<(unsigned)blocks, 256, 0, h->stream>>>(X, ldx, K, rows_or_cols, Kp, np,
+                                                                    (__nv_bfloat16*)out, ps);
+    return post_launch(h, "split_cols_kernel");
+}
+template mg_status_t bf16x_split<float>(mg_handle_t, bool, const float*, int, int, int, int, void*);
+template mg_status_t bf16x_split<double>(mg_handle_t, bool, const double*, int, int, int, int, void*);
+
+// C = alpha * (split A)(split B) + beta * C from pre-split operands.
+mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, float alpha, const void* Asplit,
+                                const void* Bsplit, float beta, float* C, int ldc, int* err) {
+    if (M == 0 || N == 0) return MG_OK;
+    const int Kp = (K + BK - 1) / BK * BK;
+    CUtensorMap ma, mb;
+    if (!make_map(&ma, Asplit, M, Kp, np, (size_t)M * Kp, BM) || !make_map(&mb, Bsplit, N, Kp, np, (size_t)N * Kp, BN))
+        return fail(h, MG_ERR_CUDA, "cuTensorMapEncodeTiled failed (M=%d N=%d Kp=%d)", M, N, Kp);
+    switch (np) {
+        case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err);
+        case 2: return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err);
+        default: return launch_gemm_np<3>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err);
+    }
+}
+
+}  // namespace mg
+
+extern "C" mg_status_t mg_sgemm_bf16x(mg_handle_t h, int nterms, int m, int n, int k, float alpha, const float* A,
+                                      int lda, const float* B, int ldb, float beta, float* C, int ldc) {
+    if (!h) return MG_ERR_ARG;
+    if (nterms < 1 || nterms > 3 || m < 0 || n < 0 || k < 0 || lda < (m > 1 ? m : 1) || ldb < (k > 1 ? k : 1) ||
+        ldc < (m > 1 ? m : 1))
+        return mg::fail(h, MG_ERR_ARG, "mg_sgemm_bf16x: bad arguments");
+    if (m == 0 || n == 0) return MG_OK;
+    if (k == 0) {
+        return mg::fail(h, MG_ERR_ARG, "mg_sgemm_bf16x: k == 0 unsupported");
+    }
+    const size_t as = mg::bf16x_split_bytes(m, k, nterms), bs = mg::bf16x_split_bytes(n, k, nterms);
+    MG_TRY(mg::ensure_ws(h, 1024 + as + bs));
+    MG_TRY(mg::ensure_hws(h, 64));
+    char* ws = (char*)h->ws;
+    int* err = (int*)ws;
+    MG_CHECK_CUDA(h, cudaMemsetAsync(err, 0, sizeof(int), h->stream));
+    void* Asp = ws + 1024;
+    void* Bsp = ws + 1024 + as;
+    MG_TRY(mg::bf16x_split<float>(h, true, A, lda, m, k, nterms, Asp));
+    MG_TRY(mg::bf16x_split<float>(h, false, B, ldb, n, k, nterms, Bsp));
+    MG_TRY(mg::bf16x_gemm_presplit(h, nterms, m, n, k, alpha, Asp, Bsp, beta, C, ldc, err));
+    return MG_OK;
+}
+
+extern "C" mg_status_t mg_bf16x_check_error(mg_handle_t h, int* device_err_flag) {
+    // reads the device error word of the last split GEMM (synchronises)
+    if (!h || !device_err_flag) return MG_ERR_ARG;
+    if (!h->ws) {
+        *device_err_flag = 0;
+        return MG_OK;
+    }
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(device_err_flag, h->ws, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    return MG_OK;
+}

@@ -1,0 +1,46 @@
+// Bounded grid-wide barrier for cooperative (co-resident) launches.
+//
+// The counter is zeroed by the host (cudaMemsetAsync) before each launch and
+// only grows; the k-th barrier waits for k * gridDim.x arrivals.  Every wait
+// is bounded: after kSpinLimit polls (~1-2 s with the back-off) the CTA
+// records MG_TIMEOUT in the error word and the caller returns, so a lost CTA
+// can never hang the GPU.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace mg {
+
+constexpr unsigned kSpinLimit = 1u << 24;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Returns false (in every thread of the CTA) if the wait timed out.
+__device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target, int* err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        if (gridDim.x > 1) {
+            __threadfence();
+            atomicAdd(counter, 1u);
+            unsigned spins = 0;
+            while (ld_acquire_u32(counter) < target) {
+                if (++spins > kSpinLimit) {
+                    atomicExch(err, 8 /* MG_TIMEOUT */);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(spins < 64 ? 20 : 100);
+            }
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+}  // namespace mg

@@ -1,0 +1,600 @@
+// Blocked right-looking LU with partial pivoting (Mat's PLU) and the narrow
+// Solve_direct on top of it.
+//
+// Reference path (Mat-8.3.1): PLU (LU/__PLU.h:152-190) -> __PLU (:93-149):
+// per BS=60 block column, the panel __PLU2_piv (:54-90: left-looking column
+// updates, __MaxAbs + first-index tie-break, row swaps, reciprocal scaling),
+// __laswp_trailing (:3-19), the unit-lower TRSM __Solve_direct_LX
+// (LU/__Base.h:95-208) on the block row, and the packed trailing update
+// A22 -= L21*U12 (__mulAB_packed_n, Mul/Mul.h:240-263).
+//
+// GPU design:
+//  - panel: one cooperative kernel, each CTA holding a slab of the panel's
+//    rows in shared memory; per column one bounded grid barrier: every CTA
+//    publishes (max |a|, first row, that row) and the row at the diagonal,
+//    then all CTAs pick the same winner (largest |a|, smallest row on ties),
+//    swap, scale by the reciprocal and apply the rank-1 update to their rows.
+//    Right-looking within the panel performs exactly the fused operations of
+//    Mat's left-looking loop in the same order, so the panel is bit-exact.
+//  - laswp: the panel's interchanges on the columns left and right of it.
+//  - trsm: one thread per right-hand column, reproducing Mat's AVX-512
+//    operation order (four partial sums per row for 8-column groups,
+//    column-oriented fused updates for the ragged columns).
+//  - trailing update: the FP64 GEMM in its in-place "C -= A*B" mode.
+//  Block size 60 = Mat's AVX-512 __BlockSize_LU, so the blocking (and with it
+//  every rounding) follows the reference.
+#include <climits>
+
+#include "grid_sync.cuh"
+#include "mg_internal.cuh"
+
+namespace {
+
+constexpr int LU_BS = 60;           // Mat-8.3.1/Mat.h:69-71 (AVX-512)
+constexpr int PANEL_MAX_NB = 96;    // unblocked path handles s <= 1.5*BS = 90
+constexpr int PANEL_THREADS = 256;
+
+struct PanelWs {
+    unsigned* bar;  // grid barrier counter
+    int* err;       // MG_TIMEOUT flag
+    int* info;      // first zero-pivot column (1-based), 0 if none
+};
+
+// Exchange area layout (bytes), per panel launch.
+template <typename T>
+struct PanelXchg {
+    T* cand_val;   // [2][P]
+    int* cand_row; // [2][P]
+    T* cand_rows;  // [2][P][nb]
+    T* diag_row;   // [2][nb]
+};
+
+template <typename T>
+__device__ __forceinline__ T ld_cg(const T* p) {
+    return __ldcg(p);
+}
+
+template <typename T>
+__device__ __forceinline__ void better(T& v, int& i, T ov, int oi) {
+    if (ov > v || (ov == v && oi < i)) {
+        v = ov;
+        i = oi;
+    }
+}
+
+// Panel factorization of columns [r0, r0+nb) over rows [r0, m).
+template <typename T>
+__global__ void __launch_bounds__(PANEL_THREADS, 1)
+    panel_kernel(T* __restrict__ A, int lda, int m, int r0, int nb, int rpc, int* __restrict__ pos,
+                 int* __restrict__ piv, PanelWs ws, PanelXchg<T> x) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* slab = reinterpret_cast<T*>(smem_raw);  // slab[c * rpc + i]
+    __shared__ T prow[PANEL_MAX_NB];
+    __shared__ T red_v[PANEL_THREADS / 32];
+    __shared__ int red_i[PANEL_THREADS / 32];
+    __shared__ int s_win, s_wcta, s_best_row;
+    __shared__ T s_piv;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int b = blockIdx.x, P = gridDim.x;
+    const int R = m - r0;
+    const int row_lo = b * rpc;
+    const int row_hi = min(R, row_lo + rpc);
+    const int nrows = max(0, row_hi - row_lo);
+
+    for (int e = tid; e < nrows * nb; e += blockDim.x) {
+        const int c = e / nrows, i = e - c * nrows;
+        slab[c * rpc + i] = A[(size_t)(r0 + row_lo + i) + (size_t)(r0 + c) * lda];
+    }
+    __syncthreads();
+
+    for (int c = 0; c < nb; ++c) {
+        const int buf = c & 1;
+        // 1. local candidate: largest |a| in column c over rows >= c, smallest row on ties
+        T best = T(-1);
+        int brow = INT_MAX;
+        for (int i = tid; i < nrows; i += blockDim.x) {
+            const int lr = row_lo + i;
+            if (lr < c) continue;
+            better(best, brow, fabs(slab[c * rpc + i]), lr);
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const T ov = __shfl_down_sync(0xffffffffu, best, off);
+            const int oi = __shfl_down_sync(0xffffffffu, brow, off);
+            better(best, brow, ov, oi);
+        }
+        if (lane == 0) {
+            red_v[warp] = best;
+            red_i[warp] = brow;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < PANEL_THREADS / 32; ++w) better(best, brow, red_v[w], red_i[w]);
+            s_best_row = brow;
+            __stcg(x.cand_val + buf * P + b, best);
+            __stcg(x.cand_row + buf * P + b, brow);
+        }
+        __syncthreads();
+        // 2. publish the candidate row and (by its owner) the diagonal row
+        {
+            const int br = s_best_row;
+            if (br != INT_MAX)
+                for (int j = tid; j < nb; j += blockDim.x)
+                    __stcg(x.cand_rows + ((size_t)buf * P + b) * nb + j, slab[j * rpc + (br - row_lo)]);
+            if (c >= row_lo && c < row_hi)
+                for (int j = tid; j < nb; j += blockDim.x)
+                    __stcg(x.diag_row + buf * nb + j, slab[j * rpc + (c - row_lo)]);
+        }
+        if (!mg::grid_barrier(ws.bar, (unsigned)(c + 1) * P, ws.err)) return;
+        // 3. the winner, identically in every CTA
+        if (warp == 0) {
+            T v = T(-1);
+            int r = INT_MAX, wc = -1;
+            for (int q = lane; q < P; q += 32) {
+                const T ov = ld_cg(x.cand_val + buf * P + q);
+                const int orow = ld_cg(x.cand_row + buf * P + q);
+                if (ov > v || (ov == v && orow < r)) {
+                    v = ov;
+                    r = orow;
+                    wc = q;
+                }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const T ov = __shfl_down_sync(0xffffffffu, v, off);
+                const int orow = __shfl_down_sync(0xffffffffu, r, off);
+                const int owc = __shfl_down_sync(0xffffffffu, wc, off);
+                if (ov > v || (ov == v && orow < r)) {
+                    v = ov;
+                    r = orow;
+                    wc = owc;
+                }
+            }
+            if (lane == 0) {
+                s_win = r;
+                s_wcta = wc;
+                s_piv = v;
+            }
+        }
+        __syncthreads();
+        const int win = s_win;
+        if (!(s_piv > T(0))) {
+            // exactly zero column: no interchange, no scaling (LAPACK semantics)
+            if (b == 0 && tid == 0) {
+                piv[c] = c;
+                atomicCAS(ws.info, 0, r0 + c + 1);
+            }
+            continue;
+        }
+        for (int j = tid; j < nb; j += blockDim.x) prow[j] = ld_cg(x.cand_rows + ((size_t)buf * P + s_wcta) * nb + j);
+        __syncthreads();
+        // 4. interchange rows c and win
+        if (win != c) {
+            if (c >= row_lo && c < row_hi)
+                for (int j = tid; j < nb; j += blockDim.x) slab[j * rpc + (c - row_lo)] = prow[j];
+            if (win >= row_lo && win < row_hi)
+                for (int j = tid; j < nb; j += blockDim.x)
+                    slab[j * rpc + (win - row_lo)] = ld_cg(x.diag_row + buf * nb + j);
+        }
+        if (b == 0 && tid == 0) {
+            piv[c] = win;
+            if (win != c) {
+                const int t = pos[r0 + c];
+                pos[r0 + c] = pos[r0 + win];
+                pos[r0 + win] = t;
+            }
+        }
+        __syncthreads();
+        // 5. scale by the reciprocal and update the rows below (fused, Mat's order)
+        const T inv = T(1) / prow[c];
+        for (int i = tid; i < nrows; i += blockDim.x) {
+            const int lr = row_lo + i;
+            if (lr <= c) continue;
+            const T l = slab[c * rpc + i] * inv;
+            slab[c * rpc + i] = l;
+            for (int j = c + 1; j < nb; ++j) slab[j * rpc + i] = fma(l, -prow[j], slab[j * rpc + i]);
+        }
+        __syncthreads();
+    }
+
+    for (int e = tid; e < nrows * nb; e += blockDim.x) {
+        const int c = e / nrows, i = e - c * nrows;
+        A[(size_t)(r0 + row_lo + i) + (size_t)(r0 + c) * lda] = slab[c * rpc + i];
+    }
+}
+
+// Interchanges rows r0+k <-> r0+piv[k] (k = 0..kc-1, in order) on columns
+// [0, c_left) and [c_right, n).
+template <typename T>
+__global__ void laswp_kernel(T* __restrict__ A, int lda, int r0, int kc, const int* __restrict__ piv, int c_left,
+                             int c_right, int n) {
+    __shared__ int sp[PANEL_MAX_NB];
+    for (int k = threadIdx.x; k < kc; k += blockDim.x) sp[k] = piv[k];
+    __syncthreads();
+    const int nl = c_left, nr = max(0, n - c_right);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nl + nr; q += gridDim.x * blockDim.x) {
+        const int col = q < nl ? q : c_right + (q - nl);
+        T* cp = A + (size_t)col * lda + r0;
+        for (int k = 0; k < kc; ++k) {
+            const int j = sp[k];
+            if (j != k) {
+                const T t = cp[k];
+                cp[k] = cp[j];
+                cp[j] = t;
+            }
+        }
+    }
+}
+
+// X (k x n) := L^{-1} X with L unit lower (k <= PANEL_MAX_NB), one thread per
+// column, Mat's AVX-512 operation order (LU/__Base.h:95-208): columns of full
+// 8-groups use four partial sums s0..s3 over j = 0,4,8.. / 1,5,.. etc. and
+// x_i = s0 + (s1 + (s2 + s3)); the remaining n % 8 columns use fused
+// column updates x[i..] += L[i..][i-1] * (-x[i-1]), skipped when x[i-1] == 0.
+template <typename T>
+__global__ void trsm_llnu_kernel(int k, int n, const T* __restrict__ L, int ldl, T* __restrict__ X, int ldx) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sL = reinterpret_cast<T*>(smem_raw);       // [k][k] column-major
+    T* sx = sL + k * k;                           // [k][blockDim]
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) sL[e] = L[(e % k) + (size_t)(e / k) * ldl];
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nt = blockDim.x, t = threadIdx.x;
+    if (col < n)
+        for (int i = 0; i < k; ++i) sx[i * nt + t] = X[i + (size_t)col * ldx];
+    __syncthreads();
+    if (col >= n) return;
+    const int n8 = (n / 8) * 8;
+    if (col < n8) {
+        for (int i = 0; i < k; ++i) {
+            T s0 = sx[i * nt + t], s1 = 0, s2 = 0, s3 = 0;
+            int j = 0;
+            for (; j + 4 <= i; j += 4) {
+                s0 = fma(-sL[i + (j + 0) * k], sx[(j + 0) * nt + t], s0);
+                s1 = fma(-sL[i + (j + 1) * k], sx[(j + 1) * nt + t], s1);
+                s2 = fma(-sL[i + (j + 2) * k], sx[(j + 2) * nt + t], s2);
+                s3 = fma(-sL[i + (j + 3) * k], sx[(j + 3) * nt + t], s3);
+            }
+            for (; j < i; ++j) s0 = fma(-sL[i + j * k], sx[j * nt + t], s0);
+            sx[i * nt + t] = s0 + (s1 + (s2 + s3));
+        }
+    } else {
+        for (int i = 1; i < k; ++i) {
+            const T a = sx[(i - 1) * nt + t];
+            if (a == T(0)) continue;
+            for (int r = i; r < k; ++r) sx[r * nt + t] = fma(sL[r + (i - 1) * k], -a, sx[r * nt + t]);
+        }
+    }
+    for (int i = 0; i < k; ++i) X[i + (size_t)col * ldx] = sx[i * nt + t];
+}
+
+__global__ void iota_kernel(int* p, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = i;
+}
+
+// ------------------------------------------------------------ narrow solve
+// Forward substitution with unit L, Mat's narrow order (LU/__Solve_direct.h:125-130):
+// x[r] receives fma(L(r,k), -x[k], x[r]) for k = 0..r-1 ascending.  Blocked by
+// 64 columns: the diagonal block by one CTA, the rows below in parallel.
+constexpr int TRSV_B = 64;
+
+template <typename T>
+__global__ void trsv_lower_diag_kernel(int n, int nrhs, const T* __restrict__ L, int ldl, T* __restrict__ X,
+                                       int ldx, int b0, int b1) {
+    // one CTA; threads over rows of the block x rhs
+    const int bs = b1 - b0;
+    for (int k = b0; k < b1; ++k) {
+        for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) {
+            const int r = b0 + q % bs, j = q / bs;
+            if (r > k) {
+                T* x = X + (size_t)j * ldx;
+                x[r] = fma(L[r + (size_t)k * ldl], -x[k], x[r]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void trsv_lower_update_kernel(int n, int nrhs, const T* __restrict__ L, int ldl, T* __restrict__ X,
+                                         int ldx, int b0, int b1) {
+    __shared__ T xs[4][TRSV_B];
+    const int bs = b1 - b0;
+    for (int j0 = 0; j0 < nrhs; j0 += 4) {
+        const int nj = min(4, nrhs - j0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < bs * nj; q += blockDim.x) xs[q / bs][q % bs] = X[b0 + q % bs + (size_t)(j0 + q / bs) * ldx];
+        __syncthreads();
+        for (int r = b1 + blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+            T acc[4];
+            for (int j = 0; j < nj; ++j) acc[j] = X[r + (size_t)(j0 + j) * ldx];
+            for (int k = 0; k < bs; ++k) {
+                const T l = L[r + (size_t)(b0 + k) * ldl];
+                for (int j = 0; j < nj; ++j) acc[j] = fma(l, -xs[j][k], acc[j]);
+            }
+            for (int j = 0; j < nj; ++j) X[r + (size_t)(j0 + j) * ldx] = acc[j];
+        }
+    }
+}
+
+// Back substitution, Mat's narrow order (:132-139): for r = n-1..0:
+// x[r] /= U(r,r); x[i] = fma(U(i,r), -x[r], x[i]) for i < r.
+template <typename T>
+__global__ void trsv_upper_diag_kernel(int n, int nrhs, const T* __restrict__ U, int ldu, T* __restrict__ X,
+                                       int ldx, int b0, int b1) {
+    const int bs = b1 - b0;
+    for (int r = b1 - 1; r >= b0; --r) {
+        for (int j = threadIdx.x; j < nrhs; j += blockDim.x) X[r + (size_t)j * ldx] /= U[r + (size_t)r * ldu];
+        __syncthreads();
+        for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) {
+            const int i = b0 + q % bs, j = q / bs;
+            if (i < r) {
+                T* x = X + (size_t)j * ldx;
+                x[i] = fma(U[i + (size_t)r * ldu], -x[r], x[i]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void trsv_upper_update_kernel(int n, int nrhs, const T* __restrict__ U, int ldu, T* __restrict__ X,
+                                         int ldx, int b0, int b1) {
+    __shared__ T xs[4][TRSV_B];
+    const int bs = b1 - b0;
+    for (int j0 = 0; j0 < nrhs; j0 += 4) {
+        const int nj = min(4, nrhs - j0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < bs * nj; q += blockDim.x) xs[q / bs][q % bs] = X[b0 + q % bs + (size_t)(j0 + q / bs) * ldx];
+        __syncthreads();
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < b0; i += gridDim.x * blockDim.x) {
+            T acc[4];
+            for (int j = 0; j < nj; ++j) acc[j] = X[i + (size_t)(j0 + j) * ldx];
+            for (int k = bs - 1; k >= 0; --k) {
+                const T u = U[i + (size_t)(b0 + k) * ldu];
+                for (int j = 0; j < nj; ++j) acc[j] = fma(u, -xs[j][k], acc[j]);
+            }
+            for (int j = 0; j < nj; ++j) X[i + (size_t)(j0 + j) * ldx] = acc[j];
+        }
+    }
+}
+
+// X[i, j] = B[pos[i], j]
+template <typename T>
+__global__ void permute_rows_kernel(int n, int nrhs, const int* __restrict__ pos, const T* __restrict__ B, int ldb,
+                                    T* __restrict__ X, int ldx) {
+    const size_t total = (size_t)n * nrhs;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % n), j = (int)(e / n);
+        X[i + (size_t)j * ldx] = B[pos[i] + (size_t)j * ldb];
+    }
+}
+
+}  // namespace
+
+namespace mg {
+
+// Workspace carve-up for one getrf call (device): barrier/err/info words,
+// piv[PANEL_MAX_NB], exchange buffers sized for num_sms CTAs.
+template <typename T>
+static size_t getrf_ws_bytes(int num_sms) {
+    const size_t P = (size_t)num_sms;
+    return 256 + 4 * PANEL_MAX_NB + 2 * P * sizeof(T) + 2 * P * sizeof(int) + 2 * P * PANEL_MAX_NB * sizeof(T) +
+           2 * PANEL_MAX_NB * sizeof(T) + 1024;
+}
+
+template <typename T>
+struct GetrfCtx {
+    PanelWs ws;
+    PanelXchg<T> x;
+    int* piv;
+};
+
+template <typename T>
+static GetrfCtx<T> carve(void* base, int num_sms) {
+    char* p = (char*)base;
+    GetrfCtx<T> c;
+    c.ws.bar = (unsigned*)p;
+    c.ws.err = (int*)(p + 64);
+    c.ws.info = (int*)(p + 128);
+    p += 256;
+    c.piv = (int*)p;
+    p += align_up(4 * PANEL_MAX_NB, 256);
+    c.x.cand_val = (T*)p;
+    p += align_up(2 * (size_t)num_sms * sizeof(T), 256);
+    c.x.cand_row = (int*)p;
+    p += align_up(2 * (size_t)num_sms * sizeof(int), 256);
+    c.x.cand_rows = (T*)p;
+    p += align_up(2 * (size_t)num_sms * PANEL_MAX_NB * sizeof(T), 256);
+    c.x.diag_row = (T*)p;
+    return c;
+}
+
+template <typename T>
+static mg_status_t launch_panel(mg_handle_t h, GetrfCtx<T>& c, T* A, int lda, int m, int r0, int nb, int* pos) {
+    const int R = m - r0;
+    const size_t cap = (size_t)(h->max_smem_optin - 2048);
+    int P;
+    if ((size_t)R * nb * sizeof(T) <= 64 * 1024) {
+        P = 1;
+    } else {
+        P = (R + 127) / 128;
+        if (P > h->num_sms) P = h->num_sms;
+    }
+    int rpc = (R + P - 1) / P;
+    if ((size_t)rpc * nb * sizeof(T) > cap) {
+        return fail(h, MG_ERR_UNSUPPORTED, "panel of %d rows x %d columns exceeds shared memory of %d CTAs", R, nb,
+                    h->num_sms);
+    }
+    const size_t smem = (size_t)rpc * nb * sizeof(T);
+    auto kern = panel_kernel<T>;
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+    MG_CHECK_CUDA(h, cudaMemsetAsync(c.ws.bar, 0, sizeof(unsigned), h->stream));
+    void* args[] = {&A, &lda, &m, &r0, &nb, &rpc, &pos, &c.piv, &c.ws, &c.x};
+    cudaError_t e;
+    if (P > 1)
+        e = cudaLaunchCooperativeKernel((const void*)kern, dim3(P), dim3(PANEL_THREADS), args, smem, h->stream);
+    else
+        e = cudaLaunchKernel((const void*)kern, dim3(1), dim3(PANEL_THREADS), args, smem, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "panel_kernel launch");
+    h->launches++;
+    return MG_OK;
+}
+
+template <typename T>
+static mg_status_t launch_laswp(mg_handle_t h, T* A, int lda, int r0, int kc, const int* piv, int c_left,
+                                int c_right, int n) {
+    const int cols = c_left + (n > c_right ? n - c_right : 0);
+    if (cols <= 0 || kc <= 0) return MG_OK;
+    const int threads = 128;
+    int blocks = (cols + threads - 1) / threads;
+    laswp_kernel<T><<<blocks, threads, 0, h->stream>>>(A, lda, r0, kc, piv, c_left, c_right, n);
+    return post_launch(h, "laswp_kernel");
+}
+
+template <typename T>
+static mg_status_t launch_trsm_llnu(mg_handle_t h, int k, int n, const T* L, int ldl, T* X, int ldx) {
+    if (n <= 0 || k <= 0) return MG_OK;
+    const int threads = 64;
+    const size_t smem = ((size_t)k * k + (size_t)k * threads) * sizeof(T);
+    auto kern = trsm_llnu_kernel<T>;
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<(n + threads - 1) / threads, threads, smem, h->stream>>>(k, n, L, ldl, X, ldx);
+    return post_launch(h, "trsm_llnu_kernel");
+}
+
+// In-place PLU; pos (device, m ints) receives Mat's permutation.  Returns
+// MG_OK, MG_SINGULAR (info = first zero-pivot column, 1-based) or an error.
+mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* pos, int* info_out) {
+    if (info_out) *info_out = 0;
+    if (m == 0 || n == 0) return MG_OK;
+    MG_TRY(ensure_ws(h, getrf_ws_bytes<double>(h->num_sms)));
+    MG_TRY(ensure_hws(h, 64));
+    GetrfCtx<double> c = carve<double>(h->ws, h->num_sms);
+    MG_CHECK_CUDA(h, cudaMemsetAsync(h->ws, 0, 256, h->stream));
+    iota_kernel<<<(m + 255) / 256, 256, 0, h->stream>>>(pos, m);
+    MG_TRY(post_launch(h, "iota_kernel"));
+
+    const int s = m < n ? m : n;
+    if (s <= LU_BS * 3 / 2) {
+        // Mat's unblocked __PLU2 (LU/__PLU.h:22-51): one panel over all s
+        // columns, interchanges on every column.
+        MG_TRY(launch_panel<double>(h, c, A, lda, m, 0, s, pos));
+        MG_TRY(launch_laswp<double>(h, A, lda, 0, s, c.piv, 0, s, n));
+        if (n > s) {
+            MG_TRY(launch_trsm_llnu<double>(h, s, n - s, A, lda, A + (size_t)s * lda, lda));
+        }
+    } else {
+        int r = 0;
+        for (; r + LU_BS <= s; r += LU_BS) {
+            MG_TRY(launch_panel<double>(h, c, A, lda, m, r, LU_BS, pos));
+            MG_TRY(launch_laswp<double>(h, A, lda, r, LU_BS, c.piv, r, r + LU_BS, n));
+            if (r + LU_BS < s) {
+                const int nt = n - (r + LU_BS);
+                double* A12 = A + r + (size_t)(r + LU_BS) * lda;
+                MG_TRY(launch_trsm_llnu<double>(h, LU_BS, nt, A + r + (size_t)r * lda, lda, A12, lda));
+                MG_TRY(dgemm_launch(h, 0, 0, m - (r + LU_BS), nt, LU_BS, -1.0, A + (r + LU_BS) + (size_t)r * lda,
+                                    lda, A12, lda, 1.0, A + (r + LU_BS) + (size_t)(r + LU_BS) * lda, lda, 0));
+            }
+        }
+        if (r < s) {
+            const int rem = s - r;
+            MG_TRY(launch_panel<double>(h, c, A, lda, m, r, rem, pos));
+            MG_TRY(launch_laswp<double>(h, A, lda, r, rem, c.piv, r, n, n));
+        }
+    }
+    int* hw = (int*)h->hws;
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, c.ws.err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw + 1, c.ws.info, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (hw[0]) return fail(h, MG_TIMEOUT, "dgetrf: a panel grid barrier timed out");
+    if (info_out) *info_out = hw[1];
+    if (hw[1]) return fail(h, MG_SINGULAR, "dgetrf: exactly zero pivot column %d", hw[1]);
+    return MG_OK;
+}
+
+// X := A^{-1} B given the in-place factors, pos from dgetrf_impl (Mat's
+// narrow substitution order for every column).
+mg_status_t dgetrs_impl(mg_handle_t h, int n, int nrhs, const double* LU, int lda, const int* pos,
+                        const double* B, int ldb, double* X, int ldx) {
+    if (n == 0 || nrhs == 0) return MG_OK;
+    {
+        const size_t total = (size_t)n * nrhs;
+        int blocks = (int)((total + 255) / 256);
+        if (blocks > h->num_sms * 8) blocks = h->num_sms * 8;
+        permute_rows_kernel<double><<<blocks, 256, 0, h->stream>>>(n, nrhs, pos, B, ldb, X, ldx);
+        MG_TRY(post_launch(h, "permute_rows_kernel"));
+    }
+    const int ublocks = h->num_sms;
+    for (int b0 = 0; b0 < n; b0 += TRSV_B) {
+        const int b1 = b0 + TRSV_B < n ? b0 + TRSV_B : n;
+        trsv_lower_diag_kernel<double><<<1, 256, 0, h->stream>>>(n, nrhs, LU, lda, X, ldx, b0, b1);
+        MG_TRY(post_launch(h, "trsv_lower_diag_kernel"));
+        if (b1 < n) {
+            int blocks = (n - b1 + 127) / 128;
+            if (blocks > ublocks) blocks = ublocks;
+            trsv_lower_update_kernel<double><<<blocks, 128, 0, h->stream>>>(n, nrhs, LU, lda, X, ldx, b0, b1);
+            MG_TRY(post_launch(h, "trsv_lower_update_kernel"));
+        }
+    }
+    const int last = ((n - 1) / TRSV_B) * TRSV_B;
+    for (int b0 = last; b0 >= 0; b0 -= TRSV_B) {
+        const int b1 = b0 + TRSV_B < n ? b0 + TRSV_B : n;
+        trsv_upper_diag_kernel<double><<<1, 256, 0, h->stream>>>(n, nrhs, LU, lda, X, ldx, b0, b1);
+        MG_TRY(post_launch(h, "trsv_upper_diag_kernel"));
+        if (b0 > 0) {
+            int blocks = (b0 + 127) / 128;
+            if (blocks > ublocks) blocks = ublocks;
+            trsv_upper_update_kernel<double><<<blocks, 128, 0, h->stream>>>(n, nrhs, LU, lda, X, ldx, b0, b1);
+            MG_TRY(post_launch(h, "trsv_upper_update_kernel"));
+        }
+    }
+    return MG_OK;
+}
+
+}  // namespace mg
+
+extern "C" {
+
+mg_status_t mg_dgetrf(mg_handle_t h, int m, int n, double* A, int lda, int* pos, int* info) {
+    if (!h) return MG_ERR_ARG;
+    if (m < 0 || n < 0 || lda < (m > 1 ? m : 1) || ((size_t)m * n && (!A || !pos)))
+        return mg::fail(h, MG_ERR_ARG, "mg_dgetrf: bad arguments (m=%d n=%d lda=%d)", m, n, lda);
+    return mg::dgetrf_impl(h, m, n, A, lda, pos, info);
+}
+
+mg_status_t mg_dgetrs(mg_handle_t h, int n, int nrhs, const double* LU, int lda, const int* pos, const double* B,
+                      int ldb, double* X, int ldx) {
+    if (!h) return MG_ERR_ARG;
+    if (n < 0 || nrhs < 0 || lda < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1) || ldx < (n > 1 ? n : 1))
+        return mg::fail(h, MG_ERR_ARG, "mg_dgetrs: bad arguments");
+    if ((size_t)n * nrhs && (!LU || !pos || !B || !X)) return mg::fail(h, MG_ERR_ARG, "mg_dgetrs: null pointer");
+    if (B == X && ldb != ldx) return mg::fail(h, MG_ERR_ARG, "mg_dgetrs: in-place B needs ldb == ldx");
+    if (B == X) return mg::fail(h, MG_ERR_ARG, "mg_dgetrs: B and X must not alias");
+    return mg::dgetrs_impl(h, n, nrhs, LU, lda, pos, B, ldb, X, ldx);
+}
+
+mg_status_t mg_dgesv(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B, int ldb, double* X,
+                     int ldx, int* info) {
+    if (!h) return MG_ERR_ARG;
+    if (n < 0 || nrhs < 0 || lda < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1) || ldx < (n > 1 ? n : 1))
+        return mg::fail(h, MG_ERR_ARG, "mg_dgesv: bad arguments");
+    if (info) *info = 0;
+    if (n == 0 || nrhs == 0) return MG_OK;
+    // Solve_direct takes A by value (LU/__Solve_direct.h:146): factor a copy.
+    const size_t abytes = mg::align_up((size_t)n * n * sizeof(double), 256);
+    const size_t pbytes = mg::align_up((size_t)n * sizeof(int), 256);
+    // the copy lives after the getrf workspace
+    const size_t base = mg::align_up(mg::getrf_ws_bytes<double>(h->num_sms), 256);
+    MG_TRY(mg::ensure_ws(h, base + abytes + pbytes));
+    double* Acopy = (double*)((char*)h->ws + base);
+    int* pos = (int*)((char*)h->ws + base + abytes);
+    MG_CHECK_CUDA(h, cudaMemcpy2DAsync(Acopy, (size_t)n * sizeof(double), A, (size_t)lda * sizeof(double),
+                                       (size_t)n * sizeof(double), n, cudaMemcpyDeviceToDevice, h->stream));
+    mg_status_t s = mg::dgetrf_impl(h, n, n, Acopy, n, pos, info);
+    if (s != MG_OK && s != MG_SINGULAR) return s;
+    MG_TRY(mg::dgetrs_impl(h, n, nrhs, Acopy, n, pos, B, ldb, X, ldx));
+    return s;
+}
+
+}  // extern "C"
