@@ -133,6 +133,48 @@ mg_status_t mg_sgemm_bf16x(mg_handle_t h, int nterms, int m, int n, int k, float
 /* Device error word of the last split GEMM (MG_TIMEOUT if a bounded wait gave up). */
 mg_status_t mg_bf16x_check_error(mg_handle_t h, int* device_err_flag);
 
+/* ------------------------------------------- mixed LU + refinement solve
+ * X = A^{-1} B (n x nrhs, nrhs <= 8) to FP64 normwise backward error:
+ * fp32 LU with partial pivoting (fp32 panels, split-BF16 tensor-core
+ * trailing updates, fp32 accumulation), then FP64 iterative refinement
+ * (r = b - A x in fp64, fp32 correction solves, fp64 update) until every
+ * column satisfies ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= tol.
+ * If refinement stalls it falls back to the plain FP64 GPU solve
+ * (mg_dgesv) and returns MG_FALLBACK_USED (or MG_IR_STALLED when fallback
+ * is off).  The mixed counterpart of Mat's Solve_direct
+ * (Mat-8.3.1/LU/__Solve_direct.h:146-220), which has no mixed precision.
+ * A and B are not modified.  Synchronises. */
+typedef struct mg_ir_opts {
+    double tol;    /* target backward error, default 1e-14 */
+    int max_iter;  /* refinement iterations, default 30 */
+    int nterms;    /* bf16 terms of the split updates (1..3), default 3 */
+    int fallback;  /* nonzero: FP64 solve when refinement stalls (default 1) */
+} mg_ir_opts;
+
+typedef struct mg_ir_report {
+    int iterations;        /* refinement steps taken */
+    int path;              /* 0 = refinement converged, 2 = FP64 fallback */
+    int info;              /* first exactly-zero pivot column of the fp32 LU (1-based) */
+    int reserved;
+    double backward_error; /* final max-over-columns normwise backward error */
+    double anorm_inf;      /* ||A||_inf */
+    double factor_ms;      /* host wall time of the fp32 factorization */
+    double refine_ms;      /* host wall time of the refinement loop */
+    double history[32];    /* backward error before each correction */
+} mg_ir_report;
+
+mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
+                         int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* report);
+
+/* ------------------------------------------------ benchmark input generators
+ * A = Q1 diag(sigma) Q2 with Q1, Q2 products of `nrefl` Householder
+ * reflectors whose vectors are iid N(0,1) (seeded), sigma geometric from 1
+ * down to sigma_min (condition number 1/sigma_min). */
+mg_status_t mg_gen_svd_matrix(mg_handle_t h, int n, double* A, int lda, uint64_t seed, int nrefl,
+                              double sigma_min);
+/* S = G G^T / n + I with G iid N(0,1) (seeded, row-major stream order). */
+mg_status_t mg_gen_spd_gram(mg_handle_t h, int n, double* S, int lds, uint64_t seed);
+
 /* Measures the FP64 peaks of this GPU with dependent-free FMA / DMMA loops
  * (TFLOP/s, counting an FMA as 2 flops).  Synchronises. */
 mg_status_t mg_measure_fp64_peaks(mg_handle_t h, double* dfma_tflops, double* dmma_tflops);

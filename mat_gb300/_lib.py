@@ -25,6 +25,16 @@ f32 = C.c_float
 pi32 = C.POINTER(C.c_int)
 pf64 = C.POINTER(C.c_double)
 
+
+class IrOpts(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("nterms", C.c_int), ("fallback", C.c_int)]
+
+
+class IrReport(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("path", C.c_int), ("info", C.c_int), ("reserved", C.c_int),
+                ("backward_error", C.c_double), ("anorm_inf", C.c_double), ("factor_ms", C.c_double),
+                ("refine_ms", C.c_double), ("history", C.c_double * 32)]
+
 # name -> (restype, argtypes); every symbol here is declared in include/mat_gpu.h
 SIGNATURES: dict[str, tuple] = {
     "mg_handle_create": (i32, [C.POINTER(vp), vp]),
@@ -50,6 +60,9 @@ SIGNATURES: dict[str, tuple] = {
     "mg_dgesv": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, pi32]),
     "mg_sgemm_bf16x": (i32, [vp, i32, i32, i32, i32, f32, vp, i32, vp, i32, f32, vp, i32]),
     "mg_bf16x_check_error": (i32, [vp, pi32]),
+    "mg_dsgesv_ir": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, C.POINTER(IrOpts), C.POINTER(IrReport)]),
+    "mg_gen_svd_matrix": (i32, [vp, i32, vp, i32, u64, i32, f64]),
+    "mg_gen_spd_gram": (i32, [vp, i32, vp, i32, u64]),
 }
 
 _lib = None

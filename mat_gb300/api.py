@@ -12,7 +12,7 @@ import ctypes as C
 
 import torch
 
-from ._lib import MatGpuError, load
+from ._lib import IrOpts, IrReport, MatGpuError, load
 
 _F64 = torch.float64
 
@@ -153,6 +153,36 @@ class Handle:
         if st not in (0, 4):
             self.check(st, "mg_dgesv")
         return X, info.value
+
+    # ----------------------------------------------------------------- mixed
+    def dsgesv_ir(self, A, B, X=None, tol=1e-14, max_iter=30, nterms=3, fallback=True):
+        """Mixed LU (fp32 + split-BF16) + FP64 refinement. Returns (X, report dict, status)."""
+        n = A.shape[0]
+        nrhs = B.shape[1]
+        if X is None:
+            X = colmajor(n, nrhs, device=B.device)
+        o = IrOpts(tol, max_iter, nterms, int(fallback))
+        r = IrReport()
+        st = self.lib.mg_dsgesv_ir(self.h, n, nrhs, _ptr(A), ld_of(A), _ptr(B), ld_of(B), _ptr(X), ld_of(X),
+                                   C.byref(o), C.byref(r))
+        if st not in (0, 6, 7):
+            self.check(st, "mg_dsgesv_ir")
+        rep = dict(iterations=r.iterations, path=r.path, info=r.info, backward_error=r.backward_error,
+                   anorm_inf=r.anorm_inf, factor_ms=r.factor_ms, refine_ms=r.refine_ms,
+                   history=[r.history[i] for i in range(min(32, r.iterations + 1))], status=st)
+        return X, rep
+
+    # ------------------------------------------------------------- generators
+    def gen_svd_matrix(self, A, seed, nrefl=64, sigma_min=1e-6):
+        n = A.shape[0]
+        self.check(self.lib.mg_gen_svd_matrix(self.h, n, _ptr(A), ld_of(A), seed, nrefl, sigma_min),
+                   "mg_gen_svd_matrix")
+        return A
+
+    def gen_spd_gram(self, S, seed):
+        n = S.shape[0]
+        self.check(self.lib.mg_gen_spd_gram(self.h, n, _ptr(S), ld_of(S), seed), "mg_gen_spd_gram")
+        return S
 
     def measure_fp64_peaks(self) -> tuple[float, float]:
         a, b = C.c_double(), C.c_double()

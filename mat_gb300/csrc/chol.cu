@@ -1,0 +1,253 @@
+// Blocked right-looking Cholesky (Mat's LLT) and the Cholesky solve.
+//
+// Reference path (Mat-8.3.1/LU/__LLT.h): LLT (:212-246) copies the lower
+// triangle and calls __LLT (:94-150), BS = 48 (AVX-512, Mat.h:73-75): per
+// block column the unblocked __LLT2 on the diagonal block (:3-13), the
+// right-side solve __Solve_direct_XLT on the blocks below (:30-40), and the
+// trailing update C -= L21 * L21^T (__times_A_BT_LLT, :59-91) on full
+// blocks from the diagonal down; matrices of at most 2*BS columns use __LLT2
+// alone; the strict upper triangle is zeroed at the end.
+//
+// GPU kernels keep Mat's per-element operation sequence (so results are
+// bit-identical): the diagonal block by one CTA with one thread per row;
+// X := X L^{-T} by one thread per row of the panel (rows are independent);
+// the trailing update by the FP64 DMMA GEMM in its in-place C -= A B^T mode
+// restricted to tiles that meet the lower triangle.
+#include "mg_internal.cuh"
+
+namespace {
+
+constexpr int LLT_BS = 48;        // Mat-8.3.1/Mat.h:73-75 (AVX-512)
+constexpr int LLT2_MAX = 2 * LLT_BS;
+
+// Unblocked Cholesky of the k x k block at L (k <= 96), in place, lower part.
+// Column jj: t = 1/sqrt(L(jj,jj)); L(r,jj) *= t for r >= jj; then for
+// i > jj: L(r,i) = fma(L(r,jj), -L(i,jj), L(r,i)) for r >= i.
+__global__ void llt2_kernel(double* __restrict__ L, int ldl, int k, int col0, int* __restrict__ info) {
+    __shared__ double s[LLT2_MAX * LLT2_MAX];  // column-major k x k
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+        const int r = e % k, c = e / k;
+        s[r + c * LLT2_MAX] = L[r + (size_t)c * ldl];
+    }
+    __syncthreads();
+    const int r = threadIdx.x;
+    for (int jj = 0; jj < k; ++jj) {
+        const double d = s[jj + jj * LLT2_MAX];
+        const double t = 1.0 / sqrt(d);
+        if (r == 0 && !(d > 0.0)) atomicCAS(info, 0, col0 + jj + 1);
+        if (r >= jj && r < k) s[r + jj * LLT2_MAX] = s[r + jj * LLT2_MAX] * t;
+        __syncthreads();
+        if (r > jj && r < k) {
+            const double lrj = s[r + jj * LLT2_MAX];
+            for (int i = jj + 1; i <= r; ++i) s[r + i * LLT2_MAX] = fma(lrj, -s[i + jj * LLT2_MAX], s[r + i * LLT2_MAX]);
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+        const int rr = e % k, c = e / k;
+        if (rr >= c) L[rr + (size_t)c * ldl] = s[rr + c * LLT2_MAX];
+    }
+}
+
+// X (rows x k) := X * Lkk^{-T} (Mat's __Solve_direct_XLT), one thread per row:
+// for j: x_j *= 1/L(j,j); x_kk = fma(x_j, -L(kk,j), x_kk) for kk > j.
+__global__ void xlt_kernel(const double* __restrict__ Ld, int ldl, double* __restrict__ X, int ldx, int rows, int k) {
+    __shared__ double sl[LLT_BS * LLT_BS];
+    __shared__ double sinv[LLT_BS];
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) sl[e] = Ld[(e % k) + (size_t)(e / k) * ldl];
+    __syncthreads();
+    for (int j = threadIdx.x; j < k; j += blockDim.x) sinv[j] = 1.0 / sl[j + j * k];
+    __syncthreads();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    double x[LLT_BS];
+#pragma unroll
+    for (int j = 0; j < LLT_BS; ++j) x[j] = j < k ? X[r + (size_t)j * ldx] : 0.0;
+#pragma unroll
+    for (int j = 0; j < LLT_BS; ++j) {
+        if (j < k) {
+            x[j] = x[j] * sinv[j];
+#pragma unroll
+            for (int kk = j + 1; kk < LLT_BS; ++kk)
+                if (kk < k) x[kk] = fma(x[j], -sl[kk + j * k], x[kk]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < LLT_BS; ++j)
+        if (j < k) X[r + (size_t)j * ldx] = x[j];
+}
+
+__global__ void zero_upper_kernel(double* __restrict__ L, int ldl, int n) {
+    const size_t total = (size_t)n * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(e % n), c = (int)(e / n);
+        if (r < c) L[r + (size_t)c * ldl] = 0.0;
+    }
+}
+
+// Forward / back substitution with L (lower, non-unit) for the Cholesky solve,
+// blocked by 64 rows like the LU narrow solve: per element a chain over k in
+// ascending (L z = b) or descending (L^T x = z) order.
+constexpr int CS_B = 64;
+
+__global__ void chol_fwd_diag_kernel(int n, int nrhs, const double* __restrict__ L, int ldl, double* __restrict__ X,
+                                     int ldx, int b0, int b1) {
+    const int bs = b1 - b0;
+    for (int k = b0; k < b1; ++k) {
+        for (int j = threadIdx.x; j < nrhs; j += blockDim.x) X[k + (size_t)j * ldx] /= L[k + (size_t)k * ldl];
+        __syncthreads();
+        for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) {
+            const int r = b0 + q % bs, j = q / bs;
+            if (r > k) X[r + (size_t)j * ldx] = fma(L[r + (size_t)k * ldl], -X[k + (size_t)j * ldx], X[r + (size_t)j * ldx]);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void chol_fwd_update_kernel(int n, int nrhs, const double* __restrict__ L, int ldl, double* __restrict__ X,
+                                       int ldx, int b0, int b1) {
+    __shared__ double xs[4][CS_B];
+    const int bs = b1 - b0;
+    for (int j0 = 0; j0 < nrhs; j0 += 4) {
+        const int nj = min(4, nrhs - j0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < bs * nj; q += blockDim.x) xs[q / bs][q % bs] = X[b0 + q % bs + (size_t)(j0 + q / bs) * ldx];
+        __syncthreads();
+        for (int r = b1 + blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+            double acc[4];
+            for (int j = 0; j < nj; ++j) acc[j] = X[r + (size_t)(j0 + j) * ldx];
+            for (int k = 0; k < bs; ++k) {
+                const double l = L[r + (size_t)(b0 + k) * ldl];
+                for (int j = 0; j < nj; ++j) acc[j] = fma(l, -xs[j][k], acc[j]);
+            }
+            for (int j = 0; j < nj; ++j) X[r + (size_t)(j0 + j) * ldx] = acc[j];
+        }
+    }
+}
+
+// L^T x = z: row i of L^T is column i of L.
+__global__ void chol_bwd_diag_kernel(int n, int nrhs, const double* __restrict__ L, int ldl, double* __restrict__ X,
+                                     int ldx, int b0, int b1) {
+    const int bs = b1 - b0;
+    for (int k = b1 - 1; k >= b0; --k) {
+        for (int j = threadIdx.x; j < nrhs; j += blockDim.x) X[k + (size_t)j * ldx] /= L[k + (size_t)k * ldl];
+        __syncthreads();
+        for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) {
+            const int i = b0 + q % bs, j = q / bs;
+            if (i < k) X[i + (size_t)j * ldx] = fma(L[k + (size_t)i * ldl], -X[k + (size_t)j * ldx], X[i + (size_t)j * ldx]);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void chol_bwd_update_kernel(int n, int nrhs, const double* __restrict__ L, int ldl, double* __restrict__ X,
+                                       int ldx, int b0, int b1) {
+    // rows i < b0: x_i -= sum_{k in block} L(k,i) x_k  (k descending); one warp per row i
+    __shared__ double xs[4][CS_B];
+    const int bs = b1 - b0;
+    const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    for (int j0 = 0; j0 < nrhs; j0 += 4) {
+        const int nj = min(4, nrhs - j0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < bs * nj; q += blockDim.x) xs[q / bs][q % bs] = X[b0 + q % bs + (size_t)(j0 + q / bs) * ldx];
+        __syncthreads();
+        for (int i = blockIdx.x * warps + (threadIdx.x >> 5); i < b0; i += gridDim.x * warps) {
+            if (lane < nj) {
+                double acc = X[i + (size_t)(j0 + lane) * ldx];
+                const double* lp = L + (size_t)i * ldl + b0;  // L(b0.., i): contiguous in column i
+                for (int k = bs - 1; k >= 0; --k) acc = fma(lp[k], -xs[lane][k], acc);
+                X[i + (size_t)(j0 + lane) * ldx] = acc;
+            }
+        }
+    }
+}
+
+}  // namespace
+
+namespace mg {
+
+mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out) {
+    if (info_out) *info_out = 0;
+    if (n == 0) return MG_OK;
+    MG_TRY(ensure_ws(h, 256));
+    MG_TRY(ensure_hws(h, 64));
+    int* dinfo = (int*)h->ws;
+    MG_CHECK_CUDA(h, cudaMemsetAsync(dinfo, 0, sizeof(int), h->stream));
+    cudaStream_t st = h->stream;
+    if (n <= 2 * LLT_BS) {
+        llt2_kernel<<<1, 128, 0, st>>>(L, ldl, n, 0, dinfo);
+        MG_TRY(post_launch(h, "llt2_kernel"));
+    } else {
+        for (int j = 0; j < n; j += LLT_BS) {
+            const int nb = n - j < LLT_BS ? n - j : LLT_BS;
+            double* D = L + j + (size_t)j * ldl;
+            llt2_kernel<<<1, 128, 0, st>>>(D, ldl, nb, j, dinfo);
+            MG_TRY(post_launch(h, "llt2_kernel"));
+            if (j + LLT_BS < n) {
+                const int rows = n - (j + LLT_BS);
+                double* P = L + (j + LLT_BS) + (size_t)j * ldl;
+                xlt_kernel<<<(rows + 127) / 128, 128, 0, st>>>(D, ldl, P, ldl, rows, LLT_BS);
+                MG_TRY(post_launch(h, "xlt_kernel"));
+                // C(i.., i..) -= P P^T on the trailing matrix, lower tiles only
+                MG_TRY(dgemm_launch(h, 0, 1, rows, rows, LLT_BS, -1.0, P, ldl, P, ldl, 1.0,
+                                    L + (j + LLT_BS) + (size_t)(j + LLT_BS) * ldl, ldl, 1));
+            }
+        }
+    }
+    zero_upper_kernel<<<h->num_sms * 8, 256, 0, st>>>(L, ldl, n);
+    MG_TRY(post_launch(h, "zero_upper_kernel"));
+    int* hw = (int*)h->hws;
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
+    if (info_out) *info_out = hw[0];
+    if (hw[0]) return fail(h, MG_NOT_SPD, "dpotrf: non-positive pivot at column %d", hw[0]);
+    return MG_OK;
+}
+
+mg_status_t dpotrs_impl(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* X, int ldx) {
+    if (n == 0 || nrhs == 0) return MG_OK;
+    cudaStream_t st = h->stream;
+    for (int b0 = 0; b0 < n; b0 += CS_B) {
+        const int b1 = b0 + CS_B < n ? b0 + CS_B : n;
+        chol_fwd_diag_kernel<<<1, 256, 0, st>>>(n, nrhs, L, ldl, X, ldx, b0, b1);
+        MG_TRY(post_launch(h, "chol_fwd_diag_kernel"));
+        if (b1 < n) {
+            int blocks = (n - b1 + 127) / 128;
+            if (blocks > h->num_sms) blocks = h->num_sms;
+            chol_fwd_update_kernel<<<blocks, 128, 0, st>>>(n, nrhs, L, ldl, X, ldx, b0, b1);
+            MG_TRY(post_launch(h, "chol_fwd_update_kernel"));
+        }
+    }
+    const int last = ((n - 1) / CS_B) * CS_B;
+    for (int b0 = last; b0 >= 0; b0 -= CS_B) {
+        const int b1 = b0 + CS_B < n ? b0 + CS_B : n;
+        chol_bwd_diag_kernel<<<1, 256, 0, st>>>(n, nrhs, L, ldl, X, ldx, b0, b1);
+        MG_TRY(post_launch(h, "chol_bwd_diag_kernel"));
+        if (b0 > 0) {
+            int blocks = (b0 + 7) / 8;
+            if (blocks > h->num_sms * 4) blocks = h->num_sms * 4;
+            chol_bwd_update_kernel<<<blocks, 256, 0, st>>>(n, nrhs, L, ldl, X, ldx, b0, b1);
+            MG_TRY(post_launch(h, "chol_bwd_update_kernel"));
+        }
+    }
+    return MG_OK;
+}
+
+}  // namespace mg
+
+extern "C" {
+
+mg_status_t mg_dpotrf(mg_handle_t h, int n, double* A, int lda, int* info) {
+    if (!h) return MG_ERR_ARG;
+    if (n < 0 || lda < (n > 1 ? n : 1) || (n && !A)) return mg::fail(h, MG_ERR_ARG, "mg_dpotrf: bad arguments");
+    return mg::dpotrf_impl(h, n, A, lda, info);
+}
+
+mg_status_t mg_dpotrs(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* B, int ldb) {
+    if (!h) return MG_ERR_ARG;
+    if (n < 0 || nrhs < 0 || ldl < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1) || ((size_t)n * nrhs && (!L || !B)))
+        return mg::fail(h, MG_ERR_ARG, "mg_dpotrs: bad arguments");
+    return mg::dpotrs_impl(h, n, nrhs, L, ldl, B, ldb);
+}
+
+}  // extern "C"

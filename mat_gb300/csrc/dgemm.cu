@@ -7,26 +7,43 @@
 // updates __mulAB_packed_n / _lower_tri_ / _upper_tri_ (Mul.h:240-322).
 //
 // Design.  tcgen05 has no f64 kind, so FP64 products run on the FP64 MMA
-// path (mma.sync m16n8k4 .f64, "DMMA").  On GB300 the FP64 rate is a few
-// flops per clock per SM, far below what HBM and shared memory can feed, so
-// the kernel is built to keep the DMMA pipe busy with the least issue
-// overhead: a 128x128 CTA tile, 8 warps with a 64x32 warp tile (16
-// independent MMAs per k-step), a 3-stage cp.async ring into padded shared
-// memory (strides chosen so fragment loads are bank-conflict free), and
-// zero-filled copies for the ragged M/N/K edges so the main loop has no edge
-// code.  The copies are 8-byte cp.async so any leading dimension and any
-// sub-matrix offset works (Mat's ld = rows is often odd).
+// path (mma.sync m16n8k4 .f64, "DMMA").  On GB300 the FP64 rate is about two
+// fused multiply-adds per clock per SM, far below what HBM and shared memory
+// can feed, so the kernel is built to keep the DMMA pipe busy: warps with
+// 8-16 independent MMAs per k-step, a 3-stage cp.async ring into padded
+// shared memory (strides chosen so fragment loads are bank-conflict free),
+// and zero-filled copies for the ragged M/N/K edges so the main loop has no
+// edge code.  The copies are 8-byte cp.async so any leading dimension and
+// any sub-matrix offset works (Mat's ld = rows is often odd).
+//
+// Every output element is one fused chain over k = 0..K-1 in order (the
+// DMMA k-step accumulates its four products in k order), starting from 0 or
+// from C in the in-place modes: exactly the per-element operation sequence
+// of Mat's micro-kernels, so results are bit-identical to Mat's operator*.
+// K is therefore never split across CTAs; small problems use a 32x32 tile
+// (one warp, up to 7 CTAs per SM) so the GPU is still filled.
 #include "mg_internal.cuh"
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 16;
-constexpr int SA = BM + 4;  // sA[k][m], stride = 4 (mod 16) doubles
-constexpr int SB = BK + 4;  // sB[n][k]
+constexpr int BK = 16;
 constexpr int STAGES = 3;
-constexpr int THREADS = 256;
-constexpr int STAGE_DOUBLES = BK * SA + BN * SB;
-constexpr size_t SMEM_BYTES = (size_t)STAGES * STAGE_DOUBLES * sizeof(double);
+constexpr int SB = BK + 4;  // sB[n][k] stride = 4 (mod 16) doubles
+
+// Tile configuration: WM x WN warps, each holding MI x NJ fragments of 16x8.
+template <int WM_, int WN_, int MI_, int NJ_>
+struct TileCfg {
+    static constexpr int WM = WM_, WN = WN_, MI = MI_, NJ = NJ_;
+    static constexpr int THREADS = WM * WN * 32;
+    static constexpr int BM = WM * MI * 16;
+    static constexpr int BN = WN * NJ * 8;
+    static constexpr int SA = BM + 4;  // sA[k][m], stride = 4 (mod 16) doubles
+    static constexpr int STAGE_DOUBLES = BK * SA + BN * SB;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE_DOUBLES * sizeof(double);
+    static_assert((BM * BK) % THREADS == 0 && (BN * BK) % THREADS == 0, "loader split");
+};
+using Big = TileCfg<2, 4, 4, 4>;    // 128 x 128, 8 warps
+using Small = TileCfg<1, 1, 2, 4>;  // 32 x 32, 1 warp
 
 __device__ __forceinline__ void cp_async8(double* smem, const double* gmem, bool pred) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -48,49 +65,32 @@ __device__ __forceinline__ void dmma_16x8x4(double (&c)[4], double a0, double a1
 }
 
 // Loads one BK slice of op(A) (rows bm.., k-columns k0..) and op(B) into a stage.
-template <int TA, int TB>
+template <class CF, int TA, int TB>
 __device__ __forceinline__ void load_stage(double* sA, double* sB, const double* __restrict__ A, int lda,
-                                           const double* __restrict__ B, int ldb, int M, int N, int K,
-                                           int bm, int bn, int k0, int tid) {
-    // op(A)(m,k): TA=0 -> A[m + k*lda], TA=1 -> A[k + m*lda]
-    if (TA == 0) {
-        const int m = tid % BM, kk = tid / BM;  // 2 k-rows per pass
-        const int gm = bm + m;
+                                           const double* __restrict__ B, int ldb, int M, int N, int K, int bm,
+                                           int bn, int k0, int tid) {
+    constexpr int NA = CF::BM * BK / CF::THREADS, NB = CF::BN * BK / CF::THREADS;
 #pragma unroll
-        for (int j = 0; j < BK / 2; ++j) {
-            const int k = kk + 2 * j, gk = k0 + k;
-            const bool p = gm < M && gk < K;
-            cp_async8(sA + k * SA + m, p ? A + gm + (size_t)gk * lda : A, p);
-        }
-    } else {
-        const int k = tid % BK, mm = tid / BK;  // 16 m per pass
-        const int gk = k0 + k;
-#pragma unroll
-        for (int j = 0; j < BM / 16; ++j) {
-            const int m = mm + 16 * j, gm = bm + m;
-            const bool p = gm < M && gk < K;
-            cp_async8(sA + k * SA + m, p ? A + gk + (size_t)gm * lda : A, p);
-        }
+    for (int j = 0; j < NA; ++j) {
+        const int e = tid + j * CF::THREADS;
+        // op(A)(m,k): TA=0 -> A[m + k*lda] (coalesce over m), TA=1 -> A[k + m*lda] (over k)
+        const int m = TA == 0 ? e % CF::BM : e / BK;
+        const int k = TA == 0 ? e / CF::BM : e % BK;
+        const int gm = bm + m, gk = k0 + k;
+        const bool p = gm < M && gk < K;
+        const double* src = TA == 0 ? A + gm + (size_t)gk * lda : A + gk + (size_t)gm * lda;
+        cp_async8(sA + k * CF::SA + m, p ? src : A, p);
     }
-    // op(B)(k,n): TB=0 -> B[k + n*ldb], TB=1 -> B[n + k*ldb]
-    if (TB == 0) {
-        const int k = tid % BK, nn = tid / BK;
-        const int gk = k0 + k;
 #pragma unroll
-        for (int j = 0; j < BN / 16; ++j) {
-            const int n = nn + 16 * j, gn = bn + n;
-            const bool p = gn < N && gk < K;
-            cp_async8(sB + n * SB + k, p ? B + gk + (size_t)gn * ldb : B, p);
-        }
-    } else {
-        const int n = tid % BN, kk = tid / BN;
-        const int gn = bn + n;
-#pragma unroll
-        for (int j = 0; j < BK / 2; ++j) {
-            const int k = kk + 2 * j, gk = k0 + k;
-            const bool p = gn < N && gk < K;
-            cp_async8(sB + n * SB + k, p ? B + gn + (size_t)gk * ldb : B, p);
-        }
+    for (int j = 0; j < NB; ++j) {
+        const int e = tid + j * CF::THREADS;
+        // op(B)(k,n): TB=0 -> B[k + n*ldb] (over k), TB=1 -> B[n + k*ldb] (over n)
+        const int k = TB == 0 ? e % BK : e / CF::BN;
+        const int n = TB == 0 ? e / BK : e % CF::BN;
+        const int gn = bn + n, gk = k0 + k;
+        const bool p = gn < N && gk < K;
+        const double* src = TB == 0 ? B + gk + (size_t)gn * ldb : B + gn + (size_t)gk * ldb;
+        cp_async8(sB + n * SB + k, p ? src : B, p);
     }
 }
 
@@ -102,25 +102,26 @@ __device__ __forceinline__ void load_stage(double* sA, double* sB, const double*
 //   2: acc = C,  acc += A*B, C = acc      (alpha == 1, beta == 1)
 //   3: acc = 0,  C = alpha*acc + beta*C   (general)
 // TRI = 1: only tiles containing elements with row >= col are computed.
-template <int TA, int TB, int MODE, int TRI>
-__global__ void __launch_bounds__(THREADS, 1)
+template <class CF, int TA, int TB, int MODE, int TRI>
+__global__ void __launch_bounds__(CF::THREADS)
     dgemm_kernel(int M, int N, int K, double alpha, const double* __restrict__ A, int lda,
                  const double* __restrict__ B, int ldb, double beta, double* __restrict__ C, int ldc) {
     extern __shared__ __align__(16) double smem[];
+    constexpr int MI = CF::MI, NJ = CF::NJ;
     const int tid = threadIdx.x;
-    const int bm = blockIdx.x * BM, bn = blockIdx.y * BN;
-    if (TRI && bm + BM - 1 < bn) return;
+    const int bm = blockIdx.x * CF::BM, bn = blockIdx.y * CF::BN;
+    if (TRI && bm + CF::BM - 1 < bn) return;
 
     const int warp = tid >> 5, lane = tid & 31;
     const int g = lane >> 2, t = lane & 3;
-    const int wm = (warp & 1) * 64;   // 2 warps along M
-    const int wn = (warp >> 1) * 32;  // 4 warps along N
+    const int wm = (warp % CF::WM) * (MI * 16);
+    const int wn = (warp / CF::WM) * (NJ * 8);
 
-    double acc[4][4][4];
+    double acc[MI][NJ][4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < MI; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < NJ; ++j)
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
                 double v = 0.0;
@@ -136,8 +137,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
     for (int s = 0; s < STAGES - 1; ++s) {
         if (s < ktiles) {
-            double* st = smem + s * STAGE_DOUBLES;
-            load_stage<TA, TB>(st, st + BK * SA, A, lda, B, ldb, M, N, K, bm, bn, s * BK, tid);
+            double* st = smem + s * CF::STAGE_DOUBLES;
+            load_stage<CF, TA, TB>(st, st + BK * CF::SA, A, lda, B, ldb, M, N, K, bm, bn, s * BK, tid);
         }
         cp_async_commit();
     }
@@ -149,40 +150,40 @@ __global__ void __launch_bounds__(THREADS, 1)
         {
             const int nk = kt + STAGES - 1;
             if (nk < ktiles) {
-                double* st = smem + (nk % STAGES) * STAGE_DOUBLES;
-                load_stage<TA, TB>(st, st + BK * SA, A, lda, B, ldb, M, N, K, bm, bn, nk * BK, tid);
+                double* st = smem + (nk % STAGES) * CF::STAGE_DOUBLES;
+                load_stage<CF, TA, TB>(st, st + BK * CF::SA, A, lda, B, ldb, M, N, K, bm, bn, nk * BK, tid);
             }
             cp_async_commit();
         }
-        const double* sA = smem + (kt % STAGES) * STAGE_DOUBLES;
-        const double* sB = sA + BK * SA;
+        const double* sA = smem + (kt % STAGES) * CF::STAGE_DOUBLES;
+        const double* sB = sA + BK * CF::SA;
 #pragma unroll
         for (int ks = 0; ks < BK; ks += 4) {
-            double a[4][2], b[4];
+            double a[MI][2], b[NJ];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                a[i][0] = sA[(ks + t) * SA + wm + 16 * i + g];
-                a[i][1] = sA[(ks + t) * SA + wm + 16 * i + g + 8];
+            for (int i = 0; i < MI; ++i) {
+                a[i][0] = sA[(ks + t) * CF::SA + wm + 16 * i + g];
+                a[i][1] = sA[(ks + t) * CF::SA + wm + 16 * i + g + 8];
                 if (MODE == 1) {
                     a[i][0] = -a[i][0];
                     a[i][1] = -a[i][1];
                 }
             }
 #pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = sB[(wn + 8 * j + g) * SB + ks + t];
+            for (int j = 0; j < NJ; ++j) b[j] = sB[(wn + 8 * j + g) * SB + ks + t];
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < MI; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) dmma_16x8x4(acc[i][j], a[i][0], a[i][1], b[j]);
+                for (int j = 0; j < NJ; ++j) dmma_16x8x4(acc[i][j], a[i][0], a[i][1], b[j]);
         }
     }
     cp_async_wait<0>();
 
     // Epilogue: c0,c1 -> (g, 2t..2t+1), c2,c3 -> (g+8, 2t..2t+1) of each 16x8 fragment.
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < MI; ++i) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < NJ; ++j) {
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
                 const int row = bm + wm + 16 * i + g + (r >= 2 ? 8 : 0);
@@ -201,19 +202,47 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
 }
 
-template <int TA, int TB, int MODE, int TRI>
-cudaError_t launch_t(cudaStream_t st, int M, int N, int K, double alpha, const double* A, int lda,
-                     const double* B, int ldb, double beta, double* C, int ldc) {
-    auto kern = dgemm_kernel<TA, TB, MODE, TRI>;
+template <class CF, int TA, int TB, int MODE, int TRI>
+cudaError_t launch_t(cudaStream_t st, int M, int N, int K, double alpha, const double* A, int lda, const double* B,
+                     int ldb, double beta, double* C, int ldc) {
+    auto kern = dgemm_kernel<CF, TA, TB, MODE, TRI>;
     static bool configured = false;  // per instantiation
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF::SMEM);
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN);
-    kern<<<grid, THREADS, SMEM_BYTES, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+    dim3 grid((M + CF::BM - 1) / CF::BM, (N + CF::BN - 1) / CF::BN);
+    kern<<<grid, CF::THREADS, CF::SMEM, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
     return cudaGetLastError();
+}
+
+template <class CF>
+cudaError_t dispatch(cudaStream_t st, int ta, int tb, int mode, int m, int n, int k, double alpha, const double* A,
+                     int lda, const double* B, int ldb, double beta, double* C, int ldc) {
+#define MG_MODE(TA, TB)                                                                              \
+    switch (mode) {                                                                                  \
+        case 0: return launch_t<CF, TA, TB, 0, 0>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc); \
+        case 1: return launch_t<CF, TA, TB, 1, 0>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc); \
+        case 2: return launch_t<CF, TA, TB, 2, 0>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc); \
+        default: return launch_t<CF, TA, TB, 3, 0>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc); \
+    }
+    if (!ta && !tb) {
+        MG_MODE(0, 0)
+    } else if (ta && !tb) {
+        MG_MODE(1, 0)
+    } else if (!ta && tb) {
+        MG_MODE(0, 1)
+    } else {
+        MG_MODE(1, 1)
+    }
+#undef MG_MODE
+}
+
+// Fraction of the machine the grid keeps busy when every SM holds `slots` CTAs.
+double fill_efficiency(long long tiles, long long slots) {
+    const long long waves = (tiles + slots - 1) / slots;
+    return (double)tiles / (double)(waves * slots);
 }
 
 // Scales C by beta (K == 0 or alpha == 0 cases).
@@ -240,32 +269,26 @@ mg_status_t dgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, in
         scale_kernel<<<h->num_sms * 4, 256, 0, st>>>(m, n, beta, C, ldc);
         return post_launch(h, "scale_kernel");
     }
-    const int mode = beta == 0.0                    ? 0
+    const int mode = beta == 0.0                      ? 0
                      : (alpha == -1.0 && beta == 1.0) ? 1
                      : (alpha == 1.0 && beta == 1.0)  ? 2
                                                       : 3;
     cudaError_t e;
-#define MG_MODE(TA, TB, MODE)                                                                \
-    e = tri ? launch_t<TA, TB, MODE, 1>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc)    \
-            : launch_t<TA, TB, MODE, 0>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
-#define MG_DISPATCH(TA, TB)          \
-    switch (mode) {                  \
-        case 0: MG_MODE(TA, TB, 0) break; \
-        case 1: MG_MODE(TA, TB, 1) break; \
-        case 2: MG_MODE(TA, TB, 2) break; \
-        default: MG_MODE(TA, TB, 3) break; \
-    }
-    if (!transA && !transB) {
-        MG_DISPATCH(0, 0)
-    } else if (transA && !transB) {
-        MG_DISPATCH(1, 0)
-    } else if (!transA && transB) {
-        MG_DISPATCH(0, 1)
+    if (tri) {
+        // Cholesky trailing update: C -= A * B^T on lower tiles only
+        if (transA || !transB || mode != 1)
+            return fail(h, MG_ERR_UNSUPPORTED, "dgemm_launch: triangular mode is C -= A*B^T only");
+        e = launch_t<Big, 0, 1, 1, 1>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
     } else {
-        MG_DISPATCH(1, 1)
+        const long long tb = (long long)((m + Big::BM - 1) / Big::BM) * ((n + Big::BN - 1) / Big::BN);
+        const long long ts = (long long)((m + Small::BM - 1) / Small::BM) * ((n + Small::BN - 1) / Small::BN);
+        // one 8-warp CTA per SM for the big tile; seven 1-warp CTAs per SM for the small one
+        const double eb = fill_efficiency(tb, h->num_sms), es = fill_efficiency(ts, 7LL * h->num_sms);
+        if (eb >= es - 0.03)
+            e = dispatch<Big>(st, transA, transB, mode, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+        else
+            e = dispatch<Small>(st, transA, transB, mode, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
     }
-#undef MG_MODE
-#undef MG_DISPATCH
     if (e != cudaSuccess) return cuda_fail(h, e, "dgemm_kernel launch");
     h->launches++;
     return MG_OK;

@@ -31,7 +31,7 @@
 namespace {
 
 constexpr int LU_BS = 60;           // Mat-8.3.1/Mat.h:69-71 (AVX-512)
-constexpr int PANEL_MAX_NB = 96;    // unblocked path handles s <= 1.5*BS = 90
+constexpr int PANEL_MAX_NB = 256;   // FP64 unblocked path: s <= 1.5*BS = 90; mixed LU: 128
 constexpr int PANEL_THREADS = 256;
 
 struct PanelWs {
@@ -413,7 +413,10 @@ static GetrfCtx<T> carve(void* base, int num_sms) {
 template <typename T>
 static mg_status_t launch_panel(mg_handle_t h, GetrfCtx<T>& c, T* A, int lda, int m, int r0, int nb, int* pos) {
     const int R = m - r0;
-    const size_t cap = (size_t)(h->max_smem_optin - 2048);
+    auto kern = panel_kernel<T>;
+    cudaFuncAttributes fa;
+    MG_CHECK_CUDA(h, cudaFuncGetAttributes(&fa, kern));
+    const size_t cap = (size_t)h->max_smem_optin - fa.sharedSizeBytes - 256;
     int P;
     if ((size_t)R * nb * sizeof(T) <= 64 * 1024) {
         P = 1;
@@ -427,8 +430,7 @@ static mg_status_t launch_panel(mg_handle_t h, GetrfCtx<T>& c, T* A, int lda, in
                     h->num_sms);
     }
     const size_t smem = (size_t)rpc * nb * sizeof(T);
-    auto kern = panel_kernel<T>;
-    MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     MG_CHECK_CUDA(h, cudaMemsetAsync(c.ws.bar, 0, sizeof(unsigned), h->stream));
     void* args[] = {&A, &lda, &m, &r0, &nb, &rpc, &pos, &c.piv, &c.ws, &c.x};
     cudaError_t e;
@@ -510,6 +512,50 @@ mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* po
     if (hw[0]) return fail(h, MG_TIMEOUT, "dgetrf: a panel grid barrier timed out");
     if (info_out) *info_out = hw[1];
     if (hw[1]) return fail(h, MG_SINGULAR, "dgetrf: exactly zero pivot column %d", hw[1]);
+    return MG_OK;
+}
+
+// ----------------------------------------------------------- mixed (fp32)
+size_t sgetrf_xchg_bytes(int num_sms) { return getrf_ws_bytes<float>(num_sms); }
+
+// FP32 blocked right-looking LU with partial pivoting for the mixed solve:
+// fp32 panels (the same cooperative panel kernel), fp32 TRSM on the block
+// row, and the trailing update A22 -= L21*U12 on the BF16 tensor cores with
+// `nterms` split terms (fp32 accumulation).  `xchg` holds
+// sgetrf_xchg_bytes(); `splitA`/`splitB` hold bf16x_split_bytes(n, nb, nterms).
+mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int nb, int nterms, void* xchg,
+                         void* splitA, void* splitB, int* gemm_err, int* info_out) {
+    if (info_out) *info_out = 0;
+    if (n == 0) return MG_OK;
+    if (nb > PANEL_MAX_NB) return fail(h, MG_ERR_ARG, "sgetrf_mixed: block size %d > %d", nb, PANEL_MAX_NB);
+    MG_TRY(ensure_hws(h, 64));
+    GetrfCtx<float> c = carve<float>(xchg, h->num_sms);
+    MG_CHECK_CUDA(h, cudaMemsetAsync(xchg, 0, 256, h->stream));
+    iota_kernel<<<(n + 255) / 256, 256, 0, h->stream>>>(pos, n);
+    MG_TRY(post_launch(h, "iota_kernel"));
+    for (int r = 0; r < n; r += nb) {
+        const int w = nb < n - r ? nb : n - r;
+        MG_TRY(launch_panel<float>(h, c, A, lda, n, r, w, pos));
+        MG_TRY(launch_laswp<float>(h, A, lda, r, w, c.piv, r, r + w, n));
+        if (r + w < n) {
+            const int nt = n - (r + w);
+            float* A12 = A + r + (size_t)(r + w) * lda;
+            MG_TRY(launch_trsm_llnu<float>(h, w, nt, A + r + (size_t)r * lda, lda, A12, lda));
+            const float* L21 = A + (r + w) + (size_t)r * lda;
+            MG_TRY(bf16x_split<float>(h, true, L21, lda, nt, w, nterms, splitA));
+            MG_TRY(bf16x_split<float>(h, false, A12, lda, nt, w, nterms, splitB));
+            MG_TRY(bf16x_gemm_presplit(h, nterms, nt, nt, w, -1.0f, splitA, splitB, 1.0f,
+                                       A + (r + w) + (size_t)(r + w) * lda, lda, gemm_err));
+        }
+    }
+    int* hw = (int*)h->hws;
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, c.ws.err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw + 1, c.ws.info, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw + 2, gemm_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (hw[0] || hw[2]) return fail(h, MG_TIMEOUT, "sgetrf_mixed: a bounded device wait timed out");
+    if (info_out) *info_out = hw[1];
+    if (hw[1]) return fail(h, MG_SINGULAR, "sgetrf_mixed: exactly zero pivot column %d", hw[1]);
     return MG_OK;
 }
 

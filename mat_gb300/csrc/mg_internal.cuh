@@ -50,6 +50,24 @@ mg_status_t dgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, in
                          double alpha, const double* A, int lda, const double* B, int ldb,
                          double beta, double* C, int ldc, int tri);
 
+// In-place FP64 Mat PLU and narrow solve (lu.cu).
+mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* pos, int* info_out);
+mg_status_t dgetrs_impl(mg_handle_t h, int n, int nrhs, const double* LU, int lda, const int* pos,
+                        const double* B, int ldb, double* X, int ldx);
+
+// Split-BF16 tensor-core GEMM pieces (gemm_bf16x.cu).
+size_t bf16x_split_bytes(int rows, int K, int np);
+template <typename TIN>
+mg_status_t bf16x_split(mg_handle_t h, bool a_side, const TIN* X, int ldx, int rows_or_cols, int K, int np,
+                        void* out);
+mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, float alpha, const void* Asplit,
+                                const void* Bsplit, float beta, float* C, int ldc, int* err);
+
+// FP32 LU with split-BF16 trailing updates (lu.cu).
+size_t sgetrf_xchg_bytes(int num_sms);
+mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int nb, int nterms, void* xchg,
+                         void* splitA, void* splitB, int* gemm_err, int* info_out);
+
 }  // namespace mg
 
 #define MG_CHECK_CUDA(h, call)                                   \

@@ -1,0 +1,414 @@
+// Mixed-precision LU solve with FP64 iterative refinement.
+//
+// There is no mixed precision in Mat; this is the fast form of Mat's
+// Solve_direct (Mat-8.3.1/LU/__Solve_direct.h:146-220) for the n = 16384,
+// 4-RHS benchmark configuration: factor in fp32 (fp32 panels, split-BF16
+// tensor-core trailing updates with fp32 accumulation), then refine in fp64:
+//     r = b - A x                 (fp64 A, fp64 FMA)
+//     eta = ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf)   per column
+//     d = U^{-1} L^{-1} P (r/s)   (fp32, s = ||r||_inf per column)
+//     x = x + s d                 (fp64)
+// until every column's normwise backward error eta <= tol.  If refinement
+// stalls (eta not halving twice in a row, or max_iter reached) the solve
+// falls back to the plain FP64 GPU path (mg_dgesv) and reports it.
+//
+// The triangular solves use precomputed inverses of the 128x128 diagonal
+// blocks, so each block step is one kernel with no intra-kernel dependency:
+// every CTA applies the block inverse to the (already final) block of the
+// right-hand side and updates its share of the rows below.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <vector>
+
+#include "mg_internal.cuh"
+
+namespace {
+
+constexpr int IR_BLOCK = 128;      // fp32 LU block / diagonal-inverse block
+constexpr int MAX_RHS = 8;
+constexpr int RES_ROWS = 256;      // rows per residual CTA
+constexpr int RES_KCHUNK = 2048;   // columns per residual CTA (k split)
+
+__global__ void d2s_kernel(const double* __restrict__ A, int lda, int n, float* __restrict__ S, int lds) {
+    const size_t total = (size_t)n * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t r = e % n, c = e / n;
+        S[r + c * lds] = (float)A[r + c * lda];
+    }
+}
+
+// partial[kc][i] = sum_{k in chunk kc} |A(i,k)|  (row sums of |A|)
+__global__ void absrow_partial_kernel(const double* __restrict__ A, int lda, int n, double* __restrict__ partial) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k0 = blockIdx.y * RES_KCHUNK, k1 = min(n, k0 + RES_KCHUNK);
+    if (i >= n) return;
+    double s = 0.0;
+    for (int k = k0; k < k1; ++k) s += fabs(A[i + (size_t)k * lda]);
+    partial[(size_t)blockIdx.y * n + i] = s;
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
+    // for non-negative doubles the bit patterns order like the values
+    atomicMax((unsigned long long*)addr, (unsigned long long)__double_as_longlong(v));
+}
+
+__global__ void absrow_reduce_kernel(const double* __restrict__ partial, int nchunks, int n, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int c = 0; c < nchunks; ++c) s += partial[(size_t)c * n + i];
+    atomic_max_nonneg(out, s);
+}
+
+// partial[kc][j][i] = sum_{k in chunk} A(i,k) X(k,j)   (fp64 FMA)
+__global__ void __launch_bounds__(RES_ROWS) residual_partial_kernel(const double* __restrict__ A, int lda, int n,
+                                                                    int nrhs, const double* __restrict__ X, int ldx,
+                                                                    double* __restrict__ partial) {
+    __shared__ double xs[MAX_RHS][256];
+    const int i = blockIdx.x * RES_ROWS + threadIdx.x;
+    const int k0 = blockIdx.y * RES_KCHUNK, k1 = min(n, k0 + RES_KCHUNK);
+    double acc[MAX_RHS];
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) acc[j] = 0.0;
+    for (int kb = k0; kb < k1; kb += 256) {
+        const int kn = min(256, k1 - kb);
+        __syncthreads();
+        for (int q = threadIdx.x; q < kn * nrhs; q += blockDim.x) xs[q / kn][q % kn] = X[kb + q % kn + (size_t)(q / kn) * ldx];
+        __syncthreads();
+        if (i < n) {
+            const double* ap = A + i + (size_t)kb * lda;
+            if (nrhs == 4) {
+                for (int k = 0; k < kn; ++k) {
+                    const double a = ap[(size_t)k * lda];
+                    acc[0] = fma(a, xs[0][k], acc[0]);
+                    acc[1] = fma(a, xs[1][k], acc[1]);
+                    acc[2] = fma(a, xs[2][k], acc[2]);
+                    acc[3] = fma(a, xs[3][k], acc[3]);
+                }
+            } else {
+                for (int k = 0; k < kn; ++k) {
+                    const double a = ap[(size_t)k * lda];
+                    for (int j = 0; j < nrhs; ++j) acc[j] = fma(a, xs[j][k], acc[j]);
+                }
+            }
+        }
+    }
+    if (i < n)
+        for (int j = 0; j < nrhs; ++j) partial[((size_t)blockIdx.y * nrhs + j) * n + i] = acc[j];
+}
+
+// r = b - sum_c partial[c]; rnorm[j] = max |r(:,j)|, xnorm[j] = max |x(:,j)|
+__global__ void residual_reduce_kernel(const double* __restrict__ partial, int nchunks, int n, int nrhs,
+                                       const double* __restrict__ B, int ldb, const double* __restrict__ X, int ldx,
+                                       double* __restrict__ R, double* __restrict__ norms) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int j = 0; j < nrhs; ++j) {
+        double s = 0.0;
+        for (int c = 0; c < nchunks; ++c) s += partial[((size_t)c * nrhs + j) * n + i];
+        const double r = B[i + (size_t)j * ldb] - s;
+        R[i + (size_t)j * n] = r;
+        atomic_max_nonneg(norms + j, fabs(r));
+        atomic_max_nonneg(norms + MAX_RHS + j, fabs(X[i + (size_t)j * ldx]));
+    }
+}
+
+// y[i][j] = float(r[pos[i]][j] / s_j)
+__global__ void prep_rhs_kernel(int n, int nrhs, const int* __restrict__ pos, const double* __restrict__ R,
+                                const double* __restrict__ scale, float* __restrict__ Y) {
+    const size_t total = (size_t)n * nrhs;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % n), j = (int)(e / n);
+        const double s = scale[j];
+        Y[e] = (float)(s > 0.0 ? R[pos[i] + (size_t)j * n] / s : 0.0);
+    }
+}
+
+__global__ void update_x_kernel(int n, int nrhs, const float* __restrict__ D, const double* __restrict__ scale,
+                                double* __restrict__ X, int ldx) {
+    const size_t total = (size_t)n * nrhs;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % n), j = (int)(e / n);
+        X[i + (size_t)j * ldx] += scale[j] * (double)D[e];
+    }
+}
+
+// Inverse of each diagonal block (unit lower when LOWER, else upper) of the
+// packed fp32 LU; one CTA per block, one thread per column of the inverse.
+template <bool LOWER>
+__global__ void inv_diag_blocks_kernel(const float* __restrict__ LU, int lda, int n, float* __restrict__ inv) {
+    extern __shared__ float sb[];  // [bs][bs] column-major block, then [bs][bs] inverse
+    const int b0 = blockIdx.x * IR_BLOCK;
+    const int bs = min(IR_BLOCK, n - b0);
+    float* blk = sb;
+    float* z = sb + IR_BLOCK * IR_BLOCK;
+    for (int e = threadIdx.x; e < bs * bs; e += blockDim.x) {
+        const int r = e % bs, c = e / bs;
+        blk[r + c * IR_BLOCK] = LU[(b0 + r) + (size_t)(b0 + c) * lda];
+    }
+    __syncthreads();
+    const int c = threadIdx.x;
+    if (c < bs) {
+        float* zc = z + c * IR_BLOCK;
+        if (LOWER) {
+            for (int i = 0; i < bs; ++i) zc[i] = 0.f;
+            zc[c] = 1.f;
+            for (int i = c + 1; i < bs; ++i) {
+                float s = 0.f;
+                for (int k = c; k < i; ++k) s = fmaf(blk[i + k * IR_BLOCK], zc[k], s);
+                zc[i] = -s;
+            }
+        } else {
+            for (int i = 0; i < bs; ++i) zc[i] = 0.f;
+            zc[c] = 1.f / blk[c + c * IR_BLOCK];
+            for (int i = c - 1; i >= 0; --i) {
+                float s = 0.f;
+                for (int k = i + 1; k <= c; ++k) s = fmaf(blk[i + k * IR_BLOCK], zc[k], s);
+                zc[i] = -s / blk[i + i * IR_BLOCK];
+            }
+        }
+    }
+    __syncthreads();
+    float* out = inv + (size_t)blockIdx.x * IR_BLOCK * IR_BLOCK;
+    for (int e = threadIdx.x; e < IR_BLOCK * IR_BLOCK; e += blockDim.x) out[e] = z[e];
+}
+
+// One block step of a blocked triangular solve with precomputed block inverses.
+// LOWER: xb = Linv_b * W[b0..b1); Out[b0..b1) = xb; W[r] -= L[r, b0..b1) xb for r >= b1.
+// UPPER: xb = Uinv_b * W[b0..b1); Out[b0..b1) = xb; W[r] -= U[r, b0..b1) xb for r < b0.
+template <bool LOWER>
+__global__ void __launch_bounds__(128) trsv_inv_step_kernel(const float* __restrict__ LU, int lda, int n, int nrhs,
+                                                            const float* __restrict__ inv_b, float* __restrict__ W,
+                                                            float* __restrict__ Out, int b0) {
+    __shared__ float wb[MAX_RHS][IR_BLOCK];
+    __shared__ float xb[MAX_RHS][IR_BLOCK];
+    const int bs = min(IR_BLOCK, n - b0);
+    for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) wb[q / bs][q % bs] = W[b0 + q % bs + (size_t)(q / bs) * n];
+    __syncthreads();
+    for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) {
+        const int r = q % bs, j = q / bs;
+        float s = 0.f;
+        for (int k = 0; k < bs; ++k) s = fmaf(inv_b[r + k * IR_BLOCK], wb[j][k], s);
+        xb[j][r] = s;
+        if (blockIdx.x == 0) Out[b0 + r + (size_t)j * n] = s;
+    }
+    __syncthreads();
+    const int lo = LOWER ? b0 + bs : 0, hi = LOWER ? n : b0;
+    for (int r = lo + blockIdx.x * blockDim.x + threadIdx.x; r < hi; r += gridDim.x * blockDim.x) {
+        float acc[MAX_RHS];
+        for (int j = 0; j < nrhs; ++j) acc[j] = W[r + (size_t)j * n];
+        const float* lp = LU + r + (size_t)b0 * lda;
+        for (int k = 0; k < bs; ++k) {
+            const float l = lp[(size_t)k * lda];
+            for (int j = 0; j < nrhs; ++j) acc[j] = fmaf(-l, xb[j][k], acc[j]);
+        }
+        for (int j = 0; j < nrhs; ++j) W[r + (size_t)j * n] = acc[j];
+    }
+}
+
+struct IrWs {
+    float* A32;
+    int* pos;
+    void* xchg;
+    void* splitA;
+    void* splitB;
+    int* gemm_err;
+    float* Linv;
+    float* Uinv;
+    double* R;
+    double* partial;
+    double* norms;  // [0..8) rnorm, [8..16) xnorm, [16] anorm, [24..32) scale
+    float* Y;
+    float* Z;
+};
+
+size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = mg::align_up(off + bytes, 1024);
+        return o;
+    };
+    const int nblk = (n + IR_BLOCK - 1) / IR_BLOCK;
+    const int kch = (n + RES_KCHUNK - 1) / RES_KCHUNK;
+    const size_t oA = take((size_t)n * n * sizeof(float));
+    const size_t oP = take((size_t)n * sizeof(int));
+    const size_t oX = take(mg::sgetrf_xchg_bytes(h->num_sms));
+    const size_t oSA = take(mg::bf16x_split_bytes(n, IR_BLOCK, nterms));
+    const size_t oSB = take(mg::bf16x_split_bytes(n, IR_BLOCK, nterms));
+    const size_t oE = take(64);
+    const size_t oLi = take((size_t)nblk * IR_BLOCK * IR_BLOCK * sizeof(float));
+    const size_t oUi = take((size_t)nblk * IR_BLOCK * IR_BLOCK * sizeof(float));
+    const size_t oR = take((size_t)n * nrhs * sizeof(double));
+    const size_t oPa = take((size_t)kch * n * std::max(nrhs, 1) * sizeof(double));
+    const size_t oN = take(64 * sizeof(double));
+    const size_t oY = take((size_t)n * nrhs * sizeof(float));
+    const size_t oZ = take((size_t)n * nrhs * sizeof(float));
+    if (w) {
+        char* b = (char*)h->ws;
+        w->A32 = (float*)(b + oA);
+        w->pos = (int*)(b + oP);
+        w->xchg = b + oX;
+        w->splitA = b + oSA;
+        w->splitB = b + oSB;
+        w->gemm_err = (int*)(b + oE);
+        w->Linv = (float*)(b + oLi);
+        w->Uinv = (float*)(b + oUi);
+        w->R = (double*)(b + oR);
+        w->partial = (double*)(b + oPa);
+        w->norms = (double*)(b + oN);
+        w->Y = (float*)(b + oY);
+        w->Z = (float*)(b + oZ);
+    }
+    return off;
+}
+
+int grid_for(size_t total, int threads, int cap) {
+    size_t b = (total + threads - 1) / threads;
+    if (b > (size_t)cap) b = cap;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+}  // namespace
+
+extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
+                                    int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* rep) {
+    using clk = std::chrono::steady_clock;
+    if (!h) return MG_ERR_ARG;
+    if (n < 0 || nrhs < 0 || nrhs > MAX_RHS || lda < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1) ||
+        ldx < (n > 1 ? n : 1))
+        return mg::fail(h, MG_ERR_ARG, "mg_dsgesv_ir: bad arguments (n=%d nrhs=%d, nrhs must be <= %d)", n, nrhs,
+                        MAX_RHS);
+    mg_ir_opts o = {1e-14, 30, 3, 1};
+    if (opts) o = *opts;
+    if (o.nterms < 1 || o.nterms > 3) return mg::fail(h, MG_ERR_ARG, "mg_dsgesv_ir: nterms must be 1..3");
+    if (o.max_iter < 1) o.max_iter = 1;
+    mg_ir_report r = {};
+    r.path = 0;
+    if (n == 0 || nrhs == 0) {
+        if (rep) *rep = r;
+        return MG_OK;
+    }
+    if (!A || !B || !X) return mg::fail(h, MG_ERR_ARG, "mg_dsgesv_ir: null pointer");
+
+    const auto t0 = clk::now();
+    MG_TRY(mg::ensure_ws(h, carve_ir(h, n, nrhs, o.nterms, nullptr)));
+    MG_TRY(mg::ensure_hws(h, 256));
+    IrWs w;
+    carve_ir(h, n, nrhs, o.nterms, &w);
+    cudaStream_t st = h->stream;
+    const int cap = h->num_sms * 8;
+    const int kch = (n + RES_KCHUNK - 1) / RES_KCHUNK;
+    const int nblk = (n + IR_BLOCK - 1) / IR_BLOCK;
+    double* hn = (double*)h->hws;
+
+    // ||A||_inf and ||B||_inf (column-wise) --------------------------------
+    MG_CHECK_CUDA(h, cudaMemsetAsync(w.gemm_err, 0, 64, st));
+    MG_CHECK_CUDA(h, cudaMemsetAsync(w.norms, 0, 64 * sizeof(double), st));
+    absrow_partial_kernel<<<dim3((n + 255) / 256, kch), 256, 0, st>>>(A, lda, n, w.partial);
+    MG_TRY(mg::post_launch(h, "absrow_partial_kernel"));
+    absrow_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kch, n, w.norms + 16);
+    MG_TRY(mg::post_launch(h, "absrow_reduce_kernel"));
+
+    // fp32 copy and mixed LU -------------------------------------------------
+    d2s_kernel<<<grid_for((size_t)n * n, 256, cap), 256, 0, st>>>(A, lda, n, w.A32, n);
+    MG_TRY(mg::post_launch(h, "d2s_kernel"));
+    int info = 0;
+    mg_status_t s = mg::sgetrf_mixed(h, n, w.A32, n, w.pos, IR_BLOCK, o.nterms, w.xchg, w.splitA, w.splitB,
+                                     w.gemm_err, &info);
+    if (s != MG_OK && s != MG_SINGULAR) return s;
+    r.info = info;
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
+    inv_diag_blocks_kernel<true><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
+                                                                                                 w.Linv);
+    MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<lower>"));
+    inv_diag_blocks_kernel<false><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
+                                                                                                  w.Uinv);
+    MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<upper>"));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
+    const auto t1 = clk::now();
+    r.factor_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+
+    // refinement --------------------------------------------------------------
+    // x = 0, so the first residual is b itself
+    MG_CHECK_CUDA(h, cudaMemset2DAsync(X, (size_t)ldx * sizeof(double), 0, (size_t)n * sizeof(double), nrhs, st));
+    double bnorm[MAX_RHS] = {0};
+    double prev_eta = INFINITY;
+    int slow = 0;
+    bool converged = false;
+    for (int it = 0; it <= o.max_iter; ++it) {
+        MG_CHECK_CUDA(h, cudaMemsetAsync(w.norms, 0, 16 * sizeof(double), st));
+        residual_partial_kernel<<<dim3((n + RES_ROWS - 1) / RES_ROWS, kch), RES_ROWS, 0, st>>>(A, lda, n, nrhs, X,
+                                                                                             ldx, w.partial);
+        MG_TRY(mg::post_launch(h, "residual_partial_kernel"));
+        residual_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kch, n, nrhs, B, ldb, X, ldx, w.R,
+                                                               w.norms);
+        MG_TRY(mg::post_launch(h, "residual_reduce_kernel"));
+        MG_CHECK_CUDA(h, cudaMemcpyAsync(hn, w.norms, 32 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
+        const double anorm = hn[16];
+        double eta = 0.0;
+        for (int j = 0; j < nrhs; ++j) {
+            if (it == 0) bnorm[j] = hn[j];  // x = 0: r = b
+            const double den = anorm * hn[MAX_RHS + j] + bnorm[j];
+            const double e = den > 0 ? hn[j] / den : 0.0;
+            eta = std::max(eta, e);
+        }
+        r.anorm_inf = anorm;
+        r.backward_error = eta;
+        if (it < 32) r.history[it] = eta;
+        r.iterations = it;
+        if (it > 0 && eta <= o.tol) {
+            converged = true;
+            break;
+        }
+        if (it > 1) {
+            slow = eta > 0.5 * prev_eta ? slow + 1 : 0;
+            if (slow >= 2) break;
+        }
+        if (it == o.max_iter) break;
+        prev_eta = eta;
+        // correction: d = U^-1 L^-1 P (r / s), x += s d
+        for (int j = 0; j < nrhs; ++j) hn[24 + j] = hn[j];
+        MG_CHECK_CUDA(h, cudaMemcpyAsync(w.norms + 24, hn + 24, MAX_RHS * sizeof(double), cudaMemcpyHostToDevice, st));
+        prep_rhs_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(n, nrhs, w.pos, w.R, w.norms + 24, w.Y);
+        MG_TRY(mg::post_launch(h, "prep_rhs_kernel"));
+        for (int b = 0; b < nblk; ++b) {
+            const int b0 = b * IR_BLOCK, rows = n - (b0 + IR_BLOCK);
+            const int g = rows > 0 ? std::min(h->num_sms, (rows + 127) / 128) : 1;
+            trsv_inv_step_kernel<true><<<g, 128, 0, st>>>(w.A32, n, n, nrhs, w.Linv + (size_t)b * IR_BLOCK * IR_BLOCK,
+                                                          w.Y, w.Z, b0);
+            MG_TRY(mg::post_launch(h, "trsv_inv_step_kernel<lower>"));
+        }
+        for (int b = nblk - 1; b >= 0; --b) {
+            const int b0 = b * IR_BLOCK;
+            const int g = b0 > 0 ? std::min(h->num_sms, (b0 + 127) / 128) : 1;
+            trsv_inv_step_kernel<false><<<g, 128, 0, st>>>(w.A32, n, n, nrhs,
+                                                           w.Uinv + (size_t)b * IR_BLOCK * IR_BLOCK, w.Z, w.Y, b0);
+            MG_TRY(mg::post_launch(h, "trsv_inv_step_kernel<upper>"));
+        }
+        update_x_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(n, nrhs, w.Y, w.norms + 24, X, ldx);
+        MG_TRY(mg::post_launch(h, "update_x_kernel"));
+    }
+    const auto t2 = clk::now();
+    r.refine_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
+    mg_status_t result = MG_OK;
+    if (!converged) {
+        if (o.fallback) {
+            int finfo = 0;
+            mg_status_t fs = mg_dgesv(h, n, nrhs, A, lda, B, ldb, X, ldx, &finfo);
+            if (fs != MG_OK) return fs;
+            r.path = 2;
+            result = MG_FALLBACK_USED;
+        } else {
+            result = mg::fail(h, MG_IR_STALLED, "refinement stalled at backward error %.3e", r.backward_error);
+        }
+    }
+    if (rep) *rep = r;
+    return result;
+}

@@ -1,6 +1,7 @@
 """Split-BF16 tcgen05 GEMM against an fp64 product of the same fp32 inputs.
-Tolerances (normwise relative): 3 terms ~ fp32 (2e-6), 2 terms ~ 16 bits
-(1e-4), 1 term = bf16 (1e-2)."""
+Tolerances (normwise relative), scaled by sqrt(k/64) for the fp32
+accumulation over k: 3 terms ~ fp32 (2e-6), 2 terms ~ 16 bits (1e-4),
+1 term = bf16 (1e-2)."""
 import numpy as np
 import pytest
 import torch
@@ -37,7 +38,7 @@ def test_split_gemm_accuracy(handle, m, n, k, nterms):
     ref = a.double() @ b.double()
     out = run(handle, a, b, nterms)
     err = (out - ref).norm() / ref.norm()
-    assert err < TOL[nterms], float(err)
+    assert err < TOL[nterms] * max(1.0, (k / 64) ** 0.5), float(err)
 
 
 def test_split_gemm_wide_exponents(handle):
@@ -45,7 +46,7 @@ def test_split_gemm_wide_exponents(handle):
     a, b = make(384, 1024, 3, 8), make(1024, 512, 4, 8)
     ref = a.double() @ b.double()
     out = run(handle, a, b, 3)
-    assert (out - ref).norm() / ref.norm() < 2e-6
+    assert (out - ref).norm() / ref.norm() < 2e-6 * 4
 
 
 def test_split_gemm_subtracting_update(handle):
