@@ -1,0 +1,338 @@
+"""Benchmark of the GB300 hot path of Mat (mixed LU + FP64 refinement solve).
+
+Headline (BASELINE metric "n=16384 LU-solve time at FP64 backward error,
+mixed+IR vs FP64; DGEMM TFLOP/s"):
+  one step = one mixed-precision LU solve with FP64 iterative refinement,
+  n = 16384, 4 right-hand sides, A = Q1 diag(sigma) Q2 (Q = 64 seeded
+  Householder reflectors each side, sigma geometric 1 -> 1e-6, cond 1e6),
+  b iid N(0,1), to normwise backward error <= 1e-14, inputs resident in HBM
+  (A is 2 GiB, larger than L2, so no flush is needed between steps).
+value = mean seconds per solve (lower is better).  Beside it on the same
+line: the plain FP64 GPU solve of the same system (the "vs FP64" half of the
+metric), the FP64 DGEMM rate at M=N=K=1024 (the "DGEMM TFLOP/s" half), an
+end-to-end leg through the C ABI with host buffers, the roofline of the
+dominant kernel (timed live with CUDA events on the library's stream), the
+oracle restatement timed on the host cores, and sampled GPU clocks.
+
+--impl reference: times the CPU implementation of the reference (the
+oracle restatement of Mat's Solve_direct; the reference itself is x86
+AVX-512 header code that is not present on the GPU host) on all host cores,
+on a bounded sample (n = 4096) scaled to n = 16384 by n^3.
+Multi-GPU: replicas only (independent solves, no collective on the path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "n=16384 LU-solve time at FP64 backward error, mixed+IR vs FP64; DGEMM TFLOP/s"
+WORKLOAD = ("mixed LU (fp32 panels + split-BF16x3 tcgen05 trailing updates) + FP64 iterative refinement, "
+            "n=16384, 4 RHS, A=Q1*diag(sigma)*Q2 with 64 Householder reflectors per side, "
+            "sigma geometric 1..1e-6 (cond 1e6), b iid N(0,1), target backward error 1e-14")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=16384)
+    p.add_argument("--nrhs", type=int, default=4)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), float(d.get("bf16_tflops", 1900.0)), \
+            float(d.get("bf16_tflops_sustained", 1700.0)), "measured"
+    return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_solve_sample(n_sample: int, nrhs: int, seed: int = 1):
+    """Times the oracle restatement of Mat's Solve_direct (narrow path) on all host cores."""
+    from mat_gb300.api import host_fill_normal
+    from oracle.api import restatement
+    o = restatement()
+    cores = os.cpu_count() or 1
+    o.set_threads(cores)
+    a = host_fill_normal(n_sample, n_sample, seed)
+    b = host_fill_normal(n_sample, nrhs, seed + 10)
+    t = time.perf_counter()
+    o.solve(a, b)
+    return time.perf_counter() - t, cores
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    n_sample = 4096
+    scale = (args.n / n_sample) ** 3
+    for _ in range(args.warmup):
+        cpu_solve_sample(2048, args.nrhs)
+    ts = []
+    cores = 1
+    for _ in range(args.steps):
+        t, cores = cpu_solve_sample(n_sample, args.nrhs)
+        ts.append(t * scale)
+    v = statistics.mean(ts)
+    sample = (f"oracle restatement of Mat Solve_direct (PLU BS=60 + narrow substitution), n={n_sample}, "
+              f"{args.nrhs} RHS, {cores} threads, time scaled by (16384/{n_sample})^3")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "FP64 LU solve (Mat Solve_direct), n=16384, 4 RHS, iid N(0,1)",
+                   "n": args.n, "nrhs": args.nrhs},
+        "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from mat_gb300.api import Handle, colmajor
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    h = Handle()
+    n, nrhs = args.n, args.nrhs
+    hbm, bf16, bf16s, peak_kind = peaks()
+
+    # inputs resident in HBM (replicas: each rank its own seed)
+    A = colmajor(n, n)
+    h.gen_svd_matrix(A, 3 + rank, nrefl=64, sigma_min=1e-6)
+    B = colmajor(n, nrhs)
+    h.fill_normal(B, 11 + rank)
+    X = colmajor(n, nrhs)
+    torch.cuda.synchronize()
+
+    for _ in range(max(3, args.warmup)):
+        h.dsgesv_ir(A, B, X)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    launches0 = h.launch_count()
+    h.profile(True)
+    reps = []
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        Xs, rep = h.dsgesv_ir(A, B, X)
+        reps.append(rep)
+    e1.record()
+    barrier()
+    launches = h.launch_count() - launches0
+    prof = h.profile_records()
+    h.profile(False)
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+
+    # the FP64 half of the metric: plain FP64 GPU solve of the same system, and accuracy
+    torch.cuda.synchronize()
+    f0 = time.perf_counter()
+    Xd, info = h.dgesv(A, B)
+    torch.cuda.synchronize()
+    fp64_s = time.perf_counter() - f0
+    fwd = float((X - Xd).norm() / Xd.norm())
+
+    # DGEMM TFLOP/s at M=N=K=1024 (row-major uniform [-1,1) seeds 0/1, stored column-major)
+    m = 1024
+    Ga, Gb = colmajor(m, m), colmajor(m, m)
+    h.fill_uniform(Ga, 0)
+    h.fill_uniform(Gb, 1)
+    Gc = h.dgemm(Ga, Gb)
+    for _ in range(5):
+        h.dgemm(Ga, Gb, Gc)
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record()
+    for _ in range(20):
+        h.dgemm(Ga, Gb, Gc)
+    g1.record()
+    torch.cuda.synchronize()
+    dgemm_ms = g0.elapsed_time(g1) / 20
+    dgemm_tf = 2 * m ** 3 / dgemm_ms / 1e9
+    dfma_tf, dmma_tf = h.measure_fp64_peaks()
+
+    # roofline of the dominant kernel (by time inside the timed region)
+    dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    tensor = dom["flops"] > 0 and dom_name in ("gemm_bf16x",)
+    traffic = None
+    tf = ROOT / "profiles" / "traffic_per_launch.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get(dom_name)
+    if tensor:
+        achieved = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
+        roof = {"kernel": dom_name, "bound": "tensor", "achieved": achieved, "peak": bf16s, "unit": "TFLOP/s",
+                "frac": achieved / bf16s, "peak_kind": f"bf16 sustained ({peak_kind})", "traffic": traffic,
+                "launches": dom["launches"], "ms_total": dom["ms"]}
+    else:
+        achieved = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
+        roof = {"kernel": dom_name, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_kind": f"hbm copy ({peak_kind})", "traffic": traffic,
+                "launches": dom["launches"], "ms_total": dom["ms"]}
+    phases = {k: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps}
+              for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}
+
+    # end to end through the C ABI: host buffers, copies inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        hA = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+        hA.copy_(A.t())  # column-major bytes of A in a row-major (n x n) pinned host buffer
+        hBt = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
+        hBt.copy_(B.t())
+        dA, dB, dX = colmajor(n, n), colmajor(n, nrhs), colmajor(n, nrhs)
+        lib, hh = h.lib, h.h
+        import ctypes as C
+        h2d = 8 * n * n + 8 * n * nrhs
+        d2h = 8 * n * nrhs
+        hXt = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
+
+        def e2e_step():
+            h.check(lib.mg_memcpy(hh, C.c_void_p(dA.data_ptr()), C.c_void_p(hA.data_ptr()), 8 * n * n, 0))
+            h.check(lib.mg_memcpy(hh, C.c_void_p(dB.data_ptr()), C.c_void_p(hBt.data_ptr()), 8 * n * nrhs, 0))
+            h.dsgesv_ir(dA, dB, dX)
+            h.check(lib.mg_memcpy(hh, C.c_void_p(hXt.data_ptr()), C.c_void_p(dX.data_ptr()), 8 * n * nrhs, 1))
+            h.check(lib.mg_synchronize(hh))
+
+        e2e_step()
+        barrier()
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        barrier()
+        e2e_s = (time.perf_counter() - w0) / args.steps
+        e2e = {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+        del hA, hBt, hXt, dA, dB, dX
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        n_sample = 4096
+        t_cpu, cores = cpu_solve_sample(n_sample, nrhs)
+        cpu = {"value": t_cpu * (n / n_sample) ** 3, "unit": "s", "cores": cores, "kind": "port",
+               "sample": f"oracle restatement of Mat Solve_direct, n={n_sample}, {nrhs} RHS, {cores} threads, "
+                         f"scaled by (n/{n_sample})^3"}
+
+    if rank == 0:
+        last = reps[-1]
+        line = {
+            "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32/bf16x3 factor + f64 refinement", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n": n, "nrhs": nrhs, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (A is 2 GiB), no flush"},
+            "fp64_solve_s": fp64_s, "mixed_vs_fp64": (ms / 1e3) / fp64_s,
+            "backward_error": last["backward_error"], "iterations": last["iterations"], "path": last["path"],
+            "forward_error_vs_fp64_solve": fwd,
+            "dgemm": {"config": "M=N=K=1024 fp64, uniform[-1,1) seeds 0/1", "ms": dgemm_ms, "tflops": dgemm_tf,
+                      "fp64_dmma_peak_tflops": dmma_tf, "fp64_dfma_peak_tflops": dfma_tf,
+                      "frac_of_fp64_peak": dgemm_tf / max(dmma_tf, dfma_tf)},
+            "roofline": roof, "phases": phases, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": launches, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

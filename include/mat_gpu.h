@@ -58,6 +58,15 @@ const char* mg_get_last_error(mg_handle_t h);
 /* Number of this library's kernel launches enqueued through `h` so far. */
 uint64_t mg_launch_count(mg_handle_t h);
 
+/* Per-phase profiling: while on, each library phase (panel, trailing GEMM,
+ * residual, ...) is bracketed by CUDA events on the handle's stream and
+ * accumulated with the algorithmic flops / bytes it performed.  Turning it
+ * on clears the records; count/get synchronise the stream. */
+mg_status_t mg_profile_enable(mg_handle_t h, int on);
+int mg_profile_count(mg_handle_t h);
+mg_status_t mg_profile_get(mg_handle_t h, int i, const char** name, double* ms, long long* launches,
+                           double* flops, double* bytes);
+
 /* ------------------------------------------------------ memory utilities
  * For callers (C, cgo, JNI, ctypes) that do not link the CUDA runtime. */
 mg_status_t mg_device_malloc(void** out, size_t bytes);
@@ -174,6 +183,69 @@ mg_status_t mg_gen_svd_matrix(mg_handle_t h, int n, double* A, int lda, uint64_t
                               double sigma_min);
 /* S = G G^T / n + I with G iid N(0,1) (seeded, row-major stream order). */
 mg_status_t mg_gen_spd_gram(mg_handle_t h, int n, double* S, int lds, uint64_t seed);
+
+/* -------------------------------------------------------------- Cholesky
+ * Mat's LLT (Mat-8.3.1/LU/__LLT.h:212-246, blocked as __LLT, :94-150,
+ * block size 48), in place: reads the lower triangle of A, leaves L there and
+ * zeroes the strict upper triangle.  Bit-identical to Mat's AVX-512 build.
+ * Returns MG_NOT_SPD with *info = first non-positive pivot column (1-based);
+ * Mat produces NaNs silently there (:7).  Synchronises. */
+mg_status_t mg_dpotrf(mg_handle_t h, int n, double* A, int lda, int* info);
+/* B := (L L^T)^{-1} B with L from mg_dpotrf (forward then back substitution). */
+mg_status_t mg_dpotrs(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* B, int ldb);
+
+/* -------------------------------------------------------------------- QR
+ * Mat's QR(A, Q, R, QR_Householder) (Mat-8.3.1/QR/QR.h:8-25, blocked
+ * Householder with block size 48, __Householder_Blocked.h:215-353): A (m x n)
+ * is not modified; Q (m x m, the full orthogonal factor as Mat forms it) and
+ * R (m x n, zero below the diagonal) are written.  R(j,j) = -sign(x0)||x||.
+ * Bit-identical to Mat's AVX-512 build when min(m, n) > 96; smaller
+ * problems agree to rounding (Mat switches to its unblocked variant).
+ * Synchronises. */
+mg_status_t mg_dqr(mg_handle_t h, int m, int n, const double* A, int lda, double* Q, int ldq,
+                   double* R, int ldr);
+/* The factorization alone, in place: R on and above the diagonal of A, the
+ * Householder vectors (unit first entry implied) below it, tau[min(m,n)] and
+ * the upper-triangular compact-WY factors T (one 48 x 48 block per 48
+ * columns, ceil(min(m,n)/48)*48*48 doubles). Synchronises. */
+mg_status_t mg_dgeqrf(mg_handle_t h, int m, int n, double* A, int lda, double* tau, double* T);
+
+/* ------------------------------------------------------------- adjoints
+ * Reverse-mode calls for the Cholesky family (Mat has no derivatives; these
+ * are the backward passes of LLT, Mat-8.3.1/LU/__LLT.h:212-246, of its
+ * triangular solves, and of the Cholesky log-determinant).
+ *
+ * mg_dpotrf_backward: given L = chol(A) (lower) and Lbar (lower triangle
+ * used), Abar = the symmetric gradient of the loss with respect to A, by the
+ * blocked reverse-mode recurrence of Murray (2016) on Phi(L^T Lbar) (Phi =
+ * lower triangle, diagonal halved).  Only L is read (no stored
+ * intermediates); uses n*n doubles of handle workspace. */
+mg_status_t mg_dpotrf_backward(mg_handle_t h, int n, const double* L, int ldl, const double* Lbar,
+                               int ldlbar, double* Abar, int ldabar);
+/* X = op(L)^{-1} B with L lower (trans = 0: L, 1: L^T): given X and Xbar,
+ * writes Bbar = op(L)^{-T} Xbar and accumulates into the lower triangle of
+ * Lbar (-tril(Bbar X^T) or -tril(X Bbar^T)); Lbar's strict upper triangle is
+ * scratch. */
+mg_status_t mg_dtrsm_backward(mg_handle_t h, int trans, int n, int nrhs, const double* L, int ldl,
+                              const double* X, int ldx, const double* Xbar, int ldxbar, double* Bbar,
+                              int ldbbar, double* Lbar, int ldlbar);
+/* logdet(A) = 2 sum log L_ii for A = L L^T (host result; synchronises), and its
+ * adjoint Lbar_ii += 2 gbar / L_ii. */
+mg_status_t mg_dlogdet_chol(mg_handle_t h, int n, const double* L, int ldl, double* host_out);
+mg_status_t mg_dlogdet_chol_backward(mg_handle_t h, int n, const double* L, int ldl, double gbar,
+                                     double* Lbar, int ldlbar);
+/* RBF kernel K(i,j) = sigma2 exp(-|x_i - x_j|^2 / (2 ell^2)) + jitter [i==j],
+ * points X (n x 3, column-major). */
+mg_status_t mg_gen_rbf_kernel(mg_handle_t h, int n, const double* X, double ell, double sigma2,
+                              double jitter, double* K, int ldk);
+/* Gaussian-process loss 0.5 y^T K^{-1} y + 0.5 logdet K with K the RBF kernel
+ * above: forward (Cholesky, two triangular solves, logdet) and backward
+ * (triangular-solve and logdet adjoints, Cholesky adjoint) in one call;
+ * returns the loss and d loss / d ell on the host and, if Kbar is not NULL,
+ * d loss / dK (symmetric).  Synchronises. */
+mg_status_t mg_gp_loss_grad(mg_handle_t h, int n, const double* X, double ell, double sigma2, double jitter,
+                            const double* y, double* host_loss, double* host_dell, double* Kbar,
+                            int ldkbar);
 
 /* Measures the FP64 peaks of this GPU with dependent-free FMA / DMMA loops
  * (TFLOP/s, counting an FMA as 2 flops).  Synchronises. */

@@ -63,6 +63,19 @@ SIGNATURES: dict[str, tuple] = {
     "mg_dsgesv_ir": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, C.POINTER(IrOpts), C.POINTER(IrReport)]),
     "mg_gen_svd_matrix": (i32, [vp, i32, vp, i32, u64, i32, f64]),
     "mg_gen_spd_gram": (i32, [vp, i32, vp, i32, u64]),
+    "mg_profile_enable": (i32, [vp, i32]),
+    "mg_profile_count": (i32, [vp]),
+    "mg_profile_get": (i32, [vp, i32, C.POINTER(C.c_char_p), pf64, C.POINTER(C.c_longlong), pf64, pf64]),
+    "mg_dpotrf": (i32, [vp, i32, vp, i32, pi32]),
+    "mg_dpotrs": (i32, [vp, i32, i32, vp, i32, vp, i32]),
+    "mg_dqr": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32]),
+    "mg_dgeqrf": (i32, [vp, i32, i32, vp, i32, vp, vp]),
+    "mg_dpotrf_backward": (i32, [vp, i32, vp, i32, vp, i32, vp, i32]),
+    "mg_dtrsm_backward": (i32, [vp, i32, i32, i32, vp, i32, vp, i32, vp, i32, vp, i32, vp, i32]),
+    "mg_dlogdet_chol": (i32, [vp, i32, vp, i32, pf64]),
+    "mg_dlogdet_chol_backward": (i32, [vp, i32, vp, i32, f64, vp, i32]),
+    "mg_gen_rbf_kernel": (i32, [vp, i32, vp, f64, f64, f64, vp, i32]),
+    "mg_gp_loss_grad": (i32, [vp, i32, vp, f64, f64, f64, vp, pf64, pf64, vp, i32]),
 }
 
 _lib = None

@@ -184,6 +184,94 @@ class Handle:
         self.check(self.lib.mg_gen_spd_gram(self.h, n, _ptr(S), ld_of(S), seed), "mg_gen_spd_gram")
         return S
 
+    # -------------------------------------------------------------- Cholesky
+    def dpotrf(self, A: torch.Tensor, check=True):
+        """In-place Mat LLT: lower triangle of A -> L, upper zeroed. Returns info."""
+        n = A.shape[0]
+        info = C.c_int(0)
+        st = self.lib.mg_dpotrf(self.h, n, _ptr(A), ld_of(A), C.byref(info))
+        if check and st not in (0, 5):
+            self.check(st, "mg_dpotrf")
+        return info.value
+
+    def dpotrs(self, L: torch.Tensor, B: torch.Tensor):
+        """In place: B := (L L^T)^-1 B."""
+        self.check(self.lib.mg_dpotrs(self.h, L.shape[0], B.shape[1], _ptr(L), ld_of(L), _ptr(B), ld_of(B)),
+                   "mg_dpotrs")
+        return B
+
+    # -------------------------------------------------------------------- QR
+    def dqr(self, A: torch.Tensor, Q: torch.Tensor | None = None, R: torch.Tensor | None = None):
+        """Mat QR(A, Q, R, QR_Householder): full m x m Q and m x n R (A unchanged)."""
+        m, n = A.shape
+        if Q is None:
+            Q = colmajor(m, m, device=A.device)
+        if R is None:
+            R = colmajor(m, n, device=A.device)
+        self.check(self.lib.mg_dqr(self.h, m, n, _ptr(A), ld_of(A), _ptr(Q), ld_of(Q), _ptr(R), ld_of(R)),
+                   "mg_dqr")
+        return Q, R
+
+    # -------------------------------------------------------------- adjoints
+    def dpotrf_backward(self, L, Lbar, Abar=None):
+        n = L.shape[0]
+        if Abar is None:
+            Abar = colmajor(n, n, device=L.device)
+        self.check(self.lib.mg_dpotrf_backward(self.h, n, _ptr(L), ld_of(L), _ptr(Lbar), ld_of(Lbar), _ptr(Abar),
+                                               ld_of(Abar)), "mg_dpotrf_backward")
+        return Abar
+
+    def dtrsm_backward(self, L, X, Xbar, Lbar, trans=False):
+        """X = op(L)^-1 B. Returns Bbar; accumulates into the lower triangle of Lbar."""
+        n, nrhs = X.shape
+        Bbar = colmajor(n, nrhs, device=X.device)
+        self.check(self.lib.mg_dtrsm_backward(self.h, int(trans), n, nrhs, _ptr(L), ld_of(L), _ptr(X), ld_of(X),
+                                              _ptr(Xbar), ld_of(Xbar), _ptr(Bbar), ld_of(Bbar), _ptr(Lbar),
+                                              ld_of(Lbar)), "mg_dtrsm_backward")
+        return Bbar
+
+    def dlogdet_chol(self, L) -> float:
+        out = C.c_double()
+        self.check(self.lib.mg_dlogdet_chol(self.h, L.shape[0], _ptr(L), ld_of(L), C.byref(out)), "mg_dlogdet_chol")
+        return out.value
+
+    def dlogdet_chol_backward(self, L, gbar, Lbar):
+        self.check(self.lib.mg_dlogdet_chol_backward(self.h, L.shape[0], _ptr(L), ld_of(L), float(gbar), _ptr(Lbar),
+                                                     ld_of(Lbar)), "mg_dlogdet_chol_backward")
+        return Lbar
+
+    def gen_rbf_kernel(self, X, ell, sigma2=1.0, jitter=1e-2, K=None):
+        n = X.shape[0]
+        if K is None:
+            K = colmajor(n, n, device=X.device)
+        self.check(self.lib.mg_gen_rbf_kernel(self.h, n, _ptr(X), ell, sigma2, jitter, _ptr(K), ld_of(K)),
+                   "mg_gen_rbf_kernel")
+        return K
+
+    def gp_loss_grad(self, X, y, ell, sigma2=1.0, jitter=1e-2, want_kbar=False):
+        n = X.shape[0]
+        loss, dell = C.c_double(), C.c_double()
+        Kb = colmajor(n, n, device=X.device) if want_kbar else None
+        self.check(self.lib.mg_gp_loss_grad(self.h, n, _ptr(X), ell, sigma2, jitter, _ptr(y), C.byref(loss),
+                                            C.byref(dell), _ptr(Kb), ld_of(Kb) if Kb is not None else n),
+                   "mg_gp_loss_grad")
+        return loss.value, dell.value, Kb
+
+    # --------------------------------------------------------------- profile
+    def profile(self, on: bool = True):
+        self.check(self.lib.mg_profile_enable(self.h, int(on)), "mg_profile_enable")
+
+    def profile_records(self) -> dict:
+        out = {}
+        for i in range(self.lib.mg_profile_count(self.h)):
+            name = C.c_char_p()
+            ms, fl, by = C.c_double(), C.c_double(), C.c_double()
+            la = C.c_longlong()
+            self.check(self.lib.mg_profile_get(self.h, i, C.byref(name), C.byref(ms), C.byref(la), C.byref(fl),
+                                               C.byref(by)), "mg_profile_get")
+            out[name.value.decode()] = dict(ms=ms.value, launches=la.value, flops=fl.value, bytes=by.value)
+        return out
+
     def measure_fp64_peaks(self) -> tuple[float, float]:
         a, b = C.c_double(), C.c_double()
         self.check(self.lib.mg_measure_fp64_peaks(self.h, C.byref(a), C.byref(b)), "mg_measure_fp64_peaks")

@@ -24,7 +24,7 @@ constexpr int LLT2_MAX = 2 * LLT_BS;
 // Column jj: t = 1/sqrt(L(jj,jj)); L(r,jj) *= t for r >= jj; then for
 // i > jj: L(r,i) = fma(L(r,jj), -L(i,jj), L(r,i)) for r >= i.
 __global__ void llt2_kernel(double* __restrict__ L, int ldl, int k, int col0, int* __restrict__ info) {
-    __shared__ double s[LLT2_MAX * LLT2_MAX];  // column-major k x k
+    extern __shared__ double s[];  // column-major k x k with stride LLT2_MAX
     for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
         const int r = e % k, c = e / k;
         s[r + c * LLT2_MAX] = L[r + (size_t)c * ldl];
@@ -174,14 +174,16 @@ mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out)
     int* dinfo = (int*)h->ws;
     MG_CHECK_CUDA(h, cudaMemsetAsync(dinfo, 0, sizeof(int), h->stream));
     cudaStream_t st = h->stream;
+    const size_t s2 = (size_t)LLT2_MAX * LLT2_MAX * sizeof(double);
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(llt2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
     if (n <= 2 * LLT_BS) {
-        llt2_kernel<<<1, 128, 0, st>>>(L, ldl, n, 0, dinfo);
+        llt2_kernel<<<1, 128, s2, st>>>(L, ldl, n, 0, dinfo);
         MG_TRY(post_launch(h, "llt2_kernel"));
     } else {
         for (int j = 0; j < n; j += LLT_BS) {
             const int nb = n - j < LLT_BS ? n - j : LLT_BS;
             double* D = L + j + (size_t)j * ldl;
-            llt2_kernel<<<1, 128, 0, st>>>(D, ldl, nb, j, dinfo);
+            llt2_kernel<<<1, 128, s2, st>>>(D, ldl, nb, j, dinfo);
             MG_TRY(post_launch(h, "llt2_kernel"));
             if (j + LLT_BS < n) {
                 const int rows = n - (j + LLT_BS);
@@ -204,7 +206,8 @@ mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out)
     return MG_OK;
 }
 
-mg_status_t dpotrs_impl(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* X, int ldx) {
+// L x = b (forward substitution), in place on X.
+mg_status_t chol_lower_solve(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* X, int ldx) {
     if (n == 0 || nrhs == 0) return MG_OK;
     cudaStream_t st = h->stream;
     for (int b0 = 0; b0 < n; b0 += CS_B) {
@@ -218,6 +221,13 @@ mg_status_t dpotrs_impl(mg_handle_t h, int n, int nrhs, const double* L, int ldl
             MG_TRY(post_launch(h, "chol_fwd_update_kernel"));
         }
     }
+    return MG_OK;
+}
+
+// L^T x = b (back substitution), in place on X.
+mg_status_t chol_lower_t_solve(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* X, int ldx) {
+    if (n == 0 || nrhs == 0) return MG_OK;
+    cudaStream_t st = h->stream;
     const int last = ((n - 1) / CS_B) * CS_B;
     for (int b0 = last; b0 >= 0; b0 -= CS_B) {
         const int b1 = b0 + CS_B < n ? b0 + CS_B : n;
@@ -231,6 +241,11 @@ mg_status_t dpotrs_impl(mg_handle_t h, int n, int nrhs, const double* L, int ldl
         }
     }
     return MG_OK;
+}
+
+mg_status_t dpotrs_impl(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* X, int ldx) {
+    MG_TRY(chol_lower_solve(h, n, nrhs, L, ldl, X, ldx));
+    return chol_lower_t_solve(h, n, nrhs, L, ldl, X, ldx);
 }
 
 }  // namespace mg

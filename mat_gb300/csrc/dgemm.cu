@@ -274,6 +274,8 @@ mg_status_t dgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, in
                      : (alpha == 1.0 && beta == 1.0)  ? 2
                                                       : 3;
     cudaError_t e;
+    ProfScope prof(h, "dgemm_f64", (tri ? 1.0 : 2.0) * m * (double)n * k,
+                   8.0 * ((double)m * k + (double)k * n + (beta == 0.0 ? 1.0 : 2.0) * m * n));
     if (tri) {
         // Cholesky trailing update: C -= A * B^T on lower tiles only
         if (transA || !transB || mode != 1)

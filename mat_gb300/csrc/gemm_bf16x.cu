@@ -65,6 +65,31 @@ __device__ __forceinline__ void tile_coords(int t, int num_m, int num_n, int& mb
     nb = r / gsize;
 }
 
+// Epilogue helpers: 32 consecutive columns of one row of C.
+__device__ __forceinline__ void epi_load(bool rd, const float* crow, int ldc, int col0, int N, float (&cv)[32]) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const int col = col0 + j;
+        cv[j] = (rd && col < N) ? crow[(size_t)col * ldc] : 0.f;
+    }
+}
+
+__device__ __forceinline__ void epi_store(bool wr, float* crow, int ldc, int col0, int N, uint32_t taddr, float alpha,
+                                          float beta, const float (&cv)[32]) {
+    uint32_t r[32];
+    tc::tmem_ld_32x32b_x32(taddr, r);
+    tc::tmem_ld_wait();
+    if (!wr) return;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const int col = col0 + j;
+        if (col < N) {
+            const float v = alpha * __uint_as_float(r[j]);
+            crow[(size_t)col * ldc] = beta == 0.f ? v : fmaf(beta, cv[j], v);
+        }
+    }
+}
+
 template <int NP>
 __global__ void __launch_bounds__(THREADS, 1)
     bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
@@ -218,23 +243,20 @@ __global__ void __launch_bounds__(THREADS, 1)
             tile_coords(t, num_m, num_n, mb, nb);
             const int row = mb * BM + row_in_tile;
             const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN);
+            // Software-pipelined by chunks of 32 columns: the C values of chunk
+            // ch+1 are loaded (32 independent loads per thread in flight) before
+            // chunk ch is combined with the accumulator and stored.
+            const bool rd = beta != 0.f && row < M;
+            const float* crow = C + (size_t)row;
+            float ca[32], cb[32];
+            epi_load(rd, crow, ldc, nb * BN, N, ca);
 #pragma unroll 1
-            for (int ch = 0; ch < BN / 32; ++ch) {
-                uint32_t r[32];
-                tc::tmem_ld_32x32b_x32(taddr + ch * 32, r);
-                tc::tmem_ld_wait();
-                const int col0 = nb * BN + ch * 32;
-                if (row < M) {
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        const int col = col0 + j;
-                        if (col < N) {
-                            float* cp = C + (size_t)row + (size_t)col * ldc;
-                            const float v = alpha * __uint_as_float(r[j]);
-                            *cp = beta == 0.f ? v : fmaf(beta, *cp, v);
-                        }
-                    }
-                }
+            for (int ch = 0; ch < BN / 32; ch += 2) {
+                epi_load(rd, crow, ldc, nb * BN + (ch + 1) * 32, N, cb);
+                epi_store(row < M, C + (size_t)row, ldc, nb * BN + ch * 32, N, taddr + ch * 32, alpha, beta, ca);
+                if (ch + 2 < BN / 32) epi_load(rd, crow, ldc, nb * BN + (ch + 2) * 32, N, ca);
+                epi_store(row < M, C + (size_t)row, ldc, nb * BN + (ch + 1) * 32, N, taddr + (ch + 1) * 32, alpha,
+                          beta, cb);
             }
             tc::tc_fence_before();
             tc::mbar_arrive(&acc_empty[buf]);
@@ -381,6 +403,10 @@ mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, floa
     CUtensorMap ma, mb;
     if (!make_map(&ma, Asplit, M, Kp, np, (size_t)M * Kp, BM) || !make_map(&mb, Bsplit, N, Kp, np, (size_t)N * Kp, BN))
         return fail(h, MG_ERR_CUDA, "cuTensorMapEncodeTiled failed (M=%d N=%d Kp=%d)", M, N, Kp);
+    const int nprod = np == 3 ? 6 : np == 2 ? 3 : 1;
+    // flops: every bf16 product the tensor cores execute; bytes: C read+write plus the split operands once
+    ProfScope prof(h, "gemm_bf16x", 2.0 * M * N * (double)Kp * nprod,
+                   (beta == 0.f ? 4.0 : 8.0) * M * N + 2.0 * np * (double)(M + N) * Kp);
     switch (np) {
         case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err);
         case 2: return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err);

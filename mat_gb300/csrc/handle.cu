@@ -63,9 +63,89 @@ mg_status_t post_launch(mg_handle_t h, const char* name) {
     return MG_OK;
 }
 
+static cudaEvent_t prof_event(mg_handle_t h) {
+    if (!h->prof_pool.empty()) {
+        cudaEvent_t e = h->prof_pool.back();
+        h->prof_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+ProfScope::ProfScope(mg_handle_t h_, const char* name, double flops_, double bytes_)
+    : h(h_), flops(flops_), bytes(bytes_) {
+    if (!h || !h->prof_on) return;
+    int idx = -1;
+    for (size_t i = 0; i < h->prof.size(); ++i)
+        if (h->prof[i].name == name) idx = (int)i;
+    if (idx < 0) {
+        h->prof.push_back({});
+        h->prof.back().name = name;
+        idx = (int)h->prof.size() - 1;
+    }
+    rec = idx;
+    a = prof_event(h);
+    cudaEventRecord(a, h->stream);
+}
+
+ProfScope::~ProfScope() {
+    if (rec < 0 || !a) return;
+    cudaEvent_t b = prof_event(h);
+    cudaEventRecord(b, h->stream);
+    h->prof_pending.push_back({rec, a, b, flops, bytes});
+}
+
+static void prof_resolve(mg_handle_t h) {
+    if (h->prof_pending.empty()) return;
+    cudaStreamSynchronize(h->stream);
+    for (auto& p : h->prof_pending) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            auto& r = h->prof[p.rec];
+            r.ms += ms;
+            r.flops += p.flops;
+            r.bytes += p.bytes;
+            r.launches += 1;
+        }
+        h->prof_pool.push_back(p.a);
+        h->prof_pool.push_back(p.b);
+    }
+    h->prof_pending.clear();
+}
+
 }  // namespace mg
 
 extern "C" {
+
+mg_status_t mg_profile_enable(mg_handle_t h, int on) {
+    if (!h) return MG_ERR_ARG;
+    mg::prof_resolve(h);
+    h->prof_on = on != 0;
+    if (on) h->prof.clear();
+    return MG_OK;
+}
+
+int mg_profile_count(mg_handle_t h) {
+    if (!h) return 0;
+    mg::prof_resolve(h);
+    return (int)h->prof.size();
+}
+
+mg_status_t mg_profile_get(mg_handle_t h, int i, const char** name, double* ms, long long* launches, double* flops,
+                           double* bytes) {
+    if (!h) return MG_ERR_ARG;
+    mg::prof_resolve(h);
+    if (i < 0 || i >= (int)h->prof.size()) return MG_ERR_ARG;
+    const auto& r = h->prof[i];
+    if (name) *name = r.name.c_str();
+    if (ms) *ms = r.ms;
+    if (launches) *launches = r.launches;
+    if (flops) *flops = r.flops;
+    if (bytes) *bytes = r.bytes;
+    return MG_OK;
+}
 
 mg_status_t mg_handle_create(mg_handle_t* out, void* cuda_stream) {
     if (!out) return MG_ERR_ARG;
@@ -89,6 +169,8 @@ mg_status_t mg_handle_create(mg_handle_t* out, void* cuda_stream) {
 
 mg_status_t mg_handle_destroy(mg_handle_t h) {
     if (!h) return MG_ERR_ARG;
+    mg::prof_resolve(h);
+    for (cudaEvent_t e : h->prof_pool) cudaEventDestroy(e);
     if (h->ws || h->hws) cudaStreamSynchronize(h->stream);
     if (h->ws) cudaFree(h->ws);
     if (h->hws) cudaFreeHost(h->hws);

@@ -268,6 +268,30 @@ __global__ void trsm_llnu_kernel(int k, int n, const T* __restrict__ L, int ldl,
     for (int i = 0; i < k; ++i) X[i + (size_t)col * ldx] = sx[i * nt + t];
 }
 
+// Inverse of the unit-lower k x k block L (k <= 128) into Linv (ld k): the
+// block is staged in shared memory and each thread forward-substitutes one
+// column of the identity there.
+__global__ void __launch_bounds__(128) inv_unit_lower_kernel(const float* __restrict__ L, int ldl, int k,
+                                                               float* __restrict__ Linv) {
+    extern __shared__ float sm[];  // [k][k] block, then [k][k] inverse (column-major)
+    float* sl = sm;
+    float* sz = sm + k * k;
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) sl[e] = L[(e % k) + (size_t)(e / k) * ldl];
+    __syncthreads();
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+        float* z = sz + (size_t)c * k;
+        for (int i = 0; i < c; ++i) z[i] = 0.f;
+        z[c] = 1.f;
+        for (int i = c + 1; i < k; ++i) {
+            float sum = 0.f;
+            for (int q = c; q < i; ++q) sum = fmaf(sl[i + q * k], z[q], sum);
+            z[i] = -sum;
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) Linv[e] = sz[e];
+}
+
 __global__ void iota_kernel(int* p, int n) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = i;
 }
@@ -431,6 +455,8 @@ static mg_status_t launch_panel(mg_handle_t h, GetrfCtx<T>& c, T* A, int lda, in
     }
     const size_t smem = (size_t)rpc * nb * sizeof(T);
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ProfScope prof(h, sizeof(T) == 8 ? "panel_f64" : "panel_f32", (double)R * nb * nb,
+                   2.0 * R * nb * sizeof(T));
     MG_CHECK_CUDA(h, cudaMemsetAsync(c.ws.bar, 0, sizeof(unsigned), h->stream));
     void* args[] = {&A, &lda, &m, &r0, &nb, &rpc, &pos, &c.piv, &c.ws, &c.x};
     cudaError_t e;
@@ -450,6 +476,7 @@ static mg_status_t launch_laswp(mg_handle_t h, T* A, int lda, int r0, int kc, co
     if (cols <= 0 || kc <= 0) return MG_OK;
     const int threads = 128;
     int blocks = (cols + threads - 1) / threads;
+    ProfScope prof(h, "laswp", 0.0, 4.0 * kc * cols * sizeof(T));
     laswp_kernel<T><<<blocks, threads, 0, h->stream>>>(A, lda, r0, kc, piv, c_left, c_right, n);
     return post_launch(h, "laswp_kernel");
 }
@@ -461,6 +488,7 @@ static mg_status_t launch_trsm_llnu(mg_handle_t h, int k, int n, const T* L, int
     const size_t smem = ((size_t)k * k + (size_t)k * threads) * sizeof(T);
     auto kern = trsm_llnu_kernel<T>;
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ProfScope prof(h, sizeof(T) == 8 ? "trsm_f64" : "trsm_f32", (double)k * k * n, 2.0 * k * n * sizeof(T));
     kern<<<(n + threads - 1) / threads, threads, smem, h->stream>>>(k, n, L, ldl, X, ldx);
     return post_launch(h, "trsm_llnu_kernel");
 }
@@ -518,16 +546,23 @@ mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* po
 // ----------------------------------------------------------- mixed (fp32)
 size_t sgetrf_xchg_bytes(int num_sms) { return getrf_ws_bytes<float>(num_sms); }
 
+size_t sgetrf_tri_bytes(int nb, int nterms) {
+    return align_up((size_t)nb * nb * sizeof(float), 1024) + bf16x_split_bytes(nb, nb, nterms);
+}
+
 // FP32 blocked right-looking LU with partial pivoting for the mixed solve:
 // fp32 panels (the same cooperative panel kernel), fp32 TRSM on the block
 // row, and the trailing update A22 -= L21*U12 on the BF16 tensor cores with
 // `nterms` split terms (fp32 accumulation).  `xchg` holds
-// sgetrf_xchg_bytes(); `splitA`/`splitB` hold bf16x_split_bytes(n, nb, nterms).
+// sgetrf_xchg_bytes(); `splitA`/`splitB` hold bf16x_split_bytes(n, nb, nterms);
+// `tri` holds sgetrf_tri_bytes(nb, nterms).  The block-row solve
+// U12 = L11^{-1} A12 is an explicit inverse of the unit-lower L11 followed by
+// a split-BF16 GEMM (the refinement absorbs its fp32-level error).
 mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int nb, int nterms, void* xchg,
-                         void* splitA, void* splitB, int* gemm_err, int* info_out) {
+                         void* splitA, void* splitB, void* tri, int* gemm_err, int* info_out) {
     if (info_out) *info_out = 0;
     if (n == 0) return MG_OK;
-    if (nb > PANEL_MAX_NB) return fail(h, MG_ERR_ARG, "sgetrf_mixed: block size %d > %d", nb, PANEL_MAX_NB);
+    if (nb > PANEL_MAX_NB || nb > 128) return fail(h, MG_ERR_ARG, "sgetrf_mixed: block size %d > 128", nb);
     MG_TRY(ensure_hws(h, 64));
     GetrfCtx<float> c = carve<float>(xchg, h->num_sms);
     MG_CHECK_CUDA(h, cudaMemsetAsync(xchg, 0, 256, h->stream));
@@ -540,10 +575,25 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
         if (r + w < n) {
             const int nt = n - (r + w);
             float* A12 = A + r + (size_t)(r + w) * lda;
-            MG_TRY(launch_trsm_llnu<float>(h, w, nt, A + r + (size_t)r * lda, lda, A12, lda));
+            {
+                ProfScope prof(h, "trsm_f32", 2.0 * w * w * (double)nt, 8.0 * w * (double)nt);
+                float* Linv = (float*)tri;
+                void* splitT = (char*)tri + align_up((size_t)nb * nb * sizeof(float), 1024);
+                const size_t ism = 2 * (size_t)w * w * sizeof(float);
+                MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_unit_lower_kernel,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism));
+                inv_unit_lower_kernel<<<1, 128, ism, h->stream>>>(A + r + (size_t)r * lda, lda, w, Linv);
+                MG_TRY(post_launch(h, "inv_unit_lower_kernel"));
+                MG_TRY(bf16x_split<float>(h, true, Linv, w, w, w, nterms, splitT));
+                MG_TRY(bf16x_split<float>(h, false, A12, lda, nt, w, nterms, splitB));
+                MG_TRY(bf16x_gemm_presplit(h, nterms, w, nt, w, 1.0f, splitT, splitB, 0.0f, A12, lda, gemm_err));
+            }
             const float* L21 = A + (r + w) + (size_t)r * lda;
-            MG_TRY(bf16x_split<float>(h, true, L21, lda, nt, w, nterms, splitA));
-            MG_TRY(bf16x_split<float>(h, false, A12, lda, nt, w, nterms, splitB));
+            {
+                ProfScope prof(h, "split", 0.0, 2.0 * nt * w * (4.0 + 2.0 * nterms));
+                MG_TRY(bf16x_split<float>(h, true, L21, lda, nt, w, nterms, splitA));
+                MG_TRY(bf16x_split<float>(h, false, A12, lda, nt, w, nterms, splitB));
+            }
             MG_TRY(bf16x_gemm_presplit(h, nterms, nt, nt, w, -1.0f, splitA, splitB, 1.0f,
                                        A + (r + w) + (size_t)(r + w) * lda, lda, gemm_err));
         }

@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "../../include/mat_gpu.h"
@@ -23,6 +24,21 @@ struct mg_handle_s {
     size_t hws_bytes = 0;
     uint64_t launches = 0;
     char last_error[512] = {0};
+    // Optional per-phase timing with CUDA events on the handle's stream.
+    struct ProfRec {
+        std::string name;
+        double ms = 0, flops = 0, bytes = 0;
+        long long launches = 0;
+    };
+    struct ProfPending {
+        int rec;
+        cudaEvent_t a, b;
+        double flops, bytes;
+    };
+    bool prof_on = false;
+    std::vector<ProfRec> prof;
+    std::vector<ProfPending> prof_pending;
+    std::vector<cudaEvent_t> prof_pool;
 };
 
 namespace mg {
@@ -42,6 +58,18 @@ mg_status_t post_launch(mg_handle_t h, const char* name);
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// Times the launches enqueued during its lifetime under `name` when the
+// handle's profiler is on (events recorded on the handle's stream); records
+// the algorithmic flops / bytes of that work for roofline reporting.
+struct ProfScope {
+    mg_handle_t h;
+    int rec = -1;
+    cudaEvent_t a = nullptr;
+    double flops, bytes;
+    ProfScope(mg_handle_t h_, const char* name, double flops_ = 0, double bytes_ = 0);
+    ~ProfScope();
+};
+
 // Internal GEMM launcher (no argument checking), used by the factorizations.
 // Computes C = alpha*op(A)*op(B) + beta*C.  `tri` = 0 full, 1 = only tiles
 // that intersect the lower triangle of C (row >= col - tile), used by the
@@ -55,6 +83,11 @@ mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* po
 mg_status_t dgetrs_impl(mg_handle_t h, int n, int nrhs, const double* LU, int lda, const int* pos,
                         const double* B, int ldb, double* X, int ldx);
 
+// Cholesky (chol.cu).
+mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out);
+mg_status_t chol_lower_solve(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* X, int ldx);
+mg_status_t chol_lower_t_solve(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* X, int ldx);
+
 // Split-BF16 tensor-core GEMM pieces (gemm_bf16x.cu).
 size_t bf16x_split_bytes(int rows, int K, int np);
 template <typename TIN>
@@ -65,8 +98,9 @@ mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, floa
 
 // FP32 LU with split-BF16 trailing updates (lu.cu).
 size_t sgetrf_xchg_bytes(int num_sms);
+size_t sgetrf_tri_bytes(int nb, int nterms);
 mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int nb, int nterms, void* xchg,
-                         void* splitA, void* splitB, int* gemm_err, int* info_out);
+                         void* splitA, void* splitB, void* tri, int* gemm_err, int* info_out);
 
 }  // namespace mg
 

@@ -62,15 +62,17 @@ __global__ void absrow_reduce_kernel(const double* __restrict__ partial, int nch
 }
 
 // partial[kc][j][i] = sum_{k in chunk} A(i,k) X(k,j)   (fp64 FMA)
+template <int NR>
 __global__ void __launch_bounds__(RES_ROWS) residual_partial_kernel(const double* __restrict__ A, int lda, int n,
-                                                                    int nrhs, const double* __restrict__ X, int ldx,
+                                                                    const double* __restrict__ X, int ldx,
                                                                     double* __restrict__ partial) {
+    constexpr int nrhs = NR;
     __shared__ double xs[MAX_RHS][256];
     const int i = blockIdx.x * RES_ROWS + threadIdx.x;
     const int k0 = blockIdx.y * RES_KCHUNK, k1 = min(n, k0 + RES_KCHUNK);
-    double acc[MAX_RHS];
+    double acc[NR];
 #pragma unroll
-    for (int j = 0; j < MAX_RHS; ++j) acc[j] = 0.0;
+    for (int j = 0; j < NR; ++j) acc[j] = 0.0;
     for (int kb = k0; kb < k1; kb += 256) {
         const int kn = min(256, k1 - kb);
         __syncthreads();
@@ -78,24 +80,17 @@ __global__ void __launch_bounds__(RES_ROWS) residual_partial_kernel(const double
         __syncthreads();
         if (i < n) {
             const double* ap = A + i + (size_t)kb * lda;
-            if (nrhs == 4) {
-                for (int k = 0; k < kn; ++k) {
-                    const double a = ap[(size_t)k * lda];
-                    acc[0] = fma(a, xs[0][k], acc[0]);
-                    acc[1] = fma(a, xs[1][k], acc[1]);
-                    acc[2] = fma(a, xs[2][k], acc[2]);
-                    acc[3] = fma(a, xs[3][k], acc[3]);
-                }
-            } else {
-                for (int k = 0; k < kn; ++k) {
-                    const double a = ap[(size_t)k * lda];
-                    for (int j = 0; j < nrhs; ++j) acc[j] = fma(a, xs[j][k], acc[j]);
-                }
+#pragma unroll 8
+            for (int k = 0; k < kn; ++k) {
+                const double a = ap[(size_t)k * lda];
+#pragma unroll
+                for (int j = 0; j < NR; ++j) acc[j] = fma(a, xs[j][k], acc[j]);
             }
         }
     }
     if (i < n)
-        for (int j = 0; j < nrhs; ++j) partial[((size_t)blockIdx.y * nrhs + j) * n + i] = acc[j];
+#pragma unroll
+        for (int j = 0; j < NR; ++j) partial[((size_t)blockIdx.y * nrhs + j) * n + i] = acc[j];
 }
 
 // r = b - sum_c partial[c]; rnorm[j] = max |r(:,j)|, xnorm[j] = max |x(:,j)|
@@ -174,37 +169,110 @@ __global__ void inv_diag_blocks_kernel(const float* __restrict__ LU, int lda, in
     for (int e = threadIdx.x; e < IR_BLOCK * IR_BLOCK; e += blockDim.x) out[e] = z[e];
 }
 
-// One block step of a blocked triangular solve with precomputed block inverses.
-// LOWER: xb = Linv_b * W[b0..b1); Out[b0..b1) = xb; W[r] -= L[r, b0..b1) xb for r >= b1.
-// UPPER: xb = Uinv_b * W[b0..b1); Out[b0..b1) = xb; W[r] -= U[r, b0..b1) xb for r < b0.
-template <bool LOWER>
-__global__ void __launch_bounds__(128) trsv_inv_step_kernel(const float* __restrict__ LU, int lda, int n, int nrhs,
-                                                            const float* __restrict__ inv_b, float* __restrict__ W,
-                                                            float* __restrict__ Out, int b0) {
+// Blocked triangular solve with precomputed inverses of the 128x128 diagonal
+// blocks.  Out[block] = inv_block * W[block]; for the lower solve the rows
+// below each finished block are updated (W[r] -= L[r, block] x_block), for
+// the upper solve the rows above.  One launch per block step: the CTA that
+// owns the next diagonal block finishes its own rows and then applies that
+// block's inverse, so the next step starts from a final x block.
+template <int NR>
+__device__ __forceinline__ void apply_block_inverse(const float* __restrict__ inv, const float* W, float* Out,
+                                                    int b0, int bs, int n) {
+    constexpr int nrhs = NR;
     __shared__ float wb[MAX_RHS][IR_BLOCK];
-    __shared__ float xb[MAX_RHS][IR_BLOCK];
-    const int bs = min(IR_BLOCK, n - b0);
+    __shared__ float part[2][MAX_RHS][IR_BLOCK];
+    __syncthreads();
     for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) wb[q / bs][q % bs] = W[b0 + q % bs + (size_t)(q / bs) * n];
     __syncthreads();
-    for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) {
-        const int r = q % bs, j = q / bs;
-        float s = 0.f;
-        for (int k = 0; k < bs; ++k) s = fmaf(inv_b[r + k * IR_BLOCK], wb[j][k], s);
-        xb[j][r] = s;
-        if (blockIdx.x == 0) Out[b0 + r + (size_t)j * n] = s;
-    }
-    __syncthreads();
-    const int lo = LOWER ? b0 + bs : 0, hi = LOWER ? n : b0;
-    for (int r = lo + blockIdx.x * blockDim.x + threadIdx.x; r < hi; r += gridDim.x * blockDim.x) {
-        float acc[MAX_RHS];
-        for (int j = 0; j < nrhs; ++j) acc[j] = W[r + (size_t)j * n];
-        const float* lp = LU + r + (size_t)b0 * lda;
-        for (int k = 0; k < bs; ++k) {
-            const float l = lp[(size_t)k * lda];
-            for (int j = 0; j < nrhs; ++j) acc[j] = fmaf(-l, xb[j][k], acc[j]);
+    const int r = threadIdx.x & (IR_BLOCK - 1), hf = threadIdx.x >> 7;
+    const int k0 = hf * (IR_BLOCK / 2), k1 = min(bs, k0 + IR_BLOCK / 2);
+    float acc[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) acc[j] = 0.f;
+    if (r < bs) {
+#pragma unroll 8
+        for (int k = k0; k < k1; ++k) {
+            const float v = inv[r + k * IR_BLOCK];
+#pragma unroll
+            for (int j = 0; j < NR; ++j) acc[j] = fmaf(v, wb[j][k], acc[j]);
         }
-        for (int j = 0; j < nrhs; ++j) W[r + (size_t)j * n] = acc[j];
     }
+#pragma unroll
+    for (int j = 0; j < NR; ++j) part[hf][j][r] = acc[j];
+    __syncthreads();
+    if (hf == 0 && r < bs)
+#pragma unroll
+        for (int j = 0; j < NR; ++j) Out[b0 + r + (size_t)j * n] = part[0][j][r] + part[1][j][r];
+}
+
+template <int NR>
+__global__ void __launch_bounds__(256) trsv_init_kernel(const float* __restrict__ inv_b, const float* __restrict__ W,
+                                                        float* __restrict__ Out, int b0, int n) {
+    apply_block_inverse<NR>(inv_b, W, Out, b0, min(IR_BLOCK, n - b0), n);
+}
+
+// LOWER: rows of blocks b+1.. (CTA i owns block b+1+i); UPPER: rows of blocks
+// 0..b-1 (CTA i owns block i).  256 threads: two threads per row, each half
+// of the block's 128 columns.
+template <bool LOWER, int NR>
+__global__ void __launch_bounds__(256) trsv_step_kernel(const float* __restrict__ LU, int lda, int n,
+                                                        const float* __restrict__ invs, float* __restrict__ W,
+                                                        float* __restrict__ Out, int b) {
+    constexpr int nrhs = NR;
+    __shared__ float xb[MAX_RHS][IR_BLOCK];
+    __shared__ float part[2][MAX_RHS][IR_BLOCK];
+    const int b0 = b * IR_BLOCK, bs = min(IR_BLOCK, n - b0);
+    const int rb = LOWER ? b + 1 + blockIdx.x : blockIdx.x;
+    const int r0 = rb * IR_BLOCK, rows = min(IR_BLOCK, n - r0);
+    for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) xb[q / bs][q % bs] = Out[b0 + q % bs + (size_t)(q / bs) * n];
+    __syncthreads();
+    const int r = threadIdx.x & (IR_BLOCK - 1), hf = threadIdx.x >> 7;
+    const int k0 = hf * (IR_BLOCK / 2), k1 = min(bs, k0 + IR_BLOCK / 2);
+    float acc[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) acc[j] = 0.f;
+    if (r < rows) {
+        const float* lp = LU + (size_t)(r0 + r) + (size_t)b0 * lda;
+#pragma unroll 16
+        for (int k = k0; k < k1; ++k) {
+            const float l = lp[(size_t)k * lda];
+#pragma unroll
+            for (int j = 0; j < NR; ++j) acc[j] = fmaf(l, xb[j][k], acc[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NR; ++j) part[hf][j][r] = acc[j];
+    __syncthreads();
+    if (hf == 0 && r < rows)
+#pragma unroll
+        for (int j = 0; j < NR; ++j) {
+            float* wp = W + r0 + r + (size_t)j * n;
+            *wp = *wp - (part[0][j][r] + part[1][j][r]);
+        }
+    const int next = LOWER ? b + 1 : b - 1;
+    if (rb == next) apply_block_inverse<NR>(invs + (size_t)next * IR_BLOCK * IR_BLOCK, W, Out, r0, rows, n);
+}
+
+// Both triangular solves of one correction (L then U), for NR right-hand sides.
+template <int NR>
+mg_status_t lu_solve_blocked(mg_handle_t h, const float* LU, int n, const float* Linv, const float* Uinv, float* Y,
+                             float* Z) {
+    cudaStream_t st = h->stream;
+    const int nblk = (n + IR_BLOCK - 1) / IR_BLOCK;
+    trsv_init_kernel<NR><<<1, 256, 0, st>>>(Linv, Y, Z, 0, n);
+    MG_TRY(mg::post_launch(h, "trsv_init_kernel"));
+    for (int b = 0; b + 1 < nblk; ++b) {
+        trsv_step_kernel<true, NR><<<nblk - 1 - b, 256, 0, st>>>(LU, n, n, Linv, Y, Z, b);
+        MG_TRY(mg::post_launch(h, "trsv_step_kernel<lower>"));
+    }
+    trsv_init_kernel<NR><<<1, 256, 0, st>>>(Uinv + (size_t)(nblk - 1) * IR_BLOCK * IR_BLOCK, Z, Y,
+                                            (nblk - 1) * IR_BLOCK, n);
+    MG_TRY(mg::post_launch(h, "trsv_init_kernel"));
+    for (int b = nblk - 1; b > 0; --b) {
+        trsv_step_kernel<false, NR><<<b, 256, 0, st>>>(LU, n, n, Uinv, Z, Y, b);
+        MG_TRY(mg::post_launch(h, "trsv_step_kernel<upper>"));
+    }
+    return MG_OK;
 }
 
 struct IrWs {
@@ -213,6 +281,7 @@ struct IrWs {
     void* xchg;
     void* splitA;
     void* splitB;
+    void* tri;
     int* gemm_err;
     float* Linv;
     float* Uinv;
@@ -237,6 +306,7 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
     const size_t oX = take(mg::sgetrf_xchg_bytes(h->num_sms));
     const size_t oSA = take(mg::bf16x_split_bytes(n, IR_BLOCK, nterms));
     const size_t oSB = take(mg::bf16x_split_bytes(n, IR_BLOCK, nterms));
+    const size_t oT = take(mg::sgetrf_tri_bytes(IR_BLOCK, nterms));
     const size_t oE = take(64);
     const size_t oLi = take((size_t)nblk * IR_BLOCK * IR_BLOCK * sizeof(float));
     const size_t oUi = take((size_t)nblk * IR_BLOCK * IR_BLOCK * sizeof(float));
@@ -252,6 +322,7 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
         w->xchg = b + oX;
         w->splitA = b + oSA;
         w->splitB = b + oSB;
+        w->tri = b + oT;
         w->gemm_err = (int*)(b + oE);
         w->Linv = (float*)(b + oLi);
         w->Uinv = (float*)(b + oUi);
@@ -305,6 +376,7 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     double* hn = (double*)h->hws;
 
     // ||A||_inf and ||B||_inf (column-wise) --------------------------------
+    mg::ProfScope* setup = new mg::ProfScope(h, "ir_setup", 0.0, 12.0 * n * (double)n);
     MG_CHECK_CUDA(h, cudaMemsetAsync(w.gemm_err, 0, 64, st));
     MG_CHECK_CUDA(h, cudaMemsetAsync(w.norms, 0, 64 * sizeof(double), st));
     absrow_partial_kernel<<<dim3((n + 255) / 256, kch), 256, 0, st>>>(A, lda, n, w.partial);
@@ -315,9 +387,10 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     // fp32 copy and mixed LU -------------------------------------------------
     d2s_kernel<<<grid_for((size_t)n * n, 256, cap), 256, 0, st>>>(A, lda, n, w.A32, n);
     MG_TRY(mg::post_launch(h, "d2s_kernel"));
+    delete setup;
     int info = 0;
     mg_status_t s = mg::sgetrf_mixed(h, n, w.A32, n, w.pos, IR_BLOCK, o.nterms, w.xchg, w.splitA, w.splitB,
-                                     w.gemm_err, &info);
+                                     w.tri, w.gemm_err, &info);
     if (s != MG_OK && s != MG_SINGULAR) return s;
     r.info = info;
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -343,12 +416,22 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     bool converged = false;
     for (int it = 0; it <= o.max_iter; ++it) {
         MG_CHECK_CUDA(h, cudaMemsetAsync(w.norms, 0, 16 * sizeof(double), st));
-        residual_partial_kernel<<<dim3((n + RES_ROWS - 1) / RES_ROWS, kch), RES_ROWS, 0, st>>>(A, lda, n, nrhs, X,
-                                                                                             ldx, w.partial);
-        MG_TRY(mg::post_launch(h, "residual_partial_kernel"));
+        mg::ProfScope* pr = new mg::ProfScope(h, "ir_residual", 2.0 * n * (double)n * nrhs, 8.0 * n * (double)n);
+        {
+            const dim3 grid((n + RES_ROWS - 1) / RES_ROWS, kch);
+            switch (nrhs) {
+#define MG_RES(NRV) \
+    case NRV: residual_partial_kernel<NRV><<<grid, RES_ROWS, 0, st>>>(A, lda, n, X, ldx, w.partial); break;
+                MG_RES(1) MG_RES(2) MG_RES(3) MG_RES(4) MG_RES(5) MG_RES(6) MG_RES(7)
+                default: residual_partial_kernel<8><<<grid, RES_ROWS, 0, st>>>(A, lda, n, X, ldx, w.partial); break;
+#undef MG_RES
+            }
+            MG_TRY(mg::post_launch(h, "residual_partial_kernel"));
+        }
         residual_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kch, n, nrhs, B, ldb, X, ldx, w.R,
                                                                w.norms);
         MG_TRY(mg::post_launch(h, "residual_reduce_kernel"));
+        delete pr;
         MG_CHECK_CUDA(h, cudaMemcpyAsync(hn, w.norms, 32 * sizeof(double), cudaMemcpyDeviceToHost, st));
         MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
         const double anorm = hn[16];
@@ -376,24 +459,22 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
         // correction: d = U^-1 L^-1 P (r / s), x += s d
         for (int j = 0; j < nrhs; ++j) hn[24 + j] = hn[j];
         MG_CHECK_CUDA(h, cudaMemcpyAsync(w.norms + 24, hn + 24, MAX_RHS * sizeof(double), cudaMemcpyHostToDevice, st));
+        mg::ProfScope* ps = new mg::ProfScope(h, "ir_trsv", 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
         prep_rhs_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(n, nrhs, w.pos, w.R, w.norms + 24, w.Y);
         MG_TRY(mg::post_launch(h, "prep_rhs_kernel"));
-        for (int b = 0; b < nblk; ++b) {
-            const int b0 = b * IR_BLOCK, rows = n - (b0 + IR_BLOCK);
-            const int g = rows > 0 ? std::min(h->num_sms, (rows + 127) / 128) : 1;
-            trsv_inv_step_kernel<true><<<g, 128, 0, st>>>(w.A32, n, n, nrhs, w.Linv + (size_t)b * IR_BLOCK * IR_BLOCK,
-                                                          w.Y, w.Z, b0);
-            MG_TRY(mg::post_launch(h, "trsv_inv_step_kernel<lower>"));
-        }
-        for (int b = nblk - 1; b >= 0; --b) {
-            const int b0 = b * IR_BLOCK;
-            const int g = b0 > 0 ? std::min(h->num_sms, (b0 + 127) / 128) : 1;
-            trsv_inv_step_kernel<false><<<g, 128, 0, st>>>(w.A32, n, n, nrhs,
-                                                           w.Uinv + (size_t)b * IR_BLOCK * IR_BLOCK, w.Z, w.Y, b0);
-            MG_TRY(mg::post_launch(h, "trsv_inv_step_kernel<upper>"));
+        switch (nrhs) {
+            case 1: MG_TRY(lu_solve_blocked<1>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
+            case 2: MG_TRY(lu_solve_blocked<2>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
+            case 3: MG_TRY(lu_solve_blocked<3>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
+            case 4: MG_TRY(lu_solve_blocked<4>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
+            case 5: MG_TRY(lu_solve_blocked<5>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
+            case 6: MG_TRY(lu_solve_blocked<6>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
+            case 7: MG_TRY(lu_solve_blocked<7>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
+            default: MG_TRY(lu_solve_blocked<8>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
         }
         update_x_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(n, nrhs, w.Y, w.norms + 24, X, ldx);
         MG_TRY(mg::post_launch(h, "update_x_kernel"));
+        delete ps;
     }
     const auto t2 = clk::now();
     r.refine_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();

@@ -1,0 +1,369 @@
+// Blocked Householder QR with the full m x m Q (Mat's QR(A, Q, R, QR_Householder)).
+//
+// Reference path (Mat-8.3.1/QR): QR (QR.h:8-25) -> __QR_HouseHolder_Blocked
+// (__Householder_Blocked.h:215-245, 336-353), BS = 48 (AVX-512, Mat.h:77-79):
+// per block of columns the panel __QR_HouseHolder_Blocked2 (:63-84: LAPACK-
+// style reflectors, v0 = 1 implicit, tau = (x0 + cr)/cr, R_rr = -cr with
+// cr = sign(x0)||x||), the upper-triangular T of the compact WY form
+// (CalculateT, :87-103), the trailing update R2 -= V (T^T (V^T R2)) (:144-212),
+// then the full Q accumulated backwards, Q_j -= V (T (V^T Q_j)) (CalculateQ,
+// :248-333), and R zeroed below the diagonal (:346-352).
+//
+// GPU design (results bit-identical to Mat's AVX-512 build for the blocked
+// path):
+//  - every dot product is computed by one warp in the reduction order of
+//    Mat's AVX-512 __dot (Calculate/__AVX512_double.h:110-133): lane p holds
+//    partial sum p (= Mat's accumulator q = p/8, lane p%8), fused over
+//    elements 32t + p, then the remaining full 8-blocks into lanes 0..7, the
+//    lane-wise (a0+a1)+(a2+a3), the fused tail and the 8->4->2->1 sum;
+//  - the panel is one cooperative kernel with one CTA per panel column and
+//    two bounded grid barriers per reflector (after the reflector, after the
+//    columns it updates);
+//  - T: one warp per inner product V_l^T V_i, then the k^2/2 recurrence;
+//  - the trailing update and the Q accumulation: three FP64 DMMA GEMMs on an
+//    explicit unit-lower V (ones on the diagonal, zeros above), whose
+//    per-element fused chains follow Mat's packed GEMMs.
+// Matrices with min(m, n) <= 2*BS use Mat's unblocked normalisation
+// (QR/__HouseHolder.h:179-208) there; this implementation factors them as a
+// single panel of the blocked algorithm, which agrees to rounding.
+#include <cmath>
+
+#include "grid_sync.cuh"
+#include "mg_internal.cuh"
+
+namespace {
+
+constexpr int QR_BS = 48;  // Mat-8.3.1/Mat.h:77-79 (AVX-512)
+constexpr int QR_THREADS = 128;
+
+// Mat's AVX-512 __dot(a, b, len), computed by one full warp; every lane returns
+// the result.  Loads bypass L1 (the operands may have been written by other
+// CTAs of the same cooperative launch).
+__device__ double warp_dot_mat(const double* __restrict__ a, const double* __restrict__ b, int len) {
+    const int lane = threadIdx.x & 31;
+    const int nb = len / 8;
+    double acc = 0.0;
+    int i = 0;
+    // four 8-lane accumulators over strides of 32 elements: lane p <- elements 32t + p
+    for (; i <= nb - 4; i += 4) acc = fma(__ldcg(a + i * 8 + lane), __ldcg(b + i * 8 + lane), acc);
+    // remaining full 8-blocks into the first accumulator (lanes 0..7)
+    for (; i < nb; ++i)
+        if (lane < 8) acc = fma(__ldcg(a + i * 8 + lane), __ldcg(b + i * 8 + lane), acc);
+    const double x1 = __shfl_down_sync(0xffffffffu, acc, 8);
+    const double x2 = __shfl_down_sync(0xffffffffu, acc, 16);
+    const double x3 = __shfl_down_sync(0xffffffffu, acc, 24);
+    double s = (acc + x1) + (x2 + x3);  // meaningful in lanes 0..7
+    const int rem = len - nb * 8;
+    if (lane < rem) s = fma(__ldcg(a + nb * 8 + lane), __ldcg(b + nb * 8 + lane), s);
+    const double s4 = __shfl_down_sync(0xffffffffu, s, 4);
+    const double h4 = s + s4;  // lanes 0..3
+    const double h2 = h4 + __shfl_down_sync(0xffffffffu, h4, 2);  // lanes 0..1
+    const double r = h2 + __shfl_down_sync(0xffffffffu, h2, 1);   // lane 0
+    return __shfl_sync(0xffffffffu, r, 0);
+}
+
+struct QrPanelWs {
+    unsigned* bar;
+    int* err;
+};
+
+// Panel of b columns at P (h rows, ld ldr).  CTA c owns column c.
+__global__ void __launch_bounds__(QR_THREADS) qr_panel_kernel(double* __restrict__ P, int ldr, int h, int b,
+                                                               double* __restrict__ tau, QrPanelWs ws) {
+    __shared__ double s_q, s_hr;
+    __shared__ int s_skip;
+    const int c = blockIdx.x;
+    const int warp = threadIdx.x >> 5;
+    unsigned phase = 0;
+    for (int r = 0; r < b; ++r) {
+        const int len = h - r;
+        double* w = P + r + (size_t)r * ldr;
+        if (c == r) {
+            if (warp == 0) {
+                const double ss = warp_dot_mat(w, w, len);
+                if (threadIdx.x == 0) {
+                    double cr = sqrt(ss);
+                    if (cr == 0.0) {
+                        tau[r] = 0.0;
+                        s_skip = 1;
+                    } else {
+                        const double x0 = __ldcg(w);
+                        if (x0 < 0.0) cr = -cr;
+                        const double w0 = x0 + cr;
+                        s_hr = 1.0 / w0;
+                        w[0] = -cr;
+                        tau[r] = w0 / cr;
+                        s_skip = 0;
+                    }
+                }
+            }
+            __syncthreads();
+            if (!s_skip)
+                for (int i = 1 + threadIdx.x; i < len; i += blockDim.x) w[i] = w[i] * s_hr;
+        }
+        if (!mg::grid_barrier(ws.bar, (++phase) * gridDim.x, ws.err)) return;
+        // apply H_r to the columns right of it (Mat skips them when the column was zero)
+        if (c > r && __ldcg(tau + r) != 0.0) {
+            double* col = P + r + (size_t)c * ldr;
+            if (warp == 0) {
+                const double d = __ldcg(col) + warp_dot_mat(w + 1, col + 1, len - 1);
+                if (threadIdx.x == 0) s_q = -d * __ldcg(tau + r);
+            }
+            __syncthreads();
+            const double q = s_q;
+            for (int i = threadIdx.x; i < len; i += blockDim.x) {
+                const double v = i == 0 ? 1.0 : __ldcg(w + i);
+                col[i] = fma(v, q, col[i]);
+            }
+        }
+        if (!mg::grid_barrier(ws.bar, (++phase) * gridDim.x, ws.err)) return;
+    }
+}
+
+// s[l + i*b] = V_l[i] + dot(V_l[i+1..], V_i[i+1..]) for l < i (one warp each).
+__global__ void qr_t_dots_kernel(const double* __restrict__ P, int ldr, int h, int b, double* __restrict__ S) {
+    const int warps = blockDim.x >> 5;
+    const int gw = blockIdx.x * warps + (threadIdx.x >> 5);
+    const int npairs = b * (b - 1) / 2;
+    if (gw >= npairs) return;
+    // decode pair index gw -> (l, i), i = 1..b-1, l = 0..i-1
+    int i = 1, base = 0;
+    while (base + i <= gw) {
+        base += i;
+        ++i;
+    }
+    const int l = gw - base;
+    const double* vl = P + (size_t)l * ldr;
+    const double* vi = P + (size_t)i * ldr;
+    const double d = warp_dot_mat(vl + i + 1, vi + i + 1, h - i - 1);
+    if ((threadIdx.x & 31) == 0) S[l + (size_t)i * b] = vl[i] + d;
+}
+
+// T (b x b, ld b, upper) from S and tau (Mat's CalculateT recurrence).
+__global__ void qr_t_kernel(const double* __restrict__ S, const double* __restrict__ tau, int b, double* __restrict__ T) {
+    __shared__ double w[QR_BS];
+    if (threadIdx.x != 0) return;
+    for (int e = 0; e < b * b; ++e) T[e] = 0.0;
+    T[0] = tau[0];
+    for (int i = 1; i < b; ++i) {
+        for (int r = 0; r < i; ++r) w[r] = 0.0;
+        for (int c = 0; c < i; ++c) {
+            const double sc = S[c + (size_t)i * b];
+            for (int r = 0; r <= c; ++r) w[r] = fma(T[r + (size_t)c * b], sc, w[r]);
+        }
+        for (int r = 0; r < i; ++r) T[r + (size_t)i * b] = w[r] * -tau[i];
+        T[i + (size_t)i * b] = tau[i];
+    }
+}
+
+// Explicit unit-lower V (h x b, ld h) from the reflectors stored below the diagonal of P.
+__global__ void qr_expand_v_kernel(const double* __restrict__ P, int ldr, int h, int b, double* __restrict__ V) {
+    const size_t total = (size_t)h * b;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(e % h), c = (int)(e / h);
+        V[e] = r > c ? P[r + (size_t)c * ldr] : (r == c ? 1.0 : 0.0);
+    }
+}
+
+__global__ void identity_kernel(double* __restrict__ Q, int ldq, int m) {
+    const size_t total = (size_t)m * m;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(e % m), c = (int)(e / m);
+        Q[r + (size_t)c * ldq] = r == c ? 1.0 : 0.0;
+    }
+}
+
+__global__ void zero_below_kernel(double* __restrict__ R, int ldr, int m, int n) {
+    const size_t total = (size_t)m * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(e % m), c = (int)(e / m);
+        if (r > c) R[r + (size_t)c * ldr] = 0.0;
+    }
+}
+
+__global__ void copy_kernel(const double* __restrict__ A, int lda, int m, int n, double* __restrict__ B, int ldb) {
+    const size_t total = (size_t)m * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(e % m), c = (int)(e / m);
+        B[r + (size_t)c * ldb] = A[r + (size_t)c * lda];
+    }
+}
+
+struct QrWs {
+    unsigned* bar;
+    int* err;
+    double* tau;  // k
+    double* T;    // ceil(k/BS) blocks of BS*BS
+    double* S;    // BS*BS
+    double* V;    // m*BS
+    double* W;    // BS*max(m,n)
+    double* W2;   // BS*max(m,n)
+};
+
+size_t carve_qr(mg_handle_t h, int m, int n, QrWs* w) {
+    const int k = m < n ? m : n;
+    const int nblk = (k + QR_BS - 1) / QR_BS;
+    const int mx = m > n ? m : n;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = mg::align_up(off + bytes, 256);
+        return o;
+    };
+    const size_t o0 = take(256);
+    const size_t oTau = take((size_t)k * 8);
+    const size_t oT = take((size_t)nblk * QR_BS * QR_BS * 8);
+    const size_t oS = take((size_t)QR_BS * QR_BS * 8);
+    const size_t oV = take((size_t)m * QR_BS * 8);
+    const size_t oW = take((size_t)QR_BS * mx * 8);
+    const size_t oW2 = take((size_t)QR_BS * mx * 8);
+    if (w) {
+        char* b = (char*)h->ws;
+        w->bar = (unsigned*)(b + o0);
+        w->err = (int*)(b + o0 + 64);
+        w->tau = (double*)(b + oTau);
+        w->T = (double*)(b + oT);
+        w->S = (double*)(b + oS);
+        w->V = (double*)(b + oV);
+        w->W = (double*)(b + oW);
+        w->W2 = (double*)(b + oW2);
+    }
+    return off;
+}
+
+int grid_cap(mg_handle_t h, size_t total) {
+    size_t g = (total + 255) / 256;
+    const size_t cap = (size_t)h->num_sms * 8;
+    return (int)(g < 1 ? 1 : g > cap ? cap : g);
+}
+
+}  // namespace
+
+namespace mg {
+
+// In place on R (m x n, ld ldr): R above the diagonal, reflectors below;
+// tau and the T blocks in the workspace carved by carve_qr.
+static mg_status_t dgeqrf_blocked(mg_handle_t h, int m, int n, double* R, int ldr, QrWs& w) {
+    const int k = m < n ? m : n;
+    cudaStream_t st = h->stream;
+    for (int j = 0; j < k; j += QR_BS) {
+        const int b = QR_BS < k - j ? QR_BS : k - j;
+        const int hh = m - j;
+        double* P = R + j + (size_t)j * ldr;
+        {
+            ProfScope prof(h, "qr_panel", 4.0 * hh * (double)b * b, 16.0 * hh * (double)b);
+            MG_CHECK_CUDA(h, cudaMemsetAsync(w.bar, 0, sizeof(unsigned), st));
+            double* tau_j = w.tau + j;
+            QrPanelWs pws{w.bar, w.err};
+            void* args[] = {&P, &ldr, (void*)&hh, (void*)&b, &tau_j, &pws};
+            cudaError_t e;
+            if (b > 1)
+                e = cudaLaunchCooperativeKernel((const void*)qr_panel_kernel, dim3(b), dim3(QR_THREADS), args, 0, st);
+            else
+                e = cudaLaunchKernel((const void*)qr_panel_kernel, dim3(1), dim3(QR_THREADS), args, 0, st);
+            if (e != cudaSuccess) return cuda_fail(h, e, "qr_panel_kernel launch");
+            h->launches++;
+        }
+        double* Tj = w.T + (size_t)(j / QR_BS) * QR_BS * QR_BS;
+        {
+            ProfScope prof(h, "qr_t", 2.0 * hh * (double)b * b / 2, 8.0 * hh * (double)b);
+            const int npairs = b * (b - 1) / 2;
+            if (npairs > 0) {
+                qr_t_dots_kernel<<<(npairs + 7) / 8, 256, 0, st>>>(P, ldr, hh, b, w.S);
+                MG_TRY(post_launch(h, "qr_t_dots_kernel"));
+            }
+            qr_t_kernel<<<1, 32, 0, st>>>(w.S, w.tau + j, b, Tj);
+            MG_TRY(post_launch(h, "qr_t_kernel"));
+        }
+        if (j + b < n) {
+            const int nc = n - j - b;
+            double* R2 = R + j + (size_t)(j + b) * ldr;
+            qr_expand_v_kernel<<<grid_cap(h, (size_t)hh * b), 256, 0, st>>>(P, ldr, hh, b, w.V);
+            MG_TRY(post_launch(h, "qr_expand_v_kernel"));
+            // W = V^T R2; W2 = T^T W; R2 -= V W2
+            MG_TRY(dgemm_launch(h, 1, 0, b, nc, hh, 1.0, w.V, hh, R2, ldr, 0.0, w.W, b, 0));
+            MG_TRY(dgemm_launch(h, 1, 0, b, nc, b, 1.0, Tj, b, w.W, b, 0.0, w.W2, b, 0));
+            MG_TRY(dgemm_launch(h, 0, 0, hh, nc, b, -1.0, w.V, hh, w.W2, b, 1.0, R2, ldr, 0));
+        }
+    }
+    return MG_OK;
+}
+
+// Q (m x m) = H_0 H_1 ... H_{k-1}, accumulated backwards from the identity.
+static mg_status_t dorgqr_full(mg_handle_t h, int m, int n, const double* R, int ldr, double* Q, int ldq, QrWs& w) {
+    const int k = m < n ? m : n;
+    cudaStream_t st = h->stream;
+    identity_kernel<<<grid_cap(h, (size_t)m * m), 256, 0, st>>>(Q, ldq, m);
+    MG_TRY(post_launch(h, "identity_kernel"));
+    if (k == 0) return MG_OK;
+    const int last = ((k - 1) / QR_BS) * QR_BS;
+    for (int j = last; j >= 0; j -= QR_BS) {
+        const int b = QR_BS < k - j ? QR_BS : k - j;
+        const int hh = m - j;
+        const double* P = R + j + (size_t)j * ldr;
+        const double* Tj = w.T + (size_t)(j / QR_BS) * QR_BS * QR_BS;
+        double* Qj = Q + j;
+        qr_expand_v_kernel<<<grid_cap(h, (size_t)hh * b), 256, 0, st>>>(P, ldr, hh, b, w.V);
+        MG_TRY(post_launch(h, "qr_expand_v_kernel"));
+        // W = V^T Q_j; W2 = T W; Q_j -= V W2
+        MG_TRY(dgemm_launch(h, 1, 0, b, m, hh, 1.0, w.V, hh, Qj, ldq, 0.0, w.W, b, 0));
+        MG_TRY(dgemm_launch(h, 0, 0, b, m, b, 1.0, Tj, b, w.W, b, 0.0, w.W2, b, 0));
+        MG_TRY(dgemm_launch(h, 0, 0, hh, m, b, -1.0, w.V, hh, w.W2, b, 1.0, Qj, ldq, 0));
+    }
+    return MG_OK;
+}
+
+}  // namespace mg
+
+extern "C" {
+
+mg_status_t mg_dgeqrf(mg_handle_t h, int m, int n, double* A, int lda, double* tau, double* T) {
+    if (!h) return MG_ERR_ARG;
+    if (m < 0 || n < 0 || lda < (m > 1 ? m : 1) || ((size_t)m * n && (!A || !tau || !T)))
+        return mg::fail(h, MG_ERR_ARG, "mg_dgeqrf: bad arguments");
+    const int k = m < n ? m : n;
+    if (k == 0) return MG_OK;
+    MG_TRY(mg::ensure_ws(h, carve_qr(h, m, n, nullptr)));
+    MG_TRY(mg::ensure_hws(h, 64));
+    QrWs w;
+    carve_qr(h, m, n, &w);
+    MG_CHECK_CUDA(h, cudaMemsetAsync(w.bar, 0, 256, h->stream));
+    MG_TRY(mg::dgeqrf_blocked(h, m, n, A, lda, w));
+    const int nblk = (k + QR_BS - 1) / QR_BS;
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(tau, w.tau, (size_t)k * 8, cudaMemcpyDeviceToDevice, h->stream));
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(T, w.T, (size_t)nblk * QR_BS * QR_BS * 8, cudaMemcpyDeviceToDevice, h->stream));
+    int* hw = (int*)h->hws;
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, w.err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (hw[0]) return mg::fail(h, MG_TIMEOUT, "dgeqrf: a panel grid barrier timed out");
+    return MG_OK;
+}
+
+mg_status_t mg_dqr(mg_handle_t h, int m, int n, const double* A, int lda, double* Q, int ldq, double* R, int ldr) {
+    if (!h) return MG_ERR_ARG;
+    if (m < 0 || n < 0 || lda < (m > 1 ? m : 1) || ldq < (m > 1 ? m : 1) || ldr < (m > 1 ? m : 1) ||
+        ((size_t)m * n && (!A || !Q || !R)))
+        return mg::fail(h, MG_ERR_ARG, "mg_dqr: bad arguments");
+    if (m == 0) return MG_OK;
+    MG_TRY(mg::ensure_ws(h, carve_qr(h, m, n, nullptr)));
+    MG_TRY(mg::ensure_hws(h, 64));
+    QrWs w;
+    carve_qr(h, m, n, &w);
+    cudaStream_t st = h->stream;
+    MG_CHECK_CUDA(h, cudaMemsetAsync(w.bar, 0, 256, st));
+    if (A != R) {
+        copy_kernel<<<grid_cap(h, (size_t)m * n), 256, 0, st>>>(A, lda, m, n, R, ldr);
+        MG_TRY(mg::post_launch(h, "copy_kernel"));
+    }
+    MG_TRY(mg::dgeqrf_blocked(h, m, n, R, ldr, w));
+    MG_TRY(mg::dorgqr_full(h, m, n, R, ldr, Q, ldq, w));
+    zero_below_kernel<<<grid_cap(h, (size_t)m * n), 256, 0, st>>>(R, ldr, m, n);
+    MG_TRY(mg::post_launch(h, "zero_below_kernel"));
+    int* hw = (int*)h->hws;
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, w.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
+    if (hw[0]) return mg::fail(h, MG_TIMEOUT, "dqr: a panel grid barrier timed out");
+    return MG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,63 @@
+// Mat call sites compiled against the drop-in header (include/mat_gpu.hpp)
+// instead of Mat.h; writes every result to <outdir>/<name>.bin (raw doubles /
+// ints) for the Python test to compare with the oracle.
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+
+#include "mat_gpu.hpp"
+
+static std::string dir;
+
+template <typename T>
+static void dump(const char* name, const T* p, size_t n) {
+    FILE* f = std::fopen((dir + "/" + name + ".bin").c_str(), "wb");
+    if (!f) std::exit(3);
+    std::fwrite(p, sizeof(T), n, f);
+    std::fclose(f);
+}
+
+int main(int argc, char** argv) {
+    if (argc < 2) return 2;
+    dir = argv[1];
+    // the same seeded inputs the test regenerates in Python
+    MAT<double> A(150, 130), B(130, 170);
+    mg_host_fill_uniform(A.data, A.rows, A.cols, A.rows, 0, -1.0, 1.0, 1);
+    mg_host_fill_uniform(B.data, B.rows, B.cols, B.rows, 1, -1.0, 1.0, 1);
+    MAT<double> C = A * B;
+    dump("gemm", C.data, (size_t)C.rows * C.cols);
+
+    MAT<double> G(300, 300), L, U;
+    mg_host_fill_normal(G.data, 300, 300, 300, 2, 1);
+    int pos[300];
+    LU_init(G, L, U);
+    PLU(G, pos, L, U);
+    dump("plu_pos", pos, 300);
+    dump("plu_L", L.data, (size_t)L.rows * L.cols);
+    dump("plu_U", U.data, (size_t)U.rows * U.cols);
+
+    MAT<double> b(300, 3);
+    mg_host_fill_normal(b.data, 300, 3, 300, 3, 1);
+    MAT<double> x = Solve_direct(G, b);
+    dump("solve", x.data, (size_t)x.rows * x.cols);
+    MAT<double> xm = Solve_mixed(G, b);
+    dump("solve_mixed", xm.data, (size_t)xm.rows * xm.cols);
+
+    double d = Det(G);
+    dump("det", &d, 1);
+
+    // S = W W^T / n + I from the same generator, computed with the drop-in product
+    MAT<double> W(200, 200), Wt(200, 200), S;
+    mg_host_fill_normal(W.data, 200, 200, 200, 4, 1);
+    for (int i = 0; i < 200; ++i)
+        for (int j = 0; j < 200; ++j) Wt(i, j) = W(j, i);
+    S = W * Wt;
+    for (int i = 0; i < 200 * 200; ++i) S.data[i] /= 200.0;
+    for (int i = 0; i < 200; ++i) S(i, i) += 1.0;
+    dump("spd", S.data, (size_t)200 * 200);
+    MAT<double> Lc(200, 200);
+    LLT(S, Lc);
+    dump("llt", Lc.data, (size_t)200 * 200);
+    std::printf("ok\n");
+    return 0;
+}

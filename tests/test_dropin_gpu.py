@@ -1,0 +1,65 @@
+"""Mat call sites compiled against include/mat_gpu.hpp (the drop-in for
+Mat.h) and linked to libmatgpu.so; results compared with the oracle
+(the restatement of Mat-8.3.1 that is bit-identical to its AVX-512 build)."""
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from mat_gb300 import LIB_PATH
+from mat_gb300.api import host_fill_normal, host_fill_uniform
+from oracle.api import restatement
+
+pytestmark = pytest.mark.gpu
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def outputs(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("no C++ compiler")
+    d = tmp_path_factory.mktemp("dropin")
+    exe = d / "dropin"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(ROOT / "tests/cpp/dropin_main.cpp"),
+                    "-L", str(LIB_PATH.parent), "-lmatgpu", f"-Wl,-rpath,{LIB_PATH.parent}", "-o", str(exe)],
+                   check=True)
+    r = subprocess.run([str(exe), str(d)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    return d
+
+
+def load(d, name, shape, dtype=np.float64):
+    a = np.fromfile(d / f"{name}.bin", dtype=dtype)
+    return a.reshape(shape[::-1]).T if len(shape) == 2 else a
+
+
+def test_operator_star_bit_identical(outputs):
+    a = host_fill_uniform(150, 130, 0)
+    b = host_fill_uniform(130, 170, 1)
+    assert np.array_equal(load(outputs, "gemm", (150, 170)), restatement().dgemm(a, b))
+
+
+def test_plu_bit_identical(outputs):
+    g = host_fill_normal(300, 300, 2)
+    pos, L, U = restatement().plu(g)
+    assert np.array_equal(load(outputs, "plu_pos", (300,), np.int32), pos)
+    assert np.array_equal(load(outputs, "plu_L", (300, 300)), L)
+    assert np.array_equal(load(outputs, "plu_U", (300, 300)), U)
+
+
+def test_solve_and_det(outputs):
+    g = host_fill_normal(300, 300, 2)
+    b = host_fill_normal(300, 3, 3)
+    assert np.array_equal(load(outputs, "solve", (300, 3)), restatement().solve(g, b))
+    xm = load(outputs, "solve_mixed", (300, 3))
+    r = b - g @ xm
+    assert (np.abs(r).max(0) / (np.abs(g).sum(1).max() * np.abs(xm).max(0) + np.abs(b).max(0))).max() <= 1e-14
+    det = load(outputs, "det", (1,))[0]
+    assert abs(det - restatement().det(g)) <= 1e-13 * abs(det)
+
+
+def test_llt_bit_identical(outputs):
+    s = load(outputs, "spd", (200, 200))
+    assert np.array_equal(load(outputs, "llt", (200, 200)), restatement().llt(np.asfortranarray(s)))
