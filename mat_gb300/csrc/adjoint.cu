@@ -287,9 +287,8 @@ mg_status_t mg_dtrsm_backward(mg_handle_t h, int trans, int n, int nrhs, const d
 
 mg_status_t mg_dlogdet_chol(mg_handle_t h, int n, const double* L, int ldl, double* host_out) {
     if (!h || n < 0 || ldl < (n > 1 ? n : 1) || !host_out || (n && !L)) return MG_ERR_ARG;
-    MG_TRY(mg::ensure_ws(h, 64));
     MG_TRY(mg::ensure_hws(h, 64));
-    double* d = (double*)h->ws;
+    double* d = (double*)(h->status + 16);
     logdet_kernel<<<1, 256, 0, h->stream>>>(L, ldl, n, d);
     MG_TRY(mg::post_launch(h, "logdet_kernel"));
     MG_CHECK_CUDA(h, cudaMemcpyAsync(h->hws, d, 8, cudaMemcpyDeviceToHost, h->stream));

@@ -169,9 +169,8 @@ namespace mg {
 mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out) {
     if (info_out) *info_out = 0;
     if (n == 0) return MG_OK;
-    MG_TRY(ensure_ws(h, 256));
     MG_TRY(ensure_hws(h, 64));
-    int* dinfo = (int*)h->ws;
+    int* dinfo = h->status;
     MG_CHECK_CUDA(h, cudaMemsetAsync(dinfo, 0, sizeof(int), h->stream));
     cudaStream_t st = h->stream;
     const size_t s2 = (size_t)LLT2_MAX * LLT2_MAX * sizeof(double);

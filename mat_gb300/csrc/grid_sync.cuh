@@ -43,4 +43,36 @@ __device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target,
     return s_ok != 0;
 }
 
+// Split form of the barrier: arrive() publishes this CTA's prior writes and
+// counts it in; wait() blocks until `target` arrivals (bounded).  Work placed
+// between the two overlaps the other CTAs' arrival.
+__device__ __forceinline__ void grid_arrive(unsigned* counter) {
+    __syncthreads();
+    if (threadIdx.x == 0 && gridDim.x > 1) {
+        __threadfence();
+        atomicAdd(counter, 1u);
+    }
+}
+
+__device__ __forceinline__ bool grid_wait(unsigned* counter, unsigned target, int* err) {
+    __shared__ int s_ok2;
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        if (gridDim.x > 1) {
+            unsigned spins = 0;
+            while (ld_acquire_u32(counter) < target) {
+                if (++spins > kSpinLimit) {
+                    atomicExch(err, 8 /* MG_TIMEOUT */);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(spins < 64 ? 20 : 100);
+            }
+        }
+        s_ok2 = ok;
+    }
+    __syncthreads();
+    return s_ok2 != 0;
+}
+
 }  // namespace mg

@@ -163,6 +163,10 @@ mg_status_t mg_handle_create(mg_handle_t* out, void* cuda_stream) {
         delete h;
         return MG_ERR_CUDA;
     }
+    if (cudaMalloc(&h->status, 4096) != cudaSuccess) {
+        delete h;
+        return MG_ERR_ALLOC;
+    }
     *out = h;
     return MG_OK;
 }
@@ -174,6 +178,7 @@ mg_status_t mg_handle_destroy(mg_handle_t h) {
     if (h->ws || h->hws) cudaStreamSynchronize(h->stream);
     if (h->ws) cudaFree(h->ws);
     if (h->hws) cudaFreeHost(h->hws);
+    if (h->status) cudaFree(h->status);
     delete h;
     return MG_OK;
 }

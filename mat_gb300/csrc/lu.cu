@@ -268,28 +268,58 @@ __global__ void trsm_llnu_kernel(int k, int n, const T* __restrict__ L, int ldl,
     for (int i = 0; i < k; ++i) X[i + (size_t)col * ldx] = sx[i * nt + t];
 }
 
-// Inverse of the unit-lower k x k block L (k <= 128) into Linv (ld k): the
-// block is staged in shared memory and each thread forward-substitutes one
-// column of the identity there.
-__global__ void __launch_bounds__(128) inv_unit_lower_kernel(const float* __restrict__ L, int ldl, int k,
-                                                               float* __restrict__ Linv) {
-    extern __shared__ float sm[];  // [k][k] block, then [k][k] inverse (column-major)
-    float* sl = sm;
-    float* sz = sm + k * k;
-    for (int e = threadIdx.x; e < k * k; e += blockDim.x) sl[e] = L[(e % k) + (size_t)(e / k) * ldl];
+// Inverse of the unit-lower k x k block L (k <= 128) into Linv (ld k) by
+// recursive doubling in shared memory: the 16 x 16 diagonal blocks are
+// inverted by substitution (one thread per column), then pairs of adjacent
+// inverted blocks are joined, inv([A 0; C B]) = [A^-1 0; -B^-1 C A^-1 B^-1],
+// for block sizes 16, 32 and 64.
+constexpr int INV_LD = 128;
+
+__global__ void __launch_bounds__(256) inv_unit_lower_kernel(const float* __restrict__ L, int ldl, int k,
+                                                               float* __restrict__ Linv, int ldinv) {
+    extern __shared__ float sm[];
+    float* sl = sm;                     // L, ld INV_LD
+    float* si = sm + INV_LD * INV_LD;   // inverse, ld INV_LD
+    float* tp = si + INV_LD * INV_LD;   // 64 x 64 scratch
+    for (int e = threadIdx.x; e < INV_LD * INV_LD; e += blockDim.x) {
+        const int r = e % INV_LD, c = e / INV_LD;
+        sl[e] = (r < k && c < k && r > c) ? L[r + (size_t)c * ldl] : 0.f;
+        si[e] = 0.f;
+    }
     __syncthreads();
+    // 16 x 16 diagonal blocks
     for (int c = threadIdx.x; c < k; c += blockDim.x) {
-        float* z = sz + (size_t)c * k;
-        for (int i = 0; i < c; ++i) z[i] = 0.f;
+        const int end = min(k, (c / 16) * 16 + 16);
+        float* z = si + c * INV_LD;
         z[c] = 1.f;
-        for (int i = c + 1; i < k; ++i) {
+        for (int i = c + 1; i < end; ++i) {
             float sum = 0.f;
-            for (int q = c; q < i; ++q) sum = fmaf(sl[i + q * k], z[q], sum);
+            for (int q = c; q < i; ++q) sum = fmaf(sl[i + q * INV_LD], z[q], sum);
             z[i] = -sum;
         }
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < k * k; e += blockDim.x) Linv[e] = sz[e];
+    for (int s = 16; s < k; s *= 2) {
+        // every pair (p, p+s) with p multiple of 2s: T = C A^-1, then X21 = -B^-1 T
+        for (int p = 0; p + s < k; p += 2 * s) {
+            const int nb = min(s, k - (p + s));  // rows of the lower block (may be partial)
+            for (int e = threadIdx.x; e < nb * s; e += blockDim.x) {
+                const int r = e % nb, c = e / nb;  // T(r, c) = sum_q C(r, q) Ainv(q, c), q >= c
+                float sum = 0.f;
+                for (int q = c; q < s; ++q) sum = fmaf(sl[(p + s + r) + (p + q) * INV_LD], si[(p + q) + (p + c) * INV_LD], sum);
+                tp[r + c * 64] = sum;
+            }
+            __syncthreads();
+            for (int e = threadIdx.x; e < nb * s; e += blockDim.x) {
+                const int r = e % nb, c = e / nb;  // X21(r, c) = -sum_q Binv(r, q) T(q, c), q <= r
+                float sum = 0.f;
+                for (int q = 0; q <= r; ++q) sum = fmaf(si[(p + s + r) + (p + s + q) * INV_LD], tp[q + c * 64], sum);
+                si[(p + s + r) + (p + c) * INV_LD] = -sum;
+            }
+            __syncthreads();
+        }
+    }
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) Linv[(e % k) + (size_t)(e / k) * ldinv] = si[(e % k) + (e / k) * INV_LD];
 }
 
 __global__ void iota_kernel(int* p, int n) {
@@ -555,11 +585,13 @@ size_t sgetrf_tri_bytes(int nb, int nterms) {
 // row, and the trailing update A22 -= L21*U12 on the BF16 tensor cores with
 // `nterms` split terms (fp32 accumulation).  `xchg` holds
 // sgetrf_xchg_bytes(); `splitA`/`splitB` hold bf16x_split_bytes(n, nb, nterms);
-// `tri` holds sgetrf_tri_bytes(nb, nterms).  The block-row solve
+// `tri` holds sgetrf_tri_bytes(nb, nterms); if Linv_all is not NULL the
+// inverse of every diagonal block of L is kept there (nb*nb floats each,
+// ld nb).  The block-row solve
 // U12 = L11^{-1} A12 is an explicit inverse of the unit-lower L11 followed by
 // a split-BF16 GEMM (the refinement absorbs its fp32-level error).
 mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int nb, int nterms, void* xchg,
-                         void* splitA, void* splitB, void* tri, int* gemm_err, int* info_out) {
+                         void* splitA, void* splitB, void* tri, float* Linv_all, int* gemm_err, int* info_out) {
     if (info_out) *info_out = 0;
     if (n == 0) return MG_OK;
     if (nb > PANEL_MAX_NB || nb > 128) return fail(h, MG_ERR_ARG, "sgetrf_mixed: block size %d > 128", nb);
@@ -568,23 +600,27 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
     MG_CHECK_CUDA(h, cudaMemsetAsync(xchg, 0, 256, h->stream));
     iota_kernel<<<(n + 255) / 256, 256, 0, h->stream>>>(pos, n);
     MG_TRY(post_launch(h, "iota_kernel"));
+    const size_t ism = (2 * (size_t)INV_LD * INV_LD + 64 * 64) * sizeof(float);
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_unit_lower_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism));
     for (int r = 0; r < n; r += nb) {
         const int w = nb < n - r ? nb : n - r;
         MG_TRY(launch_panel<float>(h, c, A, lda, n, r, w, pos));
         MG_TRY(launch_laswp<float>(h, A, lda, r, w, c.piv, r, r + w, n));
+        // inverse of the unit-lower diagonal block (kept with ld nb in Linv_all when requested)
+        float* Lout = Linv_all ? Linv_all + (size_t)(r / nb) * nb * nb : (float*)tri;
+        const int ldo = Linv_all ? nb : w;
+        if (Linv_all || r + w < n) {
+            ProfScope prof(h, "trsm_f32", 2.0 * w * w * (double)w / 3.0, 8.0 * w * (double)w);
+            inv_unit_lower_kernel<<<1, 256, ism, h->stream>>>(A + r + (size_t)r * lda, lda, w, Lout, ldo);
+            MG_TRY(post_launch(h, "inv_unit_lower_kernel"));
+        }
         if (r + w < n) {
             const int nt = n - (r + w);
             float* A12 = A + r + (size_t)(r + w) * lda;
             {
                 ProfScope prof(h, "trsm_f32", 2.0 * w * w * (double)nt, 8.0 * w * (double)nt);
-                float* Linv = (float*)tri;
                 void* splitT = (char*)tri + align_up((size_t)nb * nb * sizeof(float), 1024);
-                const size_t ism = 2 * (size_t)w * w * sizeof(float);
-                MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_unit_lower_kernel,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism));
-                inv_unit_lower_kernel<<<1, 128, ism, h->stream>>>(A + r + (size_t)r * lda, lda, w, Linv);
-                MG_TRY(post_launch(h, "inv_unit_lower_kernel"));
-                MG_TRY(bf16x_split<float>(h, true, Linv, w, w, w, nterms, splitT));
+                MG_TRY(bf16x_split<float>(h, true, Lout, ldo, w, w, nterms, splitT));
                 MG_TRY(bf16x_split<float>(h, false, A12, lda, nt, w, nterms, splitB));
                 MG_TRY(bf16x_gemm_presplit(h, nterms, w, nt, w, 1.0f, splitT, splitB, 0.0f, A12, lda, gemm_err));
             }

@@ -19,6 +19,9 @@ struct mg_handle_s {
     // Device workspace, grown on demand (cudaMalloc) and reused across calls.
     void* ws = nullptr;
     size_t ws_bytes = 0;
+    // Small device area for status words (info / error flags) that must not
+    // overlap the caller-visible workspace.
+    int* status = nullptr;
     // Pinned host workspace (status words read back by info-reporting calls).
     void* hws = nullptr;
     size_t hws_bytes = 0;
@@ -100,7 +103,7 @@ mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, floa
 size_t sgetrf_xchg_bytes(int num_sms);
 size_t sgetrf_tri_bytes(int nb, int nterms);
 mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int nb, int nterms, void* xchg,
-                         void* splitA, void* splitB, void* tri, int* gemm_err, int* info_out);
+                         void* splitA, void* splitB, void* tri, float* Linv_all, int* gemm_err, int* info_out);
 
 }  // namespace mg
 

@@ -169,62 +169,22 @@ __global__ void inv_diag_blocks_kernel(const float* __restrict__ LU, int lda, in
     for (int e = threadIdx.x; e < IR_BLOCK * IR_BLOCK; e += blockDim.x) out[e] = z[e];
 }
 
-// Blocked triangular solve with precomputed inverses of the 128x128 diagonal
-// blocks.  Out[block] = inv_block * W[block]; for the lower solve the rows
-// below each finished block are updated (W[r] -= L[r, block] x_block), for
-// the upper solve the rows above.  One launch per block step: the CTA that
-// owns the next diagonal block finishes its own rows and then applies that
-// block's inverse, so the next step starts from a final x block.
-template <int NR>
-__device__ __forceinline__ void apply_block_inverse(const float* __restrict__ inv, const float* W, float* Out,
-                                                    int b0, int bs, int n) {
-    constexpr int nrhs = NR;
-    __shared__ float wb[MAX_RHS][IR_BLOCK];
-    __shared__ float part[2][MAX_RHS][IR_BLOCK];
-    __syncthreads();
-    for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) wb[q / bs][q % bs] = W[b0 + q % bs + (size_t)(q / bs) * n];
-    __syncthreads();
-    const int r = threadIdx.x & (IR_BLOCK - 1), hf = threadIdx.x >> 7;
-    const int k0 = hf * (IR_BLOCK / 2), k1 = min(bs, k0 + IR_BLOCK / 2);
-    float acc[NR];
-#pragma unroll
-    for (int j = 0; j < NR; ++j) acc[j] = 0.f;
-    if (r < bs) {
-#pragma unroll 8
-        for (int k = k0; k < k1; ++k) {
-            const float v = inv[r + k * IR_BLOCK];
-#pragma unroll
-            for (int j = 0; j < NR; ++j) acc[j] = fmaf(v, wb[j][k], acc[j]);
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < NR; ++j) part[hf][j][r] = acc[j];
-    __syncthreads();
-    if (hf == 0 && r < bs)
-#pragma unroll
-        for (int j = 0; j < NR; ++j) Out[b0 + r + (size_t)j * n] = part[0][j][r] + part[1][j][r];
-}
-
-template <int NR>
-__global__ void __launch_bounds__(256) trsv_init_kernel(const float* __restrict__ inv_b, const float* __restrict__ W,
-                                                        float* __restrict__ Out, int b0, int n) {
-    apply_block_inverse<NR>(inv_b, W, Out, b0, min(IR_BLOCK, n - b0), n);
-}
-
-// LOWER: rows of blocks b+1.. (CTA i owns block b+1+i); UPPER: rows of blocks
-// 0..b-1 (CTA i owns block i).  256 threads: two threads per row, each half
-// of the block's 128 columns.
+// Blocked triangular solves after "pre-inversion": every block column of the
+// strictly lower part of L is replaced once, after the factorization, by
+// M(:, b) = L(:, b) * Linv_b (and the blocks above the diagonal of U by
+// N(:, b) = U(:, b) * Uinv_b).  Forward substitution then reads
+//     y_b final after the updates of blocks < b;  w_r -= M(r, b) y_b (r > b)
+// and x_b = Linv_b y_b is applied to all blocks at once at the end, so the
+// dependent chain per block step is one parallel update with no inverse on it.
 template <bool LOWER, int NR>
-__global__ void __launch_bounds__(256) trsv_step_kernel(const float* __restrict__ LU, int lda, int n,
-                                                        const float* __restrict__ invs, float* __restrict__ W,
-                                                        float* __restrict__ Out, int b) {
-    constexpr int nrhs = NR;
-    __shared__ float xb[MAX_RHS][IR_BLOCK];
-    __shared__ float part[2][MAX_RHS][IR_BLOCK];
+__global__ void __launch_bounds__(256) trsv_update_kernel(const float* __restrict__ M, int lda, int n,
+                                                          float* __restrict__ W, int b) {
+    __shared__ float yb[NR][IR_BLOCK];
+    __shared__ float part[2][NR][IR_BLOCK];
     const int b0 = b * IR_BLOCK, bs = min(IR_BLOCK, n - b0);
     const int rb = LOWER ? b + 1 + blockIdx.x : blockIdx.x;
     const int r0 = rb * IR_BLOCK, rows = min(IR_BLOCK, n - r0);
-    for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) xb[q / bs][q % bs] = Out[b0 + q % bs + (size_t)(q / bs) * n];
+    for (int q = threadIdx.x; q < bs * NR; q += blockDim.x) yb[q / bs][q % bs] = W[b0 + q % bs + (size_t)(q / bs) * n];
     __syncthreads();
     const int r = threadIdx.x & (IR_BLOCK - 1), hf = threadIdx.x >> 7;
     const int k0 = hf * (IR_BLOCK / 2), k1 = min(bs, k0 + IR_BLOCK / 2);
@@ -232,12 +192,21 @@ __global__ void __launch_bounds__(256) trsv_step_kernel(const float* __restrict_
 #pragma unroll
     for (int j = 0; j < NR; ++j) acc[j] = 0.f;
     if (r < rows) {
-        const float* lp = LU + (size_t)(r0 + r) + (size_t)b0 * lda;
-#pragma unroll 16
-        for (int k = k0; k < k1; ++k) {
-            const float l = lp[(size_t)k * lda];
+        const float* mp = M + (size_t)(r0 + r) + (size_t)b0 * lda;
+        int k = k0;
+        for (; k + 16 <= k1; k += 16) {
+            float l[16];
 #pragma unroll
-            for (int j = 0; j < NR; ++j) acc[j] = fmaf(l, xb[j][k], acc[j]);
+            for (int u = 0; u < 16; ++u) l[u] = mp[(size_t)(k + u) * lda];
+#pragma unroll
+            for (int u = 0; u < 16; ++u)
+#pragma unroll
+                for (int j = 0; j < NR; ++j) acc[j] = fmaf(l[u], yb[j][k + u], acc[j]);
+        }
+        for (; k < k1; ++k) {
+            const float l = mp[(size_t)k * lda];
+#pragma unroll
+            for (int j = 0; j < NR; ++j) acc[j] = fmaf(l, yb[j][k], acc[j]);
         }
     }
 #pragma unroll
@@ -249,28 +218,87 @@ __global__ void __launch_bounds__(256) trsv_step_kernel(const float* __restrict_
             float* wp = W + r0 + r + (size_t)j * n;
             *wp = *wp - (part[0][j][r] + part[1][j][r]);
         }
-    const int next = LOWER ? b + 1 : b - 1;
-    if (rb == next) apply_block_inverse<NR>(invs + (size_t)next * IR_BLOCK * IR_BLOCK, W, Out, r0, rows, n);
 }
 
-// Both triangular solves of one correction (L then U), for NR right-hand sides.
+// Out[block b] = inv_b * W[block b] for every block (one CTA per block, the
+// 128 x 128 inverse staged in shared memory).
+template <int NR>
+__global__ void __launch_bounds__(256) blockdiag_apply_kernel(const float* __restrict__ invs,
+                                                              const float* __restrict__ W, float* __restrict__ Out,
+                                                              int n) {
+    extern __shared__ float sinv[];  // IR_BLOCK * IR_BLOCK
+    __shared__ float wb[NR][IR_BLOCK];
+    __shared__ float part[2][NR][IR_BLOCK];
+    const int b0 = blockIdx.x * IR_BLOCK, bs = min(IR_BLOCK, n - b0);
+    const float4* src = reinterpret_cast<const float4*>(invs + (size_t)blockIdx.x * IR_BLOCK * IR_BLOCK);
+    float4* dst = reinterpret_cast<float4*>(sinv);
+    for (int e = threadIdx.x; e < IR_BLOCK * IR_BLOCK / 4; e += blockDim.x) dst[e] = src[e];
+    for (int q = threadIdx.x; q < bs * NR; q += blockDim.x) wb[q / bs][q % bs] = W[b0 + q % bs + (size_t)(q / bs) * n];
+    __syncthreads();
+    const int r = threadIdx.x & (IR_BLOCK - 1), hf = threadIdx.x >> 7;
+    const int k0 = hf * (IR_BLOCK / 2), k1 = min(bs, k0 + IR_BLOCK / 2);
+    float acc[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) acc[j] = 0.f;
+    if (r < bs)
+        for (int k = k0; k < k1; ++k) {
+            const float v = sinv[r + k * IR_BLOCK];
+#pragma unroll
+            for (int j = 0; j < NR; ++j) acc[j] = fmaf(v, wb[j][k], acc[j]);
+        }
+#pragma unroll
+    for (int j = 0; j < NR; ++j) part[hf][j][r] = acc[j];
+    __syncthreads();
+    if (hf == 0 && r < bs)
+#pragma unroll
+        for (int j = 0; j < NR; ++j) Out[b0 + r + (size_t)j * n] = part[0][j][r] + part[1][j][r];
+}
+
+// Both triangular solves of one correction: Y (in, destroyed) -> Y = U^-1 L^-1 Y, Z scratch.
 template <int NR>
 mg_status_t lu_solve_blocked(mg_handle_t h, const float* LU, int n, const float* Linv, const float* Uinv, float* Y,
                              float* Z) {
     cudaStream_t st = h->stream;
     const int nblk = (n + IR_BLOCK - 1) / IR_BLOCK;
-    trsv_init_kernel<NR><<<1, 256, 0, st>>>(Linv, Y, Z, 0, n);
-    MG_TRY(mg::post_launch(h, "trsv_init_kernel"));
+    const size_t ism = (size_t)IR_BLOCK * IR_BLOCK * sizeof(float);
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(blockdiag_apply_kernel<NR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)ism));
     for (int b = 0; b + 1 < nblk; ++b) {
-        trsv_step_kernel<true, NR><<<nblk - 1 - b, 256, 0, st>>>(LU, n, n, Linv, Y, Z, b);
-        MG_TRY(mg::post_launch(h, "trsv_step_kernel<lower>"));
+        trsv_update_kernel<true, NR><<<nblk - 1 - b, 256, 0, st>>>(LU, n, n, Y, b);
+        MG_TRY(mg::post_launch(h, "trsv_update_kernel<lower>"));
     }
-    trsv_init_kernel<NR><<<1, 256, 0, st>>>(Uinv + (size_t)(nblk - 1) * IR_BLOCK * IR_BLOCK, Z, Y,
-                                            (nblk - 1) * IR_BLOCK, n);
-    MG_TRY(mg::post_launch(h, "trsv_init_kernel"));
+    blockdiag_apply_kernel<NR><<<nblk, 256, ism, st>>>(Linv, Y, Z, n);
+    MG_TRY(mg::post_launch(h, "blockdiag_apply_kernel"));
     for (int b = nblk - 1; b > 0; --b) {
-        trsv_step_kernel<false, NR><<<b, 256, 0, st>>>(LU, n, n, Uinv, Z, Y, b);
-        MG_TRY(mg::post_launch(h, "trsv_step_kernel<upper>"));
+        trsv_update_kernel<false, NR><<<b, 256, 0, st>>>(LU, n, n, Z, b);
+        MG_TRY(mg::post_launch(h, "trsv_update_kernel<upper>"));
+    }
+    blockdiag_apply_kernel<NR><<<nblk, 256, ism, st>>>(Uinv, Z, Y, n);
+    return mg::post_launch(h, "blockdiag_apply_kernel");
+}
+
+// Replaces the off-diagonal block columns of the packed LU by M = L(:,b) Linv_b
+// (below the diagonal) and N = U(:,b) Uinv_b (above it), with split-BF16
+// tensor-core GEMMs (fp32-level accuracy).
+mg_status_t preinvert_blocks(mg_handle_t h, float* LU, int n, const float* Linv, const float* Uinv, int nterms,
+                             void* splitA, void* splitB, int* gemm_err) {
+    const int nblk = (n + IR_BLOCK - 1) / IR_BLOCK;
+    for (int b = 0; b < nblk; ++b) {
+        const int b0 = b * IR_BLOCK, bs = IR_BLOCK < n - b0 ? IR_BLOCK : n - b0, b1 = b0 + bs;
+        if (b1 < n) {  // below: (n - b1) x bs
+            float* C = LU + b1 + (size_t)b0 * n;
+            MG_TRY(mg::bf16x_split<float>(h, true, C, n, n - b1, bs, nterms, splitA));
+            MG_TRY(mg::bf16x_split<float>(h, false, Linv + (size_t)b * IR_BLOCK * IR_BLOCK, IR_BLOCK, bs, bs,
+                                          nterms, splitB));
+            MG_TRY(mg::bf16x_gemm_presplit(h, nterms, n - b1, bs, bs, 1.0f, splitA, splitB, 0.0f, C, n, gemm_err));
+        }
+        if (b0 > 0) {  // above: b0 x bs
+            float* C = LU + (size_t)b0 * n;
+            MG_TRY(mg::bf16x_split<float>(h, true, C, n, b0, bs, nterms, splitA));
+            MG_TRY(mg::bf16x_split<float>(h, false, Uinv + (size_t)b * IR_BLOCK * IR_BLOCK, IR_BLOCK, bs, bs,
+                                          nterms, splitB));
+            MG_TRY(mg::bf16x_gemm_presplit(h, nterms, b0, bs, bs, 1.0f, splitA, splitB, 0.0f, C, n, gemm_err));
+        }
     }
     return MG_OK;
 }
@@ -390,19 +418,20 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     delete setup;
     int info = 0;
     mg_status_t s = mg::sgetrf_mixed(h, n, w.A32, n, w.pos, IR_BLOCK, o.nterms, w.xchg, w.splitA, w.splitB,
-                                     w.tri, w.gemm_err, &info);
+                                     w.tri, w.Linv, w.gemm_err, &info);
     if (s != MG_OK && s != MG_SINGULAR) return s;
     r.info = info;
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
-    inv_diag_blocks_kernel<true><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
-                                                                                                 w.Linv);
-    MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<lower>"));
     inv_diag_blocks_kernel<false><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
                                                                                                   w.Uinv);
     MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<upper>"));
+    {
+        mg::ProfScope prof(h, "ir_preinvert", 2.0 * n * (double)n * IR_BLOCK * 6, 8.0 * n * (double)n);
+        MG_TRY(preinvert_blocks(h, w.A32, n, w.Linv, w.Uinv, o.nterms, w.splitA, w.splitB, w.gemm_err));
+    }
     MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
     const auto t1 = clk::now();
     r.factor_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();

@@ -19,7 +19,9 @@
 //  - the panel is one cooperative kernel with one CTA per panel column and
 //    two bounded grid barriers per reflector (after the reflector, after the
 //    columns it updates);
-//  - T: one warp per inner product V_l^T V_i, then the k^2/2 recurrence;
+//  - T: four lanes per inner product V_l^T V_i in the order of Mat's generic
+//    __dot (CalculateT passes const pointers, which selects that template),
+//    then the k^2/2 recurrence;
 //  - the trailing update and the Q accumulation: three FP64 DMMA GEMMs on an
 //    explicit unit-lower V (ones on the diagonal, zeros above), whose
 //    per-element fused chains follow Mat's packed GEMMs.
@@ -120,23 +122,50 @@ __global__ void __launch_bounds__(QR_THREADS) qr_panel_kernel(double* __restrict
     }
 }
 
-// s[l + i*b] = V_l[i] + dot(V_l[i+1..], V_i[i+1..]) for l < i (one warp each).
+// Mat's generic __dot template as the reference build evaluates it (used by
+// CalculateT, QR/__Householder_Blocked.h:95, whose operands are const): four
+// partial sums over i mod 4, the first floor(n4/32)*32 elements multiplied
+// and added separately (vectorised in the reference build), the rest fused,
+// ((t0 + t1) + t2) + t3, then a fused tail.  Computed by four consecutive
+// lanes (one partial sum each); lane q0 of the group returns the result.
+__device__ double quad_dot_generic(const double* __restrict__ a, const double* __restrict__ b, int len, int q) {
+    const int n4 = 4 * (len / 4), nv = (n4 / 32) * 32;
+    double t = 0.0;
+    int i = q;
+    for (; i < nv; i += 4) t = __dadd_rn(t, __dmul_rn(__ldcg(a + i), __ldcg(b + i)));
+    for (; i < n4; i += 4) t = fma(__ldcg(a + i), __ldcg(b + i), t);
+    // lanes q = 0..3 of a group of four consecutive lanes
+    const unsigned full = 0xffffffffu;
+    const double t1 = __shfl_down_sync(full, t, 1);
+    const double t2 = __shfl_down_sync(full, t, 2);
+    const double t3 = __shfl_down_sync(full, t, 3);
+    double ans = ((t + t1) + t2) + t3;  // meaningful in lane q == 0
+    if (q == 0)
+        for (int j = n4; j < len; ++j) ans = fma(__ldcg(a + j), __ldcg(b + j), ans);
+    return ans;
+}
+
+// s[l + i*b] = V_l[i] + dot(V_l[i+1..], V_i[i+1..]) for l < i; eight pairs per
+// warp, four lanes per pair.
 __global__ void qr_t_dots_kernel(const double* __restrict__ P, int ldr, int h, int b, double* __restrict__ S) {
-    const int warps = blockDim.x >> 5;
-    const int gw = blockIdx.x * warps + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31, q = lane & 3;
+    const int gp = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;  // pair index
     const int npairs = b * (b - 1) / 2;
-    if (gw >= npairs) return;
-    // decode pair index gw -> (l, i), i = 1..b-1, l = 0..i-1
-    int i = 1, base = 0;
-    while (base + i <= gw) {
-        base += i;
-        ++i;
+    const bool active = gp < npairs;
+    int i = 1, l = 0;
+    if (active) {
+        int base = 0;
+        while (base + i <= gp) {
+            base += i;
+            ++i;
+        }
+        l = gp - base;
     }
-    const int l = gw - base;
     const double* vl = P + (size_t)l * ldr;
     const double* vi = P + (size_t)i * ldr;
-    const double d = warp_dot_mat(vl + i + 1, vi + i + 1, h - i - 1);
-    if ((threadIdx.x & 31) == 0) S[l + (size_t)i * b] = vl[i] + d;
+    const int len = active ? h - i - 1 : 0;
+    const double d = quad_dot_generic(vl + i + 1, vi + i + 1, len, q);
+    if (active && q == 0) S[l + (size_t)i * b] = __ldcg(vl + i) + d;
 }
 
 // T (b x b, ld b, upper) from S and tau (Mat's CalculateT recurrence).
@@ -269,7 +298,7 @@ static mg_status_t dgeqrf_blocked(mg_handle_t h, int m, int n, double* R, int ld
             ProfScope prof(h, "qr_t", 2.0 * hh * (double)b * b / 2, 8.0 * hh * (double)b);
             const int npairs = b * (b - 1) / 2;
             if (npairs > 0) {
-                qr_t_dots_kernel<<<(npairs + 7) / 8, 256, 0, st>>>(P, ldr, hh, b, w.S);
+                qr_t_dots_kernel<<<(npairs * 4 + 255) / 256, 256, 0, st>>>(P, ldr, hh, b, w.S);
                 MG_TRY(post_launch(h, "qr_t_dots_kernel"));
             }
             qr_t_kernel<<<1, 32, 0, st>>>(w.S, w.tau + j, b, Tj);

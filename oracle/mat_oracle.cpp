@@ -110,6 +110,34 @@ double dot_mat(const double* a, const double* b, int len) {
     return h2[0] + h2[1];
 }
 
+// Mat's generic __dot template (Calculate/Calculate.h:266-281) as the
+// reference build evaluates it (g++ 13 -O3 with AVX-512/FMA): four partial
+// sums over i mod 4; the first floor(n4/32)*32 elements are vectorised with
+// separate multiply and add, the remaining groups of four are fused; then
+// ((t0 + t1) + t2) + t3 and a fused tail.  Overload resolution picks this
+// template wherever Mat passes const pointers, e.g. CalculateT
+// (QR/__Householder_Blocked.h:95), instead of the AVX-512 overload.
+double dot_generic(const double* a, const double* b, int len) {
+    double t0 = 0, t1 = 0, t2 = 0, t3 = 0;
+    const int n4 = 4 * (len / 4), nv = (n4 / 32) * 32;
+    int i = 0;
+    for (; i < nv; i += 4) {
+        t0 = t0 + a[i] * b[i];
+        t1 = t1 + a[i + 1] * b[i + 1];
+        t2 = t2 + a[i + 2] * b[i + 2];
+        t3 = t3 + a[i + 3] * b[i + 3];
+    }
+    for (; i < n4; i += 4) {
+        t0 = std::fma(a[i], b[i], t0);
+        t1 = std::fma(a[i + 1], b[i + 1], t1);
+        t2 = std::fma(a[i + 2], b[i + 2], t2);
+        t3 = std::fma(a[i + 3], b[i + 3], t3);
+    }
+    double ans = t0 + t1 + t2 + t3;
+    for (int j = n4; j < len; ++j) ans = std::fma(a[j], b[j], ans);
+    return ans;
+}
+
 // ---------------------------------------------------------------- TRSM
 // X(k x n) := L^{-1} X, L unit lower k x k (Mat's AVX-512 __Solve_direct_LX,
 // LU/__Base.h:95-208): 8-column blocks by four partial sums, the ragged
@@ -366,7 +394,7 @@ void qr_T(const double* V, int ldv, int h, int k, const double* tau, double* T /
         for (int l = 0; l < i; ++l) {
             const double* vl = V + (size_t)l * ldv;
             const double* vi = V + (size_t)i * ldv;
-            s[l] = vl[i] + dot_mat(vl + i + 1, vi + i + 1, h - i - 1);
+            s[l] = vl[i] + dot_generic(vl + i + 1, vi + i + 1, h - i - 1);
         }
         for (int r = 0; r < i; ++r) w[r] = 0.0;
         for (int c = 0; c < i; ++c)
@@ -416,43 +444,53 @@ void apply_block_reflector(const std::vector<double>& Vd, int h, int k, const do
 }
 
 // Unblocked Householder QR (Mat's __QR_HouseHolder + __HouseHolder_Q1,
-// QR/__HouseHolder.h:179-208, 48-79), used when min(m,n) <= 2*BS_QR.
+// QR/__HouseHolder.h:179-208, 48-79), used when min(m,n) <= 2*BS_QR.  The
+// reflectors are kept where Mat keeps them, w_r at Q + 2 m r - r^2 (length
+// m - r, scaled so that w^T w = 2), and Q is accumulated backwards in place
+// in the trailing square blocks of Q's storage exactly as Mat does.
 void qr_unblocked(int m, int n, double* R, double* Q) {
     const int k = std::min(m, n);
-    std::vector<std::vector<double>> ws(k);
     for (int r = 0; r < k; ++r) {
-        std::vector<double>& w = ws[r];
-        w.assign(R + r + (size_t)r * m, R + m + (size_t)r * m);
+        double* w = Q + 2 * (size_t)m * r - (size_t)r * r;
         const int len = m - r;
-        double cr = std::sqrt(dot_mat(w.data(), w.data(), len));
-        if (cr == 0.0) {
-            w.assign(len, 0.0);
-            continue;
-        }
+        std::memcpy(w, R + r + (size_t)r * m, sizeof(double) * len);
+        double cr = std::sqrt(dot_mat(w, w, len));
+        if (cr == 0.0) continue;
         if (w[0] < 0.0) cr = -cr;
         w[0] += cr;
         const double hr = 1.0 / std::sqrt(cr * w[0]);
         for (int i = 0; i < len; ++i) w[i] = w[i] * hr;
-        for (int c = r; c < n; ++c) {
+        for (int c = r; c < n; ++c) {  // __ApplyHouseHolderOnTheLeft2(R, w, r, r)
             double* col = R + r + (size_t)c * m;
-            const double d = -dot_mat(w.data(), col, len);
+            const double d = -dot_mat(w, col, len);
             for (int i = 0; i < len; ++i) col[i] = std::fma(w[i], d, col[i]);
         }
     }
-    // Q = H_0 H_1 ... H_{k-1} applied to I, accumulated backwards (H = I - w w^T).
-    std::fill(Q, Q + (size_t)m * m, 0.0);
-    for (int i = 0; i < m; ++i) Q[i + (size_t)i * m] = 1.0;
+    // __HouseHolder_Q1(Q, k)
+    int r2 = m - k;
+    double* T2 = Q + (size_t)m * m - (size_t)r2 * r2;
+    std::fill(T2, T2 + (size_t)r2 * r2, 0.0);
+    for (int i = 0; i < r2; ++i) T2[(size_t)i * r2 + i] = 1.0;
     for (int r = k - 1; r >= 0; --r) {
-        const std::vector<double>& w = ws[r];
-        const int len = m - r;
-        for (int c = r; c < m; ++c) {
-            double* col = Q + r + (size_t)c * m;
-            const double d = -dot_mat(w.data(), col, len);
-            for (int i = 0; i < len; ++i) col[i] = std::fma(w[i], d, col[i]);
+        const int r1 = m - r;
+        double* T1 = Q + (size_t)m * m - (size_t)r1 * r1;
+        std::fill(T1 + r1, T1 + r1 + (r1 - 1), 0.0);
+        double* w = T1;
+        for (int i = 1; i < r1; ++i) {
+            const double temp = -dot_mat(w + 1, T2 + (size_t)(i - 1) * r2, r2);
+            T1[(size_t)i * r1] = w[0] * temp;
+            double* dst = T1 + (size_t)i * r1 + 1;
+            const double* src = T2 + (size_t)(i - 1) * r2;
+            for (int e = 0; e < r2; ++e) dst[e] = std::fma(w[1 + e], temp, src[e]);  // in place, forward
         }
+        const double q = -w[0];
+        for (int e = 0; e < r1; ++e) w[e] = w[e] * q;
+        w[0] += 1.0;
+        T2 = T1;
+        r2 = r1;
     }
-    for (int j = 0; j < n; ++j)
-        for (int r = j + 1; r < m; ++r) R[r + (size_t)j * m] = 0.0;
+    // Mat's unblocked path leaves R's below-diagonal entries as the reflection
+    // computed them (rounding-level values), unlike the blocked path.
 }
 
 }  // namespace

@@ -34,6 +34,9 @@ void ref_dgemm(int m, int n, int k, const double* A, const double* B, double* C)
 void ref_plu(int m, int n, const double* A, int* pos, double* L, double* U) {
     MAT<double> a = make(m, n, A), l, u;
     LU_init(a, l, u);
+    // Mat never writes L's columns >= min(m, n) (they stay as allocated)
+    l.fill(0.0);
+    u.fill(0.0);
     PLU(a, pos, l, u);
     out(l, L);
     out(u, U);

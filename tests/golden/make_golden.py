@@ -1,0 +1,101 @@
+"""Generates the golden fixtures in this directory by running the reference
+itself: Mat-8.3.1 compiled from its own headers into oracle/_ref/libmatref.so
+(x86-64 AVX-512 build, the configuration of Mat's published numbers).
+
+Inputs come from the library's seeded generators (mg_host_fill_*), which are
+bit-identical on the host and the GPU.  Small cases keep full outputs; the
+benchmark-size cases keep SHA-256 digests of the raw column-major output
+bytes (exact, size-independent) plus a few sketch values.
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from mat_gb300.api import host_fill_normal, host_fill_uniform  # noqa: E402
+from oracle.api import reference  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.asfortranarray(a).tobytes(order="F")).hexdigest()
+
+
+def sketch(a: np.ndarray, seed: int = 99) -> list:
+    """4x4 sketch Omega^T a Psi with seeded +-1 Omega, Psi (for tolerance checks)."""
+    rng = np.random.default_rng(seed)
+    om = rng.choice([-1.0, 1.0], size=(a.shape[0], 4))
+    ps = rng.choice([-1.0, 1.0], size=(a.shape[1], 4))
+    return (om.T @ a @ ps).tolist()
+
+
+def spd(n: int, seed: int) -> np.ndarray:
+    g = host_fill_normal(n, n, seed)
+    return np.asfortranarray(g @ g.T / n + np.eye(n))
+
+
+def main():
+    ref = reference()
+    if ref is None:
+        raise SystemExit("the reference build (oracle/_ref) needs the reference tree and an x86-64 host")
+    meta = {"generator": "tests/golden/make_golden.py", "reference": "Mat-8.3.1 (AVX-512 build)", "cases": {}}
+    t0 = time.time()
+
+    # GEMM, benchmark configuration M=N=K=1024, A, B uniform [-1,1) seeds 0, 1 (row-major stream)
+    a = host_fill_uniform(1024, 1024, 0)
+    b = host_fill_uniform(1024, 1024, 1)
+    c = ref.dgemm(a, b)
+    meta["cases"]["gemm_1024"] = {"sha256": sha(c), "sum": float(c.sum()), "sketch": sketch(c)}
+    a = host_fill_uniform(61, 90, 2)
+    b = host_fill_uniform(90, 97, 3)
+    np.savez_compressed(OUT / "gemm_61x97x90.npz", c=ref.dgemm(a, b))
+
+    # PLU: full factors for small n, digests for larger
+    for n in (61, 97):
+        pos, L, U = ref.plu(host_fill_normal(n, n, 1))
+        np.savez_compressed(OUT / f"plu_{n}.npz", pos=pos, L=L, U=U)
+    for n in (257, 1000, 8192):
+        pos, L, U = ref.plu(host_fill_normal(n, n, 1))
+        np.save(OUT / f"plu_{n}_pos.npy", pos.astype(np.int32))
+        meta["cases"][f"plu_{n}"] = {"sha256_L": sha(L), "sha256_U": sha(U), "sketch_L": sketch(L),
+                                     "sketch_U": sketch(U)}
+
+    # Solve_direct (narrow path): 1 and 4 right-hand sides
+    for n, k in ((300, 4), (2048, 1)):
+        x = ref.solve(host_fill_normal(n, n, 1), host_fill_normal(n, k, 2))
+        meta["cases"][f"solve_{n}_{k}"] = {"sha256": sha(x), "x0": x[:4, 0].tolist()}
+
+    # LLT: S = G G^T / n + I
+    np.savez_compressed(OUT / "llt_97.npz", L=ref.llt(spd(97, 1)))
+    for n in (300, 8192):
+        L = ref.llt(spd(n, 1))
+        meta["cases"][f"llt_{n}"] = {"sha256": sha(L), "sketch": sketch(L)}
+
+    # QR (Householder): unblocked path in full, blocked path by digest
+    q, r = ref.qr(host_fill_normal(60, 40, 7))
+    np.savez_compressed(OUT / "qr_60x40.npz", Q=q, R=r)
+    for m, n in ((300, 200), (1000, 500)):
+        q, r = ref.qr(host_fill_normal(m, n, 7))
+        meta["cases"][f"qr_{m}x{n}"] = {"sha256_Q": sha(q), "sha256_R": sha(r), "sketch_R": sketch(r)}
+
+    # Det
+    meta["cases"]["det_150"] = {"value": ref.det(host_fill_normal(150, 150, 5))}
+
+    meta["seconds"] = round(time.time() - t0, 1)
+    (OUT / "golden.json").write_text(json.dumps(meta, indent=1))
+    print(f"golden fixtures written in {meta['seconds']} s")
+
+
+if __name__ == "__main__":
+    main()

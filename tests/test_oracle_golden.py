@@ -1,0 +1,98 @@
+"""The oracle (CPU restatement of Mat-8.3.1) pinned against golden fixtures
+produced by the reference itself (tests/golden/make_golden.py): bit-exact
+equality (full arrays or SHA-256 of the raw column-major bytes), including the
+benchmark sizes n = 8192 (PLU, LLT) and M=N=K=1024 (GEMM)."""
+import hashlib
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from mat_gb300.api import host_fill_normal, host_fill_uniform
+from oracle.api import reference, restatement
+
+G = Path(__file__).resolve().parent / "golden"
+META = json.loads((G / "golden.json").read_text())["cases"]
+
+
+def sha(a):
+    return hashlib.sha256(np.asfortranarray(a).tobytes(order="F")).hexdigest()
+
+
+def spd(n, seed):
+    g = host_fill_normal(n, n, seed)
+    return np.asfortranarray(g @ g.T / n + np.eye(n))
+
+
+@pytest.fixture(scope="module")
+def orc():
+    o = restatement()
+    o.set_threads(8)
+    return o
+
+
+def test_gemm(orc):
+    c = orc.dgemm(host_fill_uniform(61, 90, 2), host_fill_uniform(90, 97, 3))
+    assert np.array_equal(c, np.load(G / "gemm_61x97x90.npz")["c"])
+    c = orc.dgemm(host_fill_uniform(1024, 1024, 0), host_fill_uniform(1024, 1024, 1))
+    assert sha(c) == META["gemm_1024"]["sha256"]
+
+
+@pytest.mark.parametrize("n", [61, 97])
+def test_plu_small(orc, n):
+    pos, L, U = orc.plu(host_fill_normal(n, n, 1))
+    f = np.load(G / f"plu_{n}.npz")
+    assert np.array_equal(pos, f["pos"]) and np.array_equal(L, f["L"]) and np.array_equal(U, f["U"])
+
+
+@pytest.mark.parametrize("n", [257, 1000, 8192])
+def test_plu_digest(orc, n):
+    pos, L, U = orc.plu(host_fill_normal(n, n, 1))
+    assert np.array_equal(pos, np.load(G / f"plu_{n}_pos.npy"))
+    assert sha(L) == META[f"plu_{n}"]["sha256_L"] and sha(U) == META[f"plu_{n}"]["sha256_U"]
+
+
+@pytest.mark.parametrize("n,k", [(300, 4), (2048, 1)])
+def test_solve_digest(orc, n, k):
+    x = orc.solve(host_fill_normal(n, n, 1), host_fill_normal(n, k, 2))
+    assert sha(x) == META[f"solve_{n}_{k}"]["sha256"]
+
+
+def test_llt(orc):
+    assert np.array_equal(orc.llt(spd(97, 1)), np.load(G / "llt_97.npz")["L"])
+    for n in (300, 8192):
+        assert sha(orc.llt(spd(n, 1))) == META[f"llt_{n}"]["sha256"]
+
+
+def test_qr(orc):
+    q, r = orc.qr(host_fill_normal(60, 40, 7))
+    f = np.load(G / "qr_60x40.npz")
+    assert np.array_equal(q, f["Q"]) and np.array_equal(r, f["R"])
+    for m, n in ((300, 200), (1000, 500)):
+        q, r = orc.qr(host_fill_normal(m, n, 7))
+        assert sha(q) == META[f"qr_{m}x{n}"]["sha256_Q"] and sha(r) == META[f"qr_{m}x{n}"]["sha256_R"]
+
+
+def test_det(orc):
+    d = orc.det(host_fill_normal(150, 150, 5))
+    assert d == META["det_150"]["value"]
+
+
+@pytest.mark.skipif(reference() is None, reason="reference tree not present (GPU host)")
+@pytest.mark.parametrize("m,n", [(7, 7), (91, 91), (130, 61), (500, 500)])
+def test_restatement_equals_reference_build(orc, m, n):
+    """Where the reference compiles (this container), compare on extra shapes."""
+    ref = reference()
+    a = host_fill_normal(m, n, 11)
+    p1, l1, u1 = orc.plu(a)
+    p2, l2, u2 = ref.plu(a)
+    assert np.array_equal(p1, p2) and np.array_equal(l1, l2) and np.array_equal(u1, u2)
+    q1, r1 = orc.qr(a)
+    q2, r2 = ref.qr(a)
+    assert np.array_equal(q1, q2) and np.array_equal(r1, r2)
+    if m == n:
+        s = spd(n, 12)
+        assert np.array_equal(orc.llt(s), ref.llt(s))
+        b = host_fill_normal(n, 3, 13)
+        assert np.array_equal(orc.solve(a, b), ref.solve(a, b))
