@@ -40,9 +40,14 @@ def sketch(a: np.ndarray, seed: int = 99) -> list:
     return (om.T @ a @ ps).tolist()
 
 
-def spd(n: int, seed: int) -> np.ndarray:
+def spd(ref, n: int, seed: int) -> np.ndarray:
+    """S = G G^T / n + I, G iid N(0,1), formed with the reference's own operator*
+    (a fused chain per element) and one rounded multiplication by 1/n: the same
+    bits on every host and as mg_gen_spd_gram on the GPU."""
     g = host_fill_normal(n, n, seed)
-    return np.asfortranarray(g @ g.T / n + np.eye(n))
+    s = ref.dgemm(g, np.asfortranarray(g.T)) * (1.0 / n)
+    s[np.diag_indices(n)] += 1.0
+    return np.asfortranarray(s)
 
 
 def main():
@@ -77,9 +82,9 @@ def main():
         meta["cases"][f"solve_{n}_{k}"] = {"sha256": sha(x), "x0": x[:4, 0].tolist()}
 
     # LLT: S = G G^T / n + I
-    np.savez_compressed(OUT / "llt_97.npz", L=ref.llt(spd(97, 1)))
+    np.savez_compressed(OUT / "llt_97.npz", L=ref.llt(spd(ref, 97, 1)))
     for n in (300, 8192):
-        L = ref.llt(spd(n, 1))
+        L = ref.llt(spd(ref, n, 1))
         meta["cases"][f"llt_{n}"] = {"sha256": sha(L), "sketch": sketch(L)}
 
     # QR (Householder): unblocked path in full, blocked path by digest

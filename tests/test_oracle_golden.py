@@ -21,8 +21,11 @@ def sha(a):
 
 
 def spd(n, seed):
+    """The golden script's S = G G^T / n + I (fused-chain product, then 1/n)."""
     g = host_fill_normal(n, n, seed)
-    return np.asfortranarray(g @ g.T / n + np.eye(n))
+    s = restatement().dgemm(g, np.asfortranarray(g.T)) * (1.0 / n)
+    s[np.diag_indices(n)] += 1.0
+    return np.asfortranarray(s)
 
 
 @pytest.fixture(scope="module")
