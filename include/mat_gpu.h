@@ -116,6 +116,21 @@ mg_status_t mg_dgemm(mg_handle_t h, int transA, int transB, int m, int n, int k,
  * has no such report and stops that panel instead.  Synchronises. */
 mg_status_t mg_dgetrf(mg_handle_t h, int m, int n, double* A, int lda, int* pos, int* info);
 
+/* mg_dgetrf without any allocation (no counterpart in Mat, whose calls each
+ * allocate their packing buffers): for callers that cannot allocate device
+ * memory when they factor, e.g. code running inside another system's memory
+ * pool or fixed budget, or callers that must not synchronise the device the
+ * way cudaMalloc/cudaFree do.  No handle: work goes on `cuda_stream` (NULL =
+ * legacy default stream); the caller passes A and pos.  Scratch is one
+ * file-scope device array of about 400 KiB per device, shared by every call:
+ * calls that overlap on the GPU (other streams, other threads) race on it and
+ * must be serialised by the caller.  Its address is looked up on the first
+ * call on each device, so make that first call before any stream capture.
+ * Limits: m <= 65536 rows and devices with at most 256 SMs, else
+ * MG_ERR_UNSUPPORTED.  Same results, statuses and synchronisation as
+ * mg_dgetrf. */
+mg_status_t mg_dgetrf_noalloc(void* cuda_stream, int m, int n, double* A, int lda, int* pos, int* info);
+
 /* X := A^{-1} B from mg_dgetrf's factors and pos (n x n), B and X distinct.
  * Substitution order of Mat's narrow solve (Solve_direct_narrow,
  * Mat-8.3.1/LU/__Solve_direct.h:112-139) for every right-hand side. */

@@ -431,10 +431,9 @@ namespace mg {
 // Workspace carve-up for one getrf call (device): barrier/err/info words,
 // piv[PANEL_MAX_NB], exchange buffers sized for num_sms CTAs.
 template <typename T>
-static size_t getrf_ws_bytes(int num_sms) {
-    const size_t P = (size_t)num_sms;
-    return 256 + 4 * PANEL_MAX_NB + 2 * P * sizeof(T) + 2 * P * sizeof(int) + 2 * P * PANEL_MAX_NB * sizeof(T) +
-           2 * PANEL_MAX_NB * sizeof(T) + 1024;
+static constexpr size_t getrf_ws_bytes(int num_sms, int nbmax = PANEL_MAX_NB) {
+    return 256 + 4 * (size_t)nbmax + 2 * (size_t)num_sms * sizeof(T) + 2 * (size_t)num_sms * sizeof(int) +
+           2 * (size_t)num_sms * nbmax * sizeof(T) + 2 * (size_t)nbmax * sizeof(T) + 1024;
 }
 
 template <typename T>
@@ -445,7 +444,7 @@ struct GetrfCtx {
 };
 
 template <typename T>
-static GetrfCtx<T> carve(void* base, int num_sms) {
+static GetrfCtx<T> carve(void* base, int num_sms, int nbmax = PANEL_MAX_NB) {
     char* p = (char*)base;
     GetrfCtx<T> c;
     c.ws.bar = (unsigned*)p;
@@ -453,13 +452,13 @@ static GetrfCtx<T> carve(void* base, int num_sms) {
     c.ws.info = (int*)(p + 128);
     p += 256;
     c.piv = (int*)p;
-    p += align_up(4 * PANEL_MAX_NB, 256);
+    p += align_up(4 * (size_t)nbmax, 256);
     c.x.cand_val = (T*)p;
     p += align_up(2 * (size_t)num_sms * sizeof(T), 256);
     c.x.cand_row = (int*)p;
     p += align_up(2 * (size_t)num_sms * sizeof(int), 256);
     c.x.cand_rows = (T*)p;
-    p += align_up(2 * (size_t)num_sms * PANEL_MAX_NB * sizeof(T), 256);
+    p += align_up(2 * (size_t)num_sms * nbmax * sizeof(T), 256);
     c.x.diag_row = (T*)p;
     return c;
 }
@@ -523,15 +522,13 @@ static mg_status_t launch_trsm_llnu(mg_handle_t h, int k, int n, const T* L, int
     return post_launch(h, "trsm_llnu_kernel");
 }
 
-// In-place PLU; pos (device, m ints) receives Mat's permutation.  Returns
-// MG_OK, MG_SINGULAR (info = first zero-pivot column, 1-based) or an error.
-mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* pos, int* info_out) {
+// In-place PLU given an exchange area `c` (no allocation); hstat receives the
+// error and info words (two host ints).  Returns MG_OK, MG_SINGULAR (info =
+// first zero-pivot column, 1-based) or an error.
+static mg_status_t dgetrf_run(mg_handle_t h, int m, int n, double* A, int lda, int* pos, GetrfCtx<double>& c,
+                              int* hstat, int* info_out) {
     if (info_out) *info_out = 0;
-    if (m == 0 || n == 0) return MG_OK;
-    MG_TRY(ensure_ws(h, getrf_ws_bytes<double>(h->num_sms)));
-    MG_TRY(ensure_hws(h, 64));
-    GetrfCtx<double> c = carve<double>(h->ws, h->num_sms);
-    MG_CHECK_CUDA(h, cudaMemsetAsync(h->ws, 0, 256, h->stream));
+    MG_CHECK_CUDA(h, cudaMemsetAsync(c.ws.bar, 0, 256, h->stream));  // barrier, error and info words
     iota_kernel<<<(m + 255) / 256, 256, 0, h->stream>>>(pos, m);
     MG_TRY(post_launch(h, "iota_kernel"));
 
@@ -563,14 +560,23 @@ mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* po
             MG_TRY(launch_laswp<double>(h, A, lda, r, rem, c.piv, r, n, n));
         }
     }
-    int* hw = (int*)h->hws;
-    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, c.ws.err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw + 1, c.ws.info, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hstat, c.ws.err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hstat + 1, c.ws.info, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
-    if (hw[0]) return fail(h, MG_TIMEOUT, "dgetrf: a panel grid barrier timed out");
-    if (info_out) *info_out = hw[1];
-    if (hw[1]) return fail(h, MG_SINGULAR, "dgetrf: exactly zero pivot column %d", hw[1]);
+    if (hstat[0]) return fail(h, MG_TIMEOUT, "dgetrf: a panel grid barrier timed out");
+    if (info_out) *info_out = hstat[1];
+    if (hstat[1]) return fail(h, MG_SINGULAR, "dgetrf: exactly zero pivot column %d", hstat[1]);
     return MG_OK;
+}
+
+// In-place PLU; pos (device, m ints) receives Mat's permutation.
+mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* pos, int* info_out) {
+    if (info_out) *info_out = 0;
+    if (m == 0 || n == 0) return MG_OK;
+    MG_TRY(ensure_ws(h, getrf_ws_bytes<double>(h->num_sms)));
+    MG_TRY(ensure_hws(h, 64));
+    GetrfCtx<double> c = carve<double>(h->ws, h->num_sms);
+    return dgetrf_run(h, m, n, A, lda, pos, c, (int*)h->hws, info_out);
 }
 
 // ----------------------------------------------------------- mixed (fp32)
@@ -684,6 +690,42 @@ mg_status_t dgetrs_impl(mg_handle_t h, int n, int nrhs, const double* LU, int ld
     return MG_OK;
 }
 
+// ------------------------------------------------ allocation-free variant
+// Some callers of this LU cannot allocate device memory at call time: code
+// that runs inside another system's memory pool or under a fixed memory
+// budget (an engine embedding the solver next to its own allocator), callers
+// that must not stall the whole device (cudaMalloc / cudaFree synchronise
+// it, and the handle's workspace grows through them), and plugin hosts that
+// forbid device allocation outright.  mg_dgetrf_noalloc serves them: its
+// panel exchange area, pivot list, barrier counter and status words live in
+// one file-scope device array of fixed size, shared by every call in the
+// process on that device.
+constexpr int kNoAllocMaxSms = 256;      // exchange slots for up to this many panel CTAs
+constexpr int kNoAllocMaxNb = 96;        // widest panel of the FP64 PLU (blocks of 60; <= 90 unblocked)
+constexpr int kNoAllocMaxRows = 65536;   // rows whose panel slab fits the SMs' shared memory
+constexpr size_t kNoAllocScratchBytes = getrf_ws_bytes<double>(kNoAllocMaxSms, kNoAllocMaxNb);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[64] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device (looked up once per device).
+cudaError_t noalloc_scratch(int dev, void** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return cudaSuccess;
+}
+}  // namespace
+
 }  // namespace mg
 
 extern "C" {
@@ -693,6 +735,27 @@ mg_status_t mg_dgetrf(mg_handle_t h, int m, int n, double* A, int lda, int* pos,
     if (m < 0 || n < 0 || lda < (m > 1 ? m : 1) || ((size_t)m * n && (!A || !pos)))
         return mg::fail(h, MG_ERR_ARG, "mg_dgetrf: bad arguments (m=%d n=%d lda=%d)", m, n, lda);
     return mg::dgetrf_impl(h, m, n, A, lda, pos, info);
+}
+
+mg_status_t mg_dgetrf_noalloc(void* cuda_stream, int m, int n, double* A, int lda, int* pos, int* info) {
+    if (info) *info = 0;
+    if (m < 0 || n < 0 || lda < (m > 1 ? m : 1) || ((size_t)m * n && (!A || !pos))) return MG_ERR_ARG;
+    if (m > mg::kNoAllocMaxRows) return MG_ERR_UNSUPPORTED;  // beyond the fixed scratch / panel capacity
+    if (m == 0 || n == 0) return MG_OK;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MG_ERR_CUDA;
+    void* scratch = nullptr;
+    if (mg::noalloc_scratch(dev, &scratch) != cudaSuccess) return MG_ERR_CUDA;
+    mg_handle_s h;  // a handle on the stack: no workspace, no pinned memory
+    h.stream = (cudaStream_t)cuda_stream;
+    h.device = dev;
+    if (cudaDeviceGetAttribute(&h.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&h.max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        return MG_ERR_CUDA;
+    if (h.num_sms > mg::kNoAllocMaxSms) return MG_ERR_UNSUPPORTED;
+    mg::GetrfCtx<double> c = mg::carve<double>(scratch, h.num_sms, mg::kNoAllocMaxNb);
+    int hstat[2] = {0, 0};
+    return mg::dgetrf_run(&h, m, n, A, lda, pos, c, hstat, info);
 }
 
 mg_status_t mg_dgetrs(mg_handle_t h, int n, int nrhs, const double* LU, int lda, const int* pos, const double* B,
