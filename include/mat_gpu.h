@@ -190,6 +190,24 @@ typedef struct mg_ir_report {
 mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
                          int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* report);
 
+/* ----------------------------------------------- FP32 LU (mixed solve)
+ * The single-precision factorizations inside mg_dsgesv_ir, exposed for
+ * callers that refine on their own.  No counterpart in Mat (no mixed
+ * precision there); the pivoting and the pos convention are those of Mat's
+ * PLU (Mat-8.3.1/LU/__PLU.h:54-90: first row of the largest |a|, pos
+ * starts as 0..m-1 and records each interchange, A(pos[i],:) = (LU)(i,:)).
+ * An exactly zero pivot column is left unscaled and reported in info
+ * (1-based, first such column); the call then returns MG_SINGULAR.
+ *
+ * mg_sgetf2: in-place unblocked panel LU of an m x n block, n <= 128 (the
+ * panel of the mixed LU: one 16-CTA thread-block cluster for m <= 16384,
+ * a cooperative grid beyond).  Synchronises. */
+mg_status_t mg_sgetf2(mg_handle_t h, int m, int n, float* A, int lda, int* pos, int* info);
+/* mg_sgetrf: in-place blocked LU of an n x n fp32 matrix (blocks of 128:
+ * mg_sgetf2 panels, block-row solve and trailing update on the split-BF16
+ * tensor-core GEMM with 3 terms, fp32 accumulation).  Synchronises. */
+mg_status_t mg_sgetrf(mg_handle_t h, int n, float* A, int lda, int* pos, int* info);
+
 /* ------------------------------------------------ benchmark input generators
  * A = Q1 diag(sigma) Q2 with Q1, Q2 products of `nrefl` Householder
  * reflectors whose vectors are iid N(0,1) (seeded), sigma geometric from 1

@@ -57,6 +57,8 @@ SIGNATURES: dict[str, tuple] = {
     "mg_measure_fp64_peaks": (i32, [vp, pf64, pf64]),
     "mg_dgetrf": (i32, [vp, i32, i32, vp, i32, vp, pi32]),
     "mg_dgetrf_noalloc": (i32, [vp, i32, i32, vp, i32, vp, pi32]),
+    "mg_sgetf2": (i32, [vp, i32, i32, vp, i32, vp, pi32]),
+    "mg_sgetrf": (i32, [vp, i32, vp, i32, vp, pi32]),
     "mg_dgetrs": (i32, [vp, i32, i32, vp, i32, vp, vp, i32, vp, i32]),
     "mg_dgesv": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, pi32]),
     "mg_sgemm_bf16x": (i32, [vp, i32, i32, i32, i32, f32, vp, i32, vp, i32, f32, vp, i32]),

@@ -155,6 +155,28 @@ class Handle:
         return X, info.value
 
     # ----------------------------------------------------------------- mixed
+    def sgetf2(self, A: torch.Tensor, pos: torch.Tensor | None = None):
+        """In-place fp32 panel LU of A (m x n, n <= 128, column-major). Returns (pos, info)."""
+        m, n = A.shape
+        if pos is None:
+            pos = torch.empty(m, dtype=torch.int32, device=A.device)
+        info = C.c_int(0)
+        st = self.lib.mg_sgetf2(self.h, m, n, _ptr(A), ld_of(A), _ptr(pos), C.byref(info))
+        if st not in (0, 4):
+            self.check(st, "mg_sgetf2")
+        return pos, info.value
+
+    def sgetrf(self, A: torch.Tensor, pos: torch.Tensor | None = None):
+        """In-place fp32 blocked LU of A (n x n, column-major) as in the mixed solve. Returns (pos, info)."""
+        n = A.shape[0]
+        if pos is None:
+            pos = torch.empty(n, dtype=torch.int32, device=A.device)
+        info = C.c_int(0)
+        st = self.lib.mg_sgetrf(self.h, n, _ptr(A), ld_of(A), _ptr(pos), C.byref(info))
+        if st not in (0, 4):
+            self.check(st, "mg_sgetrf")
+        return pos, info.value
+
     def dsgesv_ir(self, A, B, X=None, tol=1e-14, max_iter=30, nterms=3, fallback=True):
         """Mixed LU (fp32 + split-BF16) + FP64 refinement. Returns (X, report dict, status)."""
         n = A.shape[0]

@@ -586,6 +586,17 @@ size_t sgetrf_tri_bytes(int nb, int nterms) {
     return align_up((size_t)nb * nb * sizeof(float), 1024) + bf16x_split_bytes(nb, nb, nterms);
 }
 
+// FP32 panel: one 16-CTA cluster (panel_f32.cu) when the panel is too tall
+// for one CTA's shared memory and fits the cluster; else the cooperative grid
+// (or, for short panels, the single-CTA) kernel.  Same factors either way.
+static mg_status_t launch_panel_f32(mg_handle_t h, GetrfCtx<float>& c, float* A, int lda, int m, int r0, int w,
+                                    int* pos) {
+    const int R = m - r0;
+    if ((size_t)R * w * sizeof(float) > 64 * 1024 && R >= w && R <= panel_cluster_rows(h))
+        return sgetf2_cluster(h, A, lda, m, r0, w, pos, c.piv, c.ws.info);
+    return launch_panel<float>(h, c, A, lda, m, r0, w, pos);
+}
+
 // FP32 blocked right-looking LU with partial pivoting for the mixed solve:
 // fp32 panels (the same cooperative panel kernel), fp32 TRSM on the block
 // row, and the trailing update A22 -= L21*U12 on the BF16 tensor cores with
@@ -610,7 +621,7 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_unit_lower_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism));
     for (int r = 0; r < n; r += nb) {
         const int w = nb < n - r ? nb : n - r;
-        MG_TRY(launch_panel<float>(h, c, A, lda, n, r, w, pos));
+        MG_TRY(launch_panel_f32(h, c, A, lda, n, r, w, pos));
         MG_TRY(launch_laswp<float>(h, A, lda, r, w, c.piv, r, r + w, n));
         // inverse of the unit-lower diagonal block (kept with ld nb in Linv_all when requested)
         float* Lout = Linv_all ? Linv_all + (size_t)(r / nb) * nb * nb : (float*)tri;
@@ -735,6 +746,58 @@ mg_status_t mg_dgetrf(mg_handle_t h, int m, int n, double* A, int lda, int* pos,
     if (m < 0 || n < 0 || lda < (m > 1 ? m : 1) || ((size_t)m * n && (!A || !pos)))
         return mg::fail(h, MG_ERR_ARG, "mg_dgetrf: bad arguments (m=%d n=%d lda=%d)", m, n, lda);
     return mg::dgetrf_impl(h, m, n, A, lda, pos, info);
+}
+
+mg_status_t mg_sgetf2(mg_handle_t h, int m, int n, float* A, int lda, int* pos, int* info) {
+    if (info) *info = 0;
+    if (!h) return MG_ERR_ARG;
+    if (m < 0 || n < 0 || n > 128 || lda < (m > 1 ? m : 1) || ((size_t)m * n && (!A || !pos)))
+        return mg::fail(h, MG_ERR_ARG, "mg_sgetf2: bad arguments (m=%d n=%d lda=%d, n must be <= 128)", m, n, lda);
+    if (m == 0 || n == 0) return MG_OK;
+    const int w = n < m ? n : m;
+    MG_TRY(mg::ensure_ws(h, mg::getrf_ws_bytes<float>(h->num_sms)));
+    MG_TRY(mg::ensure_hws(h, 64));
+    mg::GetrfCtx<float> c = mg::carve<float>(h->ws, h->num_sms);
+    MG_CHECK_CUDA(h, cudaMemsetAsync(c.ws.bar, 0, 256, h->stream));
+    iota_kernel<<<(m + 255) / 256, 256, 0, h->stream>>>(pos, m);
+    MG_TRY(mg::post_launch(h, "iota_kernel"));
+    MG_TRY(mg::launch_panel_f32(h, c, A, lda, m, 0, w, pos));
+    if (w < n) {  // columns right of a short panel (m < n): interchanges only
+        MG_TRY(mg::launch_laswp<float>(h, A, lda, 0, w, c.piv, 0, w, n));
+    }
+    int* hw = (int*)h->hws;
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, c.ws.err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw + 1, c.ws.info, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (hw[0]) return mg::fail(h, MG_TIMEOUT, "mg_sgetf2: a panel grid barrier timed out");
+    if (info) *info = hw[1];
+    if (hw[1]) return mg::fail(h, MG_SINGULAR, "mg_sgetf2: exactly zero pivot column %d", hw[1]);
+    return MG_OK;
+}
+
+mg_status_t mg_sgetrf(mg_handle_t h, int n, float* A, int lda, int* pos, int* info) {
+    if (info) *info = 0;
+    if (!h) return MG_ERR_ARG;
+    if (n < 0 || lda < (n > 1 ? n : 1) || (n && (!A || !pos)))
+        return mg::fail(h, MG_ERR_ARG, "mg_sgetrf: bad arguments (n=%d lda=%d)", n, lda);
+    if (n == 0) return MG_OK;
+    constexpr int nb = 128, nterms = 3;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = mg::align_up(off + bytes, 1024);
+        return o;
+    };
+    const size_t oX = take(mg::sgetrf_xchg_bytes(h->num_sms));
+    const size_t oSA = take(mg::bf16x_split_bytes(n, nb, nterms));
+    const size_t oSB = take(mg::bf16x_split_bytes(n, nb, nterms));
+    const size_t oT = take(mg::sgetrf_tri_bytes(nb, nterms));
+    const size_t oE = take(64);
+    MG_TRY(mg::ensure_ws(h, off));
+    char* b = (char*)h->ws;
+    int* gerr = (int*)(b + oE);
+    MG_CHECK_CUDA(h, cudaMemsetAsync(gerr, 0, 64, h->stream));
+    return mg::sgetrf_mixed(h, n, A, lda, pos, nb, nterms, b + oX, b + oSA, b + oSB, b + oT, nullptr, gerr, info);
 }
 
 mg_status_t mg_dgetrf_noalloc(void* cuda_stream, int m, int n, double* A, int lda, int* pos, int* info) {

@@ -26,6 +26,8 @@ struct mg_handle_s {
     void* hws = nullptr;
     size_t hws_bytes = 0;
     uint64_t launches = 0;
+    // Cluster size of the FP32 cluster panel (0: not probed yet, -1: unavailable).
+    int panel_cluster = 0;
     char last_error[512] = {0};
     // Optional per-phase timing with CUDA events on the handle's stream.
     struct ProfRec {
@@ -100,6 +102,11 @@ mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, floa
                                 const void* Bsplit, float beta, float* C, int ldc, int* err);
 
 // FP32 LU with split-BF16 trailing updates (lu.cu).
+// FP32 panel on one thread-block cluster (panel_f32.cu): rows it can take
+// (0 if unavailable), and the launch (piv relative to r0; pos updated).
+int panel_cluster_rows(mg_handle_t h);
+mg_status_t sgetf2_cluster(mg_handle_t h, float* A, int lda, int m, int r0, int w, int* pos, int* piv, int* info);
+
 size_t sgetrf_xchg_bytes(int num_sms);
 size_t sgetrf_tri_bytes(int nb, int nterms);
 mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int nb, int nterms, void* xchg,

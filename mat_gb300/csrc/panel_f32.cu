@@ -1,0 +1,471 @@
+// FP32 panel factorization (getf2: partial pivoting, first index of the
+// largest |a|, reciprocal scaling, fused rank-1 updates) on ONE thread-block
+// cluster, for the mixed-precision LU.
+//
+// Why a cluster: a panel column needs one all-CTA agreement on the pivot.
+// Through global memory (a grid barrier over ~128 CTAs) that costs several
+// L2 round trips per column, ~4.5 us; inside a cluster it is one hardware
+// cluster barrier plus one distributed-shared-memory read, well under 1 us.
+// A 16-CTA cluster cannot hold a 16384 x 128 FP32 panel (8 MiB) on chip, so
+// the panel is factored in sub-panels of 32 columns kept in registers
+// (each of the 256 threads of a CTA owns RPT <= 4 rows x 32 columns):
+//
+//   for each sub-panel S = [cs0, cs0+32):
+//     1. load my rows of S into registers
+//     2. for each column c of S: local max |a| -> publish (value, row,
+//        row data, and the diagonal row) in my shared memory -> cluster
+//        barrier -> read every CTA's candidate and row (DSMEM), choose the
+//        same winner in every CTA -> swap in registers -> scale by the
+//        reciprocal -> fused rank-1 update of my rows' remaining columns
+//     3. store S; apply S's interchanges to the panel's other columns and to
+//        pos (one gather/scatter over the touched rows, net permutation kept
+//        in a shared-memory map)
+//     4. U(S, right) = L11^{-1} A(S, right) (32 x 32 unit lower, every CTA
+//        redundantly), then A(below, right) -= L(below, S) U(S, right) for my
+//        rows, with L(below, S) still in registers.
+//
+// Every element sees the same fused operations in the same order as the
+// column-at-a-time panel (the multiplier l = a * (1/p), then a := fma(l, -u,
+// a) for the pivot columns in increasing order), so the factors are bitwise
+// those of the one-column-per-barrier cooperative panel.  Pivot rows are
+// identical as well (same comparisons on the same values).
+//
+// Only hardware cluster barriers are used: no spin-wait on memory, nothing
+// that can time out.  Double-buffered publication slots (by column parity)
+// need one barrier per column: a CTA overwrites a slot two columns later,
+// after every reader has passed the barrier of the column in between.
+#include <cooperative_groups.h>
+
+#include <climits>
+
+#include "mg_internal.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace {
+
+constexpr int CP_THREADS = 256;
+constexpr int CP_CS = 16;         // CTAs per cluster (non-portable size)
+constexpr int CP_MAX_RPT = 4;     // rows per thread
+constexpr int CP_SW = 32;       // sub-panel width (columns in registers)
+constexpr int CP_MAXW = 128;    // widest panel
+constexpr int CP_NOTHER = CP_MAXW - CP_SW;
+constexpr int CP_UB_LD = CP_SW + 4;  // padded row of ub (16-byte multiple)
+constexpr int CP_GCOLS = 12;         // columns per gather pass (>= 96 / 8)
+
+struct CpShared {
+    float ub[CP_NOTHER][CP_UB_LD];  // U(S, right), [column][row of S]
+    float l11[CP_SW][CP_SW + 1];
+    float pubrow[2][CP_SW];
+    float pubdiag[2][CP_SW];
+    float cand_val[2];
+    int cand_pos[2];
+    float prow[CP_SW];
+    float drow[CP_SW];
+    float red_v[CP_THREADS / 32];
+    int red_p[CP_THREADS / 32];
+    int piv[CP_MAXW];
+    int touch[2 * CP_SW];
+    float gbuf[CP_GCOLS * 2 * CP_SW];
+    int gpos[2 * CP_SW];
+    int s_bpos, s_win;
+    float s_pv;
+};
+
+__device__ __forceinline__ void cp_better(float& v, int& p, int& q, float ov, int op, int oq) {
+    if (ov > v || (ov == v && op < p)) {
+        v = ov;
+        p = op;
+        q = oq;
+    }
+}
+
+template <int RPT>
+__global__ void __launch_bounds__(CP_THREADS, 1)
+    panel_cluster_kernel(float* __restrict__ A, int lda, int m, int r0, int w, int* __restrict__ pos,
+                         int* __restrict__ piv_out, int* __restrict__ info) {
+    constexpr int CS = CP_CS;
+    constexpr int RPC = RPT * CP_THREADS;  // positions per CTA
+    extern __shared__ __align__(16) float dyn[];
+    float* const tile = dyn;                              // [32][RPC]: my rows of the sub-panel
+    int* const map = reinterpret_cast<int*>(dyn + CP_SW * RPC);  // map[p], p in [0, R): the row (at
+                                                          // sub-panel start) now at position p
+    __shared__ __align__(16) CpShared sh;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int q = (int)cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int R = m - r0;
+    const int row0 = q * RPC;
+    float* const P0 = A + (size_t)r0 + (size_t)r0 * lda;  // panel origin
+
+    for (int p = tid; p < R; p += CP_THREADS) map[p] = p;
+
+    float v[RPT][CP_SW];
+    const int nsub = (w + CP_SW - 1) / CP_SW;
+    for (int s = 0; s < nsub; ++s) {
+        const int cs0 = s * CP_SW;
+        const int sw = min(CP_SW, w - cs0);
+        __syncthreads();
+        // my rows of S -> registers, through the shared tile (coalesced columns)
+#pragma unroll 8
+        for (int e = tid; e < CP_SW * RPC; e += CP_THREADS) {
+            const int j = e / RPC, i = e - j * RPC, p = row0 + i;
+            tile[e] = (p < R && j < sw) ? P0[(size_t)(cs0 + j) * lda + p] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < RPT; ++k)
+#pragma unroll
+            for (int j = 0; j < CP_SW; ++j) v[k][j] = tile[j * RPC + k * CP_THREADS + tid];
+
+#pragma unroll
+        for (int c = 0; c < CP_SW; ++c) {
+            if (c < sw) {
+            const int cabs = cs0 + c;
+            const int buf = cabs & 1;
+            // 1. this CTA's candidate
+            float best = -1.f;
+            int bpos = INT_MAX, dummy = 0;
+#pragma unroll
+            for (int k = 0; k < RPT; ++k) {
+                const int p = row0 + k * CP_THREADS + tid;
+                if (p < R && p >= cabs) cp_better(best, bpos, dummy, fabsf(v[k][c]), p, 0);
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const float ov = __shfl_down_sync(0xffffffffu, best, off);
+                const int op = __shfl_down_sync(0xffffffffu, bpos, off);
+                cp_better(best, bpos, dummy, ov, op, 0);
+            }
+            if (lane == 0) {
+                sh.red_v[warp] = best;
+                sh.red_p[warp] = bpos;
+            }
+            __syncthreads();
+            if (warp == 0) {
+                best = lane < CP_THREADS / 32 ? sh.red_v[lane] : -1.f;
+                bpos = lane < CP_THREADS / 32 ? sh.red_p[lane] : INT_MAX;
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    const float ov = __shfl_down_sync(0xffffffffu, best, off);
+                    const int op = __shfl_down_sync(0xffffffffu, bpos, off);
+                    cp_better(best, bpos, dummy, ov, op, 0);
+                }
+                if (lane == 0) {
+                    sh.cand_val[buf] = best;
+                    sh.cand_pos[buf] = bpos;
+                    sh.s_bpos = bpos;
+                }
+            }
+            __syncthreads();
+            // 2. publish the candidate row and (by its owner) the diagonal row
+            {
+                const int bp = sh.s_bpos;
+#pragma unroll
+                for (int k = 0; k < RPT; ++k) {
+                    const int p = row0 + k * CP_THREADS + tid;
+                    if (p == bp) {
+#pragma unroll
+                        for (int j = 0; j < CP_SW; ++j) sh.pubrow[buf][j] = v[k][j];
+                    }
+                    if (p == cabs) {
+#pragma unroll
+                        for (int j = 0; j < CP_SW; ++j) sh.pubdiag[buf][j] = v[k][j];
+                    }
+                }
+            }
+            cluster.sync();
+            // 3. every CTA reads all candidates and rows and picks the same winner
+            if (warp == 0) {
+                float cv = -1.f;
+                int cpos = INT_MAX, cq = CS;
+                if (lane < CS) {
+                    cv = *cluster.map_shared_rank(&sh.cand_val[buf], lane);
+                    cpos = *cluster.map_shared_rank(&sh.cand_pos[buf], lane);
+                    cq = lane;
+                }
+                float rv[CS];
+#pragma unroll
+                for (int r = 0; r < CS; ++r) rv[r] = *cluster.map_shared_rank(&sh.pubrow[buf][lane], r);
+                const float dv = *cluster.map_shared_rank(&sh.pubdiag[buf][lane], cabs / RPC);
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    const float ov = __shfl_xor_sync(0xffffffffu, cv, off);
+                    const int op = __shfl_xor_sync(0xffffffffu, cpos, off);
+                    const int oq = __shfl_xor_sync(0xffffffffu, cq, off);
+                    cp_better(cv, cpos, cq, ov, op, oq);
+                }
+                float pr = 0.f;
+#pragma unroll
+                for (int r = 0; r < CS; ++r)
+                    if (r == cq) pr = rv[r];
+                sh.prow[lane] = pr;
+                sh.drow[lane] = dv;
+                if (lane == 0) {
+                    const bool ok = cv > 0.f;
+                    sh.s_win = cpos;
+                    sh.s_pv = cv;
+                    sh.piv[cabs] = ok ? cpos : cabs;
+                    sh.touch[2 * c] = cabs;
+                    sh.touch[2 * c + 1] = ok ? cpos : cabs;
+                    if (ok && cpos != cabs) {
+                        const int t = map[cabs];
+                        map[cabs] = map[cpos];
+                        map[cpos] = t;
+                    }
+                    if (!ok && q == 0) atomicCAS(info, 0, r0 + cabs + 1);
+                }
+            }
+            __syncthreads();
+            // 4. interchange, scale, update (exactly zero column: nothing, as LAPACK)
+            const float pv = sh.s_pv;
+            if (pv > 0.f) {
+                const int win = sh.s_win;
+                if (win != cabs) {
+#pragma unroll
+                    for (int k = 0; k < RPT; ++k) {
+                        const int p = row0 + k * CP_THREADS + tid;
+                        if (p == cabs) {
+#pragma unroll
+                            for (int j = 0; j < CP_SW; ++j) v[k][j] = sh.prow[j];
+                        } else if (p == win) {
+#pragma unroll
+                            for (int j = 0; j < CP_SW; ++j) v[k][j] = sh.drow[j];
+                        }
+                    }
+                }
+                const float inv = 1.f / sh.prow[c];
+                bool act[RPT];
+#pragma unroll
+                for (int k = 0; k < RPT; ++k) {
+                    const int p = row0 + k * CP_THREADS + tid;
+                    act[k] = p < R && p > cabs;
+                    if (act[k]) v[k][c] = v[k][c] * inv;
+                }
+#pragma unroll
+                for (int j = c + 1; j < CP_SW; ++j) {
+                    const float u = sh.prow[j];
+#pragma unroll
+                    for (int k = 0; k < RPT; ++k)
+                        if (act[k]) v[k][j] = fmaf(v[k][c], -u, v[k][j]);
+                }
+            }
+            }
+        }
+
+        // store my rows of the sub-panel (through the tile)
+#pragma unroll
+        for (int k = 0; k < RPT; ++k)
+#pragma unroll
+            for (int j = 0; j < CP_SW; ++j) tile[j * RPC + k * CP_THREADS + tid] = v[k][j];
+        __syncthreads();
+#pragma unroll 8
+        for (int e = tid; e < CP_SW * RPC; e += CP_THREADS) {
+            const int j = e / RPC, i = e - j * RPC, p = row0 + i;
+            if (p < R && j < sw) P0[(size_t)(cs0 + j) * lda + p] = tile[e];
+        }
+        __syncthreads();  // map, touch list final for this sub-panel
+
+        // 5. this sub-panel's interchanges on the panel's other columns
+        //    (columns are dealt to the CTAs round-robin) and on pos (CTA 0)
+        const int nt = 2 * sw;
+        const int nother = w - sw;
+        const int nmine = q < nother ? (nother - q + CS - 1) / CS : 0;
+        for (int g0 = 0; g0 < nmine; g0 += CP_GCOLS) {
+            const int gc = min(CP_GCOLS, nmine - g0);
+            for (int e = tid; e < gc * nt; e += CP_THREADS) {
+                const int jj = q + (g0 + e / nt) * CS;
+                const int col = jj < cs0 ? jj : jj + sw;
+                const int t = e % nt;
+                sh.gbuf[e] = P0[(size_t)map[sh.touch[t]] + (size_t)col * lda];
+            }
+            if (q == 0 && g0 == 0 && tid < nt) sh.gpos[tid] = pos[r0 + map[sh.touch[tid]]];
+            __syncthreads();
+            for (int e = tid; e < gc * nt; e += CP_THREADS) {
+                const int jj = q + (g0 + e / nt) * CS;
+                const int col = jj < cs0 ? jj : jj + sw;
+                const int t = e % nt;
+                P0[(size_t)sh.touch[t] + (size_t)col * lda] = sh.gbuf[e];
+            }
+            if (q == 0 && g0 == 0 && tid < nt) pos[r0 + sh.touch[tid]] = sh.gpos[tid];
+            __syncthreads();
+        }
+        if (q == 0 && nmine == 0) {  // pos only (no other columns dealt to CTA 0)
+            if (tid < nt) sh.gpos[tid] = pos[r0 + map[sh.touch[tid]]];
+            __syncthreads();
+            if (tid < nt) pos[r0 + sh.touch[tid]] = sh.gpos[tid];
+        }
+        __syncthreads();
+        if (tid < nt) map[sh.touch[tid]] = sh.touch[tid];  // back to identity for the next sub-panel
+        cluster.sync();  // swapped columns visible to the cluster
+
+        const int nright = w - cs0 - CP_SW;
+        if (nright > 0) {
+            // 6. U(S, right) = L11^{-1} A(S, right), redundantly in every CTA
+            for (int e = tid; e < CP_SW * CP_SW; e += CP_THREADS) {
+                const int i = e % CP_SW, k = e / CP_SW;
+                sh.l11[i][k] = P0[(size_t)(cs0 + i) + (size_t)(cs0 + k) * lda];
+            }
+            for (int e = tid; e < CP_SW * nright; e += CP_THREADS) {
+                const int i = e % CP_SW, jj = e / CP_SW;
+                sh.ub[jj][i] = P0[(size_t)(cs0 + i) + (size_t)(cs0 + CP_SW + jj) * lda];
+            }
+            __syncthreads();
+            if (tid < nright) {
+                float x[CP_SW];
+#pragma unroll
+                for (int i = 0; i < CP_SW; ++i) x[i] = sh.ub[tid][i];
+#pragma unroll
+                for (int k = 0; k < CP_SW; ++k)
+#pragma unroll
+                    for (int i = k + 1; i < CP_SW; ++i) x[i] = fmaf(sh.l11[i][k], -x[k], x[i]);
+#pragma unroll
+                for (int i = 0; i < CP_SW; ++i) sh.ub[tid][i] = x[i];
+            }
+            __syncthreads();
+            cluster.sync();  // every CTA has read A(S, right) before CTA 0 overwrites it
+            if (q == 0)
+                for (int e = tid; e < CP_SW * nright; e += CP_THREADS) {
+                    const int i = e % CP_SW, jj = e / CP_SW;
+                    P0[(size_t)(cs0 + i) + (size_t)(cs0 + CP_SW + jj) * lda] = sh.ub[jj][i];
+                }
+            // 7. A(below, right) -= L(below, S) U(S, right) for my rows
+            bool act[RPT];
+#pragma unroll
+            for (int k = 0; k < RPT; ++k) {
+                const int p = row0 + k * CP_THREADS + tid;
+                act[k] = p < R && p >= cs0 + CP_SW;
+            }
+            // columns in groups of 4, the next group's loads in flight during this group's FMAs
+            constexpr int G = 4;
+            const size_t ld = (size_t)lda;
+            float* const C0 = P0 + (size_t)(cs0 + CP_SW) * ld;
+            float cur[G][RPT], nxt[G][RPT];
+#pragma unroll
+            for (int g = 0; g < G; ++g)
+#pragma unroll
+                for (int k = 0; k < RPT; ++k)
+                    cur[g][k] = (g < nright && act[k]) ? C0[(size_t)g * ld + row0 + k * CP_THREADS + tid] : 0.f;
+            for (int j0 = 0; j0 < nright; j0 += G) {
+#pragma unroll
+                for (int g = 0; g < G; ++g)
+#pragma unroll
+                    for (int k = 0; k < RPT; ++k) {
+                        const int jj = j0 + G + g;
+                        nxt[g][k] = (jj < nright && act[k]) ? C0[(size_t)jj * ld + row0 + k * CP_THREADS + tid] : 0.f;
+                    }
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    const int jj = j0 + g;
+                    if (jj < nright) {
+                        const float4* u4 = reinterpret_cast<const float4*>(&sh.ub[jj][0]);
+#pragma unroll
+                        for (int k4 = 0; k4 < CP_SW / 4; ++k4) {
+                            const float4 u = u4[k4];
+#pragma unroll
+                            for (int k = 0; k < RPT; ++k) {
+                                float a = cur[g][k];
+                                a = fmaf(v[k][4 * k4 + 0], -u.x, a);
+                                a = fmaf(v[k][4 * k4 + 1], -u.y, a);
+                                a = fmaf(v[k][4 * k4 + 2], -u.z, a);
+                                a = fmaf(v[k][4 * k4 + 3], -u.w, a);
+                                cur[g][k] = a;
+                            }
+                        }
+#pragma unroll
+                        for (int k = 0; k < RPT; ++k)
+                            if (act[k]) C0[(size_t)jj * ld + row0 + k * CP_THREADS + tid] = cur[g][k];
+                    }
+                }
+#pragma unroll
+                for (int g = 0; g < G; ++g)
+#pragma unroll
+                    for (int k = 0; k < RPT; ++k) cur[g][k] = nxt[g][k];
+            }
+        }
+    }
+    if (q == 0 && tid < w) piv_out[tid] = sh.piv[tid];
+    cluster.sync();  // no CTA leaves while another may still read its shared memory
+}
+
+cudaLaunchConfig_t cluster_cfg(cudaStream_t st, size_t smem, cudaLaunchAttribute* at) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(CP_CS);
+    cfg.blockDim = dim3(CP_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = CP_CS;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
+template <int RPT>
+cudaError_t launch_cluster(cudaStream_t st, size_t smem, float* A, int lda, int m, int r0, int w, int* pos,
+                           int* piv, int* info) {
+    cudaLaunchAttribute at[1];
+    cudaLaunchConfig_t cfg = cluster_cfg(st, smem, at);
+    return cudaLaunchKernelEx(&cfg, panel_cluster_kernel<RPT>, A, lda, m, r0, w, pos, piv, info);
+}
+
+// Sets the kernel's attributes and returns how many such clusters fit.
+template <int RPT>
+int prepare(size_t smem_max) {
+    auto k = panel_cluster_kernel<RPT>;
+    int n = 0;
+    cudaLaunchAttribute at[1];
+    cudaLaunchConfig_t cfg = cluster_cfg(nullptr, smem_max, at);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max) != cudaSuccess ||
+        cudaOccupancyMaxActiveClusters(&n, k, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+}  // namespace
+
+namespace mg {
+
+// Rows the cluster panel can take (0 if 16-CTA clusters of it do not fit
+// the device; probed once per handle).
+int panel_cluster_rows(mg_handle_t h) {
+    constexpr int kRows = CP_CS * CP_MAX_RPT * CP_THREADS;
+    if (h->panel_cluster == 0) {
+        const size_t smem_max = (size_t)CP_SW * CP_MAX_RPT * CP_THREADS * sizeof(float) + (size_t)kRows * sizeof(int);
+        const bool ok = prepare<1>(smem_max) > 0 && prepare<2>(smem_max) > 0 && prepare<3>(smem_max) > 0 &&
+                        prepare<4>(smem_max) > 0;
+        h->panel_cluster = ok ? CP_CS : -1;
+    }
+    return h->panel_cluster > 0 ? kRows : 0;
+}
+
+// FP32 panel of columns [r0, r0+w) over rows [r0, m) on one cluster; piv
+// (device, w ints) receives the pivot rows relative to r0; pos is updated;
+// info receives the first exactly-zero pivot column (1-based, atomicCAS on 0).
+// The caller checks panel_cluster_rows(h) >= m - r0 and w <= 128.
+mg_status_t sgetf2_cluster(mg_handle_t h, float* A, int lda, int m, int r0, int w, int* pos, int* piv,
+                           int* info) {
+    const int R = m - r0;
+    if (w <= 0 || w > CP_MAXW || R < w || R > panel_cluster_rows(h))
+        return fail(h, MG_ERR_ARG, "sgetf2_cluster: unsupported panel %d x %d", R, w);
+    const int rpt = (R + CP_CS * CP_THREADS - 1) / (CP_CS * CP_THREADS);
+    const size_t smem = (size_t)CP_SW * rpt * CP_THREADS * sizeof(float) + (size_t)R * sizeof(int);
+    ProfScope prof(h, "panel_f32", (double)R * w * w, 2.0 * R * w * sizeof(float));
+    cudaError_t e;
+    switch (rpt) {
+        case 1: e = launch_cluster<1>(h->stream, smem, A, lda, m, r0, w, pos, piv, info); break;
+        case 2: e = launch_cluster<2>(h->stream, smem, A, lda, m, r0, w, pos, piv, info); break;
+        case 3: e = launch_cluster<3>(h->stream, smem, A, lda, m, r0, w, pos, piv, info); break;
+        default: e = launch_cluster<4>(h->stream, smem, A, lda, m, r0, w, pos, piv, info); break;
+    }
+    if (e != cudaSuccess) return cuda_fail(h, e, "panel_cluster_kernel launch");
+    h->launches++;
+    return MG_OK;
+}
+
+}  // namespace mg
