@@ -7,10 +7,12 @@
 // L2 round trips per column, ~4.5 us; inside a cluster it is one hardware
 // cluster barrier plus one distributed-shared-memory read, well under 1 us.
 // A 16-CTA cluster cannot hold a 16384 x 128 FP32 panel (8 MiB) on chip, so
-// the panel is factored in sub-panels of 32 columns kept in registers
-// (each of the 256 threads of a CTA owns RPT <= 4 rows x 32 columns):
+// the panel is factored in sub-panels of 16 columns kept in registers
+// (each of the 256 threads of a CTA owns RPT <= 4 rows x 16 columns; the
+// fully unrolled column loop of a 16-column sub-panel stays small enough for
+// the instruction cache):
 //
-//   for each sub-panel S = [cs0, cs0+32):
+//   for each sub-panel S = [cs0, cs0+16):
 //     1. load my rows of S into registers
 //     2. for each column c of S: local max |a| -> publish (value, row,
 //        row data, and the diagonal row) in my shared memory -> cluster
@@ -20,7 +22,7 @@
 //     3. store S; apply S's interchanges to the panel's other columns and to
 //        pos (one gather/scatter over the touched rows, net permutation kept
 //        in a shared-memory map)
-//     4. U(S, right) = L11^{-1} A(S, right) (32 x 32 unit lower, every CTA
+//     4. U(S, right) = L11^{-1} A(S, right) (16 x 16 unit lower, every CTA
 //        redundantly), then A(below, right) -= L(below, S) U(S, right) for my
 //        rows, with L(below, S) still in registers.
 //
@@ -47,11 +49,11 @@ namespace {
 constexpr int CP_THREADS = 256;
 constexpr int CP_CS = 16;         // CTAs per cluster (non-portable size)
 constexpr int CP_MAX_RPT = 4;     // rows per thread
-constexpr int CP_SW = 32;       // sub-panel width (columns in registers)
+constexpr int CP_SW = 16;       // sub-panel width (columns in registers)
 constexpr int CP_MAXW = 128;    // widest panel
 constexpr int CP_NOTHER = CP_MAXW - CP_SW;
 constexpr int CP_UB_LD = CP_SW + 4;  // padded row of ub (16-byte multiple)
-constexpr int CP_GCOLS = 12;         // columns per gather pass (>= 96 / 8)
+constexpr int CP_GCOLS = 8;          // columns per gather pass (>= 112 / 16)
 
 struct CpShared {
     float ub[CP_NOTHER][CP_UB_LD];  // U(S, right), [column][row of S]
@@ -87,7 +89,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
     constexpr int CS = CP_CS;
     constexpr int RPC = RPT * CP_THREADS;  // positions per CTA
     extern __shared__ __align__(16) float dyn[];
-    float* const tile = dyn;                              // [32][RPC]: my rows of the sub-panel
+    float* const tile = dyn;                              // [CP_SW][RPC]: my rows of the sub-panel
     int* const map = reinterpret_cast<int*>(dyn + CP_SW * RPC);  // map[p], p in [0, R): the row (at
                                                           // sub-panel start) now at position p
     __shared__ __align__(16) CpShared sh;
@@ -184,10 +186,11 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                     cpos = *cluster.map_shared_rank(&sh.cand_pos[buf], lane);
                     cq = lane;
                 }
+                const int jl = lane < CP_SW ? lane : 0;
                 float rv[CS];
 #pragma unroll
-                for (int r = 0; r < CS; ++r) rv[r] = *cluster.map_shared_rank(&sh.pubrow[buf][lane], r);
-                const float dv = *cluster.map_shared_rank(&sh.pubdiag[buf][lane], cabs / RPC);
+                for (int r = 0; r < CS; ++r) rv[r] = *cluster.map_shared_rank(&sh.pubrow[buf][jl], r);
+                const float dv = *cluster.map_shared_rank(&sh.pubdiag[buf][jl], cabs / RPC);
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) {
                     const float ov = __shfl_xor_sync(0xffffffffu, cv, off);
@@ -199,8 +202,10 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
 #pragma unroll
                 for (int r = 0; r < CS; ++r)
                     if (r == cq) pr = rv[r];
-                sh.prow[lane] = pr;
-                sh.drow[lane] = dv;
+                if (lane < CP_SW) {
+                    sh.prow[lane] = pr;
+                    sh.drow[lane] = dv;
+                }
                 if (lane == 0) {
                     const bool ok = cv > 0.f;
                     sh.s_win = cpos;
