@@ -355,11 +355,12 @@ bool make_map(CUtensorMap* map, const void* base, int rows, int Kp, int np, size
 
 template <int NP>
 mg_status_t launch_gemm_np(mg_handle_t h, const CUtensorMap& ma, const CUtensorMap& mb, float* C, int ldc, int M,
-                           int N, int Kp, float alpha, float beta, int* err) {
+                           int N, int Kp, float alpha, float beta, int* err, int max_ctas) {
     auto kern = bf16x_gemm_kernel<NP>;
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<NP>::SMEM));
     const int tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
-    const int grid = tiles < h->num_sms ? tiles : h->num_sms;
+    const int cap = max_ctas > 0 && max_ctas < h->num_sms ? max_ctas : h->num_sms;
+    const int grid = tiles < cap ? tiles : cap;
     kern<<<grid, THREADS, Cfg<NP>::SMEM, h->stream>>>(ma, mb, C, ldc, M, N, Kp, alpha, beta, err);
     return mg::post_launch(h, "bf16x_gemm_kernel");
 }
@@ -396,21 +397,26 @@ template mg_status_t bf16x_split<float>(mg_handle_t, bool, const float*, int, in
 template mg_status_t bf16x_split<double>(mg_handle_t, bool, const double*, int, int, int, int, void*);
 
 // C = alpha * (split A)(split B) + beta * C from pre-split operands.
+int bf16x_kpad(int K) { return (K + BK - 1) / BK * BK; }
+
 mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, float alpha, const void* Asplit,
-                                const void* Bsplit, float beta, float* C, int ldc, int* err) {
+                                const void* Bsplit, float beta, float* C, int ldc, int* err, size_t a_term,
+                                size_t b_term, int max_ctas) {
     if (M == 0 || N == 0) return MG_OK;
     const int Kp = (K + BK - 1) / BK * BK;
+    if (!a_term) a_term = (size_t)M * Kp;
+    if (!b_term) b_term = (size_t)N * Kp;
     CUtensorMap ma, mb;
-    if (!make_map(&ma, Asplit, M, Kp, np, (size_t)M * Kp, BM) || !make_map(&mb, Bsplit, N, Kp, np, (size_t)N * Kp, BN))
+    if (!make_map(&ma, Asplit, M, Kp, np, a_term, BM) || !make_map(&mb, Bsplit, N, Kp, np, b_term, BN))
         return fail(h, MG_ERR_CUDA, "cuTensorMapEncodeTiled failed (M=%d N=%d Kp=%d)", M, N, Kp);
     const int nprod = np == 3 ? 6 : np == 2 ? 3 : 1;
     // flops: every bf16 product the tensor cores execute; bytes: C read+write plus the split operands once
     ProfScope prof(h, "gemm_bf16x", 2.0 * M * N * (double)Kp * nprod,
                    (beta == 0.f ? 4.0 : 8.0) * M * N + 2.0 * np * (double)(M + N) * Kp);
     switch (np) {
-        case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err);
-        case 2: return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err);
-        default: return launch_gemm_np<3>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err);
+        case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas);
+        case 2: return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas);
+        default: return launch_gemm_np<3>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas);
     }
 }
 

@@ -20,6 +20,15 @@ mg_status_t cuda_fail(mg_handle_t h, cudaError_t e, const char* what) {
     return fail(h, MG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+mg_status_t ensure_lookahead(mg_handle_t h) {
+    if (h->la_stream) return MG_OK;
+    int least = 0, greatest = 0;
+    MG_CHECK_CUDA(h, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    MG_CHECK_CUDA(h, cudaStreamCreateWithPriority(&h->la_stream, cudaStreamNonBlocking, least));
+    for (cudaEvent_t& e : h->la_ev) MG_CHECK_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return MG_OK;
+}
+
 mg_status_t ensure_ws(mg_handle_t h, size_t bytes) {
     if (bytes <= h->ws_bytes) return MG_OK;
     bytes = align_up(bytes + (bytes >> 3), 1 << 20);
@@ -176,6 +185,12 @@ mg_status_t mg_handle_destroy(mg_handle_t h) {
     mg::prof_resolve(h);
     for (cudaEvent_t e : h->prof_pool) cudaEventDestroy(e);
     if (h->ws || h->hws) cudaStreamSynchronize(h->stream);
+    if (h->la_stream) {
+        cudaStreamSynchronize(h->la_stream);
+        cudaStreamDestroy(h->la_stream);
+    }
+    for (cudaEvent_t e : h->la_ev)
+        if (e) cudaEventDestroy(e);
     if (h->ws) cudaFree(h->ws);
     if (h->hws) cudaFreeHost(h->hws);
     if (h->status) cudaFree(h->status);

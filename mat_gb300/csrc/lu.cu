@@ -597,34 +597,64 @@ static mg_status_t launch_panel_f32(mg_handle_t h, GetrfCtx<float>& c, float* A,
     return launch_panel<float>(h, c, A, lda, m, r0, w, pos);
 }
 
-// FP32 blocked right-looking LU with partial pivoting for the mixed solve:
-// fp32 panels (the same cooperative panel kernel), fp32 TRSM on the block
-// row, and the trailing update A22 -= L21*U12 on the BF16 tensor cores with
-// `nterms` split terms (fp32 accumulation).  `xchg` holds
-// sgetrf_xchg_bytes(); `splitA`/`splitB` hold bf16x_split_bytes(n, nb, nterms);
-// `tri` holds sgetrf_tri_bytes(nb, nterms); if Linv_all is not NULL the
-// inverse of every diagonal block of L is kept there (nb*nb floats each,
-// ld nb).  The block-row solve
-// U12 = L11^{-1} A12 is an explicit inverse of the unit-lower L11 followed by
-// a split-BF16 GEMM (the refinement absorbs its fp32-level error).
+// Runs the enclosed launches on another stream of the handle (the profiler
+// records on whatever h->stream is at the time).
+struct OnStream {
+    mg_handle_t h;
+    cudaStream_t saved;
+    OnStream(mg_handle_t h_, cudaStream_t s) : h(h_), saved(h_->stream) { h->stream = s; }
+    ~OnStream() { h->stream = saved; }
+};
+
+// FP32 blocked right-looking LU with partial pivoting for the mixed solve,
+// with a look-ahead of one panel.  Step k on the handle's stream S:
+//
+//   [wait for the far update of step k-1] interchanges of panel k on the
+//   columns to its right -> U12 = L11^{-1} A12 (split-BF16 GEMM) -> split
+//   U12 -> update of the next panel's columns (near update) -> panel k+1 ->
+//   its interchanges on the columns to its left -> inverse of its L11 ->
+//   splits of L11^{-1} and L21 (L21 into the buffer of parity k+1)
+//
+// while a low-priority side stream runs the far update (the trailing
+// columns beyond the next panel) of step k on num_sms - 16 CTAs as soon as
+// the near update is done.  The panel is queued directly behind the near
+// update on S, so its 16-CTA cluster takes its SMs before the far update's
+// persistent grid fills the rest.  A panel too tall for the cluster (the
+// cooperative grid) is not overlapped.
+//
+// The trailing updates run on the BF16 tensor cores with `nterms` split
+// terms (fp32 accumulation).  `xchg` holds sgetrf_xchg_bytes(); splitA and
+// splitA2 / splitB hold bf16x_split_bytes(n, nb, nterms); `tri` holds
+// sgetrf_tri_bytes(nb, nterms); if Linv_all is not NULL the inverse of every
+// diagonal block of L is kept there (nb*nb floats each, ld nb).  The
+// block-row solve U12 = L11^{-1} A12 is an explicit inverse of L11 followed
+// by a split-BF16 GEMM (the refinement absorbs its fp32-level error).
 mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int nb, int nterms, void* xchg,
-                         void* splitA, void* splitB, void* tri, float* Linv_all, int* gemm_err, int* info_out) {
+                         void* splitA, void* splitA2, void* splitB, void* tri, float* Linv_all, int* gemm_err,
+                         int* info_out) {
     if (info_out) *info_out = 0;
     if (n == 0) return MG_OK;
     if (nb > PANEL_MAX_NB || nb > 128) return fail(h, MG_ERR_ARG, "sgetrf_mixed: block size %d > 128", nb);
     MG_TRY(ensure_hws(h, 64));
+    MG_TRY(ensure_lookahead(h));
     GetrfCtx<float> c = carve<float>(xchg, h->num_sms);
-    MG_CHECK_CUDA(h, cudaMemsetAsync(xchg, 0, 256, h->stream));
-    iota_kernel<<<(n + 255) / 256, 256, 0, h->stream>>>(pos, n);
+    const cudaStream_t S = h->stream, S2 = h->la_stream;
+    MG_CHECK_CUDA(h, cudaMemsetAsync(xchg, 0, 256, S));
+    iota_kernel<<<(n + 255) / 256, 256, 0, S>>>(pos, n);
     MG_TRY(post_launch(h, "iota_kernel"));
     const size_t ism = (2 * (size_t)INV_LD * INV_LD + 64 * 64) * sizeof(float);
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_unit_lower_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism));
-    for (int r = 0; r < n; r += nb) {
-        const int w = nb < n - r ? nb : n - r;
+    void* const splitT = (char*)tri + align_up((size_t)nb * nb * sizeof(float), 1024);
+    void* const splitL[2] = {splitA, splitA2};
+    const bool cluster_ok = panel_cluster_rows(h) > 0;
+    const int nsteps = (n + nb - 1) / nb;
+
+    // panel k and everything that depends only on it
+    auto side = [&](int k) -> mg_status_t {
+        const int r = k * nb, w = nb < n - r ? nb : n - r;
         MG_TRY(launch_panel_f32(h, c, A, lda, n, r, w, pos));
-        MG_TRY(launch_laswp<float>(h, A, lda, r, w, c.piv, r, r + w, n));
-        // inverse of the unit-lower diagonal block (kept with ld nb in Linv_all when requested)
-        float* Lout = Linv_all ? Linv_all + (size_t)(r / nb) * nb * nb : (float*)tri;
+        MG_TRY(launch_laswp<float>(h, A, lda, r, w, c.piv, r, n, n));  // columns [0, r)
+        float* Lout = Linv_all ? Linv_all + (size_t)k * nb * nb : (float*)tri;
         const int ldo = Linv_all ? nb : w;
         if (Linv_all || r + w < n) {
             ProfScope prof(h, "trsm_f32", 2.0 * w * w * (double)w / 3.0, 8.0 * w * (double)w);
@@ -633,29 +663,68 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
         }
         if (r + w < n) {
             const int nt = n - (r + w);
-            float* A12 = A + r + (size_t)(r + w) * lda;
-            {
-                ProfScope prof(h, "trsm_f32", 2.0 * w * w * (double)nt, 8.0 * w * (double)nt);
-                void* splitT = (char*)tri + align_up((size_t)nb * nb * sizeof(float), 1024);
-                MG_TRY(bf16x_split<float>(h, true, Lout, ldo, w, w, nterms, splitT));
-                MG_TRY(bf16x_split<float>(h, false, A12, lda, nt, w, nterms, splitB));
-                MG_TRY(bf16x_gemm_presplit(h, nterms, w, nt, w, 1.0f, splitT, splitB, 0.0f, A12, lda, gemm_err));
-            }
-            const float* L21 = A + (r + w) + (size_t)r * lda;
-            {
-                ProfScope prof(h, "split", 0.0, 2.0 * nt * w * (4.0 + 2.0 * nterms));
-                MG_TRY(bf16x_split<float>(h, true, L21, lda, nt, w, nterms, splitA));
-                MG_TRY(bf16x_split<float>(h, false, A12, lda, nt, w, nterms, splitB));
-            }
-            MG_TRY(bf16x_gemm_presplit(h, nterms, nt, nt, w, -1.0f, splitA, splitB, 1.0f,
-                                       A + (r + w) + (size_t)(r + w) * lda, lda, gemm_err));
+            ProfScope prof(h, "split", 0.0, 2.0 * (nt + w) * w * (4.0 + 2.0 * nterms));
+            MG_TRY(bf16x_split<float>(h, true, Lout, ldo, w, w, nterms, splitT));
+            MG_TRY(bf16x_split<float>(h, true, A + (r + w) + (size_t)r * lda, lda, nt, w, nterms, splitL[k & 1]));
         }
+        return MG_OK;
+    };
+    // a panel overlaps the previous trailing update only on the cluster path
+    auto overlappable = [&](int k) {
+        const int r = k * nb, R = n - r, w = nb < R ? nb : R;
+        return cluster_ok && (size_t)R * w * sizeof(float) > 64 * 1024 && R >= w && R <= panel_cluster_rows(h);
+    };
+
+    MG_TRY(side(0));
+    bool far_pending = false;  // a far update was issued on S2 (event la_ev[1])
+    for (int k = 0; k < nsteps; ++k) {
+        const int r = k * nb, w = nb < n - r ? nb : n - r;
+        if (r + w >= n) break;
+        const int nt = n - (r + w);
+        const int kp = bf16x_kpad(w);  // row length of this step's split terms
+        if (far_pending) MG_CHECK_CUDA(h, cudaStreamWaitEvent(S, h->la_ev[1], 0));
+        far_pending = false;
+        MG_TRY(launch_laswp<float>(h, A, lda, r, w, c.piv, 0, r + w, n));  // columns [r + w, n)
+        float* A12 = A + r + (size_t)(r + w) * lda;
+        {
+            ProfScope prof(h, "trsm_f32", 2.0 * w * w * (double)nt, 8.0 * w * (double)nt);
+            MG_TRY(bf16x_split<float>(h, false, A12, lda, nt, w, nterms, splitB));
+            MG_TRY(bf16x_gemm_presplit(h, nterms, w, nt, w, 1.0f, splitT, splitB, 0.0f, A12, lda, gemm_err));
+        }
+        {
+            ProfScope prof(h, "split", 0.0, 2.0 * nt * w * (4.0 + 2.0 * nterms));
+            MG_TRY(bf16x_split<float>(h, false, A12, lda, nt, w, nterms, splitB));
+        }
+        const void* L21 = splitL[k & 1];
+        float* A22 = A + (r + w) + (size_t)(r + w) * lda;
+        const int w1 = nb < nt ? nb : nt;  // the next panel's columns
+        MG_TRY(bf16x_gemm_presplit(h, nterms, nt, w1, w, -1.0f, L21, splitB, 1.0f, A22, lda, gemm_err, 0,
+                                   (size_t)nt * kp));
+        const bool ov = overlappable(k + 1);
+        if (nt > w1) {
+            const void* Brest = (const char*)splitB + (size_t)w1 * kp * 2;
+            if (ov) {
+                MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[0], S));
+                MG_CHECK_CUDA(h, cudaStreamWaitEvent(S2, h->la_ev[0], 0));
+                OnStream on(h, S2);
+                MG_TRY(bf16x_gemm_presplit(h, nterms, nt, nt - w1, w, -1.0f, L21, Brest, 1.0f,
+                                           A22 + (size_t)w1 * lda, lda, gemm_err, 0, (size_t)nt * kp,
+                                           h->num_sms - 16));
+                MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[1], S2));
+                far_pending = true;
+            } else {
+                MG_TRY(bf16x_gemm_presplit(h, nterms, nt, nt - w1, w, -1.0f, L21, Brest, 1.0f,
+                                           A22 + (size_t)w1 * lda, lda, gemm_err, 0, (size_t)nt * kp));
+            }
+        }
+        MG_TRY(side(k + 1));
     }
+    if (far_pending) MG_CHECK_CUDA(h, cudaStreamWaitEvent(S, h->la_ev[1], 0));
     int* hw = (int*)h->hws;
-    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, c.ws.err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw + 1, c.ws.info, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw + 2, gemm_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, c.ws.err, sizeof(int), cudaMemcpyDeviceToHost, S));
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw + 1, c.ws.info, sizeof(int), cudaMemcpyDeviceToHost, S));
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw + 2, gemm_err, sizeof(int), cudaMemcpyDeviceToHost, S));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(S));
     if (hw[0] || hw[2]) return fail(h, MG_TIMEOUT, "sgetrf_mixed: a bounded device wait timed out");
     if (info_out) *info_out = hw[1];
     if (hw[1]) return fail(h, MG_SINGULAR, "sgetrf_mixed: exactly zero pivot column %d", hw[1]);
@@ -790,6 +859,7 @@ mg_status_t mg_sgetrf(mg_handle_t h, int n, float* A, int lda, int* pos, int* in
     };
     const size_t oX = take(mg::sgetrf_xchg_bytes(h->num_sms));
     const size_t oSA = take(mg::bf16x_split_bytes(n, nb, nterms));
+    const size_t oSA2 = take(mg::bf16x_split_bytes(n, nb, nterms));
     const size_t oSB = take(mg::bf16x_split_bytes(n, nb, nterms));
     const size_t oT = take(mg::sgetrf_tri_bytes(nb, nterms));
     const size_t oE = take(64);
@@ -797,7 +867,8 @@ mg_status_t mg_sgetrf(mg_handle_t h, int n, float* A, int lda, int* pos, int* in
     char* b = (char*)h->ws;
     int* gerr = (int*)(b + oE);
     MG_CHECK_CUDA(h, cudaMemsetAsync(gerr, 0, 64, h->stream));
-    return mg::sgetrf_mixed(h, n, A, lda, pos, nb, nterms, b + oX, b + oSA, b + oSB, b + oT, nullptr, gerr, info);
+    return mg::sgetrf_mixed(h, n, A, lda, pos, nb, nterms, b + oX, b + oSA, b + oSA2, b + oSB, b + oT, nullptr, gerr,
+                            info);
 }
 
 mg_status_t mg_dgetrf_noalloc(void* cuda_stream, int m, int n, double* A, int lda, int* pos, int* info) {

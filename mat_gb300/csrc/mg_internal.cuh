@@ -28,6 +28,10 @@ struct mg_handle_s {
     uint64_t launches = 0;
     // Cluster size of the FP32 cluster panel (0: not probed yet, -1: unavailable).
     int panel_cluster = 0;
+    // Look-ahead LU: low-priority side stream (far trailing updates) and two
+    // ordering events.
+    cudaStream_t la_stream = nullptr;
+    cudaEvent_t la_ev[2] = {nullptr, nullptr};
     char last_error[512] = {0};
     // Optional per-phase timing with CUDA events on the handle's stream.
     struct ProfRec {
@@ -98,19 +102,30 @@ size_t bf16x_split_bytes(int rows, int K, int np);
 template <typename TIN>
 mg_status_t bf16x_split(mg_handle_t h, bool a_side, const TIN* X, int ldx, int rows_or_cols, int K, int np,
                         void* out);
+// a_term / b_term: elements between the split terms of A / B (0: M*Kp /
+// N*Kp, i.e. a whole split operand; larger when the operand is a row or
+// column window of a bigger split).  max_ctas > 0 caps the persistent grid.
 mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, float alpha, const void* Asplit,
-                                const void* Bsplit, float beta, float* C, int ldc, int* err);
+                                const void* Bsplit, float beta, float* C, int ldc, int* err, size_t a_term = 0,
+                                size_t b_term = 0, int max_ctas = 0);
+// K rounded up to the split GEMM's K step (elements per row of a split term).
+int bf16x_kpad(int K);
 
-// FP32 LU with split-BF16 trailing updates (lu.cu).
 // FP32 panel on one thread-block cluster (panel_f32.cu): rows it can take
 // (0 if unavailable), and the launch (piv relative to r0; pos updated).
 int panel_cluster_rows(mg_handle_t h);
 mg_status_t sgetf2_cluster(mg_handle_t h, float* A, int lda, int m, int r0, int w, int* pos, int* piv, int* info);
 
+// FP32 LU with split-BF16 trailing updates (lu.cu).  splitA and splitA2
+// each hold bf16x_split_bytes(n, nb, nterms) (the L21 split of alternate
+// steps), splitB the same, tri sgetrf_tri_bytes(nb, nterms).
 size_t sgetrf_xchg_bytes(int num_sms);
 size_t sgetrf_tri_bytes(int nb, int nterms);
 mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int nb, int nterms, void* xchg,
-                         void* splitA, void* splitB, void* tri, float* Linv_all, int* gemm_err, int* info_out);
+                         void* splitA, void* splitA2, void* splitB, void* tri, float* Linv_all, int* gemm_err,
+                         int* info_out);
+// Side stream and events of the look-ahead LU (created once per handle).
+mg_status_t ensure_lookahead(mg_handle_t h);
 
 }  // namespace mg
 

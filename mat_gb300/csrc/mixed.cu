@@ -308,6 +308,7 @@ struct IrWs {
     int* pos;
     void* xchg;
     void* splitA;
+    void* splitA2;
     void* splitB;
     void* tri;
     int* gemm_err;
@@ -333,6 +334,7 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
     const size_t oP = take((size_t)n * sizeof(int));
     const size_t oX = take(mg::sgetrf_xchg_bytes(h->num_sms));
     const size_t oSA = take(mg::bf16x_split_bytes(n, IR_BLOCK, nterms));
+    const size_t oSA2 = take(mg::bf16x_split_bytes(n, IR_BLOCK, nterms));
     const size_t oSB = take(mg::bf16x_split_bytes(n, IR_BLOCK, nterms));
     const size_t oT = take(mg::sgetrf_tri_bytes(IR_BLOCK, nterms));
     const size_t oE = take(64);
@@ -349,6 +351,7 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
         w->pos = (int*)(b + oP);
         w->xchg = b + oX;
         w->splitA = b + oSA;
+        w->splitA2 = b + oSA2;
         w->splitB = b + oSB;
         w->tri = b + oT;
         w->gemm_err = (int*)(b + oE);
@@ -417,7 +420,7 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     MG_TRY(mg::post_launch(h, "d2s_kernel"));
     delete setup;
     int info = 0;
-    mg_status_t s = mg::sgetrf_mixed(h, n, w.A32, n, w.pos, IR_BLOCK, o.nterms, w.xchg, w.splitA, w.splitB,
+    mg_status_t s = mg::sgetrf_mixed(h, n, w.A32, n, w.pos, IR_BLOCK, o.nterms, w.xchg, w.splitA, w.splitA2, w.splitB,
                                      w.tri, w.Linv, w.gemm_err, &info);
     if (s != MG_OK && s != MG_SINGULAR) return s;
     r.info = info;
