@@ -21,6 +21,7 @@
 #include <cmath>
 #include <vector>
 
+#include "grid_sync.cuh"
 #include "mg_internal.cuh"
 
 namespace {
@@ -254,6 +255,148 @@ __global__ void __launch_bounds__(256) blockdiag_apply_kernel(const float* __res
         for (int j = 0; j < NR; ++j) Out[b0 + r + (size_t)j * n] = part[0][j][r] + part[1][j][r];
 }
 
+// One blocked triangular solve as a single cooperative dataflow kernel:
+// CTA j owns row block j.  For LOWER (L unit lower, forward) it consumes the
+// solved blocks b = 0..j-1 in order, for the upper solve b = nblk-1..j+1:
+// before waiting it loads its 128x128 block T(j, b) of the packed LU into
+// registers, then waits (bounded) for block b's flag, reads x_b and
+// accumulates T(j, b) x_b.  When all are in, it forms w_j = rhs_j - sum,
+// applies the inverse of its own diagonal block (Dinv, 128 x 128, ld 128),
+// writes x_j and raises its flag.  The chain per block step is one flag
+// hand-off, one read of x_b and the owner's 128 x 128 inverse apply; every
+// other block's update overlaps it.  All CTAs must be co-resident
+// (cooperative launch); flags start at zero.
+template <bool LOWER, int NR>
+__global__ void __launch_bounds__(256) trsv_flow_kernel(const float* __restrict__ LU, int lda, int n,
+                                                        const float* __restrict__ Dinv,
+                                                        const float* __restrict__ Win, float* __restrict__ Xout,
+                                                        unsigned* __restrict__ flags, int* __restrict__ err) {
+    extern __shared__ float sdinv[];  // IR_BLOCK * IR_BLOCK
+    __shared__ float xb[NR][IR_BLOCK];
+    __shared__ float wb[NR][IR_BLOCK];
+    __shared__ float part[2][NR][IR_BLOCK];
+    __shared__ int s_ok;
+    const int nblk = gridDim.x, me = blockIdx.x;
+    const int r0 = me * IR_BLOCK, rows = min(IR_BLOCK, n - r0);
+    const int r = threadIdx.x & (IR_BLOCK - 1), hf = threadIdx.x >> 7;
+    const int k0 = hf * (IR_BLOCK / 2);
+    {  // own diagonal-block inverse, needed last
+        const float* src = Dinv + (size_t)me * IR_BLOCK * IR_BLOCK;
+        for (int e = threadIdx.x; e < IR_BLOCK * IR_BLOCK; e += blockDim.x) sdinv[e] = src[e];
+    }
+    float acc[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) acc[j] = 0.f;
+    const int nsteps = LOWER ? me : nblk - 1 - me;
+    for (int t = 0; t < nsteps; ++t) {
+        const int b = LOWER ? t : nblk - 1 - t;
+        const int c0 = b * IR_BLOCK, bs = min(IR_BLOCK, n - c0);
+        float l[IR_BLOCK / 2];
+        const float* tp = LU + (size_t)(r0 + r) + (size_t)(c0 + k0) * lda;
+#pragma unroll
+        for (int u = 0; u < IR_BLOCK / 2; ++u) l[u] = (r < rows && k0 + u < bs) ? tp[(size_t)u * lda] : 0.f;
+        if (threadIdx.x == 0) {
+            int ok = 1;
+            unsigned spins = 0;
+            while (mg::ld_acquire_u32(flags + b) == 0u) {
+                if (++spins > mg::kSpinLimit) {
+                    atomicExch(err, 8 /* MG_TIMEOUT */);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(spins < 64 ? 20 : 100);
+            }
+            s_ok = ok;
+        }
+        __syncthreads();
+        if (!s_ok) return;
+        for (int q = threadIdx.x; q < bs * NR; q += blockDim.x) {
+            const int j = q / bs, i = q - j * bs;
+            xb[j][i] = __ldcg(Xout + c0 + i + (size_t)j * n);
+        }
+        for (int q = bs + threadIdx.x; q < IR_BLOCK; q += blockDim.x)
+#pragma unroll
+            for (int j = 0; j < NR; ++j) xb[j][q] = 0.f;
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < IR_BLOCK / 2; ++u)
+#pragma unroll
+            for (int j = 0; j < NR; ++j) acc[j] = fmaf(l[u], xb[j][k0 + u], acc[j]);
+        __syncthreads();  // xb is rewritten by the next step
+    }
+#pragma unroll
+    for (int j = 0; j < NR; ++j) part[hf][j][r] = acc[j];
+    __syncthreads();
+    if (hf == 0)
+#pragma unroll
+        for (int j = 0; j < NR; ++j)
+            wb[j][r] = r < rows ? Win[r0 + r + (size_t)j * n] - (part[0][j][r] + part[1][j][r]) : 0.f;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NR; ++j) acc[j] = 0.f;
+    if (r < rows)
+        for (int k = k0; k < k0 + IR_BLOCK / 2 && k < rows; ++k) {
+            const float v = sdinv[r + k * IR_BLOCK];
+#pragma unroll
+            for (int j = 0; j < NR; ++j) acc[j] = fmaf(v, wb[j][k], acc[j]);
+        }
+#pragma unroll
+    for (int j = 0; j < NR; ++j) part[hf][j][r] = acc[j];
+    __syncthreads();
+    if (hf == 0 && r < rows)
+#pragma unroll
+        for (int j = 0; j < NR; ++j) Xout[r0 + r + (size_t)j * n] = part[0][j][r] + part[1][j][r];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicExch(flags + me, 1u);
+    }
+}
+
+// Largest block count the dataflow solve can take as one cooperative grid.
+template <int NR>
+int trsv_flow_capacity(mg_handle_t h) {
+    const size_t smem = (size_t)IR_BLOCK * IR_BLOCK * sizeof(float);
+    if (cudaFuncSetAttribute(trsv_flow_kernel<true, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(trsv_flow_kernel<false, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int a = 0, b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, trsv_flow_kernel<true, NR>, 256, smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trsv_flow_kernel<false, NR>, 256, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return std::min(a, b) * h->num_sms;
+}
+
+// Both triangular solves of one correction with the dataflow kernel:
+// Y (in) -> Z = L^-1 Y -> Y = U^-1 Z.  flags: 2 * nblk words.
+template <int NR>
+mg_status_t lu_solve_flow(mg_handle_t h, const float* LU, int n, const float* Linv, const float* Uinv, float* Y,
+                          float* Z, unsigned* flags, int* err) {
+    cudaStream_t st = h->stream;
+    const int nblk = (n + IR_BLOCK - 1) / IR_BLOCK;
+    const size_t smem = (size_t)IR_BLOCK * IR_BLOCK * sizeof(float);
+    MG_CHECK_CUDA(h, cudaMemsetAsync(flags, 0, 2 * (size_t)nblk * sizeof(unsigned), st));
+    int lda = n;
+    unsigned* fl = flags;
+    unsigned* fu = flags + nblk;
+    void* a1[] = {(void*)&LU, &lda, &n, (void*)&Linv, (void*)&Y, (void*)&Z, (void*)&fl, (void*)&err};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)trsv_flow_kernel<true, NR>, dim3(nblk), dim3(256), a1,
+                                                smem, st);
+    if (e != cudaSuccess) return mg::cuda_fail(h, e, "trsv_flow_kernel<lower> launch");
+    h->launches++;
+    void* a2[] = {(void*)&LU, &lda, &n, (void*)&Uinv, (void*)&Z, (void*)&Y, (void*)&fu, (void*)&err};
+    e = cudaLaunchCooperativeKernel((const void*)trsv_flow_kernel<false, NR>, dim3(nblk), dim3(256), a2, smem, st);
+    if (e != cudaSuccess) return mg::cuda_fail(h, e, "trsv_flow_kernel<upper> launch");
+    h->launches++;
+    return MG_OK;
+}
+
 // Both triangular solves of one correction: Y (in, destroyed) -> Y = U^-1 L^-1 Y, Z scratch.
 template <int NR>
 mg_status_t lu_solve_blocked(mg_handle_t h, const float* LU, int n, const float* Linv, const float* Uinv, float* Y,
@@ -304,6 +447,7 @@ mg_status_t preinvert_blocks(mg_handle_t h, float* LU, int n, const float* Linv,
 }
 
 struct IrWs {
+    unsigned* flags;  // dataflow triangular-solve flags, 2 * nblk
     float* A32;
     int* pos;
     void* xchg;
@@ -343,6 +487,7 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
     const size_t oR = take((size_t)n * nrhs * sizeof(double));
     const size_t oPa = take((size_t)kch * n * std::max(nrhs, 1) * sizeof(double));
     const size_t oN = take(64 * sizeof(double));
+    const size_t oF = take(2 * (size_t)nblk * sizeof(unsigned));
     const size_t oY = take((size_t)n * nrhs * sizeof(float));
     const size_t oZ = take((size_t)n * nrhs * sizeof(float));
     if (w) {
@@ -360,6 +505,7 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
         w->R = (double*)(b + oR);
         w->partial = (double*)(b + oPa);
         w->norms = (double*)(b + oN);
+        w->flags = (unsigned*)(b + oF);
         w->Y = (float*)(b + oY);
         w->Z = (float*)(b + oZ);
     }
@@ -397,7 +543,7 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
 
     const auto t0 = clk::now();
     MG_TRY(mg::ensure_ws(h, carve_ir(h, n, nrhs, o.nterms, nullptr)));
-    MG_TRY(mg::ensure_hws(h, 256));
+    MG_TRY(mg::ensure_hws(h, 512));
     IrWs w;
     carve_ir(h, n, nrhs, o.nterms, &w);
     cudaStream_t st = h->stream;
@@ -431,7 +577,16 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     inv_diag_blocks_kernel<false><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
                                                                                                   w.Uinv);
     MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<upper>"));
-    {
+    int flow_cap = 0;
+    switch (nrhs) {
+#define MG_CAP(NRV) \
+    case NRV: flow_cap = trsv_flow_capacity<NRV>(h); break;
+        MG_CAP(1) MG_CAP(2) MG_CAP(3) MG_CAP(4) MG_CAP(5) MG_CAP(6) MG_CAP(7)
+        default: flow_cap = trsv_flow_capacity<8>(h); break;
+#undef MG_CAP
+    }
+    const bool flow = nblk <= flow_cap;
+    if (!flow) {  // launch-per-block-step solves need the pre-inverted block columns
         mg::ProfScope prof(h, "ir_preinvert", 2.0 * n * (double)n * IR_BLOCK * 6, 8.0 * n * (double)n);
         MG_TRY(preinvert_blocks(h, w.A32, n, w.Linv, w.Uinv, o.nterms, w.splitA, w.splitB, w.gemm_err));
     }
@@ -465,7 +620,12 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
         MG_TRY(mg::post_launch(h, "residual_reduce_kernel"));
         delete pr;
         MG_CHECK_CUDA(h, cudaMemcpyAsync(hn, w.norms, 32 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        int* herr = (int*)(hn + 48);  // device error words: split GEMM, triangular solves
+        MG_CHECK_CUDA(h, cudaMemcpyAsync(herr, w.gemm_err, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
         MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
+        if (herr[0] || herr[1])
+            return mg::fail(h, MG_TIMEOUT, "mg_dsgesv_ir: a bounded device wait timed out (%s)",
+                            herr[0] ? "split GEMM" : "triangular solve");
         const double anorm = hn[16];
         double eta = 0.0;
         for (int j = 0; j < nrhs; ++j) {
@@ -494,15 +654,18 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
         mg::ProfScope* ps = new mg::ProfScope(h, "ir_trsv", 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
         prep_rhs_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(n, nrhs, w.pos, w.R, w.norms + 24, w.Y);
         MG_TRY(mg::post_launch(h, "prep_rhs_kernel"));
+        int* terr = w.gemm_err + 1;
         switch (nrhs) {
-            case 1: MG_TRY(lu_solve_blocked<1>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
-            case 2: MG_TRY(lu_solve_blocked<2>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
-            case 3: MG_TRY(lu_solve_blocked<3>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
-            case 4: MG_TRY(lu_solve_blocked<4>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
-            case 5: MG_TRY(lu_solve_blocked<5>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
-            case 6: MG_TRY(lu_solve_blocked<6>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
-            case 7: MG_TRY(lu_solve_blocked<7>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
-            default: MG_TRY(lu_solve_blocked<8>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z)); break;
+#define MG_SOLVE(NRV)                                                                                       \
+    case NRV:                                                                                               \
+        if (flow)                                                                                           \
+            MG_TRY(lu_solve_flow<NRV>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z, w.flags, terr));               \
+        else                                                                                                \
+            MG_TRY(lu_solve_blocked<NRV>(h, w.A32, n, w.Linv, w.Uinv, w.Y, w.Z));                           \
+        break;
+            MG_SOLVE(1) MG_SOLVE(2) MG_SOLVE(3) MG_SOLVE(4) MG_SOLVE(5) MG_SOLVE(6) MG_SOLVE(7)
+            default: MG_SOLVE(8)
+#undef MG_SOLVE
         }
         update_x_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(n, nrhs, w.Y, w.norms + 24, X, ldx);
         MG_TRY(mg::post_launch(h, "update_x_kernel"));
