@@ -55,32 +55,33 @@ constexpr int CP_NOTHER = CP_MAXW - CP_SW;
 constexpr int CP_UB_LD = CP_SW + 4;  // padded row of ub (16-byte multiple)
 constexpr int CP_GCOLS = 8;          // columns per gather pass (>= 112 / 16)
 
+// One CTA's pivot candidate for a column as read by the other CTAs: the row
+// (its sub-panel columns), |a| as bits (non-negative floats order like their
+// bit patterns) and the position; 80 bytes, read as five 16-byte loads.
+struct __align__(16) CpRec {
+    float row[CP_SW];
+    unsigned bits;
+    int pos;
+    int pad[2];
+};
+
 struct CpShared {
     float ub[CP_NOTHER][CP_UB_LD];  // U(S, right), [column][row of S]
     float l11[CP_SW][CP_SW + 1];
-    float pubrow[2][CP_SW];
-    float pubdiag[2][CP_SW];
-    float cand_val[2];
-    int cand_pos[2];
-    float prow[CP_SW];
-    float drow[CP_SW];
-    float red_v[CP_THREADS / 32];
-    int red_p[CP_THREADS / 32];
+    CpRec rec[2];                   // this CTA's candidate, by column parity
+    __align__(16) float pubdiag[2][CP_SW];
+    __align__(16) float prow[CP_SW];
+    __align__(16) float drow[CP_SW];
+    float wrow[CP_THREADS / 32][CP_SW];  // each warp's candidate row
+    unsigned wbits[CP_THREADS / 32];
+    int wpos[CP_THREADS / 32];
     int piv[CP_MAXW];
     int touch[2 * CP_SW];
     float gbuf[CP_GCOLS * 2 * CP_SW];
     int gpos[2 * CP_SW];
-    int s_bpos, s_win;
+    int s_win;
     float s_pv;
 };
-
-__device__ __forceinline__ void cp_better(float& v, int& p, int& q, float ov, int op, int oq) {
-    if (ov > v || (ov == v && op < p)) {
-        v = ov;
-        p = op;
-        q = oq;
-    }
-}
 
 template <int RPT>
 __global__ void __launch_bounds__(CP_THREADS, 1)
@@ -125,98 +126,100 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
             if (c < sw) {
             const int cabs = cs0 + c;
             const int buf = cabs & 1;
-            // 1. this CTA's candidate
-            float best = -1.f;
-            int bpos = INT_MAX, dummy = 0;
+            // 1. candidates: per thread, per warp (redux), the warp's row into its slot
+            unsigned bb = 0u;
+            int bp = INT_MAX;
 #pragma unroll
             for (int k = 0; k < RPT; ++k) {
                 const int p = row0 + k * CP_THREADS + tid;
-                if (p < R && p >= cabs) cp_better(best, bpos, dummy, fabsf(v[k][c]), p, 0);
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                const float ov = __shfl_down_sync(0xffffffffu, best, off);
-                const int op = __shfl_down_sync(0xffffffffu, bpos, off);
-                cp_better(best, bpos, dummy, ov, op, 0);
-            }
-            if (lane == 0) {
-                sh.red_v[warp] = best;
-                sh.red_p[warp] = bpos;
-            }
-            __syncthreads();
-            if (warp == 0) {
-                best = lane < CP_THREADS / 32 ? sh.red_v[lane] : -1.f;
-                bpos = lane < CP_THREADS / 32 ? sh.red_p[lane] : INT_MAX;
-#pragma unroll
-                for (int off = 16; off > 0; off >>= 1) {
-                    const float ov = __shfl_down_sync(0xffffffffu, best, off);
-                    const int op = __shfl_down_sync(0xffffffffu, bpos, off);
-                    cp_better(best, bpos, dummy, ov, op, 0);
-                }
-                if (lane == 0) {
-                    sh.cand_val[buf] = best;
-                    sh.cand_pos[buf] = bpos;
-                    sh.s_bpos = bpos;
-                }
-            }
-            __syncthreads();
-            // 2. publish the candidate row and (by its owner) the diagonal row
-            {
-                const int bp = sh.s_bpos;
-#pragma unroll
-                for (int k = 0; k < RPT; ++k) {
-                    const int p = row0 + k * CP_THREADS + tid;
-                    if (p == bp) {
-#pragma unroll
-                        for (int j = 0; j < CP_SW; ++j) sh.pubrow[buf][j] = v[k][j];
+                const float a = fabsf(v[k][c]);
+                if (p < R && p >= cabs && a >= 0.f) {  // NaN is never a candidate
+                    const unsigned ab = __float_as_uint(a);
+                    if (ab > bb || bp == INT_MAX) {
+                        bb = ab;
+                        bp = p;
                     }
-                    if (p == cabs) {
+                }
+            }
+            {
+                const unsigned wm = __reduce_max_sync(0xffffffffu, bb);
+                const int wp = (int)__reduce_min_sync(0xffffffffu, bb == wm ? (unsigned)bp : (unsigned)INT_MAX);
+                if (lane == 0) {
+                    sh.wbits[warp] = wm;
+                    sh.wpos[warp] = wp;
+                }
+                if (wp != INT_MAX && bp == wp) {  // this lane owns the warp's candidate
+                    const int k = (wp - row0) / CP_THREADS;
+#pragma unroll
+                    for (int kk = 0; kk < RPT; ++kk)
+                        if (kk == k) {
+#pragma unroll
+                            for (int j = 0; j < CP_SW; ++j) sh.wrow[warp][j] = v[kk][j];
+                        }
+                }
+#pragma unroll
+                for (int k = 0; k < RPT; ++k)  // the row at the diagonal, for the swap
+                    if (row0 + k * CP_THREADS + tid == cabs) {
 #pragma unroll
                         for (int j = 0; j < CP_SW; ++j) sh.pubdiag[buf][j] = v[k][j];
                     }
+            }
+            __syncthreads();
+            // 2. the CTA's candidate record (warp 0): best of the warps
+            if (warp == 0) {
+                const unsigned mb = lane < CP_THREADS / 32 ? sh.wbits[lane] : 0u;
+                const int mp = lane < CP_THREADS / 32 ? sh.wpos[lane] : INT_MAX;
+                const unsigned cm = __reduce_max_sync(0xffffffffu, mb);
+                const int cp = (int)__reduce_min_sync(0xffffffffu, mb == cm ? (unsigned)mp : (unsigned)INT_MAX);
+                const unsigned own = __ballot_sync(0xffffffffu, mp == cp && mp != INT_MAX);
+                const int ww = own ? __ffs(own) - 1 : 0;
+                if (lane < CP_SW) sh.rec[buf].row[lane] = sh.wrow[ww][lane];
+                if (lane == 0) {
+                    sh.rec[buf].bits = cm;
+                    sh.rec[buf].pos = cp;
                 }
             }
             cluster.sync();
-            // 3. every CTA reads all candidates and rows and picks the same winner
+            // 3. every CTA reads all records (lane l: CTA l) and picks the same winner
             if (warp == 0) {
-                float cv = -1.f;
-                int cpos = INT_MAX, cq = CS;
+                float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, q2 = q0, q3 = q0, q4 = q0;
                 if (lane < CS) {
-                    cv = *cluster.map_shared_rank(&sh.cand_val[buf], lane);
-                    cpos = *cluster.map_shared_rank(&sh.cand_pos[buf], lane);
-                    cq = lane;
+                    const float4* src = reinterpret_cast<const float4*>(cluster.map_shared_rank(&sh.rec[buf], lane));
+                    q0 = src[0];
+                    q1 = src[1];
+                    q2 = src[2];
+                    q3 = src[3];
+                    q4 = src[4];
+                } else if (lane < CS + CP_SW / 4) {
+                    const float4* src = reinterpret_cast<const float4*>(
+                        cluster.map_shared_rank(&sh.pubdiag[buf][0], cabs / RPC));
+                    q0 = src[lane - CS];
                 }
-                const int jl = lane < CP_SW ? lane : 0;
-                float rv[CS];
-#pragma unroll
-                for (int r = 0; r < CS; ++r) rv[r] = *cluster.map_shared_rank(&sh.pubrow[buf][jl], r);
-                const float dv = *cluster.map_shared_rank(&sh.pubdiag[buf][jl], cabs / RPC);
-#pragma unroll
-                for (int off = 16; off > 0; off >>= 1) {
-                    const float ov = __shfl_xor_sync(0xffffffffu, cv, off);
-                    const int op = __shfl_xor_sync(0xffffffffu, cpos, off);
-                    const int oq = __shfl_xor_sync(0xffffffffu, cq, off);
-                    cp_better(cv, cpos, cq, ov, op, oq);
+                const unsigned rb = lane < CS ? __float_as_uint(q4.x) : 0u;
+                const int rp = lane < CS ? __float_as_int(q4.y) : INT_MAX;
+                const unsigned gm = __reduce_max_sync(0xffffffffu, rb);
+                const int gp = (int)__reduce_min_sync(0xffffffffu, rb == gm ? (unsigned)rp : (unsigned)INT_MAX);
+                const unsigned own = __ballot_sync(0xffffffffu, lane < CS && rp == gp);
+                if (own && lane == __ffs(own) - 1) {
+                    float4* d = reinterpret_cast<float4*>(sh.prow);
+                    d[0] = q0;
+                    d[1] = q1;
+                    d[2] = q2;
+                    d[3] = q3;
                 }
-                float pr = 0.f;
-#pragma unroll
-                for (int r = 0; r < CS; ++r)
-                    if (r == cq) pr = rv[r];
-                if (lane < CP_SW) {
-                    sh.prow[lane] = pr;
-                    sh.drow[lane] = dv;
-                }
+                if (lane >= CS && lane < CS + CP_SW / 4) reinterpret_cast<float4*>(sh.drow)[lane - CS] = q0;
                 if (lane == 0) {
-                    const bool ok = cv > 0.f;
-                    sh.s_win = cpos;
-                    sh.s_pv = cv;
-                    sh.piv[cabs] = ok ? cpos : cabs;
+                    const float gv = __uint_as_float(gm);
+                    const bool ok = gp != INT_MAX && gv > 0.f;
+                    sh.s_win = gp;
+                    sh.s_pv = ok ? gv : 0.f;
+                    sh.piv[cabs] = ok ? gp : cabs;
                     sh.touch[2 * c] = cabs;
-                    sh.touch[2 * c + 1] = ok ? cpos : cabs;
-                    if (ok && cpos != cabs) {
+                    sh.touch[2 * c + 1] = ok ? gp : cabs;
+                    if (ok && gp != cabs) {
                         const int t = map[cabs];
-                        map[cabs] = map[cpos];
-                        map[cpos] = t;
+                        map[cabs] = map[gp];
+                        map[gp] = t;
                     }
                     if (!ok && q == 0) atomicCAS(info, 0, r0 + cabs + 1);
                 }
