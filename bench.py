@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--nrhs", type=int, default=4)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-configs", action="store_true", help="skip the other configurations' rates")
     return p.parse_args()
 
 
@@ -133,6 +134,130 @@ def cpu_solve_sample(n_sample: int, nrhs: int, seed: int = 1):
     t = time.perf_counter()
     o.solve(a, b)
     return time.perf_counter() - t, cores
+
+
+def config_rates(h, dmma_tf: float, bf16_tf: float) -> dict:
+    """The other configurations, measured after the headline (each timed once
+    after a warm-up call, wall clock around a synchronised call): FP64 LU +
+    solve, LLT (n = 8192, seed 1) and Householder QR (16384 x 4096: R alone
+    and with the full 16384 x 16384 Q); the M=N=K=16384 split-BF16 GEMM on
+    u*2^e entries (seed 3) with its error against FP64 on 256 sampled rows;
+    the Gaussian-process loss + gradient (Cholesky adjoint) at n = 8192."""
+    import ctypes as C
+
+    import torch
+
+    from mat_gb300.api import colmajor
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t, r
+
+    def rate(flops, t, peak):
+        return {"s": t, "gflops": flops / t / 1e9, "frac_of_peak": flops / t / 1e12 / peak}
+
+    out = {"fp64_peak_tflops": dmma_tf, "bf16_peak_tflops": bf16_tf}
+    n = 8192
+    A0 = colmajor(n, n)
+    h.fill_normal(A0, 1)
+    b = colmajor(n, 1)
+    h.fill_normal(b, 2)
+    A = A0.clone()
+    pos = torch.empty(n, dtype=torch.int32, device="cuda")
+
+    def lu():
+        A.copy_(A0)
+        return h.dgetrf(A, pos)
+
+    t_lu, _ = timed(lu)
+    t_sv, x = timed(lambda: h.dgetrs(A, pos, b))
+    r = b - A0 @ x
+    out["lu_8192"] = {"factor": rate(2 / 3 * n ** 3, t_lu, dmma_tf), "solve_s": t_sv,
+                      "residual_rel": float(r.norm() / (A0.norm() * x.norm()))}
+    S0 = colmajor(n, n)
+    h.gen_spd_gram(S0, 1)
+    S = S0.clone()
+
+    def llt():
+        S.copy_(S0)
+        return h.dpotrf(S)
+
+    t_llt, _ = timed(llt)
+    out["llt_8192"] = {"factor": rate(n ** 3 / 3, t_llt, dmma_tf)}
+    del A0, A, S0, S, b
+    m, k = 16384, 4096
+    Q0 = colmajor(m, k)
+    h.fill_normal(Q0, 1)
+    Qa = Q0.clone()
+    tau = torch.empty(k, dtype=torch.float64, device="cuda")
+    T = torch.empty(((k + 47) // 48) * 48 * 48, dtype=torch.float64, device="cuda")
+
+    def geqrf():
+        Qa.copy_(Q0)
+        h.check(h.lib.mg_dgeqrf(h.h, m, k, C.c_void_p(Qa.data_ptr()), m, C.c_void_p(tau.data_ptr()),
+                                C.c_void_p(T.data_ptr())), "mg_dgeqrf")
+
+    t_r, _ = timed(geqrf)
+    Qf, Rf = colmajor(m, m), colmajor(m, k)
+    t_q, _ = timed(lambda: h.dqr(Q0, Qf, Rf))
+    # flop counts: R 2mk^2 - 2k^3/3; full m x m Q from k reflectors (LAPACK dorgqr) 4m^2k - 4mk^2 + 4k^3/3
+    fr, fq = 2 * m * k * k - 2 / 3 * k ** 3, 4 * m * m * k - 4 * m * k * k + 4 / 3 * k ** 3
+    out["qr_16384x4096"] = {"r_factor": rate(fr, t_r, dmma_tf), "with_full_q": rate(fr + fq, t_q, dmma_tf)}
+    del Q0, Qa, Qf, Rf, tau, T
+    torch.cuda.empty_cache()
+    # split GEMM, entries u * 2^e
+    N = 16384
+    g = torch.Generator(device="cuda").manual_seed(3)
+
+    def wide():
+        u = torch.rand((N, N), generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+        e = torch.randint(-8, 9, (N, N), generator=g, device="cuda").to(torch.float64)
+        return (u * torch.exp2(e)).float().t().contiguous().t()
+
+    Ga, Gb = wide(), wide()
+    Gc = colmajor(N, N, dtype=torch.float32)
+    t_sg, _ = timed(lambda: h.sgemm_bf16x(Ga, Gb, Gc))
+    rows = torch.randperm(N, generator=g, device="cuda")[:256]
+    ref = Ga[rows].double() @ Gb.double()
+    d = Gc[rows].double() - ref
+    useful = 2 * N ** 3
+    out["split_gemm_16384"] = {"s": t_sg, "useful_tflops": useful / t_sg / 1e12,
+                               "bf16_pipe_tflops": 6 * useful / t_sg / 1e12,
+                               "frac_of_bf16_peak": 6 * useful / t_sg / 1e12 / bf16_tf,
+                               "max_rel_err": float(d.abs().max() / ref.abs().max()),
+                               "normwise_rel_err": float(d.norm() / ref.norm()),
+                               "error_sample": "256 random rows vs FP64 product of the same fp32 inputs"}
+    del Ga, Gb, Gc, ref, d
+    torch.cuda.empty_cache()
+    # FP64 tensor-core GEMM rate at 4096^3, for the comparison
+    Da, Db = colmajor(4096, 4096), colmajor(4096, 4096)
+    h.fill_uniform(Da, 0)
+    h.fill_uniform(Db, 1)
+    Dc = colmajor(4096, 4096)
+    t_dg, _ = timed(lambda: h.dgemm(Da, Db, Dc))
+    out["split_gemm_16384"]["fp64_gemm_tflops_4096"] = 2 * 4096 ** 3 / t_dg / 1e12
+    out["split_gemm_16384"]["speedup_vs_fp64_gemm"] = (useful / t_sg) / (2 * 4096 ** 3 / t_dg)
+    del Da, Db, Dc
+    # GP loss + gradient, FP64
+    gp = torch.Generator(device="cuda").manual_seed(5)
+    Xp = torch.rand((3, n), generator=gp, device="cuda", dtype=torch.float64).t()
+    y = torch.randn((1, n), generator=gp, device="cuda", dtype=torch.float64).t()
+    t_gp, (loss, dell, _) = timed(lambda: h.gp_loss_grad(Xp, y, 0.2))
+    out["gp_adjoint_8192_fp64"] = {"s": t_gp, "gflops": n ** 3 / t_gp / 1e9, "loss": loss, "dloss_dell": dell,
+                                   "flops_model": "n^3 (Cholesky n^3/3 + its adjoint 2n^3/3)"}
+    X32 = Xp.float().t().contiguous().t()
+    y32 = y.float().contiguous()
+    t_gp32, (loss32, dell32, _) = timed(lambda: h.sgp_loss_grad(X32, y32, 0.2))
+    out["gp_adjoint_8192_fp32"] = {"s": t_gp32, "gflops": n ** 3 / t_gp32 / 1e9, "loss": loss32,
+                                   "dloss_dell": dell32, "loss_rel_diff_vs_fp64": abs(loss32 - loss) / abs(loss),
+                                   "dell_rel_diff_vs_fp64": abs(dell32 - dell) / abs(dell),
+                                   "note": "inputs rounded to fp32; the difference is the fp32 conditioning of K"}
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_reference(args):
@@ -249,9 +374,12 @@ def run_ours(args):
     dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
     tensor = dom["flops"] > 0 and dom_name in ("gemm_bf16x",)
     traffic = None
-    tf = ROOT / "profiles" / "traffic_per_launch.json"
+    tf = ROOT / "profiles" / "traffic_per_launch.txt"
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get(dom_name)
+        for ln in tf.read_text().splitlines():
+            parts = ln.split()
+            if len(parts) == 2 and not ln.startswith("#") and parts[0] == dom_name:
+                traffic = float(parts[1])
     if tensor:
         achieved = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
         roof = {"kernel": dom_name, "bound": "tensor", "achieved": achieved, "peak": bf16s, "unit": "TFLOP/s",
@@ -304,6 +432,10 @@ def run_ours(args):
                "sample": f"oracle restatement of Mat Solve_direct, n={n_sample}, {nrhs} RHS, {cores} threads, "
                          f"scaled by (n/{n_sample})^3"}
 
+    configs = None
+    if rank == 0 and not args.no_configs:
+        configs = config_rates(h, max(dmma_tf, dfma_tf), bf16)
+
     if rank == 0:
         last = reps[-1]
         line = {
@@ -314,12 +446,12 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (A is 2 GiB), no flush"},
             "fp64_solve_s": fp64_s, "mixed_vs_fp64": (ms / 1e3) / fp64_s,
             "backward_error": last["backward_error"], "iterations": last["iterations"], "path": last["path"],
-            "forward_error_vs_fp64_solve": fwd,
+            "forward_error_vs_fp64_solve": fwd, "pivot_growth": last.get("pivot_growth"),
             "dgemm": {"config": "M=N=K=1024 fp64, uniform[-1,1) seeds 0/1", "ms": dgemm_ms, "tflops": dgemm_tf,
                       "fp64_dmma_peak_tflops": dmma_tf, "fp64_dfma_peak_tflops": dfma_tf,
                       "frac_of_fp64_peak": dgemm_tf / max(dmma_tf, dfma_tf)},
             "roofline": roof, "phases": phases, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": launches, "clocks": clocks,
+            "gpu_launches": launches, "clocks": clocks, "configs": configs,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

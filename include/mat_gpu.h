@@ -102,6 +102,12 @@ mg_status_t mg_fill_normal(mg_handle_t h, double* A, int rows, int cols, int ld,
 mg_status_t mg_dgemm(mg_handle_t h, int transA, int transB, int m, int n, int k,
                      double alpha, const double* A, int lda, const double* B, int ldb,
                      double beta, double* C, int ldc);
+/* FP32 form: Mat's operator* on MAT<float> (the same Mul/Mul.h:204-235
+ * template), C = alpha op(A) op(B) + beta C on the SIMT FP32 pipe (FFMA),
+ * 128 x 128 tiles; not bit-identical to Mat's float micro-kernel order.
+ * Also the GEMM of the FP32 Cholesky and its adjoint. */
+mg_status_t mg_sgemm(mg_handle_t h, int transA, int transB, int m, int n, int k, float alpha, const float* A,
+                     int lda, const float* B, int ldb, float beta, float* C, int ldc);
 
 /* ------------------------------------------------------------------- LU
  * In-place LU with partial pivoting, Mat's PLU (Mat-8.3.1/LU/__PLU.h:152-190,
@@ -185,6 +191,7 @@ typedef struct mg_ir_report {
     double factor_ms;      /* host wall time of the fp32 factorization */
     double refine_ms;      /* host wall time of the refinement loop */
     double history[32];    /* backward error before each correction */
+    double pivot_growth;   /* max |U(i,j)| / max |A(i,j)| of the fp32 LU (fp64 reduction) */
 } mg_ir_report;
 
 mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
@@ -226,6 +233,10 @@ mg_status_t mg_gen_spd_gram(mg_handle_t h, int n, double* S, int lds, uint64_t s
 mg_status_t mg_dpotrf(mg_handle_t h, int n, double* A, int lda, int* info);
 /* B := (L L^T)^{-1} B with L from mg_dpotrf (forward then back substitution). */
 mg_status_t mg_dpotrs(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* B, int ldb);
+/* FP32 Cholesky (LLT on MAT<float>, Mat-8.3.1/LU/__LLT.h:212-246): the same
+ * blocking (48), kernels and conventions as mg_dpotrf in fp32, trailing
+ * updates by mg_sgemm.  info / MG_NOT_SPD as mg_dpotrf.  Synchronises. */
+mg_status_t mg_spotrf(mg_handle_t h, int n, float* A, int lda, int* info);
 
 /* -------------------------------------------------------------------- QR
  * Mat's QR(A, Q, R, QR_Householder) (Mat-8.3.1/QR/QR.h:8-25, blocked
@@ -255,6 +266,9 @@ mg_status_t mg_dgeqrf(mg_handle_t h, int m, int n, double* A, int lda, double* t
  * intermediates); uses n*n doubles of handle workspace. */
 mg_status_t mg_dpotrf_backward(mg_handle_t h, int n, const double* L, int ldl, const double* Lbar,
                                int ldlbar, double* Abar, int ldabar);
+/* FP32 form of mg_dpotrf_backward (n*n floats of workspace). */
+mg_status_t mg_spotrf_backward(mg_handle_t h, int n, const float* L, int ldl, const float* Lbar, int ldlbar,
+                               float* Abar, int ldabar);
 /* X = op(L)^{-1} B with L lower (trans = 0: L, 1: L^T): given X and Xbar,
  * writes Bbar = op(L)^{-T} Xbar and accumulates into the lower triangle of
  * Lbar (-tril(Bbar X^T) or -tril(X Bbar^T)); Lbar's strict upper triangle is
@@ -279,6 +293,11 @@ mg_status_t mg_gen_rbf_kernel(mg_handle_t h, int n, const double* X, double ell,
 mg_status_t mg_gp_loss_grad(mg_handle_t h, int n, const double* X, double ell, double sigma2, double jitter,
                             const double* y, double* host_loss, double* host_dell, double* Kbar,
                             int ldkbar);
+/* FP32 form of mg_gp_loss_grad: X, y, K and every matrix step in fp32
+ * (mg_spotrf, fp32 solves, fp32 Cholesky adjoint); the scalar reductions
+ * (y^T K^-1 y, logdet, d loss / d ell) are summed in fp64. */
+mg_status_t mg_sgp_loss_grad(mg_handle_t h, int n, const float* X, float ell, float sigma2, float jitter,
+                             const float* y, double* host_loss, double* host_dell, float* Kbar, int ldkbar);
 
 /* Measures the FP64 peaks of this GPU with dependent-free FMA / DMMA loops
  * (TFLOP/s, counting an FMA as 2 flops).  Synchronises. */

@@ -146,6 +146,22 @@ inline MAT<double> operator*(const MAT<double>& A, const MAT<double>& B) {
     return C;
 }
 
+// C = A * B for MAT<float> (the same operator* template in Mat; FP32 SIMT GEMM).
+inline MAT<float> operator*(const MAT<float>& A, const MAT<float>& B) {
+    MAT<float> C(A.rows, B.cols);
+    const size_t sa = (size_t)A.rows * A.cols, sb = (size_t)B.rows * B.cols, sc = (size_t)C.rows * C.cols;
+    if (sc == 0) return C;
+    matgpu::Dev dA(sa * 4), dB(sb * 4), dC(sc * 4);
+    matgpu::h2d(dA.p, A.data, sa * 4);
+    matgpu::h2d(dB.p, B.data, sb * 4);
+    matgpu::check(mg_sgemm(matgpu::handle(), 0, 0, A.rows, B.cols, A.cols, 1.0f, (const float*)dA.p,
+                           A.rows > 1 ? A.rows : 1, (const float*)dB.p, B.rows > 1 ? B.rows : 1, 0.0f, (float*)dC.p,
+                           C.rows > 1 ? C.rows : 1),
+                  "mg_sgemm");
+    matgpu::d2h(C.data, dC.p, sc * 4);
+    return C;
+}
+
 template <typename t1, typename t2>
 void LU_init(MAT<t1>& A, MAT<t2>& L, MAT<t2>& U) {
     L.init(A.rows, A.rows);
@@ -199,6 +215,33 @@ inline void LLT(MAT<double>& A, MAT<double>& L) {
     int info = 0;
     matgpu::check(mg_dpotrf(matgpu::handle(), n, dA.d(), n, &info), "mg_dpotrf");
     matgpu::d2h(L.data, dA.p, (size_t)n * n * 8);
+}
+
+// LLT on MAT<float>.
+inline void LLT(MAT<float>& A, MAT<float>& L) {
+    const int n = A.rows;
+    L.init(n, n);
+    if (n == 0) return;
+    matgpu::Dev dA((size_t)n * n * 4);
+    matgpu::h2d(dA.p, A.data, (size_t)n * n * 4);
+    int info = 0;
+    matgpu::check(mg_spotrf(matgpu::handle(), n, (float*)dA.p, n, &info), "mg_spotrf");
+    matgpu::d2h(L.data, dA.p, (size_t)n * n * 4);
+}
+
+// QR(A, Q, R, QR_Householder): Q (m x m) and R (m x n) as Mat forms them
+// (blocked Householder).  Givens and Gram-Schmidt are not on the GPU.
+inline void QR(MAT<double>& A, MAT<double>& Q, MAT<double>& R, QR_type type) {
+    if (type != QR_Householder) throw std::runtime_error("mat_gpu: QR supports QR_Householder only");
+    const int m = A.rows, n = A.cols;
+    Q.init(m, m);
+    R.init(m, n);
+    if ((size_t)m * n == 0) return;
+    matgpu::Dev dA((size_t)m * n * 8), dQ((size_t)m * m * 8), dR((size_t)m * n * 8);
+    matgpu::h2d(dA.p, A.data, (size_t)m * n * 8);
+    matgpu::check(mg_dqr(matgpu::handle(), m, n, dA.d(), m, dQ.d(), m, dR.d(), m), "mg_dqr");
+    matgpu::d2h(Q.data, dQ.p, (size_t)m * m * 8);
+    matgpu::d2h(R.data, dR.p, (size_t)m * n * 8);
 }
 
 // X = A^{-1} B (A taken by value, as in Mat).

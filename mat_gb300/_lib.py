@@ -33,7 +33,7 @@ class IrOpts(C.Structure):
 class IrReport(C.Structure):
     _fields_ = [("iterations", C.c_int), ("path", C.c_int), ("info", C.c_int), ("reserved", C.c_int),
                 ("backward_error", C.c_double), ("anorm_inf", C.c_double), ("factor_ms", C.c_double),
-                ("refine_ms", C.c_double), ("history", C.c_double * 32)]
+                ("refine_ms", C.c_double), ("history", C.c_double * 32), ("pivot_growth", C.c_double)]
 
 # name -> (restype, argtypes); every symbol here is declared in include/mat_gpu.h
 SIGNATURES: dict[str, tuple] = {
@@ -54,6 +54,7 @@ SIGNATURES: dict[str, tuple] = {
     "mg_fill_uniform": (i32, [vp, vp, i32, i32, i32, u64, f64, f64, i32]),
     "mg_fill_normal": (i32, [vp, vp, i32, i32, i32, u64, i32]),
     "mg_dgemm": (i32, [vp, i32, i32, i32, i32, i32, f64, vp, i32, vp, i32, f64, vp, i32]),
+    "mg_sgemm": (i32, [vp, i32, i32, i32, i32, i32, f32, vp, i32, vp, i32, f32, vp, i32]),
     "mg_measure_fp64_peaks": (i32, [vp, pf64, pf64]),
     "mg_dgetrf": (i32, [vp, i32, i32, vp, i32, vp, pi32]),
     "mg_dgetrf_noalloc": (i32, [vp, i32, i32, vp, i32, vp, pi32]),
@@ -71,14 +72,17 @@ SIGNATURES: dict[str, tuple] = {
     "mg_profile_get": (i32, [vp, i32, C.POINTER(C.c_char_p), pf64, C.POINTER(C.c_longlong), pf64, pf64]),
     "mg_dpotrf": (i32, [vp, i32, vp, i32, pi32]),
     "mg_dpotrs": (i32, [vp, i32, i32, vp, i32, vp, i32]),
+    "mg_spotrf": (i32, [vp, i32, vp, i32, pi32]),
     "mg_dqr": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32]),
     "mg_dgeqrf": (i32, [vp, i32, i32, vp, i32, vp, vp]),
     "mg_dpotrf_backward": (i32, [vp, i32, vp, i32, vp, i32, vp, i32]),
+    "mg_spotrf_backward": (i32, [vp, i32, vp, i32, vp, i32, vp, i32]),
     "mg_dtrsm_backward": (i32, [vp, i32, i32, i32, vp, i32, vp, i32, vp, i32, vp, i32, vp, i32]),
     "mg_dlogdet_chol": (i32, [vp, i32, vp, i32, pf64]),
     "mg_dlogdet_chol_backward": (i32, [vp, i32, vp, i32, f64, vp, i32]),
     "mg_gen_rbf_kernel": (i32, [vp, i32, vp, f64, f64, f64, vp, i32]),
     "mg_gp_loss_grad": (i32, [vp, i32, vp, f64, f64, f64, vp, pf64, pf64, vp, i32]),
+    "mg_sgp_loss_grad": (i32, [vp, i32, vp, f32, f32, f32, vp, pf64, pf64, vp, i32]),
 }
 
 _lib = None

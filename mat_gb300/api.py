@@ -105,6 +105,18 @@ class Handle:
                                      _ptr(B), ld_of(B), beta, _ptr(C_), ld_of(C_)), "mg_dgemm")
         return C_
 
+    def sgemm(self, A, B, C_=None, alpha=1.0, beta=0.0, transA=False, transB=False):
+        """fp32 C = alpha op(A) op(B) + beta C (SIMT FFMA)."""
+        m = A.shape[1] if transA else A.shape[0]
+        k = A.shape[0] if transA else A.shape[1]
+        n = B.shape[0] if transB else B.shape[1]
+        if C_ is None:
+            C_ = colmajor(m, n, dtype=torch.float32, device=A.device)
+            beta = 0.0
+        self.check(self.lib.mg_sgemm(self.h, int(transA), int(transB), m, n, k, alpha, _ptr(A), ld_of(A), _ptr(B),
+                                     ld_of(B), beta, _ptr(C_), ld_of(C_)), "mg_sgemm")
+        return C_
+
     def sgemm_bf16x(self, A, B, C_=None, alpha=1.0, beta=0.0, nterms=3):
         """fp32 C = alpha A B + beta C on the BF16 tensor cores with `nterms` split terms."""
         m, k = A.shape
@@ -191,7 +203,8 @@ class Handle:
             self.check(st, "mg_dsgesv_ir")
         rep = dict(iterations=r.iterations, path=r.path, info=r.info, backward_error=r.backward_error,
                    anorm_inf=r.anorm_inf, factor_ms=r.factor_ms, refine_ms=r.refine_ms,
-                   history=[r.history[i] for i in range(min(32, r.iterations + 1))], status=st)
+                   history=[r.history[i] for i in range(min(32, r.iterations + 1))],
+                   pivot_growth=r.pivot_growth, status=st)
         return X, rep
 
     # ------------------------------------------------------------- generators
@@ -214,6 +227,15 @@ class Handle:
         st = self.lib.mg_dpotrf(self.h, n, _ptr(A), ld_of(A), C.byref(info))
         if check and st not in (0, 5):
             self.check(st, "mg_dpotrf")
+        return info.value
+
+    def spotrf(self, A: torch.Tensor, check=True):
+        """In-place fp32 LLT: lower triangle of A -> L, upper zeroed. Returns info."""
+        n = A.shape[0]
+        info = C.c_int(0)
+        st = self.lib.mg_spotrf(self.h, n, _ptr(A), ld_of(A), C.byref(info))
+        if check and st not in (0, 5):
+            self.check(st, "mg_spotrf")
         return info.value
 
     def dpotrs(self, L: torch.Tensor, B: torch.Tensor):
@@ -241,6 +263,14 @@ class Handle:
             Abar = colmajor(n, n, device=L.device)
         self.check(self.lib.mg_dpotrf_backward(self.h, n, _ptr(L), ld_of(L), _ptr(Lbar), ld_of(Lbar), _ptr(Abar),
                                                ld_of(Abar)), "mg_dpotrf_backward")
+        return Abar
+
+    def spotrf_backward(self, L, Lbar, Abar=None):
+        n = L.shape[0]
+        if Abar is None:
+            Abar = colmajor(n, n, dtype=torch.float32, device=L.device)
+        self.check(self.lib.mg_spotrf_backward(self.h, n, _ptr(L), ld_of(L), _ptr(Lbar), ld_of(Lbar), _ptr(Abar),
+                                               ld_of(Abar)), "mg_spotrf_backward")
         return Abar
 
     def dtrsm_backward(self, L, X, Xbar, Lbar, trans=False):
@@ -277,6 +307,16 @@ class Handle:
         self.check(self.lib.mg_gp_loss_grad(self.h, n, _ptr(X), ell, sigma2, jitter, _ptr(y), C.byref(loss),
                                             C.byref(dell), _ptr(Kb), ld_of(Kb) if Kb is not None else n),
                    "mg_gp_loss_grad")
+        return loss.value, dell.value, Kb
+
+    def sgp_loss_grad(self, X, y, ell, sigma2=1.0, jitter=1e-2, want_kbar=False):
+        """FP32 form of gp_loss_grad (X, y float32); loss and d/d ell summed in fp64."""
+        n = X.shape[0]
+        loss, dell = C.c_double(), C.c_double()
+        Kb = colmajor(n, n, dtype=torch.float32, device=X.device) if want_kbar else None
+        self.check(self.lib.mg_sgp_loss_grad(self.h, n, _ptr(X), ell, sigma2, jitter, _ptr(y), C.byref(loss),
+                                             C.byref(dell), _ptr(Kb), ld_of(Kb) if Kb is not None else n),
+                   "mg_sgp_loss_grad")
         return loss.value, dell.value, Kb
 
     # --------------------------------------------------------------- profile

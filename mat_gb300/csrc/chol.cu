@@ -12,7 +12,9 @@
 // bit-identical): the diagonal block by one CTA with one thread per row;
 // X := X L^{-T} by one thread per row of the panel (rows are independent);
 // the trailing update by the FP64 DMMA GEMM in its in-place C -= A B^T mode
-// restricted to tiles that meet the lower triangle.
+// restricted to tiles that meet the lower triangle.  The same kernels,
+// templated on the element type, give the FP32 Cholesky (mg_spotrf) with the
+// FP32 SIMT GEMM for the trailing update.
 #include "mg_internal.cuh"
 
 namespace {
@@ -23,8 +25,10 @@ constexpr int LLT2_MAX = 2 * LLT_BS;
 // Unblocked Cholesky of the k x k block at L (k <= 96), in place, lower part.
 // Column jj: t = 1/sqrt(L(jj,jj)); L(r,jj) *= t for r >= jj; then for
 // i > jj: L(r,i) = fma(L(r,jj), -L(i,jj), L(r,i)) for r >= i.
-__global__ void llt2_kernel(double* __restrict__ L, int ldl, int k, int col0, int* __restrict__ info) {
-    extern __shared__ double s[];  // column-major k x k with stride LLT2_MAX
+template <typename T>
+__global__ void llt2_kernel(T* __restrict__ L, int ldl, int k, int col0, int* __restrict__ info) {
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    T* s = reinterpret_cast<T*>(s_raw);  // column-major k x k with stride LLT2_MAX
     for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
         const int r = e % k, c = e / k;
         s[r + c * LLT2_MAX] = L[r + (size_t)c * ldl];
@@ -32,13 +36,13 @@ __global__ void llt2_kernel(double* __restrict__ L, int ldl, int k, int col0, in
     __syncthreads();
     const int r = threadIdx.x;
     for (int jj = 0; jj < k; ++jj) {
-        const double d = s[jj + jj * LLT2_MAX];
-        const double t = 1.0 / sqrt(d);
-        if (r == 0 && !(d > 0.0)) atomicCAS(info, 0, col0 + jj + 1);
+        const T d = s[jj + jj * LLT2_MAX];
+        const T t = T(1) / sqrt(d);
+        if (r == 0 && !(d > T(0))) atomicCAS(info, 0, col0 + jj + 1);
         if (r >= jj && r < k) s[r + jj * LLT2_MAX] = s[r + jj * LLT2_MAX] * t;
         __syncthreads();
         if (r > jj && r < k) {
-            const double lrj = s[r + jj * LLT2_MAX];
+            const T lrj = s[r + jj * LLT2_MAX];
             for (int i = jj + 1; i <= r; ++i) s[r + i * LLT2_MAX] = fma(lrj, -s[i + jj * LLT2_MAX], s[r + i * LLT2_MAX]);
         }
         __syncthreads();
@@ -51,18 +55,19 @@ __global__ void llt2_kernel(double* __restrict__ L, int ldl, int k, int col0, in
 
 // X (rows x k) := X * Lkk^{-T} (Mat's __Solve_direct_XLT), one thread per row:
 // for j: x_j *= 1/L(j,j); x_kk = fma(x_j, -L(kk,j), x_kk) for kk > j.
-__global__ void xlt_kernel(const double* __restrict__ Ld, int ldl, double* __restrict__ X, int ldx, int rows, int k) {
-    __shared__ double sl[LLT_BS * LLT_BS];
-    __shared__ double sinv[LLT_BS];
+template <typename T>
+__global__ void xlt_kernel(const T* __restrict__ Ld, int ldl, T* __restrict__ X, int ldx, int rows, int k) {
+    __shared__ T sl[LLT_BS * LLT_BS];
+    __shared__ T sinv[LLT_BS];
     for (int e = threadIdx.x; e < k * k; e += blockDim.x) sl[e] = Ld[(e % k) + (size_t)(e / k) * ldl];
     __syncthreads();
-    for (int j = threadIdx.x; j < k; j += blockDim.x) sinv[j] = 1.0 / sl[j + j * k];
+    for (int j = threadIdx.x; j < k; j += blockDim.x) sinv[j] = T(1) / sl[j + j * k];
     __syncthreads();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= rows) return;
-    double x[LLT_BS];
+    T x[LLT_BS];
 #pragma unroll
-    for (int j = 0; j < LLT_BS; ++j) x[j] = j < k ? X[r + (size_t)j * ldx] : 0.0;
+    for (int j = 0; j < LLT_BS; ++j) x[j] = j < k ? X[r + (size_t)j * ldx] : T(0);
 #pragma unroll
     for (int j = 0; j < LLT_BS; ++j) {
         if (j < k) {
@@ -77,11 +82,12 @@ __global__ void xlt_kernel(const double* __restrict__ Ld, int ldl, double* __res
         if (j < k) X[r + (size_t)j * ldx] = x[j];
 }
 
-__global__ void zero_upper_kernel(double* __restrict__ L, int ldl, int n) {
+template <typename T>
+__global__ void zero_upper_kernel(T* __restrict__ L, int ldl, int n) {
     const size_t total = (size_t)n * n;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const int r = (int)(e % n), c = (int)(e / n);
-        if (r < c) L[r + (size_t)c * ldl] = 0.0;
+        if (r < c) L[r + (size_t)c * ldl] = T(0);
     }
 }
 
@@ -90,7 +96,8 @@ __global__ void zero_upper_kernel(double* __restrict__ L, int ldl, int n) {
 // ascending (L z = b) or descending (L^T x = z) order.
 constexpr int CS_B = 64;
 
-__global__ void chol_fwd_diag_kernel(int n, int nrhs, const double* __restrict__ L, int ldl, double* __restrict__ X,
+template <typename T>
+__global__ void chol_fwd_diag_kernel(int n, int nrhs, const T* __restrict__ L, int ldl, T* __restrict__ X,
                                      int ldx, int b0, int b1) {
     const int bs = b1 - b0;
     for (int k = b0; k < b1; ++k) {
@@ -104,9 +111,10 @@ __global__ void chol_fwd_diag_kernel(int n, int nrhs, const double* __restrict__
     }
 }
 
-__global__ void chol_fwd_update_kernel(int n, int nrhs, const double* __restrict__ L, int ldl, double* __restrict__ X,
+template <typename T>
+__global__ void chol_fwd_update_kernel(int n, int nrhs, const T* __restrict__ L, int ldl, T* __restrict__ X,
                                        int ldx, int b0, int b1) {
-    __shared__ double xs[4][CS_B];
+    __shared__ T xs[4][CS_B];
     const int bs = b1 - b0;
     for (int j0 = 0; j0 < nrhs; j0 += 4) {
         const int nj = min(4, nrhs - j0);
@@ -114,10 +122,10 @@ __global__ void chol_fwd_update_kernel(int n, int nrhs, const double* __restrict
         for (int q = threadIdx.x; q < bs * nj; q += blockDim.x) xs[q / bs][q % bs] = X[b0 + q % bs + (size_t)(j0 + q / bs) * ldx];
         __syncthreads();
         for (int r = b1 + blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-            double acc[4];
+            T acc[4];
             for (int j = 0; j < nj; ++j) acc[j] = X[r + (size_t)(j0 + j) * ldx];
             for (int k = 0; k < bs; ++k) {
-                const double l = L[r + (size_t)(b0 + k) * ldl];
+                const T l = L[r + (size_t)(b0 + k) * ldl];
                 for (int j = 0; j < nj; ++j) acc[j] = fma(l, -xs[j][k], acc[j]);
             }
             for (int j = 0; j < nj; ++j) X[r + (size_t)(j0 + j) * ldx] = acc[j];
@@ -126,7 +134,8 @@ __global__ void chol_fwd_update_kernel(int n, int nrhs, const double* __restrict
 }
 
 // L^T x = z: row i of L^T is column i of L.
-__global__ void chol_bwd_diag_kernel(int n, int nrhs, const double* __restrict__ L, int ldl, double* __restrict__ X,
+template <typename T>
+__global__ void chol_bwd_diag_kernel(int n, int nrhs, const T* __restrict__ L, int ldl, T* __restrict__ X,
                                      int ldx, int b0, int b1) {
     const int bs = b1 - b0;
     for (int k = b1 - 1; k >= b0; --k) {
@@ -140,10 +149,11 @@ __global__ void chol_bwd_diag_kernel(int n, int nrhs, const double* __restrict__
     }
 }
 
-__global__ void chol_bwd_update_kernel(int n, int nrhs, const double* __restrict__ L, int ldl, double* __restrict__ X,
+template <typename T>
+__global__ void chol_bwd_update_kernel(int n, int nrhs, const T* __restrict__ L, int ldl, T* __restrict__ X,
                                        int ldx, int b0, int b1) {
     // rows i < b0: x_i -= sum_{k in block} L(k,i) x_k  (k descending); one warp per row i
-    __shared__ double xs[4][CS_B];
+    __shared__ T xs[4][CS_B];
     const int bs = b1 - b0;
     const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
     for (int j0 = 0; j0 < nrhs; j0 += 4) {
@@ -153,8 +163,8 @@ __global__ void chol_bwd_update_kernel(int n, int nrhs, const double* __restrict
         __syncthreads();
         for (int i = blockIdx.x * warps + (threadIdx.x >> 5); i < b0; i += gridDim.x * warps) {
             if (lane < nj) {
-                double acc = X[i + (size_t)(j0 + lane) * ldx];
-                const double* lp = L + (size_t)i * ldl + b0;  // L(b0.., i): contiguous in column i
+                T acc = X[i + (size_t)(j0 + lane) * ldx];
+                const T* lp = L + (size_t)i * ldl + b0;  // L(b0.., i): contiguous in column i
                 for (int k = bs - 1; k >= 0; --k) acc = fma(lp[k], -xs[lane][k], acc);
                 X[i + (size_t)(j0 + lane) * ldx] = acc;
             }
@@ -166,85 +176,98 @@ __global__ void chol_bwd_update_kernel(int n, int nrhs, const double* __restrict
 
 namespace mg {
 
-mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out) {
+template <typename T>
+mg_status_t potrf_impl(mg_handle_t h, int n, T* L, int ldl, int* info_out) {
     if (info_out) *info_out = 0;
     if (n == 0) return MG_OK;
     MG_TRY(ensure_hws(h, 64));
     int* dinfo = h->status;
     MG_CHECK_CUDA(h, cudaMemsetAsync(dinfo, 0, sizeof(int), h->stream));
     cudaStream_t st = h->stream;
-    const size_t s2 = (size_t)LLT2_MAX * LLT2_MAX * sizeof(double);
-    MG_CHECK_CUDA(h, cudaFuncSetAttribute(llt2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
+    const size_t s2 = (size_t)LLT2_MAX * LLT2_MAX * sizeof(T);
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(llt2_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
     if (n <= 2 * LLT_BS) {
-        llt2_kernel<<<1, 128, s2, st>>>(L, ldl, n, 0, dinfo);
+        llt2_kernel<T><<<1, 128, s2, st>>>(L, ldl, n, 0, dinfo);
         MG_TRY(post_launch(h, "llt2_kernel"));
     } else {
         for (int j = 0; j < n; j += LLT_BS) {
             const int nb = n - j < LLT_BS ? n - j : LLT_BS;
-            double* D = L + j + (size_t)j * ldl;
-            llt2_kernel<<<1, 128, s2, st>>>(D, ldl, nb, j, dinfo);
+            T* D = L + j + (size_t)j * ldl;
+            llt2_kernel<T><<<1, 128, s2, st>>>(D, ldl, nb, j, dinfo);
             MG_TRY(post_launch(h, "llt2_kernel"));
             if (j + LLT_BS < n) {
                 const int rows = n - (j + LLT_BS);
-                double* P = L + (j + LLT_BS) + (size_t)j * ldl;
-                xlt_kernel<<<(rows + 127) / 128, 128, 0, st>>>(D, ldl, P, ldl, rows, LLT_BS);
+                T* P = L + (j + LLT_BS) + (size_t)j * ldl;
+                xlt_kernel<T><<<(rows + 127) / 128, 128, 0, st>>>(D, ldl, P, ldl, rows, LLT_BS);
                 MG_TRY(post_launch(h, "xlt_kernel"));
                 // C(i.., i..) -= P P^T on the trailing matrix, lower tiles only
-                MG_TRY(dgemm_launch(h, 0, 1, rows, rows, LLT_BS, -1.0, P, ldl, P, ldl, 1.0,
-                                    L + (j + LLT_BS) + (size_t)(j + LLT_BS) * ldl, ldl, 1));
+                MG_TRY(gemm_of(h, 0, 1, rows, rows, LLT_BS, T(-1), P, ldl, P, ldl, T(1),
+                               L + (j + LLT_BS) + (size_t)(j + LLT_BS) * ldl, ldl, 1));
             }
         }
     }
-    zero_upper_kernel<<<h->num_sms * 8, 256, 0, st>>>(L, ldl, n);
+    zero_upper_kernel<T><<<h->num_sms * 8, 256, 0, st>>>(L, ldl, n);
     MG_TRY(post_launch(h, "zero_upper_kernel"));
     int* hw = (int*)h->hws;
     MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
     MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
     if (info_out) *info_out = hw[0];
-    if (hw[0]) return fail(h, MG_NOT_SPD, "dpotrf: non-positive pivot at column %d", hw[0]);
+    if (hw[0]) return fail(h, MG_NOT_SPD, "potrf: non-positive pivot at column %d", hw[0]);
     return MG_OK;
+}
+template mg_status_t potrf_impl<double>(mg_handle_t, int, double*, int, int*);
+template mg_status_t potrf_impl<float>(mg_handle_t, int, float*, int, int*);
+
+mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out) {
+    return potrf_impl<double>(h, n, L, ldl, info_out);
 }
 
 // L x = b (forward substitution), in place on X.
-mg_status_t chol_lower_solve(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* X, int ldx) {
+template <typename T>
+mg_status_t chol_lower_solve(mg_handle_t h, int n, int nrhs, const T* L, int ldl, T* X, int ldx) {
     if (n == 0 || nrhs == 0) return MG_OK;
     cudaStream_t st = h->stream;
     for (int b0 = 0; b0 < n; b0 += CS_B) {
         const int b1 = b0 + CS_B < n ? b0 + CS_B : n;
-        chol_fwd_diag_kernel<<<1, 256, 0, st>>>(n, nrhs, L, ldl, X, ldx, b0, b1);
+        chol_fwd_diag_kernel<T><<<1, 256, 0, st>>>(n, nrhs, L, ldl, X, ldx, b0, b1);
         MG_TRY(post_launch(h, "chol_fwd_diag_kernel"));
         if (b1 < n) {
             int blocks = (n - b1 + 127) / 128;
             if (blocks > h->num_sms) blocks = h->num_sms;
-            chol_fwd_update_kernel<<<blocks, 128, 0, st>>>(n, nrhs, L, ldl, X, ldx, b0, b1);
+            chol_fwd_update_kernel<T><<<blocks, 128, 0, st>>>(n, nrhs, L, ldl, X, ldx, b0, b1);
             MG_TRY(post_launch(h, "chol_fwd_update_kernel"));
         }
     }
     return MG_OK;
 }
+template mg_status_t chol_lower_solve<double>(mg_handle_t, int, int, const double*, int, double*, int);
+template mg_status_t chol_lower_solve<float>(mg_handle_t, int, int, const float*, int, float*, int);
 
 // L^T x = b (back substitution), in place on X.
-mg_status_t chol_lower_t_solve(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* X, int ldx) {
+template <typename T>
+mg_status_t chol_lower_t_solve(mg_handle_t h, int n, int nrhs, const T* L, int ldl, T* X, int ldx) {
     if (n == 0 || nrhs == 0) return MG_OK;
     cudaStream_t st = h->stream;
     const int last = ((n - 1) / CS_B) * CS_B;
     for (int b0 = last; b0 >= 0; b0 -= CS_B) {
         const int b1 = b0 + CS_B < n ? b0 + CS_B : n;
-        chol_bwd_diag_kernel<<<1, 256, 0, st>>>(n, nrhs, L, ldl, X, ldx, b0, b1);
+        chol_bwd_diag_kernel<T><<<1, 256, 0, st>>>(n, nrhs, L, ldl, X, ldx, b0, b1);
         MG_TRY(post_launch(h, "chol_bwd_diag_kernel"));
         if (b0 > 0) {
             int blocks = (b0 + 7) / 8;
             if (blocks > h->num_sms * 4) blocks = h->num_sms * 4;
-            chol_bwd_update_kernel<<<blocks, 256, 0, st>>>(n, nrhs, L, ldl, X, ldx, b0, b1);
+            chol_bwd_update_kernel<T><<<blocks, 256, 0, st>>>(n, nrhs, L, ldl, X, ldx, b0, b1);
             MG_TRY(post_launch(h, "chol_bwd_update_kernel"));
         }
     }
     return MG_OK;
 }
+template mg_status_t chol_lower_t_solve<double>(mg_handle_t, int, int, const double*, int, double*, int);
+template mg_status_t chol_lower_t_solve<float>(mg_handle_t, int, int, const float*, int, float*, int);
 
 mg_status_t dpotrs_impl(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* X, int ldx) {
-    MG_TRY(chol_lower_solve(h, n, nrhs, L, ldl, X, ldx));
-    return chol_lower_t_solve(h, n, nrhs, L, ldl, X, ldx);
+    MG_TRY(chol_lower_solve<double>(h, n, nrhs, L, ldl, X, ldx));
+    return chol_lower_t_solve<double>(h, n, nrhs, L, ldl, X, ldx);
 }
 
 }  // namespace mg
@@ -262,6 +285,12 @@ mg_status_t mg_dpotrs(mg_handle_t h, int n, int nrhs, const double* L, int ldl, 
     if (n < 0 || nrhs < 0 || ldl < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1) || ((size_t)n * nrhs && (!L || !B)))
         return mg::fail(h, MG_ERR_ARG, "mg_dpotrs: bad arguments");
     return mg::dpotrs_impl(h, n, nrhs, L, ldl, B, ldb);
+}
+
+mg_status_t mg_spotrf(mg_handle_t h, int n, float* A, int lda, int* info) {
+    if (!h) return MG_ERR_ARG;
+    if (n < 0 || lda < (n > 1 ? n : 1) || (n && !A)) return mg::fail(h, MG_ERR_ARG, "mg_spotrf: bad arguments");
+    return mg::potrf_impl<float>(h, n, A, lda, info);
 }
 
 }  // extern "C"

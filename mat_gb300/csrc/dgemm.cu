@@ -22,6 +22,8 @@
 // of Mat's micro-kernels, so results are bit-identical to Mat's operator*.
 // K is therefore never split across CTAs; small problems use a 32x32 tile
 // (one warp, up to 7 CTAs per SM) so the GPU is still filled.
+#include <algorithm>
+
 #include "mg_internal.cuh"
 
 namespace {
@@ -239,10 +241,14 @@ cudaError_t dispatch(cudaStream_t st, int ta, int tb, int mode, int m, int n, in
 #undef MG_MODE
 }
 
-// Fraction of the machine the grid keeps busy when every SM holds `slots` CTAs.
-double fill_efficiency(long long tiles, long long slots) {
-    const long long waves = (tiles + slots - 1) / slots;
-    return (double)tiles / (double)(waves * slots);
+// Output area the busiest SM computes when `tiles` tiles of bm x bn are
+// spread over the SMs.  On GB300 one warp with a few independent DMMA
+// fragments already keeps an SM's FP64 pipe busy (the pipe retires about one
+// m16n8k4 DMMA per ~290 cycles), so the time of a launch follows this area,
+// not the tile's data reuse: thin operands (M = 48 in the QR and Cholesky
+// adjoint updates) need small tiles to reach every SM.
+double busiest_sm_area(long long tiles, int num_sms, int bm, int bn) {
+    return (double)((tiles + num_sms - 1) / num_sms) * bm * bn;
 }
 
 // Scales C by beta (K == 0 or alpha == 0 cases).
@@ -280,13 +286,20 @@ mg_status_t dgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, in
         // Cholesky trailing update: C -= A * B^T on lower tiles only
         if (transA || !transB || mode != 1)
             return fail(h, MG_ERR_UNSUPPORTED, "dgemm_launch: triangular mode is C -= A*B^T only");
-        e = launch_t<Big, 0, 1, 1, 1>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+        auto lower_tiles = [&](int bm, int bn) {  // tiles meeting the lower triangle of the m x n block
+            long long c = 0;
+            for (int r0 = 0; r0 < m; r0 += bm) c += std::min<long long>((n + bn - 1) / bn, (r0 + bm - 1) / bn + 1);
+            return c;
+        };
+        if (busiest_sm_area(lower_tiles(Big::BM, Big::BN), h->num_sms, Big::BM, Big::BN) <=
+            busiest_sm_area(lower_tiles(Small::BM, Small::BN), h->num_sms, Small::BM, Small::BN))
+            e = launch_t<Big, 0, 1, 1, 1>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+        else
+            e = launch_t<Small, 0, 1, 1, 1>(st, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
     } else {
         const long long tb = (long long)((m + Big::BM - 1) / Big::BM) * ((n + Big::BN - 1) / Big::BN);
         const long long ts = (long long)((m + Small::BM - 1) / Small::BM) * ((n + Small::BN - 1) / Small::BN);
-        // one 8-warp CTA per SM for the big tile; seven 1-warp CTAs per SM for the small one
-        const double eb = fill_efficiency(tb, h->num_sms), es = fill_efficiency(ts, 7LL * h->num_sms);
-        if (eb >= es - 0.03)
+        if (busiest_sm_area(tb, h->num_sms, Big::BM, Big::BN) <= busiest_sm_area(ts, h->num_sms, Small::BM, Small::BN))
             e = dispatch<Big>(st, transA, transB, mode, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
         else
             e = dispatch<Small>(st, transA, transB, mode, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);

@@ -268,58 +268,50 @@ __global__ void trsm_llnu_kernel(int k, int n, const T* __restrict__ L, int ldl,
     for (int i = 0; i < k; ++i) X[i + (size_t)col * ldx] = sx[i * nt + t];
 }
 
-// Inverse of the unit-lower k x k block L (k <= 128) into Linv (ld k) by
-// recursive doubling in shared memory: the 16 x 16 diagonal blocks are
-// inverted by substitution (one thread per column), then pairs of adjacent
-// inverted blocks are joined, inv([A 0; C B]) = [A^-1 0; -B^-1 C A^-1 B^-1],
-// for block sizes 16, 32 and 64.
+// Inverse of the unit-lower k x k block L (k <= 128) into Linv (ld ldinv,
+// zeros above the diagonal): one warp per column j of the inverse (grid of
+// ceil(k/8) CTAs of 8 warps), L staged in shared memory.  Column j is the
+// forward substitution of e_j, x_i -= L(i,kk) x_kk for i > kk, kk = j..k-2,
+// each lane holding rows lane, lane+32, lane+64, lane+96; x_kk reaches the
+// other lanes by one shuffle per step.
 constexpr int INV_LD = 128;
 
 __global__ void __launch_bounds__(256) inv_unit_lower_kernel(const float* __restrict__ L, int ldl, int k,
                                                                float* __restrict__ Linv, int ldinv) {
-    extern __shared__ float sm[];
-    float* sl = sm;                     // L, ld INV_LD
-    float* si = sm + INV_LD * INV_LD;   // inverse, ld INV_LD
-    float* tp = si + INV_LD * INV_LD;   // 64 x 64 scratch
-    for (int e = threadIdx.x; e < INV_LD * INV_LD; e += blockDim.x) {
-        const int r = e % INV_LD, c = e / INV_LD;
-        sl[e] = (r < k && c < k && r > c) ? L[r + (size_t)c * ldl] : 0.f;
-        si[e] = 0.f;
+    extern __shared__ float sl[];  // L, ld INV_LD
+    {  // 64 loads per thread issued together (an in-order load->store loop would wait on each)
+        float t[INV_LD * INV_LD / 256];
+#pragma unroll
+        for (int q = 0; q < INV_LD * INV_LD / 256; ++q) {
+            const int e = threadIdx.x + q * 256, r = e & (INV_LD - 1), c = e / INV_LD;
+            t[q] = (r < k && c < k) ? L[r + (size_t)c * ldl] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < INV_LD * INV_LD / 256; ++q) sl[threadIdx.x + q * 256] = t[q];
     }
     __syncthreads();
-    // 16 x 16 diagonal blocks
-    for (int c = threadIdx.x; c < k; c += blockDim.x) {
-        const int end = min(k, (c / 16) * 16 + 16);
-        float* z = si + c * INV_LD;
-        z[c] = 1.f;
-        for (int i = c + 1; i < end; ++i) {
-            float sum = 0.f;
-            for (int q = c; q < i; ++q) sum = fmaf(sl[i + q * INV_LD], z[q], sum);
-            z[i] = -sum;
+    const int lane = threadIdx.x & 31;
+    const int j = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (j >= k) return;
+    float x[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) x[t] = lane + 32 * t == j ? 1.f : 0.f;
+    for (int kk = j; kk < k - 1; ++kk) {
+        const int sk = kk >> 5;
+        const float mine = sk == 0 ? x[0] : sk == 1 ? x[1] : sk == 2 ? x[2] : x[3];
+        const float xk = __shfl_sync(0xffffffffu, mine, kk & 31);
+        const float* lc = sl + kk * INV_LD;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int i = lane + 32 * t;
+            if (i > kk && i < k) x[t] = fmaf(-lc[i], xk, x[t]);
         }
     }
-    __syncthreads();
-    for (int s = 16; s < k; s *= 2) {
-        // every pair (p, p+s) with p multiple of 2s: T = C A^-1, then X21 = -B^-1 T
-        for (int p = 0; p + s < k; p += 2 * s) {
-            const int nb = min(s, k - (p + s));  // rows of the lower block (may be partial)
-            for (int e = threadIdx.x; e < nb * s; e += blockDim.x) {
-                const int r = e % nb, c = e / nb;  // T(r, c) = sum_q C(r, q) Ainv(q, c), q >= c
-                float sum = 0.f;
-                for (int q = c; q < s; ++q) sum = fmaf(sl[(p + s + r) + (p + q) * INV_LD], si[(p + q) + (p + c) * INV_LD], sum);
-                tp[r + c * 64] = sum;
-            }
-            __syncthreads();
-            for (int e = threadIdx.x; e < nb * s; e += blockDim.x) {
-                const int r = e % nb, c = e / nb;  // X21(r, c) = -sum_q Binv(r, q) T(q, c), q <= r
-                float sum = 0.f;
-                for (int q = 0; q <= r; ++q) sum = fmaf(si[(p + s + r) + (p + s + q) * INV_LD], tp[q + c * 64], sum);
-                si[(p + s + r) + (p + c) * INV_LD] = -sum;
-            }
-            __syncthreads();
-        }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const int i = lane + 32 * t;
+        if (i < k) Linv[i + (size_t)j * ldinv] = x[t];
     }
-    for (int e = threadIdx.x; e < k * k; e += blockDim.x) Linv[(e % k) + (size_t)(e / k) * ldinv] = si[(e % k) + (e / k) * INV_LD];
 }
 
 __global__ void iota_kernel(int* p, int n) {
@@ -642,7 +634,7 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
     MG_CHECK_CUDA(h, cudaMemsetAsync(xchg, 0, 256, S));
     iota_kernel<<<(n + 255) / 256, 256, 0, S>>>(pos, n);
     MG_TRY(post_launch(h, "iota_kernel"));
-    const size_t ism = (2 * (size_t)INV_LD * INV_LD + 64 * 64) * sizeof(float);
+    const size_t ism = (size_t)INV_LD * INV_LD * sizeof(float);
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_unit_lower_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism));
     void* const splitT = (char*)tri + align_up((size_t)nb * nb * sizeof(float), 1024);
     void* const splitL[2] = {splitA, splitA2};
@@ -658,7 +650,7 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
         const int ldo = Linv_all ? nb : w;
         if (Linv_all || r + w < n) {
             ProfScope prof(h, "trsm_f32", 2.0 * w * w * (double)w / 3.0, 8.0 * w * (double)w);
-            inv_unit_lower_kernel<<<1, 256, ism, h->stream>>>(A + r + (size_t)r * lda, lda, w, Lout, ldo);
+            inv_unit_lower_kernel<<<(w + 7) / 8, 256, ism, h->stream>>>(A + r + (size_t)r * lda, lda, w, Lout, ldo);
             MG_TRY(post_launch(h, "inv_unit_lower_kernel"));
         }
         if (r + w < n) {

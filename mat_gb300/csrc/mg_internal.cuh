@@ -94,8 +94,25 @@ mg_status_t dgetrs_impl(mg_handle_t h, int n, int nrhs, const double* LU, int ld
 
 // Cholesky (chol.cu).
 mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out);
-mg_status_t chol_lower_solve(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* X, int ldx);
-mg_status_t chol_lower_t_solve(mg_handle_t h, int n, int nrhs, const double* L, int ldl, double* X, int ldx);
+template <typename T>
+mg_status_t potrf_impl(mg_handle_t h, int n, T* L, int ldl, int* info_out);  // double, float
+template <typename T>
+mg_status_t chol_lower_solve(mg_handle_t h, int n, int nrhs, const T* L, int ldl, T* X, int ldx);
+template <typename T>
+mg_status_t chol_lower_t_solve(mg_handle_t h, int n, int nrhs, const T* L, int ldl, T* X, int ldx);
+
+// FP32 SIMT GEMM (sgemm.cu), the same interface as dgemm_launch.
+mg_status_t sgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, int k, float alpha, const float* A,
+                         int lda, const float* B, int ldb, float beta, float* C, int ldc, int tri);
+// GEMM of the element type: FP64 DMMA kernel, or the FP32 SIMT kernel.
+inline mg_status_t gemm_of(mg_handle_t h, int ta, int tb, int m, int n, int k, double alpha, const double* A,
+                           int lda, const double* B, int ldb, double beta, double* C, int ldc, int tri) {
+    return dgemm_launch(h, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri);
+}
+inline mg_status_t gemm_of(mg_handle_t h, int ta, int tb, int m, int n, int k, float alpha, const float* A, int lda,
+                           const float* B, int ldb, float beta, float* C, int ldc, int tri) {
+    return sgemm_launch(h, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri);
+}
 
 // Split-BF16 tensor-core GEMM pieces (gemm_bf16x.cu).
 size_t bf16x_split_bytes(int rows, int K, int np);

@@ -39,18 +39,41 @@ __global__ void d2s_kernel(const double* __restrict__ A, int lda, int n, float* 
     }
 }
 
-// partial[kc][i] = sum_{k in chunk kc} |A(i,k)|  (row sums of |A|)
-__global__ void absrow_partial_kernel(const double* __restrict__ A, int lda, int n, double* __restrict__ partial) {
+__device__ __forceinline__ void atomic_max_nonneg(double* addr, double v);
+
+// partial[kc][i] = sum_{k in chunk kc} |A(i,k)|  (row sums of |A|); also
+// *amax = max |A(i,k)| (for the pivot-growth factor)
+__global__ void absrow_partial_kernel(const double* __restrict__ A, int lda, int n, double* __restrict__ partial,
+                                      double* __restrict__ amax) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int k0 = blockIdx.y * RES_KCHUNK, k1 = min(n, k0 + RES_KCHUNK);
-    if (i >= n) return;
-    double s = 0.0;
-    for (int k = k0; k < k1; ++k) s += fabs(A[i + (size_t)k * lda]);
-    partial[(size_t)blockIdx.y * n + i] = s;
+    double s = 0.0, mx = 0.0;
+    if (i < n)
+        for (int k = k0; k < k1; ++k) {
+            const double a = fabs(A[i + (size_t)k * lda]);
+            s += a;
+            mx = fmax(mx, a);
+        }
+    if (i < n) partial[(size_t)blockIdx.y * n + i] = s;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(amax, mx);
+}
+
+// *umax = max |U(i,j)| over the upper triangle of the packed fp32 LU (one CTA
+// per column), reduced in fp64
+__global__ void absmax_upper_kernel(const float* __restrict__ LU, int n, double* __restrict__ umax) {
+    const int c = blockIdx.x;
+    float mx = 0.f;
+    for (int r = threadIdx.x; r <= c; r += blockDim.x) mx = fmaxf(mx, fabsf(LU[r + (size_t)c * n]));
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(umax, (double)mx);
 }
 
 __device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
-    // for non-negative doubles the bit patterns order like the values
+    // for non-negative doubles the bit patterns order like the values (NaN: skipped)
+    if (!(v >= 0.0)) return;
     atomicMax((unsigned long long*)addr, (unsigned long long)__double_as_longlong(v));
 }
 
@@ -280,9 +303,14 @@ __global__ void __launch_bounds__(256) trsv_flow_kernel(const float* __restrict_
     const int r0 = me * IR_BLOCK, rows = min(IR_BLOCK, n - r0);
     const int r = threadIdx.x & (IR_BLOCK - 1), hf = threadIdx.x >> 7;
     const int k0 = hf * (IR_BLOCK / 2);
-    {  // own diagonal-block inverse, needed last
-        const float* src = Dinv + (size_t)me * IR_BLOCK * IR_BLOCK;
-        for (int e = threadIdx.x; e < IR_BLOCK * IR_BLOCK; e += blockDim.x) sdinv[e] = src[e];
+    {  // own diagonal-block inverse, needed last (16-byte loads, all in flight together)
+        const float4* src = reinterpret_cast<const float4*>(Dinv + (size_t)me * IR_BLOCK * IR_BLOCK);
+        float4 t[IR_BLOCK * IR_BLOCK / 4 / 256];
+#pragma unroll
+        for (int q = 0; q < IR_BLOCK * IR_BLOCK / 4 / 256; ++q) t[q] = src[threadIdx.x + q * 256];
+#pragma unroll
+        for (int q = 0; q < IR_BLOCK * IR_BLOCK / 4 / 256; ++q)
+            reinterpret_cast<float4*>(sdinv)[threadIdx.x + q * 256] = t[q];
     }
     float acc[NR];
 #pragma unroll
@@ -556,7 +584,7 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     mg::ProfScope* setup = new mg::ProfScope(h, "ir_setup", 0.0, 12.0 * n * (double)n);
     MG_CHECK_CUDA(h, cudaMemsetAsync(w.gemm_err, 0, 64, st));
     MG_CHECK_CUDA(h, cudaMemsetAsync(w.norms, 0, 64 * sizeof(double), st));
-    absrow_partial_kernel<<<dim3((n + 255) / 256, kch), 256, 0, st>>>(A, lda, n, w.partial);
+    absrow_partial_kernel<<<dim3((n + 255) / 256, kch), 256, 0, st>>>(A, lda, n, w.partial, w.norms + 17);
     MG_TRY(mg::post_launch(h, "absrow_partial_kernel"));
     absrow_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kch, n, w.norms + 16);
     MG_TRY(mg::post_launch(h, "absrow_reduce_kernel"));
@@ -570,6 +598,8 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
                                      w.tri, w.Linv, w.gemm_err, &info);
     if (s != MG_OK && s != MG_SINGULAR) return s;
     r.info = info;
+    absmax_upper_kernel<<<n, 256, 0, st>>>(w.A32, n, w.norms + 18);
+    MG_TRY(mg::post_launch(h, "absmax_upper_kernel"));
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -635,6 +665,7 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
             eta = std::max(eta, e);
         }
         r.anorm_inf = anorm;
+        r.pivot_growth = hn[17] > 0 ? hn[18] / hn[17] : 0.0;
         r.backward_error = eta;
         if (it < 32) r.history[it] = eta;
         r.iterations = it;

@@ -319,6 +319,10 @@ static mg_status_t dgeqrf_blocked(mg_handle_t h, int m, int n, double* R, int ld
 }
 
 // Q (m x m) = H_0 H_1 ... H_{k-1}, accumulated backwards from the identity.
+// When block j is applied, Q differs from the identity only in rows and
+// columns >= j, so the block update is restricted to Q(j:m, j:m): the
+// skipped columns would receive exact zeros (fused chains over zero
+// entries), so the result is the one of the full-width update.
 static mg_status_t dorgqr_full(mg_handle_t h, int m, int n, const double* R, int ldr, double* Q, int ldq, QrWs& w) {
     const int k = m < n ? m : n;
     cudaStream_t st = h->stream;
@@ -331,13 +335,14 @@ static mg_status_t dorgqr_full(mg_handle_t h, int m, int n, const double* R, int
         const int hh = m - j;
         const double* P = R + j + (size_t)j * ldr;
         const double* Tj = w.T + (size_t)(j / QR_BS) * QR_BS * QR_BS;
-        double* Qj = Q + j;
+        double* Qj = Q + j + (size_t)j * ldq;
+        const int nq = m - j;
         qr_expand_v_kernel<<<grid_cap(h, (size_t)hh * b), 256, 0, st>>>(P, ldr, hh, b, w.V);
         MG_TRY(post_launch(h, "qr_expand_v_kernel"));
-        // W = V^T Q_j; W2 = T W; Q_j -= V W2
-        MG_TRY(dgemm_launch(h, 1, 0, b, m, hh, 1.0, w.V, hh, Qj, ldq, 0.0, w.W, b, 0));
-        MG_TRY(dgemm_launch(h, 0, 0, b, m, b, 1.0, Tj, b, w.W, b, 0.0, w.W2, b, 0));
-        MG_TRY(dgemm_launch(h, 0, 0, hh, m, b, -1.0, w.V, hh, w.W2, b, 1.0, Qj, ldq, 0));
+        // W = V^T Q_j; W2 = T W; Q_j -= V W2   (Q_j = Q(j:m, j:m))
+        MG_TRY(dgemm_launch(h, 1, 0, b, nq, hh, 1.0, w.V, hh, Qj, ldq, 0.0, w.W, b, 0));
+        MG_TRY(dgemm_launch(h, 0, 0, b, nq, b, 1.0, Tj, b, w.W, b, 0.0, w.W2, b, 0));
+        MG_TRY(dgemm_launch(h, 0, 0, hh, nq, b, -1.0, w.V, hh, w.W2, b, 1.0, Qj, ldq, 0));
     }
     return MG_OK;
 }

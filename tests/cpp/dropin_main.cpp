@@ -58,6 +58,20 @@ int main(int argc, char** argv) {
     MAT<double> Lc(200, 200);
     LLT(S, Lc);
     dump("llt", Lc.data, (size_t)200 * 200);
+    // QR(A, Q, R, QR_Householder), blocked path (min(m, n) > 96)
+    MAT<double> Aq(300, 200), Q, R;
+    mg_host_fill_normal(Aq.data, 300, 200, 300, 7, 1);
+    QR_init(Aq, Q, R);
+    QR(Aq, Q, R, QR_Householder);
+    dump("qr_Q", Q.data, (size_t)300 * 300);
+    dump("qr_R", R.data, (size_t)300 * 200);
+
+    // operator* on MAT<float>
+    MAT<float> Fa(70, 50), Fb(50, 60);
+    for (int i = 0; i < 70 * 50; ++i) Fa.data[i] = (float)A.data[i];
+    for (int i = 0; i < 50 * 60; ++i) Fb.data[i] = (float)B.data[i];
+    MAT<float> Fc = Fa * Fb;
+    dump("sgemm", Fc.data, (size_t)70 * 60);
     std::printf("ok\n");
     return 0;
 }

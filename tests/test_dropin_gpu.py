@@ -63,3 +63,18 @@ def test_solve_and_det(outputs):
 def test_llt_bit_identical(outputs):
     s = load(outputs, "spd", (200, 200))
     assert np.array_equal(load(outputs, "llt", (200, 200)), restatement().llt(np.asfortranarray(s)))
+
+
+def test_qr_bit_identical(outputs):
+    a = host_fill_normal(300, 200, 7)
+    q, r = restatement().qr(a)
+    assert np.array_equal(load(outputs, "qr_Q", (300, 300)), q)
+    assert np.array_equal(load(outputs, "qr_R", (300, 200)), r)
+
+
+def test_float_operator_star(outputs):
+    a = host_fill_uniform(150, 130, 0).reshape(-1, order="F")[:70 * 50].reshape(70, 50, order="F")
+    b = host_fill_uniform(130, 170, 1).reshape(-1, order="F")[:50 * 60].reshape(50, 60, order="F")
+    ref = a.astype(np.float32).astype(np.float64) @ b.astype(np.float32).astype(np.float64)
+    got = load(outputs, "sgemm", (70, 60), np.float32).astype(np.float64)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 2e-6

@@ -46,6 +46,12 @@ def test_mixed_ir_reaches_fp64_backward_error(handle, n, nrhs):
     Xd, info = handle.dgesv(A, B)
     xd = Xd.cpu().numpy()
     assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-7
+    # pivot growth max|U| / max|A| of the fp32 factorization, as mg_sgetrf gives it
+    A32 = A.float().t().contiguous().t()
+    handle.sgetrf(A32)
+    torch.cuda.synchronize()
+    growth = float(torch.triu(A32).abs().max()) / float(A.abs().max())
+    assert abs(rep["pivot_growth"] - growth) <= 1e-6 * growth, (rep["pivot_growth"], growth)
 
 
 def test_mixed_ir_fallback_when_refinement_stalls(handle):
