@@ -585,7 +585,7 @@ static mg_status_t launch_panel_f32(mg_handle_t h, GetrfCtx<float>& c, float* A,
                                     int* pos) {
     const int R = m - r0;
     if ((size_t)R * w * sizeof(float) > 64 * 1024 && R >= w && R <= panel_cluster_rows(h))
-        return sgetf2_cluster(h, A, lda, m, r0, w, pos, c.piv, c.ws.info);
+        return sgetf2_cluster(h, A, lda, m, r0, w, pos, c.piv, c.ws.info, c.ws.err);
     return launch_panel<float>(h, c, A, lda, m, r0, w, pos);
 }
 

@@ -131,7 +131,8 @@ int bf16x_kpad(int K);
 // FP32 panel on one thread-block cluster (panel_f32.cu): rows it can take
 // (0 if unavailable), and the launch (piv relative to r0; pos updated).
 int panel_cluster_rows(mg_handle_t h);
-mg_status_t sgetf2_cluster(mg_handle_t h, float* A, int lda, int m, int r0, int w, int* pos, int* piv, int* info);
+mg_status_t sgetf2_cluster(mg_handle_t h, float* A, int lda, int m, int r0, int w, int* pos, int* piv, int* info,
+                           int* err);
 
 // FP32 LU with split-BF16 trailing updates (lu.cu).  splitA and splitA2
 // each hold bf16x_split_bytes(n, nb, nterms) (the L21 split of alternate

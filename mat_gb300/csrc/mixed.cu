@@ -633,8 +633,9 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     bool converged = false;
     for (int it = 0; it <= o.max_iter; ++it) {
         MG_CHECK_CUDA(h, cudaMemsetAsync(w.norms, 0, 16 * sizeof(double), st));
-        mg::ProfScope* pr = new mg::ProfScope(h, "ir_residual", 2.0 * n * (double)n * nrhs, 8.0 * n * (double)n);
-        {
+        mg::ProfScope* pr = new mg::ProfScope(h, "ir_residual", it ? 2.0 * n * (double)n * nrhs : 0.0,
+                                              it ? 8.0 * n * (double)n : 0.0);
+        if (it > 0) {  // at it = 0, x = 0 and r = b: only the reduction pass below (zero chunks)
             const dim3 grid((n + RES_ROWS - 1) / RES_ROWS, kch);
             switch (nrhs) {
 #define MG_RES(NRV) \
@@ -645,8 +646,8 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
             }
             MG_TRY(mg::post_launch(h, "residual_partial_kernel"));
         }
-        residual_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kch, n, nrhs, B, ldb, X, ldx, w.R,
-                                                               w.norms);
+        residual_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, it ? kch : 0, n, nrhs, B, ldb, X, ldx,
+                                                               w.R, w.norms);
         MG_TRY(mg::post_launch(h, "residual_reduce_kernel"));
         delete pr;
         MG_CHECK_CUDA(h, cudaMemcpyAsync(hn, w.norms, 32 * sizeof(double), cudaMemcpyDeviceToHost, st));
