@@ -46,6 +46,7 @@ struct TileCfg {
 };
 using Big = TileCfg<2, 4, 4, 4>;    // 128 x 128, 8 warps
 using Small = TileCfg<1, 1, 2, 4>;  // 32 x 32, 1 warp
+using Thin = TileCfg<1, 1, 3, 2>;   // 48 x 16, 1 warp: M = 48 block-reflector products (QR, adjoint)
 
 __device__ __forceinline__ void cp_async8(double* smem, const double* gmem, bool pred) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -299,7 +300,13 @@ mg_status_t dgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, in
     } else {
         const long long tb = (long long)((m + Big::BM - 1) / Big::BM) * ((n + Big::BN - 1) / Big::BN);
         const long long ts = (long long)((m + Small::BM - 1) / Small::BM) * ((n + Small::BN - 1) / Small::BN);
-        if (busiest_sm_area(tb, h->num_sms, Big::BM, Big::BN) <= busiest_sm_area(ts, h->num_sms, Small::BM, Small::BN))
+        const long long tt = (long long)((m + Thin::BM - 1) / Thin::BM) * ((n + Thin::BN - 1) / Thin::BN);
+        const double ab = busiest_sm_area(tb, h->num_sms, Big::BM, Big::BN);
+        const double as = busiest_sm_area(ts, h->num_sms, Small::BM, Small::BN);
+        const double at = busiest_sm_area(tt, h->num_sms, Thin::BM, Thin::BN);
+        if (at < ab && at < as)
+            e = dispatch<Thin>(st, transA, transB, mode, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+        else if (ab <= as)
             e = dispatch<Big>(st, transA, transB, mode, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
         else
             e = dispatch<Small>(st, transA, transB, mode, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);

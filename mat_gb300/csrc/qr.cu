@@ -46,7 +46,19 @@ __device__ double warp_dot_mat(const double* __restrict__ a, const double* __res
     const int nb = len / 8;
     double acc = 0.0;
     int i = 0;
-    // four 8-lane accumulators over strides of 32 elements: lane p <- elements 32t + p
+    // four 8-lane accumulators over strides of 32 elements: lane p <- elements 32t + p;
+    // loads run PF steps ahead of the (ordered) fused chain
+    constexpr int PF = 16;
+    for (; i + 4 * PF <= nb; i += 4 * PF) {
+        double xa[PF], xb[PF];
+#pragma unroll
+        for (int u = 0; u < PF; ++u) {
+            xa[u] = __ldcg(a + (i + 4 * u) * 8 + lane);
+            xb[u] = __ldcg(b + (i + 4 * u) * 8 + lane);
+        }
+#pragma unroll
+        for (int u = 0; u < PF; ++u) acc = fma(xa[u], xb[u], acc);
+    }
     for (; i <= nb - 4; i += 4) acc = fma(__ldcg(a + i * 8 + lane), __ldcg(b + i * 8 + lane), acc);
     // remaining full 8-blocks into the first accumulator (lanes 0..7)
     for (; i < nb; ++i)
@@ -100,8 +112,22 @@ __global__ void __launch_bounds__(QR_THREADS) qr_panel_kernel(double* __restrict
                 }
             }
             __syncthreads();
-            if (!s_skip)
-                for (int i = 1 + threadIdx.x; i < len; i += blockDim.x) w[i] = w[i] * s_hr;
+            if (!s_skip) {
+                const double hr = s_hr;
+                for (int i0 = 1 + threadIdx.x; i0 < len; i0 += 8 * blockDim.x) {
+                    double x[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int i = i0 + u * blockDim.x;
+                        x[u] = i < len ? w[i] : 0.0;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int i = i0 + u * blockDim.x;
+                        if (i < len) w[i] = x[u] * hr;
+                    }
+                }
+            }
         }
         if (!mg::grid_barrier(ws.bar, (++phase) * gridDim.x, ws.err)) return;
         // apply H_r to the columns right of it (Mat skips them when the column was zero)
@@ -113,9 +139,19 @@ __global__ void __launch_bounds__(QR_THREADS) qr_panel_kernel(double* __restrict
             }
             __syncthreads();
             const double q = s_q;
-            for (int i = threadIdx.x; i < len; i += blockDim.x) {
-                const double v = i == 0 ? 1.0 : __ldcg(w + i);
-                col[i] = fma(v, q, col[i]);
+            for (int i0 = threadIdx.x; i0 < len; i0 += 8 * blockDim.x) {
+                double xv[8], xc[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int i = i0 + u * blockDim.x;
+                    xv[u] = i == 0 ? 1.0 : (i < len ? __ldcg(w + i) : 0.0);
+                    xc[u] = i < len ? col[i] : 0.0;
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int i = i0 + u * blockDim.x;
+                    if (i < len) col[i] = fma(xv[u], q, xc[u]);
+                }
             }
         }
         if (!mg::grid_barrier(ws.bar, (++phase) * gridDim.x, ws.err)) return;
@@ -132,7 +168,28 @@ __device__ double quad_dot_generic(const double* __restrict__ a, const double* _
     const int n4 = 4 * (len / 4), nv = (n4 / 32) * 32;
     double t = 0.0;
     int i = q;
+    constexpr int PF = 16;  // loads run PF steps ahead of the (ordered) chain
+    for (; i + 4 * (PF - 1) < nv; i += 4 * PF) {
+        double xa[PF], xb[PF];
+#pragma unroll
+        for (int u = 0; u < PF; ++u) {
+            xa[u] = __ldcg(a + i + 4 * u);
+            xb[u] = __ldcg(b + i + 4 * u);
+        }
+#pragma unroll
+        for (int u = 0; u < PF; ++u) t = __dadd_rn(t, __dmul_rn(xa[u], xb[u]));
+    }
     for (; i < nv; i += 4) t = __dadd_rn(t, __dmul_rn(__ldcg(a + i), __ldcg(b + i)));
+    for (; i + 4 * (PF - 1) < n4; i += 4 * PF) {
+        double xa[PF], xb[PF];
+#pragma unroll
+        for (int u = 0; u < PF; ++u) {
+            xa[u] = __ldcg(a + i + 4 * u);
+            xb[u] = __ldcg(b + i + 4 * u);
+        }
+#pragma unroll
+        for (int u = 0; u < PF; ++u) t = fma(xa[u], xb[u], t);
+    }
     for (; i < n4; i += 4) t = fma(__ldcg(a + i), __ldcg(b + i), t);
     // lanes q = 0..3 of a group of four consecutive lanes
     const unsigned full = 0xffffffffu;
@@ -170,19 +227,30 @@ __global__ void qr_t_dots_kernel(const double* __restrict__ P, int ldr, int h, i
 
 // T (b x b, ld b, upper) from S and tau (Mat's CalculateT recurrence).
 __global__ void qr_t_kernel(const double* __restrict__ S, const double* __restrict__ tau, int b, double* __restrict__ T) {
-    __shared__ double w[QR_BS];
-    if (threadIdx.x != 0) return;
-    for (int e = 0; e < b * b; ++e) T[e] = 0.0;
-    T[0] = tau[0];
-    for (int i = 1; i < b; ++i) {
-        for (int r = 0; r < i; ++r) w[r] = 0.0;
-        for (int c = 0; c < i; ++c) {
-            const double sc = S[c + (size_t)i * b];
-            for (int r = 0; r <= c; ++r) w[r] = fma(T[r + (size_t)c * b], sc, w[r]);
-        }
-        for (int r = 0; r < i; ++r) T[r + (size_t)i * b] = w[r] * -tau[i];
-        T[i + (size_t)i * b] = tau[i];
+    // S and T staged in shared memory; thread r owns row r of T, so every
+    // w_r = sum_c T(r, c) S(c, i) is one fused chain over c in ascending order
+    // (the order of Mat's loop) while the rows proceed in parallel.
+    __shared__ double ss[QR_BS * QR_BS], st[QR_BS * QR_BS], stau[QR_BS];
+    const int r = threadIdx.x;
+    for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
+        ss[e] = S[e];
+        st[e] = 0.0;
     }
+    if (r < b) stau[r] = tau[r];
+    __syncthreads();
+    if (r == 0) st[0] = stau[0];
+    __syncthreads();
+    for (int i = 1; i < b; ++i) {
+        if (r < i) {
+            double w = 0.0;
+            for (int c = r; c < i; ++c) w = fma(st[r + c * b], ss[c + i * b], w);
+            st[r + i * b] = w * -stau[i];
+        } else if (r == i) {
+            st[i + i * b] = stau[i];
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < b * b; e += blockDim.x) T[e] = st[e];
 }
 
 // Explicit unit-lower V (h x b, ld h) from the reflectors stored below the diagonal of P.
@@ -301,7 +369,7 @@ static mg_status_t dgeqrf_blocked(mg_handle_t h, int m, int n, double* R, int ld
                 qr_t_dots_kernel<<<(npairs * 4 + 255) / 256, 256, 0, st>>>(P, ldr, hh, b, w.S);
                 MG_TRY(post_launch(h, "qr_t_dots_kernel"));
             }
-            qr_t_kernel<<<1, 32, 0, st>>>(w.S, w.tau + j, b, Tj);
+            qr_t_kernel<<<1, 64, 0, st>>>(w.S, w.tau + j, b, Tj);
             MG_TRY(post_launch(h, "qr_t_kernel"));
         }
         if (j + b < n) {
