@@ -334,6 +334,82 @@ int grid_cap(mg_handle_t h, size_t total) {
     return (int)(g < 1 ? 1 : g > cap ? cap : g);
 }
 
+// ---------------------------------------------------------- unblocked path
+// Mat's QR for min(m, n) <= 2*BS (QR/__HouseHolder.h:179-208 and
+// __HouseHolder_Q1 :48-79): reflector r is w = x / sqrt(cr (x0 + cr)) with
+// x0 += cr (so H = I - w w^T), applied as col -= w (w^T col) to columns r..n-1
+// (R's entries below the diagonal keep the rounding-level values this leaves);
+// Q is then built backwards: with T2 the (m-r-1)-square trailing block,
+// column i >= 1 of the new (m-r)-square block is [w0 t; w[1..] t + T2(:, i-1)]
+// with t = -w[1..]^T T2(:, i-1), and column 0 is -w0 w + e0.  Mat runs this in
+// place inside Q's buffer; every new column depends only on w and T2(:, i-1),
+// which no earlier column overwrites, so the columns are computed in parallel
+// from a separate T2 buffer with the same per-element operations.
+__global__ void qru_reflector_kernel(const double* __restrict__ R, int ldr, int m, int r, double* __restrict__ w,
+                                     int* __restrict__ skip) {
+    __shared__ double s_hr;
+    __shared__ int s_skip;
+    const int len = m - r;
+    const double* x = R + r + (size_t)r * ldr;
+    for (int i = threadIdx.x; i < len; i += blockDim.x) w[i] = x[i];
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const double ss = warp_dot_mat(w, w, len);
+        if (threadIdx.x == 0) {
+            double cr = sqrt(ss);
+            if (cr == 0.0) {
+                s_skip = 1;
+            } else {
+                if (w[0] < 0.0) cr = -cr;
+                const double w0 = w[0] + cr;
+                w[0] = w0;
+                s_hr = 1.0 / sqrt(cr * w0);
+                s_skip = 0;
+            }
+            *skip = s_skip;
+        }
+    }
+    __syncthreads();
+    if (!s_skip)
+        for (int i = threadIdx.x; i < len; i += blockDim.x) w[i] = w[i] * s_hr;
+}
+
+// col -= w (w^T col) for columns r..n-1 of R, one warp per column.
+__global__ void qru_apply_kernel(double* __restrict__ R, int ldr, int m, int n, int r, const double* __restrict__ w,
+                                 const int* __restrict__ skip) {
+    if (*skip) return;
+    const int c = r + (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= n) return;
+    const int len = m - r;
+    double* col = R + r + (size_t)c * ldr;
+    const double d = -warp_dot_mat(w, col, len);
+    for (int i = lane; i < len; i += 32) col[i] = fma(w[i], d, col[i]);
+}
+
+// Columns i >= 1 of the new block B1 (r1 x r1) from T2 (r2 = r1 - 1 square), one warp per column.
+__global__ void qru_q1_kernel(const double* __restrict__ w, int r1, const double* __restrict__ T2,
+                              double* __restrict__ B1) {
+    const int i = 1 + (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= r1) return;
+    const int r2 = r1 - 1;
+    const double* src = T2 + (size_t)(i - 1) * r2;
+    const double temp = -warp_dot_mat(w + 1, src, r2);
+    double* dst = B1 + (size_t)i * r1;
+    if (lane == 0) dst[0] = w[0] * temp;
+    for (int e = lane; e < r2; e += 32) dst[1 + e] = fma(w[1 + e], temp, __ldcg(src + e));
+}
+
+// Column 0 of B1: -w0 w, then + 1 on the diagonal.
+__global__ void qru_q1_col0_kernel(const double* __restrict__ w, int r1, double* __restrict__ B1) {
+    const double q = -w[0];
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < r1; e += gridDim.x * blockDim.x) {
+        const double v = w[e] * q;
+        B1[e] = e == 0 ? v + 1.0 : v;
+    }
+}
+
 }  // namespace
 
 namespace mg {
@@ -415,6 +491,49 @@ static mg_status_t dorgqr_full(mg_handle_t h, int m, int n, const double* R, int
     return MG_OK;
 }
 
+// Mat's unblocked QR (min(m, n) <= 2*BS): R in place (ld ldr), Q (m x m, ld ldq).
+static mg_status_t dqr_unblocked(mg_handle_t h, int m, int n, double* R, int ldr, double* Q, int ldq) {
+    const int k = m < n ? m : n;
+    cudaStream_t st = h->stream;
+    // workspace: the k reflectors (packed, lengths m, m-1, ...), two m x m blocks, a flag per reflector
+    const size_t wlen = (size_t)k * m, mm = (size_t)m * m;
+    MG_TRY(ensure_ws(h, (wlen + 2 * mm) * sizeof(double) + (size_t)(k + 64) * sizeof(int) + 1024));
+    double* wv = (double*)h->ws;
+    double* B[2] = {wv + wlen, wv + wlen + mm};
+    int* skip = (int*)(B[1] + mm);
+    for (int r = 0; r < k; ++r) {
+        double* w = wv + (size_t)r * m;
+        qru_reflector_kernel<<<1, 256, 0, st>>>(R, ldr, m, r, w, skip + r);
+        MG_TRY(post_launch(h, "qru_reflector_kernel"));
+        const int cols = n - r;
+        qru_apply_kernel<<<(cols * 32 + 255) / 256, 256, 0, st>>>(R, ldr, m, n, r, w, skip + r);
+        MG_TRY(post_launch(h, "qru_apply_kernel"));
+    }
+    // T2 = identity of order m - k
+    int cur = 0;
+    const int r2 = m - k;
+    if (r2 > 0) {
+        identity_kernel<<<grid_cap(h, (size_t)r2 * r2), 256, 0, st>>>(B[cur], r2, r2);
+        MG_TRY(post_launch(h, "identity_kernel"));
+    }
+    for (int r = k - 1; r >= 0; --r) {
+        const int r1 = m - r;
+        const double* w = wv + (size_t)r * m;
+        double* B1 = B[cur ^ 1];
+        if (r1 > 1) {
+            qru_q1_kernel<<<((r1 - 1) * 32 + 255) / 256, 256, 0, st>>>(w, r1, B[cur], B1);
+            MG_TRY(post_launch(h, "qru_q1_kernel"));
+        }
+        qru_q1_col0_kernel<<<grid_cap(h, (size_t)r1), 256, 0, st>>>(w, r1, B1);
+        MG_TRY(post_launch(h, "qru_q1_col0_kernel"));
+        cur ^= 1;
+    }
+    MG_CHECK_CUDA(h, cudaMemcpy2DAsync(Q, (size_t)ldq * sizeof(double), B[cur], (size_t)m * sizeof(double),
+                                       (size_t)m * sizeof(double), m, cudaMemcpyDeviceToDevice, st));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
+    return MG_OK;
+}
+
 }  // namespace mg
 
 extern "C" {
@@ -447,6 +566,13 @@ mg_status_t mg_dqr(mg_handle_t h, int m, int n, const double* A, int lda, double
         ((size_t)m * n && (!A || !Q || !R)))
         return mg::fail(h, MG_ERR_ARG, "mg_dqr: bad arguments");
     if (m == 0) return MG_OK;
+    if ((m < n ? m : n) <= 2 * QR_BS) {  // Mat's unblocked variant (QR/__HouseHolder.h:179-208)
+        if (A != R) {
+            copy_kernel<<<grid_cap(h, (size_t)m * n), 256, 0, h->stream>>>(A, lda, m, n, R, ldr);
+            MG_TRY(mg::post_launch(h, "copy_kernel"));
+        }
+        return mg::dqr_unblocked(h, m, n, R, ldr, Q, ldq);
+    }
     MG_TRY(mg::ensure_ws(h, carve_qr(h, m, n, nullptr)));
     MG_TRY(mg::ensure_hws(h, 64));
     QrWs w;
