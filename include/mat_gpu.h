@@ -148,6 +148,13 @@ mg_status_t mg_dgetrs(mg_handle_t h, int n, int nrhs, const double* LU, int lda,
 mg_status_t mg_dgesv(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B, int ldb,
                      double* X, int ldx, int* info);
 
+/* Mat's Det(A) (Mat-8.3.1/LU/__Det.h:30-101) for n x n A (not modified):
+ * the PLU of a copy, the parity of its row permutation, then the product
+ * sign * U(0,0) * U(1,1) * ... in that order on the host, so the value
+ * equals Mat's bit for bit.  An exactly singular A gives a zero.
+ * Synchronises. */
+mg_status_t mg_ddet(mg_handle_t h, int n, const double* A, int lda, double* det);
+
 /* ------------------------------------------------- split-precision GEMM
  * C = alpha * A * B + beta * C for fp32 column-major operands on the
  * tcgen05 BF16 tensor cores: A and B are split into `nterms` bf16 terms

@@ -275,28 +275,13 @@ inline MAT<double> Solve_mixed(MAT<double>& A, MAT<double>& B, mg_ir_report* rep
     return X;
 }
 
-// Det(A) = sign(P) * prod diag(U).
+// Det(A) (Mat's Det: PLU, permutation parity, product of U's diagonal in order).
 inline double Det(MAT<double> A) {
     const int n = A.rows;
     if (n == 0) return 1.0;
-    MAT<double> L, U;
-    int* pos = new int[n];
-    PLU(A, pos, L, U);
-    // parity of the permutation
-    char* seen = new char[n]();
-    int swaps = 0;
-    for (int i = 0; i < n; ++i) {
-        if (seen[i]) continue;
-        int len = 0;
-        for (int j = i; !seen[j]; j = pos[j]) {
-            seen[j] = 1;
-            ++len;
-        }
-        swaps += len - 1;
-    }
-    double d = (swaps & 1) ? -1.0 : 1.0;
-    for (int i = 0; i < n; ++i) d = d * U(i, i);
-    delete[] seen;
-    delete[] pos;
+    matgpu::Dev dA((size_t)n * n * 8);
+    matgpu::h2d(dA.p, A.data, (size_t)n * n * 8);
+    double d = 0.0;
+    matgpu::check(mg_ddet(matgpu::handle(), n, dA.d(), n, &d), "mg_ddet");
     return d;
 }

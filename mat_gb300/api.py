@@ -167,6 +167,12 @@ class Handle:
         return X, info.value
 
     # ----------------------------------------------------------------- mixed
+    def ddet(self, A: torch.Tensor) -> float:
+        """Mat Det(A) (A untouched)."""
+        d = C.c_double()
+        self.check(self.lib.mg_ddet(self.h, A.shape[0], _ptr(A), ld_of(A), C.byref(d)), "mg_ddet")
+        return d.value
+
     def sgetf2(self, A: torch.Tensor, pos: torch.Tensor | None = None):
         """In-place fp32 panel LU of A (m x n, n <= 128, column-major). Returns (pos, info)."""
         m, n = A.shape

@@ -24,6 +24,7 @@
 //  Block size 60 = Mat's AVX-512 __BlockSize_LU, so the blocking (and with it
 //  every rounding) follows the reference.
 #include <climits>
+#include <vector>
 
 #include "grid_sync.cuh"
 #include "mg_internal.cuh"
@@ -916,6 +917,48 @@ mg_status_t mg_dgesv(mg_handle_t h, int n, int nrhs, const double* A, int lda, c
     if (s != MG_OK && s != MG_SINGULAR) return s;
     MG_TRY(mg::dgetrs_impl(h, n, nrhs, Acopy, n, pos, B, ldb, X, ldx));
     return s;
+}
+
+mg_status_t mg_ddet(mg_handle_t h, int n, const double* A, int lda, double* det) {
+    if (!h) return MG_ERR_ARG;
+    if (n < 0 || lda < (n > 1 ? n : 1) || !det || (n && !A)) return mg::fail(h, MG_ERR_ARG, "mg_ddet: bad arguments");
+    *det = 1.0;
+    if (n == 0) return MG_OK;
+    // Mat's Det (LU/__Det.h:30-101): the PLU factors, the parity of the row
+    // permutation, then the product sign * U(0,0) * U(1,1) * ... in order.
+    const size_t abytes = mg::align_up((size_t)n * n * sizeof(double), 256);
+    const size_t pbytes = mg::align_up((size_t)n * sizeof(int), 256);
+    const size_t base = mg::align_up(mg::getrf_ws_bytes<double>(h->num_sms), 256);
+    MG_TRY(mg::ensure_ws(h, base + abytes + pbytes));
+    MG_TRY(mg::ensure_hws(h, (size_t)n * (sizeof(double) + sizeof(int)) + 64));
+    double* Acopy = (double*)((char*)h->ws + base);
+    int* pos = (int*)((char*)h->ws + base + abytes);
+    MG_CHECK_CUDA(h, cudaMemcpy2DAsync(Acopy, (size_t)n * sizeof(double), A, (size_t)lda * sizeof(double),
+                                       (size_t)n * sizeof(double), n, cudaMemcpyDeviceToDevice, h->stream));
+    int info = 0;
+    mg_status_t s = mg::dgetrf_impl(h, n, n, Acopy, n, pos, &info);
+    if (s != MG_OK && s != MG_SINGULAR) return s;
+    double* hd = (double*)h->hws;
+    int* hp = (int*)(hd + n);
+    MG_CHECK_CUDA(h, cudaMemcpy2DAsync(hd, sizeof(double), Acopy, (size_t)(n + 1) * sizeof(double), sizeof(double), n,
+                                       cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hp, pos, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    std::vector<char> seen((size_t)n, 0);
+    long long swaps = 0;
+    for (int i = 0; i < n; ++i) {
+        if (seen[i]) continue;
+        int len = 0;
+        for (int j = i; !seen[j]; j = hp[j]) {
+            seen[j] = 1;
+            ++len;
+        }
+        swaps += len - 1;
+    }
+    double d = (swaps & 1) ? -1.0 : 1.0;
+    for (int i = 0; i < n; ++i) d = d * hd[i];
+    *det = d;
+    return MG_OK;
 }
 
 }  // extern "C"

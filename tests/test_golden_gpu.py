@@ -1,6 +1,6 @@
 """GPU results against the reference's own outputs (golden digests produced
 by tests/golden/make_golden.py from Mat-8.3.1): the FP64 GEMM, PLU, Solve,
-LLT and blocked QR reproduce Mat's AVX-512 results bit for bit, so the SHA-256
+LLT and QR (blocked and unblocked) reproduce Mat's AVX-512 results bit for bit, so the SHA-256
 of the raw column-major output equals the reference's, at the benchmark
 sizes (GEMM M=N=K=1024, PLU / LLT n = 8192)."""
 import hashlib
@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 import torch
 
-from mat_gb300.api import as_colmajor, colmajor
+from mat_gb300.api import as_colmajor, colmajor, host_fill_normal
 
 pytestmark = pytest.mark.gpu
 G = Path(__file__).resolve().parent / "golden"
@@ -72,3 +72,17 @@ def test_qr(handle, m, n):
     torch.cuda.synchronize()
     assert sha(R.cpu().numpy()) == META[f"qr_{m}x{n}"]["sha256_R"]
     assert sha(Q.cpu().numpy()) == META[f"qr_{m}x{n}"]["sha256_Q"]
+
+
+def test_qr_unblocked_60x40_full_arrays(handle):
+    # Mat's unblocked path (min(m, n) <= 96): Q and R as the reference returns them, bit for bit
+    f = np.load(G / "qr_60x40.npz")
+    A = as_colmajor(torch.from_numpy(host_fill_normal(60, 40, 7)))
+    Q, R = handle.dqr(A)
+    torch.cuda.synchronize()
+    assert np.array_equal(Q.cpu().numpy(), f["Q"]) and np.array_equal(R.cpu().numpy(), f["R"])
+
+
+def test_det_150(handle):
+    A = as_colmajor(torch.from_numpy(host_fill_normal(150, 150, 5)))
+    assert handle.ddet(A) == META["det_150"]["value"]
