@@ -155,6 +155,29 @@ mg_status_t mg_dgesv(mg_handle_t h, int n, int nrhs, const double* A, int lda, c
  * Synchronises. */
 mg_status_t mg_ddet(mg_handle_t h, int n, const double* A, int lda, double* det);
 
+/* Mat's Inv(A) (Mat-8.3.1/LU/__Inv.h:212-225, with __Inv :90-161 and
+ * __Inv_small :164-205) for n x n A (not modified): Ainv (ld ldinv) = A^{-1}
+ * in Mat's operation order, bit for bit.  info = the first zero-pivot
+ * column (1-based, status MG_SINGULAR) or 0; Mat does not check and neither
+ * is the inverse skipped.  Ainv may be A when ldinv == lda.  Synchronises. */
+mg_status_t mg_dinv(mg_handle_t h, int n, const double* A, int lda, double* Ainv, int ldinv, int* info);
+
+/* Mat's LU(A, L, U) without pivoting (Mat-8.3.1/LU/__LU.h:71-108) for square
+ * n x n A, in place: the unit lower factor's multipliers below the diagonal,
+ * U on and above it, bit for bit Mat's.  An exactly zero pivot gives info =
+ * its column + 1 and MG_SINGULAR (Mat's panel stops there; here the
+ * factorization goes on, so the factors then differ from Mat's).
+ * Synchronises. */
+mg_status_t mg_dlu(mg_handle_t h, int n, double* A, int lda, int* info);
+
+/* Mat's LDLT(A, L, D) (Mat-8.3.1/LU/__LLT.h:249-295, blocked __LDLT :153-209,
+ * BS = 48), in place: reads the lower triangle of A (n x n), leaves Mat's
+ * lower factor L (its diagonal as Mat computes it, d_j * (1/d_j)) with the
+ * strict upper part zeroed, and d (device, n doubles) = diag(D); bit for bit.
+ * No pivoting: an exactly zero d_j gives info = j + 1 and MG_SINGULAR (Mat
+ * does not check; the factorization runs to the end).  Synchronises. */
+mg_status_t mg_dldlt(mg_handle_t h, int n, double* A, int lda, double* d, int* info);
+
 /* ------------------------------------------------- split-precision GEMM
  * C = alpha * A * B + beta * C for fp32 column-major operands on the
  * tcgen05 BF16 tensor cores: A and B are split into `nterms` bf16 terms

@@ -6,9 +6,12 @@
 //
 //   operator*(MAT, MAT)                 Mat-8.3.1/Mul/Mul.h:204-235
 //   PLU(A, pos, L, U), PLU_getP, LU_init Mat-8.3.1/LU/__PLU.h:152-197, Mat.h:128-131
+//   LU(A, L, U) (no pivoting)           Mat-8.3.1/LU/__LU.h:71-108
 //   LLT(A, L)                           Mat-8.3.1/LU/__LLT.h:212-246
+//   LDLT(A, L, D)                       Mat-8.3.1/LU/__LLT.h:249-295
 //   Solve_direct(A, B)                  Mat-8.3.1/LU/__Solve_direct.h:146-220
 //   Det(A)                              Mat-8.3.1/LU/__Det.h:30-101
+//   Inv(A)                              Mat-8.3.1/LU/__Inv.h:212-225
 //   QR(A, Q, R, QR_Householder), QR_init Mat-8.3.1/QR/QR.h:8-25, Mat.h:132-136
 //
 // plus one call Mat does not have: Solve_mixed(A, B) (mixed-precision LU with
@@ -205,6 +208,26 @@ void PLU_getP(int* pos, MAT<t>& P) {
     for (int i = 0; i < P.rows; ++i) P(pos[i], i) = 1;
 }
 
+// LU(A, L, U) without pivoting (square A, L and U allocated as LU_init does):
+// L unit lower, U upper, bit for bit Mat's.
+inline void LU(MAT<double>& A, MAT<double>& L, MAT<double>& U) {
+    const int n = A.rows;
+    L.init(n, n);
+    U.init(n, n);
+    if (n == 0) return;
+    matgpu::Dev dA((size_t)n * n * 8);
+    matgpu::h2d(dA.p, A.data, (size_t)n * n * 8);
+    int info = 0;
+    matgpu::check(mg_dlu(matgpu::handle(), n, dA.d(), n, &info), "mg_dlu");
+    MAT<double> F(n, n);
+    matgpu::d2h(F.data, dA.p, (size_t)n * n * 8);
+    for (int c = 0; c < n; ++c)
+        for (int r = 0; r < n; ++r) {
+            L(r, c) = r > c ? F(r, c) : (r == c ? 1.0 : 0.0);
+            U(r, c) = r <= c ? F(r, c) : 0.0;
+        }
+}
+
 // LLT(A, L): reads the lower triangle of A; L lower, strict upper zeroed.
 inline void LLT(MAT<double>& A, MAT<double>& L) {
     const int n = A.rows;
@@ -215,6 +238,24 @@ inline void LLT(MAT<double>& A, MAT<double>& L) {
     int info = 0;
     matgpu::check(mg_dpotrf(matgpu::handle(), n, dA.d(), n, &info), "mg_dpotrf");
     matgpu::d2h(L.data, dA.p, (size_t)n * n * 8);
+}
+
+// LDLT(A, L, D): reads the lower triangle of A; L lower (diagonal as Mat
+// leaves it, d_j * (1/d_j)), strict upper zeroed; D = diag(d).
+inline void LDLT(MAT<double>& A, MAT<double>& L, MAT<double>& D) {
+    const int n = A.rows;
+    L.init(n, n);
+    D.init(n, n);
+    if (n == 0) return;
+    matgpu::Dev dA((size_t)n * n * 8), dd((size_t)n * 8);
+    matgpu::h2d(dA.p, A.data, (size_t)n * n * 8);
+    int info = 0;
+    matgpu::check(mg_dldlt(matgpu::handle(), n, dA.d(), n, (double*)dd.p, &info), "mg_dldlt");
+    matgpu::d2h(L.data, dA.p, (size_t)n * n * 8);
+    MAT<double> d(n, 1);
+    matgpu::d2h(d.data, dd.p, (size_t)n * 8);
+    std::memset(D.data, 0, sizeof(double) * (size_t)n * n);
+    for (int i = 0; i < n; ++i) D(i, i) = d.data[i];
 }
 
 // LLT on MAT<float>.
@@ -284,4 +325,17 @@ inline double Det(MAT<double> A) {
     double d = 0.0;
     matgpu::check(mg_ddet(matgpu::handle(), n, dA.d(), n, &d), "mg_ddet");
     return d;
+}
+
+// Inv(A) (A taken by value, as in Mat), bit for bit Mat's result.
+inline MAT<double> Inv(MAT<double> A) {
+    const int n = A.rows;
+    MAT<double> X(n, n);
+    if (n == 0) return X;
+    matgpu::Dev dA((size_t)n * n * 8), dX((size_t)n * n * 8);
+    matgpu::h2d(dA.p, A.data, (size_t)n * n * 8);
+    int info = 0;
+    matgpu::check(mg_dinv(matgpu::handle(), n, dA.d(), n, dX.d(), n, &info), "mg_dinv");
+    matgpu::d2h(X.data, dX.p, (size_t)n * n * 8);
+    return X;
 }

@@ -60,6 +60,9 @@ SIGNATURES: dict[str, tuple] = {
     "mg_dgetrf_noalloc": (i32, [vp, i32, i32, vp, i32, vp, pi32]),
     "mg_sgetf2": (i32, [vp, i32, i32, vp, i32, vp, pi32]),
     "mg_ddet": (i32, [vp, i32, vp, i32, pf64]),
+    "mg_dinv": (i32, [vp, i32, vp, i32, vp, i32, pi32]),
+    "mg_dldlt": (i32, [vp, i32, vp, i32, vp, pi32]),
+    "mg_dlu": (i32, [vp, i32, vp, i32, pi32]),
     "mg_sgetrf": (i32, [vp, i32, vp, i32, vp, pi32]),
     "mg_dgetrs": (i32, [vp, i32, i32, vp, i32, vp, vp, i32, vp, i32]),
     "mg_dgesv": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, pi32]),

@@ -173,6 +173,17 @@ class Handle:
         self.check(self.lib.mg_ddet(self.h, A.shape[0], _ptr(A), ld_of(A), C.byref(d)), "mg_ddet")
         return d.value
 
+    def dinv(self, A: torch.Tensor, Ainv: torch.Tensor | None = None):
+        """Mat Inv(A) (A untouched). Returns (Ainv, info)."""
+        n = A.shape[0]
+        if Ainv is None:
+            Ainv = colmajor(n, n, device=A.device)
+        info = C.c_int(0)
+        st = self.lib.mg_dinv(self.h, n, _ptr(A), ld_of(A), _ptr(Ainv), ld_of(Ainv), C.byref(info))
+        if st not in (0, 4):
+            self.check(st, "mg_dinv")
+        return Ainv, info.value
+
     def sgetf2(self, A: torch.Tensor, pos: torch.Tensor | None = None):
         """In-place fp32 panel LU of A (m x n, n <= 128, column-major). Returns (pos, info)."""
         m, n = A.shape
@@ -234,6 +245,26 @@ class Handle:
         if check and st not in (0, 5):
             self.check(st, "mg_dpotrf")
         return info.value
+
+    def dlu(self, A: torch.Tensor) -> int:
+        """In-place Mat LU without pivoting (square A): multipliers below the
+        diagonal, U on and above. Returns info."""
+        info = C.c_int(0)
+        st = self.lib.mg_dlu(self.h, A.shape[0], _ptr(A), ld_of(A), C.byref(info))
+        if st not in (0, 4):
+            self.check(st, "mg_dlu")
+        return info.value
+
+    def dldlt(self, A: torch.Tensor, d: torch.Tensor | None = None):
+        """In-place Mat LDLT: lower triangle of A -> L (upper zeroed); returns (d, info)."""
+        n = A.shape[0]
+        if d is None:
+            d = torch.empty(n, dtype=torch.float64, device=A.device)
+        info = C.c_int(0)
+        st = self.lib.mg_dldlt(self.h, n, _ptr(A), ld_of(A), _ptr(d), C.byref(info))
+        if st not in (0, 4):
+            self.check(st, "mg_dldlt")
+        return d, info.value
 
     def spotrf(self, A: torch.Tensor, check=True):
         """In-place fp32 LLT: lower triangle of A -> L, upper zeroed. Returns info."""

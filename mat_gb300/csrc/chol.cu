@@ -1,4 +1,5 @@
-// Blocked right-looking Cholesky (Mat's LLT) and the Cholesky solve.
+// Blocked right-looking Cholesky (Mat's LLT), LDL^T (Mat's LDLT) and the
+// Cholesky solve.
 //
 // Reference path (Mat-8.3.1/LU/__LLT.h): LLT (:212-246) copies the lower
 // triangle and calls __LLT (:94-150), BS = 48 (AVX-512, Mat.h:73-75): per
@@ -39,6 +40,7 @@ __global__ void llt2_kernel(T* __restrict__ L, int ldl, int k, int col0, int* __
         const T d = s[jj + jj * LLT2_MAX];
         const T t = T(1) / sqrt(d);
         if (r == 0 && !(d > T(0))) atomicCAS(info, 0, col0 + jj + 1);
+        __syncthreads();  // every thread has read d before row jj is scaled
         if (r >= jj && r < k) s[r + jj * LLT2_MAX] = s[r + jj * LLT2_MAX] * t;
         __syncthreads();
         if (r > jj && r < k) {
@@ -80,6 +82,58 @@ __global__ void xlt_kernel(const T* __restrict__ Ld, int ldl, T* __restrict__ X,
 #pragma unroll
     for (int j = 0; j < LLT_BS; ++j)
         if (j < k) X[r + (size_t)j * ldx] = x[j];
+}
+
+// Unblocked LDL^T of the k x k block at L (k <= 96), in place, lower part
+// (Mat's __LDLT2, LU/__LLT.h:16-27).  Column jj: d = L(jj,jj) (to d_out);
+// L(r,jj) *= 1/d for r >= jj (the diagonal becomes d * (1/d)); then for
+// i > jj: L(r,i) = fma(L(r,jj), (-L(i,jj)) d, L(r,i)) for r >= i.  info =
+// first exactly zero d (1-based).
+__global__ void ldlt2_kernel(double* __restrict__ L, int ldl, int k, int col0, double* __restrict__ d_out,
+                             int* __restrict__ info) {
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    double* s = reinterpret_cast<double*>(s_raw);  // column-major k x k with stride LLT2_MAX
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+        const int r = e % k, c = e / k;
+        s[r + c * LLT2_MAX] = L[r + (size_t)c * ldl];
+    }
+    __syncthreads();
+    const int r = threadIdx.x;
+    for (int jj = 0; jj < k; ++jj) {
+        const double d = s[jj + jj * LLT2_MAX];
+        const double t = 1.0 / d;
+        if (r == 0) {
+            d_out[col0 + jj] = d;
+            if (d == 0.0) atomicCAS(info, 0, col0 + jj + 1);
+        }
+        __syncthreads();  // every thread has read d before row jj is scaled
+        if (r >= jj && r < k) s[r + jj * LLT2_MAX] = __dmul_rn(s[r + jj * LLT2_MAX], t);
+        __syncthreads();
+        if (r > jj && r < k) {
+            const double lrj = s[r + jj * LLT2_MAX];
+            for (int i = jj + 1; i <= r; ++i)
+                s[r + i * LLT2_MAX] = fma(lrj, __dmul_rn(-s[i + jj * LLT2_MAX], d), s[r + i * LLT2_MAX]);
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+        const int rr = e % k, c = e / k;
+        if (rr >= c) L[rr + (size_t)c * ldl] = s[rr + c * LLT2_MAX];
+    }
+}
+
+// The end of Mat's __Solve_direct_XDLT (LU/__LLT.h:53-55) and the packing
+// of the trailing update's B operand (__pack_BT_block_d,
+// Mul/__pack_double.h:241-282): P(r,p) *= 1/d_p, then W(r,p) = P(r,p) d_p.
+__global__ void ldlt_scale_kernel(double* __restrict__ P, int ldp, int rows, int k, const double* __restrict__ d,
+                                  double* __restrict__ W, int ldw) {
+    const size_t total = (size_t)rows * k;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(e % rows), p = (int)(e / rows);
+        const double x = __dmul_rn(P[r + (size_t)p * ldp], 1.0 / d[p]);
+        P[r + (size_t)p * ldp] = x;
+        W[r + (size_t)p * ldw] = __dmul_rn(x, d[p]);
+    }
 }
 
 template <typename T>
@@ -222,6 +276,54 @@ mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out)
     return potrf_impl<double>(h, n, L, ldl, info_out);
 }
 
+// In-place Mat LDLT on the lower triangle of L (ld ldl): unit-like lower
+// factor (diagonal d_j * (1/d_j), as Mat leaves it), strict upper part
+// zeroed, d (device, n) the diagonal of D.
+mg_status_t dldlt_impl(mg_handle_t h, int n, double* L, int ldl, double* d, int* info_out) {
+    if (info_out) *info_out = 0;
+    if (n == 0) return MG_OK;
+    MG_TRY(ensure_hws(h, 64));
+    if (n > 2 * LLT_BS) MG_TRY(ensure_ws(h, (size_t)(n - LLT_BS) * LLT_BS * sizeof(double)));
+    int* dinfo = h->status;
+    MG_CHECK_CUDA(h, cudaMemsetAsync(dinfo, 0, sizeof(int), h->stream));
+    cudaStream_t st = h->stream;
+    const size_t s2 = (size_t)LLT2_MAX * LLT2_MAX * sizeof(double);
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(ldlt2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
+    if (n <= 2 * LLT_BS) {
+        ldlt2_kernel<<<1, 128, s2, st>>>(L, ldl, n, 0, d, dinfo);
+        MG_TRY(post_launch(h, "ldlt2_kernel"));
+    } else {
+        double* W = (double*)h->ws;
+        for (int j = 0; j < n; j += LLT_BS) {
+            const int nb = n - j < LLT_BS ? n - j : LLT_BS;
+            double* D = L + j + (size_t)j * ldl;
+            ldlt2_kernel<<<1, 128, s2, st>>>(D, ldl, nb, j, d, dinfo);
+            MG_TRY(post_launch(h, "ldlt2_kernel"));
+            if (j + LLT_BS < n) {
+                const int rows = n - (j + LLT_BS);
+                double* P = L + (j + LLT_BS) + (size_t)j * ldl;
+                xlt_kernel<double><<<(rows + 127) / 128, 128, 0, st>>>(D, ldl, P, ldl, rows, LLT_BS);
+                MG_TRY(post_launch(h, "xlt_kernel"));
+                int blocks = (int)(((size_t)rows * LLT_BS + 255) / 256);
+                if (blocks > h->num_sms * 8) blocks = h->num_sms * 8;
+                ldlt_scale_kernel<<<blocks, 256, 0, st>>>(P, ldl, rows, LLT_BS, d + j, W, rows);
+                MG_TRY(post_launch(h, "ldlt_scale_kernel"));
+                // C(i.., i..) -= P (P D)^T on the trailing matrix, lower tiles only
+                MG_TRY(dgemm_launch(h, 0, 1, rows, rows, LLT_BS, -1.0, P, ldl, W, rows, 1.0,
+                                    L + (j + LLT_BS) + (size_t)(j + LLT_BS) * ldl, ldl, 1));
+            }
+        }
+    }
+    zero_upper_kernel<double><<<h->num_sms * 8, 256, 0, st>>>(L, ldl, n);
+    MG_TRY(post_launch(h, "zero_upper_kernel"));
+    int* hw = (int*)h->hws;
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
+    if (info_out) *info_out = hw[0];
+    if (hw[0]) return fail(h, MG_SINGULAR, "ldlt: zero pivot at column %d", hw[0]);
+    return MG_OK;
+}
+
 // L x = b (forward substitution), in place on X.
 template <typename T>
 mg_status_t chol_lower_solve(mg_handle_t h, int n, int nrhs, const T* L, int ldl, T* X, int ldx) {
@@ -285,6 +387,12 @@ mg_status_t mg_dpotrs(mg_handle_t h, int n, int nrhs, const double* L, int ldl, 
     if (n < 0 || nrhs < 0 || ldl < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1) || ((size_t)n * nrhs && (!L || !B)))
         return mg::fail(h, MG_ERR_ARG, "mg_dpotrs: bad arguments");
     return mg::dpotrs_impl(h, n, nrhs, L, ldl, B, ldb);
+}
+
+mg_status_t mg_dldlt(mg_handle_t h, int n, double* A, int lda, double* d, int* info) {
+    if (!h) return MG_ERR_ARG;
+    if (n < 0 || lda < (n > 1 ? n : 1) || (n && (!A || !d))) return mg::fail(h, MG_ERR_ARG, "mg_dldlt: bad arguments");
+    return mg::dldlt_impl(h, n, A, lda, d, info);
 }
 
 mg_status_t mg_spotrf(mg_handle_t h, int n, float* A, int lda, int* info) {

@@ -66,7 +66,7 @@ __device__ __forceinline__ void better(T& v, int& i, T ov, int oi) {
 // Panel factorization of columns [r0, r0+nb) over rows [r0, m).
 template <typename T>
 __global__ void __launch_bounds__(PANEL_THREADS, 1)
-    panel_kernel(T* __restrict__ A, int lda, int m, int r0, int nb, int rpc, int* __restrict__ pos,
+    panel_kernel(T* __restrict__ A, int lda, int m, int r0, int nb, int rpc, int nopiv, int* __restrict__ pos,
                  int* __restrict__ piv, PanelWs ws, PanelXchg<T> x) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* slab = reinterpret_cast<T*>(smem_raw);  // slab[c * rpc + i]
@@ -91,12 +91,13 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1)
 
     for (int c = 0; c < nb; ++c) {
         const int buf = c & 1;
-        // 1. local candidate: largest |a| in column c over rows >= c, smallest row on ties
+        // 1. local candidate: largest |a| in column c over rows >= c, smallest
+        //    row on ties (nopiv: the diagonal row only, Mat's LU)
         T best = T(-1);
         int brow = INT_MAX;
         for (int i = tid; i < nrows; i += blockDim.x) {
             const int lr = row_lo + i;
-            if (lr < c) continue;
+            if (lr < c || (nopiv && lr != c)) continue;
             better(best, brow, fabs(slab[c * rpc + i]), lr);
         }
 #pragma unroll
@@ -265,6 +266,30 @@ __global__ void trsm_llnu_kernel(int k, int n, const T* __restrict__ L, int ldl,
             if (a == T(0)) continue;
             for (int r = i; r < k; ++r) sx[r * nt + t] = fma(sL[r + (i - 1) * k], -a, sx[r * nt + t]);
         }
+    }
+    for (int i = 0; i < k; ++i) X[i + (size_t)col * ldx] = sx[i * nt + t];
+}
+
+// X (k x n) := U^{-1} X with U upper (k <= PANEL_MAX_NB), one thread per
+// column, Mat's order for every column (LU/__Base.h:209-293 and :51-92 give
+// the same arithmetic): for i = k-1..0, x_i /= U(i,i), then
+// x_j = fma(U(j,i), -x_i, x_j) for j < i.
+template <typename T>
+__global__ void trsm_lunn_kernel(int k, int n, const T* __restrict__ U, int ldu, T* __restrict__ X, int ldx) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sU = reinterpret_cast<T*>(smem_raw);       // [k][k] column-major
+    T* sx = sU + k * k;                           // [k][blockDim]
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) sU[e] = U[(e % k) + (size_t)(e / k) * ldu];
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nt = blockDim.x, t = threadIdx.x;
+    if (col < n)
+        for (int i = 0; i < k; ++i) sx[i * nt + t] = X[i + (size_t)col * ldx];
+    __syncthreads();
+    if (col >= n) return;
+    for (int i = k - 1; i >= 0; --i) {
+        const T xi = sx[i * nt + t] / sU[i + i * k];
+        sx[i * nt + t] = xi;
+        for (int j = 0; j < i; ++j) sx[j * nt + t] = fma(sU[j + i * k], -xi, sx[j * nt + t]);
     }
     for (int i = 0; i < k; ++i) X[i + (size_t)col * ldx] = sx[i * nt + t];
 }
@@ -457,7 +482,8 @@ static GetrfCtx<T> carve(void* base, int num_sms, int nbmax = PANEL_MAX_NB) {
 }
 
 template <typename T>
-static mg_status_t launch_panel(mg_handle_t h, GetrfCtx<T>& c, T* A, int lda, int m, int r0, int nb, int* pos) {
+static mg_status_t launch_panel(mg_handle_t h, GetrfCtx<T>& c, T* A, int lda, int m, int r0, int nb, int* pos,
+                                int nopiv = 0) {
     const int R = m - r0;
     auto kern = panel_kernel<T>;
     cudaFuncAttributes fa;
@@ -480,7 +506,7 @@ static mg_status_t launch_panel(mg_handle_t h, GetrfCtx<T>& c, T* A, int lda, in
     ProfScope prof(h, sizeof(T) == 8 ? "panel_f64" : "panel_f32", (double)R * nb * nb,
                    2.0 * R * nb * sizeof(T));
     MG_CHECK_CUDA(h, cudaMemsetAsync(c.ws.bar, 0, sizeof(unsigned), h->stream));
-    void* args[] = {&A, &lda, &m, &r0, &nb, &rpc, &pos, &c.piv, &c.ws, &c.x};
+    void* args[] = {&A, &lda, &m, &r0, &nb, &rpc, &nopiv, &pos, &c.piv, &c.ws, &c.x};
     cudaError_t e;
     if (P > 1)
         e = cudaLaunchCooperativeKernel((const void*)kern, dim3(P), dim3(PANEL_THREADS), args, smem, h->stream);
@@ -515,11 +541,23 @@ static mg_status_t launch_trsm_llnu(mg_handle_t h, int k, int n, const T* L, int
     return post_launch(h, "trsm_llnu_kernel");
 }
 
+template <typename T>
+static mg_status_t launch_trsm_lunn(mg_handle_t h, int k, int n, const T* U, int ldu, T* X, int ldx) {
+    if (n <= 0 || k <= 0) return MG_OK;
+    const int threads = 64;
+    const size_t smem = ((size_t)k * k + (size_t)k * threads) * sizeof(T);
+    auto kern = trsm_lunn_kernel<T>;
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ProfScope prof(h, sizeof(T) == 8 ? "trsm_f64" : "trsm_f32", (double)k * k * n, 2.0 * k * n * sizeof(T));
+    kern<<<(n + threads - 1) / threads, threads, smem, h->stream>>>(k, n, U, ldu, X, ldx);
+    return post_launch(h, "trsm_lunn_kernel");
+}
+
 // In-place PLU given an exchange area `c` (no allocation); hstat receives the
 // error and info words (two host ints).  Returns MG_OK, MG_SINGULAR (info =
 // first zero-pivot column, 1-based) or an error.
 static mg_status_t dgetrf_run(mg_handle_t h, int m, int n, double* A, int lda, int* pos, GetrfCtx<double>& c,
-                              int* hstat, int* info_out) {
+                              int* hstat, int* info_out, int nopiv = 0) {
     if (info_out) *info_out = 0;
     MG_CHECK_CUDA(h, cudaMemsetAsync(c.ws.bar, 0, 256, h->stream));  // barrier, error and info words
     iota_kernel<<<(m + 255) / 256, 256, 0, h->stream>>>(pos, m);
@@ -529,16 +567,16 @@ static mg_status_t dgetrf_run(mg_handle_t h, int m, int n, double* A, int lda, i
     if (s <= LU_BS * 3 / 2) {
         // Mat's unblocked __PLU2 (LU/__PLU.h:22-51): one panel over all s
         // columns, interchanges on every column.
-        MG_TRY(launch_panel<double>(h, c, A, lda, m, 0, s, pos));
-        MG_TRY(launch_laswp<double>(h, A, lda, 0, s, c.piv, 0, s, n));
+        MG_TRY(launch_panel<double>(h, c, A, lda, m, 0, s, pos, nopiv));
+        if (!nopiv) MG_TRY(launch_laswp<double>(h, A, lda, 0, s, c.piv, 0, s, n));
         if (n > s) {
             MG_TRY(launch_trsm_llnu<double>(h, s, n - s, A, lda, A + (size_t)s * lda, lda));
         }
     } else {
         int r = 0;
         for (; r + LU_BS <= s; r += LU_BS) {
-            MG_TRY(launch_panel<double>(h, c, A, lda, m, r, LU_BS, pos));
-            MG_TRY(launch_laswp<double>(h, A, lda, r, LU_BS, c.piv, r, r + LU_BS, n));
+            MG_TRY(launch_panel<double>(h, c, A, lda, m, r, LU_BS, pos, nopiv));
+            if (!nopiv) MG_TRY(launch_laswp<double>(h, A, lda, r, LU_BS, c.piv, r, r + LU_BS, n));
             if (r + LU_BS < s) {
                 const int nt = n - (r + LU_BS);
                 double* A12 = A + r + (size_t)(r + LU_BS) * lda;
@@ -549,8 +587,8 @@ static mg_status_t dgetrf_run(mg_handle_t h, int m, int n, double* A, int lda, i
         }
         if (r < s) {
             const int rem = s - r;
-            MG_TRY(launch_panel<double>(h, c, A, lda, m, r, rem, pos));
-            MG_TRY(launch_laswp<double>(h, A, lda, r, rem, c.piv, r, n, n));
+            MG_TRY(launch_panel<double>(h, c, A, lda, m, r, rem, pos, nopiv));
+            if (!nopiv) MG_TRY(launch_laswp<double>(h, A, lda, r, rem, c.piv, r, n, n));
         }
     }
     MG_CHECK_CUDA(h, cudaMemcpyAsync(hstat, c.ws.err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -562,6 +600,8 @@ static mg_status_t dgetrf_run(mg_handle_t h, int m, int n, double* A, int lda, i
     return MG_OK;
 }
 
+size_t dgetrf_ws_bytes(int num_sms) { return getrf_ws_bytes<double>(num_sms); }
+
 // In-place PLU; pos (device, m ints) receives Mat's permutation.
 mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* pos, int* info_out) {
     if (info_out) *info_out = 0;
@@ -570,6 +610,21 @@ mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* po
     MG_TRY(ensure_hws(h, 64));
     GetrfCtx<double> c = carve<double>(h->ws, h->num_sms);
     return dgetrf_run(h, m, n, A, lda, pos, c, (int*)h->hws, info_out);
+}
+
+// In-place LU without pivoting (Mat's LU, LU/__LU.h:71-108) of a square
+// n x n A: the PLU pipeline with the diagonal as every pivot (the panel's
+// candidate is the diagonal row; no interchanges).  Mat's panel stops at an
+// exactly zero pivot; here info records it and the factorization goes on.
+mg_status_t dlu_nopiv_impl(mg_handle_t h, int n, double* A, int lda, int* info_out) {
+    if (info_out) *info_out = 0;
+    if (n == 0) return MG_OK;
+    const size_t base = align_up(getrf_ws_bytes<double>(h->num_sms), 256);
+    MG_TRY(ensure_ws(h, base + (size_t)n * sizeof(int)));
+    MG_TRY(ensure_hws(h, 64));
+    GetrfCtx<double> c = carve<double>(h->ws, h->num_sms);
+    int* pos = (int*)((char*)h->ws + base);
+    return dgetrf_run(h, n, n, A, lda, pos, c, (int*)h->hws, info_out, 1);
 }
 
 // ----------------------------------------------------------- mixed (fp32)
@@ -724,8 +779,19 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
     return MG_OK;
 }
 
-// X := A^{-1} B given the in-place factors, pos from dgetrf_impl (Mat's
-// narrow substitution order for every column).
+// X := A^{-1} B given the in-place factors, pos from dgetrf_impl, in the
+// operation order of Mat's Solve_direct (LU/__Solve_direct.h:146-220):
+//  * nrhs <= 4: the narrow scalar substitutions (:112-139);
+//  * n <= 90:   one unit-lower and one upper TRSM over the whole matrix (:166-190);
+//  * otherwise: __Solve_direct_LU_X (:1-66), blocks of 60 rows: forward, the
+//    block's TRSM then X(below) -= L(below, block) X(block); backward from
+//    the last block, X(above) -= U(above, block) X(block).  The products are
+//    the fused-chain DGEMM (alpha -1, beta 1), whose per-element order is
+//    that of Mat's packed kernels whatever their NC / MC tiling.
+// Mat's 8-column TRSM buffers hold 60 rows, so its one-block case with
+// 60 < n <= 90 and 8 or more right-hand sides writes past them (a crash in
+// the reference build); here that case computes the same arithmetic as
+// the rows that fit.
 mg_status_t dgetrs_impl(mg_handle_t h, int n, int nrhs, const double* LU, int lda, const int* pos,
                         const double* B, int ldb, double* X, int ldx) {
     if (n == 0 || nrhs == 0) return MG_OK;
@@ -735,6 +801,27 @@ mg_status_t dgetrs_impl(mg_handle_t h, int n, int nrhs, const double* LU, int ld
         if (blocks > h->num_sms * 8) blocks = h->num_sms * 8;
         permute_rows_kernel<double><<<blocks, 256, 0, h->stream>>>(n, nrhs, pos, B, ldb, X, ldx);
         MG_TRY(post_launch(h, "permute_rows_kernel"));
+    }
+    if (nrhs > 4) {
+        if (n <= LU_BS * 3 / 2) {
+            MG_TRY(launch_trsm_llnu<double>(h, n, nrhs, LU, lda, X, ldx));
+            return launch_trsm_lunn<double>(h, n, nrhs, LU, lda, X, ldx);
+        }
+        for (int r = 0; r < n; r += LU_BS) {
+            const int l = n - r < LU_BS ? n - r : LU_BS;
+            MG_TRY(launch_trsm_llnu<double>(h, l, nrhs, LU + r + (size_t)r * lda, lda, X + r, ldx));
+            if (r + l < n)
+                MG_TRY(dgemm_launch(h, 0, 0, n - r - l, nrhs, l, -1.0, LU + (r + l) + (size_t)r * lda, lda, X + r,
+                                    ldx, 1.0, X + r + l, ldx, 0));
+        }
+        for (int r = ((n - 1) / LU_BS) * LU_BS; r >= 0; r -= LU_BS) {
+            const int l = n - r < LU_BS ? n - r : LU_BS;
+            MG_TRY(launch_trsm_lunn<double>(h, l, nrhs, LU + r + (size_t)r * lda, lda, X + r, ldx));
+            if (r > 0)
+                MG_TRY(dgemm_launch(h, 0, 0, r, nrhs, l, -1.0, LU + (size_t)r * lda, lda, X + r, ldx, 1.0, X, ldx,
+                                    0));
+        }
+        return MG_OK;
     }
     const int ublocks = h->num_sms;
     for (int b0 = 0; b0 < n; b0 += TRSV_B) {
@@ -883,6 +970,12 @@ mg_status_t mg_dgetrf_noalloc(void* cuda_stream, int m, int n, double* A, int ld
     mg::GetrfCtx<double> c = mg::carve<double>(scratch, h.num_sms, mg::kNoAllocMaxNb);
     int hstat[2] = {0, 0};
     return mg::dgetrf_run(&h, m, n, A, lda, pos, c, hstat, info);
+}
+
+mg_status_t mg_dlu(mg_handle_t h, int n, double* A, int lda, int* info) {
+    if (!h) return MG_ERR_ARG;
+    if (n < 0 || lda < (n > 1 ? n : 1) || (n && !A)) return mg::fail(h, MG_ERR_ARG, "mg_dlu: bad arguments");
+    return mg::dlu_nopiv_impl(h, n, A, lda, info);
 }
 
 mg_status_t mg_dgetrs(mg_handle_t h, int n, int nrhs, const double* LU, int lda, const int* pos, const double* B,

@@ -91,9 +91,15 @@ mg_status_t dgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, in
 mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* pos, int* info_out);
 mg_status_t dgetrs_impl(mg_handle_t h, int n, int nrhs, const double* LU, int lda, const int* pos,
                         const double* B, int ldb, double* X, int ldx);
+// Device workspace dgetrf_impl uses at the start of h->ws (callers place
+// their own buffers after it).
+size_t dgetrf_ws_bytes(int num_sms);
+// Inverse from in-place PLU factors (inv.cu); LU's upper part is rescaled.
+mg_status_t dinv_from_lu(mg_handle_t h, int n, double* LU, const int* pos, double* X, double* Ainv, int ldinv);
 
 // Cholesky (chol.cu).
 mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out);
+mg_status_t dldlt_impl(mg_handle_t h, int n, double* L, int ldl, double* d, int* info_out);
 template <typename T>
 mg_status_t potrf_impl(mg_handle_t h, int n, T* L, int ldl, int* info_out);  // double, float
 template <typename T>

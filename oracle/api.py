@@ -31,7 +31,7 @@ class Oracle:
         self.is_ref = prefix == "ref_"
         if not self.is_ref:
             self.lib.orc_det.restype = C.c_double
-            for n in ("orc_dgetrf", "orc_plu", "orc_solve", "orc_llt"):
+            for n in ("orc_dgetrf", "orc_plu", "orc_solve", "orc_llt", "orc_inv", "orc_ldlt", "orc_lu"):
                 getattr(self.lib, n).restype = C.c_int
         else:
             self.lib.ref_det.restype = C.c_double
@@ -70,6 +70,32 @@ class Oracle:
         X = np.zeros((n, nrhs), order="F")
         self._fn("solve")(n, nrhs, _p(A), _p(B), _p(X))
         return X
+
+    def inv(self, A):
+        """Mat Inv(A) (square)."""
+        A = _f(A)
+        n = A.shape[0]
+        X = np.zeros((n, n), order="F")
+        self._fn("inv")(n, _p(A), _p(X))
+        return X
+
+    def lu(self, A):
+        """Mat LU(A, L, U) without pivoting (square): returns (L, U)."""
+        A = _f(A)
+        n = A.shape[0]
+        L = np.zeros((n, n), order="F")
+        U = np.zeros((n, n), order="F")
+        self._fn("lu")(n, _p(A), _p(L), _p(U))
+        return L, U
+
+    def ldlt(self, A):
+        """Mat LDLT(A, L, D): returns (L, D) from A's lower triangle."""
+        A = _f(A)
+        n = A.shape[0]
+        L = np.zeros((n, n), order="F")
+        D = np.zeros((n, n), order="F")
+        self._fn("ldlt")(n, _p(A), _p(L), _p(D))
+        return L, D
 
     def llt(self, A):
         A = _f(A)

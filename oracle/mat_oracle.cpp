@@ -1,6 +1,6 @@
 // ORACLE — test infrastructure only.  A CPU restatement of Mat-8.3.1's
 // algorithms for the GPU hot path (GEMM, blocked PLU, Solve_direct, blocked
-// LLT, blocked Householder QR, Det), written from the reference's behaviour,
+// LLT, blocked Householder QR, Det, Inv), written from the reference's behaviour,
 // with each routine citing the reference file:line it follows.  Only the
 // tests, the smoke check and the benchmark's CPU-baseline leg may load it.
 //
@@ -295,6 +295,53 @@ int plu_inplace(int m, int n, double* A, int lda, int* pos) {
     return info;
 }
 
+// LU without pivoting (Mat's LU / __LU / __LU2, LU/__LU.h:1-108), in place
+// on a square n x n A: the PLU recipe with the diagonal as every pivot.
+// __LU2 (:1-15): left-looking column updates, then the column below the
+// diagonal times 1 / pivot; an exactly zero pivot stops the panel (Mat's
+// `break`).  Returns 0 or 1 + the first zero-pivot column.
+int lu_nopiv_panel(double* A, int lda, int m, int r0, int bs) {
+    for (int c = 0; c < bs; ++c) {
+        const int gc = r0 + c;
+        double* col = A + (size_t)gc * lda;
+        for (int i = 0; i < c; ++i) {
+            const int gi = r0 + i;
+            const double q = -col[gi];
+            const double* li = A + (size_t)gi * lda;
+            for (int r = gi + 1; r < m; ++r) col[r] = std::fma(li[r], q, col[r]);
+        }
+        if (col[gc] == 0.0) return c;
+        const double inv = 1.0 / col[gc];
+        for (int r = gc + 1; r < m; ++r) col[r] = col[r] * inv;
+    }
+    return -1;
+}
+
+int lu_nopiv(int n, double* A, int lda) {
+    int info = 0;
+    if (n <= BS_LU * 1.5) {
+        const int brk = lu_nopiv_panel(A, lda, n, 0, n);
+        return brk >= 0 ? brk + 1 : 0;
+    }
+    int r = 0;
+    for (; r + BS_LU <= n; r += BS_LU) {
+        const int brk = lu_nopiv_panel(A, lda, n, r, BS_LU);
+        if (brk >= 0 && !info) info = r + brk + 1;
+        if (r + BS_LU < n) {
+            const int nt = n - (r + BS_LU);
+            double* A12 = A + r + (size_t)(r + BS_LU) * lda;
+            trsm_lx(BS_LU, nt, A + r + (size_t)r * lda, lda, A12, lda);
+            gemm_acc(n - (r + BS_LU), nt, BS_LU, A + (r + BS_LU) + (size_t)r * lda, lda, A12, lda,
+                     A + (r + BS_LU) + (size_t)(r + BS_LU) * lda, lda, true);
+        }
+    }
+    if (r < n) {
+        const int brk = lu_nopiv_panel(A, lda, n, r, n - r);
+        if (brk >= 0 && !info) info = r + brk + 1;
+    }
+    return info;
+}
+
 // ----------------------------------------------------------------- LLT
 // Unblocked Cholesky of a k x k block (Mat's __LLT2, LU/__LLT.h:3-13).
 void llt2(double* L, int ldl, int k) {
@@ -351,6 +398,62 @@ int llt(int n, double* L, int ldl) {
         for (int r = 0; r < i; ++r) at(L, ldl, r, i) = 0.0;
     for (int i = 0; i < n; ++i)
         if (!(at(L, ldl, i, i) > 0.0)) return i + 1;
+    return 0;
+}
+
+// Unblocked LDL^T of a k x k block (Mat's __LDLT2, LU/__LLT.h:16-27): d_j =
+// L(j,j); column j (diagonal included) times 1/d_j; then for i > j,
+// q = (-L(i,j)) d_j and L(r,i) = fma(L(r,j), q, L(r,i)) for r >= i.
+void ldlt2(double* L, int ldl, int k, double* d) {
+    for (int j = 0; j < k; ++j) {
+        d[j] = at(L, ldl, j, j);
+        const double t = 1.0 / d[j];
+        double* cj = L + (size_t)j * ldl;
+        for (int r = j; r < k; ++r) cj[r] = cj[r] * t;
+        for (int i = j + 1; i < k; ++i) {
+            const double q = -at(L, ldl, i, j) * d[j];
+            double* ci = L + (size_t)i * ldl;
+            for (int r = i; r < k; ++r) ci[r] = std::fma(cj[r], q, ci[r]);
+        }
+    }
+}
+
+// Blocked LDL^T (Mat's LDLT / __LDLT, LU/__LLT.h:153-209, 249-295): as the
+// Cholesky, with __Solve_direct_XDLT (:43-56: X := X L^{-T}, then each column
+// times 1/d_j) below the diagonal block and the trailing update
+// C -= L21 (L21 D)^T, the packed B operand holding the rounded products
+// L(c, p) d_p (__pack_BT_block_d, Mul/__pack_double.h:241-282).
+int ldlt(int n, double* L, int ldl, double* d) {
+    if (n <= 2 * BS_LLT) {
+        ldlt2(L, ldl, n, d);
+    } else {
+        std::vector<double> W;
+        for (int j = 0; j < n; j += BS_LLT) {
+            const int nb = std::min(BS_LLT, n - j);
+            ldlt2(L + j + (size_t)j * ldl, ldl, nb, d + j);
+            if (j + BS_LLT < n) {
+                const int rows = n - j - BS_LLT;
+                double* P = L + (j + BS_LLT) + (size_t)j * ldl;
+                trsm_xlt(rows, nb, L + j + (size_t)j * ldl, ldl, P, ldl);
+                for (int p = 0; p < nb; ++p) {
+                    const double t = 1.0 / d[j + p];
+                    for (int r = 0; r < rows; ++r) P[r + (size_t)p * ldl] = P[r + (size_t)p * ldl] * t;
+                }
+                W.assign((size_t)rows * nb, 0.0);
+                for (int p = 0; p < nb; ++p)
+                    for (int r = 0; r < rows; ++r) W[r + (size_t)p * rows] = P[r + (size_t)p * ldl] * d[j + p];
+                for (int i = j + BS_LLT; i < n; i += BS_LLT) {
+                    const int mb = std::min(BS_LLT, n - i);
+                    const int off = i - (j + BS_LLT);
+                    gemm_abt_sub(n - i, mb, nb, P + off, ldl, W.data() + off, rows, L + i + (size_t)i * ldl, ldl);
+                }
+            }
+        }
+    }
+    for (int i = 0; i < n; ++i)
+        for (int r = 0; r < i; ++r) at(L, ldl, r, i) = 0.0;
+    for (int i = 0; i < n; ++i)
+        if (d[i] == 0.0) return i + 1;
     return 0;
 }
 
@@ -549,9 +652,26 @@ int orc_solve(int n, int nrhs, const double* A, const double* B, double* X) {
             }
             if (n > 0) x[0] /= a[0];
         }
-    } else {
+    } else if (n <= BS_LU * 3 / 2) {
+        // one block (:166-190)
         trsm_lx(n, nrhs, a.data(), n, X, n);
         trsm_ux(n, nrhs, a.data(), n, X, n);
+    } else {
+        // __Solve_direct_LU_X (:1-66): blocks of BS_LU rows; forward, each
+        // block's TRSM then X(below) -= L(below, block) X(block); backward
+        // from the last block, X(above) -= U(above, block) X(block).  The
+        // NC / MC tiling of the products leaves each element's chain unchanged.
+        const double* ad = a.data();
+        for (int r = 0; r < n; r += BS_LU) {
+            const int l = std::min(BS_LU, n - r);
+            trsm_lx(l, nrhs, ad + r + (size_t)r * n, n, X + r, n);
+            if (r + l < n) gemm_acc(n - r - l, nrhs, l, ad + (r + l) + (size_t)r * n, n, X + r, n, X + r + l, n, true);
+        }
+        for (int r = ((n - 1) / BS_LU) * BS_LU; r >= 0; r -= BS_LU) {
+            const int l = std::min(BS_LU, n - r);
+            trsm_ux(l, nrhs, ad + r + (size_t)r * n, n, X + r, n);
+            if (r > 0) gemm_acc(r, nrhs, l, ad + (size_t)r * n, n, X + r, n, X, n, true);
+        }
     }
     return info;
 }
@@ -562,6 +682,33 @@ int orc_llt(int n, const double* A, double* L) {
     for (int c = 0; c < n; ++c)
         for (int r = c; r < n; ++r) at(L, n, r, c) = A[r + (size_t)c * n];
     return llt(n, L, n);
+}
+
+// LU(A, L, U) without pivoting (LU/__LU.h:71-108), square n: L unit lower,
+// U upper.
+int orc_lu(int n, const double* A, double* L, double* U) {
+    std::vector<double> a(A, A + (size_t)n * n);
+    const int info = lu_nopiv(n, a.data(), n);
+    for (int c = 0; c < n; ++c)
+        for (int r = 0; r < n; ++r) {
+            const double v = a[r + (size_t)c * n];
+            at(L, n, r, c) = r > c ? v : (r == c ? 1.0 : 0.0);
+            at(U, n, r, c) = r <= c ? v : 0.0;
+        }
+    return info;
+}
+
+// LDLT(A, L, D) (LU/__LLT.h:249-295): lower triangle of A in; L (upper
+// zeroed) and D = diag(d) out.
+int orc_ldlt(int n, const double* A, double* L, double* D) {
+    std::fill(L, L + (size_t)n * n, 0.0);
+    std::fill(D, D + (size_t)n * n, 0.0);
+    for (int c = 0; c < n; ++c)
+        for (int r = c; r < n; ++r) at(L, n, r, c) = A[r + (size_t)c * n];
+    std::vector<double> d(n);
+    const int info = ldlt(n, L, n, d.data());
+    for (int i = 0; i < n; ++i) at(D, n, i, i) = d[i];
+    return info;
 }
 
 // QR(A, Q, R, QR_Householder) (QR/QR.h:8-25): Q m x m, R m x n.
@@ -598,6 +745,118 @@ void orc_qr(int m, int n, const double* A, double* Q, double* R) {
     }
     for (int j = 0; j < n; ++j)
         for (int r = j + 1; r < m; ++r) R[r + (size_t)j * m] = 0.0;
+}
+
+// Row-wise right solves of Mat's Inv (AVX-512 __Solve_direct_XU / _XL,
+// LU/__Base.h:541-662, RB = 8).  Each row x of the len x n block X is
+// independent; a row in the 8-row vector part of its block (rows
+// 0 .. len - len % 8 - 1) sums the eight products q_u x_u as a tree, a row in
+// the scalar tail as a chain.  g++ contracts both (the intrinsics are plain
+// vector arithmetic to it): the tree becomes e_u = fma(x_2u, q_2u,
+// x_2u+1 q_2u+1), (e0 + e1) + (e2 + e3); the chain t = q1 x1,
+// t = fma(q0, x0, t), then t = fma(q_u, x_u, t) for u = 2..7.  Both forms
+// are pinned by the reference build's outputs.
+static double sum8_vec(const double* q, const double* x) {
+    const double e0 = std::fma(x[0], q[0], x[1] * q[1]), e1 = std::fma(x[2], q[2], x[3] * q[3]);
+    const double e2 = std::fma(x[4], q[4], x[5] * q[5]), e3 = std::fma(x[6], q[6], x[7] * q[7]);
+    return (e0 + e1) + (e2 + e3);
+}
+static double sum8_tail(const double* q, const double* x) {
+    double t = q[1] * x[1];
+    t = std::fma(q[0], x[0], t);
+    for (int u = 2; u < 8; ++u) t = std::fma(q[u], x[u], t);
+    return t;
+}
+
+// X := X U^{-1}, U unit upper n x n (diagonal not read).
+static void inv_xu(int len, int n, const double* U, int ldu, double* X, int ldx) {
+    const int lvec = len - len % 8;
+    for (int row = 0; row < len; ++row) {
+        double* x = X + row;  // x[c * ldx]
+        auto xc = [&](int c) -> double& { return x[(size_t)c * ldx]; };
+        int r = 0;
+        for (; r + 8 <= n; r += 8) {
+            for (int j = r; j < r + 8; ++j)
+                for (int i = j + 1; i < r + 8; ++i) xc(i) = std::fma(xc(j), -U[j + (size_t)i * ldu], xc(i));
+            double xv[8];
+            for (int u = 0; u < 8; ++u) xv[u] = xc(r + u);
+            for (int i = r + 8; i < n; ++i) {
+                double q[8];
+                for (int u = 0; u < 8; ++u) q[u] = -U[(r + u) + (size_t)i * ldu];
+                xc(i) = xc(i) + (row < lvec ? sum8_vec(q, xv) : sum8_tail(q, xv));
+            }
+        }
+        for (; r < n; ++r)
+            for (int i = r + 1; i < n; ++i) xc(i) = std::fma(xc(r), -U[r + (size_t)i * ldu], xc(i));
+    }
+}
+
+// X := X L^{-1}, L unit lower n x n (diagonal not read).
+static void inv_xl(int len, int n, const double* L, int ldl, double* X, int ldx) {
+    const int lvec = len - len % 8;
+    for (int row = 0; row < len; ++row) {
+        double* x = X + row;
+        auto xc = [&](int c) -> double& { return x[(size_t)c * ldx]; };
+        int r = n - 1;
+        for (; r - 7 >= 1; r -= 8) {
+            for (int j = r; j > r - 7; --j)
+                for (int i = r - 7; i < j; ++i) xc(i) = std::fma(xc(j), -L[j + (size_t)i * ldl], xc(i));
+            double xv[8];
+            for (int u = 0; u < 8; ++u) xv[u] = xc(r - u);
+            for (int i = 0; i < r - 7; ++i) {
+                double q[8];
+                for (int u = 0; u < 8; ++u) q[u] = -L[(r - u) + (size_t)i * ldl];
+                xc(i) = xc(i) + (row < lvec ? sum8_vec(q, xv) : sum8_tail(q, xv));
+            }
+        }
+        for (; r > 0; --r)
+            for (int i = 0; i < r; ++i) xc(i) = std::fma(xc(r), -L[r + (size_t)i * ldl], xc(i));
+    }
+}
+
+// Inv(A) (LU/__Inv.h:80-225): PLU; U's columns scaled by the reciprocal of
+// their diagonal, X = diag(1 / u_ii); X := X U^{-1} then X := X L^{-1}
+// (one block for n <= 90, else __Inv_X_LU's blocks of 60 with fused-chain
+// products); columns permuted, Ainv(:, pos[i]) = X(:, i).  Returns the PLU
+// zero-column index or -1.
+int orc_inv(int n, const double* A, double* Ainv) {
+    std::vector<double> a(A, A + (size_t)n * n), X((size_t)n * n, 0.0);
+    std::vector<int> pos(n);
+    const int info = plu_inplace(n, n, a.data(), n, pos.data());
+    for (int i = 0; i < n; ++i) {
+        const double t = 1.0 / a[i + (size_t)i * n];
+        for (int j = 0; j < i; ++j) a[j + (size_t)i * n] *= t;
+        X[i + (size_t)i * n] = t;
+    }
+    const double* ad = a.data();
+    double* xd = X.data();
+    if (n <= BS_LU * 3 / 2) {
+        inv_xu(n, n, ad, n, xd, n);
+        inv_xl(n, n, ad, n, xd, n);
+    } else {
+        for (int r = 0; r < n; r += BS_LU) {  // :12-44
+            const int l = std::min(BS_LU, n - r);
+            for (int i = 0; i <= r; i += BS_LU) {
+                const int m = std::min(BS_LU, n - i);
+                inv_xu(m, l, ad + r + (size_t)r * n, n, xd + i + (size_t)r * n, n);
+            }
+            const int rows = std::min(r + l, n);
+            if (r + BS_LU < n)
+                gemm_acc(rows, n - r - BS_LU, l, xd + (size_t)r * n, n, ad + r + (size_t)(r + BS_LU) * n, n,
+                         xd + (size_t)(r + BS_LU) * n, n, true);
+        }
+        for (int r = ((n - 1) / BS_LU) * BS_LU; r >= 0; r -= BS_LU) {  // :46-77
+            const int nb = std::min(BS_LU, n - r);
+            for (int i = 0; i < n; i += BS_LU) {
+                const int m = std::min(BS_LU, n - i);
+                inv_xl(m, nb, ad + r + (size_t)r * n, n, xd + i + (size_t)r * n, n);
+            }
+            if (r > 0) gemm_acc(n, r, nb, xd + (size_t)r * n, n, ad + r, n, xd, n, true);
+        }
+    }
+    for (int i = 0; i < n; ++i)
+        std::memcpy(Ainv + (size_t)pos[i] * n, xd + (size_t)i * n, sizeof(double) * n);
+    return info;
 }
 
 // Det(A) (LU/__Det.h:30-101): sign of the interchanges times the product of U's diagonal.

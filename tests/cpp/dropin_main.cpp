@@ -36,15 +36,29 @@ int main(int argc, char** argv) {
     dump("plu_L", L.data, (size_t)L.rows * L.cols);
     dump("plu_U", U.data, (size_t)U.rows * U.cols);
 
+    // LU without pivoting on a diagonally dominant matrix
+    MAT<double> Gd(200, 200), Ln, Un;
+    mg_host_fill_normal(Gd.data, 200, 200, 200, 4, 1);
+    for (int i = 0; i < 200; ++i) Gd(i, i) += 200.0;
+    LU(Gd, Ln, Un);
+    dump("lu_L", Ln.data, (size_t)200 * 200);
+    dump("lu_U", Un.data, (size_t)200 * 200);
+
     MAT<double> b(300, 3);
     mg_host_fill_normal(b.data, 300, 3, 300, 3, 1);
     MAT<double> x = Solve_direct(G, b);
     dump("solve", x.data, (size_t)x.rows * x.cols);
+    MAT<double> bw(300, 10);  // wide path (more than 4 right-hand sides)
+    mg_host_fill_normal(bw.data, 300, 10, 300, 8, 1);
+    MAT<double> xw = Solve_direct(G, bw);
+    dump("solve_wide", xw.data, (size_t)xw.rows * xw.cols);
     MAT<double> xm = Solve_mixed(G, b);
     dump("solve_mixed", xm.data, (size_t)xm.rows * xm.cols);
 
     double d = Det(G);
     dump("det", &d, 1);
+    MAT<double> Gi = Inv(G);
+    dump("inv", Gi.data, (size_t)300 * 300);
 
     // S = W W^T / n + I from the same generator, computed with the drop-in product
     MAT<double> W(200, 200), Wt(200, 200), S;
@@ -58,6 +72,10 @@ int main(int argc, char** argv) {
     MAT<double> Lc(200, 200);
     LLT(S, Lc);
     dump("llt", Lc.data, (size_t)200 * 200);
+    MAT<double> Ld, Dd;
+    LDLT(S, Ld, Dd);
+    dump("ldlt_L", Ld.data, (size_t)200 * 200);
+    dump("ldlt_D", Dd.data, (size_t)200 * 200);
     // QR(A, Q, R, QR_Householder), blocked path (min(m, n) > 96)
     MAT<double> Aq(300, 200), Q, R;
     mg_host_fill_normal(Aq.data, 300, 200, 300, 7, 1);

@@ -76,8 +76,10 @@ def main():
         meta["cases"][f"plu_{n}"] = {"sha256_L": sha(L), "sha256_U": sha(U), "sketch_L": sketch(L),
                                      "sketch_U": sketch(U)}
 
-    # Solve_direct (narrow path): 1 and 4 right-hand sides
-    for n, k in ((300, 4), (2048, 1)):
+    # Solve_direct: narrow path (1 and 4 right-hand sides); wide path with one
+    # block (n <= 90), blocked by 60 rows, 8-column groups plus ragged columns,
+    # more than one 144-column tile
+    for n, k in ((300, 4), (2048, 1), (50, 9), (300, 8), (300, 13), (1000, 150), (8192, 16)):
         x = ref.solve(host_fill_normal(n, n, 1), host_fill_normal(n, k, 2))
         meta["cases"][f"solve_{n}_{k}"] = {"sha256": sha(x), "x0": x[:4, 0].tolist()}
 
@@ -96,6 +98,37 @@ def main():
 
     # Det
     meta["cases"]["det_150"] = {"value": ref.det(host_fill_normal(150, 150, 5))}
+
+    # LU without pivoting: diagonally dominant G + n I, one block in full, blocked by digest
+    def dd(n, seed):
+        g = host_fill_normal(n, n, seed)
+        g[np.diag_indices(n)] += n
+        return np.asfortranarray(g)
+
+    L, U = ref.lu(dd(90, 4))
+    np.savez_compressed(OUT / "lu_90.npz", L=L, U=U)
+    for n in (300, 1000):
+        L, U = ref.lu(dd(n, 4))
+        meta["cases"][f"lu_{n}"] = {"sha256_L": sha(L), "sha256_U": sha(U)}
+
+    # LDLT: symmetric indefinite G + G^T (no pivoting), one block in full, blocked by digest
+    def sym(n, seed):
+        g = host_fill_normal(n, n, seed)
+        return np.asfortranarray(g + g.T)
+
+    L, D = ref.ldlt(sym(90, 3))
+    np.savez_compressed(OUT / "ldlt_90.npz", L=L, d=np.diag(D))
+    for n in (97, 300, 1000):
+        L, D = ref.ldlt(sym(n, 3))
+        meta["cases"][f"ldlt_{n}"] = {"sha256_L": sha(L), "sha256_d": sha(np.diag(D)[:, None])}
+    L, D = ref.ldlt(spd(ref, 2048, 1))
+    meta["cases"]["ldlt_spd_2048"] = {"sha256_L": sha(L), "sha256_d": sha(np.diag(D)[:, None])}
+
+    # Inv: one block (n <= 90) in full; blocked by 60 by digest
+    np.savez_compressed(OUT / "inv_61.npz", X=ref.inv(host_fill_normal(61, 61, 9)))
+    for n in (97, 300, 1000, 2048):
+        x = ref.inv(host_fill_normal(n, n, 9))
+        meta["cases"][f"inv_{n}"] = {"sha256": sha(x), "sketch": sketch(x)}
 
     meta["seconds"] = round(time.time() - t0, 1)
     (OUT / "golden.json").write_text(json.dumps(meta, indent=1))

@@ -49,20 +49,34 @@ def test_plu_bit_identical(outputs):
     assert np.array_equal(load(outputs, "plu_U", (300, 300)), U)
 
 
+def test_lu_without_pivoting(outputs):
+    a = host_fill_normal(200, 200, 4)
+    a[np.diag_indices(200)] += 200.0
+    L, U = restatement().lu(a)
+    assert np.array_equal(load(outputs, "lu_L", (200, 200)), L)
+    assert np.array_equal(load(outputs, "lu_U", (200, 200)), U)
+
+
 def test_solve_and_det(outputs):
     g = host_fill_normal(300, 300, 2)
     b = host_fill_normal(300, 3, 3)
     assert np.array_equal(load(outputs, "solve", (300, 3)), restatement().solve(g, b))
+    bw = host_fill_normal(300, 10, 8)
+    assert np.array_equal(load(outputs, "solve_wide", (300, 10)), restatement().solve(g, bw))
     xm = load(outputs, "solve_mixed", (300, 3))
     r = b - g @ xm
     assert (np.abs(r).max(0) / (np.abs(g).sum(1).max() * np.abs(xm).max(0) + np.abs(b).max(0))).max() <= 1e-14
     det = load(outputs, "det", (1,))[0]
     assert det == restatement().det(g)
+    assert np.array_equal(load(outputs, "inv", (300, 300)), restatement().inv(g))
 
 
 def test_llt_bit_identical(outputs):
     s = load(outputs, "spd", (200, 200))
     assert np.array_equal(load(outputs, "llt", (200, 200)), restatement().llt(np.asfortranarray(s)))
+    L, D = restatement().ldlt(np.asfortranarray(s))
+    assert np.array_equal(load(outputs, "ldlt_L", (200, 200)), L)
+    assert np.array_equal(load(outputs, "ldlt_D", (200, 200)), D)
 
 
 def test_qr_bit_identical(outputs):

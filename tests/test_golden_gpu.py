@@ -1,6 +1,7 @@
 """GPU results against the reference's own outputs (golden digests produced
-by tests/golden/make_golden.py from Mat-8.3.1): the FP64 GEMM, PLU, Solve,
-LLT and QR (blocked and unblocked) reproduce Mat's AVX-512 results bit for bit, so the SHA-256
+by tests/golden/make_golden.py from Mat-8.3.1): the FP64 GEMM, PLU, Solve
+(narrow and wide), LU without pivoting, LLT, LDLT, QR (blocked and
+unblocked), Det and Inv reproduce Mat's AVX-512 results bit for bit, so the SHA-256
 of the raw column-major output equals the reference's, at the benchmark
 sizes (GEMM M=N=K=1024, PLU / LLT n = 8192)."""
 import hashlib
@@ -45,7 +46,7 @@ def test_plu(handle, n):
     assert sha(U) == META[f"plu_{n}"]["sha256_U"]
 
 
-@pytest.mark.parametrize("n,k", [(300, 4), (2048, 1)])
+@pytest.mark.parametrize("n,k", [(300, 4), (2048, 1), (50, 9), (300, 8), (300, 13), (1000, 150), (8192, 16)])
 def test_solve(handle, n, k):
     A, B = colmajor(n, n), colmajor(n, k)
     handle.fill_normal(A, 1)
@@ -86,3 +87,78 @@ def test_qr_unblocked_60x40_full_arrays(handle):
 def test_det_150(handle):
     A = as_colmajor(torch.from_numpy(host_fill_normal(150, 150, 5)))
     assert handle.ddet(A) == META["det_150"]["value"]
+
+
+def test_inv_61_full_array(handle):
+    A = as_colmajor(torch.from_numpy(host_fill_normal(61, 61, 9)))
+    X, info = handle.dinv(A)
+    torch.cuda.synchronize()
+    assert info == 0 and np.array_equal(X.cpu().numpy(), np.load(G / "inv_61.npz")["X"])
+
+
+@pytest.mark.parametrize("n", [97, 300, 1000, 2048])
+def test_inv(handle, n):
+    A = colmajor(n, n)
+    handle.fill_normal(A, 9)
+    X, info = handle.dinv(A)
+    torch.cuda.synchronize()
+    assert info == 0 and sha(X.cpu().numpy()) == META[f"inv_{n}"]["sha256"]
+
+
+def sym(n, seed):
+    g = host_fill_normal(n, n, seed)
+    return np.asfortranarray(g + g.T)
+
+
+def test_ldlt_90_full_arrays(handle):
+    f = np.load(G / "ldlt_90.npz")
+    A = as_colmajor(torch.from_numpy(sym(90, 3)))
+    d, info = handle.dldlt(A)
+    torch.cuda.synchronize()
+    assert np.array_equal(A.cpu().numpy(), f["L"]) and np.array_equal(d.cpu().numpy(), f["d"])
+
+
+@pytest.mark.parametrize("n", [97, 300, 1000])
+def test_ldlt(handle, n):
+    A = as_colmajor(torch.from_numpy(sym(n, 3)))
+    d, info = handle.dldlt(A)
+    torch.cuda.synchronize()
+    assert sha(A.cpu().numpy()) == META[f"ldlt_{n}"]["sha256_L"]
+    assert sha(d.cpu().numpy()[:, None]) == META[f"ldlt_{n}"]["sha256_d"]
+
+
+def test_ldlt_spd_2048(handle):
+    S = colmajor(2048, 2048)
+    handle.gen_spd_gram(S, 1)
+    d, info = handle.dldlt(S)
+    torch.cuda.synchronize()
+    assert info == 0
+    assert sha(S.cpu().numpy()) == META["ldlt_spd_2048"]["sha256_L"]
+    assert sha(d.cpu().numpy()[:, None]) == META["ldlt_spd_2048"]["sha256_d"]
+
+
+def dd(n, seed=4):
+    g = host_fill_normal(n, n, seed)
+    g[np.diag_indices(n)] += n
+    return np.asfortranarray(g)
+
+
+def lu_factors(A):
+    f = A.cpu().numpy()
+    return np.tril(f, -1) + np.eye(f.shape[0]), np.triu(f)
+
+
+def test_lu_90_full_arrays(handle):
+    f = np.load(G / "lu_90.npz")
+    A = as_colmajor(torch.from_numpy(dd(90)))
+    assert handle.dlu(A) == 0
+    L, U = lu_factors(A)
+    assert np.array_equal(L, f["L"]) and np.array_equal(U, f["U"])
+
+
+@pytest.mark.parametrize("n", [300, 1000])
+def test_lu(handle, n):
+    A = as_colmajor(torch.from_numpy(dd(n)))
+    assert handle.dlu(A) == 0
+    L, U = lu_factors(A)
+    assert sha(L) == META[f"lu_{n}"]["sha256_L"] and sha(U) == META[f"lu_{n}"]["sha256_U"]

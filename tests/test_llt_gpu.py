@@ -1,6 +1,7 @@
-"""Mat LLT (blocked Cholesky) on the GPU against the oracle (bit-identical
-restatement of Mat-8.3.1's AVX-512 LLT); factors within 1e-13 normwise
-relative, non-SPD detection, and the Cholesky solve."""
+"""Mat LLT (blocked Cholesky) and LDLT on the GPU against the oracle
+(bit-identical restatement of Mat-8.3.1's AVX-512 build); Cholesky factors
+within 1e-13 normwise relative, LDLT bit for bit, non-SPD / zero-pivot
+detection, and the Cholesky solve."""
 import numpy as np
 import pytest
 import torch
@@ -59,3 +60,42 @@ def test_cholesky_solve(handle, n, nrhs):
     torch.cuda.synchronize()
     x = X.cpu().numpy()
     assert np.linalg.norm(s @ x - b) / (np.linalg.norm(s) * np.linalg.norm(x)) < 1e-15
+
+
+def sym(n, seed=3):
+    g = host_fill_normal(n, n, seed)
+    return np.asfortranarray(g + g.T)
+
+
+@pytest.mark.parametrize("n", [1, 2, 47, 48, 96, 97, 145, 300, 1000])
+@pytest.mark.parametrize("kind", ["spd", "indefinite"])
+def test_ldlt_bit_identical(handle, n, kind):
+    """Mat's LDLT (no pivoting) bit for bit: L (with Mat's d (1/d) diagonal) and d."""
+    a = spd(n) if kind == "spd" else sym(n)
+    A = as_colmajor(torch.from_numpy(a))
+    d, info = handle.dldlt(A)
+    torch.cuda.synchronize()
+    L0, D0 = restatement().ldlt(a)
+    assert info == 0
+    assert np.array_equal(A.cpu().numpy(), L0)
+    assert np.array_equal(d.cpu().numpy(), np.diag(D0))
+
+
+def test_ldlt_reads_lower_triangle_only(handle):
+    a = sym(130)
+    junk = a.copy()
+    junk[np.triu_indices(130, 1)] = np.nan
+    A = as_colmajor(torch.from_numpy(np.asfortranarray(junk)))
+    d, info = handle.dldlt(A)
+    torch.cuda.synchronize()
+    L0, D0 = restatement().ldlt(a)
+    assert np.array_equal(A.cpu().numpy(), L0) and np.array_equal(d.cpu().numpy(), np.diag(D0))
+
+
+def test_ldlt_zero_pivot_reports_column(handle):
+    a = sym(60)
+    a[0, :] = 0.0
+    a[:, 0] = 0.0
+    A = as_colmajor(torch.from_numpy(np.asfortranarray(a)))
+    d, info = handle.dldlt(A)
+    assert info == 1

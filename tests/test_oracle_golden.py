@@ -56,10 +56,44 @@ def test_plu_digest(orc, n):
     assert sha(L) == META[f"plu_{n}"]["sha256_L"] and sha(U) == META[f"plu_{n}"]["sha256_U"]
 
 
-@pytest.mark.parametrize("n,k", [(300, 4), (2048, 1)])
+@pytest.mark.parametrize("n,k", [(300, 4), (2048, 1), (50, 9), (300, 8), (300, 13), (1000, 150)])
 def test_solve_digest(orc, n, k):
     x = orc.solve(host_fill_normal(n, n, 1), host_fill_normal(n, k, 2))
     assert sha(x) == META[f"solve_{n}_{k}"]["sha256"]
+
+
+def test_lu_without_pivoting(orc):
+    def dd(n):
+        g = host_fill_normal(n, n, 4)
+        g[np.diag_indices(n)] += n
+        return np.asfortranarray(g)
+
+    f = np.load(G / "lu_90.npz")
+    L, U = orc.lu(dd(90))
+    assert np.array_equal(L, f["L"]) and np.array_equal(U, f["U"])
+    for n in (300, 1000):
+        L, U = orc.lu(dd(n))
+        assert sha(L) == META[f"lu_{n}"]["sha256_L"] and sha(U) == META[f"lu_{n}"]["sha256_U"]
+
+
+def sym(n, seed):
+    g = host_fill_normal(n, n, seed)
+    return np.asfortranarray(g + g.T)
+
+
+def test_ldlt(orc):
+    f = np.load(G / "ldlt_90.npz")
+    L, D = orc.ldlt(sym(90, 3))
+    assert np.array_equal(L, f["L"]) and np.array_equal(np.diag(D), f["d"])
+    for n in (97, 300, 1000):
+        L, D = orc.ldlt(sym(n, 3))
+        assert sha(L) == META[f"ldlt_{n}"]["sha256_L"] and sha(np.diag(D)[:, None]) == META[f"ldlt_{n}"]["sha256_d"]
+
+
+def test_inv(orc):
+    assert np.array_equal(orc.inv(host_fill_normal(61, 61, 9)), np.load(G / "inv_61.npz")["X"])
+    for n in (97, 300, 1000):
+        assert sha(orc.inv(host_fill_normal(n, n, 9))) == META[f"inv_{n}"]["sha256"]
 
 
 def test_llt(orc):
@@ -97,5 +131,13 @@ def test_restatement_equals_reference_build(orc, m, n):
     if m == n:
         s = spd(n, 12)
         assert np.array_equal(orc.llt(s), ref.llt(s))
-        b = host_fill_normal(n, 3, 13)
-        assert np.array_equal(orc.solve(a, b), ref.solve(a, b))
+        assert np.array_equal(orc.inv(a), ref.inv(a))
+        for x, y in zip(orc.ldlt(s), ref.ldlt(s)):
+            assert np.array_equal(x, y)
+        for x, y in zip(orc.lu(a), ref.lu(a)):
+            assert np.array_equal(x, y)
+        for k in (3, 8, 11):
+            if k >= 8 and 60 < n <= 90:
+                continue  # the reference's one-block 8-column path overruns its 60-row buffer there
+            b = host_fill_normal(n, k, 13)
+            assert np.array_equal(orc.solve(a, b), ref.solve(a, b))
