@@ -63,6 +63,10 @@ uint64_t mg_launch_count(mg_handle_t h);
  * accumulated with the algorithmic flops / bytes it performed.  Turning it
  * on clears the records; count/get synchronise the stream. */
 mg_status_t mg_profile_enable(mg_handle_t h, int on);
+/* Restricts the timing to phases named `name` (NULL or "" = every phase), so
+ * that timing one kernel family adds two event records per launch of it
+ * only. */
+mg_status_t mg_profile_only(mg_handle_t h, const char* name);
 int mg_profile_count(mg_handle_t h);
 mg_status_t mg_profile_get(mg_handle_t h, int i, const char** name, double* ms, long long* launches,
                            double* flops, double* bytes);

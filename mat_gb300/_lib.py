@@ -72,6 +72,7 @@ SIGNATURES: dict[str, tuple] = {
     "mg_gen_svd_matrix": (i32, [vp, i32, vp, i32, u64, i32, f64]),
     "mg_gen_spd_gram": (i32, [vp, i32, vp, i32, u64]),
     "mg_profile_enable": (i32, [vp, i32]),
+    "mg_profile_only": (i32, [vp, C.c_char_p]),
     "mg_profile_count": (i32, [vp]),
     "mg_profile_get": (i32, [vp, i32, C.POINTER(C.c_char_p), pf64, C.POINTER(C.c_longlong), pf64, pf64]),
     "mg_dpotrf": (i32, [vp, i32, vp, i32, pi32]),

@@ -357,7 +357,10 @@ class Handle:
         return loss.value, dell.value, Kb
 
     # --------------------------------------------------------------- profile
-    def profile(self, on: bool = True):
+    def profile(self, on: bool = True, only: str | None = None):
+        """Per-phase CUDA-event timing on the library's streams (all phases, or
+        only those named `only`)."""
+        self.check(self.lib.mg_profile_only(self.h, (only or "").encode()), "mg_profile_only")
         self.check(self.lib.mg_profile_enable(self.h, int(on)), "mg_profile_enable")
 
     def profile_records(self) -> dict:

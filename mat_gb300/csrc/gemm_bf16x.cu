@@ -20,10 +20,13 @@
 //               and one elected lane issues tcgen05.mma (M=128, N=256, K=16),
 //               committing each stage back to the producer and each finished
 //               tile to the epilogue.
-//   warps 2-5   epilogue: tcgen05.ld the accumulator (each warp its 32 TMEM
-//               lanes = 32 rows), apply alpha/beta, store C coalesced by
-//               column.  Two accumulators let tile t+1's MMAs run under tile
-//               t's epilogue.
+//   warps 2-9   epilogue: tcgen05.ld the accumulator (each warp its 32 TMEM
+//               lanes = 32 rows, warps w and w+4 the two halves of the
+//               columns), apply alpha/beta, store C coalesced by column.  Two
+//               accumulators let tile t+1's MMAs run under tile t's
+//               epilogue; two warps per lane quarter keep twice the C loads
+//               in flight, which the read-modify-write of C in a K = 128
+//               trailing update needs to approach HBM speed.
 // Every mbarrier wait is bounded; on a timeout the kernel records MG_TIMEOUT,
 // drains its own outstanding copies/MMAs and frees TMEM before returning.
 #include <cuda_bf16.h>
@@ -34,7 +37,8 @@
 namespace {
 
 constexpr int BM = 128, BN = 256, BK = 32;  // BK * 2 B = 64 B = one swizzle row
-constexpr int THREADS = 192;
+constexpr int EPI_WARPS = 8;  // two per TMEM lane quarter, each half of the tile's columns
+constexpr int THREADS = 64 + 32 * EPI_WARPS;
 constexpr int TMEM_COLS = 512;
 
 template <int NP>
@@ -120,7 +124,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&acc_full[b], 1);
-            tc::mbar_init(&acc_empty[b], 128);
+            tc::mbar_init(&acc_empty[b], 32 * EPI_WARPS);
         }
         tc::mbar_init(mma_done, 1);
         tc::fence_barrier_init();
@@ -230,6 +234,8 @@ __global__ void __launch_bounds__(THREADS, 1)
         // ------------------------------------------------------------------ epilogue
         const int q = warp & 3;  // TMEM lane quarter this warp may access
         const int row_in_tile = q * 32 + lane;
+        constexpr int CH_PER = BN / 32 / (EPI_WARPS / 4);  // 32-column chunks per warp
+        const int ch0 = ((warp - 2) / 4) * CH_PER;           // this warp's first chunk
         int it = 0;
         for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
             const int buf = it & 1;
@@ -249,12 +255,12 @@ __global__ void __launch_bounds__(THREADS, 1)
             const bool rd = beta != 0.f && row < M;
             const float* crow = C + (size_t)row;
             float ca[32], cb[32];
-            epi_load(rd, crow, ldc, nb * BN, N, ca);
+            epi_load(rd, crow, ldc, nb * BN + ch0 * 32, N, ca);
 #pragma unroll 1
-            for (int ch = 0; ch < BN / 32; ch += 2) {
+            for (int ch = ch0; ch < ch0 + CH_PER; ch += 2) {
                 epi_load(rd, crow, ldc, nb * BN + (ch + 1) * 32, N, cb);
                 epi_store(row < M, C + (size_t)row, ldc, nb * BN + ch * 32, N, taddr + ch * 32, alpha, beta, ca);
-                if (ch + 2 < BN / 32) epi_load(rd, crow, ldc, nb * BN + (ch + 2) * 32, N, ca);
+                if (ch + 2 < ch0 + CH_PER) epi_load(rd, crow, ldc, nb * BN + (ch + 2) * 32, N, ca);
                 epi_store(row < M, C + (size_t)row, ldc, nb * BN + (ch + 1) * 32, N, taddr + (ch + 1) * 32, alpha,
                           beta, cb);
             }

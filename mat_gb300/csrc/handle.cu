@@ -86,6 +86,7 @@ static cudaEvent_t prof_event(mg_handle_t h) {
 ProfScope::ProfScope(mg_handle_t h_, const char* name, double flops_, double bytes_)
     : h(h_), flops(flops_), bytes(bytes_) {
     if (!h || !h->prof_on) return;
+    if (!h->prof_only.empty() && h->prof_only != name) return;
     int idx = -1;
     for (size_t i = 0; i < h->prof.size(); ++i)
         if (h->prof[i].name == name) idx = (int)i;
@@ -133,6 +134,12 @@ mg_status_t mg_profile_enable(mg_handle_t h, int on) {
     mg::prof_resolve(h);
     h->prof_on = on != 0;
     if (on) h->prof.clear();
+    return MG_OK;
+}
+
+mg_status_t mg_profile_only(mg_handle_t h, const char* name) {
+    if (!h) return MG_ERR_ARG;
+    h->prof_only = name ? name : "";
     return MG_OK;
 }
 

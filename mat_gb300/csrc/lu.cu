@@ -666,8 +666,8 @@ struct OnStream {
 // while a low-priority side stream runs the far update (the trailing
 // columns beyond the next panel) of step k on num_sms - 16 CTAs as soon as
 // the near update is done.  The panel is queued directly behind the near
-// update on S, so its 16-CTA cluster takes its SMs before the far update's
-// persistent grid fills the rest.  A panel too tall for the cluster (the
+// update on S and submitted before the far update, so its 16-CTA cluster
+// takes its SMs before the far update's persistent grid fills the rest.  A panel too tall for the cluster (the
 // cooperative grid) is not overlapped.
 //
 // The trailing updates run on the BF16 tensor cores with `nterms` split
@@ -697,10 +697,13 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
     const bool cluster_ok = panel_cluster_rows(h) > 0;
     const int nsteps = (n + nb - 1) / nb;
 
-    // panel k and everything that depends only on it
-    auto side = [&](int k) -> mg_status_t {
+    // panel k, then everything that depends only on it
+    auto panel = [&](int k) -> mg_status_t {
         const int r = k * nb, w = nb < n - r ? nb : n - r;
-        MG_TRY(launch_panel_f32(h, c, A, lda, n, r, w, pos));
+        return launch_panel_f32(h, c, A, lda, n, r, w, pos);
+    };
+    auto after_panel = [&](int k) -> mg_status_t {
+        const int r = k * nb, w = nb < n - r ? nb : n - r;
         MG_TRY(launch_laswp<float>(h, A, lda, r, w, c.piv, r, n, n));  // columns [0, r)
         float* Lout = Linv_all ? Linv_all + (size_t)k * nb * nb : (float*)tri;
         const int ldo = Linv_all ? nb : w;
@@ -723,7 +726,8 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
         return cluster_ok && (size_t)R * w * sizeof(float) > 64 * 1024 && R >= w && R <= panel_cluster_rows(h);
     };
 
-    MG_TRY(side(0));
+    MG_TRY(panel(0));
+    MG_TRY(after_panel(0));
     bool far_pending = false;  // a far update was issued on S2 (event la_ev[1])
     for (int k = 0; k < nsteps; ++k) {
         const int r = k * nb, w = nb < n - r ? nb : n - r;
@@ -749,23 +753,29 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
         MG_TRY(bf16x_gemm_presplit(h, nterms, nt, w1, w, -1.0f, L21, splitB, 1.0f, A22, lda, gemm_err, 0,
                                    (size_t)nt * kp));
         const bool ov = overlappable(k + 1);
-        if (nt > w1) {
-            const void* Brest = (const char*)splitB + (size_t)w1 * kp * 2;
-            if (ov) {
-                MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[0], S));
-                MG_CHECK_CUDA(h, cudaStreamWaitEvent(S2, h->la_ev[0], 0));
+        const void* Brest = (const char*)splitB + (size_t)w1 * kp * 2;
+        if (nt > w1 && ov) {
+            // the panel is submitted before the far update, so that its
+            // cluster is placed while the GPU is still free of the far
+            // update's persistent grid
+            MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[0], S));
+            MG_TRY(panel(k + 1));
+            MG_CHECK_CUDA(h, cudaStreamWaitEvent(S2, h->la_ev[0], 0));
+            {
                 OnStream on(h, S2);
                 MG_TRY(bf16x_gemm_presplit(h, nterms, nt, nt - w1, w, -1.0f, L21, Brest, 1.0f,
                                            A22 + (size_t)w1 * lda, lda, gemm_err, 0, (size_t)nt * kp,
                                            h->num_sms - 16));
                 MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[1], S2));
-                far_pending = true;
-            } else {
+            }
+            far_pending = true;
+        } else {
+            if (nt > w1)
                 MG_TRY(bf16x_gemm_presplit(h, nterms, nt, nt - w1, w, -1.0f, L21, Brest, 1.0f,
                                            A22 + (size_t)w1 * lda, lda, gemm_err, 0, (size_t)nt * kp));
-            }
+            MG_TRY(panel(k + 1));
         }
-        MG_TRY(side(k + 1));
+        MG_TRY(after_panel(k + 1));
     }
     if (far_pending) MG_CHECK_CUDA(h, cudaStreamWaitEvent(S, h->la_ev[1], 0));
     int* hw = (int*)h->hws;

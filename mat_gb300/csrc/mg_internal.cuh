@@ -45,6 +45,7 @@ struct mg_handle_s {
         double flops, bytes;
     };
     bool prof_on = false;
+    std::string prof_only;  // when not empty, only scopes of this name are timed
     std::vector<ProfRec> prof;
     std::vector<ProfPending> prof_pending;
     std::vector<cudaEvent_t> prof_pool;
