@@ -69,12 +69,33 @@ __device__ __forceinline__ void tile_coords(int t, int num_m, int num_n, int& mb
     nb = r / gsize;
 }
 
+// C streams through L2 once per update: its loads and stores carry an
+// evict-first L2 policy so that they do not push out what is reused (the
+// split operands, and the panel that a concurrent factorization step works
+// on), and the loads do not allocate in L1.
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ float ld_stream(const float* p, uint64_t pol) {
+    float v;
+    asm volatile("ld.global.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;\n" : "=f"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+__device__ __forceinline__ void st_stream(float* p, float v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;\n" ::"l"(p), "f"(v), "l"(pol) : "memory");
+}
+
 // Epilogue helpers: 32 consecutive columns of one row of C.
 __device__ __forceinline__ void epi_load(bool rd, const float* crow, int ldc, int col0, int N, float (&cv)[32]) {
+    const uint64_t pol = l2_evict_first_policy();
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
         const int col = col0 + j;
-        cv[j] = (rd && col < N) ? crow[(size_t)col * ldc] : 0.f;
+        cv[j] = (rd && col < N) ? ld_stream(crow + (size_t)col * ldc, pol) : 0.f;
     }
 }
 
@@ -84,12 +105,13 @@ __device__ __forceinline__ void epi_store(bool wr, float* crow, int ldc, int col
     tc::tmem_ld_32x32b_x32(taddr, r);
     tc::tmem_ld_wait();
     if (!wr) return;
+    const uint64_t pol = l2_evict_first_policy();
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
         const int col = col0 + j;
         if (col < N) {
             const float v = alpha * __uint_as_float(r[j]);
-            crow[(size_t)col * ldc] = beta == 0.f ? v : fmaf(beta, cv[j], v);
+            st_stream(crow + (size_t)col * ldc, beta == 0.f ? v : fmaf(beta, cv[j], v), pol);
         }
     }
 }
