@@ -69,13 +69,18 @@ __device__ __forceinline__ void tile_coords(int t, int num_m, int num_n, int& mb
     nb = r / gsize;
 }
 
-// C streams through L2 once per update: its loads and stores carry an
-// evict-first L2 policy so that they do not push out what is reused (the
-// split operands, and the panel that a concurrent factorization step works
-// on), and the loads do not allocate in L1.
-__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+// A C that streams through L2 once (a far trailing update, a large product)
+// is loaded and stored with an evict-first L2 policy, so that it does not
+// push out what is reused (the split operands, and the panel that a
+// concurrent factorization step works on); a C that is read again soon (the
+// next panel's columns) keeps the normal policy.  The loads do not allocate
+// in L1.
+__device__ __forceinline__ uint64_t l2_policy(bool stream) {
     uint64_t p;
-    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+    if (stream)
+        asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+    else
+        asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;\n" : "=l"(p));
     return p;
 }
 
@@ -90,8 +95,8 @@ __device__ __forceinline__ void st_stream(float* p, float v, uint64_t pol) {
 }
 
 // Epilogue helpers: 32 consecutive columns of one row of C.
-__device__ __forceinline__ void epi_load(bool rd, const float* crow, int ldc, int col0, int N, float (&cv)[32]) {
-    const uint64_t pol = l2_evict_first_policy();
+__device__ __forceinline__ void epi_load(bool rd, const float* crow, int ldc, int col0, int N, uint64_t pol,
+                                         float (&cv)[32]) {
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
         const int col = col0 + j;
@@ -99,13 +104,12 @@ __device__ __forceinline__ void epi_load(bool rd, const float* crow, int ldc, in
     }
 }
 
-__device__ __forceinline__ void epi_store(bool wr, float* crow, int ldc, int col0, int N, uint32_t taddr, float alpha,
+__device__ __forceinline__ void epi_store(bool wr, float* crow, int ldc, int col0, int N, uint64_t pol, uint32_t taddr, float alpha,
                                           float beta, const float (&cv)[32]) {
     uint32_t r[32];
     tc::tmem_ld_32x32b_x32(taddr, r);
     tc::tmem_ld_wait();
     if (!wr) return;
-    const uint64_t pol = l2_evict_first_policy();
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
         const int col = col0 + j;
@@ -120,7 +124,7 @@ template <int NP>
 __global__ void __launch_bounds__(THREADS, 1)
     bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       float* __restrict__ C, int ldc, int M, int N, int Kp, float alpha, float beta,
-                      int* __restrict__ err) {
+                      int stream_c, int* __restrict__ err) {
     using CF = Cfg<NP>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -277,13 +281,14 @@ __global__ void __launch_bounds__(THREADS, 1)
             const bool rd = beta != 0.f && row < M;
             const float* crow = C + (size_t)row;
             float ca[32], cb[32];
-            epi_load(rd, crow, ldc, nb * BN + ch0 * 32, N, ca);
+            const uint64_t pol = l2_policy(stream_c != 0);
+            epi_load(rd, crow, ldc, nb * BN + ch0 * 32, N, pol, ca);
 #pragma unroll 1
             for (int ch = ch0; ch < ch0 + CH_PER; ch += 2) {
-                epi_load(rd, crow, ldc, nb * BN + (ch + 1) * 32, N, cb);
-                epi_store(row < M, C + (size_t)row, ldc, nb * BN + ch * 32, N, taddr + ch * 32, alpha, beta, ca);
-                if (ch + 2 < ch0 + CH_PER) epi_load(rd, crow, ldc, nb * BN + (ch + 2) * 32, N, ca);
-                epi_store(row < M, C + (size_t)row, ldc, nb * BN + (ch + 1) * 32, N, taddr + (ch + 1) * 32, alpha,
+                epi_load(rd, crow, ldc, nb * BN + (ch + 1) * 32, N, pol, cb);
+                epi_store(row < M, C + (size_t)row, ldc, nb * BN + ch * 32, N, pol, taddr + ch * 32, alpha, beta, ca);
+                if (ch + 2 < ch0 + CH_PER) epi_load(rd, crow, ldc, nb * BN + (ch + 2) * 32, N, pol, ca);
+                epi_store(row < M, C + (size_t)row, ldc, nb * BN + (ch + 1) * 32, N, pol, taddr + (ch + 1) * 32, alpha,
                           beta, cb);
             }
             tc::tc_fence_before();
@@ -350,6 +355,120 @@ __global__ void split_cols_kernel(const TIN* __restrict__ B, int ldb, int K, int
     }
 }
 
+// U12 := L11^{-1} A12 (FP32, L11 unit lower w x w, w <= 128) and the split
+// terms of U12 as the B operand of the trailing updates ([term][column][Kp],
+// zero rows w .. Kp-1), in one pass: one CTA per 64 columns of A12, four
+// threads per column; in each 16-row block thread g of a column holds rows
+// g, g+4, g+8, g+12.  L11 sits row-major and the columns column-major in
+// shared memory, both with a pitch of 4 mod 32 words, which makes every
+// access conflict-free: the coalesced global loads and stores (a warp on 32
+// consecutive rows of a column), the four rows of L a warp reads at once, a
+// column's 16-row slices read as float4s, and the 8 columns x 4 rows of a
+// warp's solution values.  Per 16-row block: the updates from every earlier
+// block (16 products per row and block), then the 16 x 16 unit-lower solve,
+// each solved value passed by a shuffle inside the column's group of four.
+// This replaces an explicit inverse of L11, two splits and a tensor-core
+// product on the critical path of every step of the mixed LU.
+constexpr int TS_W = 128;  // widest panel
+constexpr int TS_C = 64;   // columns per CTA
+constexpr int TS_THREADS = 4 * TS_C;
+constexpr int TS_P = TS_W + 4;  // pitch of both shared arrays (words)
+constexpr size_t TS_SMEM = (size_t)(TS_W * TS_P + TS_C * TS_P) * sizeof(float);
+
+__global__ void __launch_bounds__(TS_THREADS) trsm_split_kernel(const float* __restrict__ L, int lda,
+                                                               float* __restrict__ A12, int nt, int w, int np, int Kp,
+                                                               size_t part_stride, __nv_bfloat16* __restrict__ out) {
+    extern __shared__ __align__(16) float ts_sm[];
+    float* const sL = ts_sm;                // [TS_W][TS_P]: L11(i, j) at i * TS_P + j, strict lower part only
+    float* const sx = ts_sm + TS_W * TS_P;  // [TS_C][TS_P]: row i of column c at c * TS_P + i
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int c = (tid >> 5) * 8 + (lane >> 2);  // my column (of this CTA's TS_C)
+    const int g = lane & 3;                      // my rows g, g+4, g+8, g+12 of each 16-row block
+    const int c0 = blockIdx.x * TS_C;
+    const int ncol = min(TS_C, nt - c0);
+    float* const xc = sx + c * TS_P;
+    // loads in batches of 32 per thread, all in flight together (a load ->
+    // shared store loop would wait for each one)
+    for (int e0 = 0; e0 < TS_W * TS_W; e0 += 32 * TS_THREADS) {
+        float t[32];
+#pragma unroll
+        for (int u = 0; u < 32; ++u) {
+            const int e = e0 + tid + u * TS_THREADS, i = e % TS_W, j = e / TS_W;
+            t[u] = (i < w && j < i) ? L[i + (size_t)j * lda] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 32; ++u) {
+            const int e = e0 + tid + u * TS_THREADS, i = e % TS_W, j = e / TS_W;
+            sL[i * TS_P + j] = t[u];
+        }
+    }
+    {
+        float t[TS_W * TS_C / TS_THREADS];
+#pragma unroll
+        for (int u = 0; u < TS_W * TS_C / TS_THREADS; ++u) {
+            const int e = tid + u * TS_THREADS, i = e % TS_W, cc = e / TS_W;
+            t[u] = (i < w && cc < ncol) ? A12[i + (size_t)(c0 + cc) * lda] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < TS_W * TS_C / TS_THREADS; ++u) {
+            const int e = tid + u * TS_THREADS, i = e % TS_W, cc = e / TS_W;
+            sx[cc * TS_P + i] = t[u];
+        }
+    }
+    __syncthreads();
+    for (int I = 0; I < w; I += 16) {
+        float xi[4];  // rows I + g + 4a
+#pragma unroll
+        for (int a = 0; a < 4; ++a) xi[a] = xc[I + g + 4 * a];
+        for (int J = 0; J < I; J += 16) {
+            float xj[16];
+#pragma unroll
+            for (int b4 = 0; b4 < 4; ++b4) {
+                const float4 v = reinterpret_cast<const float4*>(xc + J)[b4];
+                xj[4 * b4 + 0] = v.x;
+                xj[4 * b4 + 1] = v.y;
+                xj[4 * b4 + 2] = v.z;
+                xj[4 * b4 + 3] = v.w;
+            }
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const float4* lr = reinterpret_cast<const float4*>(sL + (I + g + 4 * a) * TS_P + J);
+#pragma unroll
+                for (int b4 = 0; b4 < 4; ++b4) {
+                    const float4 l = lr[b4];
+                    xi[a] = fmaf(-l.x, xj[4 * b4 + 0], xi[a]);
+                    xi[a] = fmaf(-l.y, xj[4 * b4 + 1], xi[a]);
+                    xi[a] = fmaf(-l.z, xj[4 * b4 + 2], xi[a]);
+                    xi[a] = fmaf(-l.w, xj[4 * b4 + 3], xi[a]);
+                }
+            }
+        }
+        // the 16 x 16 diagonal block: x_b final -> the rows below it in the block
+#pragma unroll
+        for (int b = 0; b < 16; ++b) {
+            const float xb = __shfl_sync(0xffffffffu, xi[b >> 2], (lane & ~3) | (b & 3));
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+                if (g + 4 * a > b) xi[a] = fmaf(-sL[(I + g + 4 * a) * TS_P + I + b], xb, xi[a]);
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a) xc[I + g + 4 * a] = xi[a];
+        __syncwarp();  // a column's four threads share one warp
+    }
+    __syncthreads();
+    for (int e = tid; e < Kp * ncol; e += TS_THREADS) {
+        const int i = e % Kp, cc = e / Kp;
+        const float v = i < w ? sx[cc * TS_P + i] : 0.f;
+        if (i < w) A12[i + (size_t)(c0 + cc) * lda] = v;
+        __nv_bfloat16 h0, h1, h2;
+        split3(v, h0, h1, h2);
+        const size_t o = (size_t)(c0 + cc) * Kp + i;
+        out[o] = h0;
+        if (np > 1) out[part_stride + o] = h1;
+        if (np > 2) out[2 * part_stride + o] = h2;
+    }
+}
+
 // --------------------------------------------------------------- tensor maps
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -383,13 +502,13 @@ bool make_map(CUtensorMap* map, const void* base, int rows, int Kp, int np, size
 
 template <int NP>
 mg_status_t launch_gemm_np(mg_handle_t h, const CUtensorMap& ma, const CUtensorMap& mb, float* C, int ldc, int M,
-                           int N, int Kp, float alpha, float beta, int* err, int max_ctas) {
+                           int N, int Kp, float alpha, float beta, int* err, int max_ctas, int stream_c) {
     auto kern = bf16x_gemm_kernel<NP>;
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<NP>::SMEM));
     const int tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
     const int cap = max_ctas > 0 && max_ctas < h->num_sms ? max_ctas : h->num_sms;
     const int grid = tiles < cap ? tiles : cap;
-    kern<<<grid, THREADS, Cfg<NP>::SMEM, h->stream>>>(ma, mb, C, ldc, M, N, Kp, alpha, beta, err);
+    kern<<<grid, THREADS, Cfg<NP>::SMEM, h->stream>>>(ma, mb, C, ldc, M, N, Kp, alpha, beta, stream_c, err);
     return mg::post_launch(h, "bf16x_gemm_kernel");
 }
 
@@ -424,12 +543,22 @@ mg_status_t bf16x_split(mg_handle_t h, bool a_side, const TIN* X, int ldx, int r
 template mg_status_t bf16x_split<float>(mg_handle_t, bool, const float*, int, int, int, int, void*);
 template mg_status_t bf16x_split<double>(mg_handle_t, bool, const double*, int, int, int, int, void*);
 
+mg_status_t bf16x_trsm_split(mg_handle_t h, const float* L11, int lda, float* A12, int nt, int w, int np, void* out) {
+    if (nt <= 0 || w <= 0) return MG_OK;
+    if (w > TS_W) return fail(h, MG_ERR_ARG, "bf16x_trsm_split: panel width %d > %d", w, TS_W);
+    const int Kp = (w + BK - 1) / BK * BK;
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(trsm_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TS_SMEM));
+    trsm_split_kernel<<<(nt + TS_C - 1) / TS_C, TS_THREADS, TS_SMEM, h->stream>>>(L11, lda, A12, nt, w, np, Kp,
+                                                                                 (size_t)nt * Kp, (__nv_bfloat16*)out);
+    return post_launch(h, "trsm_split_kernel");
+}
+
 // C = alpha * (split A)(split B) + beta * C from pre-split operands.
 int bf16x_kpad(int K) { return (K + BK - 1) / BK * BK; }
 
 mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, float alpha, const void* Asplit,
                                 const void* Bsplit, float beta, float* C, int ldc, int* err, size_t a_term,
-                                size_t b_term, int max_ctas) {
+                                size_t b_term, int max_ctas, bool stream_c) {
     if (M == 0 || N == 0) return MG_OK;
     const int Kp = (K + BK - 1) / BK * BK;
     if (!a_term) a_term = (size_t)M * Kp;
@@ -442,9 +571,9 @@ mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, floa
     ProfScope prof(h, "gemm_bf16x", 2.0 * M * N * (double)Kp * nprod,
                    (beta == 0.f ? 4.0 : 8.0) * M * N + 2.0 * np * (double)(M + N) * Kp);
     switch (np) {
-        case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas);
-        case 2: return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas);
-        default: return launch_gemm_np<3>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas);
+        case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c);
+        case 2: return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c);
+        default: return launch_gemm_np<3>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c);
     }
 }
 

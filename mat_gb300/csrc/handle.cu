@@ -26,6 +26,8 @@ mg_status_t ensure_lookahead(mg_handle_t h) {
     MG_CHECK_CUDA(h, cudaDeviceGetStreamPriorityRange(&least, &greatest));
     MG_CHECK_CUDA(h, cudaStreamCreateWithPriority(&h->la_stream, cudaStreamNonBlocking, least));
     for (cudaEvent_t& e : h->la_ev) MG_CHECK_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    MG_CHECK_CUDA(h, cudaStreamCreateWithFlags(&h->pp_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : h->pp_ev) MG_CHECK_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return MG_OK;
 }
 
@@ -197,6 +199,12 @@ mg_status_t mg_handle_destroy(mg_handle_t h) {
         cudaStreamDestroy(h->la_stream);
     }
     for (cudaEvent_t e : h->la_ev)
+        if (e) cudaEventDestroy(e);
+    if (h->pp_stream) {
+        cudaStreamSynchronize(h->pp_stream);
+        cudaStreamDestroy(h->pp_stream);
+    }
+    for (cudaEvent_t e : h->pp_ev)
         if (e) cudaEventDestroy(e);
     if (h->ws) cudaFree(h->ws);
     if (h->hws) cudaFreeHost(h->hws);

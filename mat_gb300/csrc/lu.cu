@@ -294,52 +294,6 @@ __global__ void trsm_lunn_kernel(int k, int n, const T* __restrict__ U, int ldu,
     for (int i = 0; i < k; ++i) X[i + (size_t)col * ldx] = sx[i * nt + t];
 }
 
-// Inverse of the unit-lower k x k block L (k <= 128) into Linv (ld ldinv,
-// zeros above the diagonal): one warp per column j of the inverse (grid of
-// ceil(k/8) CTAs of 8 warps), L staged in shared memory.  Column j is the
-// forward substitution of e_j, x_i -= L(i,kk) x_kk for i > kk, kk = j..k-2,
-// each lane holding rows lane, lane+32, lane+64, lane+96; x_kk reaches the
-// other lanes by one shuffle per step.
-constexpr int INV_LD = 128;
-
-__global__ void __launch_bounds__(256) inv_unit_lower_kernel(const float* __restrict__ L, int ldl, int k,
-                                                               float* __restrict__ Linv, int ldinv) {
-    extern __shared__ float sl[];  // L, ld INV_LD
-    {  // 64 loads per thread issued together (an in-order load->store loop would wait on each)
-        float t[INV_LD * INV_LD / 256];
-#pragma unroll
-        for (int q = 0; q < INV_LD * INV_LD / 256; ++q) {
-            const int e = threadIdx.x + q * 256, r = e & (INV_LD - 1), c = e / INV_LD;
-            t[q] = (r < k && c < k) ? L[r + (size_t)c * ldl] : 0.f;
-        }
-#pragma unroll
-        for (int q = 0; q < INV_LD * INV_LD / 256; ++q) sl[threadIdx.x + q * 256] = t[q];
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int j = blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (j >= k) return;
-    float x[4];
-#pragma unroll
-    for (int t = 0; t < 4; ++t) x[t] = lane + 32 * t == j ? 1.f : 0.f;
-    for (int kk = j; kk < k - 1; ++kk) {
-        const int sk = kk >> 5;
-        const float mine = sk == 0 ? x[0] : sk == 1 ? x[1] : sk == 2 ? x[2] : x[3];
-        const float xk = __shfl_sync(0xffffffffu, mine, kk & 31);
-        const float* lc = sl + kk * INV_LD;
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const int i = lane + 32 * t;
-            if (i > kk && i < k) x[t] = fmaf(-lc[i], xk, x[t]);
-        }
-    }
-#pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        const int i = lane + 32 * t;
-        if (i < k) Linv[i + (size_t)j * ldinv] = x[t];
-    }
-}
-
 __global__ void iota_kernel(int* p, int n) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = i;
 }
@@ -630,10 +584,6 @@ mg_status_t dlu_nopiv_impl(mg_handle_t h, int n, double* A, int lda, int* info_o
 // ----------------------------------------------------------- mixed (fp32)
 size_t sgetrf_xchg_bytes(int num_sms) { return getrf_ws_bytes<float>(num_sms); }
 
-size_t sgetrf_tri_bytes(int nb, int nterms) {
-    return align_up((size_t)nb * nb * sizeof(float), 1024) + bf16x_split_bytes(nb, nb, nterms);
-}
-
 // FP32 panel: one 16-CTA cluster (panel_f32.cu) when the panel is too tall
 // for one CTA's shared memory and fits the cluster; else the cooperative grid
 // (or, for short panels, the single-CTA) kernel.  Same factors either way.
@@ -658,28 +608,25 @@ struct OnStream {
 // with a look-ahead of one panel.  Step k on the handle's stream S:
 //
 //   [wait for the far update of step k-1] interchanges of panel k on the
-//   columns to its right -> U12 = L11^{-1} A12 (split-BF16 GEMM) -> split
-//   U12 -> update of the next panel's columns (near update) -> panel k+1 ->
-//   its interchanges on the columns to its left -> inverse of its L11 ->
-//   splits of L11^{-1} and L21 (L21 into the buffer of parity k+1)
+//   columns to its right -> U12 = L11^{-1} A12 and its split terms (one
+//   kernel) -> update of the next panel's columns (near update) -> panel
+//   k+1 -> its interchanges on the columns to its left -> split of its L21
+//   (into the buffer of parity k+1)
 //
 // while a low-priority side stream runs the far update (the trailing
 // columns beyond the next panel) of step k on num_sms - 16 CTAs as soon as
 // the near update is done.  The panel is queued directly behind the near
 // update on S and submitted before the far update, so its 16-CTA cluster
-// takes its SMs before the far update's persistent grid fills the rest.  A panel too tall for the cluster (the
-// cooperative grid) is not overlapped.
+// takes its SMs before the far update's persistent grid fills the rest.  A
+// panel too tall for the cluster (the cooperative grid) is not overlapped.
 //
 // The trailing updates run on the BF16 tensor cores with `nterms` split
 // terms (fp32 accumulation).  `xchg` holds sgetrf_xchg_bytes(); splitA and
-// splitA2 / splitB hold bf16x_split_bytes(n, nb, nterms); `tri` holds
-// sgetrf_tri_bytes(nb, nterms); if Linv_all is not NULL the inverse of every
-// diagonal block of L is kept there (nb*nb floats each, ld nb).  The
-// block-row solve U12 = L11^{-1} A12 is an explicit inverse of L11 followed
-// by a split-BF16 GEMM (the refinement absorbs its fp32-level error).
+// splitA2 / splitB hold bf16x_split_bytes(n, nb, nterms).  The block-row
+// solve U12 = L11^{-1} A12 is one FP32 substitution kernel that also writes
+// U12's split terms (bf16x_trsm_split).
 mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int nb, int nterms, void* xchg,
-                         void* splitA, void* splitA2, void* splitB, void* tri, float* Linv_all, int* gemm_err,
-                         int* info_out) {
+                         void* splitA, void* splitA2, void* splitB, int* gemm_err, int* info_out) {
     if (info_out) *info_out = 0;
     if (n == 0) return MG_OK;
     if (nb > PANEL_MAX_NB || nb > 128) return fail(h, MG_ERR_ARG, "sgetrf_mixed: block size %d > 128", nb);
@@ -690,9 +637,6 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
     MG_CHECK_CUDA(h, cudaMemsetAsync(xchg, 0, 256, S));
     iota_kernel<<<(n + 255) / 256, 256, 0, S>>>(pos, n);
     MG_TRY(post_launch(h, "iota_kernel"));
-    const size_t ism = (size_t)INV_LD * INV_LD * sizeof(float);
-    MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_unit_lower_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism));
-    void* const splitT = (char*)tri + align_up((size_t)nb * nb * sizeof(float), 1024);
     void* const splitL[2] = {splitA, splitA2};
     const bool cluster_ok = panel_cluster_rows(h) > 0;
     const int nsteps = (n + nb - 1) / nb;
@@ -702,22 +646,31 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
         const int r = k * nb, w = nb < n - r ? nb : n - r;
         return launch_panel_f32(h, c, A, lda, n, r, w, pos);
     };
+    // after panel k, on the side stream P (off the critical path): its
+    // interchanges on the columns to its left and the split of its L21; the
+    // next near update waits for them (event pp_ev[1]), and so, through it,
+    // does the panel that next overwrites the pivot list
+    bool pp_pending = false;
     auto after_panel = [&](int k) -> mg_status_t {
         const int r = k * nb, w = nb < n - r ? nb : n - r;
-        MG_TRY(launch_laswp<float>(h, A, lda, r, w, c.piv, r, n, n));  // columns [0, r)
-        float* Lout = Linv_all ? Linv_all + (size_t)k * nb * nb : (float*)tri;
-        const int ldo = Linv_all ? nb : w;
-        if (Linv_all || r + w < n) {
-            ProfScope prof(h, "trsm_f32", 2.0 * w * w * (double)w / 3.0, 8.0 * w * (double)w);
-            inv_unit_lower_kernel<<<(w + 7) / 8, 256, ism, h->stream>>>(A + r + (size_t)r * lda, lda, w, Lout, ldo);
-            MG_TRY(post_launch(h, "inv_unit_lower_kernel"));
+        MG_CHECK_CUDA(h, cudaEventRecord(h->pp_ev[0], S));
+        MG_CHECK_CUDA(h, cudaStreamWaitEvent(h->pp_stream, h->pp_ev[0], 0));
+        {
+            OnStream on(h, h->pp_stream);
+            MG_TRY(launch_laswp<float>(h, A, lda, r, w, c.piv, r, n, n));  // columns [0, r)
+            if (r + w < n) {
+                const int nt = n - (r + w);
+                ProfScope prof(h, "split", 0.0, 2.0 * nt * w * (4.0 + 2.0 * nterms));
+                MG_TRY(bf16x_split<float>(h, true, A + (r + w) + (size_t)r * lda, lda, nt, w, nterms, splitL[k & 1]));
+            }
+            MG_CHECK_CUDA(h, cudaEventRecord(h->pp_ev[1], h->pp_stream));
         }
-        if (r + w < n) {
-            const int nt = n - (r + w);
-            ProfScope prof(h, "split", 0.0, 2.0 * (nt + w) * w * (4.0 + 2.0 * nterms));
-            MG_TRY(bf16x_split<float>(h, true, Lout, ldo, w, w, nterms, splitT));
-            MG_TRY(bf16x_split<float>(h, true, A + (r + w) + (size_t)r * lda, lda, nt, w, nterms, splitL[k & 1]));
-        }
+        pp_pending = true;
+        return MG_OK;
+    };
+    auto wait_after_panel = [&]() -> mg_status_t {
+        if (pp_pending) MG_CHECK_CUDA(h, cudaStreamWaitEvent(S, h->pp_ev[1], 0));
+        pp_pending = false;
         return MG_OK;
     };
     // a panel overlaps the previous trailing update only on the cluster path
@@ -739,19 +692,15 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
         MG_TRY(launch_laswp<float>(h, A, lda, r, w, c.piv, 0, r + w, n));  // columns [r + w, n)
         float* A12 = A + r + (size_t)(r + w) * lda;
         {
-            ProfScope prof(h, "trsm_f32", 2.0 * w * w * (double)nt, 8.0 * w * (double)nt);
-            MG_TRY(bf16x_split<float>(h, false, A12, lda, nt, w, nterms, splitB));
-            MG_TRY(bf16x_gemm_presplit(h, nterms, w, nt, w, 1.0f, splitT, splitB, 0.0f, A12, lda, gemm_err));
+            ProfScope prof(h, "trsm_f32", (double)w * w * (double)nt, 8.0 * w * (double)nt);
+            MG_TRY(bf16x_trsm_split(h, A + r + (size_t)r * lda, lda, A12, nt, w, nterms, splitB));
         }
-        {
-            ProfScope prof(h, "split", 0.0, 2.0 * nt * w * (4.0 + 2.0 * nterms));
-            MG_TRY(bf16x_split<float>(h, false, A12, lda, nt, w, nterms, splitB));
-        }
+        MG_TRY(wait_after_panel());
         const void* L21 = splitL[k & 1];
         float* A22 = A + (r + w) + (size_t)(r + w) * lda;
         const int w1 = nb < nt ? nb : nt;  // the next panel's columns
         MG_TRY(bf16x_gemm_presplit(h, nterms, nt, w1, w, -1.0f, L21, splitB, 1.0f, A22, lda, gemm_err, 0,
-                                   (size_t)nt * kp));
+                                   (size_t)nt * kp, 0, false));  // the next panel: kept in L2
         const bool ov = overlappable(k + 1);
         const void* Brest = (const char*)splitB + (size_t)w1 * kp * 2;
         if (nt > w1 && ov) {
@@ -778,6 +727,7 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
         MG_TRY(after_panel(k + 1));
     }
     if (far_pending) MG_CHECK_CUDA(h, cudaStreamWaitEvent(S, h->la_ev[1], 0));
+    MG_TRY(wait_after_panel());
     int* hw = (int*)h->hws;
     MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, c.ws.err, sizeof(int), cudaMemcpyDeviceToHost, S));
     MG_CHECK_CUDA(h, cudaMemcpyAsync(hw + 1, c.ws.info, sizeof(int), cudaMemcpyDeviceToHost, S));
@@ -951,14 +901,12 @@ mg_status_t mg_sgetrf(mg_handle_t h, int n, float* A, int lda, int* pos, int* in
     const size_t oSA = take(mg::bf16x_split_bytes(n, nb, nterms));
     const size_t oSA2 = take(mg::bf16x_split_bytes(n, nb, nterms));
     const size_t oSB = take(mg::bf16x_split_bytes(n, nb, nterms));
-    const size_t oT = take(mg::sgetrf_tri_bytes(nb, nterms));
     const size_t oE = take(64);
     MG_TRY(mg::ensure_ws(h, off));
     char* b = (char*)h->ws;
     int* gerr = (int*)(b + oE);
     MG_CHECK_CUDA(h, cudaMemsetAsync(gerr, 0, 64, h->stream));
-    return mg::sgetrf_mixed(h, n, A, lda, pos, nb, nterms, b + oX, b + oSA, b + oSA2, b + oSB, b + oT, nullptr, gerr,
-                            info);
+    return mg::sgetrf_mixed(h, n, A, lda, pos, nb, nterms, b + oX, b + oSA, b + oSA2, b + oSB, gerr, info);
 }
 
 mg_status_t mg_dgetrf_noalloc(void* cuda_stream, int m, int n, double* A, int lda, int* pos, int* info) {

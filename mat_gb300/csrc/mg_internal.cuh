@@ -32,6 +32,10 @@ struct mg_handle_s {
     // ordering events.
     cudaStream_t la_stream = nullptr;
     cudaEvent_t la_ev[2] = {nullptr, nullptr};
+    // Side stream (normal priority) for the work that follows a panel
+    // off the critical path, and its two ordering events.
+    cudaStream_t pp_stream = nullptr;
+    cudaEvent_t pp_ev[2] = {nullptr, nullptr};
     char last_error[512] = {0};
     // Optional per-phase timing with CUDA events on the handle's stream.
     struct ProfRec {
@@ -129,11 +133,17 @@ mg_status_t bf16x_split(mg_handle_t h, bool a_side, const TIN* X, int ldx, int r
 // a_term / b_term: elements between the split terms of A / B (0: M*Kp /
 // N*Kp, i.e. a whole split operand; larger when the operand is a row or
 // column window of a bigger split).  max_ctas > 0 caps the persistent grid.
+// stream_c: C passes through L2 once (evict-first policy); false when C is
+// read again soon (the next panel's columns).
 mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, float alpha, const void* Asplit,
                                 const void* Bsplit, float beta, float* C, int ldc, int* err, size_t a_term = 0,
-                                size_t b_term = 0, int max_ctas = 0);
+                                size_t b_term = 0, int max_ctas = 0, bool stream_c = true);
 // K rounded up to the split GEMM's K step (elements per row of a split term).
 int bf16x_kpad(int K);
+// A12 (w x nt, ld lda) := L11^{-1} A12 with L11 (w x w, ld lda) unit lower,
+// w <= 128, in FP32; out receives U12's np split terms as a B operand
+// (bf16x_split_bytes(nt, w, np)).
+mg_status_t bf16x_trsm_split(mg_handle_t h, const float* L11, int lda, float* A12, int nt, int w, int np, void* out);
 
 // FP32 panel on one thread-block cluster (panel_f32.cu): rows it can take
 // (0 if unavailable), and the launch (piv relative to r0; pos updated).
@@ -143,12 +153,10 @@ mg_status_t sgetf2_cluster(mg_handle_t h, float* A, int lda, int m, int r0, int 
 
 // FP32 LU with split-BF16 trailing updates (lu.cu).  splitA and splitA2
 // each hold bf16x_split_bytes(n, nb, nterms) (the L21 split of alternate
-// steps), splitB the same, tri sgetrf_tri_bytes(nb, nterms).
+// steps), splitB the same.
 size_t sgetrf_xchg_bytes(int num_sms);
-size_t sgetrf_tri_bytes(int nb, int nterms);
 mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int nb, int nterms, void* xchg,
-                         void* splitA, void* splitA2, void* splitB, void* tri, float* Linv_all, int* gemm_err,
-                         int* info_out);
+                         void* splitA, void* splitA2, void* splitB, int* gemm_err, int* info_out);
 // Side stream and events of the look-ahead LU (created once per handle).
 mg_status_t ensure_lookahead(mg_handle_t h);
 

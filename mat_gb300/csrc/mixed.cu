@@ -31,33 +31,55 @@ constexpr int MAX_RHS = 8;
 constexpr int RES_ROWS = 256;      // rows per residual CTA
 constexpr int RES_KCHUNK = 2048;   // columns per residual CTA (k split)
 
-__global__ void d2s_kernel(const double* __restrict__ A, int lda, int n, float* __restrict__ S, int lds) {
-    const size_t total = (size_t)n * n;
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-        const size_t r = e % n, c = e / n;
-        S[r + c * lds] = (float)A[r + c * lda];
-    }
-}
-
 __device__ __forceinline__ void atomic_max_nonneg(double* addr, double v);
 
-// partial[kc][i] = sum_{k in chunk kc} |A(i,k)|  (row sums of |A|); also
-// *amax = max |A(i,k)| (for the pivot-growth factor)
-__global__ void absrow_partial_kernel(const double* __restrict__ A, int lda, int n, double* __restrict__ partial,
-                                      double* __restrict__ amax) {
+// The fp32 copy of A and the row sums of |A| in one pass over A (one read
+// of the FP64 matrix): S(i,k) = fp32(A(i,k)), partial[kc][i] = sum over the
+// chunk kc of |A(i,k)|, *amax = max |A(i,k)|.  Threads run down rows
+// (coalesced), eight columns' loads in flight per thread.  The FP64 pipe is
+// the scarce unit here, so each element costs one conversion on it: the
+// maximum compares the bit patterns of |a| as integers, the sums add the
+// fp32 values in groups of eight and only the group sums in FP64 (relative
+// error ~1e-7 in the norm, which only scales the backward error).
+__global__ void d2s_absrow_kernel(const double* __restrict__ A, int lda, int n, float* __restrict__ S, int lds,
+                                  double* __restrict__ partial, double* __restrict__ amax) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int k0 = blockIdx.y * RES_KCHUNK, k1 = min(n, k0 + RES_KCHUNK);
-    double s = 0.0, mx = 0.0;
-    if (i < n)
-        for (int k = k0; k < k1; ++k) {
-            const double a = fabs(A[i + (size_t)k * lda]);
-            s += a;
-            mx = fmax(mx, a);
-        }
-    if (i < n) partial[(size_t)blockIdx.y * n + i] = s;
+    double s = 0.0;
+    unsigned long long mxb = 0ull;  // bits of max |a| (non-negative doubles order like their bits)
+    if (i < n) {
+        int k = k0;
+        for (; k + 8 <= k1; k += 8) {
+            double a[8];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
-    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(amax, mx);
+            for (int u = 0; u < 8; ++u) a[u] = A[i + (size_t)(k + u) * lda];
+            float g = 0.f;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const float f = (float)a[u];
+                S[i + (size_t)(k + u) * lds] = f;
+                g += fabsf(f);
+                const unsigned long long b = (unsigned long long)__double_as_longlong(a[u]) & 0x7fffffffffffffffull;
+                mxb = b > mxb ? b : mxb;
+            }
+            s += (double)g;
+        }
+        for (; k < k1; ++k) {
+            const double a = A[i + (size_t)k * lda];
+            const float f = (float)a;
+            S[i + (size_t)k * lds] = f;
+            s += (double)fabsf(f);
+            const unsigned long long b = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
+            mxb = b > mxb ? b : mxb;
+        }
+        partial[(size_t)blockIdx.y * n + i] = s;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long o = __shfl_down_sync(0xffffffffu, mxb, off);
+        mxb = o > mxb ? o : mxb;
+    }
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(amax, __longlong_as_double((long long)mxb));
 }
 
 // *umax = max |U(i,j)| over the upper triangle of the packed fp32 LU (one CTA
@@ -482,7 +504,6 @@ struct IrWs {
     void* splitA;
     void* splitA2;
     void* splitB;
-    void* tri;
     int* gemm_err;
     float* Linv;
     float* Uinv;
@@ -508,7 +529,6 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
     const size_t oSA = take(mg::bf16x_split_bytes(n, IR_BLOCK, nterms));
     const size_t oSA2 = take(mg::bf16x_split_bytes(n, IR_BLOCK, nterms));
     const size_t oSB = take(mg::bf16x_split_bytes(n, IR_BLOCK, nterms));
-    const size_t oT = take(mg::sgetrf_tri_bytes(IR_BLOCK, nterms));
     const size_t oE = take(64);
     const size_t oLi = take((size_t)nblk * IR_BLOCK * IR_BLOCK * sizeof(float));
     const size_t oUi = take((size_t)nblk * IR_BLOCK * IR_BLOCK * sizeof(float));
@@ -526,7 +546,6 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
         w->splitA = b + oSA;
         w->splitA2 = b + oSA2;
         w->splitB = b + oSB;
-        w->tri = b + oT;
         w->gemm_err = (int*)(b + oE);
         w->Linv = (float*)(b + oLi);
         w->Uinv = (float*)(b + oUi);
@@ -584,18 +603,17 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     mg::ProfScope* setup = new mg::ProfScope(h, "ir_setup", 0.0, 12.0 * n * (double)n);
     MG_CHECK_CUDA(h, cudaMemsetAsync(w.gemm_err, 0, 64, st));
     MG_CHECK_CUDA(h, cudaMemsetAsync(w.norms, 0, 64 * sizeof(double), st));
-    absrow_partial_kernel<<<dim3((n + 255) / 256, kch), 256, 0, st>>>(A, lda, n, w.partial, w.norms + 17);
-    MG_TRY(mg::post_launch(h, "absrow_partial_kernel"));
+    // fp32 copy and the row sums of |A| (one pass), then ||A||_inf
+    d2s_absrow_kernel<<<dim3((n + 255) / 256, kch), 256, 0, st>>>(A, lda, n, w.A32, n, w.partial, w.norms + 17);
+    MG_TRY(mg::post_launch(h, "d2s_absrow_kernel"));
     absrow_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kch, n, w.norms + 16);
     MG_TRY(mg::post_launch(h, "absrow_reduce_kernel"));
-
-    // fp32 copy and mixed LU -------------------------------------------------
-    d2s_kernel<<<grid_for((size_t)n * n, 256, cap), 256, 0, st>>>(A, lda, n, w.A32, n);
-    MG_TRY(mg::post_launch(h, "d2s_kernel"));
     delete setup;
+
+    // mixed LU ---------------------------------------------------------------
     int info = 0;
     mg_status_t s = mg::sgetrf_mixed(h, n, w.A32, n, w.pos, IR_BLOCK, o.nterms, w.xchg, w.splitA, w.splitA2, w.splitB,
-                                     w.tri, w.Linv, w.gemm_err, &info);
+                                     w.gemm_err, &info);
     if (s != MG_OK && s != MG_SINGULAR) return s;
     r.info = info;
     absmax_upper_kernel<<<n, 256, 0, st>>>(w.A32, n, w.norms + 18);
@@ -604,6 +622,12 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
                                           2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
+    // inverses of the diagonal blocks of L and U (the solves' block steps);
+    // L's blocks are final once their panel is done (later interchanges only
+    // touch rows below them)
+    inv_diag_blocks_kernel<true><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
+                                                                                                 w.Linv);
+    MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<lower>"));
     inv_diag_blocks_kernel<false><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
                                                                                                   w.Uinv);
     MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<upper>"));
