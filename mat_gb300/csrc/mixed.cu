@@ -35,51 +35,99 @@ __device__ __forceinline__ void atomic_max_nonneg(double* addr, double v);
 
 // The fp32 copy of A and the row sums of |A| in one pass over A (one read
 // of the FP64 matrix): S(i,k) = fp32(A(i,k)), partial[kc][i] = sum over the
-// chunk kc of |A(i,k)|, *amax = max |A(i,k)|.  Threads run down rows
-// (coalesced), eight columns' loads in flight per thread.  The FP64 pipe is
-// the scarce unit here, so each element costs one conversion on it: the
-// maximum compares the bit patterns of |a| as integers, the sums add the
-// fp32 values in groups of eight and only the group sums in FP64 (relative
-// error ~1e-7 in the norm, which only scales the backward error).
-__global__ void d2s_absrow_kernel(const double* __restrict__ A, int lda, int n, float* __restrict__ S, int lds,
-                                  double* __restrict__ partial, double* __restrict__ amax) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int k0 = blockIdx.y * RES_KCHUNK, k1 = min(n, k0 + RES_KCHUNK);
-    double s = 0.0;
-    unsigned long long mxb = 0ull;  // bits of max |a| (non-negative doubles order like their bits)
-    if (i < n) {
+// column chunk kc (D2S_KCHUNK columns) of |A(i,k)|, *amax = max |A(i,k)|.
+// Each thread takes four consecutive rows (two 16-byte loads and one
+// 16-byte store per column; a CTA covers 1024 rows, 8 KB of a column), eight
+// columns' loads in flight.  Nothing runs on the FP64 pipe: the conversion
+// is d2f_rn, the maximum and the chunk sums use the fp32 values (relative
+// error ~1e-5 at most in ||A||_inf, which only scales the backward error;
+// max |A| feeds the pivot-growth report).  Needs lda and n multiples of 4
+// (checked by the caller, else d2s_absrow_scalar_kernel).
+constexpr int D2S_KCHUNK = 256;
+constexpr int D2S_ROWS = 1024;  // rows per CTA (256 threads x 4)
+
+// double -> float, round to nearest even, with 32-bit integer operations
+// for values in the normal float range (on GB300 the conversion instruction,
+// and 64-bit integer arithmetic, run on the FP64 pipe, which limited this
+// pass): the exponent is rebased by 1023 - 127, the top 23 mantissa bits
+// are kept, and the 29 dropped ones round up when above half an ulp or at
+// half with an odd kept part (ties to even); a carry out of the mantissa
+// moves into the exponent, up to +inf.  Zeros, subnormal results,
+// infinities and NaNs take the hardware conversion.
+__device__ __forceinline__ float d2f_rn(double d) {
+    const unsigned int hi = (unsigned int)__double2hiint(d), lo = (unsigned int)__double2loint(d);
+    const unsigned int e = (hi >> 20) & 0x7ffu;
+    if (e - 897u <= 1150u - 897u) {
+        unsigned int f = ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+        const unsigned int rnd = (lo >> 28) & 1u, sticky = (lo & 0x0fffffffu) != 0u;
+        f += rnd & (sticky | (f & 1u));
+        return __uint_as_float(f | (hi & 0x80000000u));
+    }
+    return (float)d;
+}
+
+__global__ void __launch_bounds__(256) d2s_absrow_kernel(const double* __restrict__ A, int lda, int n,
+                                                         float* __restrict__ S, int lds, double* __restrict__ partial,
+                                                         double* __restrict__ amax) {
+    const int i0 = blockIdx.x * D2S_ROWS + 4 * threadIdx.x;
+    const int k0 = blockIdx.y * D2S_KCHUNK, k1 = min(n, k0 + D2S_KCHUNK);
+    float s[4] = {0.f, 0.f, 0.f, 0.f};
+    float mx = 0.f;
+    if (i0 < n) {  // n is a multiple of 4 here
         int k = k0;
         for (; k + 8 <= k1; k += 8) {
-            double a[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) a[u] = A[i + (size_t)(k + u) * lda];
-            float g = 0.f;
+            double2 a[8][2];
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
-                const float f = (float)a[u];
-                S[i + (size_t)(k + u) * lds] = f;
-                g += fabsf(f);
-                const unsigned long long b = (unsigned long long)__double_as_longlong(a[u]) & 0x7fffffffffffffffull;
-                mxb = b > mxb ? b : mxb;
+                const double2* p = reinterpret_cast<const double2*>(A + i0 + (size_t)(k + u) * lda);
+                a[u][0] = p[0];
+                a[u][1] = p[1];
             }
-            s += (double)g;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const float4 f = make_float4(d2f_rn(a[u][0].x), d2f_rn(a[u][0].y), d2f_rn(a[u][1].x), d2f_rn(a[u][1].y));
+                *reinterpret_cast<float4*>(S + i0 + (size_t)(k + u) * lds) = f;
+                s[0] += fabsf(f.x);
+                s[1] += fabsf(f.y);
+                s[2] += fabsf(f.z);
+                s[3] += fabsf(f.w);
+                mx = fmaxf(mx, fmaxf(fmaxf(fabsf(f.x), fabsf(f.y)), fmaxf(fabsf(f.z), fabsf(f.w))));
+            }
         }
-        for (; k < k1; ++k) {
-            const double a = A[i + (size_t)k * lda];
-            const float f = (float)a;
-            S[i + (size_t)k * lds] = f;
-            s += (double)fabsf(f);
-            const unsigned long long b = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
-            mxb = b > mxb ? b : mxb;
-        }
-        partial[(size_t)blockIdx.y * n + i] = s;
+        for (; k < k1; ++k)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const float f = d2f_rn(A[i0 + r + (size_t)k * lda]);
+                S[i0 + r + (size_t)k * lds] = f;
+                s[r] += fabsf(f);
+                mx = fmaxf(mx, fabsf(f));
+            }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) partial[(size_t)blockIdx.y * n + i0 + r] = (double)s[r];
     }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const unsigned long long o = __shfl_down_sync(0xffffffffu, mxb, off);
-        mxb = o > mxb ? o : mxb;
+    for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(amax, (double)mx);
+}
+
+// The same for any lda / lds (one row per thread, scalar accesses).
+__global__ void d2s_absrow_scalar_kernel(const double* __restrict__ A, int lda, int n, float* __restrict__ S, int lds,
+                                         double* __restrict__ partial, double* __restrict__ amax) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k0 = blockIdx.y * D2S_KCHUNK, k1 = min(n, k0 + D2S_KCHUNK);
+    float s = 0.f, mx = 0.f;
+    if (i < n) {
+        for (int k = k0; k < k1; ++k) {
+            const float f = d2f_rn(A[i + (size_t)k * lda]);
+            S[i + (size_t)k * lds] = f;
+            s += fabsf(f);
+            mx = fmaxf(mx, fabsf(f));
+        }
+        partial[(size_t)blockIdx.y * n + i] = (double)s;
     }
-    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(amax, __longlong_as_double((long long)mxb));
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(amax, (double)mx);
 }
 
 // *umax = max |U(i,j)| over the upper triangle of the packed fp32 LU (one CTA
@@ -533,7 +581,8 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
     const size_t oLi = take((size_t)nblk * IR_BLOCK * IR_BLOCK * sizeof(float));
     const size_t oUi = take((size_t)nblk * IR_BLOCK * IR_BLOCK * sizeof(float));
     const size_t oR = take((size_t)n * nrhs * sizeof(double));
-    const size_t oPa = take((size_t)kch * n * std::max(nrhs, 1) * sizeof(double));
+    const int kd2s = (n + D2S_KCHUNK - 1) / D2S_KCHUNK;
+    const size_t oPa = take((size_t)std::max(kch * std::max(nrhs, 1), kd2s) * n * sizeof(double));
     const size_t oN = take(64 * sizeof(double));
     const size_t oF = take(2 * (size_t)nblk * sizeof(unsigned));
     const size_t oY = take((size_t)n * nrhs * sizeof(float));
@@ -604,9 +653,17 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     MG_CHECK_CUDA(h, cudaMemsetAsync(w.gemm_err, 0, 64, st));
     MG_CHECK_CUDA(h, cudaMemsetAsync(w.norms, 0, 64 * sizeof(double), st));
     // fp32 copy and the row sums of |A| (one pass), then ||A||_inf
-    d2s_absrow_kernel<<<dim3((n + 255) / 256, kch), 256, 0, st>>>(A, lda, n, w.A32, n, w.partial, w.norms + 17);
-    MG_TRY(mg::post_launch(h, "d2s_absrow_kernel"));
-    absrow_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kch, n, w.norms + 16);
+    const int kd2s = (n + D2S_KCHUNK - 1) / D2S_KCHUNK;
+    if ((lda & 3) == 0 && (n & 3) == 0 && ((reinterpret_cast<uintptr_t>(A) & 15) == 0)) {
+        d2s_absrow_kernel<<<dim3((n + D2S_ROWS - 1) / D2S_ROWS, kd2s), 256, 0, st>>>(A, lda, n, w.A32, n, w.partial,
+                                                                                   w.norms + 17);
+        MG_TRY(mg::post_launch(h, "d2s_absrow_kernel"));
+    } else {
+        d2s_absrow_scalar_kernel<<<dim3((n + 255) / 256, kd2s), 256, 0, st>>>(A, lda, n, w.A32, n, w.partial,
+                                                                            w.norms + 17);
+        MG_TRY(mg::post_launch(h, "d2s_absrow_scalar_kernel"));
+    }
+    absrow_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kd2s, n, w.norms + 16);
     MG_TRY(mg::post_launch(h, "absrow_reduce_kernel"));
     delete setup;
 

@@ -31,7 +31,7 @@ def backward_error(a, x, b):
     return (np.abs(r).max(0) / (np.abs(a).sum(1).max() * np.abs(x).max(0) + np.abs(b).max(0))).max()
 
 
-@pytest.mark.parametrize("n,nrhs", [(300, 1), (1024, 4), (2500, 4)])
+@pytest.mark.parametrize("n,nrhs", [(300, 1), (1024, 4), (2500, 4), (1001, 3)])  # 1001: unaligned columns
 def test_mixed_ir_reaches_fp64_backward_error(handle, n, nrhs):
     A = svd_matrix(handle, n)
     B = colmajor(n, nrhs)
