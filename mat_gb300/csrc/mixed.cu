@@ -382,9 +382,12 @@ __global__ void __launch_bounds__(256) trsv_flow_kernel(const float* __restrict_
         for (int q = 0; q < IR_BLOCK * IR_BLOCK / 4 / 256; ++q)
             reinterpret_cast<float4*>(sdinv)[threadIdx.x + q * 256] = t[q];
     }
-    float acc[NR];
+    float acc[NR], win[NR];  // this block's right-hand side, loaded now: it is needed at the end of the chain
 #pragma unroll
-    for (int j = 0; j < NR; ++j) acc[j] = 0.f;
+    for (int j = 0; j < NR; ++j) {
+        acc[j] = 0.f;
+        win[j] = (hf == 0 && r < rows) ? Win[r0 + r + (size_t)j * n] : 0.f;
+    }
     const int nsteps = LOWER ? me : nblk - 1 - me;
     for (int t = 0; t < nsteps; ++t) {
         const int b = LOWER ? t : nblk - 1 - t;
@@ -402,7 +405,7 @@ __global__ void __launch_bounds__(256) trsv_flow_kernel(const float* __restrict_
                     ok = 0;
                     break;
                 }
-                __nanosleep(spins < 64 ? 20 : 100);
+                if (spins > 4096) __nanosleep(100);  // a block step takes a few us: poll tightly first
             }
             s_ok = ok;
         }
@@ -428,7 +431,7 @@ __global__ void __launch_bounds__(256) trsv_flow_kernel(const float* __restrict_
     if (hf == 0)
 #pragma unroll
         for (int j = 0; j < NR; ++j)
-            wb[j][r] = r < rows ? Win[r0 + r + (size_t)j * n] - (part[0][j][r] + part[1][j][r]) : 0.f;
+            wb[j][r] = r < rows ? win[j] - (part[0][j][r] + part[1][j][r]) : 0.f;
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < NR; ++j) acc[j] = 0.f;
