@@ -124,7 +124,7 @@ template <int NP>
 __global__ void __launch_bounds__(THREADS, 1)
     bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       float* __restrict__ C, int ldc, int M, int N, int Kp, float alpha, float beta,
-                      int stream_c, int* __restrict__ err) {
+                      int stream_c, int two_pass, int* __restrict__ err) {
     using CF = Cfg<NP>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -141,6 +141,11 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int num_m = (M + BM - 1) / BM, num_n = (N + BN - 1) / BN;
     const int total = num_m * num_n;
     const int kblocks = Kp / BK;
+    // two_pass (NP >= 2): every k-block's lower-order products first, then
+    // a second pass over K for the leading product A_0 B_0 alone, so that
+    // the tensor cores' accumulation (which rounds relative to the running
+    // sum) adds the small terms while the accumulator is still small
+    const int npass = (two_pass && NP >= 2) ? 2 : 1;
 
     if (threadIdx.x == 0) {
         s_abort = 0;
@@ -178,7 +183,10 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
                 int mb, nb;
                 tile_coords(t, num_m, num_n, mb, nb);
-                for (int kb = 0; kb < kblocks; ++kb) {
+                for (int ks = 0; ks < npass * kblocks && ok; ++ks) {
+                    const int kb = ks % kblocks;
+                    // the leading-product pass needs only the terms A_0, B_0
+                    const int nterm = (npass == 2 && ks >= kblocks) ? 1 : NP;
                     if (!tc::mbar_wait(&empty[stage], phase ^ 1)) {
                         ok = false;
                         break;
@@ -188,8 +196,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                         break;
                     }
                     unsigned char* st = smem + (size_t)stage * CF::STAGE;
-                    tc::mbar_arrive_expect_tx(&full[stage], CF::STAGE);
-                    for (int p = 0; p < NP; ++p) {
+                    tc::mbar_arrive_expect_tx(&full[stage], (uint32_t)nterm * (CF::A_TILE + CF::B_TILE));
+                    for (int p = 0; p < nterm; ++p) {
                         tc::tma_load_3d(st + p * CF::A_TILE, &tmA, &full[stage], kb * BK, mb * BM, p);
                         tc::tma_load_3d(st + NP * CF::A_TILE + p * CF::B_TILE, &tmB, &full[stage], kb * BK,
                                         nb * BN, p);
@@ -223,15 +231,21 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
                 tc::tc_fence_after();
                 const uint32_t d = tmem_base + (uint32_t)(buf * BN);
-                for (int kb = 0; kb < kblocks; ++kb) {
+                for (int ks = 0; ks < npass * kblocks; ++ks) {
                     if (!tc::mbar_wait(&full[stage], phase) || *(volatile int*)&s_abort) {
                         ok = false;
                         break;
                     }
                     tc::tc_fence_after();
                     const uint32_t st = tc::smem_u32(smem + (size_t)stage * CF::STAGE);
+                    // products of this k-block: all (one pass), the lower-order
+                    // ones (first pass) or the leading one (second pass); the
+                    // leading product is the last of the list
+                    const int p_lo = (npass == 2 && ks >= kblocks) ? CF::NPROD - 1 : 0;
+                    const int p_hi = (npass == 2 && ks < kblocks) ? CF::NPROD - 1 : CF::NPROD;
 #pragma unroll
                     for (int p = 0; p < CF::NPROD; ++p) {
+                        if (p < p_lo || p >= p_hi) continue;
                         const uint32_t a0 = st + prod_a(NP, p) * CF::A_TILE;
                         const uint32_t b0 = st + NP * CF::A_TILE + prod_b(NP, p) * CF::B_TILE;
 #pragma unroll
@@ -239,7 +253,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             // advance 16 bf16 = 32 B inside the 64-byte swizzled row
                             const uint64_t ad = tc::smem_desc_sw64(a0 + kk * 32);
                             const uint64_t bd = tc::smem_desc_sw64(b0 + kk * 32);
-                            tc::mma_bf16(d, ad, bd, idesc, (kb | p | kk) != 0);
+                            tc::mma_bf16(d, ad, bd, idesc, (ks | (p - p_lo) | kk) != 0);
                         }
                     }
                     tc::mma_commit(&empty[stage]);
@@ -502,13 +516,15 @@ bool make_map(CUtensorMap* map, const void* base, int rows, int Kp, int np, size
 
 template <int NP>
 mg_status_t launch_gemm_np(mg_handle_t h, const CUtensorMap& ma, const CUtensorMap& mb, float* C, int ldc, int M,
-                           int N, int Kp, float alpha, float beta, int* err, int max_ctas, int stream_c) {
+                           int N, int Kp, float alpha, float beta, int* err, int max_ctas, int stream_c,
+                           int two_pass) {
     auto kern = bf16x_gemm_kernel<NP>;
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<NP>::SMEM));
     const int tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
     const int cap = max_ctas > 0 && max_ctas < h->num_sms ? max_ctas : h->num_sms;
     const int grid = tiles < cap ? tiles : cap;
-    kern<<<grid, THREADS, Cfg<NP>::SMEM, h->stream>>>(ma, mb, C, ldc, M, N, Kp, alpha, beta, stream_c, err);
+    kern<<<grid, THREADS, Cfg<NP>::SMEM, h->stream>>>(ma, mb, C, ldc, M, N, Kp, alpha, beta, stream_c, two_pass,
+                                                       err);
     return mg::post_launch(h, "bf16x_gemm_kernel");
 }
 
@@ -558,7 +574,7 @@ int bf16x_kpad(int K) { return (K + BK - 1) / BK * BK; }
 
 mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, float alpha, const void* Asplit,
                                 const void* Bsplit, float beta, float* C, int ldc, int* err, size_t a_term,
-                                size_t b_term, int max_ctas, bool stream_c) {
+                                size_t b_term, int max_ctas, bool stream_c, bool two_pass) {
     if (M == 0 || N == 0) return MG_OK;
     const int Kp = (K + BK - 1) / BK * BK;
     if (!a_term) a_term = (size_t)M * Kp;
@@ -571,9 +587,11 @@ mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, floa
     ProfScope prof(h, "gemm_bf16x", 2.0 * M * N * (double)Kp * nprod,
                    (beta == 0.f ? 4.0 : 8.0) * M * N + 2.0 * np * (double)(M + N) * Kp);
     switch (np) {
-        case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c);
-        case 2: return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c);
-        default: return launch_gemm_np<3>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c);
+        case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, 0);
+        case 2:
+            return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass);
+        default:
+            return launch_gemm_np<3>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass);
     }
 }
 

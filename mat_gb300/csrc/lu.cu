@@ -700,7 +700,7 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
         float* A22 = A + (r + w) + (size_t)(r + w) * lda;
         const int w1 = nb < nt ? nb : nt;  // the next panel's columns
         MG_TRY(bf16x_gemm_presplit(h, nterms, nt, w1, w, -1.0f, L21, splitB, 1.0f, A22, lda, gemm_err, 0,
-                                   (size_t)nt * kp, 0, false));  // the next panel: kept in L2
+                                   (size_t)nt * kp, 0, false, true));  // the next panel: kept in L2
         const bool ov = overlappable(k + 1);
         const void* Brest = (const char*)splitB + (size_t)w1 * kp * 2;
         if (nt > w1 && ov) {
@@ -714,14 +714,15 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
                 OnStream on(h, S2);
                 MG_TRY(bf16x_gemm_presplit(h, nterms, nt, nt - w1, w, -1.0f, L21, Brest, 1.0f,
                                            A22 + (size_t)w1 * lda, lda, gemm_err, 0, (size_t)nt * kp,
-                                           h->num_sms - 16));
+                                           h->num_sms - 16, true, true));
                 MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[1], S2));
             }
             far_pending = true;
         } else {
             if (nt > w1)
                 MG_TRY(bf16x_gemm_presplit(h, nterms, nt, nt - w1, w, -1.0f, L21, Brest, 1.0f,
-                                           A22 + (size_t)w1 * lda, lda, gemm_err, 0, (size_t)nt * kp));
+                                           A22 + (size_t)w1 * lda, lda, gemm_err, 0, (size_t)nt * kp, 0, true,
+                                           true));
             MG_TRY(panel(k + 1));
         }
         MG_TRY(after_panel(k + 1));
