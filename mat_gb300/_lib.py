@@ -67,6 +67,7 @@ SIGNATURES: dict[str, tuple] = {
     "mg_dgetrs": (i32, [vp, i32, i32, vp, i32, vp, vp, i32, vp, i32]),
     "mg_dgesv": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, pi32]),
     "mg_sgemm_bf16x": (i32, [vp, i32, i32, i32, i32, f32, vp, i32, vp, i32, f32, vp, i32]),
+    "mg_sgemm_bf16x_ex": (i32, [vp, i32, i32, i32, i32, i32, f32, vp, i32, vp, i32, f32, vp, i32]),
     "mg_bf16x_check_error": (i32, [vp, pi32]),
     "mg_dsgesv_ir": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, C.POINTER(IrOpts), C.POINTER(IrReport)]),
     "mg_gen_svd_matrix": (i32, [vp, i32, vp, i32, u64, i32, f64]),

@@ -117,15 +117,16 @@ class Handle:
                                      ld_of(B), beta, _ptr(C_), ld_of(C_)), "mg_sgemm")
         return C_
 
-    def sgemm_bf16x(self, A, B, C_=None, alpha=1.0, beta=0.0, nterms=3):
-        """fp32 C = alpha A B + beta C on the BF16 tensor cores with `nterms` split terms."""
+    def sgemm_bf16x(self, A, B, C_=None, alpha=1.0, beta=0.0, nterms=3, ordered=False):
+        """fp32 C = alpha A B + beta C on the BF16 tensor cores with `nterms` split
+        terms; ordered: lower-order products first (more accurate, slower)."""
         m, k = A.shape
         n = B.shape[1]
         if C_ is None:
             C_ = colmajor(m, n, dtype=torch.float32, device=A.device)
             beta = 0.0
-        self.check(self.lib.mg_sgemm_bf16x(self.h, nterms, m, n, k, alpha, _ptr(A), ld_of(A), _ptr(B), ld_of(B),
-                                           beta, _ptr(C_), ld_of(C_)), "mg_sgemm_bf16x")
+        self.check(self.lib.mg_sgemm_bf16x_ex(self.h, nterms, 1 if ordered else 0, m, n, k, alpha, _ptr(A), ld_of(A),
+                                              _ptr(B), ld_of(B), beta, _ptr(C_), ld_of(C_)), "mg_sgemm_bf16x_ex")
         flag = C.c_int(0)
         self.check(self.lib.mg_bf16x_check_error(self.h, C.byref(flag)), "mg_bf16x_check_error")
         if flag.value:

@@ -599,13 +599,20 @@ mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, floa
 
 extern "C" mg_status_t mg_sgemm_bf16x(mg_handle_t h, int nterms, int m, int n, int k, float alpha, const float* A,
                                       int lda, const float* B, int ldb, float beta, float* C, int ldc) {
+    return mg_sgemm_bf16x_ex(h, nterms, 0, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+extern "C" mg_status_t mg_sgemm_bf16x_ex(mg_handle_t h, int nterms, int flags, int m, int n, int k, float alpha,
+                                         const float* A, int lda, const float* B, int ldb, float beta, float* C,
+                                         int ldc) {
     if (!h) return MG_ERR_ARG;
+    if (flags & ~MG_BF16X_ORDERED) return mg::fail(h, MG_ERR_ARG, "mg_sgemm_bf16x_ex: unknown flags %d", flags);
     if (nterms < 1 || nterms > 3 || m < 0 || n < 0 || k < 0 || lda < (m > 1 ? m : 1) || ldb < (k > 1 ? k : 1) ||
         ldc < (m > 1 ? m : 1))
-        return mg::fail(h, MG_ERR_ARG, "mg_sgemm_bf16x: bad arguments");
+        return mg::fail(h, MG_ERR_ARG, "mg_sgemm_bf16x_ex: bad arguments");
     if (m == 0 || n == 0) return MG_OK;
     if (k == 0) {
-        return mg::fail(h, MG_ERR_ARG, "mg_sgemm_bf16x: k == 0 unsupported");
+        return mg::fail(h, MG_ERR_ARG, "mg_sgemm_bf16x_ex: k == 0 unsupported");
     }
     const size_t as = mg::bf16x_split_bytes(m, k, nterms), bs = mg::bf16x_split_bytes(n, k, nterms);
     MG_TRY(mg::ensure_ws(h, 1024 + as + bs));
@@ -617,7 +624,8 @@ extern "C" mg_status_t mg_sgemm_bf16x(mg_handle_t h, int nterms, int m, int n, i
     void* Bsp = ws + 1024 + as;
     MG_TRY(mg::bf16x_split<float>(h, true, A, lda, m, k, nterms, Asp));
     MG_TRY(mg::bf16x_split<float>(h, false, B, ldb, n, k, nterms, Bsp));
-    MG_TRY(mg::bf16x_gemm_presplit(h, nterms, m, n, k, alpha, Asp, Bsp, beta, C, ldc, err));
+    MG_TRY(mg::bf16x_gemm_presplit(h, nterms, m, n, k, alpha, Asp, Bsp, beta, C, ldc, err, 0, 0, 0, true,
+                                   (flags & MG_BF16X_ORDERED) != 0));
     return MG_OK;
 }
 

@@ -21,11 +21,11 @@ def make(m, n, seed, scale_exp=0):
     return u.float()
 
 
-def run(handle, a, b, nterms, c0=None, alpha=1.0, beta=0.0):
+def run(handle, a, b, nterms, c0=None, alpha=1.0, beta=0.0, ordered=False):
     A = a.cuda().t().contiguous().t()
     B = b.cuda().t().contiguous().t()
     Cd = None if c0 is None else c0.cuda().t().contiguous().t()
-    out = handle.sgemm_bf16x(A, B, Cd, alpha=alpha, beta=beta, nterms=nterms)
+    out = handle.sgemm_bf16x(A, B, Cd, alpha=alpha, beta=beta, nterms=nterms, ordered=ordered)
     torch.cuda.synchronize()
     return out.cpu().double()
 
@@ -33,12 +33,22 @@ def run(handle, a, b, nterms, c0=None, alpha=1.0, beta=0.0):
 @pytest.mark.parametrize("m,n,k", [(128, 256, 32), (1, 1, 1), (200, 300, 70), (129, 257, 33), (512, 768, 1024),
                                    (1000, 130, 96)])
 @pytest.mark.parametrize("nterms", [3, 2, 1])
-def test_split_gemm_accuracy(handle, m, n, k, nterms):
+@pytest.mark.parametrize("ordered", [False, True])
+def test_split_gemm_accuracy(handle, m, n, k, nterms, ordered):
     a, b = make(m, k, 1), make(k, n, 2)
     ref = a.double() @ b.double()
-    out = run(handle, a, b, nterms)
+    out = run(handle, a, b, nterms, ordered=ordered)
     err = (out - ref).norm() / ref.norm()
     assert err < TOL[nterms] * max(1.0, (k / 64) ** 0.5), float(err)
+
+
+def test_split_gemm_ordered_is_more_accurate(handle):
+    # the lower-order products accumulated before the leading one
+    a, b = make(512, 4096, 8, 8), make(4096, 384, 9, 8)
+    ref = a.double() @ b.double()
+    e1 = float((run(handle, a, b, 3) - ref).norm() / ref.norm())
+    e2 = float((run(handle, a, b, 3, ordered=True) - ref).norm() / ref.norm())
+    assert e2 < 0.6 * e1, (e2, e1)
 
 
 def test_split_gemm_wide_exponents(handle):
@@ -53,5 +63,6 @@ def test_split_gemm_subtracting_update(handle):
     # the LU trailing update form: C := C - A B
     a, b, c = make(300, 128, 5), make(128, 520, 6), make(300, 520, 7)
     ref = c.double() - a.double() @ b.double()
-    out = run(handle, a, b, 3, c0=c, alpha=-1.0, beta=1.0)
-    assert (out - ref).norm() / ref.norm() < 2e-6
+    for ordered in (False, True):
+        out = run(handle, a, b, 3, c0=c, alpha=-1.0, beta=1.0, ordered=ordered)
+        assert (out - ref).norm() / ref.norm() < 2e-6
