@@ -26,7 +26,7 @@ mg_status_t ensure_lookahead(mg_handle_t h) {
     MG_CHECK_CUDA(h, cudaDeviceGetStreamPriorityRange(&least, &greatest));
     MG_CHECK_CUDA(h, cudaStreamCreateWithPriority(&h->la_stream, cudaStreamNonBlocking, least));
     for (cudaEvent_t& e : h->la_ev) MG_CHECK_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    MG_CHECK_CUDA(h, cudaStreamCreateWithFlags(&h->pp_stream, cudaStreamNonBlocking));
+    MG_CHECK_CUDA(h, cudaStreamCreateWithPriority(&h->pp_stream, cudaStreamNonBlocking, greatest));
     for (cudaEvent_t& e : h->pp_ev) MG_CHECK_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return MG_OK;
 }

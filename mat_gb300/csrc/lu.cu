@@ -507,11 +507,28 @@ static mg_status_t launch_trsm_lunn(mg_handle_t h, int k, int n, const T* U, int
     return post_launch(h, "trsm_lunn_kernel");
 }
 
+// Runs the enclosed launches on another stream of the handle (the profiler
+// records on whatever h->stream is at the time).
+struct OnStream {
+    mg_handle_t h;
+    cudaStream_t saved;
+    OnStream(mg_handle_t h_, cudaStream_t s) : h(h_), saved(h_->stream) { h->stream = s; }
+    ~OnStream() { h->stream = saved; }
+};
+
 // In-place PLU given an exchange area `c` (no allocation); hstat receives the
 // error and info words (two host ints).  Returns MG_OK, MG_SINGULAR (info =
 // first zero-pivot column, 1-based) or an error.
+//
+// Blocked path with a look-ahead of one panel (lookahead != 0): after the
+// block-row solve of step k, the next panel's 60 columns are updated first
+// (near update) and panel k+1 starts right behind it, while the rest of
+// the trailing matrix (far update) runs on the handle's low-priority side
+// stream; step k+1's interchanges wait for it.  Every element of the
+// trailing matrix still receives one fused chain over the step's 60
+// columns in the same order, so the factors are those of the plain loop.
 static mg_status_t dgetrf_run(mg_handle_t h, int m, int n, double* A, int lda, int* pos, GetrfCtx<double>& c,
-                              int* hstat, int* info_out, int nopiv = 0) {
+                              int* hstat, int* info_out, int nopiv = 0, int lookahead = 0) {
     if (info_out) *info_out = 0;
     MG_CHECK_CUDA(h, cudaMemsetAsync(c.ws.bar, 0, 256, h->stream));  // barrier, error and info words
     iota_kernel<<<(m + 255) / 256, 256, 0, h->stream>>>(pos, m);
@@ -527,18 +544,53 @@ static mg_status_t dgetrf_run(mg_handle_t h, int m, int n, double* A, int lda, i
             MG_TRY(launch_trsm_llnu<double>(h, s, n - s, A, lda, A + (size_t)s * lda, lda));
         }
     } else {
+        if (lookahead) MG_TRY(ensure_lookahead(h));
+        const cudaStream_t S = h->stream;
+        bool far_pending = false;  // a far update was issued on the side stream (event la_ev[1])
         int r = 0;
+        bool have_panel = false;   // panel r already factored (by the look-ahead)
         for (; r + LU_BS <= s; r += LU_BS) {
-            MG_TRY(launch_panel<double>(h, c, A, lda, m, r, LU_BS, pos, nopiv));
+            if (!have_panel) MG_TRY(launch_panel<double>(h, c, A, lda, m, r, LU_BS, pos, nopiv));
+            have_panel = false;
+            if (far_pending) MG_CHECK_CUDA(h, cudaStreamWaitEvent(S, h->la_ev[1], 0));
+            far_pending = false;
             if (!nopiv) MG_TRY(launch_laswp<double>(h, A, lda, r, LU_BS, c.piv, r, r + LU_BS, n));
             if (r + LU_BS < s) {
                 const int nt = n - (r + LU_BS);
+                const int mt = m - (r + LU_BS);
                 double* A12 = A + r + (size_t)(r + LU_BS) * lda;
+                const double* L21 = A + (r + LU_BS) + (size_t)r * lda;
+                double* A22 = A + (r + LU_BS) + (size_t)(r + LU_BS) * lda;
                 MG_TRY(launch_trsm_llnu<double>(h, LU_BS, nt, A + r + (size_t)r * lda, lda, A12, lda));
-                MG_TRY(dgemm_launch(h, 0, 0, m - (r + LU_BS), nt, LU_BS, -1.0, A + (r + LU_BS) + (size_t)r * lda,
-                                    lda, A12, lda, 1.0, A + (r + LU_BS) + (size_t)(r + LU_BS) * lda, lda, 0));
+                const int r1 = r + LU_BS;  // the next panel's first column
+                const bool next_full = r1 + LU_BS <= s;
+                if (lookahead && next_full && nt > LU_BS) {
+                    MG_TRY(dgemm_launch(h, 0, 0, mt, LU_BS, LU_BS, -1.0, L21, lda, A12, lda, 1.0, A22, lda, 0));
+                    MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[0], S));
+                    // the next panel on the high-priority side stream: its grid
+                    // takes SMs ahead of the far update's tiles as they free up
+                    MG_CHECK_CUDA(h, cudaStreamWaitEvent(h->pp_stream, h->la_ev[0], 0));
+                    {
+                        OnStream on(h, h->pp_stream);
+                        MG_TRY(launch_panel<double>(h, c, A, lda, m, r1, LU_BS, pos, nopiv));
+                        MG_CHECK_CUDA(h, cudaEventRecord(h->pp_ev[0], h->pp_stream));
+                    }
+                    MG_CHECK_CUDA(h, cudaStreamWaitEvent(S, h->pp_ev[0], 0));
+                    have_panel = true;
+                    MG_CHECK_CUDA(h, cudaStreamWaitEvent(h->la_stream, h->la_ev[0], 0));
+                    {
+                        OnStream on(h, h->la_stream);
+                        MG_TRY(dgemm_launch(h, 0, 0, mt, nt - LU_BS, LU_BS, -1.0, L21, lda,
+                                            A12 + (size_t)LU_BS * lda, lda, 1.0, A22 + (size_t)LU_BS * lda, lda, 0));
+                        MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[1], h->la_stream));
+                    }
+                    far_pending = true;
+                } else {
+                    MG_TRY(dgemm_launch(h, 0, 0, mt, nt, LU_BS, -1.0, L21, lda, A12, lda, 1.0, A22, lda, 0));
+                }
             }
         }
+        if (far_pending) MG_CHECK_CUDA(h, cudaStreamWaitEvent(S, h->la_ev[1], 0));
         if (r < s) {
             const int rem = s - r;
             MG_TRY(launch_panel<double>(h, c, A, lda, m, r, rem, pos, nopiv));
@@ -563,7 +615,7 @@ mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* po
     MG_TRY(ensure_ws(h, getrf_ws_bytes<double>(h->num_sms)));
     MG_TRY(ensure_hws(h, 64));
     GetrfCtx<double> c = carve<double>(h->ws, h->num_sms);
-    return dgetrf_run(h, m, n, A, lda, pos, c, (int*)h->hws, info_out);
+    return dgetrf_run(h, m, n, A, lda, pos, c, (int*)h->hws, info_out, 0, 1);
 }
 
 // In-place LU without pivoting (Mat's LU, LU/__LU.h:71-108) of a square
@@ -595,14 +647,6 @@ static mg_status_t launch_panel_f32(mg_handle_t h, GetrfCtx<float>& c, float* A,
     return launch_panel<float>(h, c, A, lda, m, r0, w, pos);
 }
 
-// Runs the enclosed launches on another stream of the handle (the profiler
-// records on whatever h->stream is at the time).
-struct OnStream {
-    mg_handle_t h;
-    cudaStream_t saved;
-    OnStream(mg_handle_t h_, cudaStream_t s) : h(h_), saved(h_->stream) { h->stream = s; }
-    ~OnStream() { h->stream = saved; }
-};
 
 // FP32 blocked right-looking LU with partial pivoting for the mixed solve,
 // with a look-ahead of one panel.  Step k on the handle's stream S:

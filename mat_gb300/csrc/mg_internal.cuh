@@ -32,8 +32,9 @@ struct mg_handle_s {
     // ordering events.
     cudaStream_t la_stream = nullptr;
     cudaEvent_t la_ev[2] = {nullptr, nullptr};
-    // Side stream (normal priority) for the work that follows a panel
-    // off the critical path, and its two ordering events.
+    // Side stream (highest priority) for panels and the work that follows a
+    // panel, running beside a far trailing update, and its two ordering
+    // events.
     cudaStream_t pp_stream = nullptr;
     cudaEvent_t pp_ev[2] = {nullptr, nullptr};
     char last_error[512] = {0};
