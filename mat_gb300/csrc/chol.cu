@@ -244,21 +244,62 @@ mg_status_t potrf_impl(mg_handle_t h, int n, T* L, int ldl, int* info_out) {
         llt2_kernel<T><<<1, 128, s2, st>>>(L, ldl, n, 0, dinfo);
         MG_TRY(post_launch(h, "llt2_kernel"));
     } else {
-        for (int j = 0; j < n; j += LLT_BS) {
+        // Look-ahead of one block column: after step j's panel solve, the next
+        // block column is updated first (near update), its diagonal block and
+        // panel solve run on the high-priority side stream, and the rest of
+        // the trailing matrix (far update) on the low-priority one; step
+        // j+48's near update waits for the far update.  Every lower element
+        // still receives step j's fused chain over 48 columns in order.
+        MG_TRY(ensure_lookahead(h));
+        auto diag_and_panel = [&](int j) -> mg_status_t {
             const int nb = n - j < LLT_BS ? n - j : LLT_BS;
             T* D = L + j + (size_t)j * ldl;
-            llt2_kernel<T><<<1, 128, s2, st>>>(D, ldl, nb, j, dinfo);
+            llt2_kernel<T><<<1, 128, s2, h->stream>>>(D, ldl, nb, j, dinfo);
             MG_TRY(post_launch(h, "llt2_kernel"));
             if (j + LLT_BS < n) {
                 const int rows = n - (j + LLT_BS);
-                T* P = L + (j + LLT_BS) + (size_t)j * ldl;
-                xlt_kernel<T><<<(rows + 127) / 128, 128, 0, st>>>(D, ldl, P, ldl, rows, LLT_BS);
+                xlt_kernel<T><<<(rows + 127) / 128, 128, 0, h->stream>>>(D, ldl, L + (j + LLT_BS) + (size_t)j * ldl,
+                                                                          ldl, rows, LLT_BS);
                 MG_TRY(post_launch(h, "xlt_kernel"));
+            }
+            return MG_OK;
+        };
+        bool far_pending = false, have = false;
+        for (int j = 0; j < n; j += LLT_BS) {
+            if (!have) MG_TRY(diag_and_panel(j));
+            have = false;
+            if (j + LLT_BS >= n) break;
+            const int rows = n - (j + LLT_BS);
+            T* P = L + (j + LLT_BS) + (size_t)j * ldl;
+            T* C = L + (j + LLT_BS) + (size_t)(j + LLT_BS) * ldl;
+            if (far_pending) MG_CHECK_CUDA(h, cudaStreamWaitEvent(st, h->la_ev[1], 0));
+            far_pending = false;
+            const int nb1 = rows < LLT_BS ? rows : LLT_BS;  // the next block column
+            if (rows > nb1) {
+                MG_TRY(gemm_of(h, 0, 1, rows, nb1, LLT_BS, T(-1), P, ldl, P, ldl, T(1), C, ldl, 1));
+                MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[0], st));
+                MG_CHECK_CUDA(h, cudaStreamWaitEvent(h->pp_stream, h->la_ev[0], 0));
+                {
+                    OnStream on(h, h->pp_stream);
+                    MG_TRY(diag_and_panel(j + LLT_BS));
+                    MG_CHECK_CUDA(h, cudaEventRecord(h->pp_ev[0], h->pp_stream));
+                }
+                MG_CHECK_CUDA(h, cudaStreamWaitEvent(st, h->pp_ev[0], 0));
+                have = true;
+                MG_CHECK_CUDA(h, cudaStreamWaitEvent(h->la_stream, h->la_ev[0], 0));
+                {
+                    OnStream on(h, h->la_stream);
+                    MG_TRY(gemm_of(h, 0, 1, rows - nb1, rows - nb1, LLT_BS, T(-1), P + nb1, ldl, P + nb1, ldl, T(1),
+                                   C + nb1 + (size_t)nb1 * ldl, ldl, 1));
+                    MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[1], h->la_stream));
+                }
+                far_pending = true;
+            } else {
                 // C(i.., i..) -= P P^T on the trailing matrix, lower tiles only
-                MG_TRY(gemm_of(h, 0, 1, rows, rows, LLT_BS, T(-1), P, ldl, P, ldl, T(1),
-                               L + (j + LLT_BS) + (size_t)(j + LLT_BS) * ldl, ldl, 1));
+                MG_TRY(gemm_of(h, 0, 1, rows, rows, LLT_BS, T(-1), P, ldl, P, ldl, T(1), C, ldl, 1));
             }
         }
+        if (far_pending) MG_CHECK_CUDA(h, cudaStreamWaitEvent(st, h->la_ev[1], 0));
     }
     zero_upper_kernel<T><<<h->num_sms * 8, 256, 0, st>>>(L, ldl, n);
     MG_TRY(post_launch(h, "zero_upper_kernel"));

@@ -507,14 +507,6 @@ static mg_status_t launch_trsm_lunn(mg_handle_t h, int k, int n, const T* U, int
     return post_launch(h, "trsm_lunn_kernel");
 }
 
-// Runs the enclosed launches on another stream of the handle (the profiler
-// records on whatever h->stream is at the time).
-struct OnStream {
-    mg_handle_t h;
-    cudaStream_t saved;
-    OnStream(mg_handle_t h_, cudaStream_t s) : h(h_), saved(h_->stream) { h->stream = s; }
-    ~OnStream() { h->stream = saved; }
-};
 
 // In-place PLU given an exchange area `c` (no allocation); hstat receives the
 // error and info words (two host ints).  Returns MG_OK, MG_SINGULAR (info =

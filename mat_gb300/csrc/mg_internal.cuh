@@ -164,6 +164,16 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
 // Side stream and events of the look-ahead LU (created once per handle).
 mg_status_t ensure_lookahead(mg_handle_t h);
 
+// Runs the enclosed launches on another stream of the handle (the profiler
+// records on whatever h->stream is at the time).
+struct OnStream {
+    mg_handle_t h;
+    cudaStream_t saved;
+    OnStream(mg_handle_t h_, cudaStream_t s) : h(h_), saved(h_->stream) { h->stream = s; }
+    ~OnStream() { h->stream = saved; }
+};
+
+
 }  // namespace mg
 
 #define MG_CHECK_CUDA(h, call)                                   \
