@@ -47,6 +47,11 @@ struct TileCfg {
 using Big = TileCfg<2, 4, 4, 4>;    // 128 x 128, 8 warps
 using Small = TileCfg<1, 1, 2, 4>;  // 32 x 32, 1 warp
 using Thin = TileCfg<1, 1, 3, 2>;   // 48 x 16, 1 warp: M = 48 block-reflector products (QR, adjoint)
+// 16 x 16, 1 warp: products with few outputs and a long K (the QR's V^T R2
+// late in the factorization); one SM's FP64 pipe takes a DMMA only every
+// ~290 cycles, so two accumulator chains keep it busy and the small tile
+// spreads the outputs over more SMs.
+using Tiny = TileCfg<1, 1, 1, 2>;
 
 __device__ __forceinline__ void cp_async8(double* smem, const double* gmem, bool pred) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -304,7 +309,13 @@ mg_status_t dgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, in
         const double ab = busiest_sm_area(tb, h->num_sms, Big::BM, Big::BN);
         const double as = busiest_sm_area(ts, h->num_sms, Small::BM, Small::BN);
         const double at = busiest_sm_area(tt, h->num_sms, Thin::BM, Thin::BN);
-        if (at < ab && at < as)
+        const long long tn = (long long)((m + Tiny::BM - 1) / Tiny::BM) * ((n + Tiny::BN - 1) / Tiny::BN);
+        const double an = busiest_sm_area(tn, h->num_sms, Tiny::BM, Tiny::BN);
+        // the 16 x 16 tile reloads more operand bytes per flop: only when it
+        // shortens the busiest SM's work clearly
+        if (an < 0.75 * std::min(at, std::min(ab, as)))
+            e = dispatch<Tiny>(st, transA, transB, mode, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+        else if (at < ab && at < as)
             e = dispatch<Thin>(st, transA, transB, mode, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
         else if (ab <= as)
             e = dispatch<Big>(st, transA, transB, mode, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
