@@ -36,7 +36,7 @@
 namespace {
 
 constexpr int QR_BS = 48;  // Mat-8.3.1/Mat.h:77-79 (AVX-512)
-constexpr int QR_THREADS = 128;
+constexpr int QR_THREADS = 512;  // one CTA per panel column: its loops over the column keep many loads in flight
 
 // Mat's AVX-512 __dot(a, b, len), computed by one full warp; every lane returns
 // the result.  Loads bypass L1 (the operands may have been written by other
@@ -76,6 +76,79 @@ __device__ double warp_dot_mat(const double* __restrict__ a, const double* __res
     return __shfl_sync(0xffffffffu, r, 0);
 }
 
+// The same __dot(a, b, len) computed by a whole CTA of QR_THREADS threads:
+// all threads stage the operands through shared memory in chunks of
+// QR_DOT_CH elements (each thread keeps its chunk loads in flight together),
+// and warp 0 runs the 32 ordered fused chains of warp_dot_mat on them (lane
+// p <- elements 32t + p), then the identical tail and reduction.  One warp
+// streaming both operands from L2 alone kept too few loads in flight (about
+// 64 us for a 16384-element dot).  Call from every thread of the CTA; every
+// thread returns the result.  sbuf holds 2 * QR_DOT_CH doubles.
+constexpr int QR_DOT_CH = 2048;
+
+__device__ double block_dot_mat(const double* __restrict__ a, const double* __restrict__ b, int len,
+                                double* sbuf, double* s_out) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nb = len / 8;
+    const int nmain = 32 * (nb / 4);  // elements of the 32-strided fused chains
+    double acc = 0.0;
+    for (int c0 = 0; c0 < nmain; c0 += QR_DOT_CH) {
+        const int cn = min(QR_DOT_CH, nmain - c0);
+        __syncthreads();  // the previous chunk is consumed
+        {
+            constexpr int PER = QR_DOT_CH / QR_THREADS;
+            double ta[PER], tb[PER];
+#pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                const int e = tid + u * QR_THREADS;
+                ta[u] = e < cn ? __ldcg(a + c0 + e) : 0.0;
+                tb[u] = e < cn ? __ldcg(b + c0 + e) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                const int e = tid + u * QR_THREADS;
+                sbuf[e] = ta[u];
+                sbuf[QR_DOT_CH + e] = tb[u];
+            }
+        }
+        __syncthreads();
+        if (warp == 0) {
+            // eight shared loads ahead of the ordered chain (cn is a multiple of 32)
+            int t = lane;
+            for (; t + 7 * 32 < cn; t += 8 * 32) {
+                double xa[8], xb[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    xa[u] = sbuf[t + 32 * u];
+                    xb[u] = sbuf[QR_DOT_CH + t + 32 * u];
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) acc = fma(xa[u], xb[u], acc);
+            }
+            for (; t < cn; t += 32) acc = fma(sbuf[t], sbuf[QR_DOT_CH + t], acc);
+        }
+    }
+    if (warp == 0) {
+        int i = nb / 4 * 4;
+        // remaining full 8-blocks into the first accumulator (lanes 0..7)
+        for (; i < nb; ++i)
+            if (lane < 8) acc = fma(__ldcg(a + i * 8 + lane), __ldcg(b + i * 8 + lane), acc);
+        const double x1 = __shfl_down_sync(0xffffffffu, acc, 8);
+        const double x2 = __shfl_down_sync(0xffffffffu, acc, 16);
+        const double x3 = __shfl_down_sync(0xffffffffu, acc, 24);
+        double sx = (acc + x1) + (x2 + x3);
+        const int rem = len - nb * 8;
+        if (lane < rem) sx = fma(__ldcg(a + nb * 8 + lane), __ldcg(b + nb * 8 + lane), sx);
+        const double s4 = __shfl_down_sync(0xffffffffu, sx, 4);
+        const double h4 = sx + s4;
+        const double h2 = h4 + __shfl_down_sync(0xffffffffu, h4, 2);
+        const double r = h2 + __shfl_down_sync(0xffffffffu, h2, 1);
+        if (lane == 0) *s_out = r;
+    }
+    __syncthreads();
+    return *s_out;
+}
+
 struct QrPanelWs {
     unsigned* bar;
     int* err;
@@ -84,17 +157,17 @@ struct QrPanelWs {
 // Panel of b columns at P (h rows, ld ldr).  CTA c owns column c.
 __global__ void __launch_bounds__(QR_THREADS) qr_panel_kernel(double* __restrict__ P, int ldr, int h, int b,
                                                                double* __restrict__ tau, QrPanelWs ws) {
-    __shared__ double s_q, s_hr;
+    __shared__ double s_q, s_hr, s_dot;
     __shared__ int s_skip;
+    __shared__ double sbuf[2 * QR_DOT_CH];
     const int c = blockIdx.x;
-    const int warp = threadIdx.x >> 5;
     unsigned phase = 0;
     for (int r = 0; r < b; ++r) {
         const int len = h - r;
         double* w = P + r + (size_t)r * ldr;
         if (c == r) {
-            if (warp == 0) {
-                const double ss = warp_dot_mat(w, w, len);
+            const double ss = block_dot_mat(w, w, len, sbuf, &s_dot);
+            {
                 if (threadIdx.x == 0) {
                     double cr = sqrt(ss);
                     if (cr == 0.0) {
@@ -133,8 +206,8 @@ __global__ void __launch_bounds__(QR_THREADS) qr_panel_kernel(double* __restrict
         // apply H_r to the columns right of it (Mat skips them when the column was zero)
         if (c > r && __ldcg(tau + r) != 0.0) {
             double* col = P + r + (size_t)c * ldr;
-            if (warp == 0) {
-                const double d = __ldcg(col) + warp_dot_mat(w + 1, col + 1, len - 1);
+            {
+                const double d = __ldcg(col) + block_dot_mat(w + 1, col + 1, len - 1, sbuf, &s_dot);
                 if (threadIdx.x == 0) s_q = -d * __ldcg(tau + r);
             }
             __syncthreads();
