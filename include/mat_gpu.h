@@ -39,7 +39,8 @@ typedef enum mg_status {
     MG_IR_STALLED = 6,       /* refinement did not reach the requested tolerance   */
     MG_FALLBACK_USED = 7,    /* mixed solve fell back to GMRES-IR or the FP64 path */
     MG_TIMEOUT = 8,          /* a bounded device-side wait gave up                 */
-    MG_ERR_UNSUPPORTED = 9   /* option not supported on this device                */
+    MG_ERR_UNSUPPORTED = 9,  /* option not supported on this device                */
+    MG_NOT_CONVERGED = 10    /* an iteration did not converge within its budget    */
 } mg_status_t;
 
 typedef struct mg_handle_s* mg_handle_t;
@@ -181,6 +182,27 @@ mg_status_t mg_dlu(mg_handle_t h, int n, double* A, int lda, int* info);
  * No pivoting: an exactly zero d_j gives info = j + 1 and MG_SINGULAR (Mat
  * does not check; the factorization runs to the end).  Synchronises. */
 mg_status_t mg_dldlt(mg_handle_t h, int n, double* A, int lda, double* d, int* info);
+
+/* ------------------------------------------- symmetric eigendecomposition
+ * Mat-8.1 snapshot's EVD_Q(A, E, Q, eps, EVD_QR) (Mat-8.1/EVD/EVD_Q.h:7-35,
+ * EVD/__QR.h:145-169); results bit for bit those of its AVX-512 build.
+ *
+ * mg_dtridiag81: __EVD_Q_Householder (EVD/__QR.h:2-47) and __Householder_Q2
+ * (QR/__Householder.h:124-152).  Reads the lower triangle of the symmetric A
+ * (n x n), leaves the Householder reflectors below its diagonal, and writes
+ * d (device, n) = the diagonal and e (device, n - 1) = the off-diagonal of
+ * T = Q^T A Q, and Q (n x n).  Synchronises. */
+mg_status_t mg_dtridiag81(mg_handle_t h, int n, double* A, int lda, double* Q, int ldq, double* d, double* e);
+
+/* mg_devd_q: the whole EVD_Q with EVD_QR: A's lower triangle is read (A is
+ * not modified unless A == E); E (n x n) receives diag(eigenvalues) and Q the
+ * eigenvectors (A Q = Q E); w (device, n, may be NULL) the eigenvalues.  eps
+ * is Mat's absolute deflation threshold on the off-diagonal.  The QR sweeps'
+ * scalar recurrence runs on the host and the rotations are applied on the
+ * GPU.  Mat iterates without limit; here after 64 n sweeps the call returns
+ * MG_NOT_CONVERGED.  Synchronises. */
+mg_status_t mg_devd_q(mg_handle_t h, int n, const double* A, int lda, double eps, double* E, int lde, double* Q,
+                      int ldq, double* w);
 
 /* ------------------------------------------------- split-precision GEMM
  * C = alpha * A * B + beta * C for fp32 column-major operands on the

@@ -63,6 +63,8 @@ SIGNATURES: dict[str, tuple] = {
     "mg_dinv": (i32, [vp, i32, vp, i32, vp, i32, pi32]),
     "mg_dldlt": (i32, [vp, i32, vp, i32, vp, pi32]),
     "mg_dlu": (i32, [vp, i32, vp, i32, pi32]),
+    "mg_dtridiag81": (i32, [vp, i32, vp, i32, vp, i32, vp, vp]),
+    "mg_devd_q": (i32, [vp, i32, vp, i32, f64, vp, i32, vp, i32, vp]),
     "mg_sgetrf": (i32, [vp, i32, vp, i32, vp, pi32]),
     "mg_dgetrs": (i32, [vp, i32, i32, vp, i32, vp, vp, i32, vp, i32]),
     "mg_dgesv": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, pi32]),

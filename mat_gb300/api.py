@@ -267,6 +267,28 @@ class Handle:
             self.check(st, "mg_dldlt")
         return d, info.value
 
+    def dtridiag81(self, A: torch.Tensor):
+        """Mat-8.1 EVD_Q tridiagonalisation of the symmetric A (lower triangle
+        read; reflectors left below its diagonal): returns (Q, d, e) with
+        Q^T A Q = tridiag(e, d, e)."""
+        n = A.shape[0]
+        Q = colmajor(n, n, device=A.device)
+        d = torch.empty(n, dtype=torch.float64, device=A.device)
+        e = torch.empty(max(n - 1, 1), dtype=torch.float64, device=A.device)
+        self.check(self.lib.mg_dtridiag81(self.h, n, _ptr(A), ld_of(A), _ptr(Q), ld_of(Q), _ptr(d), _ptr(e)),
+                   "mg_dtridiag81")
+        return Q, d, e[: n - 1]
+
+    def devd_q(self, A: torch.Tensor, eps: float, E: torch.Tensor | None = None, Q: torch.Tensor | None = None):
+        """Mat-8.1 EVD_Q(A, E, Q, eps, EVD_QR): returns (w, E, Q), A Q = Q E, E = diag(w)."""
+        n = A.shape[0]
+        E = colmajor(n, n, device=A.device) if E is None else E
+        Q = colmajor(n, n, device=A.device) if Q is None else Q
+        w = torch.empty(n, dtype=torch.float64, device=A.device)
+        self.check(self.lib.mg_devd_q(self.h, n, _ptr(A), ld_of(A), float(eps), _ptr(E), ld_of(E), _ptr(Q),
+                                      ld_of(Q), _ptr(w)), "mg_devd_q")
+        return w, E, Q
+
     def spotrf(self, A: torch.Tensor, check=True):
         """In-place fp32 LLT: lower triangle of A -> L, upper zeroed. Returns info."""
         n = A.shape[0]

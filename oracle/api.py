@@ -28,12 +28,13 @@ class Oracle:
     def __init__(self, path, prefix):
         self.lib = C.CDLL(str(path))
         self.prefix = prefix
-        self.is_ref = prefix == "ref_"
+        self.is_ref = prefix.startswith("ref")
         if not self.is_ref:
             self.lib.orc_det.restype = C.c_double
-            for n in ("orc_dgetrf", "orc_plu", "orc_solve", "orc_llt", "orc_inv", "orc_ldlt", "orc_lu"):
+            for n in ("orc_dgetrf", "orc_plu", "orc_solve", "orc_llt", "orc_inv", "orc_ldlt", "orc_lu",
+                      "orc_evd_q81"):
                 getattr(self.lib, n).restype = C.c_int
-        else:
+        elif prefix == "ref_":
             self.lib.ref_det.restype = C.c_double
 
     def _fn(self, name):
@@ -112,6 +113,33 @@ class Oracle:
         self._fn("qr")(m, n, _p(A), _p(Q), _p(R))
         return Q, R
 
+    def tridiag81(self, A):
+        """Mat-8.1 EVD_Q tridiagonalisation: returns (Q, d, e), Q^T A Q = tridiag(e, d, e)."""
+        A = _f(A)
+        n = A.shape[0]
+        Q = np.zeros((n, n), order="F")
+        d = np.zeros(n)
+        e = np.zeros(max(n - 1, 1))
+        if self.is_ref:
+            self._fn("tridiag")(n, _p(A), _p(Q), _p(d), _p(e))
+        else:
+            self.lib.orc_tridiag81(n, _p(A), n, _p(Q), n, _p(d), _p(e))
+        return Q, d, e[: n - 1]
+
+    def evd_q81(self, A, eps):
+        """Mat-8.1 EVD_Q(A, E, Q, eps, EVD_QR): returns (w, Q), A Q = Q diag(w)."""
+        A = _f(A)
+        n = A.shape[0]
+        Q = np.zeros((n, n), order="F")
+        if self.is_ref:
+            E = np.zeros((n, n), order="F")
+            self._fn("evd_q")(n, _p(A), C.c_double(eps), _p(E), _p(Q))
+            return np.diag(E).copy(), Q
+        w = np.zeros(n)
+        if self.lib.orc_evd_q81(n, _p(A), C.c_double(eps), _p(w), _p(Q)) != 0:
+            raise RuntimeError("EVD_Q: QR sweeps did not converge")
+        return w, Q
+
     def det(self, A):
         A = _f(A)
         return float(self._fn("det")(A.shape[0], _p(A)))
@@ -126,6 +154,13 @@ def restatement() -> Oracle:
 def reference() -> Oracle | None:
     lib = _build.build_ref()
     return Oracle(lib, "ref_") if lib else None
+
+
+@lru_cache(maxsize=None)
+def reference81() -> Oracle | None:
+    """The Mat-8.1 snapshot's EVD_Q path (entry points prefixed ref81_)."""
+    lib = _build.build_ref81()
+    return Oracle(lib, "ref81_") if lib else None
 
 
 def dgemm(A, B):

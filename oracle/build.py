@@ -6,6 +6,8 @@
 - _ref/libmatref.so: the reference Mat-8.3.1 compiled from its own headers
   with ref_shim/ (only where the reference tree exists; x86-64 AVX-512 build,
   Mat's configuration for its published numbers).
+- _ref/libmat81ref.so: the Mat-8.1 snapshot's EVD_Q tridiagonalisation and QR
+  iteration compiled from its own headers with ref81_shim/ (same conditions).
 """
 from __future__ import annotations
 
@@ -20,6 +22,8 @@ ORACLE_LIB = HERE / "liboracle.so"
 REF_DIR = HERE / "_ref"
 REF_LIB = REF_DIR / "libmatref.so"
 REFERENCE_ROOT = Path("/root/reference/Mat-8.3.1")
+REF81_LIB = REF_DIR / "libmat81ref.so"
+REFERENCE81_ROOT = Path("/root/reference/Mat-8.1")
 
 
 def _cxx() -> str:
@@ -59,9 +63,25 @@ def build_ref(force: bool = False) -> Path | None:
     return REF_LIB
 
 
+def build_ref81(force: bool = False) -> Path | None:
+    """Compiles the Mat-8.1 snapshot's EVD_Q tridiagonalisation and QR iteration (ref81_wrap.cpp)."""
+    if not REFERENCE81_ROOT.exists() or platform.machine() not in ("x86_64", "AMD64"):
+        return None
+    src = HERE / "ref81_wrap.cpp"
+    deps = [src, *sorted((HERE / "ref81_shim").rglob("*.h")), Path(__file__)]
+    if force or _stale(REF81_LIB, deps):
+        REF_DIR.mkdir(exist_ok=True)
+        cmd = [_cxx(), "-O3", "-std=c++17", "-fPIC", "-shared", "-D__AVX512__", "-mavx512f", "-mavx512dq",
+               "-mavx512vl", "-mfma", "-I", str(HERE / "ref81_shim"), "-I", str(REFERENCE81_ROOT), str(src),
+               "-o", str(REF81_LIB)]
+        subprocess.run(cmd, check=True)
+    return REF81_LIB
+
+
 def build(force: bool = False, verbose: bool = False) -> None:
     o = build_oracle(force)
     r = build_ref(force)
+    build_ref81(force)
     if verbose:
         print(f"built {o}" + (f" and {r}" if r else " (reference tree absent: no _ref build)"), file=sys.stderr)
 

@@ -882,3 +882,222 @@ double orc_det(int n, const double* A) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Mat-8.1 snapshot: EVD_Q's Householder tridiagonalisation and the Q it forms
+// (EVD/__QR.h:2-47, QR/__Householder.h:124-152).  These use the snapshot's
+// own AVX-512 helpers (SIMD/__AVX512_double.h), whose dot product differs
+// from Mat-8.3.1's.
+
+// Mat-8.1's __dot (SIMD/__AVX512_double.h:111-124): one 8-lane fused
+// accumulator over the full 8-blocks, the masked fused tail into lanes
+// 0..rem-1 of the same accumulator, then the 8 -> 4 -> 2 -> 1 horizontal sum
+// of _mm512_reduce_add_pd.
+static double dot81(const double* a, const double* b, int len) {
+    double acc[8] = {0};
+    const int nb = len / 8;
+    for (int i = 0; i < nb; ++i)
+        for (int l = 0; l < 8; ++l) acc[l] = std::fma(a[i * 8 + l], b[i * 8 + l], acc[l]);
+    const int rem = len - nb * 8;
+    for (int l = 0; l < rem; ++l) acc[l] = std::fma(a[nb * 8 + l], b[nb * 8 + l], acc[l]);
+    double h4[4], h2[2];
+    for (int l = 0; l < 4; ++l) h4[l] = acc[l] + acc[l + 4];
+    for (int l = 0; l < 2; ++l) h2[l] = h4[l] + h4[l + 2];
+    return h2[0] + h2[1];
+}
+
+// __EVD_Q_Householder (EVD/__QR.h:2-47) on column-major storage: step m
+// reduces the trailing N' = n - m matrix W (only its lower triangle is read)
+// with the reflector w of its first column, w = (x + sign(x0)||x|| e0) /
+// sqrt(cr (x0 + cr)), through v = W22 w (the column-wise fused chains of
+// __mixed, then the dot of the rest of each column), h = v.w and the rank-2
+// update W' = W22 - w v^T - v w^T + h w w^T, evaluated per column i as
+// fma(w_k, fma(w_i, h, -v_i), fma(v_k, -w_i, W22_ki)) (g++ contracts
+// -v[i] + w[i]*hr).  d = diagonal, e = off-diagonal (e_m = -cr), U = the
+// reflectors (column m holds w_m in rows m+1..n-1).
+static void tridiag81(int n, const double* A, int lda, double* d, double* e, std::vector<double>& U) {
+    std::vector<double> W((size_t)n * n), Wn((size_t)n * n), v(n), w(n);
+    for (int j = 0; j < n; ++j)
+        for (int i = j; i < n; ++i) W[(size_t)j * n + i] = A[(size_t)j * lda + i];
+    U.assign((size_t)n * n, 0.0);
+    int N = n;  // leading dimension (= order) of the current trailing matrix
+    for (int m = 0; m + 2 < n; ++m, --N) {
+        const int nn = N - 1;
+        const double temp = W[0];
+        for (int k = 0; k < nn; ++k) w[k] = W[1 + k];
+        double cr = std::sqrt(dot81(w.data(), w.data(), nn));
+        if (w[0] < 0.0) cr = -cr;
+        w[0] = w[0] + cr;
+        const double hr = 1.0 / std::sqrt(cr * w[0]);
+        for (int k = 0; k < nn; ++k) w[k] = w[k] * hr;
+        auto Wc = [&](int r, int c) { return W[(size_t)c * N + r]; };
+        for (int k = 0; k < nn; ++k) v[k] = 0.0;
+        for (int i = 0; i < nn; ++i)
+            for (int k = i; k < nn; ++k) v[k] = std::fma(Wc(1 + k, 1 + i), w[i], v[k]);
+        for (int i = 0; i < nn; ++i)
+            v[i] = v[i] + dot81(&W[(size_t)(i + 1) * N + i + 2], &w[i + 1], nn - i - 1);
+        const double h = dot81(v.data(), w.data(), nn);
+        for (int i = 0; i < nn; ++i) {
+            const double q = std::fma(w[i], h, -v[i]);
+            for (int k = i; k < nn; ++k)
+                Wn[(size_t)i * nn + k] = std::fma(w[k], q, std::fma(v[k], -w[i], Wc(1 + k, 1 + i)));
+        }
+        std::swap(W, Wn);
+        d[m] = temp;
+        e[m] = -cr;
+        for (int k = 0; k < nn; ++k) U[(size_t)m * n + m + 1 + k] = w[k];
+    }
+    if (n >= 2) {
+        d[n - 2] = W[0];
+        d[n - 1] = W[3];
+        e[n - 2] = W[1];
+    } else if (n == 1) {
+        d[0] = W[0];
+    }
+}
+
+// __Householder_Q2 (QR/__Householder.h:124-152): Q accumulated backwards from
+// the trailing 2 x 2 identity; at level r (order t = n - r) column 0 is e0
+// and column i >= 1 is (0, M_{:,i-1} + w_r (-dot(w_r, M_{:,i-1}))), M the
+// previous level's (t - 1) x (t - 1) matrix.
+static void form_q81(int n, const std::vector<double>& U, double* Q, int ldq) {
+    if (n == 1) {
+        Q[0] = 1.0;
+        return;
+    }
+    std::vector<double> M(4, 0.0), Mn;
+    M[0] = M[3] = 1.0;
+    for (int r = n - 3; r >= 0; --r) {
+        const int t = n - r, t2 = t - 1;
+        const double* u = &U[(size_t)r * n + r + 1];
+        Mn.assign((size_t)t * t, 0.0);
+        Mn[0] = 1.0;
+        for (int i = 1; i < t; ++i) {
+            const double* mc = &M[(size_t)(i - 1) * t2];
+            const double s = -dot81(u, mc, t2);
+            for (int k = 0; k < t2; ++k) Mn[(size_t)i * t + 1 + k] = std::fma(u[k], s, mc[k]);
+        }
+        std::swap(M, Mn);
+    }
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) Q[(size_t)j * ldq + i] = M[(size_t)j * n + i];
+}
+
+// One plane rotation of __EVD_Q_Givens (EVD/__QR.h:78-96 and 109-136) on the
+// pair (a_i, a_i1, b_i) from the ratio t: it returns (c, s) of the rotation
+// applied to Q's columns i, i+1.  `small` selects the branch whose t is
+// numerator / denominator with the smaller magnitude on top of b (first
+// branch: s^2 = 1/(t^2 + 1); second: c^2 = 1/(t^2 + 1)).  The reference build
+// contracts t*t + 1, c2*temp + s2*temp_2 (first product), the added or
+// subtracted 2*cs*b_i, and -cs*temp + cs*temp_2 + (c2 - s2)*b_i (first and
+// last products).
+static void rot81(double* a, double* b, int i, double t, bool first, double& c, double& s) {
+    double c2, s2, cs;
+    if (first) {
+        s2 = 1.0 / std::fma(t, t, 1.0);
+        c2 = 1.0 - s2;
+        cs = t * s2;
+    } else {
+        c2 = 1.0 / std::fma(t, t, 1.0);
+        s2 = 1.0 - c2;
+        cs = t * c2;
+    }
+    const double temp = a[i], temp_2 = a[i + 1];
+    const double cs2 = 2.0 * cs;
+    a[i] = std::fma(cs2, b[i], std::fma(c2, temp, s2 * temp_2));
+    a[i + 1] = std::fma(-cs2, b[i], std::fma(s2, temp, c2 * temp_2));
+    b[i] = std::fma(c2 - s2, b[i], std::fma(-cs, temp, cs * temp_2));
+    if (first) {
+        s = std::sqrt(s2);
+        c = t * s;
+    } else {
+        c = std::sqrt(c2);
+        s = t * c;
+    }
+}
+
+// __ApplyGivensOnTheRight(Q[i], Q[i+1], c, s, rows) (SIMD/__AVX512_double.h:1-20).
+static void apply_rot81(double* Q, int n, int i, double c, double s) {
+    double* x = Q + (size_t)i * n;
+    double* y = Q + (size_t)(i + 1) * n;
+    for (int r = 0; r < n; ++r) {
+        const double xi = x[r], yi = y[r];
+        x[r] = std::fma(xi, c, yi * s);
+        y[r] = std::fma(-xi, s, yi * c);
+    }
+}
+
+// __EVD_Q_Givens (EVD/__QR.h:50-142): implicit single-shift QR sweeps on the
+// tridiagonal (a = diagonal, b = off-diagonal, indices m..n inclusive) with
+// absolute deflation threshold eps, splitting at interior negligible b_i by
+// recursion; every rotation is applied to Q's columns.  The shift is the
+// eigenvalue of the trailing 2 x 2 block nearer a_n (the reference build
+// evaluates c2^2 - 4 (a_{n-1} a_n - b_{n-1}^2) with both leading products
+// fused).  Returns false when the sweep budget runs out.
+static bool givens81(double* a, double* b, double* Q, int N, int m, int n, double eps, long long& budget) {
+    while (n > m) {
+        if (std::fabs(b[m]) < eps) {
+            ++m;
+            continue;
+        }
+        if (std::fabs(b[n - 1]) < eps) {
+            --n;
+            continue;
+        }
+        for (int i = m + 1; i < n - 1; ++i) {
+            if (std::fabs(b[i]) < eps) {
+                if (!givens81(a, b, Q, N, m, i, eps, budget)) return false;
+                m = i + 1;
+            }
+        }
+        if (--budget < 0) return false;
+        double c2 = a[n - 1] + a[n];
+        double s2 = std::sqrt(std::fma(c2, c2, -(std::fma(a[n - 1], a[n], -(b[n - 1] * b[n - 1])) * 4.0)));
+        double t = (c2 - 2.0 * a[n] > 0) ? (c2 - s2) * 0.5 : (c2 + s2) * 0.5;
+        double c, s;
+        if (std::fabs(b[m]) > std::fabs(a[m] - t))
+            rot81(a, b, m, (a[m] - t) / b[m], true, c, s);
+        else
+            rot81(a, b, m, b[m] / (a[m] - t), false, c, s);
+        double B = s * b[m + 1];
+        b[m + 1] = c * b[m + 1];
+        apply_rot81(Q, N, m, c, s);
+        for (int i = m + 1; i < n; ++i) {
+            if (std::fabs(B) > std::fabs(b[i - 1]))
+                rot81(a, b, i, b[i - 1] / B, true, c, s);
+            else
+                rot81(a, b, i, B / b[i - 1], false, c, s);
+            b[i - 1] = std::fma(c, b[i - 1], s * B);
+            B = s * b[i + 1];
+            b[i + 1] = c * b[i + 1];
+            apply_rot81(Q, N, i, c, s);
+        }
+    }
+    return true;
+}
+
+extern "C" {
+
+// The tridiagonalisation of EVD_Q (Mat-8.1/EVD/__QR.h:2-47, with Q formed by
+// QR/__Householder.h:124-152): A symmetric n x n (lower triangle read),
+// d (n), e (n - 1), Q (n x n, ld ldq) with Q^T A Q = tridiag(e, d, e).
+void orc_tridiag81(int n, const double* A, int lda, double* Q, int ldq, double* d, double* e) {
+    std::vector<double> U;
+    tridiag81(n, A, lda, d, e, U);
+    form_q81(n, U, Q, ldq);
+}
+
+
+// EVD_Q(A, E, Q, eps, EVD_QR) of the Mat-8.1 snapshot (EVD/EVD_Q.h:7-35 ->
+// EVD/__QR.h:145-169): eigenvalues in w (E's diagonal), eigenvectors in Q's
+// columns (n x n, ld n).  Returns 0, or 1 when the QR sweeps did not deflate
+// within 64 n sweeps (the reference loops on).
+int orc_evd_q81(int n, const double* A, double eps, double* w, double* Q) {
+    std::vector<double> e((size_t)n + 1, 0.0);
+    orc_tridiag81(n, A, n, Q, n, w, e.data());
+    e[n > 0 ? n - 1 : 0] = 0.0;
+    long long budget = 64LL * n;
+    return givens81(w, e.data(), Q, n, 0, n - 1, eps, budget) ? 0 : 1;
+}
+
+}  // extern "C"

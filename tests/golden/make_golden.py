@@ -1,6 +1,7 @@
 """Generates the golden fixtures in this directory by running the reference
 itself: Mat-8.3.1 compiled from its own headers into oracle/_ref/libmatref.so
-(x86-64 AVX-512 build, the configuration of Mat's published numbers).
+(x86-64 AVX-512 build, the configuration of Mat's published numbers), and the
+Mat-8.1 snapshot's EVD_Q path into oracle/_ref/libmat81ref.so.
 
 Inputs come from the library's seeded generators (mg_host_fill_*), which are
 bit-identical on the host and the GPU.  Small cases keep full outputs; the
@@ -23,9 +24,10 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
 from mat_gb300.api import host_fill_normal, host_fill_uniform  # noqa: E402
-from oracle.api import reference  # noqa: E402
+from oracle.api import reference, reference81  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
+EVD_EPS = 1e-10  # absolute deflation threshold of the EVD_Q cases
 
 
 def sha(a: np.ndarray) -> str:
@@ -129,6 +131,23 @@ def main():
     for n in (97, 300, 1000, 2048):
         x = ref.inv(host_fill_normal(n, n, 9))
         meta["cases"][f"inv_{n}"] = {"sha256": sha(x), "sketch": sketch(x)}
+
+    # EVD_Q of the Mat-8.1 snapshot (oracle/_ref/libmat81ref.so): symmetric G + G^T;
+    # tridiagonalisation (Q, d, e) and the whole EVD_Q with EVD_QR (w, Q) at an
+    # absolute deflation threshold; one case in full, larger ones by digest
+    ref81 = reference81()
+    if ref81 is None:
+        raise SystemExit("the Mat-8.1 reference build (oracle/_ref/libmat81ref.so) is missing")
+    meta["evd81"] = {"reference": "Mat-8.1 snapshot (AVX-512 build)", "eps": EVD_EPS}
+    q, d, e = ref81.tridiag81(sym(37, 21))
+    w, qe = ref81.evd_q81(sym(37, 21), EVD_EPS)
+    np.savez_compressed(OUT / "evd81_37.npz", Q=q, d=d, e=e, w=w, Qe=qe)
+    for n in (64, 200, 500):
+        q, d, e = ref81.tridiag81(sym(n, 21))
+        w, qe = ref81.evd_q81(sym(n, 21), EVD_EPS)
+        meta["cases"][f"tridiag81_{n}"] = {"sha256_Q": sha(q), "sha256_d": sha(d[:, None]),
+                                           "sha256_e": sha(e[:, None])}
+        meta["cases"][f"evd81_{n}"] = {"sha256_w": sha(w[:, None]), "sha256_Q": sha(qe)}
 
     meta["seconds"] = round(time.time() - t0, 1)
     (OUT / "golden.json").write_text(json.dumps(meta, indent=1))

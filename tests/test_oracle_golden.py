@@ -141,3 +141,61 @@ def test_restatement_equals_reference_build(orc, m, n):
                 continue  # the reference's one-block 8-column path overruns its 60-row buffer there
             b = host_fill_normal(n, k, 13)
             assert np.array_equal(orc.solve(a, b), ref.solve(a, b))
+
+
+# ---------------------------------------------------------------- Mat-8.1 EVD_Q
+EVD_EPS = json.loads((G / "golden.json").read_text())["evd81"]["eps"]
+
+
+def sym(n, seed):
+    g = host_fill_normal(n, n, seed)
+    return np.asfortranarray(g + g.T)
+
+
+def test_tridiag81_and_evd_q81(orc):
+    """The Mat-8.1 tridiagonalisation and EVD_Q (EVD_QR) bit for bit: n = 37 in
+    full, n = 64, 200, 500 by digest."""
+    f = np.load(G / "evd81_37.npz")
+    q, d, e = orc.tridiag81(sym(37, 21))
+    assert np.array_equal(q, f["Q"]) and np.array_equal(d, f["d"]) and np.array_equal(e, f["e"])
+    w, qe = orc.evd_q81(sym(37, 21), EVD_EPS)
+    assert np.array_equal(w, f["w"]) and np.array_equal(qe, f["Qe"])
+    for n in (64, 200, 500):
+        q, d, e = orc.tridiag81(sym(n, 21))
+        c = META[f"tridiag81_{n}"]
+        assert (sha(q), sha(d[:, None]), sha(e[:, None])) == (c["sha256_Q"], c["sha256_d"], c["sha256_e"])
+        w, qe = orc.evd_q81(sym(n, 21), EVD_EPS)
+        assert (sha(w[:, None]), sha(qe)) == (META[f"evd81_{n}"]["sha256_w"], META[f"evd81_{n}"]["sha256_Q"])
+
+
+def test_evd_q81_properties(orc):
+    """Q^T A Q is the tridiagonal; the eigenpairs satisfy A Q = Q diag(w)."""
+    a = sym(150, 5)
+    q, d, e = orc.tridiag81(a)
+    t = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+    assert np.abs(q.T @ q - np.eye(150)).max() < 1e-13
+    assert np.abs(q.T @ a @ q - t).max() < 1e-12 * np.abs(a).max()
+    w, qe = orc.evd_q81(a, 1e-10)
+    assert np.abs(a @ qe - qe * w).max() < 1e-9
+    assert np.allclose(np.sort(w), np.linalg.eigvalsh(a), atol=1e-10)
+
+
+def test_evd_q81_budget():
+    """With eps = 0 no off-diagonal ever counts as negligible: Mat would loop
+    on; the oracle (like the library) stops after 64 n sweeps."""
+    with pytest.raises(RuntimeError):
+        restatement().evd_q81(sym(12, 3), 0.0)
+
+
+@pytest.mark.parametrize("n", [2, 3, 8, 9, 33, 130])
+def test_evd81_restatement_equals_reference_build(orc, n):
+    from oracle.api import reference81
+
+    ref = reference81()
+    if ref is None:
+        pytest.skip("the Mat-8.1 reference build needs the reference tree and an x86-64 host")
+    a = sym(n, 40 + n)
+    for x, y in zip(orc.tridiag81(a), ref.tridiag81(a)):
+        assert np.array_equal(x, y)
+    for x, y in zip(orc.evd_q81(a, 1e-11), ref.evd_q81(a, 1e-11)):
+        assert np.array_equal(x, y)
