@@ -40,7 +40,9 @@
 //    chunks; the application is independent per row of Q (one thread per row,
 //    the carried column in a register, loads of the sweep's next columns
 //    issued ahead).
+#include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "grid_sync.cuh"
@@ -50,6 +52,12 @@ namespace {
 
 constexpr int TD_THREADS = 256;
 constexpr int TD_WARPS = TD_THREADS / 32;
+constexpr int TD_CH = 128;                           // fused-chain stage: columns per chunk
+constexpr int TD_BUF = TD_CH * 32;                   // doubles per chain chunk (32 rows)
+constexpr int TD_SMEM_DBL = 2 * TD_BUF + 2 * TD_CH;  // dynamic shared memory, doubles
+constexpr int TD_STAGE = TD_BUF;                     // phase 2 keeps v and w on chip when nn <= this
+constexpr int TD_COLREG = TD_STAGE / TD_THREADS;     // column-0 values per thread (phase 2, CTA 0)
+constexpr int TD_PER = (TD_BUF + TD_THREADS - 32 - 1) / (TD_THREADS - 32);  // chunk loads per producer thread
 
 // Mat-8.1 __dot reduction of the eight lane accumulators of an aligned group
 // of eight lanes; the result is valid in the group's first lane.  All 32
@@ -115,17 +123,47 @@ struct TdArgs {
     double* vd;  // n: column-dot part of v
     unsigned* bar;
     int* err;
+    int stage_cap;  // phase 2 keeps v, w and column 0 on chip while nn <= stage_cap (<= TD_STAGE)
 };
 
-// All steps m = 0 .. n-3 of __EVD_Q_Householder.  Cooperative launch; the
-// barrier counter starts at zero.
+// Stages chunk c0 .. c0+TD_CH-1 of the columns 0..ncol-1 of the trailing
+// matrix's rows k0 .. k0+31 (buf[c 32 + r] = T[(c0+c) ld + k0+r], zero
+// outside) and the matching reflector entries, with nthr threads (id tid).
+__device__ __forceinline__ void td_chain_load(const double* T, int ld, const double* w, int nn, int k0, int ncol,
+                                              int c0, double* buf, double* wb, int tid, int nthr) {
+    double v[TD_PER + 2];
+#pragma unroll
+    for (int u = 0; u < TD_PER + 2; ++u) {
+        const int idx = tid + u * nthr;
+        const int c = idx >> 5, r = idx & 31;
+        v[u] = (idx < TD_BUF && c0 + c < ncol && k0 + r < nn) ? __ldcg(T + (size_t)(c0 + c) * ld + k0 + r) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < TD_PER + 2; ++u) {
+        const int idx = tid + u * nthr;
+        if (idx < TD_BUF) buf[idx] = v[u];
+    }
+    if (tid < TD_CH) wb[tid] = c0 + tid < ncol ? __ldcg(w + c0 + tid) : 0.0;
+}
+
+// All steps m = 0 .. n-3 of __EVD_Q_Householder.  Cooperative launch (at
+// least two CTAs); the barrier counter starts at zero.
+//  phase 1: CTAs 0 .. nchc-1 run the fused chains of v, 32 elements per CTA:
+//           seven warps stage the rows' columns chunk by chunk in shared
+//           memory while warp 0 runs the 32 chains on the previous chunk; the
+//           other CTAs' warps take the column dots, one warp per column (all
+//           32 lanes load, lanes 0..7 run Mat's eight ordered chains on
+//           shuffled operands);
+//  phase 2: every CTA stages v and w in shared memory and computes h; CTA 0
+//           updates column 0, keeps it on chip and forms the next reflector;
+//           the warps of CTAs 1.. update columns 1.. (above stage_cap the same
+//           steps read v, w and the column from global memory).
 __global__ void __launch_bounds__(TD_THREADS) tridiag81_kernel(TdArgs a) {
+    extern __shared__ __align__(16) double smem[];
     const int G = gridDim.x, cta = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int gw = warp * G + cta;  // grid-wide warp id, consecutive ids on different CTAs
-    const int NWG = G * TD_WARPS;
     const int n = a.n, ld = a.ld;
-    __shared__ double s_h;
+    __shared__ double s_h, s_w0, s_hr;
     unsigned target = 0;
     if (cta == 0 && warp == 0) td_reflector(a.W, n - 1, a.d, a.e);
     if (!mg::grid_barrier(a.bar, target += G, a.err)) return;
@@ -135,86 +173,216 @@ __global__ void __launch_bounds__(TD_THREADS) tridiag81_kernel(TdArgs a) {
         double* T = a.W + (size_t)(m + 1) * ld + (m + 1);  // T[i ld + k] = W_m(1+k, 1+i)
         // ---- phase 1: v = W22 w
         const int nchain = (nn + 31) / 32;
-        const int nchw = min(nchain, NWG / 2);  // chain workers; the other warps take the column dots
-        if (gw < nchw) {
+        const int nchc = min(nchain, G / 2);
+        if (cta < nchc) {
             // v_k = fma chain over i = 0..k of W22(k, i) w_i (EVD/__QR.h:27-29)
-            for (int cw = gw; cw < nchain; cw += nchw) {
-            const int k = cw * 32 + lane;
-            const int imax = min(cw * 32 + 31, nn - 1);
-            double acc = 0.0;
-            int i = 0;
-            for (; i + 7 <= imax; i += 8) {
-                double xt[8], xw[8];
+            double* buf = smem;
+            double* wb = smem + 2 * TD_BUF;
+            for (int cb = cta; cb < nchain; cb += nchc) {
+                const int k0 = cb * 32, ncol = min(k0 + 32, nn);
+                const int nchunk = (ncol + TD_CH - 1) / TD_CH;
+                td_chain_load(T, ld, w, nn, k0, ncol, 0, buf, wb, tid, TD_THREADS);
+                __syncthreads();
+                double acc = 0.0;
+                for (int t = 0; t < nchunk; ++t) {
+                    if (warp == 0) {
+                        const double* cur = buf + (t & 1) * TD_BUF;
+                        const double* cw = wb + (t & 1) * TD_CH;
+                        const int c0 = t * TD_CH;
+                        const int clim = min(min(TD_CH, ncol - c0), k0 + lane - c0 + 1);  // columns i <= k
+                        int c = 0;
+                        for (; c + 8 <= clim; c += 8) {
+                            double xt[8], xw[8];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    xt[u] = k < nn ? __ldcg(T + (size_t)(i + u) * ld + k) : 0.0;
-                    xw[u] = __ldcg(w + i + u);
+                            for (int u = 0; u < 8; ++u) {
+                                xt[u] = cur[(c + u) * 32 + lane];
+                                xw[u] = cw[c + u];
+                            }
+#pragma unroll
+                            for (int u = 0; u < 8; ++u) acc = fma(xt[u], xw[u], acc);
+                        }
+                        for (; c < clim; ++c) acc = fma(cur[c * 32 + lane], cw[c], acc);
+                    } else if (t + 1 < nchunk) {
+                        td_chain_load(T, ld, w, nn, k0, ncol, (t + 1) * TD_CH, buf + ((t + 1) & 1) * TD_BUF,
+                                      wb + ((t + 1) & 1) * TD_CH, tid - 32, TD_THREADS - 32);
+                    }
+                    __syncthreads();
                 }
-#pragma unroll
-                for (int u = 0; u < 8; ++u)
-                    if (i + u <= k) acc = fma(xt[u], xw[u], acc);
-            }
-            for (; i <= imax; ++i)
-                if (i <= k && k < nn) acc = fma(__ldcg(T + (size_t)i * ld + k), __ldcg(w + i), acc);
-            if (k < nn) a.vc[k] = acc;
+                if (warp == 0 && k0 + lane < nn) a.vc[k0 + lane] = acc;
             }
         } else {
-            // v_i += dot(W22(i+1:, i), w(i+1:)) (EVD/__QR.h:30-32), eight lanes per column
-            const int ndw = (NWG - nchw) * 4;
-            const int grp = lane >> 3, l = lane & 7;
-            for (int i0 = (gw - nchw) * 4; i0 < nn; i0 += ndw) {
-                const int i = i0 + grp;
-                const int len = i < nn ? nn - i - 1 : 0;
+            // v_i += dot(W22(i+1:, i), w(i+1:)) (EVD/__QR.h:30-32), one warp per column
+            const int ndw = (G - nchc) * TD_WARPS;
+            for (int i = warp * (G - nchc) + (cta - nchc); i < nn; i += ndw) {
+                const int len = nn - i - 1;
+                const double* pa = T + (size_t)i * ld + i + 1;
+                const double* pb = w + i + 1;
                 double acc = 0.0;
-                if (len > 0) acc = dot8_lane(T + (size_t)i * ld + i + 1, w + i + 1, len, l);
+                for (int base = 0; base < len; base += 256) {
+                    double xa[8], xb[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int e = base + 32 * u + lane;
+                        xa[u] = e < len ? __ldcg(pa + e) : 0.0;
+                        xb[u] = e < len ? __ldcg(pb + e) : 0.0;
+                    }
+                    // lane l (< 8) takes the elements base + 8j + l, j = 0..31, in order
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const int src = ((j & 3) << 3) | (lane & 7);
+                        const double x = __shfl_sync(0xffffffffu, xa[j >> 2], src);
+                        const double y = __shfl_sync(0xffffffffu, xb[j >> 2], src);
+                        if (lane < 8 && base + 8 * j + lane < len) acc = fma(x, y, acc);
+                    }
+                }
                 const double r = red8(acc);
-                if (l == 0 && i < nn) a.vd[i] = r;
+                if (lane == 0) a.vd[i] = r;
             }
         }
         if (!mg::grid_barrier(a.bar, target += G, a.err)) return;
         // ---- phase 2: h = v.w, then the rank-2 update (EVD/__QR.h:34-39)
+        const bool staged = nn <= a.stage_cap;
+        double* sv = smem;
+        double* sw = smem + TD_STAGE;
+        if (staged) {
+            for (int k = tid; k < nn; k += TD_THREADS) {
+                sv[k] = __dadd_rn(__ldcg(a.vc + k), __ldcg(a.vd + k));
+                sw[k] = __ldcg(w + k);
+            }
+            __syncthreads();
+        }
         if (warp == 0) {
             double acc = 0.0;
             if (lane < 8) {
-                int e = lane;
-                for (; e + 7 * 8 < nn; e += 8 * 8) {
-                    double xv[8], xw[8];
+                if (staged) {
+                    int e = lane;
+                    for (; e + 7 * 8 < nn; e += 8 * 8) {
+                        double xv[8], xw[8];
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        const int q = e + 8 * u;
-                        xv[u] = __dadd_rn(__ldcg(a.vc + q), __ldcg(a.vd + q));
-                        xw[u] = __ldcg(w + q);
+                        for (int u = 0; u < 8; ++u) {
+                            xv[u] = sv[e + 8 * u];
+                            xw[u] = sw[e + 8 * u];
+                        }
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) acc = fma(xv[u], xw[u], acc);
                     }
+                    for (; e < nn; e += 8) acc = fma(sv[e], sw[e], acc);
+                } else {
+                    int e = lane;
+                    for (; e + 7 * 8 < nn; e += 8 * 8) {
+                        double xv[8], xw[8];
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) acc = fma(xv[u], xw[u], acc);
+                        for (int u = 0; u < 8; ++u) {
+                            const int q = e + 8 * u;
+                            xv[u] = __dadd_rn(__ldcg(a.vc + q), __ldcg(a.vd + q));
+                            xw[u] = __ldcg(w + q);
+                        }
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) acc = fma(xv[u], xw[u], acc);
+                    }
+                    for (; e < nn; e += 8)
+                        acc = fma(__dadd_rn(__ldcg(a.vc + e), __ldcg(a.vd + e)), __ldcg(w + e), acc);
                 }
-                for (; e < nn; e += 8) acc = fma(__dadd_rn(__ldcg(a.vc + e), __ldcg(a.vd + e)), __ldcg(w + e), acc);
             }
             const double hh = red8(acc);
             if (lane == 0) s_h = hh;
         }
         __syncthreads();
         const double h = s_h;
-        auto update_column = [&](int i) {
-            const double wi = __ldcg(w + i);
-            const double vi = __dadd_rn(__ldcg(a.vc + i), __ldcg(a.vd + i));
-            const double q = fma(wi, h, -vi);
-            double* col = T + (size_t)i * ld;
-            for (int k = i + lane; k < nn; k += 32) {
-                const double vk = __dadd_rn(__ldcg(a.vc + k), __ldcg(a.vd + k));
-                col[k] = fma(__ldcg(w + k), q, fma(vk, -wi, __ldcg(col + k)));
-            }
-        };
-        if (gw == 0) {
-            update_column(0);
-            if (m + 3 < n) {
-                // the next reflector from the updated first column (EVD/__QR.h:16-24)
-                __threadfence();
-                __syncwarp();
-                td_reflector(T, nn - 1, a.d + m + 1, a.e + m + 1);
+        if (cta == 0) {
+            if (staged) {
+                // column 0 of W_{m+1}, kept in registers, then on chip for the reflector
+                const double w0v = sw[0], q = fma(w0v, h, -sv[0]);
+                double cv[TD_COLREG];
+#pragma unroll
+                for (int t = 0; t < TD_COLREG; ++t) {
+                    const int k = tid + t * TD_THREADS;
+                    cv[t] = 0.0;
+                    if (k < nn) {
+                        cv[t] = fma(sw[k], q, fma(sv[k], -w0v, __ldcg(T + k)));
+                        T[k] = cv[t];
+                    }
+                }
+                if (m + 3 < n) {
+                    __syncthreads();  // v and w are no longer read
+                    double* scol = smem;
+#pragma unroll
+                    for (int t = 0; t < TD_COLREG; ++t) {
+                        const int k = tid + t * TD_THREADS;
+                        if (k < nn) scol[k] = cv[t];
+                    }
+                    __syncthreads();
+                    // the next reflector from the updated first column (EVD/__QR.h:16-24)
+                    const int len = nn - 1;
+                    if (warp == 0) {
+                        double acc = 0.0;
+                        if (lane < 8) {
+                            int e = lane;
+                            for (; e + 7 * 8 < len; e += 8 * 8) {
+                                double xa[8];
+#pragma unroll
+                                for (int u = 0; u < 8; ++u) xa[u] = scol[1 + e + 8 * u];
+#pragma unroll
+                                for (int u = 0; u < 8; ++u) acc = fma(xa[u], xa[u], acc);
+                            }
+                            for (; e < len; e += 8) acc = fma(scol[1 + e], scol[1 + e], acc);
+                        }
+                        const double ss = red8(acc);
+                        if (lane == 0) {
+                            const double x0 = scol[1];
+                            double cr = sqrt(ss);
+                            if (x0 < 0.0) cr = -cr;
+                            const double w0 = __dadd_rn(x0, cr);
+                            s_w0 = w0;
+                            s_hr = 1.0 / sqrt(__dmul_rn(cr, w0));
+                            a.d[m + 1] = scol[0];
+                            a.e[m + 1] = -cr;
+                        }
+                    }
+                    __syncthreads();
+                    const double w0 = s_w0, hr = s_hr;
+                    for (int k = tid; k < len; k += TD_THREADS) T[1 + k] = __dmul_rn(k == 0 ? w0 : scol[1 + k], hr);
+                }
+            } else if (warp == 0) {
+                const double wi = __ldcg(w), q = fma(wi, h, -__dadd_rn(__ldcg(a.vc), __ldcg(a.vd)));
+                for (int k = lane; k < nn; k += 32) {
+                    const double vk = __dadd_rn(__ldcg(a.vc + k), __ldcg(a.vd + k));
+                    T[k] = fma(__ldcg(w + k), q, fma(vk, -wi, __ldcg(T + k)));
+                }
+                if (m + 3 < n) {
+                    __threadfence();
+                    __syncwarp();
+                    td_reflector(T, nn - 1, a.d + m + 1, a.e + m + 1);
+                }
             }
         } else {
-            for (int i = gw; i < nn; i += NWG - 1 > 0 ? NWG - 1 : 1) update_column(i);
+            // columns 1 .. nn-1 over the warps of CTAs 1 .. G-1
+            const int nw2 = (G - 1) * TD_WARPS;
+            for (int i = 1 + warp * (G - 1) + (cta - 1); i < nn; i += nw2) {
+                double* col = T + (size_t)i * ld;
+                if (staged) {
+                    const double wi = sw[i], q = fma(wi, h, -sv[i]);
+                    int k = i + lane;
+                    for (; k + 7 * 32 < nn; k += 8 * 32) {
+                        double x[8];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) x[u] = __ldcg(col + k + 32 * u);
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const int kk = k + 32 * u;
+                            col[kk] = fma(sw[kk], q, fma(sv[kk], -wi, x[u]));
+                        }
+                    }
+                    for (; k < nn; k += 32) col[k] = fma(sw[k], q, fma(sv[k], -wi, __ldcg(col + k)));
+                } else {
+                    const double wi = __ldcg(w + i);
+                    const double q = fma(wi, h, -__dadd_rn(__ldcg(a.vc + i), __ldcg(a.vd + i)));
+                    for (int k = i + lane; k < nn; k += 32) {
+                        const double vk = __dadd_rn(__ldcg(a.vc + k), __ldcg(a.vd + k));
+                        col[k] = fma(__ldcg(w + k), q, fma(vk, -wi, __ldcg(col + k)));
+                    }
+                }
+            }
         }
         if (!mg::grid_barrier(a.bar, target += G, a.err)) return;
     }
@@ -272,6 +440,76 @@ __global__ void formq81_kernel(const double* __restrict__ U, int ldu, int n, dou
     }
 }
 
+// The same Q formation with a CTA's FQ_COLS columns of Q and the reflector
+// (double-buffered) in shared memory, for n <= FQ_NMAX: warp 0 runs the
+// columns' dot chains (eight lanes per column) while warps 1.. stage the next
+// reflector; then all threads apply the axpy on chip.  Columns start as e_j;
+// the kernel writes every column of Q.
+constexpr int FQ_COLS = 4;
+constexpr int FQ_THREADS = 128;
+constexpr int FQ_NMAX = 4096;
+
+__global__ void __launch_bounds__(FQ_THREADS) formq81_smem_kernel(const double* __restrict__ U, int ldu, int n,
+                                                                  double* __restrict__ Q, int ldq) {
+    extern __shared__ __align__(16) double fsm[];
+    double* qs = fsm;                  // FQ_COLS x n
+    double* us = fsm + FQ_COLS * n;    // 2 x n
+    __shared__ double s_s[FQ_COLS];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int j0 = blockIdx.x * FQ_COLS;
+    for (int c = 0; c < FQ_COLS; ++c)
+        for (int r = tid; r < n; r += FQ_THREADS) qs[c * n + r] = j0 + c == r ? 1.0 : 0.0;
+    const int rtop = min(j0 + FQ_COLS - 2, n - 3);
+    if (rtop >= 0)
+        for (int e = tid; e < n - rtop - 1; e += FQ_THREADS) us[e] = __ldg(U + (size_t)rtop * ldu + rtop + 1 + e);
+    __syncthreads();
+    for (int r = rtop, b = 0; r >= 0; --r, b ^= 1) {
+        const int len = n - r - 1;
+        const double* u = us + b * n;
+        if (warp == 0) {
+            const int grp = lane >> 3, l = lane & 7, j = j0 + grp;
+            const bool act = j < n && j >= r + 1;
+            const double* qc = qs + grp * n + r + 1;
+            double acc = 0.0;
+            if (act) {
+                int e = l;
+                for (; e + 7 * 8 < len; e += 8 * 8) {
+                    double xa[8], xb[8];
+#pragma unroll
+                    for (int t = 0; t < 8; ++t) {
+                        xa[t] = u[e + 8 * t];
+                        xb[t] = qc[e + 8 * t];
+                    }
+#pragma unroll
+                    for (int t = 0; t < 8; ++t) acc = fma(xa[t], xb[t], acc);
+                }
+                for (; e < len; e += 8) acc = fma(u[e], qc[e], acc);
+            }
+            const double sred = red8(acc);
+            if (l == 0) s_s[grp] = act ? -sred : 0.0;
+        } else if (r > 0) {
+            const int rn = r - 1;
+            double* un = us + (b ^ 1) * n;
+            for (int e = tid - 32; e < n - rn - 1; e += FQ_THREADS - 32)
+                un[e] = __ldg(U + (size_t)rn * ldu + rn + 1 + e);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < FQ_COLS; ++c) {
+            const int j = j0 + c;
+            if (j < n && j >= r + 1) {
+                const double sc = s_s[c];
+                double* qc = qs + c * n + r + 1;
+                for (int e = tid; e < len; e += FQ_THREADS) qc[e] = fma(u[e], sc, qc[e]);
+            }
+        }
+        __syncthreads();
+    }
+    for (int c = 0; c < FQ_COLS; ++c)
+        if (j0 + c < n)
+            for (int r = tid; r < n; r += FQ_THREADS) Q[(size_t)(j0 + c) * ldq + r] = qs[c * n + r];
+}
+
 __global__ void evd_identity_kernel(double* __restrict__ Q, int ldq, int n) {
     const size_t total = (size_t)n * n;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
@@ -301,42 +539,96 @@ struct Sweep {
     int start, len, off, pad;
 };
 
-// The rotations of a chunk of sweeps applied to Q's columns, one thread per
-// row of Q: sweep (start, len) rotates the column pairs (start, start+1), ...,
-// (start+len-1, start+len) in order, each by (c, s):
-// x' = fma(x, c, y s), y' = fma(-x, s, y c) (SIMD/__AVX512_double.h:1-20).
-__global__ void rot81_kernel(double* __restrict__ Q, int ldq, int n, const Sweep* __restrict__ sw, int nsw,
-                             const double2* __restrict__ cs) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n) return;
-    double* row = Q + r;
-    for (int si = 0; si < nsw; ++si) {
+// The rotations of a chunk of sweeps applied to Q's columns: sweep (start,
+// len) rotates the column pairs (start, start+1), ..., (start+len-1,
+// start+len) in order, each by (c, s): x' = fma(x, c, y s),
+// y' = fma(-x, s, y c) (SIMD/__AVX512_double.h:1-20).  Every row is
+// independent; a warp holds 32 rows (one per lane) and carries the current
+// column in a register.  One warp instruction of FP64 work keeps the SM
+// sub-partition's FP64 pipe busy for many cycles whatever the active lanes,
+// so a lone warp per row strip is bound by the rotation count: ROT_WARPS
+// warps share each 32-row strip instead, warp w applying the sweeps
+// s = w, w + ROT_WARPS, ... .  A sweep may touch a column only after every
+// earlier sweep still in flight has finished with it: each warp publishes in
+// shared memory (sweep << 32 | P), "columns < P are final for this sweep",
+// after every batch of ROT_PF rotations, and waits (bounded) on the others'
+// words before the batch.  Rows are read and written through L1 (the warps
+// of one CTA share an SM).
+constexpr int ROT_WARPS = 4;
+constexpr int ROT_PF = 16;  // rotations per batch (the loads of a batch are in flight together)
+
+__device__ __forceinline__ bool rot_wait(volatile unsigned long long* prog, int s, int need, int* err) {
+    bool ok = true;
+    if ((threadIdx.x & 31) == 0) {
+        for (int q = s - 1; q >= 0 && q > s - ROT_WARPS; --q) {
+            const unsigned long long want = ((unsigned long long)q << 32) | (unsigned)need;
+            unsigned spins = 0;
+            while (prog[q % ROT_WARPS] < want) {
+                if (++spins > mg::kSpinLimit) {
+                    atomicExch(err, 8 /* MG_TIMEOUT */);
+                    ok = false;
+                    break;
+                }
+                if (spins > 64) __nanosleep(32);
+            }
+            if (!ok) break;
+        }
+        __threadfence_block();
+    }
+    const bool all_ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+    __syncwarp();  // the other lanes' loads come after lane 0 saw the flags
+    return all_ok;
+}
+
+__global__ void __launch_bounds__(32 * ROT_WARPS) rot81_kernel(double* __restrict__ Q, int ldq, int n,
+                                                               const Sweep* __restrict__ sw, int nsw,
+                                                               const double2* __restrict__ cs, int* err) {
+    __shared__ unsigned long long prog[ROT_WARPS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int r = blockIdx.x * 32 + lane;
+    const bool live = r < n;
+    double* row = Q + (live ? r : 0);
+    if (lane == 0) prog[warp] = (unsigned long long)warp << 32;  // sweep `warp`, nothing final yet
+    __syncthreads();
+    volatile unsigned long long* vprog = prog;
+    for (int si = warp; si < nsw; si += ROT_WARPS) {
         const Sweep S = sw[si];
         const double2* p = cs + S.off;
-        double x = row[(size_t)S.start * ldq];
-        int k = 0;
-        for (; k + 8 <= S.len; k += 8) {
-            double y[8];
-            double2 c[8];
+        double x = 0.0;
+        for (int k = 0; k < S.len; k += ROT_PF) {
+            const int nb = min(ROT_PF, S.len - k);
+            // this batch reads columns up to start + k + nb
+            if (!rot_wait(vprog, si, S.start + k + nb + 1, err)) return;
+            if (k == 0 && live) x = row[(size_t)S.start * ldq];
+            double y[ROT_PF];
+            double2 c[ROT_PF];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                y[u] = row[(size_t)(S.start + k + 1 + u) * ldq];
-                c[u] = __ldg(p + k + u);
+            for (int u = 0; u < ROT_PF; ++u) {
+                y[u] = (u < nb && live) ? row[(size_t)(S.start + k + 1 + u) * ldq] : 0.0;
+                c[u] = u < nb ? __ldg(p + k + u) : make_double2(0.0, 0.0);
             }
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                row[(size_t)(S.start + k + u) * ldq] = fma(x, c[u].x, __dmul_rn(y[u], c[u].y));
-                x = fma(-x, c[u].y, __dmul_rn(y[u], c[u].x));
+            for (int u = 0; u < ROT_PF; ++u) {
+                if (u < nb) {
+                    const double xn = fma(x, c[u].x, __dmul_rn(y[u], c[u].y));
+                    if (live) row[(size_t)(S.start + k + u) * ldq] = xn;
+                    x = fma(-x, c[u].y, __dmul_rn(y[u], c[u].x));
+                }
             }
+            if (k + nb == S.len && live) row[(size_t)(S.start + S.len) * ldq] = x;
+            __threadfence_block();
+            __syncwarp();
+            if (lane == 0)
+                vprog[warp] = k + nb == S.len
+                                  ? (unsigned long long)(si + ROT_WARPS) << 32  // sweep done: the next one, nothing final
+                                  : ((unsigned long long)si << 32) | (unsigned)(S.start + k + nb);
         }
-        for (; k < S.len; ++k) {
-            const double y = row[(size_t)(S.start + k + 1) * ldq];
-            const double2 c = __ldg(p + k);
-            row[(size_t)(S.start + k) * ldq] = fma(x, c.x, __dmul_rn(y, c.y));
-            x = fma(-x, c.y, __dmul_rn(y, c.x));
+        if (S.len == 0) {
+            __syncwarp();
+            if (lane == 0) vprog[warp] = (unsigned long long)(si + ROT_WARPS) << 32;
         }
-        row[(size_t)(S.start + S.len) * ldq] = x;
     }
+    if (lane == 0) vprog[warp] = ~0ull;
 }
 
 int evd_grid(mg_handle_t h, size_t total) {
@@ -436,6 +728,7 @@ struct GpuRotSink final : RotSink {
     mg_handle_t h;
     double* Q;
     int ldq, n;
+    int* err = nullptr;    // device error word (MG_TIMEOUT if a bounded wait gave up)
     size_t cap_rot, cap_sw;
     double2* hcs[2];
     Sweep* hsw[2];
@@ -446,6 +739,7 @@ struct GpuRotSink final : RotSink {
     int cur = 0;
     size_t nrot = 0, nsw = 0;
     long long total_rot = 0;
+    double wait_ms = 0;  // host time spent waiting for the GPU to free a staging area
     mg_status_t st = MG_OK;
 
     bool flush() {
@@ -458,7 +752,7 @@ struct GpuRotSink final : RotSink {
             st = mg::cuda_fail(h, e, "EVD_Q rotation upload");
             return false;
         }
-        rot81_kernel<<<(n + 127) / 128, 128, 0, s>>>(Q, ldq, n, dsw[cur], (int)nsw, dcs[cur]);
+        rot81_kernel<<<(n + 31) / 32, 32 * ROT_WARPS, 0, s>>>(Q, ldq, n, dsw[cur], (int)nsw, dcs[cur], err);
         if ((st = mg::post_launch(h, "rot81_kernel")) != MG_OK) return false;
         if ((e = cudaEventRecord(done[cur], s)) != cudaSuccess) {
             st = mg::cuda_fail(h, e, "cudaEventRecord");
@@ -467,9 +761,14 @@ struct GpuRotSink final : RotSink {
         used[cur] = true;
         cur ^= 1;
         nrot = nsw = 0;
-        if (used[cur] && (e = cudaEventSynchronize(done[cur])) != cudaSuccess) {
-            st = mg::cuda_fail(h, e, "cudaEventSynchronize");
-            return false;
+        if (used[cur]) {
+            const auto t0 = std::chrono::steady_clock::now();
+            e = cudaEventSynchronize(done[cur]);
+            wait_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            if (e != cudaSuccess) {
+                st = mg::cuda_fail(h, e, "cudaEventSynchronize");
+                return false;
+            }
         }
         return true;
     }
@@ -514,13 +813,22 @@ static mg_status_t tridiag81(mg_handle_t h, int n, double* W, int ldw, double** 
     MG_CHECK_CUDA(h, cudaMemsetAsync(a.e, 0, vb, st));
     if (n >= 3) {
         ProfScope prof(h, "tridiag81", 4.0 / 3.0 * n * (double)n * n, 8.0 * n * (double)n * n / 1.5);
+        const int smem = TD_SMEM_DBL * (int)sizeof(double);
+        MG_CHECK_CUDA(h, cudaFuncSetAttribute(tridiag81_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         int per_sm = 0;
-        MG_CHECK_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag81_kernel, TD_THREADS, 0));
+        MG_CHECK_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag81_kernel, TD_THREADS, smem));
         if (per_sm < 1) return fail(h, MG_ERR_CUDA, "tridiag81_kernel: no co-resident CTA");
         const int G = h->num_sms * (per_sm < 2 ? per_sm : 2);
+        if (G < 2) return fail(h, MG_ERR_UNSUPPORTED, "tridiag81_kernel needs two co-resident CTAs");
+        // MG_TRIDIAG_STAGE_CAP lowers the on-chip threshold of phase 2 (test hook for the global-memory path)
+        a.stage_cap = TD_STAGE;
+        if (const char* cap = getenv("MG_TRIDIAG_STAGE_CAP")) {
+            const int c = atoi(cap);
+            if (c >= 0 && c < TD_STAGE) a.stage_cap = c;
+        }
         void* args[] = {&a};
         cudaError_t e = cudaLaunchCooperativeKernel((const void*)tridiag81_kernel, dim3(G), dim3(TD_THREADS), args,
-                                                    0, st);
+                                                    (size_t)smem, st);
         if (e != cudaSuccess) return cuda_fail(h, e, "tridiag81_kernel launch");
         h->launches++;
     }
@@ -534,6 +842,13 @@ static mg_status_t tridiag81(mg_handle_t h, int n, double* W, int ldw, double** 
 static mg_status_t formq81(mg_handle_t h, int n, const double* U, int ldu, double* Q, int ldq) {
     cudaStream_t st = h->stream;
     ProfScope prof(h, "formq81", 4.0 / 3.0 * n * (double)n * n, 0);
+    const int fq_smem = (FQ_COLS + 2) * n * (int)sizeof(double);
+    if (n >= 3 && n <= FQ_NMAX && fq_smem <= h->max_smem_optin) {
+        MG_CHECK_CUDA(h, cudaFuncSetAttribute(formq81_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              fq_smem));
+        formq81_smem_kernel<<<(n + FQ_COLS - 1) / FQ_COLS, FQ_THREADS, fq_smem, st>>>(U, ldu, n, Q, ldq);
+        return post_launch(h, "formq81_smem_kernel");
+    }
     evd_identity_kernel<<<evd_grid(h, (size_t)n * n), 256, 0, st>>>(Q, ldq, n);
     MG_TRY(post_launch(h, "evd_identity_kernel"));
     if (n >= 3) {
@@ -607,6 +922,8 @@ mg_status_t mg_devd_q(mg_handle_t h, int n, const double* A, int lda, double eps
     const size_t base = mg::align_up(td_ws_bytes(n), 256);
     MG_TRY(mg::ensure_ws(h, base + 2 * chunk_bytes));
     MG_TRY(mg::ensure_hws(h, 2 * chunk_bytes + 256));
+    sink.err = (int*)((char*)h->ws + 64);
+    MG_CHECK_CUDA(h, cudaMemsetAsync(sink.err, 0, sizeof(int), st));
     for (int i = 0; i < 2; ++i) {
         char* dbase = (char*)h->ws + base + i * chunk_bytes;
         char* hbase = (char*)h->hws + 256 + i * chunk_bytes;
@@ -620,7 +937,11 @@ mg_status_t mg_devd_q(mg_handle_t h, int n, const double* A, int lda, double eps
     bool ok;
     {
         mg::ProfScope prof(h, "qr_sweeps81", 0, 0);
+        const auto t0 = std::chrono::steady_clock::now();
         ok = qr_sweeps(a.data(), b.data(), 0, n - 1, eps, budget, sink) && sink.flush();
+        const double host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        mg::prof_host(h, "qr_sweeps81_host", host_ms - sink.wait_ms, (double)sink.total_rot);
+        mg::prof_host(h, "qr_sweeps81_wait", sink.wait_ms, 0);
     }
     mg_status_t ret = sink.st;
     // eigenvalues into E's diagonal (EVD/__QR.h:161-168) and optionally into w
@@ -641,6 +962,7 @@ mg_status_t mg_devd_q(mg_handle_t h, int n, const double* A, int lda, double eps
     if (ret == MG_OK && se != cudaSuccess) ret = mg::cuda_fail(h, se, "cudaStreamSynchronize");
     for (int i = 0; i < 2; ++i) cudaEventDestroy(sink.done[i]);
     if (ret != MG_OK) return ret;
+    MG_TRY(mg::td_check(h, "mg_devd_q rotations"));
     if (!ok) return mg::fail(h, MG_NOT_CONVERGED, "mg_devd_q: the QR sweeps did not deflate within %d sweeps", 64 * n);
     return MG_OK;
 }

@@ -109,6 +109,24 @@ ProfScope::~ProfScope() {
     h->prof_pending.push_back({rec, a, b, flops, bytes});
 }
 
+void prof_host(mg_handle_t h, const char* name, double ms, double count) {
+    if (!h || !h->prof_on) return;
+    if (!h->prof_only.empty() && h->prof_only != name) return;
+    for (auto& r : h->prof)
+        if (r.name == name) {
+            r.ms += ms;
+            r.flops += count;
+            r.launches += 1;
+            return;
+        }
+    h->prof.push_back({});
+    auto& r = h->prof.back();
+    r.name = name;
+    r.ms = ms;
+    r.flops = count;
+    r.launches = 1;
+}
+
 static void prof_resolve(mg_handle_t h) {
     if (h->prof_pending.empty()) return;
     cudaStreamSynchronize(h->stream);

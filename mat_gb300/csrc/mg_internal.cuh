@@ -76,6 +76,10 @@ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 // Times the launches enqueued during its lifetime under `name` when the
 // handle's profiler is on (events recorded on the handle's stream); records
 // the algorithmic flops / bytes of that work for roofline reporting.
+// A host-timed phase in the profile (ms of host time; `count` is added to
+// the record's flops field, e.g. a number of items processed).
+void prof_host(mg_handle_t h, const char* name, double ms, double count);
+
 struct ProfScope {
     mg_handle_t h;
     int rec = -1;

@@ -124,3 +124,15 @@ def test_evd_q81_bad_arguments(handle):
     A = as_colmajor(torch.from_numpy(sym(8, 1)))
     with pytest.raises(MatGpuError):
         handle.devd_q(A, -1.0)
+
+
+@pytest.mark.parametrize("cap", ["0", "100"])
+def test_tridiag81_global_memory_path(handle, monkeypatch, cap):
+    """Above the on-chip capacity (n > 4097) the update reads v, w and the first
+    column from global memory; the test hook lowers the threshold so both paths
+    (all steps, or the first ones) run at a small size, bit for bit."""
+    monkeypatch.setenv("MG_TRIDIAG_STAGE_CAP", cap)
+    a = sym(300, 17)
+    q, d, e = gpu_tridiag(handle, a)
+    q0, d0, e0 = restatement().tridiag81(a)
+    assert np.array_equal(d, d0) and np.array_equal(e, e0) and np.array_equal(q, q0)
