@@ -142,7 +142,9 @@ def config_rates(h, dmma_tf: float, bf16_tf: float) -> dict:
     solve, LLT (n = 8192, seed 1) and Householder QR (16384 x 4096: R alone
     and with the full 16384 x 16384 Q); the M=N=K=16384 split-BF16 GEMM on
     u*2^e entries (seed 3) with its error against FP64 on 256 sampled rows;
-    the Gaussian-process loss + gradient (Cholesky adjoint) at n = 8192."""
+    the Gaussian-process loss + gradient (Cholesky adjoint) at n = 8192; the
+    Mat-8.1 EVD_Q (tridiagonalisation with Q, and the whole eigendecomposition)
+    at n = 1024 and 4096."""
     import ctypes as C
 
     import torch
@@ -262,6 +264,27 @@ def config_rates(h, dmma_tf: float, bf16_tf: float) -> dict:
                                    "dloss_dell": dell32, "loss_rel_diff_vs_fp64": abs(loss32 - loss) / abs(loss),
                                    "dell_rel_diff_vs_fp64": abs(dell32 - dell) / abs(dell),
                                    "note": "inputs rounded to fp32; the difference is the fp32 conditioning of K"}
+    torch.cuda.empty_cache()
+    # EVD_Q of the Mat-8.1 snapshot (EVD_QR): symmetric G + G^T, G iid N(0,1) (seed 7)
+    for ne in (1024, 4096):
+        G7 = colmajor(ne, ne)
+        h.fill_normal(G7, 7)
+        Sy = (G7 + G7.T).t().contiguous().t()
+        Wk = Sy.clone()
+
+        def tridiag():
+            Wk.copy_(Sy)
+            return h.dtridiag81(Wk)
+
+        t_td, _ = timed(tridiag)
+        t_ev, (w, _, Qe) = timed(lambda: h.devd_q(Sy, 1e-11))
+        res = (Sy @ Qe - Qe * w).abs().max().item()
+        orth = (Qe.T @ Qe - torch.eye(ne, dtype=torch.float64, device="cuda")).abs().max().item()
+        out[f"evd_q81_{ne}"] = {"tridiag_with_q_s": t_td, "evd_s": t_ev, "eps": 1e-11,
+                                "max_abs_residual_AQ_minus_QE": res, "max_abs_QtQ_minus_I": orth,
+                                "flops_model": "tridiagonalisation 4n^3/3 + Q 4n^3/3 (+ the QR sweeps)",
+                                "tridiag_with_q_gflops": 8 / 3 * ne ** 3 / t_td / 1e9}
+        del G7, Sy, Wk, w, Qe
     torch.cuda.empty_cache()
     return out
 

@@ -13,6 +13,8 @@
 //   Det(A)                              Mat-8.3.1/LU/__Det.h:30-101
 //   Inv(A)                              Mat-8.3.1/LU/__Inv.h:212-225
 //   QR(A, Q, R, QR_Householder), QR_init Mat-8.3.1/QR/QR.h:8-25, Mat.h:132-136
+//   EVD_Q(A, E, Q, eps, EVD_QR), EVD_init declared by Mat-8.3.1/Mat.h:32, 120
+//                                       (defined in Mat-8.1/EVD/EVD_Q.h:7-35)
 //
 // plus one call Mat does not have: Solve_mixed(A, B) (mixed-precision LU with
 // FP64 refinement; FP64 backward error, much faster on GB300).
@@ -33,6 +35,7 @@
 
 #ifndef XiangZiMatImport
 enum QR_type { QR_Householder, QR_Givens, QR_GramSchmidt };
+enum EVD_type { EVD_QR, EVD_Jacobi };
 #endif
 
 template <typename T>
@@ -283,6 +286,29 @@ inline void QR(MAT<double>& A, MAT<double>& Q, MAT<double>& R, QR_type type) {
     matgpu::check(mg_dqr(matgpu::handle(), m, n, dA.d(), m, dQ.d(), m, dR.d(), m), "mg_dqr");
     matgpu::d2h(Q.data, dQ.p, (size_t)m * m * 8);
     matgpu::d2h(R.data, dR.p, (size_t)m * n * 8);
+}
+
+template <typename t1, typename t2>
+void EVD_init(MAT<t1>& A, MAT<t2>& E, MAT<t2>& X) {
+    E.init(A.rows, A.rows);
+    X.init(A.rows, A.rows);
+}
+
+// EVD_Q(A, E, Q, eps, EVD_QR) of symmetric A (its lower triangle is read):
+// E = diag(eigenvalues), Q the eigenvectors (A Q = Q E), bit for bit the
+// Mat-8.1 snapshot's result (Householder tridiagonalisation, implicit QR
+// sweeps with absolute deflation threshold eps).  Mat iterates without limit;
+// here a matrix that does not deflate within 64 n sweeps throws.
+inline void EVD_Q(MAT<double>& A, MAT<double>& E, MAT<double>& Q, double eps, EVD_type type) {
+    if (type != EVD_QR) throw std::runtime_error("mat_gpu: EVD_Q supports EVD_QR only");
+    const int n = A.rows;
+    EVD_init(A, E, Q);
+    if (n == 0) return;
+    matgpu::Dev dA((size_t)n * n * 8), dE((size_t)n * n * 8), dQ((size_t)n * n * 8);
+    matgpu::h2d(dA.p, A.data, (size_t)n * n * 8);
+    matgpu::check(mg_devd_q(matgpu::handle(), n, dA.d(), n, eps, dE.d(), n, dQ.d(), n, nullptr), "mg_devd_q");
+    matgpu::d2h(E.data, dE.p, (size_t)n * n * 8);
+    matgpu::d2h(Q.data, dQ.p, (size_t)n * n * 8);
 }
 
 // X = A^{-1} B (A taken by value, as in Mat).

@@ -84,6 +84,15 @@ int main(int argc, char** argv) {
     dump("qr_Q", Q.data, (size_t)300 * 300);
     dump("qr_R", R.data, (size_t)300 * 200);
 
+    // EVD_Q(A, E, Q, eps, EVD_QR) of the symmetric W + W^T
+    MAT<double> Sy(150, 150), Ev, Qv;
+    for (int i = 0; i < 150; ++i)
+        for (int j = 0; j < 150; ++j) Sy(i, j) = W(i, j) + W(j, i);
+    EVD_init(Sy, Ev, Qv);
+    EVD_Q(Sy, Ev, Qv, 1e-10, EVD_QR);
+    dump("evd_E", Ev.data, (size_t)150 * 150);
+    dump("evd_Q", Qv.data, (size_t)150 * 150);
+
     // operator* on MAT<float>
     MAT<float> Fa(70, 50), Fb(50, 60);
     for (int i = 0; i < 70 * 50; ++i) Fa.data[i] = (float)A.data[i];

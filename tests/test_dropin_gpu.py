@@ -86,6 +86,16 @@ def test_qr_bit_identical(outputs):
     assert np.array_equal(load(outputs, "qr_R", (300, 200)), r)
 
 
+def test_evd_q_bit_identical(outputs):
+    """EVD_Q(A, E, Q, eps, EVD_QR) through the drop-in header, on W + W^T
+    (W the 200 x 200 seed-4 normal matrix, its leading 150 x 150 block)."""
+    w = host_fill_normal(200, 200, 4)[:150, :150]
+    a = np.asfortranarray(w + w.T)
+    w0, q0 = restatement().evd_q81(a, 1e-10)
+    assert np.array_equal(load(outputs, "evd_E", (150, 150)), np.diag(w0))
+    assert np.array_equal(load(outputs, "evd_Q", (150, 150)), q0)
+
+
 def test_float_operator_star(outputs):
     a = host_fill_uniform(150, 130, 0).reshape(-1, order="F")[:70 * 50].reshape(70, 50, order="F")
     b = host_fill_uniform(130, 170, 1).reshape(-1, order="F")[:50 * 60].reshape(50, 60, order="F")
