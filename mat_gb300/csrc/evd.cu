@@ -554,7 +554,7 @@ struct Sweep {
 // after every batch of ROT_PF rotations, and waits (bounded) on the others'
 // words before the batch.  Rows are read and written through L1 (the warps
 // of one CTA share an SM).
-constexpr int ROT_WARPS = 4;
+constexpr int ROT_WARPS = 8;
 constexpr int ROT_PF = 16;  // rotations per batch (the loads of a batch are in flight together)
 
 __device__ __forceinline__ bool rot_wait(volatile unsigned long long* prog, int s, int need, int* err) {
