@@ -348,8 +348,11 @@ def e2e_run(h, A, B, n, nrhs, steps, barrier, warmup=3):
         step()
     barrier()
     w0 = time.perf_counter()
+    per_step = []
     for _ in range(steps):
+        t = time.perf_counter()
         step()
+        per_step.append((time.perf_counter() - t) * 1e3)
     barrier()
     e2e_s = (time.perf_counter() - w0) / steps
     c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -358,6 +361,7 @@ def e2e_run(h, A, B, n, nrhs, steps, barrier, warmup=3):
     c1.record()
     torch.cuda.synchronize()
     out = {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+           "step_ms": [round(x, 2) for x in per_step],
            "h2d_ms": c0.elapsed_time(c1), "h2d_gbs": 8 * n * n / (c0.elapsed_time(c1) * 1e6)}
     del hA, hBt, hXt, dA, dB, dX
     return out

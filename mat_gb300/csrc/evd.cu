@@ -40,6 +40,7 @@
 //    chunks; the application is independent per row of Q (one thread per row,
 //    the carried column in a register, loads of the sweep's next columns
 //    issued ahead).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
@@ -894,21 +895,9 @@ mg_status_t mg_devd_q(mg_handle_t h, int n, const double* A, int lda, double eps
         return mg::fail(h, MG_ERR_ARG, "mg_devd_q: bad arguments");
     if (n == 0) return MG_OK;
     cudaStream_t st = h->stream;
-    MG_TRY(mg::ensure_hws(h, 64));
-    // E is the work matrix, as in Mat (EVD/EVD_Q.h:9-10)
-    if (A != E) {
-        evd_copy_lower_kernel<<<evd_grid(h, (size_t)n * n), 256, 0, st>>>(A, lda, n, E, lde);
-        MG_TRY(mg::post_launch(h, "evd_copy_lower_kernel"));
-    }
-    double *dd, *de;
-    MG_TRY(mg::tridiag81(h, n, E, lde, &dd, &de));
-    MG_TRY(mg::formq81(h, n, E, lde, Q, ldq));
-    std::vector<double> a(n), b((size_t)n + 1, 0.0);
-    MG_CHECK_CUDA(h, cudaMemcpyAsync(a.data(), dd, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
-    if (n > 1) MG_CHECK_CUDA(h, cudaMemcpyAsync(b.data(), de, (size_t)(n - 1) * 8, cudaMemcpyDeviceToHost, st));
-    MG_TRY(mg::td_check(h, "mg_devd_q"));
-    b[n - 1] = 0.0;  // EVD/__QR.h:154-157
-    // rotation chunks: two pinned staging areas and two device areas after the tridiagonalisation workspace
+    // rotation chunks: two pinned staging areas and two device areas after the
+    // tridiagonalisation workspace; the workspaces are sized first (growing
+    // them later would move the tridiagonalisation's vectors)
     GpuRotSink sink;
     sink.h = h;
     sink.Q = Q;
@@ -920,13 +909,52 @@ mg_status_t mg_devd_q(mg_handle_t h, int n, const double* A, int lda, double eps
     const size_t chunk_bytes = mg::align_up(sink.cap_rot * sizeof(double2), 256) +
                                mg::align_up(sink.cap_sw * sizeof(Sweep), 256);
     const size_t base = mg::align_up(td_ws_bytes(n), 256);
+    const size_t hv = mg::align_up((size_t)(n + 1) * 8, 256);
+    const size_t hbase0 = 256 + 2 * hv;  // pinned: status word, d, e, then the chunks
     MG_TRY(mg::ensure_ws(h, base + 2 * chunk_bytes));
-    MG_TRY(mg::ensure_hws(h, 2 * chunk_bytes + 256));
+    MG_TRY(mg::ensure_hws(h, hbase0 + 2 * chunk_bytes));
+    MG_TRY(mg::ensure_lookahead(h));
+    // E is the work matrix, as in Mat (EVD/EVD_Q.h:9-10)
+    if (A != E) {
+        evd_copy_lower_kernel<<<evd_grid(h, (size_t)n * n), 256, 0, st>>>(A, lda, n, E, lde);
+        MG_TRY(mg::post_launch(h, "evd_copy_lower_kernel"));
+    }
+    double *dd, *de;
+    MG_TRY(mg::tridiag81(h, n, E, lde, &dd, &de));
+    // d, e and the barrier status go to the host on the side stream as soon as
+    // the tridiagonalisation is done: the host recurrence then runs beside
+    // the Q formation (the rotations follow it on the handle's stream)
+    cudaEvent_t td_done;
+    MG_CHECK_CUDA(h, cudaEventCreateWithFlags(&td_done, cudaEventDisableTiming));
+    MG_CHECK_CUDA(h, cudaEventRecord(td_done, st));
+    MG_TRY(mg::formq81(h, n, E, lde, Q, ldq));
+    int* herr = (int*)h->hws;
+    double* hd = (double*)((char*)h->hws + 256);
+    double* he = (double*)((char*)h->hws + 256 + hv);
+    {
+        cudaStream_t side = h->pp_stream;
+        cudaError_t e = cudaStreamWaitEvent(side, td_done, 0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hd, dd, (size_t)n * 8, cudaMemcpyDeviceToHost, side);
+        if (e == cudaSuccess && n > 1) e = cudaMemcpyAsync(he, de, (size_t)(n - 1) * 8, cudaMemcpyDeviceToHost, side);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(herr, (char*)h->ws + 64, sizeof(int), cudaMemcpyDeviceToHost, side);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(side);
+        cudaEventDestroy(td_done);
+        if (e != cudaSuccess) return mg::cuda_fail(h, e, "mg_devd_q: tridiagonal copy");
+    }
+    if (herr[0]) {
+        cudaStreamSynchronize(st);
+        return mg::fail(h, MG_TIMEOUT, "mg_devd_q: a grid barrier timed out");
+    }
+    std::vector<double> a(hd, hd + n), b((size_t)n + 1, 0.0);
+    if (n > 1) std::copy(he, he + (n - 1), b.begin());
+    b[n - 1] = 0.0;  // EVD/__QR.h:154-157
+    // after the host read the status word: reset it for the rotation kernels
     sink.err = (int*)((char*)h->ws + 64);
     MG_CHECK_CUDA(h, cudaMemsetAsync(sink.err, 0, sizeof(int), st));
     for (int i = 0; i < 2; ++i) {
         char* dbase = (char*)h->ws + base + i * chunk_bytes;
-        char* hbase = (char*)h->hws + 256 + i * chunk_bytes;
+        char* hbase = (char*)h->hws + hbase0 + i * chunk_bytes;
         sink.dcs[i] = (double2*)dbase;
         sink.dsw[i] = (Sweep*)(dbase + mg::align_up(sink.cap_rot * sizeof(double2), 256));
         sink.hcs[i] = (double2*)hbase;
