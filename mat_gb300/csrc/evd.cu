@@ -844,7 +844,13 @@ static mg_status_t formq81(mg_handle_t h, int n, const double* U, int ldu, doubl
     cudaStream_t st = h->stream;
     ProfScope prof(h, "formq81", 4.0 / 3.0 * n * (double)n * n, 0);
     const int fq_smem = (FQ_COLS + 2) * n * (int)sizeof(double);
-    if (n >= 3 && n <= FQ_NMAX && fq_smem <= h->max_smem_optin) {
+    // MG_FORMQ_NMAX lowers the order up to which Q is formed on chip (test hook for the global-memory kernel)
+    int nmax = FQ_NMAX;
+    if (const char* v = getenv("MG_FORMQ_NMAX")) {
+        const int c = atoi(v);
+        if (c >= 0 && c < FQ_NMAX) nmax = c;
+    }
+    if (n >= 3 && n <= nmax && fq_smem <= h->max_smem_optin) {
         MG_CHECK_CUDA(h, cudaFuncSetAttribute(formq81_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               fq_smem));
         formq81_smem_kernel<<<(n + FQ_COLS - 1) / FQ_COLS, FQ_THREADS, fq_smem, st>>>(U, ldu, n, Q, ldq);

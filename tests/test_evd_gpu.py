@@ -136,3 +136,29 @@ def test_tridiag81_global_memory_path(handle, monkeypatch, cap):
     q, d, e = gpu_tridiag(handle, a)
     q0, d0, e0 = restatement().tridiag81(a)
     assert np.array_equal(d, d0) and np.array_equal(e, e0) and np.array_equal(q, q0)
+
+
+def test_formq81_global_memory_kernel(handle, monkeypatch):
+    """Q from the reflectors with the global-memory kernel (used above n = 4096),
+    forced at a small size by the test hook, bit for bit."""
+    monkeypatch.setenv("MG_FORMQ_NMAX", "0")
+    a = sym(300, 19)
+    q, d, e = gpu_tridiag(handle, a)
+    q0, d0, e0 = restatement().tridiag81(a)
+    assert np.array_equal(d, d0) and np.array_equal(e, e0) and np.array_equal(q, q0)
+
+
+def test_tridiag81_large_properties(handle):
+    """n = 4200: the first steps exceed the on-chip capacity (global-memory
+    update) and Q is formed by the global-memory kernel; Q orthogonal and
+    Q^T A Q tridiagonal with the returned d, e."""
+    n = 4200
+    a = sym(n, 23)
+    At = torch.from_numpy(a).cuda()
+    A = At.t().contiguous().t().clone()
+    Q, d, e = handle.dtridiag81(A)
+    torch.cuda.synchronize()
+    T = torch.diag(d) + torch.diag(e, 1) + torch.diag(e, -1)
+    nrm = At.abs().max().item()
+    assert (Q.T @ Q - torch.eye(n, dtype=torch.float64, device="cuda")).abs().max().item() < 1e-12
+    assert (Q.T @ At @ Q - T).abs().max().item() < 1e-11 * nrm * 10
