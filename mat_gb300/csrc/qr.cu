@@ -526,10 +526,22 @@ static mg_status_t dgeqrf_blocked(mg_handle_t h, int m, int n, double* R, int ld
             double* R2 = R + j + (size_t)(j + b) * ldr;
             qr_expand_v_kernel<<<grid_cap(h, (size_t)hh * b), 256, 0, st>>>(P, ldr, hh, b, w.V);
             MG_TRY(post_launch(h, "qr_expand_v_kernel"));
-            // W = V^T R2; W2 = T^T W; R2 -= V W2
-            MG_TRY(dgemm_launch(h, 1, 0, b, nc, hh, 1.0, w.V, hh, R2, ldr, 0.0, w.W, b, 0));
-            MG_TRY(dgemm_launch(h, 1, 0, b, nc, b, 1.0, Tj, b, w.W, b, 0.0, w.W2, b, 0));
-            MG_TRY(dgemm_launch(h, 0, 0, hh, nc, b, -1.0, w.V, hh, w.W2, b, 1.0, R2, ldr, 0));
+            // W = V^T R2; W2 = T^T W; R2 -= V W2.  The first product (48 outputs per
+            // column, K = hh) is bound by the length of its fused K chains, not by
+            // its width: a look-ahead that updates the next panel's columns first
+            // put a second chain on the critical path and was slower.
+            {
+                ProfScope p1(h, "qr_vtr", 2.0 * b * (double)nc * hh, 0);
+                MG_TRY(dgemm_launch(h, 1, 0, b, nc, hh, 1.0, w.V, hh, R2, ldr, 0.0, w.W, b, 0));
+            }
+            {
+                ProfScope p2(h, "qr_tw", 2.0 * b * (double)nc * b, 0);
+                MG_TRY(dgemm_launch(h, 1, 0, b, nc, b, 1.0, Tj, b, w.W, b, 0.0, w.W2, b, 0));
+            }
+            {
+                ProfScope p3(h, "qr_vw", 2.0 * hh * (double)nc * b, 0);
+                MG_TRY(dgemm_launch(h, 0, 0, hh, nc, b, -1.0, w.V, hh, w.W2, b, 1.0, R2, ldr, 0));
+            }
         }
     }
     return MG_OK;
