@@ -47,11 +47,17 @@ struct TileCfg {
 using Big = TileCfg<2, 4, 4, 4>;    // 128 x 128, 8 warps
 using Small = TileCfg<1, 1, 2, 4>;  // 32 x 32, 1 warp
 using Thin = TileCfg<1, 1, 3, 2>;   // 48 x 16, 1 warp: M = 48 block-reflector products (QR, adjoint)
-// 16 x 16, 1 warp: products with few outputs and a long K (the QR's V^T R2
-// late in the factorization); one SM's FP64 pipe takes a DMMA only every
-// ~290 cycles, so two accumulator chains keep it busy and the small tile
-// spreads the outputs over more SMs.
+// 16 x 16, 1 warp: products with few outputs and a moderate K; the small
+// tile spreads the outputs over more SMs.  (An SM takes a DMMA about every
+// 270 cycles, but through four sub-partition pipes of about 1,100 cycles each:
+// a lone warp per SM keeps only one of them issuing.)
 using Tiny = TileCfg<1, 1, 1, 2>;
+// 16 x 32, 4 warps of one 16x8 accumulator each: products with few rows and
+// a long K (W = V^T R2 of the QR, M = 48, K = the panel height).  Each
+// accumulator is one fused K chain; spreading the chains over four warps per
+// CTA keeps every sub-partition's FP64 pipe issuing, where the 1-warp tiles
+// left two or three of an SM's four idle.
+using Quad = TileCfg<1, 4, 1, 1>;
 
 __device__ __forceinline__ void cp_async8(double* smem, const double* gmem, bool pred) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -313,7 +319,9 @@ mg_status_t dgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, in
         const double an = busiest_sm_area(tn, h->num_sms, Tiny::BM, Tiny::BN);
         // the 16 x 16 tile reloads more operand bytes per flop: only when it
         // shortens the busiest SM's work clearly
-        if (an < 0.75 * std::min(at, std::min(ab, as)))
+        if (m <= 64 && k >= 2048)
+            e = dispatch<Quad>(st, transA, transB, mode, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+        else if (an < 0.75 * std::min(at, std::min(ab, as)))
             e = dispatch<Tiny>(st, transA, transB, mode, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
         else if (at < ab && at < as)
             e = dispatch<Thin>(st, transA, transB, mode, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
