@@ -23,6 +23,7 @@ Multi-GPU: replicas only (independent solves, no collective on the path).
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -347,6 +348,8 @@ def e2e_run(h, A, B, n, nrhs, steps, barrier, warmup=3):
     for _ in range(max(1, warmup)):
         step()
     barrier()
+    gc.collect()
+    gc.disable()  # no collector pass inside the timed steps
     w0 = time.perf_counter()
     per_step = []
     for _ in range(steps):
@@ -355,6 +358,7 @@ def e2e_run(h, A, B, n, nrhs, steps, barrier, warmup=3):
         per_step.append((time.perf_counter() - t) * 1e3)
     barrier()
     e2e_s = (time.perf_counter() - w0) / steps
+    gc.enable()
     c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     c0.record()
     h.check(lib.mg_memcpy(hh, C.c_void_p(dA.data_ptr()), C.c_void_p(hA.data_ptr()), 8 * n * n, 0))
@@ -409,6 +413,8 @@ def run_ours(args):
               for k, v in sorted(prof_all.items(), key=lambda kv: -kv[1]["ms"])}
 
     # the timed region, without any per-phase events (they would perturb it)
+    gc.collect()
+    gc.disable()  # no collector pass inside the timed region
     sampler = ClockSampler(local)
     sampler.start()
     launches0 = h.launch_count()
@@ -424,6 +430,7 @@ def run_ours(args):
     barrier()
     launches = h.launch_count() - launches0
     clocks = sampler.stop()
+    gc.enable()
     ms = e0.elapsed_time(e1) / args.steps
     t = torch.tensor([ms], device="cuda", dtype=torch.float64)
     if world > 1:
