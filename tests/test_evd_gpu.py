@@ -162,3 +162,15 @@ def test_tridiag81_large_properties(handle):
     nrm = At.abs().max().item()
     assert (Q.T @ Q - torch.eye(n, dtype=torch.float64, device="cuda")).abs().max().item() < 1e-12
     assert (Q.T @ At @ Q - T).abs().max().item() < 1e-11 * nrm * 10
+
+
+def test_evd_q81_in_place(handle):
+    """A == E (Mat allows EVD_Q(A, A, Q, ...)): the same result, E overwritten."""
+    a = sym(97, 29)
+    A = as_colmajor(torch.from_numpy(a))
+    w, E, Q = handle.devd_q(A, EPS, E=A)
+    torch.cuda.synchronize()
+    w0, Q0 = restatement().evd_q81(a, EPS)
+    assert E.data_ptr() == A.data_ptr()
+    assert np.array_equal(w.cpu().numpy(), w0) and np.array_equal(Q.cpu().numpy(), Q0)
+    assert np.array_equal(A.cpu().numpy(), np.diag(w0))
