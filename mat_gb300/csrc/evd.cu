@@ -783,6 +783,18 @@ struct GpuRotSink final : RotSink {
         hcs[cur][nrot++] = make_double2(c, s);
         ++total_rot;
     }
+    ~GpuRotSink() override {
+        for (cudaEvent_t& e : done)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
+// An event destroyed on every return path.
+struct ScopedEvent {
+    cudaEvent_t e = nullptr;
+    ~ScopedEvent() {
+        if (e) cudaEventDestroy(e);
+    }
 };
 
 // Device workspace of the tridiagonalisation: barrier + error word, d, e, vc, vd.
@@ -930,22 +942,21 @@ mg_status_t mg_devd_q(mg_handle_t h, int n, const double* A, int lda, double eps
     // d, e and the barrier status go to the host on the side stream as soon as
     // the tridiagonalisation is done: the host recurrence then runs beside
     // the Q formation (the rotations follow it on the handle's stream)
-    cudaEvent_t td_done;
-    MG_CHECK_CUDA(h, cudaEventCreateWithFlags(&td_done, cudaEventDisableTiming));
-    MG_CHECK_CUDA(h, cudaEventRecord(td_done, st));
+    ScopedEvent td_done;
+    MG_CHECK_CUDA(h, cudaEventCreateWithFlags(&td_done.e, cudaEventDisableTiming));
+    MG_CHECK_CUDA(h, cudaEventRecord(td_done.e, st));
     MG_TRY(mg::formq81(h, n, E, lde, Q, ldq));
     int* herr = (int*)h->hws;
     double* hd = (double*)((char*)h->hws + 256);
     double* he = (double*)((char*)h->hws + 256 + hv);
     {
         cudaStream_t side = h->pp_stream;
-        cudaError_t e = cudaStreamWaitEvent(side, td_done, 0);
+        cudaError_t e = cudaStreamWaitEvent(side, td_done.e, 0);
         if (e == cudaSuccess) e = cudaMemcpyAsync(hd, dd, (size_t)n * 8, cudaMemcpyDeviceToHost, side);
         if (e == cudaSuccess && n > 1) e = cudaMemcpyAsync(he, de, (size_t)(n - 1) * 8, cudaMemcpyDeviceToHost, side);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(herr, (char*)h->ws + 64, sizeof(int), cudaMemcpyDeviceToHost, side);
         if (e == cudaSuccess) e = cudaStreamSynchronize(side);
-        cudaEventDestroy(td_done);
         if (e != cudaSuccess) return mg::cuda_fail(h, e, "mg_devd_q: tridiagonal copy");
     }
     if (herr[0]) {
@@ -994,7 +1005,6 @@ mg_status_t mg_devd_q(mg_handle_t h, int n, const double* A, int lda, double eps
     }
     cudaError_t se = cudaStreamSynchronize(st);
     if (ret == MG_OK && se != cudaSuccess) ret = mg::cuda_fail(h, se, "cudaStreamSynchronize");
-    for (int i = 0; i < 2; ++i) cudaEventDestroy(sink.done[i]);
     if (ret != MG_OK) return ret;
     MG_TRY(mg::td_check(h, "mg_devd_q rotations"));
     if (!ok) return mg::fail(h, MG_NOT_CONVERGED, "mg_devd_q: the QR sweeps did not deflate within %d sweeps", 64 * n);
