@@ -204,6 +204,14 @@ mg_status_t mg_dtridiag81(mg_handle_t h, int n, double* A, int lda, double* Q, i
 mg_status_t mg_devd_q(mg_handle_t h, int n, const double* A, int lda, double eps, double* E, int lde, double* Q,
                       int ldq, double* w);
 
+/* mg_dsteqr81_host: the host half of mg_devd_q on its own, eigenvalues only:
+ * Mat-8.1's implicit QR sweeps (EVD/__QR.h:50-142) on the tridiagonal with
+ * diagonal d (host, n; overwritten with the eigenvalues, in Mat's order) and
+ * off-diagonal e (host, n - 1), absolute deflation threshold eps.  rotations
+ * (may be NULL) receives the number of plane rotations.  No GPU work, no
+ * handle.  MG_NOT_CONVERGED after 64 n sweeps. */
+mg_status_t mg_dsteqr81_host(int n, double* d, const double* e, double eps, long long* rotations);
+
 /* ------------------------------------------------- split-precision GEMM
  * C = alpha * A * B + beta * C for fp32 column-major operands on the
  * tcgen05 BF16 tensor cores: A and B are split into `nterms` bf16 terms

@@ -15,6 +15,7 @@ MG_STATUS = {
     0: "MG_OK", 1: "MG_ERR_ARG", 2: "MG_ERR_CUDA", 3: "MG_ERR_ALLOC", 4: "MG_SINGULAR",
     5: "MG_NOT_SPD", 6: "MG_IR_STALLED", 7: "MG_FALLBACK_USED", 8: "MG_TIMEOUT",
     9: "MG_ERR_UNSUPPORTED",
+    10: "MG_NOT_CONVERGED",
 }
 
 vp = C.c_void_p
@@ -65,6 +66,7 @@ SIGNATURES: dict[str, tuple] = {
     "mg_dlu": (i32, [vp, i32, vp, i32, pi32]),
     "mg_dtridiag81": (i32, [vp, i32, vp, i32, vp, i32, vp, vp]),
     "mg_devd_q": (i32, [vp, i32, vp, i32, f64, vp, i32, vp, i32, vp]),
+    "mg_dsteqr81_host": (i32, [i32, vp, vp, f64, C.POINTER(C.c_longlong)]),
     "mg_sgetrf": (i32, [vp, i32, vp, i32, vp, pi32]),
     "mg_dgetrs": (i32, [vp, i32, i32, vp, i32, vp, vp, i32, vp, i32]),
     "mg_dgesv": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, pi32]),

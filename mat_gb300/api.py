@@ -411,6 +411,19 @@ def host_fill_uniform(rows: int, cols: int, seed: int, lo=-1.0, hi=1.0, rowmajor
     return a
 
 
+def host_steqr81(d, e, eps: float):
+    """Mat-8.1 EVD_Q's QR sweeps on the host (no GPU): eigenvalues of the
+    tridiagonal (d, e) in Mat's order, and the number of plane rotations."""
+    import numpy as np
+    d = np.array(d, dtype=np.float64)
+    e = np.ascontiguousarray(e, dtype=np.float64)
+    rot = C.c_longlong(0)
+    st = load().mg_dsteqr81_host(len(d), d.ctypes.data, e.ctypes.data if len(e) else None, float(eps), C.byref(rot))
+    if st != 0:
+        raise MatGpuError(st, "mg_dsteqr81_host")
+    return d, rot.value
+
+
 def host_fill_normal(rows: int, cols: int, seed: int, rowmajor_stream=True):
     """Seeded N(0,1) matrix on the host (numpy, column-major), bit-identical to fill_normal."""
     import numpy as np

@@ -722,6 +722,13 @@ bool qr_sweeps(double* a, double* b, int m, int n, double eps, long long& budget
     return true;
 }
 
+// Counts the rotations (the eigenvalue-only host entry point).
+struct CountSink final : RotSink {
+    long long count = 0;
+    bool sweep(int, int) override { return true; }
+    void rot(double, double) override { ++count; }
+};
+
 // Streams the rotations to the GPU in chunks: two pinned staging areas and
 // two device areas used in turn; a chunk is launched when the next sweep does
 // not fit, while the host goes on with the recurrence.
@@ -1009,6 +1016,21 @@ mg_status_t mg_devd_q(mg_handle_t h, int n, const double* A, int lda, double eps
     MG_TRY(mg::td_check(h, "mg_devd_q rotations"));
     if (!ok) return mg::fail(h, MG_NOT_CONVERGED, "mg_devd_q: the QR sweeps did not deflate within %d sweeps", 64 * n);
     return MG_OK;
+}
+
+// Host only: the QR sweeps of EVD_Q on a tridiagonal (EVD/__QR.h:50-142),
+// eigenvalues only.  No CUDA call.
+mg_status_t mg_dsteqr81_host(int n, double* d, const double* e, double eps, long long* rotations) {
+    if (n < 0 || (n > 0 && !d) || (n > 1 && !e) || !(eps >= 0.0)) return MG_ERR_ARG;
+    if (rotations) *rotations = 0;
+    if (n == 0) return MG_OK;
+    std::vector<double> b((size_t)n + 1, 0.0);
+    if (n > 1) std::copy(e, e + (n - 1), b.begin());
+    CountSink sink;
+    long long budget = 64LL * n;
+    const bool ok = qr_sweeps(d, b.data(), 0, n - 1, eps, budget, sink);
+    if (rotations) *rotations = sink.count;
+    return ok ? MG_OK : MG_NOT_CONVERGED;
 }
 
 }  // extern "C"

@@ -255,6 +255,7 @@ const char* mg_status_string(mg_status_t s) {
         case MG_FALLBACK_USED: return "MG_FALLBACK_USED";
         case MG_TIMEOUT: return "MG_TIMEOUT";
         case MG_ERR_UNSUPPORTED: return "MG_ERR_UNSUPPORTED";
+        case MG_NOT_CONVERGED: return "MG_NOT_CONVERGED";
     }
     return "MG_UNKNOWN";
 }
