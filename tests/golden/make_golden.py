@@ -142,7 +142,7 @@ def main():
     q, d, e = ref81.tridiag81(sym(37, 21))
     w, qe = ref81.evd_q81(sym(37, 21), EVD_EPS)
     np.savez_compressed(OUT / "evd81_37.npz", Q=q, d=d, e=e, w=w, Qe=qe)
-    for n in (64, 200, 500):
+    for n in (64, 200, 500, 1000):
         q, d, e = ref81.tridiag81(sym(n, 21))
         w, qe = ref81.evd_q81(sym(n, 21), EVD_EPS)
         meta["cases"][f"tridiag81_{n}"] = {"sha256_Q": sha(q), "sha256_d": sha(d[:, None]),

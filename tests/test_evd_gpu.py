@@ -57,7 +57,7 @@ def test_tridiag81_golden(handle):
     f = np.load(G / "evd81_37.npz")
     q, d, e = gpu_tridiag(handle, sym(37, 21))
     assert np.array_equal(q, f["Q"]) and np.array_equal(d, f["d"]) and np.array_equal(e, f["e"])
-    for n in (64, 200, 500):
+    for n in (64, 200, 500, 1000):
         q, d, e = gpu_tridiag(handle, sym(n, 21))
         c = META[f"tridiag81_{n}"]
         assert (sha(q), sha(d[:, None]), sha(e[:, None])) == (c["sha256_Q"], c["sha256_d"], c["sha256_e"])
@@ -72,7 +72,7 @@ def test_tridiag81_reads_lower_triangle_only(handle):
     assert np.array_equal(d, d0) and np.array_equal(e, e0) and np.array_equal(q, q0)
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 7, 37, 64, 200, 500])
+@pytest.mark.parametrize("n", [1, 2, 3, 7, 37, 64, 200, 500, 1000])
 def test_evd_q81_bit_identical(handle, n):
     a = sym(n, 21)
     w, E, Q = gpu_evd(handle, a, EPS)

@@ -154,13 +154,13 @@ def sym(n, seed):
 
 def test_tridiag81_and_evd_q81(orc):
     """The Mat-8.1 tridiagonalisation and EVD_Q (EVD_QR) bit for bit: n = 37 in
-    full, n = 64, 200, 500 by digest."""
+    full, n = 64, 200, 500, 1000 by digest."""
     f = np.load(G / "evd81_37.npz")
     q, d, e = orc.tridiag81(sym(37, 21))
     assert np.array_equal(q, f["Q"]) and np.array_equal(d, f["d"]) and np.array_equal(e, f["e"])
     w, qe = orc.evd_q81(sym(37, 21), EVD_EPS)
     assert np.array_equal(w, f["w"]) and np.array_equal(qe, f["Qe"])
-    for n in (64, 200, 500):
+    for n in (64, 200, 500, 1000):
         q, d, e = orc.tridiag81(sym(n, 21))
         c = META[f"tridiag81_{n}"]
         assert (sha(q), sha(d[:, None]), sha(e[:, None])) == (c["sha256_Q"], c["sha256_d"], c["sha256_e"])
