@@ -14,10 +14,13 @@ end-to-end leg through the C ABI with host buffers, the roofline of the
 dominant kernel (timed live with CUDA events on the library's stream), the
 oracle restatement timed on the host cores, and sampled GPU clocks.
 
---impl reference: times the CPU implementation of the reference (the
-oracle restatement of Mat's Solve_direct; the reference itself is x86
-AVX-512 header code that is not present on the GPU host) on all host cores,
-on a bounded sample (n = 4096) scaled to n = 16384 by n^3.
+--impl reference: times the CPU implementation of the reference on the same
+system (the oracle restatement of Mat's Solve_direct, bit-identical to Mat's
+own results; the reference itself is x86 AVX-512 header code absent from the
+GPU host) on all host cores: each step one whole n = 16384, 4-RHS solve of
+the same A and B, regenerated on the host by the oracle from the same seeded
+streams (bit-identical to the GPU generator).  It loads no part of this
+library.  Warm-up steps solve an n = 2048 system of the same recipe.
 Multi-GPU: replicas only (independent solves, no collective on the path).
 """
 from __future__ import annotations
@@ -37,9 +40,19 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "n=16384 LU-solve time at FP64 backward error, mixed+IR vs FP64; DGEMM TFLOP/s"
-WORKLOAD = ("mixed LU (fp32 panels + split-BF16x3 tcgen05 trailing updates) + FP64 iterative refinement, "
-            "n=16384, 4 RHS, A=Q1*diag(sigma)*Q2 with 64 Householder reflectors per side, "
-            "sigma geometric 1..1e-6 (cond 1e6), b iid N(0,1), target backward error 1e-14")
+WORKLOAD = ("LU solve of A X = B to FP64 normwise backward error <= 1e-14, n=16384, 4 RHS, "
+            "A=Q1*diag(sigma)*Q2 with 64 Householder reflectors per side (seed 3), "
+            "sigma geometric 1..1e-6 (cond 1e6), B iid N(0,1) (seed 11)")
+METHOD = ("mixed LU (fp32 panels + split-BF16x3 tcgen05 trailing updates) + FP64 iterative refinement "
+          "on one GB300")
+REF_METHOD = ("Mat Solve_direct (narrow path: blocked PLU, BS=60, then scalar substitutions) in FP64, the "
+              "oracle restatement (bit-identical to Mat-8.3.1), all host threads")
+
+
+def bench_config(n: int, nrhs: int, world: int) -> dict:
+    """The workload both arms run (identical dicts: the same system, seeds and target)."""
+    return {"workload": WORKLOAD, "n": n, "nrhs": nrhs, "seed_A": 3, "seed_B": 11,
+            "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (A is 2 GiB), no flush"}
 
 
 def parse():
@@ -123,18 +136,31 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_solve_sample(n_sample: int, nrhs: int, seed: int = 1):
-    """Times the oracle restatement of Mat's Solve_direct (narrow path) on all host cores."""
-    from mat_gb300.api import host_fill_normal
+def host_system(n: int, nrhs: int, seed_a: int = 3, seed_b: int = 11):
+    """The benchmark system regenerated on the host by the oracle (same seeded
+    streams and operation order as the GPU generator: bit-identical)."""
+    from oracle.api import gen_svd_matrix, host_fill_normal
+    return gen_svd_matrix(n, seed_a, 64, 1e-6), host_fill_normal(n, nrhs, seed_b)
+
+
+def cpu_solve(A, B):
+    """One FP64 Solve_direct of the oracle restatement on all host cores: (seconds, cores, X)."""
     from oracle.api import restatement
     o = restatement()
     cores = os.cpu_count() or 1
     o.set_threads(cores)
-    a = host_fill_normal(n_sample, n_sample, seed)
-    b = host_fill_normal(n_sample, nrhs, seed + 10)
     t = time.perf_counter()
-    o.solve(a, b)
-    return time.perf_counter() - t, cores
+    X = o.solve(A, B)
+    return time.perf_counter() - t, cores, X
+
+
+def backward_error(A, X, B) -> float:
+    """max over columns of ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf)."""
+    import numpy as np
+    R = B - A @ X
+    an = float(np.abs(A).sum(axis=1).max())
+    return float(max(np.abs(R[:, j]).max() / (an * np.abs(X[:, j]).max() + np.abs(B[:, j]).max())
+                     for j in range(B.shape[1])))
 
 
 def config_rates(h, dmma_tf: float, bf16_tf: float) -> dict:
@@ -294,24 +320,29 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    n_sample = 4096
-    scale = (args.n / n_sample) ** 3
+    n, nrhs = args.n, args.nrhs
     for _ in range(args.warmup):
-        cpu_solve_sample(2048, args.nrhs)
+        Aw, Bw = host_system(2048, nrhs)
+        cpu_solve(Aw, Bw)
+    t0 = time.perf_counter()
+    A, B = host_system(n, nrhs)
+    gen_s = time.perf_counter() - t0
     ts = []
     cores = 1
+    X = None
     for _ in range(args.steps):
-        t, cores = cpu_solve_sample(n_sample, args.nrhs)
-        ts.append(t * scale)
+        t, cores, X = cpu_solve(A, B)
+        ts.append(t)
     v = statistics.mean(ts)
-    sample = (f"oracle restatement of Mat Solve_direct (PLU BS=60 + narrow substitution), n={n_sample}, "
-              f"{args.nrhs} RHS, {cores} threads, time scaled by (16384/{n_sample})^3")
+    sample = (f"one whole Solve_direct per step (A copied, PLU, substitutions) on the benchmark system, "
+              f"n={n}, {nrhs} RHS, {cores} threads; warm-up steps at n=2048")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "FP64 LU solve (Mat Solve_direct), n=16384, 4 RHS, iid N(0,1)",
-                   "n": args.n, "nrhs": args.nrhs},
+        "config": bench_config(n, nrhs, world), "method": REF_METHOD,
+        "backward_error": backward_error(A, X, B), "step_s": [round(x, 3) for x in ts],
+        "input_generation_s": gen_s,
         "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -506,13 +537,23 @@ def run_ours(args):
                 "launches": dom["launches"], "ms_total": dom["ms"], "ms_per_step_with_events": ms_profiled}
 
 
+    # the CPU baseline on the same system: the oracle's host copy of A and B
+    # (checked equal to the GPU's bit for bit), one whole FP64 Solve_direct on
+    # all host cores, whose solution is also compared with the FP64 GPU solve
     cpu = None
     if rank == 0 and not args.no_cpu:
-        n_sample = 4096
-        t_cpu, cores = cpu_solve_sample(n_sample, nrhs)
-        cpu = {"value": t_cpu * (n / n_sample) ** 3, "unit": "s", "cores": cores, "kind": "port",
-               "sample": f"oracle restatement of Mat Solve_direct, n={n_sample}, {nrhs} RHS, {cores} threads, "
-                         f"scaled by (n/{n_sample})^3"}
+        import numpy as np
+        hA, hB = host_system(n, nrhs, 3 + rank, 11 + rank)
+        same_A = bool(torch.equal(torch.from_numpy(hA).to("cuda"), A))
+        same_B = bool(torch.equal(torch.from_numpy(hB).to("cuda"), B))
+        t_cpu, cores, Xc = cpu_solve(hA, hB)
+        cpu = {"value": t_cpu, "unit": "s", "cores": cores, "kind": "port",
+               "sample": f"one whole oracle Solve_direct (Mat's FP64 narrow path) of the benchmark system, n={n}, "
+                         f"{nrhs} RHS, {cores} threads",
+               "input_equals_gpu_input": same_A and same_B,
+               "fp64_gpu_solve_equals_oracle": bool(np.array_equal(Xd.cpu().numpy(), Xc)),
+               "backward_error": backward_error(hA, Xc, hB)}
+        del hA, hB, Xc
 
     configs = None
     if rank == 0 and not args.no_configs:
@@ -524,8 +565,7 @@ def run_ours(args):
             "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32/bf16x3 factor + f64 refinement", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n": n, "nrhs": nrhs, "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (A is 2 GiB), no flush"},
+            "config": bench_config(n, nrhs, world), "method": METHOD,
             "fp64_solve_s": fp64_s, "mixed_vs_fp64": (ms / 1e3) / fp64_s,
             "backward_error": last["backward_error"], "iterations": last["iterations"], "path": last["path"],
             "forward_error_vs_fp64_solve": fwd, "pivot_growth": last.get("pivot_growth"),

@@ -1,6 +1,7 @@
 // Seeded benchmark-input generators built from the library's own kernels.
 //
-// mg_gen_svd_matrix: A = Q1 diag(sigma) Q2, each Q a product of `nrefl`
+// mg_gen_svd_matrix: A = Q1 diag(sigma) Q2 (sigma_r = sigma_min^(r/(n-1)),
+// mgrng::geometric_at), each Q a product of `nrefl`
 // Householder reflectors H = I - tau v v^T (tau = 2 / v^T v, v iid N(0,1)),
 // applied in compact WY form Q = I - V T V^T (T upper triangular, the
 // forward recurrence of the block reflector) with three FP64 GEMMs per side.
@@ -9,6 +10,7 @@
 #include <vector>
 
 #include "mg_internal.cuh"
+#include "rng.cuh"
 
 namespace {
 
@@ -16,9 +18,7 @@ __global__ void diag_fill_kernel(double* A, int lda, int n, double sigma_min) {
     const size_t total = (size_t)n * n;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const size_t r = e % n, c = e / n;
-        double v = 0.0;
-        if (r == c) v = n > 1 ? pow(sigma_min, (double)r / (double)(n - 1)) : 1.0;
-        A[r + c * lda] = v;
+        A[r + c * lda] = r == c ? mgrng::geometric_at((int)r, n, sigma_min) : 0.0;
     }
 }
 
@@ -45,7 +45,8 @@ void build_T(int k, const std::vector<double>& G, std::vector<double>& T) {
 
 extern "C" mg_status_t mg_gen_svd_matrix(mg_handle_t h, int n, double* A, int lda, uint64_t seed, int nrefl,
                                          double sigma_min) {
-    if (!h || n < 0 || lda < (n > 1 ? n : 1) || nrefl < 0 || (n && !A)) return MG_ERR_ARG;
+    if (!h || n < 0 || lda < (n > 1 ? n : 1) || nrefl < 0 || (n && !A) || !(sigma_min > 0.0 && sigma_min <= 1.0))
+        return MG_ERR_ARG;
     if (n == 0) return MG_OK;
     const int k = nrefl;
     // workspace: V1, V2 (n x k), W, W2 (k x n), G, T (k x k)

@@ -89,6 +89,31 @@ MG_HD double log_series(double x) {
     return radd(rmul(de, ln2_hi), radd(lnm, rmul(de, ln2_lo)));
 }
 
+// e^x for x <= 0 of moderate size: x = k ln 2 + f with k the integer nearest
+// x / ln 2 (|f| <= ln 2 / 2), e^f by its Taylor series to degree 17 (the
+// dropped terms are below 1e-21 relative), then the exact scaling by 2^k.
+MG_HD double exp_series(double x) {
+    const double kd = floor(radd(rmul(x, 1.44269504088896340736), 0.5));
+    const double ln2_hi = 6.93147180369123816490e-01;  // 32 significant bits: kd * ln2_hi is exact
+    const double ln2_lo = 1.90821492927058770002e-10;
+    const double f = radd(radd(x, -rmul(kd, ln2_hi)), -rmul(kd, ln2_lo));
+    double p = rdiv(1.0, 355687428096000.0);  // 1/17!
+    double fact = 355687428096000.0;
+    for (int i = 17; i >= 1; --i) {
+        fact = rdiv(fact, (double)i);  // (i-1)! exactly
+        p = radd(rmul(p, f), rdiv(1.0, fact));
+    }
+    return ldexp(p, (int)kd);
+}
+
+// sigma_r = sigma_min^(r / (n-1)), r = 0..n-1, sigma_min in (0, 1]: the
+// geometric singular values of the Q1 diag(sigma) Q2 test matrices, from
+// the series above so that the host and the device agree bit for bit.
+MG_HD double geometric_at(int r, int n, double sigma_min) {
+    if (n <= 1) return 1.0;
+    return exp_series(rmul(rdiv((double)r, (double)(n - 1)), log_series(sigma_min)));
+}
+
 MG_HD uint64_t stream_key(uint64_t seed, uint64_t salt) { return mix64(seed * 0xD1B54A32D192ED03ull + salt); }
 
 MG_HD double uniform_at(uint64_t key, uint64_t idx, double lo, double hi) {

@@ -34,6 +34,13 @@ class Oracle:
             for n in ("orc_dgetrf", "orc_plu", "orc_solve", "orc_llt", "orc_inv", "orc_ldlt", "orc_lu",
                       "orc_evd_q81"):
                 getattr(self.lib, n).restype = C.c_int
+            self.lib.orc_host_fill_uniform.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_double,
+                                                       C.c_double, C.c_int]
+            self.lib.orc_host_fill_uniform.restype = None
+            self.lib.orc_host_fill_normal.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_int]
+            self.lib.orc_host_fill_normal.restype = None
+            self.lib.orc_gen_svd_matrix.argtypes = [C.c_int, _P, C.c_int, C.c_uint64, C.c_int, C.c_double]
+            self.lib.orc_gen_svd_matrix.restype = C.c_int
         elif prefix == "ref_":
             self.lib.ref_det.restype = C.c_double
 
@@ -165,3 +172,29 @@ def reference81() -> Oracle | None:
 
 def dgemm(A, B):
     return restatement().dgemm(A, B)
+
+
+# The library's seeded inputs regenerated by the oracle (same streams, same
+# bits as mg_host_fill_* and the GPU generators).
+
+def host_fill_uniform(rows: int, cols: int, seed: int, lo=-1.0, hi=1.0, rowmajor_stream=True) -> np.ndarray:
+    a = np.empty((rows, cols), order="F")
+    if rows and cols:
+        restatement().lib.orc_host_fill_uniform(_p(a), rows, cols, max(rows, 1), seed, lo, hi,
+                                                int(rowmajor_stream))
+    return a
+
+
+def host_fill_normal(rows: int, cols: int, seed: int, rowmajor_stream=True) -> np.ndarray:
+    a = np.empty((rows, cols), order="F")
+    if rows and cols:
+        restatement().lib.orc_host_fill_normal(_p(a), rows, cols, max(rows, 1), seed, int(rowmajor_stream))
+    return a
+
+
+def gen_svd_matrix(n: int, seed: int, nrefl: int = 64, sigma_min: float = 1e-6) -> np.ndarray:
+    """A = Q1 diag(sigma) Q2 as the library's mg_gen_svd_matrix makes it (bit for bit)."""
+    a = np.empty((n, n), order="F")
+    if restatement().lib.orc_gen_svd_matrix(n, _p(a), max(n, 1), seed, nrefl, sigma_min) != 0:
+        raise ValueError("gen_svd_matrix: invalid arguments")
+    return a

@@ -21,9 +21,14 @@ HERE = Path(__file__).resolve().parent
 ORACLE_LIB = HERE / "liboracle.so"
 REF_DIR = HERE / "_ref"
 REF_LIB = REF_DIR / "libmatref.so"
-REFERENCE_ROOT = Path("/root/reference/Mat-8.3.1")
+# The reference tree (read only; absent on the GPU host).  MAT_REFERENCE_ROOT
+# overrides where it is looked for.
+REFERENCE_TREE = Path(os.environ.get("MAT_REFERENCE_ROOT", "/root/reference"))
+REFERENCE_ROOT = REFERENCE_TREE / "Mat-8.3.1"
 REF81_LIB = REF_DIR / "libmat81ref.so"
-REFERENCE81_ROOT = Path("/root/reference/Mat-8.1")
+REFERENCE81_ROOT = REFERENCE_TREE / "Mat-8.1"
+# the seeded input streams the oracle shares with the library
+RNG_HEADER = HERE.parent / "mat_gb300" / "csrc" / "rng.cuh"
 
 
 def _cxx() -> str:
@@ -41,7 +46,7 @@ def _stale(lib: Path, deps: list[Path]) -> bool:
 
 def build_oracle(force: bool = False) -> Path:
     src = HERE / "mat_oracle.cpp"
-    if force or _stale(ORACLE_LIB, [src, Path(__file__)]):
+    if force or _stale(ORACLE_LIB, [src, RNG_HEADER, Path(__file__)]):
         cmd = [_cxx(), "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
                *_arch_flags(), str(src), "-o", str(ORACLE_LIB)]
         subprocess.run(cmd, check=True)

@@ -19,9 +19,19 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
+#include <atomic>
+#include <condition_variable>
 #include <functional>
+#include <memory>
+#include <mutex>
 #include <thread>
 #include <vector>
+
+#include <unistd.h>
+
+// The seeded input streams (counter-based, bit-identical on the host and the
+// GPU) are the library's; the oracle generates the same inputs from them.
+#include "../mat_gb300/csrc/rng.cuh"
 
 namespace {
 
@@ -34,57 +44,265 @@ constexpr int BS_QR = 48;
 
 inline double& at(double* A, int lda, int r, int c) { return A[r + (size_t)c * lda]; }
 
+// ------------------------------------------------------------ host threads
+// The reference is single-threaded; the restatement spreads independent
+// elements over host threads without changing any element's operation
+// sequence, so its results do not depend on the thread count.
+//
+// Pool: persistent workers; run(nt, fn) calls fn(tid, nt) on nt threads (the
+// caller is thread 0) and returns when all have finished.  A pool created
+// before a fork() is rebuilt in the child (its workers did not survive).
+class Pool {
+public:
+    ~Pool() { stop(); }
+
+    void run(int nt, const std::function<void(int, int)>& fn) {
+        nt = std::max(1, nt);
+        if (nt == 1 || in_job()) {  // nested inside a job: run inline
+            fn(0, 1);
+            return;
+        }
+        std::lock_guard<std::mutex> serial(run_mu_);
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            ensure(nt - 1);
+            job_ = &fn;
+            job_nt_ = nt;
+            pending_ = nt - 1;
+            ++gen_;
+        }
+        cv_.notify_all();
+        in_job() = true;
+        fn(0, nt);
+        in_job() = false;
+        std::unique_lock<std::mutex> g(mu_);
+        done_cv_.wait(g, [&] { return pending_ == 0; });
+        job_ = nullptr;
+    }
+
+private:
+    static bool& in_job() {
+        static thread_local bool flag = false;
+        return flag;
+    }
+    // called with mu_ held, before the job's generation is published: a new
+    // worker starts from the current generation and so sees the next job
+    void ensure(int workers) {
+        if (pid_ != getpid()) {  // after a fork: the old workers do not exist here
+            for (auto& t : th_) t.detach();
+            th_.clear();
+            pid_ = getpid();
+            quit_ = false;
+        }
+        while ((int)th_.size() < workers) {
+            const int id = (int)th_.size() + 1;
+            const uint64_t start = gen_;
+            th_.emplace_back([this, id, start] { loop(id, start); });
+        }
+    }
+    void loop(int id, uint64_t seen) {
+        in_job() = true;
+        for (;;) {
+            const std::function<void(int, int)>* job = nullptr;
+            int nt = 0;
+            {
+                std::unique_lock<std::mutex> g(mu_);
+                cv_.wait(g, [&] { return quit_ || gen_ != seen; });
+                if (quit_) return;
+                seen = gen_;
+                job = job_;
+                nt = job_nt_;
+            }
+            if (id < nt) {
+                (*job)(id, nt);
+                std::lock_guard<std::mutex> g(mu_);
+                if (--pending_ == 0) done_cv_.notify_all();
+            }
+        }
+    }
+    void stop() {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            quit_ = true;
+        }
+        cv_.notify_all();
+        for (auto& t : th_)
+            if (t.joinable()) {
+                if (pid_ == getpid())
+                    t.join();
+                else
+                    t.detach();
+            }
+    }
+
+    std::vector<std::thread> th_;
+    std::mutex mu_, run_mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(int, int)>* job_ = nullptr;
+    int job_nt_ = 0, pending_ = 0;
+    uint64_t gen_ = 0;
+    bool quit_ = false;
+    pid_t pid_ = getpid();
+};
+
+Pool& pool() {
+    static Pool p;
+    return p;
+}
+
+// Sense-reversing spin barrier for phases inside one Pool::run.
+class SpinBarrier {
+public:
+    explicit SpinBarrier(int n) : n_(n) {}
+    void wait() {
+        const int ph = phase_.load(std::memory_order_acquire);
+        if (count_.fetch_add(1, std::memory_order_acq_rel) == n_ - 1) {
+            count_.store(0, std::memory_order_relaxed);
+            phase_.store(ph + 1, std::memory_order_release);
+            return;
+        }
+        for (unsigned spins = 0; phase_.load(std::memory_order_acquire) == ph; ++spins)
+            if ((spins & 1023u) == 1023u) std::this_thread::yield();
+    }
+
+private:
+    const int n_;
+    std::atomic<int> count_{0};
+    std::atomic<int> phase_{0};
+};
+
+// Splits [0, n) into nt contiguous chunks; chunk t is [lo, hi).
+inline void chunk(int n, int t, int nt, int& lo, int& hi) {
+    const int q = n / nt, r = n % nt;
+    lo = t * q + std::min(t, r);
+    hi = lo + q + (t < r ? 1 : 0);
+}
+
 // Runs fn(lo, hi) over [0, n) split into contiguous chunks across threads.
 void parallel_cols(int n, const std::function<void(int, int)>& fn) {
     const int t = std::max(1, std::min(g_threads, n));
-    if (t == 1) {
-        fn(0, n);
-        return;
-    }
-    std::vector<std::thread> th;
-    const int chunk = (n + t - 1) / t;
-    for (int i = 0; i < t; ++i) {
-        const int lo = i * chunk, hi = std::min(n, lo + chunk);
-        if (lo < hi) th.emplace_back(fn, lo, hi);
-    }
-    for (auto& x : th) x.join();
-}
-
-// C(m x n) (+|-)= A(m x k) * B(k x n): per element a sequential fused chain
-// over p = 0..k-1 (Mat's micro-kernels load C and fmadd / fnmadd into it,
-// Mul/__micro_kernel_packed_double.h:14-110 and :301-398).
-void gemm_acc(int m, int n, int k, const double* A, int lda, const double* B, int ldb, double* C, int ldc,
-              bool subtract) {
-    if (m <= 0 || n <= 0 || k <= 0) return;
-    parallel_cols(n, [&](int j0, int j1) {
-        constexpr int MB = 256;
-        for (int i0 = 0; i0 < m; i0 += MB) {
-            const int i1 = std::min(m, i0 + MB);
-            for (int j = j0; j < j1; ++j) {
-                double* c = C + (size_t)j * ldc;
-                for (int p = 0; p < k; ++p) {
-                    const double b = subtract ? -B[p + (size_t)j * ldb] : B[p + (size_t)j * ldb];
-                    const double* a = A + (size_t)p * lda;
-                    for (int i = i0; i < i1; ++i) c[i] = std::fma(a[i], b, c[i]);
-                }
-            }
-        }
+    pool().run(t, [&](int tid, int nt) {
+        int lo, hi;
+        chunk(n, tid, nt, lo, hi);
+        if (lo < hi) fn(lo, hi);
     });
 }
 
-// C -= A * B^T with B given as rows (Mat's __times_A_BT_LLT, LU/__LLT.h:59-91).
-void gemm_abt_sub(int m, int n, int k, const double* A, int lda, const double* B, int ldb, double* C, int ldc) {
+// ------------------------------------------------------------------ GEMM
+// C(m x n) (+|-)= A(m x k) * op(B): per element a sequential fused chain over
+// p = 0..k-1 starting from C (Mat's micro-kernels load C and fmadd / fnmadd
+// into it, Mul/__micro_kernel_packed_double.h:14-110 and :301-398; fnmadd
+// c - a b is fma(a, -b, c)).  Mat's own KC blocking stores the partial chain
+// to C and reloads it, which changes nothing, and neither does the blocking
+// here: A is packed in slivers of MR rows, op(B) (negated when subtracting)
+// in slivers of NR columns, per KC block of k; an MR x NR register tile runs
+// each element's chain over the block; tiles are spread over the threads.
+constexpr int MR = 8, NR = 6, KC = 256;
+constexpr int TILE_MS = 16, TILE_NS = 16;  // slivers per tile: 128 rows x 96 columns
+
+// Full MR x NR tile read from and written to C in place.
+inline void ukernel_c(int kc, const double* __restrict ap, const double* __restrict bp, double* __restrict c,
+                      int ldc) {
+    double acc[NR][MR];
+    for (int j = 0; j < NR; ++j)
+        for (int i = 0; i < MR; ++i) acc[j][i] = c[i + (size_t)j * ldc];
+    for (int p = 0; p < kc; ++p) {
+        const double* a = ap + (size_t)p * MR;
+        const double* b = bp + (size_t)p * NR;
+#pragma GCC unroll 8
+        for (int j = 0; j < NR; ++j) {
+            const double bj = b[j];
+#pragma GCC unroll 8
+            for (int i = 0; i < MR; ++i) acc[j][i] = std::fma(a[i], bj, acc[j][i]);
+        }
+    }
+    for (int j = 0; j < NR; ++j)
+        for (int i = 0; i < MR; ++i) c[i + (size_t)j * ldc] = acc[j][i];
+}
+
+// transB: op(B) = B^T with B given as n x k rows (ld ldb).
+void gemm_core(int m, int n, int k, const double* A, int lda, const double* B, int ldb, bool transB, double* C,
+               int ldc, bool subtract) {
     if (m <= 0 || n <= 0 || k <= 0) return;
-    parallel_cols(n, [&](int j0, int j1) {
-        for (int j = j0; j < j1; ++j) {
+    auto bval = [&](int p, int j) { return transB ? B[j + (size_t)p * ldb] : B[p + (size_t)j * ldb]; };
+    if ((double)m * n * k < 4.0e5 || m < MR) {
+        for (int j = 0; j < n; ++j) {
             double* c = C + (size_t)j * ldc;
             for (int p = 0; p < k; ++p) {
-                const double b = -B[j + (size_t)p * ldb];
+                const double b = subtract ? -bval(p, j) : bval(p, j);
                 const double* a = A + (size_t)p * lda;
                 for (int i = 0; i < m; ++i) c[i] = std::fma(a[i], b, c[i]);
             }
         }
-    });
+        return;
+    }
+    const int ms = (m + MR - 1) / MR, ns = (n + NR - 1) / NR;
+    const int nrb = (ms + TILE_MS - 1) / TILE_MS, ncb = (ns + TILE_NS - 1) / TILE_NS;
+    const int kcmax = std::min(KC, k);
+    std::vector<double> Ap((size_t)ms * kcmax * MR), Bp((size_t)ns * kcmax * NR);
+    const int nt = std::max(1, std::min(g_threads, nrb * ncb));
+    for (int p0 = 0; p0 < k; p0 += KC) {
+        const int kc = std::min(KC, k - p0);
+        std::atomic<int> next{0};
+        SpinBarrier bar(nt);
+        pool().run(nt, [&](int tid, int nth) {
+            int lo, hi;
+            chunk(ms, tid, nth, lo, hi);
+            for (int s = lo; s < hi; ++s) {
+                double* dst = Ap.data() + (size_t)s * kc * MR;
+                const int r0 = s * MR, rows = std::min(MR, m - r0);
+                for (int p = 0; p < kc; ++p) {
+                    const double* src = A + r0 + (size_t)(p0 + p) * lda;
+                    for (int i = 0; i < rows; ++i) dst[(size_t)p * MR + i] = src[i];
+                    for (int i = rows; i < MR; ++i) dst[(size_t)p * MR + i] = 0.0;
+                }
+            }
+            chunk(ns, tid, nth, lo, hi);
+            for (int t = lo; t < hi; ++t) {
+                double* dst = Bp.data() + (size_t)t * kc * NR;
+                const int c0 = t * NR, cols = std::min(NR, n - c0);
+                for (int j = 0; j < NR; ++j)
+                    for (int p = 0; p < kc; ++p) {
+                        double v = j < cols ? bval(p0 + p, c0 + j) : 0.0;
+                        dst[(size_t)p * NR + j] = subtract ? -v : v;
+                    }
+            }
+            bar.wait();
+            for (int tile = next.fetch_add(1); tile < nrb * ncb; tile = next.fetch_add(1)) {
+                const int cb = tile / nrb, rb = tile % nrb;
+                const int t1 = std::min(ns, (cb + 1) * TILE_NS), s1 = std::min(ms, (rb + 1) * TILE_MS);
+                for (int t = cb * TILE_NS; t < t1; ++t) {
+                    const double* bp = Bp.data() + (size_t)t * kc * NR;
+                    const int c0 = t * NR, cols = std::min(NR, n - c0);
+                    for (int s = rb * TILE_MS; s < s1; ++s) {
+                        const double* ap = Ap.data() + (size_t)s * kc * MR;
+                        const int r0 = s * MR, rows = std::min(MR, m - r0);
+                        double* c = C + r0 + (size_t)c0 * ldc;
+                        if (rows == MR && cols == NR) {
+                            ukernel_c(kc, ap, bp, c, ldc);
+                        } else {
+                            double buf[MR * NR] = {0};
+                            for (int j = 0; j < cols; ++j)
+                                for (int i = 0; i < rows; ++i) buf[i + j * MR] = c[i + (size_t)j * ldc];
+                            ukernel_c(kc, ap, bp, buf, MR);
+                            for (int j = 0; j < cols; ++j)
+                                for (int i = 0; i < rows; ++i) c[i + (size_t)j * ldc] = buf[i + j * MR];
+                        }
+                    }
+                }
+            }
+        });
+    }
+}
+
+void gemm_acc(int m, int n, int k, const double* A, int lda, const double* B, int ldb, double* C, int ldc,
+              bool subtract) {
+    gemm_core(m, n, k, A, lda, B, ldb, false, C, ldc, subtract);
+}
+
+// C -= A * B^T with B given as rows (Mat's __times_A_BT_LLT, LU/__LLT.h:59-91).
+void gemm_abt_sub(int m, int n, int k, const double* A, int lda, const double* B, int ldb, double* C, int ldc) {
+    gemm_core(m, n, k, A, lda, B, ldb, true, C, ldc, true);
 }
 
 // Mat's AVX-512 dot product (Calculate/__AVX512_double.h:110-133): four
@@ -143,33 +361,69 @@ double dot_generic(const double* a, const double* b, int len) {
 // LU/__Base.h:95-208): 8-column blocks by four partial sums, the ragged
 // columns by column-oriented fused updates.
 void trsm_lx(int k, int n, const double* L, int ldl, double* X, int ldx) {
-    int c = 0;
-    for (; c + 8 <= n; c += 8) {
-        for (int i = 0; i < k; ++i) {
-            for (int r = 0; r < 8; ++r) {
-                double* xc = X + (size_t)(c + r) * ldx;
-                double s0 = xc[i], s1 = 0, s2 = 0, s3 = 0;
-                int j = 0;
-                for (; j + 4 <= i; j += 4) {
-                    s0 = std::fma(-L[i + (size_t)(j + 0) * ldl], xc[j + 0], s0);
-                    s1 = std::fma(-L[i + (size_t)(j + 1) * ldl], xc[j + 1], s1);
-                    s2 = std::fma(-L[i + (size_t)(j + 2) * ldl], xc[j + 2], s2);
-                    s3 = std::fma(-L[i + (size_t)(j + 3) * ldl], xc[j + 3], s3);
+    const int nb8 = n / 8;
+    std::vector<double> nl((size_t)k * k);
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < i; ++j) nl[(size_t)i * k + j] = -L[i + (size_t)j * ldl];
+    // every column is independent: the 8-column blocks and the ragged tail are spread over threads
+    auto cols = [&](int b0, int b1) {
+        for (int b = b0; b < b1; ++b) {
+            if (b < nb8) {
+                // the 8 columns packed row by row (xb[j][r]), L's rows negated
+                // (nl[i][j] = -L(i,j)): the same four partial chains per element
+                // (j mod 4, in order) as Mat's 8-column register solve
+                const int c = 8 * b;
+                double xb[8 * 64 * 2];
+                std::vector<double> big;
+                double* x8 = xb;
+                if (k > 128) {
+                    big.resize((size_t)8 * k);
+                    x8 = big.data();
                 }
-                for (; j < i; ++j) s0 = std::fma(-L[i + (size_t)j * ldl], xc[j], s0);
-                xc[i] = s0 + (s1 + (s2 + s3));
+                for (int r = 0; r < 8; ++r)
+                    for (int i = 0; i < k; ++i) x8[i * 8 + r] = X[i + (size_t)(c + r) * ldx];
+                for (int i = 0; i < k; ++i) {
+                    const double* li = nl.data() + (size_t)i * k;
+                    double s0[8], s1[8], s2[8], s3[8];
+                    for (int r = 0; r < 8; ++r) {
+                        s0[r] = x8[i * 8 + r];
+                        s1[r] = s2[r] = s3[r] = 0.0;
+                    }
+                    int j = 0;
+                    for (; j + 4 <= i; j += 4) {
+                        const double l0 = li[j], l1 = li[j + 1], l2 = li[j + 2], l3 = li[j + 3];
+                        const double* x0 = x8 + j * 8;
+                        for (int r = 0; r < 8; ++r) {
+                            s0[r] = std::fma(l0, x0[r], s0[r]);
+                            s1[r] = std::fma(l1, x0[8 + r], s1[r]);
+                            s2[r] = std::fma(l2, x0[16 + r], s2[r]);
+                            s3[r] = std::fma(l3, x0[24 + r], s3[r]);
+                        }
+                    }
+                    for (; j < i; ++j)
+                        for (int r = 0; r < 8; ++r) s0[r] = std::fma(li[j], x8[j * 8 + r], s0[r]);
+                    for (int r = 0; r < 8; ++r) x8[i * 8 + r] = s0[r] + (s1[r] + (s2[r] + s3[r]));
+                }
+                for (int r = 0; r < 8; ++r)
+                    for (int i = 0; i < k; ++i) X[i + (size_t)(c + r) * ldx] = x8[i * 8 + r];
+            } else {
+                for (int c = 8 * nb8; c < n; ++c) {
+                    double* x = X + (size_t)c * ldx;
+                    for (int i = 1; i < k; ++i) {
+                        const double a = x[i - 1];
+                        if (a == 0.0) continue;
+                        const double* li = L + (size_t)(i - 1) * ldl;
+                        for (int r = i; r < k; ++r) x[r] = std::fma(li[r], -a, x[r]);
+                    }
+                }
             }
         }
-    }
-    for (; c < n; ++c) {
-        double* x = X + (size_t)c * ldx;
-        for (int i = 1; i < k; ++i) {
-            const double a = x[i - 1];
-            if (a == 0.0) continue;
-            const double* li = L + (size_t)(i - 1) * ldl;
-            for (int r = i; r < k; ++r) x[r] = std::fma(li[r], -a, x[r]);
-        }
-    }
+    };
+    const int nblocks = nb8 + (n % 8 ? 1 : 0);
+    if ((double)nblocks * k * k < 2.0e5)
+        cols(0, nblocks);
+    else
+        parallel_cols(nblocks, cols);
 }
 
 // X(k x n) := U^{-1} X, U upper k x k (generic __Solve_direct_UX, LU/__Base.h:51-92).
@@ -189,10 +443,12 @@ void trsm_ux(int k, int n, const double* U, int ldu, double* X, int ldx) {
 // Panel LU with partial pivoting on columns [r0, r0+bs) (Mat's __PLU2_piv,
 // LU/__PLU.h:54-90; with r0 = 0 and bs = all columns it is __PLU2,
 // :22-51).  Left-looking column updates, first index attaining max |a|,
-// row swaps over columns [0, r0+bs), multiplication by the reciprocal.
+// row swaps, multiplication by the reciprocal.  Mat swaps the rows over
+// columns [0, r0+bs); the swaps of the finished columns left of the panel
+// (pure moves of values nothing reads again) are left to the caller.
 // Returns the panel column at which a zero column stopped it (Mat's
 // `break`), or -1.
-int plu_panel(double* A, int lda, int m, int r0, int bs, int* pos, int* piv) {
+int plu_panel_serial(double* A, int lda, int m, int r0, int bs, int* pos, int* piv) {
     for (int i = 0; i < bs; ++i) piv[i] = i;
     for (int c = 0; c < bs; ++c) {
         const int gc = r0 + c;
@@ -217,7 +473,7 @@ int plu_panel(double* A, int lda, int m, int r0, int bs, int* pos, int* piv) {
             }
         piv[c] = j - r0;
         if (j != gc) {
-            for (int cc = 0; cc < r0 + bs; ++cc) std::swap(at(A, lda, gc, cc), at(A, lda, j, cc));
+            for (int cc = r0; cc < r0 + bs; ++cc) std::swap(at(A, lda, gc, cc), at(A, lda, j, cc));
             std::swap(pos[gc], pos[j]);
         }
         const double inv = 1.0 / col[gc];
@@ -226,15 +482,112 @@ int plu_panel(double* A, int lda, int m, int r0, int bs, int* pos, int* piv) {
     return -1;
 }
 
+// The same panel with its rows spread over threads.  Per column c: the rows
+// above the diagonal (the U part, a serial chain through the pivots) on one
+// thread, which also forms q_i = -A(r0+i, c); then every thread takes a
+// chunk of the rows [r0+c, m), scales its rows of column c-1 by the previous
+// pivot's reciprocal, applies fma(L(r, i), q_i, .) for i = 0..c-1 in order,
+// and finds its chunk's first largest |a|; one thread picks the first
+// largest over the chunks (Mat's first index) and swaps the two rows over
+// the panel's columns.  Each element sees Mat's operations in Mat's order.
+int plu_panel_parallel(double* A, int lda, int m, int r0, int bs, int* pos, int* piv, int nt) {
+    for (int i = 0; i < bs; ++i) piv[i] = i;
+    std::vector<double> q(bs), tmax(nt);
+    std::vector<int> targ(nt);
+    int brk = -1;
+    double inv_prev = 0.0;
+    SpinBarrier bar(nt);
+    pool().run(nt, [&](int tid, int nth) {
+        for (int c = 0; c < bs; ++c) {
+            const int gc = r0 + c;
+            double* col = A + (size_t)gc * lda;
+            if (tid == 0) {
+                for (int i = 0; i < c; ++i) {
+                    const int gi = r0 + i;
+                    q[i] = -col[gi];
+                    const double* li = A + (size_t)gi * lda;
+                    for (int r = gi + 1; r < gc; ++r) col[r] = std::fma(li[r], q[i], col[r]);
+                }
+            }
+            bar.wait();
+            int lo, hi;
+            chunk(m - gc, tid, nth, lo, hi);
+            lo += gc;
+            hi += gc;
+            if (c > 0) {
+                double* pc = col - lda;
+                for (int r = lo; r < hi; ++r) pc[r] = pc[r] * inv_prev;
+            }
+            for (int i = 0; i < c; ++i) {
+                const double* li = A + (size_t)(r0 + i) * lda;
+                const double qi = q[i];
+                for (int r = lo; r < hi; ++r) col[r] = std::fma(li[r], qi, col[r]);
+            }
+            double lmax = 0.0;
+            int larg = -1;
+            for (int r = lo; r < hi; ++r) lmax = std::max(lmax, std::fabs(col[r]));
+            for (int r = lo; r < hi; ++r)
+                if (std::fabs(col[r]) == lmax) {
+                    larg = r;
+                    break;
+                }
+            tmax[tid] = lmax;
+            targ[tid] = larg;
+            bar.wait();
+            if (tid == 0) {
+                double maxv = 0.0;
+                for (int t = 0; t < nth; ++t) maxv = std::max(maxv, tmax[t]);
+                if (maxv == 0.0) {
+                    piv[c] = c;
+                    brk = c;
+                } else {
+                    int j = gc;
+                    for (int t = 0; t < nth; ++t)
+                        if (targ[t] >= 0 && tmax[t] == maxv) {
+                            j = targ[t];
+                            break;
+                        }
+                    piv[c] = j - r0;
+                    if (j != gc) {
+                        for (int cc = r0; cc < r0 + bs; ++cc) std::swap(at(A, lda, gc, cc), at(A, lda, j, cc));
+                        std::swap(pos[gc], pos[j]);
+                    }
+                    inv_prev = 1.0 / col[gc];
+                }
+            }
+            bar.wait();
+            if (brk >= 0) return;
+        }
+        const int gl = r0 + bs - 1;
+        int lo, hi;
+        chunk(m - gl - 1, tid, nth, lo, hi);
+        double* lc = A + (size_t)gl * lda;
+        for (int r = gl + 1 + lo; r < gl + 1 + hi; ++r) lc[r] = lc[r] * inv_prev;
+    });
+    return brk;
+}
+
+int plu_panel(double* A, int lda, int m, int r0, int bs, int* pos, int* piv) {
+    const int nt = std::min(g_threads, (m - r0) / 1024);
+    if (nt < 2) return plu_panel_serial(A, lda, m, r0, bs, pos, piv);
+    return plu_panel_parallel(A, lda, m, r0, bs, pos, piv, nt);
+}
+
 // Applies a panel's interchanges to columns [c0, c1) (Mat's __laswp_trailing, LU/__PLU.h:3-19).
 void laswp(double* A, int lda, int r0, int kcount, int c0, int c1, const int* piv) {
-    for (int c = c0; c < c1; ++c) {
-        double* col = A + (size_t)c * lda;
-        for (int k = 0; k < kcount; ++k) {
-            const int i = r0 + k, j = r0 + piv[k];
-            if (i != j) std::swap(col[i], col[j]);
+    auto cols = [&](int lo, int hi) {
+        for (int c = c0 + lo; c < c0 + hi; ++c) {
+            double* col = A + (size_t)c * lda;
+            for (int k = 0; k < kcount; ++k) {
+                const int i = r0 + k, j = r0 + piv[k];
+                if (i != j) std::swap(col[i], col[j]);
+            }
         }
-    }
+    };
+    if (c1 - c0 < 256)
+        cols(0, std::max(0, c1 - c0));
+    else
+        parallel_cols(c1 - c0, cols);
 }
 
 // In-place blocked right-looking PLU (Mat's PLU / __PLU, LU/__PLU.h:93-190).
@@ -274,10 +627,12 @@ int plu_inplace(int m, int n, double* A, int lda, int* pos) {
         }
         return info;
     }
+    std::vector<int> allpiv(s);  // the row each row r was swapped with (absolute)
     int r = 0;
     for (; r + BS_LU <= s; r += BS_LU) {
         const int brk = plu_panel(A, lda, m, r, BS_LU, pos, piv.data());
         if (brk >= 0 && !info) info = r + brk + 1;
+        for (int k = 0; k < BS_LU; ++k) allpiv[r + k] = r + piv[k];
         laswp(A, lda, r, BS_LU, r + BS_LU, n, piv.data());
         if (r + BS_LU < s) {
             const int nt = n - (r + BS_LU);
@@ -291,7 +646,19 @@ int plu_inplace(int m, int n, double* A, int lda, int* pos) {
         const int rem = s - r;
         const int brk = plu_panel(A, lda, m, r, rem, pos, piv.data());
         if (brk >= 0 && !info) info = r + brk + 1;
+        for (int k = 0; k < rem; ++k) allpiv[r + k] = r + piv[k];
     }
+    // Mat's interchanges of the columns left of each panel, applied at the
+    // end: column c receives every later panel's swaps in order (each column
+    // stays in cache while it takes them)
+    const int last = r < s ? r : r - BS_LU;
+    parallel_cols(std::max(0, last), [&](int c0, int c1) {
+        for (int c = c0; c < c1; ++c) {
+            double* col = A + (size_t)c * lda;
+            for (int k = (c / BS_LU + 1) * BS_LU; k < s; ++k)
+                if (allpiv[k] != k) std::swap(col[k], col[allpiv[k]]);
+        }
+    });
     return info;
 }
 
@@ -596,6 +963,109 @@ void qr_unblocked(int m, int n, double* R, double* Q) {
     // computed them (rounding-level values), unlike the blocked path.
 }
 
+// Solve_direct_narrow's substitutions (LU/__Solve_direct.h:118-139) on the
+// in-place factors a (unit L below the diagonal, U on and above it) for up
+// to four right-hand sides X (n x nrhs, ld n).  Forward: for k = 0..n-2,
+// x[r] = fma(L(r,k), -x[k], x[r]) for r > k; backward: for r = n-1..1,
+// x[r] /= U(r,r), x[i] = fma(U(i,r), -x[r], x[i]) for i < r; x[0] /= U(0,0).
+// Blocks of NB columns: the rows inside the block on one thread (the serial
+// chain), the rows outside it spread over threads; each element still sees
+// its updates in Mat's order.
+void narrow_substitution(int n, int nrhs, const double* a, double* X) {
+    constexpr int NB = 256;
+    const int nt = std::min(g_threads, n / 1024);
+    SpinBarrier bar(std::max(nt, 1));
+    pool().run(std::max(nt, 1), [&](int tid, int nth) {
+        for (int b0 = 0; b0 < n; b0 += NB) {
+            const int b1 = std::min(n, b0 + NB);
+            if (tid == 0)
+                for (int k = b0; k < std::min(b1, n - 1); ++k) {
+                    const double* lk = a + (size_t)k * n;
+                    for (int j = 0; j < nrhs; ++j) {
+                        double* x = X + (size_t)j * n;
+                        const double q = -x[k];
+                        for (int r = k + 1; r < b1; ++r) x[r] = std::fma(lk[r], q, x[r]);
+                    }
+                }
+            bar.wait();
+            int lo, hi;
+            chunk(n - b1, tid, nth, lo, hi);
+            lo += b1;
+            hi += b1;
+            for (int k = b0; k < b1 && lo < hi; ++k) {
+                const double* lk = a + (size_t)k * n;
+                for (int j = 0; j < nrhs; ++j) {
+                    double* x = X + (size_t)j * n;
+                    const double q = -x[k];
+                    for (int r = lo; r < hi; ++r) x[r] = std::fma(lk[r], q, x[r]);
+                }
+            }
+            bar.wait();
+        }
+        for (int b1 = n; b1 > 0; b1 -= NB) {
+            const int b0 = std::max(0, b1 - NB);
+            if (tid == 0)
+                for (int r = b1 - 1; r >= b0; --r) {
+                    const double* ur = a + (size_t)r * n;
+                    for (int j = 0; j < nrhs; ++j) {
+                        double* x = X + (size_t)j * n;
+                        x[r] /= ur[r];
+                        if (r == 0) continue;
+                        const double q = -x[r];
+                        for (int i = b0; i < r; ++i) x[i] = std::fma(ur[i], q, x[i]);
+                    }
+                }
+            bar.wait();
+            int lo, hi;
+            chunk(b0, tid, nth, lo, hi);
+            for (int r = b1 - 1; r >= b0 && lo < hi; --r) {
+                const double* ur = a + (size_t)r * n;
+                for (int j = 0; j < nrhs; ++j) {
+                    double* x = X + (size_t)j * n;
+                    const double q = -x[r];
+                    for (int i = lo; i < hi; ++i) x[i] = std::fma(ur[i], q, x[i]);
+                }
+            }
+            bar.wait();
+        }
+    });
+}
+
+// ------------------------------------------------------ seeded inputs
+// The library's seeded matrices (mg_host_fill_*, mg_gen_svd_matrix)
+// regenerated on the host: each entry depends only on (seed, index), so the
+// fill is spread over threads by columns.
+void host_fill(double* A, int rows, int cols, int ld, uint64_t key, double lo, double hi, bool rowmajor,
+               bool normal) {
+    auto fill = [&](int c0, int c1) {
+        for (int c = c0; c < c1; ++c)
+            for (int r = 0; r < rows; ++r) {
+                const uint64_t idx = rowmajor ? (uint64_t)r * cols + c : (uint64_t)r + (uint64_t)c * rows;
+                A[r + (size_t)c * ld] = normal ? mgrng::normal_at(key, idx) : mgrng::uniform_at(key, idx, lo, hi);
+            }
+    };
+    if ((size_t)rows * cols < (1u << 16))
+        fill(0, cols);
+    else
+        parallel_cols(cols, fill);
+}
+
+// T (k x k, upper) of Q = H_0 ... H_{k-1} = I - V T V^T from G = V^T V, the
+// forward recurrence of the block reflector (plain multiply and add, no
+// contraction), as mg_gen_svd_matrix forms it on the host.
+void svd_build_T(int k, const std::vector<double>& G, std::vector<double>& T) {
+    T.assign((size_t)k * k, 0.0);
+    for (int i = 0; i < k; ++i) {
+        const double tau = 2.0 / G[i + (size_t)i * k];
+        for (int r = 0; r < i; ++r) {
+            double s = 0.0;
+            for (int c = r; c < i; ++c) s += T[r + (size_t)c * k] * G[c + (size_t)i * k];
+            T[r + (size_t)i * k] = -tau * s;
+        }
+        T[i + (size_t)i * k] = tau;
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -606,6 +1076,60 @@ void orc_set_threads(int n) { g_threads = std::max(1, n); }
 void orc_dgemm(int m, int n, int k, const double* A, int lda, const double* B, int ldb, double* C, int ldc) {
     for (int j = 0; j < n; ++j) std::memset(C + (size_t)j * ldc, 0, sizeof(double) * (size_t)std::max(m, 0));
     gemm_acc(m, n, k, A, lda, B, ldb, C, ldc, false);
+}
+
+void orc_host_fill_uniform(double* A, int rows, int cols, int ld, uint64_t seed, double lo, double hi,
+                           int rowmajor_stream) {
+    if (!A || rows <= 0 || cols <= 0) return;
+    host_fill(A, rows, cols, ld, mgrng::stream_key(seed, mgrng::kSaltUniform), lo, hi, rowmajor_stream != 0, false);
+}
+
+void orc_host_fill_normal(double* A, int rows, int cols, int ld, uint64_t seed, int rowmajor_stream) {
+    if (!A || rows <= 0 || cols <= 0) return;
+    host_fill(A, rows, cols, ld, mgrng::stream_key(seed, mgrng::kSaltNormal), 0, 0, rowmajor_stream != 0, true);
+}
+
+// The library's mg_gen_svd_matrix on the host: A = Q1 diag(sigma) Q2,
+// sigma_r = mgrng::geometric_at(r, n, sigma_min), V1, V2 (n x k) iid N(0,1)
+// with seeds 2 seed + 1 and 2 seed + 2 (row-major streams), G = V^T V and T
+// as above, then A := A - V (T (V^T A)) with V1 and A := A - ((A V) T) V^T
+// with V2.  Every product is a fused chain in order from zero (or from A for
+// the subtractions), as the GPU's FP64 GEMM computes it, so the result is
+// the GPU's bit for bit.  Returns 0, or 1 for invalid arguments.
+int orc_gen_svd_matrix(int n, double* A, int lda, uint64_t seed, int nrefl, double sigma_min) {
+    if (n < 0 || lda < std::max(n, 1) || nrefl < 0 || (n && !A) || !(sigma_min > 0.0 && sigma_min <= 1.0)) return 1;
+    if (n == 0) return 0;
+    parallel_cols(n, [&](int c0, int c1) {
+        for (int c = c0; c < c1; ++c) {
+            double* col = A + (size_t)c * lda;
+            std::fill(col, col + n, 0.0);
+            col[c] = mgrng::geometric_at(c, n, sigma_min);
+        }
+    });
+    const int k = nrefl;
+    if (k == 0) return 0;
+    const size_t nk = (size_t)n * k;
+    std::vector<double> V(nk), Vt(nk), W(nk), W2(nk), G((size_t)k * k), T;
+    for (int side = 0; side < 2; ++side) {
+        orc_host_fill_normal(V.data(), n, k, n, seed * 2 + 1 + side, 1);
+        for (int c = 0; c < k; ++c)
+            for (int r = 0; r < n; ++r) Vt[c + (size_t)r * k] = V[r + (size_t)c * n];
+        std::fill(G.begin(), G.end(), 0.0);
+        gemm_acc(k, k, n, Vt.data(), k, V.data(), n, G.data(), k, false);
+        svd_build_T(k, G, T);
+        std::fill(W.begin(), W.end(), 0.0);
+        std::fill(W2.begin(), W2.end(), 0.0);
+        if (side == 0) {
+            gemm_acc(k, n, n, Vt.data(), k, A, lda, W.data(), k, false);   // W = V^T A
+            gemm_acc(k, n, k, T.data(), k, W.data(), k, W2.data(), k, false);  // W2 = T W
+            gemm_acc(n, n, k, V.data(), n, W2.data(), k, A, lda, true);    // A -= V W2
+        } else {
+            gemm_acc(n, k, n, A, lda, V.data(), n, W.data(), n, false);    // W = A V
+            gemm_acc(n, k, k, W.data(), n, T.data(), k, W2.data(), n, false);  // W2 = W T
+            gemm_core(n, n, k, W2.data(), n, V.data(), n, true, A, lda, true);  // A -= W2 V^T
+        }
+    }
+    return 0;
 }
 
 // In-place Mat PLU: A := L\U (unit L below the diagonal), pos as Mat returns it.
@@ -631,37 +1155,29 @@ int orc_plu(int m, int n, const double* A, int* pos, double* L, double* U) {
 // sides, Mat's narrow path: in-place PLU, permute, scalar forward and back
 // substitution (:112-139).  Wider: blocked substitution by the same TRSMs.
 int orc_solve(int n, int nrhs, const double* A, const double* B, double* X) {
-    std::vector<double> a(A, A + (size_t)n * n);
+    // A is taken by value (Mat copies it); the copy and the substitutions are
+    // spread over threads, each element keeping its operation sequence.
+    std::unique_ptr<double[]> abuf(new double[(size_t)n * n + 1]);
+    double* ad_w = abuf.get();
+    parallel_cols(n, [&](int c0, int c1) {
+        std::memcpy(ad_w + (size_t)c0 * n, A + (size_t)c0 * n, sizeof(double) * (size_t)n * (c1 - c0));
+    });
     std::vector<int> pos(n);
-    const int info = plu_inplace(n, n, a.data(), n, pos.data());
+    const int info = plu_inplace(n, n, ad_w, n, pos.data());
     for (int j = 0; j < nrhs; ++j)
         for (int i = 0; i < n; ++i) X[i + (size_t)j * n] = B[pos[i] + (size_t)j * n];
+    const double* ad = ad_w;
     if (nrhs <= 4) {
-        for (int j = 0; j < nrhs; ++j) {
-            double* x = X + (size_t)j * n;
-            for (int k = 0; k < n - 1; ++k) {
-                const double q = -x[k];
-                const double* lk = a.data() + (size_t)k * n;
-                for (int r = k + 1; r < n; ++r) x[r] = std::fma(lk[r], q, x[r]);
-            }
-            for (int r = n - 1; r > 0; --r) {
-                x[r] /= a[r + (size_t)r * n];
-                const double q = -x[r];
-                const double* ur = a.data() + (size_t)r * n;
-                for (int i = 0; i < r; ++i) x[i] = std::fma(ur[i], q, x[i]);
-            }
-            if (n > 0) x[0] /= a[0];
-        }
+        narrow_substitution(n, nrhs, ad, X);
     } else if (n <= BS_LU * 3 / 2) {
         // one block (:166-190)
-        trsm_lx(n, nrhs, a.data(), n, X, n);
-        trsm_ux(n, nrhs, a.data(), n, X, n);
+        trsm_lx(n, nrhs, ad, n, X, n);
+        trsm_ux(n, nrhs, ad, n, X, n);
     } else {
         // __Solve_direct_LU_X (:1-66): blocks of BS_LU rows; forward, each
         // block's TRSM then X(below) -= L(below, block) X(block); backward
         // from the last block, X(above) -= U(above, block) X(block).  The
         // NC / MC tiling of the products leaves each element's chain unchanged.
-        const double* ad = a.data();
         for (int r = 0; r < n; r += BS_LU) {
             const int l = std::min(BS_LU, n - r);
             trsm_lx(l, nrhs, ad + r + (size_t)r * n, n, X + r, n);

@@ -3,12 +3,17 @@ itself: Mat-8.3.1 compiled from its own headers into oracle/_ref/libmatref.so
 (x86-64 AVX-512 build, the configuration of Mat's published numbers), and the
 Mat-8.1 snapshot's EVD_Q path into oracle/_ref/libmat81ref.so.
 
-Inputs come from the library's seeded generators (mg_host_fill_*), which are
-bit-identical on the host and the GPU.  Small cases keep full outputs; the
-benchmark-size cases keep SHA-256 digests of the raw column-major output
-bytes (exact, size-independent) plus a few sketch values.
+Inputs come from the library's seeded streams as the oracle regenerates
+them (oracle.api.host_fill_*, gen_svd_matrix: bit-identical to the library's
+host and GPU generators).  Small cases keep full outputs; the benchmark-size
+cases keep SHA-256 digests of the raw column-major output bytes (exact,
+size-independent) plus a few sketch values.
 
 Run from the repository root:  python tests/golden/make_golden.py
+  --large: only (re)computes the benchmark-configuration cases (the solves
+  at n = 8192 x 1 and 16384 x 4 on their benchmark inputs, and the
+  Householder QR of 16384 x 4096 with its full Q; about five minutes of the
+  single-threaded reference) and merges them into golden.json.
 """
 from __future__ import annotations
 
@@ -23,8 +28,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
-from mat_gb300.api import host_fill_normal, host_fill_uniform  # noqa: E402
-from oracle.api import reference, reference81  # noqa: E402
+from oracle.api import gen_svd_matrix, host_fill_normal, host_fill_uniform, reference, reference81  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
 EVD_EPS = 1e-10  # absolute deflation threshold of the EVD_Q cases
@@ -52,7 +56,45 @@ def spd(ref, n: int, seed: int) -> np.ndarray:
     return np.asfortranarray(s)
 
 
+def large(ref):
+    """The benchmark configurations themselves: FP64 Solve_direct at n = 8192
+    with 1 right-hand side (A, b iid N(0,1), seeds 1, 2), at n = 16384 with 4
+    (the mixed solve's system: A = Q1 diag(sigma) Q2 from gen_svd_matrix seed
+    3, 64 reflectors per side, sigma 1 .. 1e-6; B iid N(0,1) seed 11), and
+    QR(A, Q, R, QR_Householder) of a 16384 x 4096 A iid N(0,1) (seed 1)."""
+    out = {}
+    t = time.time()
+    x = ref.solve(host_fill_normal(8192, 8192, 1), host_fill_normal(8192, 1, 2))
+    out["solve_8192_1"] = {"sha256": sha(x), "x0": x[:4, 0].tolist(), "seconds": round(time.time() - t, 1)}
+    t = time.time()
+    a = gen_svd_matrix(16384, 3, 64, 1e-6)
+    b = host_fill_normal(16384, 4, 11)
+    x = ref.solve(a, b)
+    out["solve_svd_16384_4"] = {"sha256": sha(x), "sha256_A": sha(a), "x0": x[:4, 0].tolist(),
+                                "seconds": round(time.time() - t, 1)}
+    del a, b, x
+    t = time.time()
+    q, r = ref.qr(host_fill_normal(16384, 4096, 1))
+    out["qr_16384x4096"] = {"sha256_Q": sha(q), "sha256_R": sha(r), "sketch_R": sketch(r),
+                            "seconds": round(time.time() - t, 1)}
+    return out
+
+
 def main():
+    ref = reference()
+    if ref is None:
+        raise SystemExit("the reference build (oracle/_ref) needs the reference tree and an x86-64 host")
+    if "--large" in sys.argv:
+        path = OUT / "golden.json"
+        meta = json.loads(path.read_text())
+        meta["cases"].update(large(ref))
+        path.write_text(json.dumps(meta, indent=1))
+        print("benchmark-configuration cases merged into golden.json")
+        return
+    main_all(ref)
+
+
+def main_all(ref):
     ref = reference()
     if ref is None:
         raise SystemExit("the reference build (oracle/_ref) needs the reference tree and an x86-64 host")

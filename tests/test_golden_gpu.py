@@ -162,3 +162,41 @@ def test_lu(handle, n):
     assert handle.dlu(A) == 0
     L, U = lu_factors(A)
     assert sha(L) == META[f"lu_{n}"]["sha256_L"] and sha(U) == META[f"lu_{n}"]["sha256_U"]
+
+
+# ------------------------------------------- the benchmark configurations
+# Digests of the reference's own results at the BASELINE sizes (make_golden.py
+# --large; the single-threaded reference takes about five minutes for them).
+
+def test_solve_8192_1_benchmark(handle):
+    """Config 2's FP64 solve: A, b iid N(0,1) (seeds 1, 2), n = 8192, 1 RHS."""
+    A, B = colmajor(8192, 8192), colmajor(8192, 1)
+    handle.fill_normal(A, 1)
+    handle.fill_normal(B, 2)
+    X, info = handle.dgesv(A, B)
+    torch.cuda.synchronize()
+    assert sha(X.cpu().numpy()) == META["solve_8192_1"]["sha256"]
+
+
+def test_solve_16384_4_benchmark(handle):
+    """Config 3's FP64 side: the mixed solve's system (A = Q1 diag(sigma) Q2,
+    seed 3, cond 1e6; B seed 11), solved by the FP64 GPU path bit for bit as
+    Mat's Solve_direct solves it."""
+    n = 16384
+    A, B = colmajor(n, n), colmajor(n, 4)
+    handle.gen_svd_matrix(A, 3, nrefl=64, sigma_min=1e-6)
+    handle.fill_normal(B, 11)
+    X, info = handle.dgesv(A, B)
+    torch.cuda.synchronize()
+    assert sha(X.cpu().numpy()) == META["solve_svd_16384_4"]["sha256"]
+
+
+def test_qr_16384x4096_benchmark(handle):
+    """Config 2's Householder QR with Mat's full 16384 x 16384 Q, bit for bit."""
+    m, k = 16384, 4096
+    A = colmajor(m, k)
+    handle.fill_normal(A, 1)
+    Q, R = handle.dqr(A)
+    torch.cuda.synchronize()
+    assert sha(R.cpu().numpy()) == META["qr_16384x4096"]["sha256_R"]
+    assert sha(Q.cpu().numpy()) == META["qr_16384x4096"]["sha256_Q"]

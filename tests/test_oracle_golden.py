@@ -9,7 +9,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from mat_gb300.api import host_fill_normal, host_fill_uniform
+from oracle.api import host_fill_normal, host_fill_uniform
 from oracle.api import reference, restatement
 
 G = Path(__file__).resolve().parent / "golden"
@@ -199,3 +199,16 @@ def test_evd81_restatement_equals_reference_build(orc, n):
         assert np.array_equal(x, y)
     for x, y in zip(orc.evd_q81(a, 1e-11), ref.evd_q81(a, 1e-11)):
         assert np.array_equal(x, y)
+
+
+def test_solve_benchmark_configs(orc):
+    """The oracle's Solve_direct on the BASELINE systems against the
+    reference's digests: n = 8192 with 1 RHS, and the mixed solve's n = 16384
+    system with 4 RHS (whose input digest is checked too)."""
+    from oracle.api import gen_svd_matrix
+    x = orc.solve(host_fill_normal(8192, 8192, 1), host_fill_normal(8192, 1, 2))
+    assert sha(x) == META["solve_8192_1"]["sha256"]
+    a = gen_svd_matrix(16384, 3, 64, 1e-6)
+    assert sha(a) == META["solve_svd_16384_4"]["sha256_A"]
+    x = orc.solve(a, host_fill_normal(16384, 4, 11))
+    assert sha(x) == META["solve_svd_16384_4"]["sha256"]
