@@ -136,10 +136,19 @@ mg_status_t mg_dgetrf(mg_handle_t h, int m, int n, double* A, int lda, int* pos,
  * file-scope device array of about 400 KiB per device, shared by every call:
  * calls that overlap on the GPU (other streams, other threads) race on it and
  * must be serialised by the caller.  Its address is looked up on the first
- * call on each device, so make that first call before any stream capture.
- * Limits: m <= 65536 rows and devices with at most 256 SMs, else
- * MG_ERR_UNSUPPORTED.  Same results, statuses and synchronisation as
- * mg_dgetrf. */
+ * call on each device and kept, so make that first call before any stream
+ * capture; a cudaDeviceReset (or other teardown of the device's primary
+ * context) invalidates the kept address, and the entry point must not be
+ * called on that device afterwards.  MG_ERR_UNSUPPORTED, returned before
+ * anything is launched, means one of: m > 65536; more than 256 SMs; or the
+ * first panel's slab does not fit shared memory: the panel is min(m, n)
+ * columns wide when min(m, n) <= 90 (else 60) and its m rows are spread over
+ * P = min(SMs, ceil(m / 128)) CTAs (one CTA when the slab is <= 64 KiB),
+ * each holding ceil(m / P) rows x width doubles within the opt-in shared
+ * memory per block (about 227 KiB on GB300: at width 90, m up to about
+ * 48,000 rows; at width 60, every m <= 65536).  mg_dgetrf has the same
+ * panel limit.  Otherwise the same results (bit for bit), statuses and
+ * synchronisation as mg_dgetrf. */
 mg_status_t mg_dgetrf_noalloc(void* cuda_stream, int m, int n, double* A, int lda, int* pos, int* info);
 
 /* X := A^{-1} B from mg_dgetrf's factors and pos (n x n), B and X distinct.
@@ -242,9 +251,17 @@ mg_status_t mg_bf16x_check_error(mg_handle_t h, int* device_err_flag);
  * trailing updates, fp32 accumulation), then FP64 iterative refinement
  * (r = b - A x in fp64, fp32 correction solves, fp64 update) until every
  * column satisfies ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= tol.
- * If refinement stalls it falls back to the plain FP64 GPU solve
- * (mg_dgesv) and returns MG_FALLBACK_USED (or MG_IR_STALLED when fallback
- * is off).  The mixed counterpart of Mat's Solve_direct
+ * If refinement stalls (the backward error not halving twice in a row, or
+ * max_iter reached), GMRES-IR takes over: refinement steps whose correction
+ * solves A d = r by FP64 GMRES (restart length 40, classical Gram-Schmidt
+ * twice) left-preconditioned by the fp32 factors applied in FP64 arithmetic,
+ * from x = 0 (Carson & Higham, "Accelerating the solution of linear systems
+ * by iterative refinement in three precisions", SIAM J. Sci. Comput. 2018);
+ * it converges well beyond plain refinement's condition-number range.  If
+ * that stalls too, the solve falls back to the plain FP64 GPU solve
+ * (mg_dgesv).  Either takeover returns MG_FALLBACK_USED (report.path 1 or
+ * 2); with both off, or fallback off after GMRES-IR stalled, MG_IR_STALLED.
+ * The mixed counterpart of Mat's Solve_direct
  * (Mat-8.3.1/LU/__Solve_direct.h:146-220), which has no mixed precision.
  * A and B are not modified.  Synchronises. */
 typedef struct mg_ir_opts {
@@ -252,13 +269,18 @@ typedef struct mg_ir_opts {
     int max_iter;  /* refinement iterations, default 30 */
     int nterms;    /* bf16 terms of the split updates (1..3), default 3 */
     int fallback;  /* nonzero: FP64 solve when refinement stalls (default 1) */
+    int gmres;     /* nonzero: GMRES-IR when plain refinement stalls, before the
+                      FP64 fallback (default 1; n up to the dataflow solves' size) */
+    int panel;     /* FP32 panel pivoting: 0 = default, 1 = partial pivoting,
+                      2 = tournament pivoting (one pivot agreement per 16 columns) */
+    int reserved;
 } mg_ir_opts;
 
 typedef struct mg_ir_report {
-    int iterations;        /* refinement steps taken */
-    int path;              /* 0 = refinement converged, 2 = FP64 fallback */
+    int iterations;        /* refinement steps taken (plain and GMRES-IR outer steps) */
+    int path;              /* 0 = refinement converged, 1 = GMRES-IR converged, 2 = FP64 fallback */
     int info;              /* first exactly-zero pivot column of the fp32 LU (1-based) */
-    int reserved;
+    int gmres_iterations;  /* GMRES (inner) iterations of GMRES-IR, 0 if it did not run */
     double backward_error; /* final max-over-columns normwise backward error */
     double anorm_inf;      /* ||A||_inf */
     double factor_ms;      /* host wall time of the fp32 factorization */
@@ -291,7 +313,10 @@ mg_status_t mg_sgetrf(mg_handle_t h, int n, float* A, int lda, int* pos, int* in
 /* ------------------------------------------------ benchmark input generators
  * A = Q1 diag(sigma) Q2 with Q1, Q2 products of `nrefl` Householder
  * reflectors whose vectors are iid N(0,1) (seeded), sigma geometric from 1
- * down to sigma_min (condition number 1/sigma_min). */
+ * down to sigma_min (condition number 1/sigma_min; 0 < sigma_min <= 1, else
+ * MG_ERR_ARG).  Every operation has a fixed order and rounding (fused-chain
+ * products, sigma from a series in basic arithmetic), so a host restatement
+ * reproduces A bit for bit. */
 mg_status_t mg_gen_svd_matrix(mg_handle_t h, int n, double* A, int lda, uint64_t seed, int nrefl,
                               double sigma_min);
 /* S = G G^T / n + I with G iid N(0,1) (seeded, row-major stream order). */
@@ -375,6 +400,17 @@ mg_status_t mg_sgp_loss_grad(mg_handle_t h, int n, const float* X, float ell, fl
 /* Measures the FP64 peaks of this GPU with dependent-free FMA / DMMA loops
  * (TFLOP/s, counting an FMA as 2 flops).  Synchronises. */
 mg_status_t mg_measure_fp64_peaks(mg_handle_t h, double* dfma_tflops, double* dmma_tflops);
+
+/* Self-test of the bounded device-side waits (no counterpart in Mat, which
+ * has no error channel: a zero pivot is a silent break,
+ * Mat-8.3.1/LU/__PLU.h:68-71).  Runs the library's own wait code with a
+ * budget of `poll_limit` polls (1 .. 2^24): kind 0 = the grid barrier of the
+ * cooperative kernels, in a cooperative launch of 8 CTAs of which CTA
+ * `withhold` (0..7) never arrives; kind 1 = an mbarrier wait on a phase that
+ * nothing completes.  withhold < 0 lets every wait complete.  Returns
+ * MG_TIMEOUT when the wait ran out (the kernel records it and returns: no
+ * trap, no hang, the handle stays usable), MG_OK otherwise.  Synchronises. */
+mg_status_t mg_selftest_bounded_wait(mg_handle_t h, int kind, int withhold, unsigned poll_limit);
 
 #ifdef __cplusplus
 }

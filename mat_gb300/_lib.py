@@ -28,11 +28,12 @@ pf64 = C.POINTER(C.c_double)
 
 
 class IrOpts(C.Structure):
-    _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("nterms", C.c_int), ("fallback", C.c_int)]
+    _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("nterms", C.c_int), ("fallback", C.c_int),
+                ("gmres", C.c_int), ("panel", C.c_int), ("reserved", C.c_int)]
 
 
 class IrReport(C.Structure):
-    _fields_ = [("iterations", C.c_int), ("path", C.c_int), ("info", C.c_int), ("reserved", C.c_int),
+    _fields_ = [("iterations", C.c_int), ("path", C.c_int), ("info", C.c_int), ("gmres_iterations", C.c_int),
                 ("backward_error", C.c_double), ("anorm_inf", C.c_double), ("factor_ms", C.c_double),
                 ("refine_ms", C.c_double), ("history", C.c_double * 32), ("pivot_growth", C.c_double)]
 
@@ -57,6 +58,7 @@ SIGNATURES: dict[str, tuple] = {
     "mg_dgemm": (i32, [vp, i32, i32, i32, i32, i32, f64, vp, i32, vp, i32, f64, vp, i32]),
     "mg_sgemm": (i32, [vp, i32, i32, i32, i32, i32, f32, vp, i32, vp, i32, f32, vp, i32]),
     "mg_measure_fp64_peaks": (i32, [vp, pf64, pf64]),
+    "mg_selftest_bounded_wait": (i32, [vp, i32, i32, C.c_uint]),
     "mg_dgetrf": (i32, [vp, i32, i32, vp, i32, vp, pi32]),
     "mg_dgetrf_noalloc": (i32, [vp, i32, i32, vp, i32, vp, pi32]),
     "mg_sgetf2": (i32, [vp, i32, i32, vp, i32, vp, pi32]),

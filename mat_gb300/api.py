@@ -207,21 +207,23 @@ class Handle:
             self.check(st, "mg_sgetrf")
         return pos, info.value
 
-    def dsgesv_ir(self, A, B, X=None, tol=1e-14, max_iter=30, nterms=3, fallback=True):
-        """Mixed LU (fp32 + split-BF16) + FP64 refinement. Returns (X, report dict, status)."""
+    def dsgesv_ir(self, A, B, X=None, tol=1e-14, max_iter=30, nterms=3, fallback=True, gmres=True, panel=0):
+        """Mixed LU (fp32 + split-BF16) + FP64 refinement, GMRES-IR and the FP64
+        fallback when refinement stalls. Returns (X, report dict with the status)."""
         n = A.shape[0]
         nrhs = B.shape[1]
         if X is None:
             X = colmajor(n, nrhs, device=B.device)
-        o = IrOpts(tol, max_iter, nterms, int(fallback))
+        o = IrOpts(tol, max_iter, nterms, int(fallback), int(gmres), int(panel), 0)
         r = IrReport()
         st = self.lib.mg_dsgesv_ir(self.h, n, nrhs, _ptr(A), ld_of(A), _ptr(B), ld_of(B), _ptr(X), ld_of(X),
                                    C.byref(o), C.byref(r))
         if st not in (0, 6, 7):
             self.check(st, "mg_dsgesv_ir")
-        rep = dict(iterations=r.iterations, path=r.path, info=r.info, backward_error=r.backward_error,
-                   anorm_inf=r.anorm_inf, factor_ms=r.factor_ms, refine_ms=r.refine_ms,
-                   history=[r.history[i] for i in range(min(32, r.iterations + 1))],
+        nh = min(32, r.iterations + 1)
+        rep = dict(iterations=r.iterations, path=r.path, info=r.info, gmres_iterations=r.gmres_iterations,
+                   backward_error=r.backward_error, anorm_inf=r.anorm_inf, factor_ms=r.factor_ms,
+                   refine_ms=r.refine_ms, history=[r.history[i] for i in range(nh)],
                    pivot_growth=r.pivot_growth, status=st)
         return X, rep
 

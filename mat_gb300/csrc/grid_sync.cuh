@@ -18,8 +18,10 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
     return v;
 }
 
-// Returns false (in every thread of the CTA) if the wait timed out.
-__device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target, int* err) {
+// Returns false (in every thread of the CTA) if the wait timed out.  `limit`
+// is the poll budget (the self-test lowers it to make a wait run out).
+__device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target, int* err,
+                                             unsigned limit = kSpinLimit) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -29,7 +31,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target,
             atomicAdd(counter, 1u);
             unsigned spins = 0;
             while (ld_acquire_u32(counter) < target) {
-                if (++spins > kSpinLimit) {
+                if (++spins > limit) {
                     atomicExch(err, 8 /* MG_TIMEOUT */);
                     ok = 0;
                     break;

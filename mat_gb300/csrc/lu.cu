@@ -304,8 +304,8 @@ __global__ void iota_kernel(int* p, int n) {
 // 64 columns: the diagonal block by one CTA, the rows below in parallel.
 constexpr int TRSV_B = 64;
 
-template <typename T>
-__global__ void trsv_lower_diag_kernel(int n, int nrhs, const T* __restrict__ L, int ldl, T* __restrict__ X,
+template <typename TM, typename T>
+__global__ void trsv_lower_diag_kernel(int n, int nrhs, const TM* __restrict__ L, int ldl, T* __restrict__ X,
                                        int ldx, int b0, int b1) {
     // one CTA; threads over rows of the block x rhs
     const int bs = b1 - b0;
@@ -314,15 +314,15 @@ __global__ void trsv_lower_diag_kernel(int n, int nrhs, const T* __restrict__ L,
             const int r = b0 + q % bs, j = q / bs;
             if (r > k) {
                 T* x = X + (size_t)j * ldx;
-                x[r] = fma(L[r + (size_t)k * ldl], -x[k], x[r]);
+                x[r] = fma((T)L[r + (size_t)k * ldl], -x[k], x[r]);
             }
         }
         __syncthreads();
     }
 }
 
-template <typename T>
-__global__ void trsv_lower_update_kernel(int n, int nrhs, const T* __restrict__ L, int ldl, T* __restrict__ X,
+template <typename TM, typename T>
+__global__ void trsv_lower_update_kernel(int n, int nrhs, const TM* __restrict__ L, int ldl, T* __restrict__ X,
                                          int ldx, int b0, int b1) {
     __shared__ T xs[4][TRSV_B];
     const int bs = b1 - b0;
@@ -335,7 +335,7 @@ __global__ void trsv_lower_update_kernel(int n, int nrhs, const T* __restrict__ 
             T acc[4];
             for (int j = 0; j < nj; ++j) acc[j] = X[r + (size_t)(j0 + j) * ldx];
             for (int k = 0; k < bs; ++k) {
-                const T l = L[r + (size_t)(b0 + k) * ldl];
+                const T l = (T)L[r + (size_t)(b0 + k) * ldl];
                 for (int j = 0; j < nj; ++j) acc[j] = fma(l, -xs[j][k], acc[j]);
             }
             for (int j = 0; j < nj; ++j) X[r + (size_t)(j0 + j) * ldx] = acc[j];
@@ -345,26 +345,26 @@ __global__ void trsv_lower_update_kernel(int n, int nrhs, const T* __restrict__ 
 
 // Back substitution, Mat's narrow order (:132-139): for r = n-1..0:
 // x[r] /= U(r,r); x[i] = fma(U(i,r), -x[r], x[i]) for i < r.
-template <typename T>
-__global__ void trsv_upper_diag_kernel(int n, int nrhs, const T* __restrict__ U, int ldu, T* __restrict__ X,
+template <typename TM, typename T>
+__global__ void trsv_upper_diag_kernel(int n, int nrhs, const TM* __restrict__ U, int ldu, T* __restrict__ X,
                                        int ldx, int b0, int b1) {
     const int bs = b1 - b0;
     for (int r = b1 - 1; r >= b0; --r) {
-        for (int j = threadIdx.x; j < nrhs; j += blockDim.x) X[r + (size_t)j * ldx] /= U[r + (size_t)r * ldu];
+        for (int j = threadIdx.x; j < nrhs; j += blockDim.x) X[r + (size_t)j * ldx] /= (T)U[r + (size_t)r * ldu];
         __syncthreads();
         for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) {
             const int i = b0 + q % bs, j = q / bs;
             if (i < r) {
                 T* x = X + (size_t)j * ldx;
-                x[i] = fma(U[i + (size_t)r * ldu], -x[r], x[i]);
+                x[i] = fma((T)U[i + (size_t)r * ldu], -x[r], x[i]);
             }
         }
         __syncthreads();
     }
 }
 
-template <typename T>
-__global__ void trsv_upper_update_kernel(int n, int nrhs, const T* __restrict__ U, int ldu, T* __restrict__ X,
+template <typename TM, typename T>
+__global__ void trsv_upper_update_kernel(int n, int nrhs, const TM* __restrict__ U, int ldu, T* __restrict__ X,
                                          int ldx, int b0, int b1) {
     __shared__ T xs[4][TRSV_B];
     const int bs = b1 - b0;
@@ -377,7 +377,7 @@ __global__ void trsv_upper_update_kernel(int n, int nrhs, const T* __restrict__ 
             T acc[4];
             for (int j = 0; j < nj; ++j) acc[j] = X[i + (size_t)(j0 + j) * ldx];
             for (int k = bs - 1; k >= 0; --k) {
-                const T u = U[i + (size_t)(b0 + k) * ldu];
+                const T u = (T)U[i + (size_t)(b0 + k) * ldu];
                 for (int j = 0; j < nj; ++j) acc[j] = fma(u, -xs[j][k], acc[j]);
             }
             for (int j = 0; j < nj; ++j) X[i + (size_t)(j0 + j) * ldx] = acc[j];
@@ -435,13 +435,14 @@ static GetrfCtx<T> carve(void* base, int num_sms, int nbmax = PANEL_MAX_NB) {
     return c;
 }
 
+// The cooperative panel keeps an R x nb slab in the shared memory of P CTAs
+// (one CTA up to 64 KiB of slab, else P = min(SMs, ceil(R / 128))); it
+// fits when each CTA's ceil(R / P) rows x nb fit its opt-in shared memory.
 template <typename T>
-static mg_status_t launch_panel(mg_handle_t h, GetrfCtx<T>& c, T* A, int lda, int m, int r0, int nb, int* pos,
-                                int nopiv = 0) {
-    const int R = m - r0;
-    auto kern = panel_kernel<T>;
+static cudaError_t panel_geometry(const mg_handle_s* h, int R, int nb, int* P_out, int* rpc_out, bool* fits) {
     cudaFuncAttributes fa;
-    MG_CHECK_CUDA(h, cudaFuncGetAttributes(&fa, kern));
+    const cudaError_t e = cudaFuncGetAttributes(&fa, panel_kernel<T>);
+    if (e != cudaSuccess) return e;
     const size_t cap = (size_t)h->max_smem_optin - fa.sharedSizeBytes - 256;
     int P;
     if ((size_t)R * nb * sizeof(T) <= 64 * 1024) {
@@ -450,8 +451,21 @@ static mg_status_t launch_panel(mg_handle_t h, GetrfCtx<T>& c, T* A, int lda, in
         P = (R + 127) / 128;
         if (P > h->num_sms) P = h->num_sms;
     }
-    int rpc = (R + P - 1) / P;
-    if ((size_t)rpc * nb * sizeof(T) > cap) {
+    *P_out = P;
+    *rpc_out = (R + P - 1) / P;
+    *fits = (size_t)*rpc_out * nb * sizeof(T) <= cap;
+    return cudaSuccess;
+}
+
+template <typename T>
+static mg_status_t launch_panel(mg_handle_t h, GetrfCtx<T>& c, T* A, int lda, int m, int r0, int nb, int* pos,
+                                int nopiv = 0) {
+    const int R = m - r0;
+    auto kern = panel_kernel<T>;
+    int P = 1, rpc = R;
+    bool fits = false;
+    MG_CHECK_CUDA(h, panel_geometry<T>(h, R, nb, &P, &rpc, &fits));
+    if (!fits) {
         return fail(h, MG_ERR_UNSUPPORTED, "panel of %d rows x %d columns exceeds shared memory of %d CTAs", R, nb,
                     h->num_sms);
     }
@@ -776,6 +790,38 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
     return MG_OK;
 }
 
+// Mat's narrow substitutions (LU/__Solve_direct.h:118-139) on in-place
+// factors of element type TM, in FP64: blocks of TRSV_B rows, the block's
+// triangle on one CTA, the rows outside it by a grid.
+template <typename TM>
+static mg_status_t narrow_subst(mg_handle_t h, int n, int nrhs, const TM* LU, int lda, double* X, int ldx) {
+    const int ublocks = h->num_sms;
+    for (int b0 = 0; b0 < n; b0 += TRSV_B) {
+        const int b1 = b0 + TRSV_B < n ? b0 + TRSV_B : n;
+        trsv_lower_diag_kernel<TM, double><<<1, 256, 0, h->stream>>>(n, nrhs, LU, lda, X, ldx, b0, b1);
+        MG_TRY(post_launch(h, "trsv_lower_diag_kernel"));
+        if (b1 < n) {
+            int blocks = (n - b1 + 127) / 128;
+            if (blocks > ublocks) blocks = ublocks;
+            trsv_lower_update_kernel<TM, double><<<blocks, 128, 0, h->stream>>>(n, nrhs, LU, lda, X, ldx, b0, b1);
+            MG_TRY(post_launch(h, "trsv_lower_update_kernel"));
+        }
+    }
+    const int last = ((n - 1) / TRSV_B) * TRSV_B;
+    for (int b0 = last; b0 >= 0; b0 -= TRSV_B) {
+        const int b1 = b0 + TRSV_B < n ? b0 + TRSV_B : n;
+        trsv_upper_diag_kernel<TM, double><<<1, 256, 0, h->stream>>>(n, nrhs, LU, lda, X, ldx, b0, b1);
+        MG_TRY(post_launch(h, "trsv_upper_diag_kernel"));
+        if (b0 > 0) {
+            int blocks = (b0 + 127) / 128;
+            if (blocks > ublocks) blocks = ublocks;
+            trsv_upper_update_kernel<TM, double><<<blocks, 128, 0, h->stream>>>(n, nrhs, LU, lda, X, ldx, b0, b1);
+            MG_TRY(post_launch(h, "trsv_upper_update_kernel"));
+        }
+    }
+    return MG_OK;
+}
+
 // X := A^{-1} B given the in-place factors, pos from dgetrf_impl, in the
 // operation order of Mat's Solve_direct (LU/__Solve_direct.h:146-220):
 //  * nrhs <= 4: the narrow scalar substitutions (:112-139);
@@ -820,31 +866,23 @@ mg_status_t dgetrs_impl(mg_handle_t h, int n, int nrhs, const double* LU, int ld
         }
         return MG_OK;
     }
-    const int ublocks = h->num_sms;
-    for (int b0 = 0; b0 < n; b0 += TRSV_B) {
-        const int b1 = b0 + TRSV_B < n ? b0 + TRSV_B : n;
-        trsv_lower_diag_kernel<double><<<1, 256, 0, h->stream>>>(n, nrhs, LU, lda, X, ldx, b0, b1);
-        MG_TRY(post_launch(h, "trsv_lower_diag_kernel"));
-        if (b1 < n) {
-            int blocks = (n - b1 + 127) / 128;
-            if (blocks > ublocks) blocks = ublocks;
-            trsv_lower_update_kernel<double><<<blocks, 128, 0, h->stream>>>(n, nrhs, LU, lda, X, ldx, b0, b1);
-            MG_TRY(post_launch(h, "trsv_lower_update_kernel"));
-        }
-    }
-    const int last = ((n - 1) / TRSV_B) * TRSV_B;
-    for (int b0 = last; b0 >= 0; b0 -= TRSV_B) {
-        const int b1 = b0 + TRSV_B < n ? b0 + TRSV_B : n;
-        trsv_upper_diag_kernel<double><<<1, 256, 0, h->stream>>>(n, nrhs, LU, lda, X, ldx, b0, b1);
-        MG_TRY(post_launch(h, "trsv_upper_diag_kernel"));
-        if (b0 > 0) {
-            int blocks = (b0 + 127) / 128;
-            if (blocks > ublocks) blocks = ublocks;
-            trsv_upper_update_kernel<double><<<blocks, 128, 0, h->stream>>>(n, nrhs, LU, lda, X, ldx, b0, b1);
-            MG_TRY(post_launch(h, "trsv_upper_update_kernel"));
-        }
-    }
-    return MG_OK;
+    return narrow_subst<double>(h, n, nrhs, LU, lda, X, ldx);
+}
+
+// X := (LU)^{-1} P B in FP64 arithmetic for factors held in fp32 (the mixed
+// LU's, whose pos follows Mat's convention): the same narrow substitution
+// kernels with each fp32 factor entry widened exactly to fp64.  This is a
+// fixed linear operator M^{-1}, M = P^T L U, as GMRES-IR's preconditioner
+// needs.
+mg_status_t lu_solve_f32_factors(mg_handle_t h, int n, int nrhs, const float* LU, int lda, const int* pos,
+                                 const double* B, int ldb, double* X, int ldx) {
+    if (n == 0 || nrhs == 0) return MG_OK;
+    const size_t total = (size_t)n * nrhs;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > h->num_sms * 8) blocks = h->num_sms * 8;
+    permute_rows_kernel<double><<<blocks, 256, 0, h->stream>>>(n, nrhs, pos, B, ldb, X, ldx);
+    MG_TRY(post_launch(h, "permute_rows_kernel"));
+    return narrow_subst<float>(h, n, nrhs, LU, lda, X, ldx);
 }
 
 // ------------------------------------------------ allocation-free variant
@@ -962,6 +1000,13 @@ mg_status_t mg_dgetrf_noalloc(void* cuda_stream, int m, int n, double* A, int ld
         cudaDeviceGetAttribute(&h.max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
         return MG_ERR_CUDA;
     if (h.num_sms > mg::kNoAllocMaxSms) return MG_ERR_UNSUPPORTED;
+    // the first (tallest) panel decides whether the slab fits: refuse before any launch
+    const int s = m < n ? m : n;
+    int P = 1, rpc = m;
+    bool fits = false;
+    if (mg::panel_geometry<double>(&h, m, s <= LU_BS * 3 / 2 ? s : LU_BS, &P, &rpc, &fits) != cudaSuccess)
+        return MG_ERR_CUDA;
+    if (!fits) return MG_ERR_UNSUPPORTED;
     mg::GetrfCtx<double> c = mg::carve<double>(scratch, h.num_sms, mg::kNoAllocMaxNb);
     int hstat[2] = {0, 0};
     return mg::dgetrf_run(&h, m, n, A, lda, pos, c, hstat, info);

@@ -99,6 +99,9 @@ mg_status_t dgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, in
 
 // In-place FP64 Mat PLU and narrow solve (lu.cu).
 mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* pos, int* info_out);
+// X := (P^T L U)^{-1} B in FP64 for the mixed LU's fp32 in-place factors (lu.cu).
+mg_status_t lu_solve_f32_factors(mg_handle_t h, int n, int nrhs, const float* LU, int lda, const int* pos,
+                                 const double* B, int ldb, double* X, int ldx);
 mg_status_t dgetrs_impl(mg_handle_t h, int n, int nrhs, const double* LU, int lda, const int* pos,
                         const double* B, int ldb, double* X, int ldx);
 // Device workspace dgetrf_impl uses at the start of h->ws (callers place

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <optional>
 #include <vector>
 
 #include "grid_sync.cuh"
@@ -220,6 +221,89 @@ __global__ void update_x_kernel(int n, int nrhs, const float* __restrict__ D, co
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const int i = (int)(e % n), j = (int)(e / n);
         X[i + (size_t)j * ldx] += scale[j] * (double)D[e];
+    }
+}
+
+// ---------------------------------------------------------------- GMRES-IR
+// GMRES for the correction equation A d = r, left-preconditioned by the fp32
+// factors (M = P^T L U applied in FP64), one Krylov basis per right-hand
+// side, all columns advancing in lockstep.  Basis vectors are stored
+// [k][j][i] (vector k of column j, row i), so vector k of every column is an
+// n x nrhs block with leading dimension n, the residual kernel's X layout.
+constexpr int GM_RESTART = 40;   // Krylov vectors per correction (no restart)
+constexpr int GM_CTAS = 64;      // CTAs of the Gram-Schmidt dot products
+constexpr int GM_THREADS = 256;
+
+// Y(:, j) = sum over the k chunks of partial (A V in FP64, fixed order)
+__global__ void matvec_reduce_kernel(const double* __restrict__ partial, int nchunks, int n, int nrhs,
+                                     double* __restrict__ Y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int j = 0; j < nrhs; ++j) {
+        double s = 0.0;
+        for (int c = 0; c < nchunks; ++c) s += partial[((size_t)c * nrhs + j) * n + i];
+        Y[i + (size_t)j * n] = s;
+    }
+}
+
+// partial[cta][q], q = k * nrhs + j < nv * nrhs: this CTA's share of
+// V_k(:, j) . W(:, j), summed in a fixed order (each thread its strided rows,
+// then a butterfly over the warp, then the warps in order): deterministic.
+__global__ void __launch_bounds__(GM_THREADS) gs_dots_kernel(int n, int nv, int nrhs, const double* __restrict__ V,
+                                                             const double* __restrict__ W,
+                                                             double* __restrict__ partial, int pstride) {
+    __shared__ double ws[GM_THREADS / 32];
+    const int chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int q = 0; q < nv * nrhs; ++q) {
+        const int k = q / nrhs, j = q - k * nrhs;
+        const double* v = V + ((size_t)k * nrhs + j) * n;
+        const double* x = W + (size_t)j * n;
+        double acc = 0.0;
+        for (int i = lo + threadIdx.x; i < hi; i += GM_THREADS) acc = fma(v[i], x[i], acc);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+        if (lane == 0) ws[warp] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int u = 0; u < GM_THREADS / 32; ++u) t += ws[u];
+            partial[(size_t)blockIdx.x * pstride + q] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// W(:, j) -= sum_{k < nv} c[k][j] V_k(:, j)
+__global__ void gs_update_kernel(int n, int nv, int nrhs, const double* __restrict__ V, const double* __restrict__ c,
+                                 double* __restrict__ W) {
+    const size_t total = (size_t)n * nrhs;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % n), j = (int)(e / n);
+        double acc = W[e];
+        for (int k = 0; k < nv; ++k) acc = fma(-c[k * nrhs + j], V[((size_t)k * nrhs + j) * n + i], acc);
+        W[e] = acc;
+    }
+}
+
+// Vout(:, j) = W(:, j) * inv[j]
+__global__ void gs_scale_kernel(int n, int nrhs, const double* __restrict__ W, const double* __restrict__ inv,
+                                double* __restrict__ Vout) {
+    const size_t total = (size_t)n * nrhs;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
+        Vout[e] = W[e] * inv[e / n];
+}
+
+// X(:, j) += sum_{k < nv} y[k][j] V_k(:, j)
+__global__ void gm_update_x_kernel(int n, int nv, int nrhs, const double* __restrict__ V, const double* __restrict__ y,
+                                   double* __restrict__ X, int ldx) {
+    const size_t total = (size_t)n * nrhs;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % n), j = (int)(e / n);
+        double acc = X[i + (size_t)j * ldx];
+        for (int k = 0; k < nv; ++k) acc = fma(y[k * nrhs + j], V[((size_t)k * nrhs + j) * n + i], acc);
+        X[i + (size_t)j * ldx] = acc;
     }
 }
 
@@ -563,6 +647,10 @@ struct IrWs {
     double* norms;  // [0..8) rnorm, [8..16) xnorm, [16] anorm, [24..32) scale
     float* Y;
     float* Z;
+    double* gV;     // GMRES basis, (GM_RESTART + 1) x nrhs x n
+    double* gW;     // n x nrhs
+    double* gP;     // Gram-Schmidt partial sums, GM_CTAS x (GM_RESTART + 1) x nrhs
+    double* gC;     // coefficients for the device, (GM_RESTART + 1) x nrhs
 };
 
 size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
@@ -590,6 +678,10 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
     const size_t oF = take(2 * (size_t)nblk * sizeof(unsigned));
     const size_t oY = take((size_t)n * nrhs * sizeof(float));
     const size_t oZ = take((size_t)n * nrhs * sizeof(float));
+    const size_t ogV = take((size_t)(GM_RESTART + 1) * nrhs * n * sizeof(double));
+    const size_t ogW = take((size_t)n * nrhs * sizeof(double));
+    const size_t ogP = take((size_t)GM_CTAS * (GM_RESTART + 1) * nrhs * sizeof(double));
+    const size_t ogC = take((size_t)(GM_RESTART + 1) * nrhs * sizeof(double));
     if (w) {
         char* b = (char*)h->ws;
         w->A32 = (float*)(b + oA);
@@ -607,6 +699,10 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
         w->flags = (unsigned*)(b + oF);
         w->Y = (float*)(b + oY);
         w->Z = (float*)(b + oZ);
+        w->gV = (double*)(b + ogV);
+        w->gW = (double*)(b + ogW);
+        w->gP = (double*)(b + ogP);
+        w->gC = (double*)(b + ogC);
     }
     return off;
 }
@@ -628,7 +724,7 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
         ldx < (n > 1 ? n : 1))
         return mg::fail(h, MG_ERR_ARG, "mg_dsgesv_ir: bad arguments (n=%d nrhs=%d, nrhs must be <= %d)", n, nrhs,
                         MAX_RHS);
-    mg_ir_opts o = {1e-14, 30, 3, 1};
+    mg_ir_opts o = {1e-14, 30, 3, 1, 1, 0, 0};
     if (opts) o = *opts;
     if (o.nterms < 1 || o.nterms > 3) return mg::fail(h, MG_ERR_ARG, "mg_dsgesv_ir: nterms must be 1..3");
     if (o.max_iter < 1) o.max_iter = 1;
@@ -642,7 +738,7 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
 
     const auto t0 = clk::now();
     MG_TRY(mg::ensure_ws(h, carve_ir(h, n, nrhs, o.nterms, nullptr)));
-    MG_TRY(mg::ensure_hws(h, 512));
+    MG_TRY(mg::ensure_hws(h, 512 + sizeof(double) * GM_CTAS * (GM_RESTART + 1) * MAX_RHS));
     IrWs w;
     carve_ir(h, n, nrhs, o.nterms, &w);
     cudaStream_t st = h->stream;
@@ -652,7 +748,8 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     double* hn = (double*)h->hws;
 
     // ||A||_inf and ||B||_inf (column-wise) --------------------------------
-    mg::ProfScope* setup = new mg::ProfScope(h, "ir_setup", 0.0, 12.0 * n * (double)n);
+    std::optional<mg::ProfScope> setup;  // closed (its events recorded and released) on every return path
+    setup.emplace(h, "ir_setup", 0.0, 12.0 * n * (double)n);
     MG_CHECK_CUDA(h, cudaMemsetAsync(w.gemm_err, 0, 64, st));
     MG_CHECK_CUDA(h, cudaMemsetAsync(w.norms, 0, 64 * sizeof(double), st));
     // fp32 copy and the row sums of |A| (one pass), then ||A||_inf
@@ -668,7 +765,7 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     }
     absrow_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kd2s, n, w.norms + 16);
     MG_TRY(mg::post_launch(h, "absrow_reduce_kernel"));
-    delete setup;
+    setup.reset();
 
     // mixed LU ---------------------------------------------------------------
     int info = 0;
@@ -709,31 +806,32 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     r.factor_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
 
     // refinement --------------------------------------------------------------
-    // x = 0, so the first residual is b itself
-    MG_CHECK_CUDA(h, cudaMemset2DAsync(X, (size_t)ldx * sizeof(double), 0, (size_t)n * sizeof(double), nrhs, st));
-    double bnorm[MAX_RHS] = {0};
-    double prev_eta = INFINITY;
-    int slow = 0;
-    bool converged = false;
-    for (int it = 0; it <= o.max_iter; ++it) {
-        MG_CHECK_CUDA(h, cudaMemsetAsync(w.norms, 0, 16 * sizeof(double), st));
-        mg::ProfScope* pr = new mg::ProfScope(h, "ir_residual", it ? 2.0 * n * (double)n * nrhs : 0.0,
-                                              it ? 8.0 * n * (double)n : 0.0);
-        if (it > 0) {  // at it = 0, x = 0 and r = b: only the reduction pass below (zero chunks)
-            const dim3 grid((n + RES_ROWS - 1) / RES_ROWS, kch);
-            switch (nrhs) {
+    const dim3 rgrid((n + RES_ROWS - 1) / RES_ROWS, kch);
+    // partial sums of A V (V n x nrhs, ld ldv) in w.partial, fp64 FMA
+    auto launch_av = [&](const double* V, int ldv) -> mg_status_t {
+        switch (nrhs) {
 #define MG_RES(NRV) \
-    case NRV: residual_partial_kernel<NRV><<<grid, RES_ROWS, 0, st>>>(A, lda, n, X, ldx, w.partial); break;
-                MG_RES(1) MG_RES(2) MG_RES(3) MG_RES(4) MG_RES(5) MG_RES(6) MG_RES(7)
-                default: residual_partial_kernel<8><<<grid, RES_ROWS, 0, st>>>(A, lda, n, X, ldx, w.partial); break;
+    case NRV: residual_partial_kernel<NRV><<<rgrid, RES_ROWS, 0, st>>>(A, lda, n, V, ldv, w.partial); break;
+            MG_RES(1) MG_RES(2) MG_RES(3) MG_RES(4) MG_RES(5) MG_RES(6) MG_RES(7)
+            default: residual_partial_kernel<8><<<rgrid, RES_ROWS, 0, st>>>(A, lda, n, V, ldv, w.partial); break;
 #undef MG_RES
-            }
-            MG_TRY(mg::post_launch(h, "residual_partial_kernel"));
         }
-        residual_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, it ? kch : 0, n, nrhs, B, ldb, X, ldx,
-                                                               w.R, w.norms);
-        MG_TRY(mg::post_launch(h, "residual_reduce_kernel"));
-        delete pr;
+        return mg::post_launch(h, "residual_partial_kernel");
+    };
+    double bnorm[MAX_RHS] = {0};
+    int nres = 0;  // residuals evaluated (plain and GMRES-IR steps): the history index
+    // r = b - A x in fp64 (x_zero: x = 0, r = b) and the max-over-columns
+    // normwise backward error; also checks the device error words
+    auto residual = [&](bool x_zero, double* eta_out) -> mg_status_t {
+        MG_CHECK_CUDA(h, cudaMemsetAsync(w.norms, 0, 16 * sizeof(double), st));
+        {
+            mg::ProfScope pr(h, "ir_residual", x_zero ? 0.0 : 2.0 * n * (double)n * nrhs,
+                             x_zero ? 0.0 : 8.0 * n * (double)n);
+            if (!x_zero) MG_TRY(launch_av(X, ldx));
+            residual_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, x_zero ? 0 : kch, n, nrhs, B, ldb, X,
+                                                                   ldx, w.R, w.norms);
+            MG_TRY(mg::post_launch(h, "residual_reduce_kernel"));
+        }
         MG_CHECK_CUDA(h, cudaMemcpyAsync(hn, w.norms, 32 * sizeof(double), cudaMemcpyDeviceToHost, st));
         int* herr = (int*)(hn + 48);  // device error words: split GEMM, triangular solves
         MG_CHECK_CUDA(h, cudaMemcpyAsync(herr, w.gemm_err, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -744,7 +842,7 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
         const double anorm = hn[16];
         double eta = 0.0;
         for (int j = 0; j < nrhs; ++j) {
-            if (it == 0) bnorm[j] = hn[j];  // x = 0: r = b
+            if (x_zero) bnorm[j] = hn[j];  // x = 0: r = b
             const double den = anorm * hn[MAX_RHS + j] + bnorm[j];
             const double e = den > 0 ? hn[j] / den : 0.0;
             eta = std::max(eta, e);
@@ -752,7 +850,20 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
         r.anorm_inf = anorm;
         r.pivot_growth = hn[17] > 0 ? hn[18] / hn[17] : 0.0;
         r.backward_error = eta;
-        if (it < 32) r.history[it] = eta;
+        if (nres < 32) r.history[nres] = eta;
+        ++nres;
+        *eta_out = eta;
+        return MG_OK;
+    };
+
+    // plain refinement: x = 0, so the first residual is b itself
+    MG_CHECK_CUDA(h, cudaMemset2DAsync(X, (size_t)ldx * sizeof(double), 0, (size_t)n * sizeof(double), nrhs, st));
+    double prev_eta = INFINITY;
+    int slow = 0;
+    bool converged = false;
+    for (int it = 0; it <= o.max_iter; ++it) {
+        double eta = 0.0;
+        MG_TRY(residual(it == 0, &eta));
         r.iterations = it;
         if (it > 0 && eta <= o.tol) {
             converged = true;
@@ -767,7 +878,7 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
         // correction: d = U^-1 L^-1 P (r / s), x += s d
         for (int j = 0; j < nrhs; ++j) hn[24 + j] = hn[j];
         MG_CHECK_CUDA(h, cudaMemcpyAsync(w.norms + 24, hn + 24, MAX_RHS * sizeof(double), cudaMemcpyHostToDevice, st));
-        mg::ProfScope* ps = new mg::ProfScope(h, "ir_trsv", 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
+        mg::ProfScope ps(h, "ir_trsv", 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
         prep_rhs_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(n, nrhs, w.pos, w.R, w.norms + 24, w.Y);
         MG_TRY(mg::post_launch(h, "prep_rhs_kernel"));
         int* terr = w.gemm_err + 1;
@@ -785,11 +896,140 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
         }
         update_x_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(n, nrhs, w.Y, w.norms + 24, X, ldx);
         MG_TRY(mg::post_launch(h, "update_x_kernel"));
-        delete ps;
+    }
+
+    // GMRES-IR: each correction A d = r solved by FP64 GMRES left-
+    // preconditioned by the fp32 factors (applied in FP64: the fixed operator
+    // M^{-1}, M = P^T L U), from x = 0.  Needs the factors as factored (the
+    // launch-per-block solves of very large n pre-invert L's and U's block
+    // columns in place).
+    if (!converged && o.gmres && flow) {
+        constexpr int kOuter = 10;
+        constexpr double kInnerTol = 1e-8;
+        const int pstride = (GM_RESTART + 1) * nrhs;
+        double* hp = hn + 64;  // GM_CTAS x pstride partial sums
+        const int egrid = grid_for((size_t)n * nrhs, 256, cap);
+        std::vector<double> H((size_t)nrhs * (GM_RESTART + 1) * GM_RESTART), g((size_t)nrhs * (GM_RESTART + 1)),
+            cs((size_t)nrhs * GM_RESTART), sn((size_t)nrhs * GM_RESTART), beta(nrhs), coef((size_t)pstride);
+        auto Hat = [&](int j, int i, int k) -> double& { return H[((size_t)j * (GM_RESTART + 1) + i) * GM_RESTART + k]; };
+        // host sums (CTAs in order) of V_k(:, j) . Wv(:, j), k < nv -> coef[k * nrhs + j]
+        auto dots = [&](const double* Vb, int nv, const double* Wv) -> mg_status_t {
+            gs_dots_kernel<<<GM_CTAS, GM_THREADS, 0, st>>>(n, nv, nrhs, Vb, Wv, w.gP, pstride);
+            MG_TRY(mg::post_launch(h, "gs_dots_kernel"));
+            MG_CHECK_CUDA(h, cudaMemcpy2DAsync(hp, (size_t)nv * nrhs * sizeof(double), w.gP, pstride * sizeof(double),
+                                               (size_t)nv * nrhs * sizeof(double), GM_CTAS, cudaMemcpyDeviceToHost,
+                                               st));
+            MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
+            for (int q = 0; q < nv * nrhs; ++q) {
+                double t = 0.0;
+                for (int c = 0; c < GM_CTAS; ++c) t += hp[(size_t)c * nv * nrhs + q];
+                coef[q] = t;
+            }
+            return MG_OK;
+        };
+        auto upload = [&](int count) -> mg_status_t {  // coef[0 .. count) -> w.gC
+            MG_CHECK_CUDA(h, cudaMemcpyAsync(w.gC, coef.data(), (size_t)count * sizeof(double),
+                                             cudaMemcpyHostToDevice, st));
+            return MG_OK;
+        };
+        MG_CHECK_CUDA(h, cudaMemset2DAsync(X, (size_t)ldx * sizeof(double), 0, (size_t)n * sizeof(double), nrhs, st));
+        prev_eta = INFINITY;
+        slow = 0;
+        for (int ot = 0; ot < kOuter; ++ot) {
+            double eta = 0.0;
+            MG_TRY(residual(ot == 0, &eta));
+            r.iterations += 1;
+            if (eta <= o.tol) {
+                converged = true;
+                r.path = 1;
+                break;
+            }
+            if (ot > 1) {
+                slow = eta > 0.5 * prev_eta ? slow + 1 : 0;
+                if (slow >= 2) break;
+            }
+            prev_eta = eta;
+            mg::ProfScope pg(h, "gmres", 0.0, 0.0);
+            // V_0 = z / beta, z = M^{-1} r
+            MG_TRY(mg::lu_solve_f32_factors(h, n, nrhs, w.A32, n, w.pos, w.R, n, w.gW, n));
+            MG_TRY(dots(w.gW, 1, w.gW));
+            for (int j = 0; j < nrhs; ++j) {
+                beta[j] = std::sqrt(coef[j]);
+                coef[j] = beta[j] > 0.0 ? 1.0 / beta[j] : 0.0;
+            }
+            MG_TRY(upload(nrhs));
+            gs_scale_kernel<<<egrid, 256, 0, st>>>(n, nrhs, w.gW, w.gC, w.gV);
+            MG_TRY(mg::post_launch(h, "gs_scale_kernel"));
+            std::fill(H.begin(), H.end(), 0.0);
+            std::fill(g.begin(), g.end(), 0.0);
+            for (int j = 0; j < nrhs; ++j) g[(size_t)j * (GM_RESTART + 1)] = beta[j];
+            int kk = 0;
+            for (int k = 0; k < GM_RESTART; ++k) {
+                const double* Vk = w.gV + (size_t)k * nrhs * n;
+                // w = M^{-1} A V_k (A V_k summed into w.R, free until the next residual)
+                MG_TRY(launch_av(Vk, n));
+                matvec_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kch, n, nrhs, w.R);
+                MG_TRY(mg::post_launch(h, "matvec_reduce_kernel"));
+                MG_TRY(mg::lu_solve_f32_factors(h, n, nrhs, w.A32, n, w.pos, w.R, n, w.gW, n));
+                // classical Gram-Schmidt, twice
+                for (int pass = 0; pass < 2; ++pass) {
+                    MG_TRY(dots(w.gV, k + 1, w.gW));
+                    for (int i = 0; i <= k; ++i)
+                        for (int j = 0; j < nrhs; ++j) Hat(j, i, k) += coef[i * nrhs + j];
+                    MG_TRY(upload((k + 1) * nrhs));
+                    gs_update_kernel<<<egrid, 256, 0, st>>>(n, k + 1, nrhs, w.gV, w.gC, w.gW);
+                    MG_TRY(mg::post_launch(h, "gs_update_kernel"));
+                }
+                MG_TRY(dots(w.gW, 1, w.gW));
+                for (int j = 0; j < nrhs; ++j) {
+                    const double hn1 = std::sqrt(coef[j]);
+                    Hat(j, k + 1, k) = hn1;
+                    coef[j] = hn1 > 0.0 ? 1.0 / hn1 : 0.0;
+                }
+                MG_TRY(upload(nrhs));
+                gs_scale_kernel<<<egrid, 256, 0, st>>>(n, nrhs, w.gW, w.gC, w.gV + (size_t)(k + 1) * nrhs * n);
+                MG_TRY(mg::post_launch(h, "gs_scale_kernel"));
+                // Givens rotations of column k of each column's Hessenberg matrix
+                bool done = true;
+                for (int j = 0; j < nrhs; ++j) {
+                    double* cj = cs.data() + (size_t)j * GM_RESTART;
+                    double* sj = sn.data() + (size_t)j * GM_RESTART;
+                    double* gj = g.data() + (size_t)j * (GM_RESTART + 1);
+                    for (int i = 0; i < k; ++i) {
+                        const double t = cj[i] * Hat(j, i, k) + sj[i] * Hat(j, i + 1, k);
+                        Hat(j, i + 1, k) = -sj[i] * Hat(j, i, k) + cj[i] * Hat(j, i + 1, k);
+                        Hat(j, i, k) = t;
+                    }
+                    const double a0 = Hat(j, k, k), b0 = Hat(j, k + 1, k), rho = std::hypot(a0, b0);
+                    cj[k] = rho > 0.0 ? a0 / rho : 1.0;
+                    sj[k] = rho > 0.0 ? b0 / rho : 0.0;
+                    Hat(j, k, k) = rho;
+                    Hat(j, k + 1, k) = 0.0;
+                    gj[k + 1] = -sj[k] * gj[k];
+                    gj[k] = cj[k] * gj[k];
+                    if (std::fabs(gj[k + 1]) > kInnerTol * beta[j]) done = false;
+                }
+                kk = k + 1;
+                if (done) break;
+            }
+            // y = H(0:kk, 0:kk)^{-1} g(0:kk) per column; x += V y
+            for (int j = 0; j < nrhs; ++j) {
+                const double* gj = g.data() + (size_t)j * (GM_RESTART + 1);
+                for (int i = kk - 1; i >= 0; --i) {
+                    double t = gj[i];
+                    for (int l = i + 1; l < kk; ++l) t -= Hat(j, i, l) * coef[l * nrhs + j];
+                    coef[i * nrhs + j] = Hat(j, i, i) != 0.0 ? t / Hat(j, i, i) : 0.0;
+                }
+            }
+            MG_TRY(upload(kk * nrhs));
+            gm_update_x_kernel<<<egrid, 256, 0, st>>>(n, kk, nrhs, w.gV, w.gC, X, ldx);
+            MG_TRY(mg::post_launch(h, "gm_update_x_kernel"));
+            r.gmres_iterations += kk;
+        }
     }
     const auto t2 = clk::now();
     r.refine_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
-    mg_status_t result = MG_OK;
+    mg_status_t result = converged && r.path == 1 ? MG_FALLBACK_USED : MG_OK;
     if (!converged) {
         if (o.fallback) {
             int finfo = 0;

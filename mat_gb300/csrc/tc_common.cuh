@@ -37,10 +37,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait on phase `parity`; returns false after ~kWaitLimit polls.
+// Bounded wait on phase `parity`; returns false after `limit` polls
+// (~kWaitLimit by default; the self-test lowers it to make a wait run out).
 constexpr uint32_t kWaitLimit = 1u << 26;
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitLimit; ++i) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = kWaitLimit) {
+    for (uint32_t i = 0; i < limit; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
         if (i > 1024) __nanosleep(32);
     }

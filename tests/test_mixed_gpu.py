@@ -56,17 +56,35 @@ def test_mixed_ir_reaches_fp64_backward_error(handle, n, nrhs):
 
 def test_mixed_ir_fallback_when_refinement_stalls(handle):
     # one bf16 term (8-bit products) cannot reach 1e-14 at condition 1e6:
-    # refinement stalls and the solve falls back to the FP64 path
+    # plain refinement stalls; with GMRES-IR off the FP64 fallback takes over
     n = 512
     A = svd_matrix(handle, n)
     B = colmajor(n, 2)
     handle.fill_normal(B, 12)
-    X, rep = handle.dsgesv_ir(A, B, nterms=1, max_iter=6)
+    X, rep = handle.dsgesv_ir(A, B, nterms=1, max_iter=6, gmres=False)
     torch.cuda.synchronize()
+    assert rep["status"] == 7 and rep["path"] == 2, rep  # MG_FALLBACK_USED, FP64 path
     a, b, x = A.cpu().numpy(), B.cpu().numpy(), X.cpu().numpy()
     assert backward_error(a, x, b) <= 1e-14
-    if rep["path"] == 2:
-        assert rep["status"] == 7  # MG_FALLBACK_USED
-    # and with the fallback disabled it reports the stall instead
-    X2, rep2 = handle.dsgesv_ir(A, B, nterms=1, max_iter=2, fallback=False)
-    assert rep2["status"] in (0, 6)
+    # and with every takeover disabled it reports the stall instead
+    X2, rep2 = handle.dsgesv_ir(A, B, nterms=1, max_iter=6, fallback=False, gmres=False)
+    assert rep2["status"] == 6 and rep2["backward_error"] > 1e-14, rep2  # MG_IR_STALLED
+
+
+@pytest.mark.parametrize("n,sigma_min", [(2048, 1e-9), (4096, 1e-9)])
+def test_gmres_ir_beyond_plain_refinement(handle, n, sigma_min):
+    """At condition 1e9 plain refinement with the fp32 factors stalls; GMRES-IR
+    (FP64 GMRES preconditioned by the same factors) reaches 1e-14 and reports
+    path 1, with no FP64 refactorization."""
+    A = svd_matrix(handle, n, seed=7, sigma_min=sigma_min)
+    B = colmajor(n, 4)
+    handle.fill_normal(B, 13)
+    a, b = A.cpu().numpy(), B.cpu().numpy()
+    Xp, rp = handle.dsgesv_ir(A, B, fallback=False, gmres=False)
+    torch.cuda.synchronize()
+    assert rp["status"] == 6, rp  # plain refinement alone does not get there
+    X, rep = handle.dsgesv_ir(A, B, fallback=False, gmres=True)
+    torch.cuda.synchronize()
+    assert rep["status"] == 7 and rep["path"] == 1 and rep["gmres_iterations"] > 0, rep
+    eta = backward_error(a, X.cpu().numpy(), b)
+    assert eta <= 1e-14, (eta, rep)
