@@ -292,6 +292,22 @@ typedef struct mg_ir_report {
 mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
                          int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* report);
 
+/* Mixed-precision solve for symmetric positive definite A (no mixed
+ * precision in Mat; the FP64 counterpart is Mat's LLT, Mat-8.3.1/LU/__LLT.h:
+ * 94-150, with the Cholesky solve): fp32 Cholesky of A's lower triangle in
+ * blocks of 96 columns (fp32 diagonal blocks and block-column solves, the
+ * trailing updates C -= L21 L21^T on the split-BF16 tensor cores, fp32
+ * accumulation), its factor rewritten as the LU of the same matrix
+ * (L D^-1)(D L^T), D = diag(L), then the refinement of mg_dsgesv_ir:
+ * FP64 residuals with all of A (both triangles: pass the full symmetric
+ * matrix), GMRES-IR, FP64 fallback (mg_dgesv).  If the fp32 Cholesky breaks
+ * down (a non-positive pivot, possible for nearly singular A) the solve
+ * goes straight to the FP64 fallback (MG_FALLBACK_USED, path 2), or returns
+ * MG_NOT_SPD with report.info when fallback is off.  opts.panel is ignored.
+ * Synchronises. */
+mg_status_t mg_dsposv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
+                         int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* report);
+
 /* ----------------------------------------------- FP32 LU (mixed solve)
  * The single-precision factorizations inside mg_dsgesv_ir, exposed for
  * callers that refine on their own.  No counterpart in Mat (no mixed
@@ -305,6 +321,21 @@ mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double* A, int ld
  * panel of the mixed LU: one 16-CTA thread-block cluster for m <= 16384,
  * a cooperative grid beyond).  Synchronises. */
 mg_status_t mg_sgetf2(mg_handle_t h, int m, int n, float* A, int lda, int* pos, int* info);
+/* mg_sgetf2 with options.  MG_PANEL_TOURNAMENT: tournament pivoting on the
+ * cluster path (Grigori, Demmel & Xiang's CALU, SIAM J. Matrix Anal. Appl.
+ * 2011).  Per 16-column sub-panel the pivot rows are chosen by a reduction
+ * tree of partial-pivoting eliminations, each level passing on the rows it
+ * picked as they were when the sub-panel started: each warp over its own
+ * rows, each CTA over its warps' picks, then (in every CTA alike) pairs of
+ * CTAs and finally all 16 CTAs of the cluster; the 16 pivots are swapped to
+ * the diagonal in order and the sub-panel eliminated without further
+ * pivoting.  One cluster-wide exchange per 16 columns instead of one per
+ * column.  The pivots may differ from partial pivoting's (|L| is no longer
+ * bounded by 1); pos, info and the update order are as for mg_sgetf2.
+ * Panels off the cluster path (m > 16384, or slabs up to 64 KiB) use partial
+ * pivoting. */
+#define MG_PANEL_TOURNAMENT 1
+mg_status_t mg_sgetf2_ex(mg_handle_t h, int flags, int m, int n, float* A, int lda, int* pos, int* info);
 /* mg_sgetrf: in-place blocked LU of an n x n fp32 matrix (blocks of 128:
  * mg_sgetf2 panels, block-row solve and trailing update on the split-BF16
  * tensor-core GEMM with 3 terms, fp32 accumulation).  Synchronises. */

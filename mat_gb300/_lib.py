@@ -62,6 +62,7 @@ SIGNATURES: dict[str, tuple] = {
     "mg_dgetrf": (i32, [vp, i32, i32, vp, i32, vp, pi32]),
     "mg_dgetrf_noalloc": (i32, [vp, i32, i32, vp, i32, vp, pi32]),
     "mg_sgetf2": (i32, [vp, i32, i32, vp, i32, vp, pi32]),
+    "mg_sgetf2_ex": (i32, [vp, i32, i32, i32, vp, i32, vp, pi32]),
     "mg_ddet": (i32, [vp, i32, vp, i32, pf64]),
     "mg_dinv": (i32, [vp, i32, vp, i32, vp, i32, pi32]),
     "mg_dldlt": (i32, [vp, i32, vp, i32, vp, pi32]),
@@ -76,6 +77,7 @@ SIGNATURES: dict[str, tuple] = {
     "mg_sgemm_bf16x_ex": (i32, [vp, i32, i32, i32, i32, i32, f32, vp, i32, vp, i32, f32, vp, i32]),
     "mg_bf16x_check_error": (i32, [vp, pi32]),
     "mg_dsgesv_ir": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, C.POINTER(IrOpts), C.POINTER(IrReport)]),
+    "mg_dsposv_ir": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, C.POINTER(IrOpts), C.POINTER(IrReport)]),
     "mg_gen_svd_matrix": (i32, [vp, i32, vp, i32, u64, i32, f64]),
     "mg_gen_spd_gram": (i32, [vp, i32, vp, i32, u64]),
     "mg_profile_enable": (i32, [vp, i32]),

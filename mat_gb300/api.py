@@ -185,13 +185,15 @@ class Handle:
             self.check(st, "mg_dinv")
         return Ainv, info.value
 
-    def sgetf2(self, A: torch.Tensor, pos: torch.Tensor | None = None):
-        """In-place fp32 panel LU of A (m x n, n <= 128, column-major). Returns (pos, info)."""
+    def sgetf2(self, A: torch.Tensor, pos: torch.Tensor | None = None, tournament: bool = False):
+        """In-place fp32 panel LU of A (m x n, n <= 128, column-major), partial or
+        tournament pivoting. Returns (pos, info)."""
         m, n = A.shape
         if pos is None:
             pos = torch.empty(m, dtype=torch.int32, device=A.device)
         info = C.c_int(0)
-        st = self.lib.mg_sgetf2(self.h, m, n, _ptr(A), ld_of(A), _ptr(pos), C.byref(info))
+        st = self.lib.mg_sgetf2_ex(self.h, 1 if tournament else 0, m, n, _ptr(A), ld_of(A), _ptr(pos),
+                                   C.byref(info))
         if st not in (0, 4):
             self.check(st, "mg_sgetf2")
         return pos, info.value
@@ -207,25 +209,31 @@ class Handle:
             self.check(st, "mg_sgetrf")
         return pos, info.value
 
-    def dsgesv_ir(self, A, B, X=None, tol=1e-14, max_iter=30, nterms=3, fallback=True, gmres=True, panel=0):
+    def dsgesv_ir(self, A, B, X=None, tol=1e-14, max_iter=30, nterms=3, fallback=True, gmres=True, panel=0,
+                  spd=False):
         """Mixed LU (fp32 + split-BF16) + FP64 refinement, GMRES-IR and the FP64
-        fallback when refinement stalls. Returns (X, report dict with the status)."""
+        fallback when refinement stalls; spd=True: the fp32 Cholesky form
+        (mg_dsposv_ir). Returns (X, report dict with the status)."""
         n = A.shape[0]
         nrhs = B.shape[1]
         if X is None:
             X = colmajor(n, nrhs, device=B.device)
         o = IrOpts(tol, max_iter, nterms, int(fallback), int(gmres), int(panel), 0)
         r = IrReport()
-        st = self.lib.mg_dsgesv_ir(self.h, n, nrhs, _ptr(A), ld_of(A), _ptr(B), ld_of(B), _ptr(X), ld_of(X),
-                                   C.byref(o), C.byref(r))
+        fn = self.lib.mg_dsposv_ir if spd else self.lib.mg_dsgesv_ir
+        st = fn(self.h, n, nrhs, _ptr(A), ld_of(A), _ptr(B), ld_of(B), _ptr(X), ld_of(X), C.byref(o), C.byref(r))
         if st not in (0, 6, 7):
-            self.check(st, "mg_dsgesv_ir")
+            self.check(st, "mg_dsposv_ir" if spd else "mg_dsgesv_ir")
         nh = min(32, r.iterations + 1)
         rep = dict(iterations=r.iterations, path=r.path, info=r.info, gmres_iterations=r.gmres_iterations,
                    backward_error=r.backward_error, anorm_inf=r.anorm_inf, factor_ms=r.factor_ms,
                    refine_ms=r.refine_ms, history=[r.history[i] for i in range(nh)],
                    pivot_growth=r.pivot_growth, status=st)
         return X, rep
+
+    def dsposv_ir(self, A, B, X=None, **kw):
+        """Mixed-precision SPD solve (fp32 Cholesky with split-BF16 updates + FP64 refinement)."""
+        return self.dsgesv_ir(A, B, X, spd=True, **kw)
 
     # ------------------------------------------------------------- generators
     def gen_svd_matrix(self, A, seed, nrefl=64, sigma_min=1e-6):

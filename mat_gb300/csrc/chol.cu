@@ -57,30 +57,30 @@ __global__ void llt2_kernel(T* __restrict__ L, int ldl, int k, int col0, int* __
 
 // X (rows x k) := X * Lkk^{-T} (Mat's __Solve_direct_XLT), one thread per row:
 // for j: x_j *= 1/L(j,j); x_kk = fma(x_j, -L(kk,j), x_kk) for kk > j.
-template <typename T>
+template <typename T, int KB = LLT_BS>
 __global__ void xlt_kernel(const T* __restrict__ Ld, int ldl, T* __restrict__ X, int ldx, int rows, int k) {
-    __shared__ T sl[LLT_BS * LLT_BS];
-    __shared__ T sinv[LLT_BS];
+    __shared__ T sl[KB * KB];
+    __shared__ T sinv[KB];
     for (int e = threadIdx.x; e < k * k; e += blockDim.x) sl[e] = Ld[(e % k) + (size_t)(e / k) * ldl];
     __syncthreads();
     for (int j = threadIdx.x; j < k; j += blockDim.x) sinv[j] = T(1) / sl[j + j * k];
     __syncthreads();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= rows) return;
-    T x[LLT_BS];
+    T x[KB];
 #pragma unroll
-    for (int j = 0; j < LLT_BS; ++j) x[j] = j < k ? X[r + (size_t)j * ldx] : T(0);
+    for (int j = 0; j < KB; ++j) x[j] = j < k ? X[r + (size_t)j * ldx] : T(0);
 #pragma unroll
-    for (int j = 0; j < LLT_BS; ++j) {
+    for (int j = 0; j < KB; ++j) {
         if (j < k) {
             x[j] = x[j] * sinv[j];
 #pragma unroll
-            for (int kk = j + 1; kk < LLT_BS; ++kk)
+            for (int kk = j + 1; kk < KB; ++kk)
                 if (kk < k) x[kk] = fma(x[j], -sl[kk + j * k], x[kk]);
         }
     }
 #pragma unroll
-    for (int j = 0; j < LLT_BS; ++j)
+    for (int j = 0; j < KB; ++j)
         if (j < k) X[r + (size_t)j * ldx] = x[j];
 }
 
@@ -226,6 +226,29 @@ __global__ void chol_bwd_update_kernel(int n, int nrhs, const T* __restrict__ L,
     }
 }
 
+// The Cholesky factor L (lower, fp32) rewritten as the packed LU of the same
+// matrix, L L^T = (L D^-1)(D L^T) with D = diag(L), so that the mixed
+// solve's LU refinement applies to it unchanged: pass 1 writes U(r, c) =
+// L(r, r) L(c, r) on and above the diagonal (reading the lower triangle),
+// pass 2 the unit-lower part L(r, c) / L(c, c) below it.  d holds diag(L).
+__global__ void chol_diag_kernel(const float* __restrict__ L, int ldl, int n, float* __restrict__ d) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) d[i] = L[i + (size_t)i * ldl];
+}
+__global__ void chol_to_lu_upper_kernel(float* __restrict__ A, int lda, int n, const float* __restrict__ d) {
+    const size_t total = (size_t)n * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(e % n), c = (int)(e / n);
+        if (r <= c) A[r + (size_t)c * lda] = d[r] * A[c + (size_t)r * lda];
+    }
+}
+__global__ void chol_to_lu_lower_kernel(float* __restrict__ A, int lda, int n, const float* __restrict__ d) {
+    const size_t total = (size_t)n * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(e % n), c = (int)(e / n);
+        if (r > c) A[r + (size_t)c * lda] = A[r + (size_t)c * lda] / d[c];
+    }
+}
+
 }  // namespace
 
 namespace mg {
@@ -315,6 +338,69 @@ template mg_status_t potrf_impl<float>(mg_handle_t, int, float*, int, int*);
 
 mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out) {
     return potrf_impl<double>(h, n, L, ldl, info_out);
+}
+
+// FP32 Cholesky for the mixed SPD solve (no counterpart in Mat, whose LLT,
+// LU/__LLT.h:94-150, is FP64): right-looking, blocks of 96 columns; the
+// diagonal block and the block column below it as in the FP32 Cholesky
+// (llt2_kernel, xlt_kernel), the trailing update C -= L21 L21^T on the
+// tensor cores from one split of L21 (split-BF16, `nterms` terms, fp32
+// accumulation, lower-order products first), which serves as both operands
+// (the B operand's rows are L21's rows).  The update covers the whole
+// trailing square; only its lower triangle is read later.  `split` holds
+// bf16x_split_bytes(n, 96, nterms).  info: first non-positive pivot (the
+// fp32 factorization of an SPD matrix can break down near singularity).
+mg_status_t spotrf_mixed(mg_handle_t h, int n, float* L, int ldl, int nterms, void* split, int* gemm_err,
+                         int* info_out) {
+    constexpr int NB = 96;
+    if (info_out) *info_out = 0;
+    if (n == 0) return MG_OK;
+    MG_TRY(ensure_hws(h, 64));
+    int* dinfo = h->status;
+    cudaStream_t st = h->stream;
+    MG_CHECK_CUDA(h, cudaMemsetAsync(dinfo, 0, sizeof(int), st));
+    const size_t s2 = (size_t)LLT2_MAX * LLT2_MAX * sizeof(float);
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(llt2_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
+    for (int j = 0; j < n; j += NB) {
+        const int nb = n - j < NB ? n - j : NB;
+        float* D = L + j + (size_t)j * ldl;
+        {
+            ProfScope prof(h, "potrf_diag_f32", (double)nb * nb * nb / 3.0, 8.0 * nb * nb);
+            llt2_kernel<float><<<1, 128, s2, st>>>(D, ldl, nb, j, dinfo);
+            MG_TRY(post_launch(h, "llt2_kernel"));
+        }
+        if (j + nb >= n) break;
+        const int rows = n - (j + nb);
+        float* P = L + (j + nb) + (size_t)j * ldl;
+        float* C = L + (j + nb) + (size_t)(j + nb) * ldl;
+        {
+            ProfScope prof(h, "trsm_f32", (double)rows * nb * nb, 8.0 * rows * nb);
+            xlt_kernel<float, NB><<<(rows + 127) / 128, 128, 0, st>>>(D, ldl, P, ldl, rows, nb);
+            MG_TRY(post_launch(h, "xlt_kernel"));
+        }
+        {
+            ProfScope prof(h, "split", 0.0, 2.0 * rows * nb * (4.0 + 2.0 * nterms));
+            MG_TRY(bf16x_split<float>(h, true, P, ldl, rows, nb, nterms, split));
+        }
+        MG_TRY(bf16x_gemm_presplit(h, nterms, rows, rows, nb, -1.0f, split, split, 1.0f, C, ldl, gemm_err, 0, 0, 0,
+                                   true, true));
+    }
+    int* hw = (int*)h->hws;
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
+    if (info_out) *info_out = hw[0];
+    if (hw[0]) return fail(h, MG_NOT_SPD, "spotrf_mixed: non-positive pivot at column %d", hw[0]);
+    return MG_OK;
+}
+
+mg_status_t chol_to_lu_f32(mg_handle_t h, int n, float* A, int lda, float* dscratch) {
+    const int grid = h->num_sms * 8;
+    chol_diag_kernel<<<(n + 255) / 256, 256, 0, h->stream>>>(A, lda, n, dscratch);
+    MG_TRY(post_launch(h, "chol_diag_kernel"));
+    chol_to_lu_upper_kernel<<<grid, 256, 0, h->stream>>>(A, lda, n, dscratch);
+    MG_TRY(post_launch(h, "chol_to_lu_upper_kernel"));
+    chol_to_lu_lower_kernel<<<grid, 256, 0, h->stream>>>(A, lda, n, dscratch);
+    return post_launch(h, "chol_to_lu_lower_kernel");
 }
 
 // In-place Mat LDLT on the lower triangle of L (ld ldl): unit-like lower

@@ -646,10 +646,10 @@ size_t sgetrf_xchg_bytes(int num_sms) { return getrf_ws_bytes<float>(num_sms); }
 // for one CTA's shared memory and fits the cluster; else the cooperative grid
 // (or, for short panels, the single-CTA) kernel.  Same factors either way.
 static mg_status_t launch_panel_f32(mg_handle_t h, GetrfCtx<float>& c, float* A, int lda, int m, int r0, int w,
-                                    int* pos) {
+                                    int* pos, bool tourn = false) {
     const int R = m - r0;
     if ((size_t)R * w * sizeof(float) > 64 * 1024 && R >= w && R <= panel_cluster_rows(h))
-        return sgetf2_cluster(h, A, lda, m, r0, w, pos, c.piv, c.ws.info, c.ws.err);
+        return sgetf2_cluster(h, A, lda, m, r0, w, pos, c.piv, c.ws.info, c.ws.err, tourn);
     return launch_panel<float>(h, c, A, lda, m, r0, w, pos);
 }
 
@@ -676,7 +676,7 @@ static mg_status_t launch_panel_f32(mg_handle_t h, GetrfCtx<float>& c, float* A,
 // solve U12 = L11^{-1} A12 is one FP32 substitution kernel that also writes
 // U12's split terms (bf16x_trsm_split).
 mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int nb, int nterms, void* xchg,
-                         void* splitA, void* splitA2, void* splitB, int* gemm_err, int* info_out) {
+                         void* splitA, void* splitA2, void* splitB, int* gemm_err, int* info_out, bool tourn) {
     if (info_out) *info_out = 0;
     if (n == 0) return MG_OK;
     if (nb > PANEL_MAX_NB || nb > 128) return fail(h, MG_ERR_ARG, "sgetrf_mixed: block size %d > 128", nb);
@@ -694,7 +694,7 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
     // panel k, then everything that depends only on it
     auto panel = [&](int k) -> mg_status_t {
         const int r = k * nb, w = nb < n - r ? nb : n - r;
-        return launch_panel_f32(h, c, A, lda, n, r, w, pos);
+        return launch_panel_f32(h, c, A, lda, n, r, w, pos, tourn);
     };
     // after panel k, on the side stream P (off the critical path): its
     // interchanges on the columns to its left and the split of its L21; the
@@ -932,11 +932,11 @@ mg_status_t mg_dgetrf(mg_handle_t h, int m, int n, double* A, int lda, int* pos,
     return mg::dgetrf_impl(h, m, n, A, lda, pos, info);
 }
 
-mg_status_t mg_sgetf2(mg_handle_t h, int m, int n, float* A, int lda, int* pos, int* info) {
+mg_status_t mg_sgetf2_ex(mg_handle_t h, int flags, int m, int n, float* A, int lda, int* pos, int* info) {
     if (info) *info = 0;
     if (!h) return MG_ERR_ARG;
     if (m < 0 || n < 0 || n > 128 || lda < (m > 1 ? m : 1) || ((size_t)m * n && (!A || !pos)))
-        return mg::fail(h, MG_ERR_ARG, "mg_sgetf2: bad arguments (m=%d n=%d lda=%d, n must be <= 128)", m, n, lda);
+        return mg::fail(h, MG_ERR_ARG, "mg_sgetf2_ex: bad arguments (m=%d n=%d lda=%d, n must be <= 128)", m, n, lda);
     if (m == 0 || n == 0) return MG_OK;
     const int w = n < m ? n : m;
     MG_TRY(mg::ensure_ws(h, mg::getrf_ws_bytes<float>(h->num_sms)));
@@ -945,7 +945,7 @@ mg_status_t mg_sgetf2(mg_handle_t h, int m, int n, float* A, int lda, int* pos, 
     MG_CHECK_CUDA(h, cudaMemsetAsync(c.ws.bar, 0, 256, h->stream));
     iota_kernel<<<(m + 255) / 256, 256, 0, h->stream>>>(pos, m);
     MG_TRY(mg::post_launch(h, "iota_kernel"));
-    MG_TRY(mg::launch_panel_f32(h, c, A, lda, m, 0, w, pos));
+    MG_TRY(mg::launch_panel_f32(h, c, A, lda, m, 0, w, pos, (flags & MG_PANEL_TOURNAMENT) != 0));
     if (w < n) {  // columns right of a short panel (m < n): interchanges only
         MG_TRY(mg::launch_laswp<float>(h, A, lda, 0, w, c.piv, 0, w, n));
     }
@@ -957,6 +957,10 @@ mg_status_t mg_sgetf2(mg_handle_t h, int m, int n, float* A, int lda, int* pos, 
     if (info) *info = hw[1];
     if (hw[1]) return mg::fail(h, MG_SINGULAR, "mg_sgetf2: exactly zero pivot column %d", hw[1]);
     return MG_OK;
+}
+
+mg_status_t mg_sgetf2(mg_handle_t h, int m, int n, float* A, int lda, int* pos, int* info) {
+    return mg_sgetf2_ex(h, 0, m, n, A, lda, pos, info);
 }
 
 mg_status_t mg_sgetrf(mg_handle_t h, int n, float* A, int lda, int* pos, int* info) {

@@ -159,15 +159,23 @@ mg_status_t bf16x_trsm_split(mg_handle_t h, const float* L11, int lda, float* A1
 // FP32 panel on one thread-block cluster (panel_f32.cu): rows it can take
 // (0 if unavailable), and the launch (piv relative to r0; pos updated).
 int panel_cluster_rows(mg_handle_t h);
+// tourn: tournament pivoting (one pivot agreement per 16-column sub-panel,
+// CALU's TSLU over the cluster's CTAs) instead of partial pivoting.
 mg_status_t sgetf2_cluster(mg_handle_t h, float* A, int lda, int m, int r0, int w, int* pos, int* piv, int* info,
-                           int* err);
+                           int* err, bool tourn = false);
 
 // FP32 LU with split-BF16 trailing updates (lu.cu).  splitA and splitA2
 // each hold bf16x_split_bytes(n, nb, nterms) (the L21 split of alternate
 // steps), splitB the same.
 size_t sgetrf_xchg_bytes(int num_sms);
 mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int nb, int nterms, void* xchg,
-                         void* splitA, void* splitA2, void* splitB, int* gemm_err, int* info_out);
+                         void* splitA, void* splitA2, void* splitB, int* gemm_err, int* info_out,
+                         bool tourn = false);
+// FP32 Cholesky with split-BF16 trailing updates for the mixed SPD solve, and
+// the rewrite of its factor as the packed LU of the same matrix (chol.cu).
+mg_status_t spotrf_mixed(mg_handle_t h, int n, float* L, int ldl, int nterms, void* split, int* gemm_err,
+                         int* info_out);
+mg_status_t chol_to_lu_f32(mg_handle_t h, int n, float* A, int lda, float* dscratch);
 // Side stream and events of the look-ahead LU (created once per handle).
 mg_status_t ensure_lookahead(mg_handle_t h);
 

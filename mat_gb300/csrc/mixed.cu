@@ -716,17 +716,24 @@ int grid_for(size_t total, int threads, int cap) {
 
 }  // namespace
 
-extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
-                                    int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* rep) {
+static __global__ void pos_iota_kernel(int* pos, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) pos[i] = i;
+}
+
+// The mixed solve: the fp32 factorization (LU with partial or tournament
+// pivoting; for spd, Cholesky rewritten as the packed LU of the same
+// matrix), then plain refinement, GMRES-IR and the FP64 fallback.
+static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B, int ldb,
+                               double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* rep, bool spd) {
     using clk = std::chrono::steady_clock;
     if (!h) return MG_ERR_ARG;
     if (n < 0 || nrhs < 0 || nrhs > MAX_RHS || lda < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1) ||
         ldx < (n > 1 ? n : 1))
-        return mg::fail(h, MG_ERR_ARG, "mg_dsgesv_ir: bad arguments (n=%d nrhs=%d, nrhs must be <= %d)", n, nrhs,
+        return mg::fail(h, MG_ERR_ARG, "mixed solve: bad arguments (n=%d nrhs=%d, nrhs must be <= %d)", n, nrhs,
                         MAX_RHS);
     mg_ir_opts o = {1e-14, 30, 3, 1, 1, 0, 0};
     if (opts) o = *opts;
-    if (o.nterms < 1 || o.nterms > 3) return mg::fail(h, MG_ERR_ARG, "mg_dsgesv_ir: nterms must be 1..3");
+    if (o.nterms < 1 || o.nterms > 3) return mg::fail(h, MG_ERR_ARG, "mixed solve: nterms must be 1..3");
     if (o.max_iter < 1) o.max_iter = 1;
     mg_ir_report r = {};
     r.path = 0;
@@ -734,7 +741,7 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
         if (rep) *rep = r;
         return MG_OK;
     }
-    if (!A || !B || !X) return mg::fail(h, MG_ERR_ARG, "mg_dsgesv_ir: null pointer");
+    if (!A || !B || !X) return mg::fail(h, MG_ERR_ARG, "mixed solve: null pointer");
 
     const auto t0 = clk::now();
     MG_TRY(mg::ensure_ws(h, carve_ir(h, n, nrhs, o.nterms, nullptr)));
@@ -767,11 +774,34 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     MG_TRY(mg::post_launch(h, "absrow_reduce_kernel"));
     setup.reset();
 
-    // mixed LU ---------------------------------------------------------------
+    // fp32 factorization ---------------------------------------------------------
     int info = 0;
-    mg_status_t s = mg::sgetrf_mixed(h, n, w.A32, n, w.pos, IR_BLOCK, o.nterms, w.xchg, w.splitA, w.splitA2, w.splitB,
-                                     w.gemm_err, &info);
-    if (s != MG_OK && s != MG_SINGULAR) return s;
+    mg_status_t s = MG_OK;
+    if (spd) {
+        // Cholesky of the lower triangle, then L L^T as a packed LU with pos = identity
+        pos_iota_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.pos, n);
+        MG_TRY(mg::post_launch(h, "pos_iota_kernel"));
+        s = mg::spotrf_mixed(h, n, w.A32, n, o.nterms, w.splitA, w.gemm_err, &info);
+        if (s != MG_OK && s != MG_NOT_SPD) return s;
+        if (s == MG_NOT_SPD) {  // the fp32 Cholesky broke down: straight to the FP64 solve
+            r.info = info;
+            if (!o.fallback) {
+                if (rep) *rep = r;
+                return mg::fail(h, MG_NOT_SPD, "mg_dsposv_ir: fp32 Cholesky broke down at column %d", info);
+            }
+            int finfo = 0;
+            const mg_status_t fs = mg_dgesv(h, n, nrhs, A, lda, B, ldb, X, ldx, &finfo);
+            if (fs != MG_OK) return fs;
+            r.path = 2;
+            if (rep) *rep = r;
+            return MG_FALLBACK_USED;
+        }
+        MG_TRY(mg::chol_to_lu_f32(h, n, w.A32, n, w.Y));
+    } else {
+        s = mg::sgetrf_mixed(h, n, w.A32, n, w.pos, IR_BLOCK, o.nterms, w.xchg, w.splitA, w.splitA2, w.splitB,
+                             w.gemm_err, &info, o.panel == 2);
+        if (s != MG_OK && s != MG_SINGULAR) return s;
+    }
     r.info = info;
     absmax_upper_kernel<<<n, 256, 0, st>>>(w.A32, n, w.norms + 18);
     MG_TRY(mg::post_launch(h, "absmax_upper_kernel"));
@@ -837,7 +867,7 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
         MG_CHECK_CUDA(h, cudaMemcpyAsync(herr, w.gemm_err, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
         MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
         if (herr[0] || herr[1])
-            return mg::fail(h, MG_TIMEOUT, "mg_dsgesv_ir: a bounded device wait timed out (%s)",
+            return mg::fail(h, MG_TIMEOUT, "mixed solve: a bounded device wait timed out (%s)",
                             herr[0] ? "split GEMM" : "triangular solve");
         const double anorm = hn[16];
         double eta = 0.0;
@@ -1043,4 +1073,14 @@ extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double
     }
     if (rep) *rep = r;
     return result;
+}
+
+extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
+                                    int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* rep) {
+    return mixed_solve(h, n, nrhs, A, lda, B, ldb, X, ldx, opts, rep, false);
+}
+
+extern "C" mg_status_t mg_dsposv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
+                                    int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* rep) {
+    return mixed_solve(h, n, nrhs, A, lda, B, ldb, X, ldx, opts, rep, true);
 }

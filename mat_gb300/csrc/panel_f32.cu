@@ -94,6 +94,118 @@ struct CpShared {
     float s_pv[2];
 };
 
+// Tournament pivoting (TOURN): per sub-panel, one exchange of candidate rows
+// instead of one agreement per column.  Every CTA receives all 16 CTAs' 16
+// candidates (their rows as the sub-panel started, and their positions) and
+// the rows then at the sub-panel's 16 diagonal positions.
+struct TsShared {
+    CpRec cand[CP_CS][CP_SW];                 // [sender rank][column picked for]; pos < 0: no candidate
+    __align__(16) float top[CP_SW][CP_SW];    // rows at positions cs0 .. cs0+15 as the sub-panel started
+    CpRec mine[CP_SW];                        // this CTA's candidates
+    float T[CP_SW][CP_SW + 1];                // the factored diagonal block
+    int win[CP_SW];                           // the winners' positions (pivot order); -1: zero column
+    int winslot[CP_SW];                       // their slot in the last level's candidate list
+    int ok;
+    __align__(8) uint64_t mbar;               // receive barrier (transaction bytes), one phase per sub-panel
+};
+
+__device__ __forceinline__ uint32_t ts_rx_bytes(int R, int cs0) {
+    const int ntop = min(CP_SW, R - cs0);
+    return (uint32_t)(CP_CS * CP_SW * sizeof(CpRec) + ntop * CP_SW * sizeof(float));
+}
+
+// One warp's elimination with partial pivoting over NPL rows per lane (u:
+// working copies, updated in place; pos < 0: no row) across the sub-panel's
+// sw <= 16 columns: per column the first largest |a| among the rows not yet
+// picked (the smaller position on ties), then for the others l = a * (1/p),
+// a_j := fma(l, -p_j, a_j).  pk[c] = lane * 8 + k of the row picked for
+// column c (the same in every lane), or -1 if no nonzero was left.  The
+// result depends only on the set of rows, not on how they sit in the warp.
+template <int NPL>
+__device__ __forceinline__ void warp_pick(float (&u)[NPL][CP_SW], const int (&pos)[NPL], int sw, int (&pk)[CP_SW]) {
+    const int lane = threadIdx.x & 31;
+    unsigned chosen = 0u;
+#pragma unroll
+    for (int c = 0; c < CP_SW; ++c) {
+        pk[c] = -1;
+        if (c < sw) {
+            unsigned bb = 0u;
+            int bp = INT_MAX, bk = 0;
+#pragma unroll
+            for (int k = 0; k < NPL; ++k) {
+                if (pos[k] >= 0 && !((chosen >> k) & 1u)) {
+                    const float a = fabsf(u[k][c]);
+                    if (a >= 0.f) {  // NaN is never picked
+                        const unsigned ab = __float_as_uint(a);
+                        if (bp == INT_MAX || ab > bb || (ab == bb && pos[k] < bp)) {
+                            bb = ab;
+                            bp = pos[k];
+                            bk = k;
+                        }
+                    }
+                }
+            }
+            const unsigned wm = __reduce_max_sync(0xffffffffu, bp == INT_MAX ? 0u : bb);
+            const unsigned wp =
+                __reduce_min_sync(0xffffffffu, (bp != INT_MAX && bb == wm) ? (unsigned)bp : 0xffffffffu);
+            if (wm != 0u && wp != 0xffffffffu) {  // the same in every lane
+                const unsigned own = __ballot_sync(0xffffffffu, bp == (int)wp);
+                const int ol = __ffs(own) - 1;
+                const int okk = __shfl_sync(0xffffffffu, bk, ol);
+                pk[c] = ol * 8 + okk;
+                if (lane == ol) chosen |= 1u << bk;
+                float pr[CP_SW];
+#pragma unroll
+                for (int j = c; j < CP_SW; ++j) {
+                    float val = u[0][j];
+#pragma unroll
+                    for (int k = 1; k < NPL; ++k)
+                        if (bk == k) val = u[k][j];
+                    pr[j] = __shfl_sync(0xffffffffu, val, ol);
+                }
+                const float inv = 1.f / pr[c];
+#pragma unroll
+                for (int k = 0; k < NPL; ++k) {
+                    if (pos[k] >= 0 && !((chosen >> k) & 1u)) {
+                        const float l = u[k][c] * inv;
+#pragma unroll
+                        for (int j = c + 1; j < CP_SW; ++j) u[k][j] = fmaf(l, -pr[j], u[k][j]);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// A warp's tournament level over candidate records: lane l takes records
+// in[l + 32 t], t < NPL (n records in all); the picks go to out[c] (the
+// record as it came in; pos -1 where column c had no pick) and slot[c]
+// receives the index of the picked record in `in`.
+template <int NPL>
+__device__ __forceinline__ void warp_level(const CpRec* in, int n, int sw, CpRec* out, int* slot) {
+    const int lane = threadIdx.x & 31;
+    float u[NPL][CP_SW];
+    int pos[NPL];
+#pragma unroll
+    for (int t = 0; t < NPL; ++t) {
+        const int q = lane + 32 * t;
+        pos[t] = q < n ? in[q].pos : -1;
+#pragma unroll
+        for (int j = 0; j < CP_SW; ++j) u[t][j] = q < n ? in[q].row[j] : 0.f;
+    }
+    int pk[CP_SW];
+    warp_pick<NPL>(u, pos, sw, pk);
+#pragma unroll
+    for (int c = 0; c < CP_SW; ++c) {
+        const int q = pk[c] < 0 ? -1 : (pk[c] >> 3) + 32 * (pk[c] & 7);
+        if (lane < CP_SW) out[c].row[lane] = q < 0 ? 0.f : in[q].row[lane];
+        if (lane == 0) {
+            out[c].pos = q < 0 ? -1 : in[q].pos;
+            if (slot) slot[c] = q;
+        }
+    }
+}
+
 // Bytes each CTA receives per column: 16 records and the diagonal row.
 constexpr uint32_t CP_RX_BYTES = CP_CS * sizeof(CpRec) + CP_SW * sizeof(float);
 
@@ -111,7 +223,7 @@ __device__ __forceinline__ void st_async16(uint32_t dst, float4 v, uint32_t mbar
                  : "memory");
 }
 
-template <int RPT>
+template <int RPT, bool TOURN>
 __global__ void __launch_bounds__(CP_THREADS, 1)
     panel_cluster_kernel(float* __restrict__ A, int lda, int m, int r0, int w, int* __restrict__ pos,
                          int* __restrict__ piv_out, int* __restrict__ info, int* __restrict__ err) {
@@ -122,6 +234,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
     int* const map = reinterpret_cast<int*>(dyn + CP_SW * RPC);  // map[p], p in [0, R): the row (at
                                                           // sub-panel start) now at position p
     __shared__ __align__(16) CpShared sh;
+    __shared__ __align__(16) TsShared ts;  // used by the tournament form only
     cg::cluster_group cluster = cg::this_cluster();
     const int q = (int)cluster.block_rank();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -131,11 +244,17 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
 
     for (int p = tid; p < R; p += CP_THREADS) map[p] = p;
     if (tid == 0) {
-        tc::mbar_init(&sh.mbar[0], 1);
-        tc::mbar_init(&sh.mbar[1], 1);
-        tc::fence_barrier_init();
-        tc::mbar_arrive_expect_tx(&sh.mbar[0], CP_RX_BYTES);
-        tc::mbar_arrive_expect_tx(&sh.mbar[1], CP_RX_BYTES);
+        if constexpr (TOURN) {
+            tc::mbar_init(&ts.mbar, 1);
+            tc::fence_barrier_init();
+            tc::mbar_arrive_expect_tx(&ts.mbar, ts_rx_bytes(R, 0));
+        } else {
+            tc::mbar_init(&sh.mbar[0], 1);
+            tc::mbar_init(&sh.mbar[1], 1);
+            tc::fence_barrier_init();
+            tc::mbar_arrive_expect_tx(&sh.mbar[0], CP_RX_BYTES);
+            tc::mbar_arrive_expect_tx(&sh.mbar[1], CP_RX_BYTES);
+        }
     }
     cluster.sync();  // every CTA's receive barriers are armed before the first record is sent
     bool rx_failed = false;  // warp 0: a receive wait gave up (error recorded; later waits skipped)
@@ -296,6 +415,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
             __syncthreads();
         };
 
+        if constexpr (!TOURN) {
 #pragma unroll
         for (int c = 0; c < CP_SW; ++c) {
             if (c < sw) {
@@ -339,6 +459,210 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                     }
                 }
             }
+        }
+        } else {
+            // ---- tournament pivoting for the sub-panel (CALU's TSLU: Grigori,
+            // Demmel & Xiang, "CALU: a communication optimal LU factorization
+            // algorithm", SIAM J. Matrix Anal. Appl. 2011), as a reduction
+            // tree of partial-pivoting eliminations, each level passing on the
+            // rows it picked as they were when the sub-panel started:
+            //   L1 each warp over its own rows (RPT per lane),
+            //   L2 warp 0 over the 8 warps' picks of its CTA,
+            //   exchange: every CTA's 16 picks to every CTA of the cluster,
+            //   L3 warp w over the picks of CTAs 2w and 2w+1, then
+            //   L4 warp 0 over those 8 warps' picks: the 16 pivots, in order.
+            // Every level is warp-level (shuffles and reductions, no CTA
+            // barrier per column); levels L3 and L4 run identically in every CTA.
+            CpRec* const wc = reinterpret_cast<CpRec*>(tile);  // the tile is free until the store
+            {   // L1
+                float u[RPT][CP_SW];
+                int pos[RPT];
+#pragma unroll
+                for (int k = 0; k < RPT; ++k) {
+                    const int p = row0 + k * CP_THREADS + tid;
+                    pos[k] = (p < R && p >= cs0) ? p : -1;
+#pragma unroll
+                    for (int j = 0; j < CP_SW; ++j) u[k][j] = v[k][j];
+                }
+                int pk[CP_SW];
+                warp_pick<RPT>(u, pos, sw, pk);
+                CpRec* const mw = wc + warp * CP_SW;
+#pragma unroll
+                for (int c = 0; c < CP_SW; ++c) {
+                    if (pk[c] < 0) {
+                        if (lane == 0) mw[c].pos = -1;
+                    } else if (lane == (pk[c] >> 3)) {
+                        const int kw = pk[c] & 7;
+#pragma unroll
+                        for (int k = 0; k < RPT; ++k)
+                            if (k == kw) {
+#pragma unroll
+                                for (int j = 0; j < CP_SW; ++j) mw[c].row[j] = v[k][j];
+                                mw[c].pos = pos[k];
+                            }
+                    }
+                }
+            }
+            __syncthreads();
+            if (warp == 0) warp_level<4>(wc, 8 * CP_SW, sw, ts.mine, nullptr);  // L2
+            __syncthreads();
+            // exchange: candidates and the diagonal rows to every CTA of the cluster
+            {
+                const int dest = tid >> 4, c = tid & 15;
+                const float4* src = reinterpret_cast<const float4*>(&ts.mine[c]);
+                const uint32_t dst = cluster_addr(&ts.cand[q][c], dest);
+                const uint32_t bar = cluster_addr(&ts.mbar, dest);
+#pragma unroll
+                for (int u4 = 0; u4 < 5; ++u4) st_async16(dst + 16u * u4, src[u4], bar);
+            }
+            const int ntop = min(CP_SW, R - cs0);
+#pragma unroll
+            for (int k = 0; k < RPT; ++k) {
+                const int p = row0 + k * CP_THREADS + tid;
+                if (p >= cs0 && p < cs0 + ntop) {
+                    for (int dest = 0; dest < CS; ++dest) {
+                        const uint32_t dst = cluster_addr(&ts.top[p - cs0][0], dest);
+                        const uint32_t bar = cluster_addr(&ts.mbar, dest);
+#pragma unroll
+                        for (int u4 = 0; u4 < CP_SW / 4; ++u4)
+                            st_async16(dst + 16u * u4,
+                                       make_float4(v[k][4 * u4], v[k][4 * u4 + 1], v[k][4 * u4 + 2], v[k][4 * u4 + 3]),
+                                       bar);
+                    }
+                }
+            }
+            if (tid == 0) {
+                int ok = 0;
+                if (!rx_failed) {
+                    ok = tc::mbar_wait(&ts.mbar, (uint32_t)(s & 1)) ? 1 : 0;
+                    if (!ok) atomicExch(err, 8 /* MG_TIMEOUT */);
+                }
+                if (ok && s + 1 < nsub) tc::mbar_arrive_expect_tx(&ts.mbar, ts_rx_bytes(R, cs0 + CP_SW));
+                ts.ok = ok;
+            }
+            __syncthreads();
+            if (!ts.ok) {
+                rx_failed = true;
+                for (int e = tid; e < CS * CP_SW; e += CP_THREADS) (&ts.cand[0][0])[e].pos = -1;
+                __syncthreads();
+            }
+            warp_level<1>(&ts.cand[0][0] + warp * 32, 32, sw, wc + warp * CP_SW, nullptr);  // L3
+            __syncthreads();
+            if (warp == 0) {  // L4: the pivots
+                float u[4][CP_SW];
+                int pos[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int qq = lane + 32 * t;
+                    pos[t] = wc[qq].pos;
+#pragma unroll
+                    for (int j = 0; j < CP_SW; ++j) u[t][j] = wc[qq].row[j];
+                }
+                int pk[CP_SW];
+                warp_pick<4>(u, pos, sw, pk);
+                if (lane < CP_SW) {
+                    const int c = lane;
+                    int qsel = -1;
+#pragma unroll
+                    for (int cc = 0; cc < CP_SW; ++cc)
+                        if (cc == c) qsel = pk[cc] < 0 ? -1 : (pk[cc] >> 3) + 32 * (pk[cc] & 7);
+                    ts.win[c] = (c < sw && qsel >= 0) ? wc[qsel].pos : -1;
+                    ts.winslot[c] = qsel;
+                }
+            }
+            __syncthreads();
+            // T4. the interchanges: winner c moves to position cs0 + c (Mat's
+            //     swap sequence, tracked in map), as partial pivoting records them
+            if (tid == 0) {
+                for (int c = 0; c < sw; ++c) {
+                    const int cabs = cs0 + c;
+                    int cur = cabs;
+                    const int g = ts.win[c];
+                    if (g >= 0) {
+                        cur = g;
+                        if (map[g] != g)
+                            for (int t = 0; t < 2 * c; ++t)
+                                if (map[sh.touch[t]] == g) {
+                                    cur = sh.touch[t];
+                                    break;
+                                }
+                    } else if (q == 0) {
+                        atomicCAS(info, 0, r0 + cabs + 1);
+                    }
+                    sh.piv[cabs] = cur;
+                    sh.touch[2 * c] = cabs;
+                    sh.touch[2 * c + 1] = cur;
+                    if (cur != cabs) {
+                        const int t = map[cabs];
+                        map[cabs] = map[cur];
+                        map[cur] = t;
+                    }
+                }
+            }
+            __syncthreads();
+            // the row (as the sub-panel started) now at each touched position
+            auto row_of = [&](int r) -> const float* {
+                for (int c = 0; c < sw; ++c)
+                    if (ts.win[c] == r) return wc[ts.winslot[c]].row;
+                // a displaced diagonal row (the interchanges move only those and
+                // the winners; the clamp keeps a broken invariant in bounds)
+                const int t = r - cs0;
+                return ts.top[t >= 0 && t < CP_SW ? t : 0];
+            };
+            // T5. the diagonal block, factored without further pivoting (one warp,
+            //     lane i holds row i), then every other row of mine eliminated with
+            //     it: l = a * (1 / u_kk), a_j -= l u_kj, the fused operations of
+            //     the partial-pivoting panel
+            if (warp == 0) {
+                float t[CP_SW];
+                const bool rowok = lane < sw;
+                const float* src = rowok ? row_of(map[cs0 + lane]) : nullptr;
+#pragma unroll
+                for (int j = 0; j < CP_SW; ++j) t[j] = rowok ? src[j] : 0.f;
+#pragma unroll
+                for (int k = 0; k < CP_SW; ++k) {
+                    float rk[CP_SW];
+#pragma unroll
+                    for (int j = 0; j < CP_SW; ++j) rk[j] = __shfl_sync(0xffffffffu, t[j], k);
+                    if (k < sw && lane > k && rowok && rk[k] != 0.f) {
+                        const float l = t[k] * (1.f / rk[k]);
+                        t[k] = l;
+#pragma unroll
+                        for (int j = 0; j < CP_SW; ++j)
+                            if (j > k) t[j] = fmaf(l, -rk[j], t[j]);
+                    }
+                }
+                if (rowok)
+#pragma unroll
+                    for (int j = 0; j < CP_SW; ++j) ts.T[lane][j] = t[j];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < RPT; ++k) {
+                const int p = row0 + k * CP_THREADS + tid;
+                if (p >= R || p < cs0) continue;
+                if (p < cs0 + sw) {
+#pragma unroll
+                    for (int j = 0; j < CP_SW; ++j) v[k][j] = ts.T[p - cs0][j];
+                    continue;
+                }
+                if (map[p] != p) {  // a row moved here by the interchanges
+                    const float* src = row_of(map[p]);
+#pragma unroll
+                    for (int j = 0; j < CP_SW; ++j) v[k][j] = src[j];
+                }
+#pragma unroll
+                for (int c = 0; c < CP_SW; ++c) {
+                    if (c < sw && ts.T[c][c] != 0.f) {
+                        const float l = v[k][c] * (1.f / ts.T[c][c]);
+                        v[k][c] = l;
+#pragma unroll
+                        for (int j = 0; j < CP_SW; ++j)
+                            if (j > c) v[k][j] = fmaf(l, -ts.T[c][j], v[k][j]);
+                    }
+                }
+            }
+            __syncthreads();  // the tile (candidate records) is rewritten by the store below
         }
 
         // store my rows of the sub-panel (through the tile)
@@ -491,18 +815,18 @@ cudaLaunchConfig_t cluster_cfg(cudaStream_t st, size_t smem, cudaLaunchAttribute
     return cfg;
 }
 
-template <int RPT>
+template <int RPT, bool TOURN>
 cudaError_t launch_cluster(cudaStream_t st, size_t smem, float* A, int lda, int m, int r0, int w, int* pos,
                            int* piv, int* info, int* err) {
     cudaLaunchAttribute at[1];
     cudaLaunchConfig_t cfg = cluster_cfg(st, smem, at);
-    return cudaLaunchKernelEx(&cfg, panel_cluster_kernel<RPT>, A, lda, m, r0, w, pos, piv, info, err);
+    return cudaLaunchKernelEx(&cfg, panel_cluster_kernel<RPT, TOURN>, A, lda, m, r0, w, pos, piv, info, err);
 }
 
 // Sets the kernel's attributes and returns how many such clusters fit.
-template <int RPT>
+template <int RPT, bool TOURN>
 int prepare(size_t smem_max) {
-    auto k = panel_cluster_kernel<RPT>;
+    auto k = panel_cluster_kernel<RPT, TOURN>;
     int n = 0;
     cudaLaunchAttribute at[1];
     cudaLaunchConfig_t cfg = cluster_cfg(nullptr, smem_max, at);
@@ -525,8 +849,10 @@ int panel_cluster_rows(mg_handle_t h) {
     constexpr int kRows = CP_CS * CP_MAX_RPT * CP_THREADS;
     if (h->panel_cluster == 0) {
         const size_t smem_max = (size_t)CP_SW * CP_MAX_RPT * CP_THREADS * sizeof(float) + (size_t)kRows * sizeof(int);
-        const bool ok = prepare<1>(smem_max) > 0 && prepare<2>(smem_max) > 0 && prepare<3>(smem_max) > 0 &&
-                        prepare<4>(smem_max) > 0;
+        const bool ok = prepare<1, false>(smem_max) > 0 && prepare<2, false>(smem_max) > 0 &&
+                        prepare<3, false>(smem_max) > 0 && prepare<4, false>(smem_max) > 0 &&
+                        prepare<1, true>(smem_max) > 0 && prepare<2, true>(smem_max) > 0 &&
+                        prepare<3, true>(smem_max) > 0 && prepare<4, true>(smem_max) > 0;
         h->panel_cluster = ok ? CP_CS : -1;
     }
     return h->panel_cluster > 0 ? kRows : 0;
@@ -538,7 +864,7 @@ int panel_cluster_rows(mg_handle_t h) {
 // err receives MG_TIMEOUT if a receive wait gave up.
 // The caller checks panel_cluster_rows(h) >= m - r0 and w <= 128.
 mg_status_t sgetf2_cluster(mg_handle_t h, float* A, int lda, int m, int r0, int w, int* pos, int* piv,
-                           int* info, int* err) {
+                           int* info, int* err, bool tourn) {
     const int R = m - r0;
     if (w <= 0 || w > CP_MAXW || R < w || R > panel_cluster_rows(h))
         return fail(h, MG_ERR_ARG, "sgetf2_cluster: unsupported panel %d x %d", R, w);
@@ -546,12 +872,14 @@ mg_status_t sgetf2_cluster(mg_handle_t h, float* A, int lda, int m, int r0, int 
     const size_t smem = (size_t)CP_SW * rpt * CP_THREADS * sizeof(float) + (size_t)R * sizeof(int);
     ProfScope prof(h, "panel_f32", (double)R * w * w, 2.0 * R * w * sizeof(float));
     cudaError_t e;
+#define MG_LC(RPTV, TV) launch_cluster<RPTV, TV>(h->stream, smem, A, lda, m, r0, w, pos, piv, info, err)
     switch (rpt) {
-        case 1: e = launch_cluster<1>(h->stream, smem, A, lda, m, r0, w, pos, piv, info, err); break;
-        case 2: e = launch_cluster<2>(h->stream, smem, A, lda, m, r0, w, pos, piv, info, err); break;
-        case 3: e = launch_cluster<3>(h->stream, smem, A, lda, m, r0, w, pos, piv, info, err); break;
-        default: e = launch_cluster<4>(h->stream, smem, A, lda, m, r0, w, pos, piv, info, err); break;
+        case 1: e = tourn ? MG_LC(1, true) : MG_LC(1, false); break;
+        case 2: e = tourn ? MG_LC(2, true) : MG_LC(2, false); break;
+        case 3: e = tourn ? MG_LC(3, true) : MG_LC(3, false); break;
+        default: e = tourn ? MG_LC(4, true) : MG_LC(4, false); break;
     }
+#undef MG_LC
     if (e != cudaSuccess) return cuda_fail(h, e, "panel_cluster_kernel launch");
     h->launches++;
     return MG_OK;
