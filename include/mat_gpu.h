@@ -107,10 +107,13 @@ mg_status_t mg_fill_normal(mg_handle_t h, double* A, int rows, int cols, int ld,
 mg_status_t mg_dgemm(mg_handle_t h, int transA, int transB, int m, int n, int k,
                      double alpha, const double* A, int lda, const double* B, int ldb,
                      double beta, double* C, int ldc);
-/* FP32 form: Mat's operator* on MAT<float> (the same Mul/Mul.h:204-235
- * template), C = alpha op(A) op(B) + beta C on the SIMT FP32 pipe (FFMA),
- * 128 x 128 tiles; not bit-identical to Mat's float micro-kernel order.
- * Also the GEMM of the FP32 Cholesky and its adjoint. */
+/* FP32 form: C = alpha op(A) op(B) + beta C on the SIMT FP32 pipe (FFMA),
+ * 128 x 128 tiles, IEEE fp32 accumulation; not bit-identical to Mat's float
+ * micro-kernel order.  Mat's operator* on MAT<float> (the same
+ * Mul/Mul.h:204-235 template) runs this for small products and the
+ * split-BF16 tensor-core GEMM (mg_sgemm_bf16x_ex, 3 terms, ordered) for
+ * large ones (k >= 32, m n k >= 2^27), as do the GEMMs inside the FP32
+ * Cholesky, its adjoint and the FP32 Gaussian-process loss. */
 mg_status_t mg_sgemm(mg_handle_t h, int transA, int transB, int m, int n, int k, float alpha, const float* A,
                      int lda, const float* B, int ldb, float beta, float* C, int ldc);
 

@@ -152,7 +152,10 @@ inline MAT<double> operator*(const MAT<double>& A, const MAT<double>& B) {
     return C;
 }
 
-// C = A * B for MAT<float> (the same operator* template in Mat; FP32 SIMT GEMM).
+// C = A * B for MAT<float> (the same operator* template in Mat).  Products
+// with k >= 32 and m n k >= 2^27 run on the tensor cores as split-BF16 (3
+// terms, lower-order products first, fp32 accumulation: fp32-class accuracy),
+// the rest on the FP32 SIMT GEMM.
 inline MAT<float> operator*(const MAT<float>& A, const MAT<float>& B) {
     MAT<float> C(A.rows, B.cols);
     const size_t sa = (size_t)A.rows * A.cols, sb = (size_t)B.rows * B.cols, sc = (size_t)C.rows * C.cols;
@@ -160,10 +163,15 @@ inline MAT<float> operator*(const MAT<float>& A, const MAT<float>& B) {
     matgpu::Dev dA(sa * 4), dB(sb * 4), dC(sc * 4);
     matgpu::h2d(dA.p, A.data, sa * 4);
     matgpu::h2d(dB.p, B.data, sb * 4);
-    matgpu::check(mg_sgemm(matgpu::handle(), 0, 0, A.rows, B.cols, A.cols, 1.0f, (const float*)dA.p,
-                           A.rows > 1 ? A.rows : 1, (const float*)dB.p, B.rows > 1 ? B.rows : 1, 0.0f, (float*)dC.p,
-                           C.rows > 1 ? C.rows : 1),
-                  "mg_sgemm");
+    const int lda = A.rows > 1 ? A.rows : 1, ldb = B.rows > 1 ? B.rows : 1, ldc = C.rows > 1 ? C.rows : 1;
+    if (A.cols >= 32 && (double)A.rows * B.cols * A.cols >= (double)(1 << 27))
+        matgpu::check(mg_sgemm_bf16x_ex(matgpu::handle(), 3, MG_BF16X_ORDERED, A.rows, B.cols, A.cols, 1.0f,
+                                        (const float*)dA.p, lda, (const float*)dB.p, ldb, 0.0f, (float*)dC.p, ldc),
+                      "mg_sgemm_bf16x_ex");
+    else
+        matgpu::check(mg_sgemm(matgpu::handle(), 0, 0, A.rows, B.cols, A.cols, 1.0f, (const float*)dA.p, lda,
+                               (const float*)dB.p, ldb, 0.0f, (float*)dC.p, ldc),
+                      "mg_sgemm");
     matgpu::d2h(C.data, dC.p, sc * 4);
     return C;
 }

@@ -329,6 +329,11 @@ mg_status_t potrf_impl(mg_handle_t h, int n, T* L, int ldl, int* info_out) {
     int* hw = (int*)h->hws;
     MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
     MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
+    if (sizeof(T) == 4) {  // the FP32 trailing updates may have run on the tensor cores
+        int terr = 0;
+        MG_TRY(tc_sgemm_error(h, &terr));
+        if (terr) return fail(h, MG_TIMEOUT, "potrf: a tensor-core update's bounded wait gave up");
+    }
     if (info_out) *info_out = hw[0];
     if (hw[0]) return fail(h, MG_NOT_SPD, "potrf: non-positive pivot at column %d", hw[0]);
     return MG_OK;

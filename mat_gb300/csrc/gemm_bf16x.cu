@@ -634,9 +634,12 @@ extern "C" mg_status_t mg_bf16x_check_error(mg_handle_t h, int* device_err_flag)
     if (!h || !device_err_flag) return MG_ERR_ARG;
     if (!h->ws) {
         *device_err_flag = 0;
-        return MG_OK;
+        return mg::tc_sgemm_error(h, device_err_flag);
     }
     MG_CHECK_CUDA(h, cudaMemcpyAsync(device_err_flag, h->ws, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    int terr = 0;  // and the FP32 GEMMs of the factorizations that ran on the tensor cores
+    MG_TRY(mg::tc_sgemm_error(h, &terr));
+    *device_err_flag |= terr;
     return MG_OK;
 }

@@ -225,6 +225,7 @@ mg_status_t mg_handle_destroy(mg_handle_t h) {
     for (cudaEvent_t e : h->pp_ev)
         if (e) cudaEventDestroy(e);
     if (h->ws) cudaFree(h->ws);
+    if (h->tcws) cudaFree(h->tcws);
     if (h->hws) cudaFreeHost(h->hws);
     if (h->status) cudaFree(h->status);
     delete h;

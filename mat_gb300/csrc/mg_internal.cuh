@@ -22,6 +22,11 @@ struct mg_handle_s {
     // Small device area for status words (info / error flags) that must not
     // overlap the caller-visible workspace.
     int* status = nullptr;
+    // Split operands of FP32 GEMMs run on the tensor cores: three regions,
+    // one per stream a factorization issues GEMMs on (the handle's stream,
+    // the look-ahead side streams), after 4 KiB of error words.
+    void* tcws = nullptr;
+    size_t tcws_bytes = 0;
     // Pinned host workspace (status words read back by info-reporting calls).
     void* hws = nullptr;
     size_t hws_bytes = 0;
@@ -128,9 +133,18 @@ inline mg_status_t gemm_of(mg_handle_t h, int ta, int tb, int m, int n, int k, d
                            int lda, const double* B, int ldb, double beta, double* C, int ldc, int tri) {
     return dgemm_launch(h, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri);
 }
+// The FP32 GEMM of the factorizations and adjoints: large products (k >= 32,
+// m n k >= 2^27) run on the tensor cores as split-BF16 products (3 terms,
+// lower-order products first, fp32 accumulation; the whole m x n block is
+// computed when tri is set, callers read its lower part only), the rest on
+// the SIMT FP32 kernel.
+mg_status_t sgemm_auto(mg_handle_t h, int ta, int tb, int m, int n, int k, float alpha, const float* A, int lda,
+                       const float* B, int ldb, float beta, float* C, int ldc, int tri);
+// Sticky error word of those tensor-core GEMMs (MG_TIMEOUT after a bounded wait gave up), or 0.
+mg_status_t tc_sgemm_error(mg_handle_t h, int* err_out);
 inline mg_status_t gemm_of(mg_handle_t h, int ta, int tb, int m, int n, int k, float alpha, const float* A, int lda,
                            const float* B, int ldb, float beta, float* C, int ldc, int tri) {
-    return sgemm_launch(h, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri);
+    return sgemm_auto(h, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri);
 }
 
 // Split-BF16 tensor-core GEMM pieces (gemm_bf16x.cu).
