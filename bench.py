@@ -266,6 +266,13 @@ def config_rates(h, dmma_tf: float, bf16_tf: float) -> dict:
     out["split_gemm_16384"]["ordered"] = {"s": t_so, "useful_tflops": useful / t_so / 1e12,
                                           "max_rel_err": float(d.abs().max() / ref.abs().max()),
                                           "normwise_rel_err": float(d.norm() / ref.norm())}
+    # the same inputs through the SIMT FP32 GEMM (IEEE fp32 accumulation): the
+    # accuracy the split form is compared with
+    t_ss, _ = timed(lambda: h.sgemm(Ga, Gb, Gc))
+    d = Gc[rows].double() - ref
+    out["split_gemm_16384"]["fp32_simt"] = {"s": t_ss, "tflops": useful / t_ss / 1e12,
+                                           "max_rel_err": float(d.abs().max() / ref.abs().max()),
+                                           "normwise_rel_err": float(d.norm() / ref.norm())}
     del Ga, Gb, Gc, ref, d
     torch.cuda.empty_cache()
     # FP64 tensor-core GEMM rate at 4096^3, for the comparison
@@ -291,6 +298,43 @@ def config_rates(h, dmma_tf: float, bf16_tf: float) -> dict:
                                    "dloss_dell": dell32, "loss_rel_diff_vs_fp64": abs(loss32 - loss) / abs(loss),
                                    "dell_rel_diff_vs_fp64": abs(dell32 - dell) / abs(dell),
                                    "note": "inputs rounded to fp32; the difference is the fp32 conditioning of K"}
+    # the mixed SPD solve on the Gaussian-process kernel (fp32 Cholesky with
+    # split-BF16 updates + FP64 refinement) against the FP64 Cholesky solve
+    K = h.gen_rbf_kernel(Xp, 0.2, 1.0, 1e-2)
+    yk = y.clone()
+    t_spd, (Xs, rs) = timed(lambda: h.dsposv_ir(K, yk))
+
+    def chol64():
+        L = K.clone()
+        h.dpotrf(L)
+        return h.dpotrs(L, yk.clone())
+
+    t_c64, Xc = timed(chol64)
+    out["mixed_spd_solve_8192"] = {"s": t_spd, "fp64_cholesky_solve_s": t_c64, "speedup": t_c64 / t_spd,
+                                   "iterations": rs["iterations"], "backward_error": rs["backward_error"],
+                                   "path": rs["path"], "rel_diff_vs_fp64": float((Xs - Xc).norm() / Xc.norm()),
+                                   "matrix": "RBF kernel, lengthscale 0.2, unit variance, + 1e-2 I, n = 8192"}
+    del K, Xs, Xc
+    torch.cuda.empty_cache()
+    # GMRES-IR beyond plain refinement: the benchmark recipe at condition 1e10
+    nA = 16384
+    Ag = colmajor(nA, nA)
+    h.gen_svd_matrix(Ag, 7, nrefl=64, sigma_min=1e-10)
+    Bg = colmajor(nA, 4)
+    h.fill_normal(Bg, 13)
+    t_g, (Xg, rg) = timed(lambda: h.dsgesv_ir(Ag, Bg, fallback=False))
+    out["gmres_ir_16384_cond1e10"] = {"s": t_g, "status": rg["status"], "path": rg["path"],
+                                     "iterations": rg["iterations"], "gmres_iterations": rg["gmres_iterations"],
+                                     "backward_error": rg["backward_error"], "history": rg["history"]}
+    # the tournament-pivoting panel in the same mixed solve (benchmark system)
+    Ab = colmajor(nA, nA)
+    h.gen_svd_matrix(Ab, 3, nrefl=64, sigma_min=1e-6)
+    t_t, (Xt, rt) = timed(lambda: h.dsgesv_ir(Ab, Bg, panel=2))
+    t_p, _ = timed(lambda: h.dsgesv_ir(Ab, Bg, panel=1))
+    out["mixed_solve_panel_pivoting"] = {"partial_s": t_p, "tournament_s": t_t, "tournament_iterations": rt["iterations"],
+                                         "tournament_backward_error": rt["backward_error"],
+                                         "tournament_pivot_growth": rt["pivot_growth"]}
+    del Ag, Bg, Ab, Xg, Xt
     torch.cuda.empty_cache()
     # EVD_Q of the Mat-8.1 snapshot (EVD_QR): symmetric G + G^T, G iid N(0,1) (seed 7)
     for ne in (1024, 4096):

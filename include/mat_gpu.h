@@ -311,6 +311,29 @@ mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double* A, int ld
 mg_status_t mg_dsposv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
                          int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* report);
 
+/* Mixed-precision solve through Householder QR (no mixed precision in Mat;
+ * the FP64 counterpart is Mat's blocked Householder QR,
+ * Mat-8.3.1/QR/__Householder_Blocked.h:63-353): n x n A factored by
+ * mg_sgeqrf (fp32, the norm / beta / tau of every reflector in FP64, the
+ * trailing updates on the split-BF16 tensor cores), then refined in FP64:
+ * r = b - A x, d = R^{-1} Q^T r applied in FP64 arithmetic with the fp32
+ * reflectors, T factors and R, x += d; GMRES-IR (the same operator as its
+ * preconditioner) and the FP64 fallback as in mg_dsgesv_ir.  The report's
+ * pivot_growth is max |R| / max |A|.  opts.panel is ignored.  Synchronises. */
+mg_status_t mg_dsqrsv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
+                         int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* report);
+/* The FP32 Householder QR of that solve, for m x n A (m >= n), in place: R on
+ * and above the diagonal, the reflectors v below it (v_c = 1 implicit, LAPACK
+ * layout as in Mat's blocked panel, QR/__Householder_Blocked.h:63-84).
+ * Panels of 128 columns, one cooperative grid each (two bounded grid
+ * barriers per column; alpha, beta = -sign(alpha) ||x||, tau = (beta -
+ * alpha) / beta and the scaling 1 / (alpha - beta) in FP64), then T (the
+ * compact WY factor, fp32) and R2 -= V (T^T (V^T R2)) with the products on the
+ * split-BF16 tensor cores.  tau: n doubles (device); T: ceil(n / 128) blocks
+ * of 128 x 128 floats (device, block b column-major with ld 128).
+ * Synchronises. */
+mg_status_t mg_sgeqrf(mg_handle_t h, int m, int n, float* A, int lda, double* tau, float* T);
+
 /* ----------------------------------------------- FP32 LU (mixed solve)
  * The single-precision factorizations inside mg_dsgesv_ir, exposed for
  * callers that refine on their own.  No counterpart in Mat (no mixed

@@ -78,6 +78,8 @@ SIGNATURES: dict[str, tuple] = {
     "mg_bf16x_check_error": (i32, [vp, pi32]),
     "mg_dsgesv_ir": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, C.POINTER(IrOpts), C.POINTER(IrReport)]),
     "mg_dsposv_ir": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, C.POINTER(IrOpts), C.POINTER(IrReport)]),
+    "mg_dsqrsv_ir": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, C.POINTER(IrOpts), C.POINTER(IrReport)]),
+    "mg_sgeqrf": (i32, [vp, i32, i32, vp, i32, vp, vp]),
     "mg_gen_svd_matrix": (i32, [vp, i32, vp, i32, u64, i32, f64]),
     "mg_gen_spd_gram": (i32, [vp, i32, vp, i32, u64]),
     "mg_profile_enable": (i32, [vp, i32]),

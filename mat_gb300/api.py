@@ -210,7 +210,7 @@ class Handle:
         return pos, info.value
 
     def dsgesv_ir(self, A, B, X=None, tol=1e-14, max_iter=30, nterms=3, fallback=True, gmres=True, panel=0,
-                  spd=False):
+                  spd=False, qr=False):
         """Mixed LU (fp32 + split-BF16) + FP64 refinement, GMRES-IR and the FP64
         fallback when refinement stalls; spd=True: the fp32 Cholesky form
         (mg_dsposv_ir). Returns (X, report dict with the status)."""
@@ -220,10 +220,11 @@ class Handle:
             X = colmajor(n, nrhs, device=B.device)
         o = IrOpts(tol, max_iter, nterms, int(fallback), int(gmres), int(panel), 0)
         r = IrReport()
-        fn = self.lib.mg_dsposv_ir if spd else self.lib.mg_dsgesv_ir
-        st = fn(self.h, n, nrhs, _ptr(A), ld_of(A), _ptr(B), ld_of(B), _ptr(X), ld_of(X), C.byref(o), C.byref(r))
+        name = "mg_dsqrsv_ir" if qr else "mg_dsposv_ir" if spd else "mg_dsgesv_ir"
+        st = getattr(self.lib, name)(self.h, n, nrhs, _ptr(A), ld_of(A), _ptr(B), ld_of(B), _ptr(X), ld_of(X),
+                                     C.byref(o), C.byref(r))
         if st not in (0, 6, 7):
-            self.check(st, "mg_dsposv_ir" if spd else "mg_dsgesv_ir")
+            self.check(st, name)
         nh = min(32, r.iterations + 1)
         rep = dict(iterations=r.iterations, path=r.path, info=r.info, gmres_iterations=r.gmres_iterations,
                    backward_error=r.backward_error, anorm_inf=r.anorm_inf, factor_ms=r.factor_ms,
@@ -234,6 +235,19 @@ class Handle:
     def dsposv_ir(self, A, B, X=None, **kw):
         """Mixed-precision SPD solve (fp32 Cholesky with split-BF16 updates + FP64 refinement)."""
         return self.dsgesv_ir(A, B, X, spd=True, **kw)
+
+    def dsqrsv_ir(self, A, B, X=None, **kw):
+        """Mixed-precision solve through Householder QR (fp32 QR with FP64 norms, split-BF16
+        updates; FP64 refinement)."""
+        return self.dsgesv_ir(A, B, X, qr=True, **kw)
+
+    def sgeqrf(self, A):
+        """In-place fp32 Householder QR of A (m x n, m >= n). Returns (tau float64, T blocks float32)."""
+        m, n = A.shape
+        tau = torch.empty(n, dtype=torch.float64, device=A.device)
+        T = torch.empty(((n + 127) // 128) * 128 * 128, dtype=torch.float32, device=A.device)
+        self.check(self.lib.mg_sgeqrf(self.h, m, n, _ptr(A), ld_of(A), _ptr(tau), _ptr(T)), "mg_sgeqrf")
+        return tau, T
 
     # ------------------------------------------------------------- generators
     def gen_svd_matrix(self, A, seed, nrefl=64, sigma_min=1e-6):

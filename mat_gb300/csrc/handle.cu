@@ -225,7 +225,9 @@ mg_status_t mg_handle_destroy(mg_handle_t h) {
     for (cudaEvent_t e : h->pp_ev)
         if (e) cudaEventDestroy(e);
     if (h->ws) cudaFree(h->ws);
-    if (h->tcws) cudaFree(h->tcws);
+    for (int i = 0; i < 3; ++i)
+        if (h->tcws[i]) cudaFree(h->tcws[i]);
+    if (h->tcerr) cudaFree(h->tcerr);
     if (h->hws) cudaFreeHost(h->hws);
     if (h->status) cudaFree(h->status);
     delete h;

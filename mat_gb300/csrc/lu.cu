@@ -869,6 +869,25 @@ mg_status_t dgetrs_impl(mg_handle_t h, int n, int nrhs, const double* LU, int ld
     return narrow_subst<double>(h, n, nrhs, LU, lda, X, ldx);
 }
 
+// X := U^{-1} X in FP64 for an upper triangle held in fp32 (the mixed QR's R).
+mg_status_t upper_solve_f32_factors(mg_handle_t h, int n, int nrhs, const float* U, int ldu, double* X, int ldx) {
+    if (n == 0 || nrhs == 0) return MG_OK;
+    const int ublocks = h->num_sms;
+    const int last = ((n - 1) / TRSV_B) * TRSV_B;
+    for (int b0 = last; b0 >= 0; b0 -= TRSV_B) {
+        const int b1 = b0 + TRSV_B < n ? b0 + TRSV_B : n;
+        trsv_upper_diag_kernel<float, double><<<1, 256, 0, h->stream>>>(n, nrhs, U, ldu, X, ldx, b0, b1);
+        MG_TRY(post_launch(h, "trsv_upper_diag_kernel"));
+        if (b0 > 0) {
+            int blocks = (b0 + 127) / 128;
+            if (blocks > ublocks) blocks = ublocks;
+            trsv_upper_update_kernel<float, double><<<blocks, 128, 0, h->stream>>>(n, nrhs, U, ldu, X, ldx, b0, b1);
+            MG_TRY(post_launch(h, "trsv_upper_update_kernel"));
+        }
+    }
+    return MG_OK;
+}
+
 // X := (LU)^{-1} P B in FP64 arithmetic for factors held in fp32 (the mixed
 // LU's, whose pos follows Mat's convention): the same narrow substitution
 // kernels with each fp32 factor entry widened exactly to fp64.  This is a

@@ -22,11 +22,12 @@ struct mg_handle_s {
     // Small device area for status words (info / error flags) that must not
     // overlap the caller-visible workspace.
     int* status = nullptr;
-    // Split operands of FP32 GEMMs run on the tensor cores: three regions,
-    // one per stream a factorization issues GEMMs on (the handle's stream,
-    // the look-ahead side streams), after 4 KiB of error words.
-    void* tcws = nullptr;
-    size_t tcws_bytes = 0;
+    // Split operands of FP32 GEMMs run on the tensor cores: one area per
+    // stream a factorization issues GEMMs on (the handle's stream, the
+    // look-ahead side streams), and their error words.
+    void* tcws[3] = {nullptr, nullptr, nullptr};
+    size_t tcws_bytes[3] = {0, 0, 0};
+    int* tcerr = nullptr;
     // Pinned host workspace (status words read back by info-reporting calls).
     void* hws = nullptr;
     size_t hws_bytes = 0;
@@ -104,6 +105,15 @@ mg_status_t dgemm_launch(mg_handle_t h, int transA, int transB, int m, int n, in
 
 // In-place FP64 Mat PLU and narrow solve (lu.cu).
 mg_status_t dgetrf_impl(mg_handle_t h, int m, int n, double* A, int lda, int* pos, int* info_out);
+// X := U^{-1} X in FP64 for an fp32 upper triangle (lu.cu).
+mg_status_t upper_solve_f32_factors(mg_handle_t h, int n, int nrhs, const float* U, int ldu, double* X, int ldx);
+// Mixed FP32 Householder QR (qr_mixed.cu): workspace bytes, the factorization
+// (tau in FP64, T blocks of 128 x 128 fp32), and X := R^{-1} Q^T B in FP64
+// (square A) with the same workspace.
+size_t qr_mixed_ws_bytes(int m, int n, int num_sms);
+mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double* tau, float* T, void* ws, int* err);
+mg_status_t qr_solve_f32_factors(mg_handle_t h, int n, int nrhs, const float* A, int lda, const float* T,
+                                 const double* B, int ldb, double* X, int ldx, void* ws);
 // X := (P^T L U)^{-1} B in FP64 for the mixed LU's fp32 in-place factors (lu.cu).
 mg_status_t lu_solve_f32_factors(mg_handle_t h, int n, int nrhs, const float* LU, int lda, const int* pos,
                                  const double* B, int ldb, double* X, int ldx);

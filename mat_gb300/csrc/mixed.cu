@@ -307,6 +307,13 @@ __global__ void gm_update_x_kernel(int n, int nv, int nrhs, const double* __rest
     }
 }
 
+// X(:, j) += D(:, j)  (FP64 correction of the QR-form refinement)
+__global__ void add_correction_kernel(int n, int nrhs, const double* __restrict__ D, double* __restrict__ X, int ldx) {
+    const size_t total = (size_t)n * nrhs;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
+        X[(e % n) + (e / n) * (size_t)ldx] += D[e];
+}
+
 // Inverse of each diagonal block (unit lower when LOWER, else upper) of the
 // packed fp32 LU; one CTA per block, one thread per column of the inverse.
 template <bool LOWER>
@@ -651,9 +658,10 @@ struct IrWs {
     double* gW;     // n x nrhs
     double* gP;     // Gram-Schmidt partial sums, GM_CTAS x (GM_RESTART + 1) x nrhs
     double* gC;     // coefficients for the device, (GM_RESTART + 1) x nrhs
+    void* qws;      // mixed QR: panel reflectors, products, partial sums (QR mode only)
 };
 
-size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
+size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w, bool qr = false) {
     size_t off = 0;
     auto take = [&](size_t bytes) {
         const size_t o = off;
@@ -682,6 +690,7 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
     const size_t ogW = take((size_t)n * nrhs * sizeof(double));
     const size_t ogP = take((size_t)GM_CTAS * (GM_RESTART + 1) * nrhs * sizeof(double));
     const size_t ogC = take((size_t)(GM_RESTART + 1) * nrhs * sizeof(double));
+    const size_t oQ = take(qr ? mg::qr_mixed_ws_bytes(n, n, h->num_sms) : 0);
     if (w) {
         char* b = (char*)h->ws;
         w->A32 = (float*)(b + oA);
@@ -703,6 +712,7 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w) {
         w->gW = (double*)(b + ogW);
         w->gP = (double*)(b + ogP);
         w->gC = (double*)(b + ogC);
+        w->qws = qr ? b + oQ : nullptr;
     }
     return off;
 }
@@ -723,8 +733,11 @@ static __global__ void pos_iota_kernel(int* pos, int n) {
 // The mixed solve: the fp32 factorization (LU with partial or tournament
 // pivoting; for spd, Cholesky rewritten as the packed LU of the same
 // matrix), then plain refinement, GMRES-IR and the FP64 fallback.
+enum class MixedKind { LU, SPD, QR };
+
 static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B, int ldb,
-                               double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* rep, bool spd) {
+                               double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* rep, MixedKind kind) {
+    const bool spd = kind == MixedKind::SPD, qr = kind == MixedKind::QR;
     using clk = std::chrono::steady_clock;
     if (!h) return MG_ERR_ARG;
     if (n < 0 || nrhs < 0 || nrhs > MAX_RHS || lda < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1) ||
@@ -744,10 +757,10 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
     if (!A || !B || !X) return mg::fail(h, MG_ERR_ARG, "mixed solve: null pointer");
 
     const auto t0 = clk::now();
-    MG_TRY(mg::ensure_ws(h, carve_ir(h, n, nrhs, o.nterms, nullptr)));
+    MG_TRY(mg::ensure_ws(h, carve_ir(h, n, nrhs, o.nterms, nullptr, qr)));
     MG_TRY(mg::ensure_hws(h, 512 + sizeof(double) * GM_CTAS * (GM_RESTART + 1) * MAX_RHS));
     IrWs w;
-    carve_ir(h, n, nrhs, o.nterms, &w);
+    carve_ir(h, n, nrhs, o.nterms, &w, qr);
     cudaStream_t st = h->stream;
     const int cap = h->num_sms * 8;
     const int kch = (n + RES_KCHUNK - 1) / RES_KCHUNK;
@@ -797,6 +810,10 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
             return MG_FALLBACK_USED;
         }
         MG_TRY(mg::chol_to_lu_f32(h, n, w.A32, n, w.Y));
+    } else if (qr) {
+        // Householder QR of the fp32 copy: R and the reflectors in A32, T blocks
+        // in Linv's area, tau (FP64) in Uinv's
+        MG_TRY(mg::sgeqrf_mixed(h, n, n, w.A32, n, (double*)w.Uinv, w.Linv, w.qws, w.gemm_err + 2));
     } else {
         s = mg::sgetrf_mixed(h, n, w.A32, n, w.pos, IR_BLOCK, o.nterms, w.xchg, w.splitA, w.splitA2, w.splitB,
                              w.gemm_err, &info, o.panel == 2);
@@ -805,31 +822,34 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
     r.info = info;
     absmax_upper_kernel<<<n, 256, 0, st>>>(w.A32, n, w.norms + 18);
     MG_TRY(mg::post_launch(h, "absmax_upper_kernel"));
-    MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
-    MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
-    // inverses of the diagonal blocks of L and U (the solves' block steps);
-    // L's blocks are final once their panel is done (later interchanges only
-    // touch rows below them)
-    inv_diag_blocks_kernel<true><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
-                                                                                                 w.Linv);
-    MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<lower>"));
-    inv_diag_blocks_kernel<false><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
-                                                                                                  w.Uinv);
-    MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<upper>"));
-    int flow_cap = 0;
-    switch (nrhs) {
-#define MG_CAP(NRV) \
-    case NRV: flow_cap = trsv_flow_capacity<NRV>(h); break;
-        MG_CAP(1) MG_CAP(2) MG_CAP(3) MG_CAP(4) MG_CAP(5) MG_CAP(6) MG_CAP(7)
-        default: flow_cap = trsv_flow_capacity<8>(h); break;
-#undef MG_CAP
-    }
-    const bool flow = nblk <= flow_cap;
-    if (!flow) {  // launch-per-block-step solves need the pre-inverted block columns
-        mg::ProfScope prof(h, "ir_preinvert", 2.0 * n * (double)n * IR_BLOCK * 6, 8.0 * n * (double)n);
-        MG_TRY(preinvert_blocks(h, w.A32, n, w.Linv, w.Uinv, o.nterms, w.splitA, w.splitB, w.gemm_err));
+    bool flow = false;
+    if (!qr) {
+        MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
+        MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
+        // inverses of the diagonal blocks of L and U (the solves' block steps);
+        // L's blocks are final once their panel is done (later interchanges only
+        // touch rows below them)
+        inv_diag_blocks_kernel<true><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
+                                                                                                     w.Linv);
+        MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<lower>"));
+        inv_diag_blocks_kernel<false><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
+                                                                                                      w.Uinv);
+        MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<upper>"));
+        int flow_cap = 0;
+        switch (nrhs) {
+    #define MG_CAP(NRV) \
+        case NRV: flow_cap = trsv_flow_capacity<NRV>(h); break;
+            MG_CAP(1) MG_CAP(2) MG_CAP(3) MG_CAP(4) MG_CAP(5) MG_CAP(6) MG_CAP(7)
+            default: flow_cap = trsv_flow_capacity<8>(h); break;
+    #undef MG_CAP
+        }
+        flow = nblk <= flow_cap;
+        if (!flow) {  // launch-per-block-step solves need the pre-inverted block columns
+            mg::ProfScope prof(h, "ir_preinvert", 2.0 * n * (double)n * IR_BLOCK * 6, 8.0 * n * (double)n);
+            MG_TRY(preinvert_blocks(h, w.A32, n, w.Linv, w.Uinv, o.nterms, w.splitA, w.splitB, w.gemm_err));
+        }
     }
     MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
     const auto t1 = clk::now();
@@ -863,12 +883,12 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
             MG_TRY(mg::post_launch(h, "residual_reduce_kernel"));
         }
         MG_CHECK_CUDA(h, cudaMemcpyAsync(hn, w.norms, 32 * sizeof(double), cudaMemcpyDeviceToHost, st));
-        int* herr = (int*)(hn + 48);  // device error words: split GEMM, triangular solves
-        MG_CHECK_CUDA(h, cudaMemcpyAsync(herr, w.gemm_err, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        int* herr = (int*)(hn + 48);  // device error words: split GEMM, triangular solves, QR panel
+        MG_CHECK_CUDA(h, cudaMemcpyAsync(herr, w.gemm_err, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
         MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
-        if (herr[0] || herr[1])
+        if (herr[0] || herr[1] || herr[2])
             return mg::fail(h, MG_TIMEOUT, "mixed solve: a bounded device wait timed out (%s)",
-                            herr[0] ? "split GEMM" : "triangular solve");
+                            herr[0] ? "split GEMM" : herr[1] ? "triangular solve" : "QR panel");
         const double anorm = hn[16];
         double eta = 0.0;
         for (int j = 0; j < nrhs; ++j) {
@@ -905,6 +925,13 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
         }
         if (it == o.max_iter) break;
         prev_eta = eta;
+        if (qr) {  // correction d = R^{-1} Q^T r in FP64 with the fp32 factors, x += d
+            mg::ProfScope ps(h, "ir_qr_solve", 4.0 * n * (double)n * nrhs, 6.0 * n * (double)n);
+            MG_TRY(mg::qr_solve_f32_factors(h, n, nrhs, w.A32, n, w.Linv, w.R, n, w.gW, n, w.qws));
+            add_correction_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(n, nrhs, w.gW, X, ldx);
+            MG_TRY(mg::post_launch(h, "add_correction_kernel"));
+            continue;
+        }
         // correction: d = U^-1 L^-1 P (r / s), x += s d
         for (int j = 0; j < nrhs; ++j) hn[24 + j] = hn[j];
         MG_CHECK_CUDA(h, cudaMemcpyAsync(w.norms + 24, hn + 24, MAX_RHS * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -933,7 +960,12 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
     // M^{-1}, M = P^T L U), from x = 0.  Needs the factors as factored (the
     // launch-per-block solves of very large n pre-invert L's and U's block
     // columns in place).
-    if (!converged && o.gmres && flow) {
+    // the preconditioner of GMRES-IR: M^{-1} applied in FP64 with the fp32 factors
+    auto precond = [&](const double* Src, double* Dst) -> mg_status_t {
+        if (qr) return mg::qr_solve_f32_factors(h, n, nrhs, w.A32, n, w.Linv, Src, n, Dst, n, w.qws);
+        return mg::lu_solve_f32_factors(h, n, nrhs, w.A32, n, w.pos, Src, n, Dst, n);
+    };
+    if (!converged && o.gmres && (flow || qr)) {
         constexpr int kOuter = 10;
         constexpr double kInnerTol = 1e-8;
         const int pstride = (GM_RESTART + 1) * nrhs;
@@ -981,7 +1013,7 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
             prev_eta = eta;
             mg::ProfScope pg(h, "gmres", 0.0, 0.0);
             // V_0 = z / beta, z = M^{-1} r
-            MG_TRY(mg::lu_solve_f32_factors(h, n, nrhs, w.A32, n, w.pos, w.R, n, w.gW, n));
+            MG_TRY(precond(w.R, w.gW));
             MG_TRY(dots(w.gW, 1, w.gW));
             for (int j = 0; j < nrhs; ++j) {
                 beta[j] = std::sqrt(coef[j]);
@@ -1000,7 +1032,7 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
                 MG_TRY(launch_av(Vk, n));
                 matvec_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kch, n, nrhs, w.R);
                 MG_TRY(mg::post_launch(h, "matvec_reduce_kernel"));
-                MG_TRY(mg::lu_solve_f32_factors(h, n, nrhs, w.A32, n, w.pos, w.R, n, w.gW, n));
+                MG_TRY(precond(w.R, w.gW));
                 // classical Gram-Schmidt, twice
                 for (int pass = 0; pass < 2; ++pass) {
                     MG_TRY(dots(w.gV, k + 1, w.gW));
@@ -1077,10 +1109,15 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
 
 extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
                                     int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* rep) {
-    return mixed_solve(h, n, nrhs, A, lda, B, ldb, X, ldx, opts, rep, false);
+    return mixed_solve(h, n, nrhs, A, lda, B, ldb, X, ldx, opts, rep, MixedKind::LU);
 }
 
 extern "C" mg_status_t mg_dsposv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
                                     int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* rep) {
-    return mixed_solve(h, n, nrhs, A, lda, B, ldb, X, ldx, opts, rep, true);
+    return mixed_solve(h, n, nrhs, A, lda, B, ldb, X, ldx, opts, rep, MixedKind::SPD);
+}
+
+extern "C" mg_status_t mg_dsqrsv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
+                                    int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* rep) {
+    return mixed_solve(h, n, nrhs, A, lda, B, ldb, X, ldx, opts, rep, MixedKind::QR);
 }

@@ -1,0 +1,371 @@
+// Mixed-precision Householder QR: the FP32 form of Mat's blocked Householder
+// QR (Mat-8.3.1/QR/__Householder_Blocked.h:63-245, FP64 there) for the mixed
+// QR solve.  Panels of QB = 128 columns; per column the norm, beta and tau
+// are formed in FP64 from the fp32 column (the reflector generation
+// spec keeps in FP64), the vector and the panel's other columns in
+// fp32; the compact WY factor T in fp32; the trailing update
+// R2 -= V (T^T (V^T R2)) as three FP32 GEMMs whose large products run on the
+// split-BF16 tensor cores (sgemm_auto: 3 terms, lower-order products first,
+// fp32 accumulation).
+//
+// Reflector c of a panel: x = the column from row c down, alpha = x_c,
+// beta = -sign(alpha) sqrt(alpha^2 + |x below c|^2), tau = (beta - alpha) /
+// beta, v = x / (alpha - beta) below c, v_c = 1 (LAPACK's dlarfg, which Mat's
+// blocked panel also follows, :63-84); R(c,c) = beta.  H = I - tau v v^T.
+//
+// The panel runs as one cooperative grid: its rows dealt to P CTAs in
+// contiguous runs (the slab in shared memory); per column two bounded grid
+// barriers (the norm's partial sums, then the dot products of v with the
+// panel's other columns), every CTA summing the partials in the same order.
+#include <cmath>
+
+#include "grid_sync.cuh"
+#include "mg_internal.cuh"
+
+namespace {
+
+constexpr int QB = 128;
+constexpr int QP_THREADS = 256;
+
+__device__ __forceinline__ double block_sum(double v, double* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int u = 0; u < QP_THREADS / 32; ++u) t += red[u];
+    return t;
+}
+
+// xp: [P][QB + 2] doubles (norm partial, unused, dot partials); x0: the
+// column's diagonal element, published by its owner; tau (w doubles); V the
+// explicit reflectors (h x w, ld ldv: 1 on the diagonal, 0 above).
+__global__ void __launch_bounds__(QP_THREADS, 1)
+    qr_panel_f32_kernel(float* __restrict__ A, int lda, int m, int j0, int w, int rpc, float* __restrict__ V, int ldv,
+                        double* __restrict__ tau, double* __restrict__ xp, double* __restrict__ x0, unsigned* bar,
+                        int* err) {
+    extern __shared__ __align__(16) float slab[];  // [w][rpc]
+    __shared__ double red[QP_THREADS / 32];
+    __shared__ double s_coef[QB];                  // tau * (v . a_jj) for the update
+    __shared__ double s_tau, s_scal, s_beta;
+    __shared__ int s_ok;
+    const int P = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int h = m - j0;
+    const int r0 = b * rpc, r1 = min(h, r0 + rpc);
+    float* const P0 = A + j0 + (size_t)j0 * lda;
+    const int stride = QB + 2;
+    for (int e = tid; e < w * rpc; e += QP_THREADS) {
+        const int c = e / rpc, i = e - c * rpc;
+        slab[e] = r0 + i < h ? P0[r0 + i + (size_t)c * lda] : 0.f;
+    }
+    __syncthreads();
+    unsigned target = 0;
+    bool ok = true;
+    for (int c = 0; c < w && ok; ++c) {
+        float* col = slab + (size_t)c * rpc;
+        // 1. partial sum of squares below the diagonal; the owner publishes x_c
+        double s = 0.0;
+        for (int i = tid; i < rpc; i += QP_THREADS) {
+            const int gi = r0 + i;
+            if (gi > c && gi < h) {
+                const double x = col[i];
+                s = fma(x, x, s);
+            }
+        }
+        s = block_sum(s, red);
+        if (tid == 0) {
+            xp[(size_t)b * stride] = s;
+            if (c >= r0 && c < r1) *x0 = col[c - r0];
+        }
+        target += P;
+        ok = mg::grid_barrier(bar, target, err);
+        if (!ok) break;
+        // 2. beta, tau (FP64, identical in every CTA); scale my part of v
+        if (tid == 0) {
+            double xn2 = 0.0;
+            for (int u = 0; u < P; ++u) xn2 += __ldcg(&xp[(size_t)u * stride]);
+            const double alpha = __ldcg(x0);
+            if (xn2 == 0.0) {  // nothing below the diagonal: H = I
+                s_tau = 0.0;
+                s_scal = 0.0;
+                s_beta = alpha;
+            } else {
+                const double beta = -copysign(sqrt(fma(alpha, alpha, xn2)), alpha);
+                s_tau = (beta - alpha) / beta;
+                s_scal = 1.0 / (alpha - beta);
+                s_beta = beta;
+            }
+            if (b == 0) tau[c] = s_tau;
+        }
+        __syncthreads();
+        const double tc = s_tau;
+        for (int i = tid; i < rpc; i += QP_THREADS) {
+            const int gi = r0 + i;
+            if (gi > c && gi < h) col[i] = (float)(col[i] * s_scal);
+            else if (gi == c) col[i] = (float)s_beta;
+        }
+        __syncthreads();
+        // 3. partial dots v . a_jj for the panel's later columns (v_c = 1), a warp per column
+        for (int jj = c + 1 + warp; jj < w; jj += QP_THREADS / 32) {
+            const float* a = slab + (size_t)jj * rpc;
+            double d = 0.0;
+            for (int i = lane; i < rpc; i += 32) {
+                const int gi = r0 + i;
+                if (gi == c) d += a[i];
+                else if (gi > c && gi < h) d = fma((double)col[i], (double)a[i], d);
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xffffffffu, d, off);
+            if (lane == 0) xp[(size_t)b * stride + 2 + jj] = d;
+        }
+        target += P;
+        ok = mg::grid_barrier(bar, target, err);
+        if (!ok) break;
+        // 4. a_jj -= (tau (v . a_jj)) v on my rows
+        for (int jj = c + 1 + tid; jj < w; jj += QP_THREADS) {
+            double d = 0.0;
+            for (int u = 0; u < P; ++u) d += __ldcg(&xp[(size_t)u * stride + 2 + jj]);
+            s_coef[jj] = tc * d;
+        }
+        __syncthreads();
+        for (int e = tid; e < (w - c - 1) * rpc; e += QP_THREADS) {
+            const int jj = c + 1 + e / rpc, i = e % rpc, gi = r0 + i;
+            if (gi >= c && gi < h) {
+                float* a = slab + (size_t)jj * rpc;
+                const float vi = gi == c ? 1.f : col[i];
+                a[i] = fmaf((float)(-s_coef[jj]), vi, a[i]);
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) s_ok = ok ? 1 : 0;
+    __syncthreads();
+    // write back: R (upper, diagonal = beta) and v below it; V explicit
+    for (int e = tid; e < w * rpc; e += QP_THREADS) {
+        const int c = e / rpc, i = e - c * rpc, gi = r0 + i;
+        if (gi < h) {
+            P0[gi + (size_t)c * lda] = slab[e];
+            V[gi + (size_t)c * ldv] = gi < c ? 0.f : gi == c ? 1.f : slab[e];
+        }
+    }
+}
+
+// T (w x w, upper, fp32, ld QB) of H_0 ... H_{w-1} = I - V T V^T from
+// G = V^T V: T(c,c) = tau_c, T(0:c, c) = -tau_c T(0:c, 0:c) G(0:c, c), summed
+// in FP64.  One CTA of QB threads; T's columns in dynamic shared memory.
+__global__ void qr_tfactor_kernel(const float* __restrict__ G, int ldg, const double* __restrict__ tau, int w,
+                                  float* __restrict__ T) {
+    extern __shared__ float t[];  // [QB][QB + 1]: t[r * (QB + 1) + c]
+    constexpr int LD = QB + 1;
+    for (int e = threadIdx.x; e < QB * LD; e += blockDim.x) t[e] = 0.f;
+    __syncthreads();
+    const int r = threadIdx.x;
+    for (int c = 0; c < w; ++c) {
+        double sr = 0.0;
+        if (r < c)
+            for (int k = r; k < c; ++k) sr = fma((double)t[r * LD + k], (double)G[k + (size_t)c * ldg], sr);
+        if (r < c) t[r * LD + c] = (float)(-tau[c] * sr);
+        if (r == c) t[c * LD + c] = (float)tau[c];
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < QB * QB; e += blockDim.x) {
+        const int rr = e % QB, cc = e / QB;
+        T[e] = (rr < w && cc < w) ? t[rr * LD + cc] : 0.f;
+    }
+}
+
+// ---- Q^T applied to X (n x nrhs, FP64) with the fp32 reflectors of one panel
+// (A32 below the diagonal of columns j0 .. j0+w, v_c = 1) and its T, in FP64:
+// X(j0:, :) -= V (T^T (V^T X(j0:, :))).
+constexpr int QT_CTAS = 64;
+
+__global__ void qt_dots_kernel(const float* __restrict__ A, int lda, int m, int j0, int w, const double* __restrict__ X,
+                               int ldx, int nrhs, double* __restrict__ part) {
+    const int h = m - j0;
+    const int chunk = (h + gridDim.x - 1) / gridDim.x;
+    const int lo = blockIdx.x * chunk, hi = min(h, lo + chunk);
+    for (int q = threadIdx.x; q < w * nrhs; q += blockDim.x) {
+        const int c = q % w, j = q / w;
+        const float* v = A + j0 + (size_t)(j0 + c) * lda;
+        const double* x = X + j0 + (size_t)j * ldx;
+        double d = 0.0;
+        for (int i = max(lo, c); i < hi; ++i) d = fma(i == c ? 1.0 : (double)v[i], x[i], d);
+        part[(size_t)blockIdx.x * w * nrhs + q] = d;
+    }
+}
+
+__global__ void qt_tw_kernel(const double* __restrict__ part, int nparts, const float* __restrict__ T, int w, int nrhs,
+                             double* __restrict__ y) {
+    __shared__ double wv[QB * 8];
+    for (int q = threadIdx.x; q < w * nrhs; q += blockDim.x) {
+        double d = 0.0;
+        for (int u = 0; u < nparts; ++u) d += part[(size_t)u * w * nrhs + q];
+        wv[q] = d;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < w * nrhs; q += blockDim.x) {
+        const int c = q % w, j = q / w;
+        double d = 0.0;
+        for (int k = 0; k <= c; ++k) d = fma((double)T[k + (size_t)c * QB], wv[k + j * w], d);  // (T^T w)_c
+        y[q] = d;
+    }
+}
+
+__global__ void qt_update_kernel(const float* __restrict__ A, int lda, int m, int j0, int w, const double* __restrict__ y,
+                                 int nrhs, double* __restrict__ X, int ldx) {
+    const int h = m - j0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < h; i += gridDim.x * blockDim.x) {
+        const int cmax = min(w - 1, i);
+        for (int j = 0; j < nrhs; ++j) {
+            double acc = X[j0 + i + (size_t)j * ldx];
+            for (int c = 0; c <= cmax; ++c) {
+                const double v = c == i ? 1.0 : (double)A[j0 + i + (size_t)(j0 + c) * lda];
+                acc = fma(-v, y[c + j * w], acc);
+            }
+            X[j0 + i + (size_t)j * ldx] = acc;
+        }
+    }
+}
+
+__global__ void copy_f64_kernel(int n, int nrhs, const double* __restrict__ B, int ldb, double* __restrict__ X,
+                                int ldx) {
+    const size_t total = (size_t)n * nrhs;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
+        X[(e % n) + (e / n) * (size_t)ldx] = B[(e % n) + (e / n) * (size_t)ldb];
+}
+
+}  // namespace
+
+namespace mg {
+
+size_t qr_mixed_ws_bytes(int m, int n, int num_sms) {
+    const int P = num_sms;
+    return align_up((size_t)m * QB * sizeof(float), 1024)                  // V
+           + align_up((size_t)QB * n * sizeof(float), 1024) * 2             // W, W2
+           + align_up((size_t)QB * QB * sizeof(float), 1024)                // G
+           + align_up((size_t)P * (QB + 2) * sizeof(double), 1024)          // panel partials
+           + align_up((size_t)QT_CTAS * QB * 8 * sizeof(double), 1024)      // Q^T partials
+           + align_up((size_t)QB * 8 * sizeof(double), 1024)                // T^T w
+           + 4096;                                                          // barrier, x0, error
+}
+
+// In-place FP32 Householder QR of the m x n (m >= n) matrix A (ld lda):
+// R on and above the diagonal, the reflectors below it (v_c = 1 implicit);
+// tau (n doubles), T (ceil(n / QB) blocks of QB x QB fp32).  ws holds
+// qr_mixed_ws_bytes(m, n, num_sms); err receives MG_TIMEOUT from a panel wait.
+mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double* tau, float* T, void* ws, int* err) {
+    if (n == 0) return MG_OK;
+    const int P0max = h->num_sms;
+    char* p = (char*)ws;
+    auto take = [&](size_t bytes) { char* q = p; p += align_up(bytes, 1024); return q; };
+    float* V = (float*)take((size_t)m * QB * sizeof(float));
+    float* W = (float*)take((size_t)QB * n * sizeof(float));
+    float* W2 = (float*)take((size_t)QB * n * sizeof(float));
+    float* G = (float*)take((size_t)QB * QB * sizeof(float));
+    double* xp = (double*)take((size_t)P0max * (QB + 2) * sizeof(double));
+    take((size_t)QT_CTAS * QB * 8 * sizeof(double));
+    take((size_t)QB * 8 * sizeof(double));
+    unsigned* bar = (unsigned*)p;
+    double* x0 = (double*)(p + 256);
+    const cudaStream_t st = h->stream;
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(qr_panel_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          h->max_smem_optin - 4096));
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(qr_tfactor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)(QB * (QB + 1) * sizeof(float))));
+    for (int j0 = 0; j0 < n; j0 += QB) {
+        const int w = n - j0 < QB ? n - j0 : QB;
+        const int hgt = m - j0;
+        int P = (hgt + 255) / 256;
+        if (P > P0max) P = P0max;
+        int rpc = (hgt + P - 1) / P;
+        while ((size_t)rpc * w * sizeof(float) > (size_t)h->max_smem_optin - 4096 && P < P0max) {
+            ++P;
+            rpc = (hgt + P - 1) / P;
+        }
+        const size_t smem = (size_t)rpc * w * sizeof(float);
+        if (smem > (size_t)h->max_smem_optin - 4096)
+            return fail(h, MG_ERR_UNSUPPORTED, "sgeqrf_mixed: panel of %d rows does not fit the SMs", hgt);
+        {
+            ProfScope prof(h, "qr_panel_f32", 4.0 * hgt * (double)w * w / 2, 8.0 * hgt * (double)w);
+            MG_CHECK_CUDA(h, cudaMemsetAsync(bar, 0, sizeof(unsigned), st));
+            int lda_ = lda, m_ = m, j0_ = j0, w_ = w, rpc_ = rpc, ldv = hgt;
+            float* A_ = A;
+            double* tau_ = tau + j0;
+            void* args[] = {&A_, &lda_, &m_, &j0_, &w_, &rpc_, &V, &ldv, &tau_, &xp, &x0, &bar, &err};
+            const cudaError_t e = cudaLaunchCooperativeKernel((const void*)qr_panel_f32_kernel, dim3(P),
+                                                              dim3(QP_THREADS), args, smem, st);
+            if (e != cudaSuccess) return cuda_fail(h, e, "qr_panel_f32_kernel launch");
+            h->launches++;
+        }
+        float* Tb = T + (size_t)(j0 / QB) * QB * QB;
+        MG_TRY(sgemm_auto(h, 1, 0, w, w, hgt, 1.f, V, hgt, V, hgt, 0.f, G, QB, 0));
+        qr_tfactor_kernel<<<1, QB, QB * (QB + 1) * sizeof(float), st>>>(G, QB, tau + j0, w, Tb);
+        MG_TRY(post_launch(h, "qr_tfactor_kernel"));
+        const int nt = n - j0 - w;
+        if (nt > 0) {  // R2 -= V (T^T (V^T R2))
+            float* R2 = A + j0 + (size_t)(j0 + w) * lda;
+            MG_TRY(sgemm_auto(h, 1, 0, w, nt, hgt, 1.f, V, hgt, R2, lda, 0.f, W, QB, 0));
+            MG_TRY(sgemm_auto(h, 1, 0, w, nt, w, 1.f, Tb, QB, W, QB, 0.f, W2, QB, 0));
+            MG_TRY(sgemm_auto(h, 0, 0, hgt, nt, w, -1.f, V, hgt, W2, QB, 1.f, R2, lda, 0));
+        }
+    }
+    return MG_OK;
+}
+
+// X := R^{-1} (Q^T B)(0:n) in FP64 for the fp32 factors of sgeqrf_mixed
+// (square use: m = n): Q^T applied panel by panel, then the upper solve.
+mg_status_t qr_solve_f32_factors(mg_handle_t h, int n, int nrhs, const float* A, int lda, const float* T,
+                                 const double* B, int ldb, double* X, int ldx, void* ws) {
+    if (n == 0 || nrhs == 0) return MG_OK;
+    if (nrhs > 8) return fail(h, MG_ERR_ARG, "qr_solve_f32_factors: at most 8 right-hand sides");
+    char* p = (char*)ws;
+    auto take = [&](size_t bytes) { char* q = p; p += align_up(bytes, 1024); return q; };
+    take((size_t)n * QB * sizeof(float));
+    take((size_t)QB * n * sizeof(float));
+    take((size_t)QB * n * sizeof(float));
+    take((size_t)QB * QB * sizeof(float));
+    take((size_t)h->num_sms * (QB + 2) * sizeof(double));
+    double* part = (double*)take((size_t)QT_CTAS * QB * 8 * sizeof(double));
+    double* y = (double*)take((size_t)QB * 8 * sizeof(double));
+    const cudaStream_t st = h->stream;
+    const int cap = h->num_sms * 8;
+    int g = (int)(((size_t)n * nrhs + 255) / 256);
+    copy_f64_kernel<<<g < cap ? g : cap, 256, 0, st>>>(n, nrhs, B, ldb, X, ldx);
+    MG_TRY(post_launch(h, "copy_f64_kernel"));
+    for (int j0 = 0; j0 < n; j0 += QB) {
+        const int w = n - j0 < QB ? n - j0 : QB;
+        qt_dots_kernel<<<QT_CTAS, 256, 0, st>>>(A, lda, n, j0, w, X, ldx, nrhs, part);
+        MG_TRY(post_launch(h, "qt_dots_kernel"));
+        qt_tw_kernel<<<1, 256, 0, st>>>(part, QT_CTAS, T + (size_t)(j0 / QB) * QB * QB, w, nrhs, y);
+        MG_TRY(post_launch(h, "qt_tw_kernel"));
+        int gu = (n - j0 + 255) / 256;
+        qt_update_kernel<<<gu < cap ? gu : cap, 256, 0, st>>>(A, lda, n, j0, w, y, nrhs, X, ldx);
+        MG_TRY(post_launch(h, "qt_update_kernel"));
+    }
+    return upper_solve_f32_factors(h, n, nrhs, A, lda, X, ldx);
+}
+
+}  // namespace mg
+
+extern "C" mg_status_t mg_sgeqrf(mg_handle_t h, int m, int n, float* A, int lda, double* tau, float* T) {
+    if (!h) return MG_ERR_ARG;
+    if (m < 0 || n < 0 || m < n || lda < (m > 1 ? m : 1) || (n && (!A || !tau || !T)))
+        return mg::fail(h, MG_ERR_ARG, "mg_sgeqrf: bad arguments (m=%d n=%d lda=%d; m >= n)", m, n, lda);
+    if (n == 0) return MG_OK;
+    const size_t wsb = mg::qr_mixed_ws_bytes(m, n, h->num_sms);
+    MG_TRY(mg::ensure_ws(h, wsb + 256));
+    MG_TRY(mg::ensure_hws(h, 64));
+    int* err = (int*)((char*)h->ws + wsb);
+    MG_CHECK_CUDA(h, cudaMemsetAsync(err, 0, sizeof(int), h->stream));
+    MG_TRY(mg::sgeqrf_mixed(h, m, n, A, lda, tau, T, h->ws, err));
+    int* hw = (int*)h->hws;
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (hw[0]) return mg::fail(h, MG_TIMEOUT, "mg_sgeqrf: a panel grid barrier timed out");
+    int terr = 0;
+    MG_TRY(mg::tc_sgemm_error(h, &terr));
+    if (terr) return mg::fail(h, MG_TIMEOUT, "mg_sgeqrf: a tensor-core update's bounded wait gave up");
+    return MG_OK;
+}

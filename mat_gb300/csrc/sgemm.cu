@@ -157,27 +157,29 @@ namespace {
 
 int tc_slot(mg_handle_t h) { return h->stream && h->stream == h->la_stream ? 1 : h->stream && h->stream == h->pp_stream ? 2 : 0; }
 
-constexpr size_t kTcErrBytes = 4096;
-
-// Grows the tensor-core split area to three regions of `region` bytes.  A
-// growth waits for the whole device: a region may be in use on any of the
-// handle's streams.
-mg_status_t ensure_tcws(mg_handle_t h, size_t region) {
-    region = align_up(region, 1 << 20);
-    if (h->tcws && kTcErrBytes + 3 * region <= h->tcws_bytes) return MG_OK;
-    if (h->tcws) {
-        MG_CHECK_CUDA(h, cudaDeviceSynchronize());
-        MG_CHECK_CUDA(h, cudaFree(h->tcws));
-        h->tcws = nullptr;
-        h->tcws_bytes = 0;
+// Grows the split area of `slot` to `bytes`.  A growth waits for the whole
+// device: the area may be in use on any of the handle's streams.
+mg_status_t ensure_tcws(mg_handle_t h, int slot, size_t bytes) {
+    if (!h->tcerr) {
+        if (cudaMalloc((void**)&h->tcerr, 3 * 64 * sizeof(int)) != cudaSuccess) {
+            h->tcerr = nullptr;
+            return fail(h, MG_ERR_ALLOC, "tensor-core GEMM error words: cudaMalloc failed");
+        }
+        MG_CHECK_CUDA(h, cudaMemset(h->tcerr, 0, 3 * 64 * sizeof(int)));
     }
-    const size_t bytes = kTcErrBytes + 3 * region;
-    if (cudaMalloc(&h->tcws, bytes) != cudaSuccess) {
-        h->tcws = nullptr;
+    if (bytes <= h->tcws_bytes[slot]) return MG_OK;
+    bytes = align_up(bytes + (bytes >> 3), 1 << 20);
+    if (h->tcws[slot]) {
+        MG_CHECK_CUDA(h, cudaDeviceSynchronize());
+        MG_CHECK_CUDA(h, cudaFree(h->tcws[slot]));
+        h->tcws[slot] = nullptr;
+        h->tcws_bytes[slot] = 0;
+    }
+    if (cudaMalloc(&h->tcws[slot], bytes) != cudaSuccess) {
+        h->tcws[slot] = nullptr;
         return fail(h, MG_ERR_ALLOC, "tensor-core GEMM area cudaMalloc(%zu) failed", bytes);
     }
-    MG_CHECK_CUDA(h, cudaMemset(h->tcws, 0, kTcErrBytes));
-    h->tcws_bytes = bytes;
+    h->tcws_bytes[slot] = bytes;
     return MG_OK;
 }
 
@@ -189,11 +191,10 @@ mg_status_t sgemm_auto(mg_handle_t h, int ta, int tb, int m, int n, int k, float
         return sgemm_launch(h, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri);
     constexpr int np = 3;
     const size_t as = align_up(bf16x_split_bytes(m, k, np), 1024), bs = align_up(bf16x_split_bytes(n, k, np), 1024);
-    MG_TRY(ensure_tcws(h, as + bs));
-    const size_t region = (h->tcws_bytes - kTcErrBytes) / 3;
     const int slot = tc_slot(h);
-    char* base = (char*)h->tcws + kTcErrBytes + (size_t)slot * region;
-    int* err = (int*)h->tcws + 64 * slot;
+    MG_TRY(ensure_tcws(h, slot, as + bs));
+    char* base = (char*)h->tcws[slot];
+    int* err = h->tcerr + 64 * slot;
     // op(A) rows as split rows: A itself (ta = 0) or the columns of A (ta = 1);
     // op(B) columns as split rows: the columns of B (tb = 0) or its rows (tb = 1)
     MG_TRY(bf16x_split<float>(h, ta == 0, A, lda, m, k, np, base));
@@ -203,9 +204,9 @@ mg_status_t sgemm_auto(mg_handle_t h, int ta, int tb, int m, int n, int k, float
 
 mg_status_t tc_sgemm_error(mg_handle_t h, int* err_out) {
     *err_out = 0;
-    if (!h->tcws) return MG_OK;
+    if (!h->tcerr) return MG_OK;
     int e[3 * 64];
-    MG_CHECK_CUDA(h, cudaMemcpyAsync(e, h->tcws, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
+    MG_CHECK_CUDA(h, cudaMemcpyAsync(e, h->tcerr, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
     MG_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
     *err_out = e[0] | e[64] | e[128];
     return MG_OK;
