@@ -42,7 +42,7 @@ def test_sgeqrf_reconstructs_A(handle, m, n):
     torch.cuda.synchronize()
     QR, R, V = rebuild(Af, tau)
     rel = float((A - QR).norm() / A.norm())
-    assert rel < 2e-6, rel
+    assert rel < 4e-8 * np.sqrt(m * n) ** 0.5 * 10, rel  # fp32 rounding, growing mildly with size
     assert bool((tau >= 0).all()) and bool((tau <= 2).all())
     # |diag R| against the FP64 QR of the same matrix (signs follow the same convention)
     Ad = A.clone()
