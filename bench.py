@@ -1,7 +1,7 @@
 """Benchmark of the GB300 hot path of Mat (mixed LU + FP64 refinement solve).
 
-Headline (BASELINE metric "n=16384 LU-solve time at FP64 backward error,
-mixed+IR vs FP64; DGEMM TFLOP/s"):
+Headline (metric "n=16384 LU-solve time at FP64 backward error, mixed+IR vs
+FP64; DGEMM TFLOP/s"):
   one step = one mixed-precision LU solve with FP64 iterative refinement,
   n = 16384, 4 right-hand sides, A = Q1 diag(sigma) Q2 (Q = 64 seeded
   Householder reflectors each side, sigma geometric 1 -> 1e-6, cond 1e6),
@@ -167,11 +167,16 @@ def config_rates(h, dmma_tf: float, bf16_tf: float) -> dict:
     """The other configurations, measured after the headline (each timed once
     after a warm-up call, wall clock around a synchronised call): FP64 LU +
     solve, LLT (n = 8192, seed 1) and Householder QR (16384 x 4096: R alone
-    and with the full 16384 x 16384 Q); the M=N=K=16384 split-BF16 GEMM on
-    u*2^e entries (seed 3) with its error against FP64 on 256 sampled rows;
-    the Gaussian-process loss + gradient (Cholesky adjoint) at n = 8192; the
-    Mat-8.1 EVD_Q (tridiagonalisation with Q, and the whole eigendecomposition)
-    at n = 1024 and 4096."""
+    and with the full 16384 x 16384 Q), and the mixed QR's fp32 factorization
+    of the same matrix; the mixed QR solve of the benchmark recipe at
+    n = 8192 beside the mixed and FP64 LU solves; the M=N=K=16384 split-BF16
+    GEMM on u*2^e entries (seed 3) with its error against FP64 on 256 sampled
+    rows, and the SIMT FP32 GEMM's error on the same inputs; the
+    Gaussian-process loss + gradient (Cholesky adjoint) at n = 8192 in FP64 and
+    FP32, and the mixed SPD solve of its kernel matrix; GMRES-IR at n = 16384,
+    cond 1e10; the mixed solve with tournament panels; the Mat-8.1 EVD_Q
+    (tridiagonalisation with Q, and the whole eigendecomposition) at n = 1024
+    and 4096."""
     import ctypes as C
 
     import torch
@@ -236,7 +241,42 @@ def config_rates(h, dmma_tf: float, bf16_tf: float) -> dict:
     # flop counts: R 2mk^2 - 2k^3/3; full m x m Q from k reflectors (LAPACK dorgqr) 4m^2k - 4mk^2 + 4k^3/3
     fr, fq = 2 * m * k * k - 2 / 3 * k ** 3, 4 * m * m * k - 4 * m * k * k + 4 / 3 * k ** 3
     out["qr_16384x4096"] = {"r_factor": rate(fr, t_r, dmma_tf), "with_full_q": rate(fr + fq, t_q, dmma_tf)}
-    del Q0, Qa, Qf, Rf, tau, T
+    del Qf, Rf, tau, T
+    torch.cuda.empty_cache()
+    # the mixed QR's fp32 factorization (FP64 norm/beta/tau, split-BF16 trailing
+    # updates) of the same 16384 x 4096 matrix, against the FP64 R factor above
+    Q32 = Q0.float().t().contiguous().t()
+    Qs = Q32.clone()
+
+    def sgeqrf():
+        Qs.copy_(Q32)
+        return h.sgeqrf(Qs)
+
+    t_s, _ = timed(sgeqrf)
+    h.profile(True)
+    sgeqrf()
+    torch.cuda.synchronize()
+    prs = h.profile_records()
+    h.profile(False)
+    out["sgeqrf_16384x4096"] = {"s": t_s, "useful_tflops": fr / t_s / 1e12, "speedup_vs_fp64_r_factor": t_r / t_s,
+                                "phases_ms": {k: round(v["ms"], 3) for k, v in prs.items()}}
+    del Q0, Qa, Q32, Qs
+    torch.cuda.empty_cache()
+    # the mixed QR solve (benchmark recipe, n = 8192) against the mixed LU solve
+    # and the FP64 LU solve of the same system
+    nq = 8192
+    Aq = colmajor(nq, nq)
+    h.gen_svd_matrix(Aq, 3, nrefl=64, sigma_min=1e-6)
+    Bq = colmajor(nq, 4)
+    h.fill_normal(Bq, 11)
+    t_qs, (Xq, rq) = timed(lambda: h.dsqrsv_ir(Aq, Bq))
+    t_ls, _ = timed(lambda: h.dsgesv_ir(Aq, Bq))
+    t_d, _ = timed(lambda: h.dgesv(Aq, Bq))
+    out["mixed_qr_solve_8192"] = {"s": t_qs, "mixed_lu_solve_s": t_ls, "fp64_lu_solve_s": t_d,
+                                  "iterations": rq["iterations"], "path": rq["path"],
+                                  "backward_error": rq["backward_error"], "factor_ms": rq["factor_ms"],
+                                  "refine_ms": rq["refine_ms"]}
+    del Aq, Bq, Xq
     torch.cuda.empty_cache()
     # split GEMM, entries u * 2^e
     N = 16384

@@ -7,10 +7,9 @@
 // L2 round trips per column, ~4.5 us; inside a 16-CTA cluster each CTA pushes
 // its candidate into every CTA's shared memory and waits on a local barrier.
 // A 16-CTA cluster cannot hold a 16384 x 128 FP32 panel (8 MiB) on chip, so
-// the panel is factored in sub-panels of 16 columns kept in registers
-// (each of the 256 threads of a CTA owns RPT <= 4 rows x 16 columns; the
-// fully unrolled column loop of a 16-column sub-panel stays small enough for
-// the instruction cache):
+// the panel is factored in sub-panels of 16 columns kept in registers (each
+// of the 256 threads of a CTA owns RPT <= 4 rows x 16 columns, in a rotating
+// window so that the column loop stays rolled):
 //
 //   for each sub-panel S = [cs0, cs0+16):
 //     1. load my rows of S into registers
@@ -18,10 +17,11 @@
 //        winner row into shared memory -> warp 0 forms the CTA's 80-byte
 //        record (row, |a| bits, position) and stores it with st.async into
 //        slot [my rank] of every CTA (the diagonal row's owner also sends
-//        that row), completing bytes on the receiver's mbarrier -> wait on
-//        the local mbarrier for 16 records + the diagonal row -> the same
-//        winner in every CTA -> swap in registers -> scale by the reciprocal
-//        -> fused rank-1 update of my rows' remaining columns
+//        that row), completing bytes on the receiver's mbarrier -> every warp
+//        waits on the local mbarrier for 16 records + the diagonal row and
+//        picks the same winner as every other warp and CTA -> swap in
+//        registers -> scale by the reciprocal -> fused rank-1 update of my
+//        rows' remaining columns
 //     3. store S; apply S's interchanges to the panel's other columns and to
 //        pos (one gather/scatter over the touched rows, net permutation kept
 //        in a shared-memory map)
@@ -37,8 +37,11 @@
 //
 // Receive slots and mbarriers are double-buffered by column parity: a CTA
 // sends its record for column c+2 only after receiving every record of
-// column c+1, and every CTA sends that only after it has consumed its slots of
-// column c and re-armed their mbarrier (expect 1344 bytes).  Waits are
+// column c+1, and every CTA sends that only after all of its warps have
+// consumed their slots of column c (its one CTA barrier per column) and warp 0
+// has re-armed their mbarrier (expect 1344 bytes).  The waits acquire at
+// cluster scope, and the other lanes of a warp read the records only after a
+// __syncwarp behind the waiting lane.  Waits are
 // bounded: on a timeout the kernel records MG_TIMEOUT, skips later waits and
 // runs on to the end, so every CTA executes the same cluster barriers.
 // Global loads inside the kernel go to L2 (__ldcg): rows of the panel are
@@ -47,6 +50,7 @@
 #include <cooperative_groups.h>
 
 #include <climits>
+#include <type_traits>
 
 #include "mg_internal.cuh"
 #include "tc_common.cuh"
@@ -74,24 +78,21 @@ struct __align__(16) CpRec {
     int pad[2];
 };
 
+constexpr int CP_NW = CP_THREADS / 32;  // warps per CTA
+constexpr int CP_NREC = CP_CS;          // records a CTA receives per column: one per CTA
+
 struct CpShared {
     float ub[CP_NOTHER][CP_UB_LD];  // U(S, right), [column][row of S]
     float l11[CP_SW][CP_SW + 1];
-    CpRec recv[2][CP_CS];            // every CTA's candidate for the column, by column parity
+    CpRec recv[2][CP_NREC];          // the candidates for the column, by column parity
     __align__(16) float recv_diag[2][CP_SW];  // the row at the diagonal (sent by its owner)
     __align__(8) uint64_t mbar[2];            // receive barriers (transaction bytes), by parity
-    __align__(16) float pubdiag[2][CP_SW];
-    __align__(16) float prow[2][CP_SW];  // the pivot row of a column, by parity
-    __align__(16) float drow[2][CP_SW];  // the row at the diagonal, by parity
-    __align__(16) float wrow[CP_THREADS / 32][CP_SW];  // each warp's candidate row
-    unsigned wbits[CP_THREADS / 32];
-    int wpos[CP_THREADS / 32];
+    CpRec wst[CP_NW];                         // each warp's candidate record, staged for sending
+    __align__(16) float wdiag[CP_NW][CP_SW];  // the diagonal row, staged by the warp holding it
     int piv[CP_MAXW];
     int touch[2 * CP_SW];
     float gbuf[CP_GCOLS * 2 * CP_SW];
     int gpos[2 * CP_SW];
-    int s_win[2];
-    float s_pv[2];
 };
 
 // Tournament pivoting (TOURN): per sub-panel, one exchange of candidate rows
@@ -206,8 +207,8 @@ __device__ __forceinline__ void warp_level(const CpRec* in, int n, int sw, CpRec
     }
 }
 
-// Bytes each CTA receives per column: 16 records and the diagonal row.
-constexpr uint32_t CP_RX_BYTES = CP_CS * sizeof(CpRec) + CP_SW * sizeof(float);
+// Bytes each CTA receives per column: the candidate records and the diagonal row.
+constexpr uint32_t CP_RX_BYTES = CP_NREC * sizeof(CpRec) + CP_SW * sizeof(float);
 
 __device__ __forceinline__ uint32_t cluster_addr(const void* local, int rank) {
     uint32_t out;
@@ -257,7 +258,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         }
     }
     cluster.sync();  // every CTA's receive barriers are armed before the first record is sent
-    bool rx_failed = false;  // warp 0: a receive wait gave up (error recorded; later waits skipped)
+    bool rx_failed = false;  // this warp: a receive wait gave up (error recorded; later waits skipped)
 
     float v[RPT][CP_SW];
     const int nsub = (w + CP_SW - 1) / CP_SW;
@@ -283,124 +284,137 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
 #pragma unroll
             for (int j = 0; j < CP_SW; ++j) v[k][j] = tile[j * RPC + k * CP_THREADS + tid];
 
-        // steps 1-2 for sub-panel column cc: candidates, warp slots, the CTA's record
-        auto publish = [&](const int cc) {
-            const int cabs = cs0 + cc;
-            const int buf = cabs & 1;
-            unsigned bb = 0u;
-            int bp = INT_MAX;
+        if constexpr (!TOURN) {
+            // Column loop over a rotating register window, so that every step runs
+            // the same code at fixed register indices (a rolled loop: the fully
+            // unrolled 16 columns are slower, instruction-fetch bound).  At step c
+            // position 0 of v holds column c and positions 1 .. 15-c columns
+            // c+1 .. 15; each step shifts the window left by one and puts column
+            // c's multipliers (or the untouched column of a finished row) at its
+            // last position.  The first 8 steps shift all 16 positions; the last
+            // 8 columns are then at positions 0..7 and only those shift (half the
+            // update work of a 16-wide window); the halves swap at the end.
+            // Shift positions 0 .. W-1 of every row of mine left by one, n times:
+            auto rotate_n = [&](auto WT, const int n) {
+                constexpr int W = decltype(WT)::value;
+#pragma unroll 1
+                for (int r = 0; r < n; ++r)
 #pragma unroll
-            for (int k = 0; k < RPT; ++k) {
-                const int p = row0 + k * CP_THREADS + tid;
-                const float a = fabsf(v[k][cc]);
-                if (p < R && p >= cabs && a >= 0.f) {  // NaN is never a candidate
-                    const unsigned ab = __float_as_uint(a);
-                    if (ab > bb || bp == INT_MAX) {
-                        bb = ab;
-                        bp = p;
+                    for (int k = 0; k < RPT; ++k) {
+                        const float v0 = v[k][0];
+#pragma unroll
+                        for (int j = 1; j < W; ++j) v[k][j - 1] = v[k][j];
+                        v[k][W - 1] = v0;
+                    }
+            };
+            auto step = [&](auto WT, const int c) {
+                constexpr int W = decltype(WT)::value;  // window width: positions 0 .. W-1 shift
+                const int cabs = cs0 + c;
+                const int buf = cabs & 1;
+                // 1. this thread's and this warp's candidate (first largest |a|
+                //    among the rows at or below the diagonal; NaN never wins)
+                unsigned bb = 0u;
+                int bp = INT_MAX, bk = 0;
+#pragma unroll
+                for (int k = 0; k < RPT; ++k) {
+                    const int p = row0 + k * CP_THREADS + tid;
+                    const float a = fabsf(v[k][0]);
+                    if (p < R && p >= cabs && a >= 0.f) {
+                        const unsigned ab = __float_as_uint(a);
+                        if (ab > bb || bp == INT_MAX) {
+                            bb = ab;
+                            bp = p;
+                            bk = k;
+                        }
                     }
                 }
-            }
-            const unsigned wm = __reduce_max_sync(0xffffffffu, bb);
-            const int wp = (int)__reduce_min_sync(0xffffffffu, bb == wm ? (unsigned)bp : (unsigned)INT_MAX);
-            if (lane == 0) {
-                sh.wbits[warp] = wm;
-                sh.wpos[warp] = wp;
-            }
-            if (wp != INT_MAX && bp == wp) {  // this lane owns the warp's candidate
-                const int kw = (wp - row0) / CP_THREADS;
+                const unsigned wm = __reduce_max_sync(0xffffffffu, bb);
+                const int wp = (int)__reduce_min_sync(0xffffffffu, bb == wm ? (unsigned)bp : (unsigned)INT_MAX);
+                const int dq = cabs / RPC;                         // CTA holding the diagonal row
+                const int dt = q == dq ? cabs - row0 : -1;         // its position in my rows
+                const int dk = dt >= 0 ? dt / CP_THREADS : 0;
+                const int dthr = dt >= 0 ? dt - dk * CP_THREADS : -1;
+                __syncwarp();  // the previous column's staged rows have been read
+                if (wp != INT_MAX && bp == wp) {
+                    float4* s4 = reinterpret_cast<float4*>(sh.wst[warp].row);
 #pragma unroll
-                for (int k = 0; k < RPT; ++k)
-                    if (k == kw) {
+                    for (int k = 0; k < RPT; ++k)
+                        if (k == bk)
 #pragma unroll
-                        for (int j = 0; j < CP_SW; ++j)
-                            sh.wrow[warp][j] = v[k][j];
+                            for (int u4 = 0; u4 < CP_SW / 4; ++u4)
+                                s4[u4] = make_float4(v[k][4 * u4], v[k][4 * u4 + 1], v[k][4 * u4 + 2], v[k][4 * u4 + 3]);
+                }
+                if (lane == 0) {
+                    sh.wst[warp].bits = wm;
+                    sh.wst[warp].pos = wp;
+                }
+                if (tid == dthr) {
+                    float4* d4 = reinterpret_cast<float4*>(sh.wdiag[warp]);
+#pragma unroll
+                    for (int k = 0; k < RPT; ++k)
+                        if (k == dk)
+#pragma unroll
+                            for (int u4 = 0; u4 < CP_SW / 4; ++u4)
+                                d4[u4] = make_float4(v[k][4 * u4], v[k][4 * u4 + 1], v[k][4 * u4 + 2], v[k][4 * u4 + 3]);
+                }
+                __syncthreads();
+                // 2. warp 0: the CTA's record from its warps' records, pushed into
+                //    slot [my rank] of every CTA (lane l -> CTA l); lanes 16..19 push
+                //    the diagonal row if this CTA holds it
+                if (warp == 0) {
+                    const unsigned mb = lane < CP_NW ? sh.wst[lane].bits : 0u;
+                    const int mp = lane < CP_NW ? sh.wst[lane].pos : INT_MAX;
+                    const unsigned cm = __reduce_max_sync(0xffffffffu, mb);
+                    const int cp = (int)__reduce_min_sync(0xffffffffu, mb == cm ? (unsigned)mp : (unsigned)INT_MAX);
+                    const unsigned own = __ballot_sync(0xffffffffu, lane < CP_NW && mp == cp);
+                    const int ww = own ? __ffs(own) - 1 : 0;
+                    if (lane < CS) {
+                        const float4* wr = reinterpret_cast<const float4*>(sh.wst[ww].row);
+                        const uint32_t dst = cluster_addr(&sh.recv[buf][q], lane);
+                        const uint32_t bar = cluster_addr(&sh.mbar[buf], lane);
+#pragma unroll
+                        for (int u4 = 0; u4 < CP_SW / 4; ++u4) st_async16(dst + 16u * u4, wr[u4], bar);
+                        st_async16(dst + 64, make_float4(__uint_as_float(cm), __int_as_float(cp), 0.f, 0.f), bar);
+                    } else if (dthr >= 0) {
+                        const float4* d4 = reinterpret_cast<const float4*>(sh.wdiag[dthr >> 5]);
+                        const uint32_t dst = cluster_addr(&sh.recv_diag[buf][0], lane - CS);
+                        const uint32_t bar = cluster_addr(&sh.mbar[buf], lane - CS);
+#pragma unroll
+                        for (int u4 = 0; u4 < CP_SW / 4; ++u4) st_async16(dst + 16u * u4, d4[u4], bar);
                     }
-            }
-#pragma unroll
-            for (int k = 0; k < RPT; ++k)  // the row at the diagonal, for the swap
-                if (row0 + k * CP_THREADS + tid == cabs) {
-#pragma unroll
-                    for (int j = 0; j < CP_SW; ++j)
-                        sh.pubdiag[buf][j] = v[k][j];
                 }
-            __syncthreads();
-// 2. the CTA's candidate record (warp 0), pushed into every CTA's receive slot
-            //    (lane l -> CTA l), and by the diagonal's owner CTA the diagonal row
-            if (warp == 0) {
-                const unsigned mb = lane < CP_THREADS / 32 ? sh.wbits[lane] : 0u;
-                const int mp = lane < CP_THREADS / 32 ? sh.wpos[lane] : INT_MAX;
-                const unsigned cm = __reduce_max_sync(0xffffffffu, mb);
-                const int cp = (int)__reduce_min_sync(0xffffffffu, mb == cm ? (unsigned)mp : (unsigned)INT_MAX);
-                const unsigned own = __ballot_sync(0xffffffffu, mp == cp && mp != INT_MAX);
-                const int ww = own ? __ffs(own) - 1 : 0;
-                const float4* wr = reinterpret_cast<const float4*>(&sh.wrow[ww][0]);
-                const float4 e0 = wr[0], e1 = wr[1], e2 = wr[2], e3 = wr[3];
-                const float4 e4 = make_float4(__uint_as_float(cm), __int_as_float(cp), 0.f, 0.f);
-                if (lane < CS) {
-                    const uint32_t dst = cluster_addr(&sh.recv[buf][q], lane);
-                    const uint32_t bar = cluster_addr(&sh.mbar[buf], lane);
-                    st_async16(dst, e0, bar);
-                    st_async16(dst + 16, e1, bar);
-                    st_async16(dst + 32, e2, bar);
-                    st_async16(dst + 48, e3, bar);
-                    st_async16(dst + 64, e4, bar);
-                } else if (q == cabs / RPC) {
-                    const float4* dr = reinterpret_cast<const float4*>(&sh.pubdiag[buf][0]);
-                    const uint32_t dst = cluster_addr(&sh.recv_diag[buf][0], lane - CS);
-                    const uint32_t bar = cluster_addr(&sh.mbar[buf], lane - CS);
-#pragma unroll
-                    for (int u = 0; u < CP_SW / 4; ++u) st_async16(dst + 16 * u, dr[u], bar);
-                }
-            }
-        };
-        // step 3 for sub-panel column cc: wait, read the records, the winner
-        auto receive = [&](const int cc) {
-            const int cabs = cs0 + cc;
-            const int c = cc;
-            const int buf = cabs & 1;
-            // 3. wait for the 16 records and the diagonal row, pick the same winner in every CTA
-            if (warp == 0) {
+                // 3. every warp: wait for the records and the diagonal row, pick the
+                //    same winner (first largest |a|) as every other warp and CTA
                 int ok = 1;
-                if (lane == 0 && !rx_failed) {
-                    ok = tc::mbar_wait(&sh.mbar[buf], (uint32_t)((cabs >> 1) & 1)) ? 1 : 0;
-                    if (ok)
-                        tc::mbar_arrive_expect_tx(&sh.mbar[buf], CP_RX_BYTES);  // re-arm for column cabs + 2
-                    else
-                        atomicExch(err, 8 /* MG_TIMEOUT */);
+                if (lane == 0) {
+                    ok = rx_failed ? 0 : (tc::mbar_wait_cluster(&sh.mbar[buf], (uint32_t)((cabs >> 1) & 1)) ? 1 : 0);
+                    if (!ok && !rx_failed) atomicExch(err, 8 /* MG_TIMEOUT */);
+                    if (ok && warp == 0) tc::mbar_arrive_expect_tx(&sh.mbar[buf], CP_RX_BYTES);  // column cabs + 2
                 }
                 ok = __shfl_sync(0xffffffffu, ok, 0);
                 if (!ok) rx_failed = true;
-                __syncwarp();
-                float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, q2 = q0, q3 = q0, q4 = q0;
-                if (lane < CS) {
-                    const float4* src = reinterpret_cast<const float4*>(&sh.recv[buf][lane]);
-                    q0 = src[0];
-                    q1 = src[1];
-                    q2 = src[2];
-                    q3 = src[3];
-                    q4 = src[4];
-                } else if (lane < CS + CP_SW / 4) {
-                    q0 = reinterpret_cast<const float4*>(&sh.recv_diag[buf][0])[lane - CS];
+                __syncwarp();  // the other lanes' reads of the records after lane 0's acquire
+                unsigned rb = 0u;
+                int rp = INT_MAX, rs = 0;
+#pragma unroll
+                for (int t = 0; t < (CP_NREC + 31) / 32; ++t) {
+                    const int idx = lane + 32 * t;
+                    if (idx < CP_NREC) {
+                        const uint2 kv = *reinterpret_cast<const uint2*>(&sh.recv[buf][idx].bits);
+                        const int pp = (int)kv.y;
+                        if (pp != INT_MAX && (rp == INT_MAX || kv.x > rb || (kv.x == rb && pp < rp))) {
+                            rb = kv.x;
+                            rp = pp;
+                            rs = idx;
+                        }
+                    }
                 }
-                const unsigned rb = lane < CS ? __float_as_uint(q4.x) : 0u;
-                const int rp = lane < CS ? __float_as_int(q4.y) : INT_MAX;
                 const unsigned gm = __reduce_max_sync(0xffffffffu, rb);
                 const int gp = (int)__reduce_min_sync(0xffffffffu, rb == gm ? (unsigned)rp : (unsigned)INT_MAX);
-                const unsigned gown = __ballot_sync(0xffffffffu, lane < CS && rp == gp);
-                if (gown && lane == __ffs(gown) - 1) {
-                    float4* d = reinterpret_cast<float4*>(sh.prow[buf]);
-                    d[0] = q0;
-                    d[1] = q1;
-                    d[2] = q2;
-                    d[3] = q3;
-                }
-                if (lane >= CS && lane < CS + CP_SW / 4) reinterpret_cast<float4*>(sh.drow[buf])[lane - CS] = q0;
-                if (lane == 0) {
-                    const float gv = __uint_as_float(gm);
-                    const bool okp = gp >= 0 && gp < R && gv > 0.f;
-                    sh.s_win[buf] = okp ? gp : cabs;
-                    sh.s_pv[buf] = okp ? gv : 0.f;
+                const unsigned gown = __ballot_sync(0xffffffffu, rp == gp && gp != INT_MAX);
+                const int gslot = __shfl_sync(0xffffffffu, rs, gown ? __ffs(gown) - 1 : 0);
+                const bool okp = gp >= 0 && gp < R && __uint_as_float(gm) > 0.f;
+                if (warp == 0 && lane == 0) {
                     sh.piv[cabs] = okp ? gp : cabs;
                     sh.touch[2 * c] = cabs;
                     sh.touch[2 * c + 1] = okp ? gp : cabs;
@@ -411,55 +425,71 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                     }
                     if (!okp && q == 0) atomicCAS(info, 0, r0 + cabs + 1);
                 }
-            }
-            __syncthreads();
-        };
-
-        if constexpr (!TOURN) {
+                // 4. interchange, scale, update, shift the window (an exactly zero
+                //    column: shift only, as LAPACK leaves it)
+                if (okp) {
+                    float u[CP_SW];
+                    {
+                        const float4* u4p = reinterpret_cast<const float4*>(sh.recv[buf][gslot].row);
 #pragma unroll
-        for (int c = 0; c < CP_SW; ++c) {
-            if (c < sw) {
-                const int cabs = cs0 + c;
-                const int buf = cabs & 1;
-                publish(c);
-                receive(c);
-                // 4. interchange, scale, update (exactly zero column: nothing, as LAPACK)
-                const float* ur = sh.prow[buf];
-                if (sh.s_pv[buf] > 0.f) {
-                    const int win = sh.s_win[buf];
-                    if (win != cabs) {
+                        for (int u4 = 0; u4 < CP_SW / 4; ++u4) {
+                            const float4 t4 = u4p[u4];
+                            u[4 * u4] = t4.x;
+                            u[4 * u4 + 1] = t4.y;
+                            u[4 * u4 + 2] = t4.z;
+                            u[4 * u4 + 3] = t4.w;
+                        }
+                    }
+                    if (gp != cabs) {
 #pragma unroll
                         for (int k = 0; k < RPT; ++k) {
                             const int p = row0 + k * CP_THREADS + tid;
                             if (p == cabs) {
 #pragma unroll
-                                for (int j = 0; j < CP_SW; ++j) v[k][j] = ur[j];
-                            } else if (p == win) {
+                                for (int j = 0; j < CP_SW; ++j) v[k][j] = u[j];
+                            } else if (p == gp) {
 #pragma unroll
-                                for (int j = 0; j < CP_SW; ++j) v[k][j] = sh.drow[buf][j];
+                                for (int j = 0; j < CP_SW; ++j) v[k][j] = sh.recv_diag[buf][j];
                             }
                         }
                     }
-                    const float inv = 1.f / ur[c];
-                    float lk[RPT];  // multipliers of column c for my rows
-                    bool ak[RPT];   // my rows below the pivot
+                    const float inv = 1.f / u[0];
+                    const int na = CP_SW - 1 - c;  // columns right of the pivot: positions 1 .. na
 #pragma unroll
                     for (int k = 0; k < RPT; ++k) {
                         const int p = row0 + k * CP_THREADS + tid;
-                        ak[k] = p < R && p > cabs;
-                        lk[k] = ak[k] ? v[k][c] * inv : 0.f;
-                        if (ak[k]) v[k][c] = lk[k];
-                    }
+                        const bool ak = p < R && p > cabs;
+                        const float l = v[k][0] * inv;
+                        const float v0 = v[k][0];
 #pragma unroll
-                    for (int j = c + 1; j < CP_SW; ++j) {
-                        const float u = ur[j];
-#pragma unroll
-                        for (int k = 0; k < RPT; ++k)
-                            if (ak[k]) v[k][j] = fmaf(lk[k], -u, v[k][j]);
+                        for (int j = 1; j < W; ++j) {
+                            const float x = v[k][j];
+                            v[k][j - 1] = (ak && j <= na) ? fmaf(l, -u[j], x) : x;
+                        }
+                        v[k][W - 1] = ak ? l : v0;
                     }
+                } else {
+                    rotate_n(WT, 1);
                 }
+            };
+#pragma unroll 1
+            for (int c = 0; c < min(sw, CP_SW / 2); ++c) step(std::integral_constant<int, CP_SW>{}, c);
+            if (sw <= CP_SW / 2) {
+                rotate_n(std::integral_constant<int, CP_SW>{}, CP_SW - sw);
+            } else {
+#pragma unroll 1
+                for (int c = CP_SW / 2; c < sw; ++c) step(std::integral_constant<int, CP_SW / 2>{}, c);
+                rotate_n(std::integral_constant<int, CP_SW / 2>{}, CP_SW - sw);
+#pragma unroll
+                for (int k = 0; k < RPT; ++k)
+#pragma unroll
+                    for (int j = 0; j < CP_SW / 2; ++j) {
+                        const float t = v[k][j];
+                        v[k][j] = v[k][j + CP_SW / 2];
+                        v[k][j + CP_SW / 2] = t;
+                    }
             }
-        }
+            __syncthreads();  // piv, touch and map of this sub-panel complete
         } else {
             // ---- tournament pivoting for the sub-panel (CALU's TSLU: Grigori,
             // Demmel & Xiang, "CALU: a communication optimal LU factorization
@@ -534,7 +564,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
             if (tid == 0) {
                 int ok = 0;
                 if (!rx_failed) {
-                    ok = tc::mbar_wait(&ts.mbar, (uint32_t)(s & 1)) ? 1 : 0;
+                    ok = tc::mbar_wait_cluster(&ts.mbar, (uint32_t)(s & 1)) ? 1 : 0;
                     if (!ok) atomicExch(err, 8 /* MG_TIMEOUT */);
                 }
                 if (ok && s + 1 < nsub) tc::mbar_arrive_expect_tx(&ts.mbar, ts_rx_bytes(R, cs0 + CP_SW));

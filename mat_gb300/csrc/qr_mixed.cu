@@ -1,9 +1,9 @@
 // Mixed-precision Householder QR: the FP32 form of Mat's blocked Householder
 // QR (Mat-8.3.1/QR/__Householder_Blocked.h:63-245, FP64 there) for the mixed
-// QR solve.  Panels of QB = 128 columns; per column the norm, beta and tau
-// are formed in FP64 from the fp32 column (the reflector generation
-// spec keeps in FP64), the vector and the panel's other columns in
-// fp32; the compact WY factor T in fp32; the trailing update
+// QR solve.  Panels of QB = 128 columns; per column the norm, beta, tau and
+// the scale factor of the reflector are formed in FP64 from the fp32 column,
+// the reflector, its dot products with the panel's other columns and their
+// updates in fp32; the compact WY factor T in fp32; the trailing update
 // R2 -= V (T^T (V^T R2)) as three FP32 GEMMs whose large products run on the
 // split-BF16 tensor cores (sgemm_auto: 3 terms, lower-order products first,
 // fp32 accumulation).
@@ -27,30 +27,40 @@ namespace {
 constexpr int QB = 128;
 constexpr int QP_THREADS = 256;
 
-__device__ __forceinline__ double block_sum(double v, double* red) {
+// Sum of one double per thread over the CTA, valid in thread 0 (a shuffle
+// tree per warp, then warp 0 over the warps' sums, in a fixed order).
+__device__ __forceinline__ double block_sum0(double v, double* red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    __syncthreads();
     if (lane == 0) red[warp] = v;
     __syncthreads();
     double t = 0.0;
-    for (int u = 0; u < QP_THREADS / 32; ++u) t += red[u];
+    if (warp == 0) {
+        t = lane < QP_THREADS / 32 ? red[lane] : 0.0;
+#pragma unroll
+        for (int off = QP_THREADS / 64; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    }
     return t;
 }
 
 // xp: [P][QB + 2] doubles (norm partial, unused, dot partials); x0: the
 // column's diagonal element, published by its owner; tau (w doubles); V the
 // explicit reflectors (h x w, ld ldv: 1 on the diagonal, 0 above).
+// FP64: the column's sum of squares (each square exact, summed in double),
+// the cross-CTA sums, alpha, beta, tau and the scale 1 / (alpha - beta).
+// FP32: the scaling of the column by that factor, the dot products of v with
+// the panel's later columns (per lane, then a warp tree; the per-CTA partial
+// goes on in double) and the rank-1 updates.
 __global__ void __launch_bounds__(QP_THREADS, 1)
     qr_panel_f32_kernel(float* __restrict__ A, int lda, int m, int j0, int w, int rpc, float* __restrict__ V, int ldv,
                         double* __restrict__ tau, double* __restrict__ xp, double* __restrict__ x0, unsigned* bar,
                         int* err) {
     extern __shared__ __align__(16) float slab[];  // [w][rpc]
     __shared__ double red[QP_THREADS / 32];
-    __shared__ double s_coef[QB];                  // tau * (v . a_jj) for the update
-    __shared__ double s_tau, s_scal, s_beta;
-    __shared__ int s_ok;
+    __shared__ float s_coef[QB];                   // -tau * (v . a_jj) for the update
+    __shared__ double s_tau, s_beta;
+    __shared__ float s_scalf;
     const int P = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int h = m - j0;
     const int r0 = b * rpc, r1 = min(h, r0 + rpc);
@@ -65,7 +75,7 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
     bool ok = true;
     for (int c = 0; c < w && ok; ++c) {
         float* col = slab + (size_t)c * rpc;
-        // 1. partial sum of squares below the diagonal; the owner publishes x_c
+        // 1. partial sum of squares below the diagonal (FP64); the owner publishes x_c
         double s = 0.0;
         for (int i = tid; i < rpc; i += QP_THREADS) {
             const int gi = r0 + i;
@@ -74,7 +84,7 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
                 s = fma(x, x, s);
             }
         }
-        s = block_sum(s, red);
+        s = block_sum0(s, red);
         if (tid == 0) {
             xp[(size_t)b * stride] = s;
             if (c >= r0 && c < r1) *x0 = col[c - r0];
@@ -82,43 +92,44 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
         target += P;
         ok = mg::grid_barrier(bar, target, err);
         if (!ok) break;
-        // 2. beta, tau (FP64, identical in every CTA); scale my part of v
+        // 2. beta, tau, the scale (FP64, identical in every CTA); scale my part of v
         if (tid == 0) {
             double xn2 = 0.0;
             for (int u = 0; u < P; ++u) xn2 += __ldcg(&xp[(size_t)u * stride]);
             const double alpha = __ldcg(x0);
             if (xn2 == 0.0) {  // nothing below the diagonal: H = I
                 s_tau = 0.0;
-                s_scal = 0.0;
+                s_scalf = 0.f;
                 s_beta = alpha;
             } else {
                 const double beta = -copysign(sqrt(fma(alpha, alpha, xn2)), alpha);
                 s_tau = (beta - alpha) / beta;
-                s_scal = 1.0 / (alpha - beta);
+                s_scalf = (float)(1.0 / (alpha - beta));
                 s_beta = beta;
             }
             if (b == 0) tau[c] = s_tau;
         }
         __syncthreads();
         const double tc = s_tau;
+        const float scf = s_scalf, betaf = (float)s_beta;
         for (int i = tid; i < rpc; i += QP_THREADS) {
             const int gi = r0 + i;
-            if (gi > c && gi < h) col[i] = (float)(col[i] * s_scal);
-            else if (gi == c) col[i] = (float)s_beta;
+            if (gi > c && gi < h) col[i] = col[i] * scf;
+            else if (gi == c) col[i] = betaf;
         }
         __syncthreads();
         // 3. partial dots v . a_jj for the panel's later columns (v_c = 1), a warp per column
         for (int jj = c + 1 + warp; jj < w; jj += QP_THREADS / 32) {
             const float* a = slab + (size_t)jj * rpc;
-            double d = 0.0;
+            float d = 0.f;
             for (int i = lane; i < rpc; i += 32) {
                 const int gi = r0 + i;
                 if (gi == c) d += a[i];
-                else if (gi > c && gi < h) d = fma((double)col[i], (double)a[i], d);
+                else if (gi > c && gi < h) d = fmaf(col[i], a[i], d);
             }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xffffffffu, d, off);
-            if (lane == 0) xp[(size_t)b * stride + 2 + jj] = d;
+            if (lane == 0) xp[(size_t)b * stride + 2 + jj] = (double)d;
         }
         target += P;
         ok = mg::grid_barrier(bar, target, err);
@@ -127,21 +138,19 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
         for (int jj = c + 1 + tid; jj < w; jj += QP_THREADS) {
             double d = 0.0;
             for (int u = 0; u < P; ++u) d += __ldcg(&xp[(size_t)u * stride + 2 + jj]);
-            s_coef[jj] = tc * d;
+            s_coef[jj] = (float)(-tc * d);
         }
         __syncthreads();
-        for (int e = tid; e < (w - c - 1) * rpc; e += QP_THREADS) {
-            const int jj = c + 1 + e / rpc, i = e % rpc, gi = r0 + i;
-            if (gi >= c && gi < h) {
-                float* a = slab + (size_t)jj * rpc;
-                const float vi = gi == c ? 1.f : col[i];
-                a[i] = fmaf((float)(-s_coef[jj]), vi, a[i]);
+        for (int jj = c + 1; jj < w; ++jj) {
+            float* a = slab + (size_t)jj * rpc;
+            const float cf = s_coef[jj];
+            for (int i = tid; i < rpc; i += QP_THREADS) {
+                const int gi = r0 + i;
+                if (gi >= c && gi < h) a[i] = fmaf(cf, gi == c ? 1.f : col[i], a[i]);
             }
         }
         __syncthreads();
     }
-    if (tid == 0) s_ok = ok ? 1 : 0;
-    __syncthreads();
     // write back: R (upper, diagonal = beta) and v below it; V explicit
     for (int e = tid; e < w * rpc; e += QP_THREADS) {
         const int c = e / rpc, i = e - c * rpc, gi = r0 + i;

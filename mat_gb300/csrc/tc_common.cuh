@@ -48,6 +48,29 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
     return false;
 }
 
+// The same wait with acquire semantics at cluster scope: for barriers whose
+// transactions are stores from other CTAs of the cluster (st.async), whose
+// completion releases at cluster scope.  Threads other than the waiting one
+// must still be ordered after it (__syncwarp / __syncthreads) before reading.
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, "
+        "p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity, uint32_t limit = kWaitLimit) {
+    for (uint32_t i = 0; i < limit; ++i) {
+        if (mbar_try_wait_cluster(bar, parity)) return true;
+        if (i > 1024) __nanosleep(32);
+    }
+    return false;
+}
+
 // 3-D tiled TMA load into shared memory, completion counted on `bar`.
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y,
                                             int z) {

@@ -1,4 +1,4 @@
-"""FP32 forms (Mat's templates on MAT<float>; config 5 "run in FP32"):
+"""FP32 forms (Mat's templates on MAT<float>, the Gaussian-process workload run in FP32):
 mg_sgemm against the FP64 product of the same fp32 inputs (normwise, 2e-6
 scaled by sqrt(k/64) for the fp32 accumulation); mg_spotrf against the FP64
 Cholesky of the same matrix; the FP32 Cholesky adjoint and the FP32

@@ -165,11 +165,11 @@ def test_lu(handle, n):
 
 
 # ------------------------------------------- the benchmark configurations
-# Digests of the reference's own results at the BASELINE sizes (make_golden.py
+# Digests of the reference's own results at the benchmark sizes (make_golden.py
 # --large; the single-threaded reference takes about five minutes for them).
 
 def test_solve_8192_1_benchmark(handle):
-    """Config 2's FP64 solve: A, b iid N(0,1) (seeds 1, 2), n = 8192, 1 RHS."""
+    """The FP64 solve benchmark: A, b iid N(0,1) (seeds 1, 2), n = 8192, 1 RHS."""
     A, B = colmajor(8192, 8192), colmajor(8192, 1)
     handle.fill_normal(A, 1)
     handle.fill_normal(B, 2)
@@ -179,7 +179,7 @@ def test_solve_8192_1_benchmark(handle):
 
 
 def test_solve_16384_4_benchmark(handle):
-    """Config 3's FP64 side: the mixed solve's system (A = Q1 diag(sigma) Q2,
+    """The FP64 side of the mixed-solve benchmark: its system (A = Q1 diag(sigma) Q2,
     seed 3, cond 1e6; B seed 11), solved by the FP64 GPU path bit for bit as
     Mat's Solve_direct solves it."""
     n = 16384
@@ -192,7 +192,7 @@ def test_solve_16384_4_benchmark(handle):
 
 
 def test_qr_16384x4096_benchmark(handle):
-    """Config 2's Householder QR with Mat's full 16384 x 16384 Q, bit for bit."""
+    """The Householder QR benchmark with Mat's full 16384 x 16384 Q, bit for bit."""
     m, k = 16384, 4096
     A = colmajor(m, k)
     handle.fill_normal(A, 1)

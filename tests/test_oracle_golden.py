@@ -202,7 +202,7 @@ def test_evd81_restatement_equals_reference_build(orc, n):
 
 
 def test_solve_benchmark_configs(orc):
-    """The oracle's Solve_direct on the BASELINE systems against the
+    """The oracle's Solve_direct on the benchmark systems against the
     reference's digests: n = 8192 with 1 RHS, and the mixed solve's n = 16384
     system with 4 RHS (whose input digest is checked too)."""
     from oracle.api import gen_svd_matrix

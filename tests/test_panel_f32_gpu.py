@@ -1,8 +1,9 @@
 """FP32 LU of the mixed solve: the panel (mg_sgetf2) against a restatement of
 the fp32 partial-pivoting LU with exactly rounded fused updates, on the
-cluster path (m <= 16384, 1..4 rows per thread, ragged sub-panels, clusters
-with idle CTAs) and the cooperative-grid path (m > 16384); exact zero
-columns and tied candidates; and the blocked mg_sgetrf by its defining
+cluster path (m <= 16384; clusters of 1, 2, 4, 8 and 16 CTAs, 1..4 rows
+per thread, ragged sub-panels, clusters with idle CTAs) and the
+cooperative-grid path (m > 16384); exact zero columns and tied candidates;
+and the blocked mg_sgetrf by its defining
 properties (|L| <= 1, P A = L U to fp32 accuracy).
 """
 import numpy as np
@@ -48,7 +49,8 @@ def run_panel(handle, a: np.ndarray):
 
 
 @pytest.mark.parametrize("m,n", [(300, 128), (4096, 128), (5000, 128), (9000, 101), (16384, 128), (3000, 77),
-                                 (20000, 100), (128, 128), (700, 40)])
+                                 (20000, 100), (128, 128), (700, 40), (1000, 1), (777, 17), (1025, 128),
+                                 (1800, 128), (2048, 64), (8192, 128), (8193, 96)])
 def test_sgetf2_matches_restatement(handle, m, n):
     rng = np.random.default_rng(m * 131 + n)
     a = rng.standard_normal((m, n)).astype(np.float32)
