@@ -87,8 +87,7 @@ struct CpShared {
     CpRec recv[2][CP_NREC];          // the candidates for the column, by column parity
     __align__(16) float recv_diag[2][CP_SW];  // the row at the diagonal (sent by its owner)
     __align__(8) uint64_t mbar[2];            // receive barriers (transaction bytes), by parity
-    CpRec wst[CP_NW];                         // each warp's candidate record, staged for sending
-    __align__(16) float wdiag[CP_NW][CP_SW];  // the diagonal row, staged by the warp holding it
+    uint2 wkey[2][CP_NW];                     // each warp's candidate (|a| bits, position), by parity
     int piv[CP_MAXW];
     int touch[2 * CP_SW];
     float gbuf[CP_GCOLS * 2 * CP_SW];
@@ -307,6 +306,23 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                         v[k][W - 1] = v0;
                     }
             };
+            // the warp of this CTA holding position pp (-1: not a row of this CTA)
+            auto warp_of = [&](int pp) {
+                const int i = pp - row0;
+                return (i >= 0 && i < RPC) ? (i % CP_THREADS) >> 5 : -1;
+            };
+            // position pp (a row of this warp) broadcast to every lane of the warp
+            auto bcast_row = [&](int pp, float(&r)[CP_SW]) {
+                const int i = pp - row0, ol = i & 31, okk = i / CP_THREADS;
+#pragma unroll
+                for (int j = 0; j < CP_SW; ++j) {
+                    float x = v[0][j];
+#pragma unroll
+                    for (int k = 1; k < RPT; ++k)
+                        if (okk == k) x = v[k][j];
+                    r[j] = __shfl_sync(0xffffffffu, x, ol);
+                }
+            };
             auto step = [&](auto WT, const int c) {
                 constexpr int W = decltype(WT)::value;  // window width: positions 0 .. W-1 shift
                 const int cabs = cs0 + c;
@@ -314,7 +330,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                 // 1. this thread's and this warp's candidate (first largest |a|
                 //    among the rows at or below the diagonal; NaN never wins)
                 unsigned bb = 0u;
-                int bp = INT_MAX, bk = 0;
+                int bp = INT_MAX;
 #pragma unroll
                 for (int k = 0; k < RPT; ++k) {
                     const int p = row0 + k * CP_THREADS + tid;
@@ -324,63 +340,44 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                         if (ab > bb || bp == INT_MAX) {
                             bb = ab;
                             bp = p;
-                            bk = k;
                         }
                     }
                 }
                 const unsigned wm = __reduce_max_sync(0xffffffffu, bb);
                 const int wp = (int)__reduce_min_sync(0xffffffffu, bb == wm ? (unsigned)bp : (unsigned)INT_MAX);
-                const int dq = cabs / RPC;                         // CTA holding the diagonal row
-                const int dt = q == dq ? cabs - row0 : -1;         // its position in my rows
-                const int dk = dt >= 0 ? dt / CP_THREADS : 0;
-                const int dthr = dt >= 0 ? dt - dk * CP_THREADS : -1;
-                __syncwarp();  // the previous column's staged rows have been read
-                if (wp != INT_MAX && bp == wp) {
-                    float4* s4 = reinterpret_cast<float4*>(sh.wst[warp].row);
-#pragma unroll
-                    for (int k = 0; k < RPT; ++k)
-                        if (k == bk)
-#pragma unroll
-                            for (int u4 = 0; u4 < CP_SW / 4; ++u4)
-                                s4[u4] = make_float4(v[k][4 * u4], v[k][4 * u4 + 1], v[k][4 * u4 + 2], v[k][4 * u4 + 3]);
-                }
-                if (lane == 0) {
-                    sh.wst[warp].bits = wm;
-                    sh.wst[warp].pos = wp;
-                }
-                if (tid == dthr) {
-                    float4* d4 = reinterpret_cast<float4*>(sh.wdiag[warp]);
-#pragma unroll
-                    for (int k = 0; k < RPT; ++k)
-                        if (k == dk)
-#pragma unroll
-                            for (int u4 = 0; u4 < CP_SW / 4; ++u4)
-                                d4[u4] = make_float4(v[k][4 * u4], v[k][4 * u4 + 1], v[k][4 * u4 + 2], v[k][4 * u4 + 3]);
-                }
+                if (lane == 0) sh.wkey[buf][warp] = make_uint2(wm, (unsigned)wp);
                 __syncthreads();
-                // 2. warp 0: the CTA's record from its warps' records, pushed into
-                //    slot [my rank] of every CTA (lane l -> CTA l); lanes 16..19 push
-                //    the diagonal row if this CTA holds it
-                if (warp == 0) {
-                    const unsigned mb = lane < CP_NW ? sh.wst[lane].bits : 0u;
-                    const int mp = lane < CP_NW ? sh.wst[lane].pos : INT_MAX;
-                    const unsigned cm = __reduce_max_sync(0xffffffffu, mb);
-                    const int cp = (int)__reduce_min_sync(0xffffffffu, mb == cm ? (unsigned)mp : (unsigned)INT_MAX);
-                    const unsigned own = __ballot_sync(0xffffffffu, lane < CP_NW && mp == cp);
-                    const int ww = own ? __ffs(own) - 1 : 0;
+                // 2. every warp: the CTA's candidate from its warps' keys; the warp
+                //    holding it broadcasts the row and pushes the record into slot
+                //    [my rank] of every CTA (lane l -> CTA l); the warp holding the
+                //    diagonal row pushes that row (lanes 16..31 -> CTA lane - 16)
+                const uint2 kk = lane < CP_NW ? sh.wkey[buf][lane] : make_uint2(0u, (unsigned)INT_MAX);
+                const unsigned cm = __reduce_max_sync(0xffffffffu, kk.x);
+                const int cp = (int)__reduce_min_sync(0xffffffffu, kk.x == cm ? kk.y : (unsigned)INT_MAX);
+                const int cw = cp == INT_MAX ? 0 : warp_of(cp);  // no candidate: warp 0 sends an empty record
+                if (warp == cw) {
+                    float r[CP_SW];
+                    bcast_row(cp == INT_MAX ? row0 : cp, r);
                     if (lane < CS) {
-                        const float4* wr = reinterpret_cast<const float4*>(sh.wst[ww].row);
                         const uint32_t dst = cluster_addr(&sh.recv[buf][q], lane);
                         const uint32_t bar = cluster_addr(&sh.mbar[buf], lane);
 #pragma unroll
-                        for (int u4 = 0; u4 < CP_SW / 4; ++u4) st_async16(dst + 16u * u4, wr[u4], bar);
+                        for (int u4 = 0; u4 < CP_SW / 4; ++u4)
+                            st_async16(dst + 16u * u4, make_float4(r[4 * u4], r[4 * u4 + 1], r[4 * u4 + 2], r[4 * u4 + 3]),
+                                       bar);
                         st_async16(dst + 64, make_float4(__uint_as_float(cm), __int_as_float(cp), 0.f, 0.f), bar);
-                    } else if (dthr >= 0) {
-                        const float4* d4 = reinterpret_cast<const float4*>(sh.wdiag[dthr >> 5]);
+                    }
+                }
+                if (warp == warp_of(cabs)) {
+                    float r[CP_SW];
+                    bcast_row(cabs, r);
+                    if (lane >= CS) {
                         const uint32_t dst = cluster_addr(&sh.recv_diag[buf][0], lane - CS);
                         const uint32_t bar = cluster_addr(&sh.mbar[buf], lane - CS);
 #pragma unroll
-                        for (int u4 = 0; u4 < CP_SW / 4; ++u4) st_async16(dst + 16u * u4, d4[u4], bar);
+                        for (int u4 = 0; u4 < CP_SW / 4; ++u4)
+                            st_async16(dst + 16u * u4, make_float4(r[4 * u4], r[4 * u4 + 1], r[4 * u4 + 2], r[4 * u4 + 3]),
+                                       bar);
                     }
                 }
                 // 3. every warp: wait for the records and the diagonal row, pick the
@@ -440,7 +437,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                             u[4 * u4 + 3] = t4.w;
                         }
                     }
-                    if (gp != cabs) {
+                    if (gp != cabs && (warp == warp_of(cabs) || warp == warp_of(gp))) {
 #pragma unroll
                         for (int k = 0; k < RPT; ++k) {
                             const int p = row0 + k * CP_THREADS + tid;
