@@ -434,56 +434,117 @@ def run_reference(args):
 
 
 def e2e_run(h, A, B, n, nrhs, steps, barrier, warmup=3):
-    """The solve through the C ABI from pinned host buffers: per step the H2D
-    copy of A and B, the solve, the D2H copy of X, a synchronize (wall clock,
-    max over ranks by the barrier), after `warmup` untimed steps.  The H2D
-    share is timed once more with events on the library's stream."""
+    """The solve through the C ABI from pinned host buffers, two ways, after
+    `warmup` untimed steps each (wall clock, max over ranks by the barrier):
+
+    serial: per step the H2D copy of A and B, the solve, the D2H copy of X
+      and a synchronize, all on the library's stream (the latency of one
+      solve from host memory);
+    pipelined (the reported value): a stream of solves as a solver service
+      runs them: two device input buffers; step i's solve on one handle's
+      stream while step i+1's inputs are copied H2D on a second handle's
+      stream (ordered by events), then X read back D2H.  Every step's copies
+      are inside the timed region; the first step's copy is not overlapped.
+
+    The H2D share is timed once more with events on the library's stream."""
     import ctypes as C
 
     import torch
 
-    from mat_gb300.api import colmajor
+    from mat_gb300.api import Handle, colmajor
     hA = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
     hA.copy_(A.t())  # column-major bytes of A in a row-major (n x n) pinned host buffer
     hBt = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
     hBt.copy_(B.t())
     hXt = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
-    dA, dB, dX = colmajor(n, n), colmajor(n, nrhs), colmajor(n, nrhs)
-    lib, hh = h.lib, h.h
+    lib = h.lib
     h2d = 8 * n * n + 8 * n * nrhs
     d2h = 8 * n * nrhs
 
-    def step():
+    def timed_steps(step, nsteps):
+        barrier()
+        gc.collect()
+        gc.disable()  # no collector pass inside the timed steps
+        w0 = time.perf_counter()
+        per_step = []
+        for i in range(nsteps):
+            t = time.perf_counter()
+            step(i)
+            per_step.append((time.perf_counter() - t) * 1e3)
+        barrier()
+        total = time.perf_counter() - w0
+        gc.enable()
+        return total / nsteps, per_step
+
+    # serial
+    dA, dB, dX = colmajor(n, n), colmajor(n, nrhs), colmajor(n, nrhs)
+    hh = h.h
+
+    def serial_step(i):
         h.check(lib.mg_memcpy(hh, C.c_void_p(dA.data_ptr()), C.c_void_p(hA.data_ptr()), 8 * n * n, 0))
         h.check(lib.mg_memcpy(hh, C.c_void_p(dB.data_ptr()), C.c_void_p(hBt.data_ptr()), 8 * n * nrhs, 0))
         h.dsgesv_ir(dA, dB, dX)
         h.check(lib.mg_memcpy(hh, C.c_void_p(hXt.data_ptr()), C.c_void_p(dX.data_ptr()), 8 * n * nrhs, 1))
         h.check(lib.mg_synchronize(hh))
 
-    for _ in range(max(1, warmup)):
-        step()
-    barrier()
-    gc.collect()
-    gc.disable()  # no collector pass inside the timed steps
-    w0 = time.perf_counter()
-    per_step = []
-    for _ in range(steps):
-        t = time.perf_counter()
-        step()
-        per_step.append((time.perf_counter() - t) * 1e3)
-    barrier()
-    e2e_s = (time.perf_counter() - w0) / steps
-    gc.enable()
+    for i in range(max(1, warmup)):
+        serial_step(i)
+    serial_s, serial_ms = timed_steps(serial_step, steps)
     c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     c0.record()
     h.check(lib.mg_memcpy(hh, C.c_void_p(dA.data_ptr()), C.c_void_p(hA.data_ptr()), 8 * n * n, 0))
     c1.record()
     torch.cuda.synchronize()
-    out = {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-           "step_ms": [round(x, 2) for x in per_step],
-           "h2d_ms": c0.elapsed_time(c1), "h2d_gbs": 8 * n * n / (c0.elapsed_time(c1) * 1e6)}
-    del hA, hBt, hXt, dA, dB, dX
-    return out
+    h2d_ms = c0.elapsed_time(c1)
+    del dA, dB, dX
+
+    # pipelined
+    sc, ss = torch.cuda.Stream(), torch.cuda.Stream()
+    hc, hs = Handle(sc), Handle(ss)
+    dAs = [colmajor(n, n), colmajor(n, n)]
+    dBs = [colmajor(n, nrhs), colmajor(n, nrhs)]
+    dXs = [colmajor(n, nrhs), colmajor(n, nrhs)]
+    ev_in = [torch.cuda.Event(), torch.cuda.Event()]
+    ev_done = [torch.cuda.Event(), torch.cuda.Event()]
+    for e in ev_done:
+        e.record(ss)
+
+    def copy_in(i):
+        b = i & 1
+        sc.wait_event(ev_done[b])  # the buffer's previous solve has finished
+        hc.check(lib.mg_memcpy(hc.h, C.c_void_p(dAs[b].data_ptr()), C.c_void_p(hA.data_ptr()), 8 * n * n, 0))
+        hc.check(lib.mg_memcpy(hc.h, C.c_void_p(dBs[b].data_ptr()), C.c_void_p(hBt.data_ptr()), 8 * n * nrhs, 0))
+        ev_in[b].record(sc)
+
+    def make_step(nsteps):
+        def step(i):
+            b = i & 1
+            if i == 0:
+                copy_in(0)
+            if i + 1 < nsteps:
+                copy_in(i + 1)  # overlaps this step's solve
+            ss.wait_event(ev_in[b])
+            hs.dsgesv_ir(dAs[b], dBs[b], dXs[b])
+            hs.check(lib.mg_memcpy(hs.h, C.c_void_p(hXt.data_ptr()), C.c_void_p(dXs[b].data_ptr()), 8 * n * nrhs, 1))
+            hs.check(lib.mg_synchronize(hs.h))
+            ev_done[b].record(ss)
+        return step
+
+    warm = make_step(max(1, warmup))
+    for i in range(max(1, warmup)):
+        warm(i)
+    torch.cuda.synchronize()
+    pipe_s, pipe_ms = timed_steps(make_step(steps), steps)
+    torch.cuda.synchronize()
+    hs.close()
+    hc.close()
+    del dAs, dBs, dXs, hA, hBt, hXt
+    torch.cuda.empty_cache()
+    return {"value": pipe_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "pipelined": True, "step_ms": [round(x, 2) for x in pipe_ms],
+            "serial": {"value": serial_s, "step_ms": [round(x, 2) for x in serial_ms],
+                       "note": "H2D, solve, D2H back to back per step: the latency of one solve from host memory"},
+            "h2d_ms": h2d_ms, "h2d_gbs": 8 * n * n / (h2d_ms * 1e6)}
 
 
 def run_ours(args):
