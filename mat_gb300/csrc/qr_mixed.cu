@@ -14,9 +14,9 @@
 // blocked panel also follows, :63-84); R(c,c) = beta.  H = I - tau v v^T.
 //
 // The panel runs as one cooperative grid: its rows dealt to P CTAs in
-// contiguous runs (the slab in shared memory); per column two bounded grid
-// barriers (the norm's partial sums, then the dot products of v with the
-// panel's other columns), every CTA summing the partials in the same order.
+// contiguous runs (the slab in shared memory); per column one bounded grid
+// barrier (the norm's and the dot products' partial sums together), every
+// CTA summing the partials in the same order.
 #include <cmath>
 
 #include "grid_sync.cuh"
@@ -44,23 +44,28 @@ __device__ __forceinline__ double block_sum0(double v, double* red) {
     return t;
 }
 
-// xp: [P][QB + 2] doubles (norm partial, unused, dot partials); x0: the
-// column's diagonal element, published by its owner; tau (w doubles); V the
-// explicit reflectors (h x w, ld ldv: 1 on the diagonal, 0 above).
-// FP64: the column's sum of squares (each square exact, summed in double),
-// the cross-CTA sums, alpha, beta, tau and the scale 1 / (alpha - beta).
-// FP32: the scaling of the column by that factor, the dot products of v with
-// the panel's later columns (per lane, then a warp tree; the per-CTA partial
-// goes on in double) and the rank-1 updates.
+// One grid barrier per column.  Before it every CTA publishes, for the rows
+// below the diagonal, its partial sum of squares of the column x (FP64) and
+// its partial dots of x with the panel's later columns a_j (fp32); the owner
+// of the diagonal row publishes that row.  After it every CTA forms, in the
+// same order, S = |x below c|^2, alpha = x_c, beta = -sign(alpha)
+// sqrt(alpha^2 + S), tau = (beta - alpha) / beta and the scale 1 / (alpha -
+// beta) (FP64), and v . a_j = a_j(c) + scale * (x . a_j) with v = x * scale
+// below the diagonal and v_c = 1, so the dots need no second exchange.
+// xp: [2][P][QB + 2] doubles by column parity (the norm partial, then the
+// fp32 dot partials packed into the rest); drow: [2][QB] floats by parity,
+// the diagonal row; tau (w doubles); V the explicit reflectors (h x w, ld
+// ldv: 1 on the diagonal, 0 above).  On this part a warp instruction of the
+// FP64 pipe costs about 70 cycles of its sub-partition, so the FP64 work per
+// column is kept to a few instructions per CTA.
 __global__ void __launch_bounds__(QP_THREADS, 1)
     qr_panel_f32_kernel(float* __restrict__ A, int lda, int m, int j0, int w, int rpc, float* __restrict__ V, int ldv,
-                        double* __restrict__ tau, double* __restrict__ xp, double* __restrict__ x0, unsigned* bar,
+                        double* __restrict__ tau, double* __restrict__ xp, float* __restrict__ drow, unsigned* bar,
                         int* err) {
     extern __shared__ __align__(16) float slab[];  // [w][rpc]
     __shared__ double red[QP_THREADS / 32];
     __shared__ float s_coef[QB];                   // -tau * (v . a_jj) for the update
-    __shared__ double s_tau, s_beta;
-    __shared__ float s_scalf;
+    __shared__ double s_tau, s_beta, s_scal;
     const int P = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int h = m - j0;
     const int r0 = b * rpc, r1 = min(h, r0 + rpc);
@@ -75,7 +80,23 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
     bool ok = true;
     for (int c = 0; c < w && ok; ++c) {
         float* col = slab + (size_t)c * rpc;
-        // 1. partial sum of squares below the diagonal (FP64); the owner publishes x_c
+        double* const xpc = xp + (size_t)(c & 1) * P * stride;
+        float* const drc = drow + (c & 1) * QB;
+        // 1. partials below the diagonal: sum of squares (FP64), dots with the
+        //    later columns (fp32, a warp per column); the diagonal row (owner)
+        for (int jj = c + 1 + warp; jj < w; jj += QP_THREADS / 32) {
+            const float* a = slab + (size_t)jj * rpc;
+            float d = 0.f;
+            for (int i = lane; i < rpc; i += 32) {
+                const int gi = r0 + i;
+                if (gi > c && gi < h) d = fmaf(col[i], a[i], d);
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xffffffffu, d, off);
+            if (lane == 0) reinterpret_cast<float*>(xpc + (size_t)b * stride + 2)[jj] = d;
+        }
+        if (c >= r0 && c < r1)
+            for (int jj = c + tid; jj < w; jj += QP_THREADS) drc[jj] = slab[(size_t)jj * rpc + (c - r0)];
         double s = 0.0;
         for (int i = tid; i < rpc; i += QP_THREADS) {
             const int gi = r0 + i;
@@ -85,60 +106,47 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
             }
         }
         s = block_sum0(s, red);
-        if (tid == 0) {
-            xp[(size_t)b * stride] = s;
-            if (c >= r0 && c < r1) *x0 = col[c - r0];
-        }
+        if (tid == 0) xpc[(size_t)b * stride] = s;
         target += P;
         ok = mg::grid_barrier(bar, target, err);
         if (!ok) break;
-        // 2. beta, tau, the scale (FP64, identical in every CTA); scale my part of v
-        if (tid == 0) {
+        // 2. S over the CTAs (a shuffle tree, fixed order), then beta, tau and
+        //    the scale in FP64, identical in every CTA
+        if (warp == 0) {
             double xn2 = 0.0;
-            for (int u = 0; u < P; ++u) xn2 += __ldcg(&xp[(size_t)u * stride]);
-            const double alpha = __ldcg(x0);
-            if (xn2 == 0.0) {  // nothing below the diagonal: H = I
-                s_tau = 0.0;
-                s_scalf = 0.f;
-                s_beta = alpha;
-            } else {
-                const double beta = -copysign(sqrt(fma(alpha, alpha, xn2)), alpha);
-                s_tau = (beta - alpha) / beta;
-                s_scalf = (float)(1.0 / (alpha - beta));
-                s_beta = beta;
+            for (int u = lane; u < P; u += 32) xn2 += __ldcg(&xpc[(size_t)u * stride]);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) xn2 += __shfl_xor_sync(0xffffffffu, xn2, off);
+            if (lane == 0) {
+                const double alpha = (double)__ldcg(&drc[c]);
+                if (xn2 == 0.0) {  // nothing below the diagonal: H = I
+                    s_tau = 0.0;
+                    s_scal = 0.0;
+                    s_beta = alpha;
+                } else {
+                    const double beta = -copysign(sqrt(fma(alpha, alpha, xn2)), alpha);
+                    s_tau = (beta - alpha) / beta;
+                    s_scal = 1.0 / (alpha - beta);
+                    s_beta = beta;
+                }
+                if (b == 0) tau[c] = s_tau;
             }
-            if (b == 0) tau[c] = s_tau;
         }
         __syncthreads();
-        const double tc = s_tau;
-        const float scf = s_scalf, betaf = (float)s_beta;
+        const double tc = s_tau, sc = s_scal;
+        // 3. v . a_jj = a_jj(c) + scale (x . a_jj), the CTAs' fp32 partials in a fixed order
+        for (int jj = c + 1 + tid; jj < w; jj += QP_THREADS) {
+            float d = 0.f;
+            for (int u = 0; u < P; ++u) d += __ldcg(reinterpret_cast<const float*>(xpc + (size_t)u * stride + 2) + jj);
+            s_coef[jj] = (float)(-tc * fma(sc, (double)d, (double)__ldcg(&drc[jj])));
+        }
+        __syncthreads();
+        // 4. v below the diagonal, beta on it; a_jj -= (tau (v . a_jj)) v on my rows
+        const float scf = (float)sc, betaf = (float)s_beta;
         for (int i = tid; i < rpc; i += QP_THREADS) {
             const int gi = r0 + i;
             if (gi > c && gi < h) col[i] = col[i] * scf;
             else if (gi == c) col[i] = betaf;
-        }
-        __syncthreads();
-        // 3. partial dots v . a_jj for the panel's later columns (v_c = 1), a warp per column
-        for (int jj = c + 1 + warp; jj < w; jj += QP_THREADS / 32) {
-            const float* a = slab + (size_t)jj * rpc;
-            float d = 0.f;
-            for (int i = lane; i < rpc; i += 32) {
-                const int gi = r0 + i;
-                if (gi == c) d += a[i];
-                else if (gi > c && gi < h) d = fmaf(col[i], a[i], d);
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xffffffffu, d, off);
-            if (lane == 0) xp[(size_t)b * stride + 2 + jj] = (double)d;
-        }
-        target += P;
-        ok = mg::grid_barrier(bar, target, err);
-        if (!ok) break;
-        // 4. a_jj -= (tau (v . a_jj)) v on my rows
-        for (int jj = c + 1 + tid; jj < w; jj += QP_THREADS) {
-            double d = 0.0;
-            for (int u = 0; u < P; ++u) d += __ldcg(&xp[(size_t)u * stride + 2 + jj]);
-            s_coef[jj] = (float)(-tc * d);
         }
         __syncthreads();
         for (int jj = c + 1; jj < w; ++jj) {
@@ -254,10 +262,10 @@ size_t qr_mixed_ws_bytes(int m, int n, int num_sms) {
     return align_up((size_t)m * QB * sizeof(float), 1024)                  // V
            + align_up((size_t)QB * n * sizeof(float), 1024) * 2             // W, W2
            + align_up((size_t)QB * QB * sizeof(float), 1024)                // G
-           + align_up((size_t)P * (QB + 2) * sizeof(double), 1024)          // panel partials
+           + align_up((size_t)2 * P * (QB + 2) * sizeof(double), 1024)      // panel partials (by parity)
            + align_up((size_t)QT_CTAS * QB * 8 * sizeof(double), 1024)      // Q^T partials
            + align_up((size_t)QB * 8 * sizeof(double), 1024)                // T^T w
-           + 4096;                                                          // barrier, x0, error
+           + 4096;                                                          // barrier, diagonal rows, error
 }
 
 // In-place FP32 Householder QR of the m x n (m >= n) matrix A (ld lda):
@@ -273,11 +281,11 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
     float* W = (float*)take((size_t)QB * n * sizeof(float));
     float* W2 = (float*)take((size_t)QB * n * sizeof(float));
     float* G = (float*)take((size_t)QB * QB * sizeof(float));
-    double* xp = (double*)take((size_t)P0max * (QB + 2) * sizeof(double));
+    double* xp = (double*)take((size_t)2 * P0max * (QB + 2) * sizeof(double));
     take((size_t)QT_CTAS * QB * 8 * sizeof(double));
     take((size_t)QB * 8 * sizeof(double));
     unsigned* bar = (unsigned*)p;
-    double* x0 = (double*)(p + 256);
+    float* drow = (float*)(p + 256);  // [2][QB]
     const cudaStream_t st = h->stream;
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(qr_panel_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           h->max_smem_optin - 4096));
@@ -302,7 +310,7 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
             int lda_ = lda, m_ = m, j0_ = j0, w_ = w, rpc_ = rpc, ldv = hgt;
             float* A_ = A;
             double* tau_ = tau + j0;
-            void* args[] = {&A_, &lda_, &m_, &j0_, &w_, &rpc_, &V, &ldv, &tau_, &xp, &x0, &bar, &err};
+            void* args[] = {&A_, &lda_, &m_, &j0_, &w_, &rpc_, &V, &ldv, &tau_, &xp, &drow, &bar, &err};
             const cudaError_t e = cudaLaunchCooperativeKernel((const void*)qr_panel_f32_kernel, dim3(P),
                                                               dim3(QP_THREADS), args, smem, st);
             if (e != cudaSuccess) return cuda_fail(h, e, "qr_panel_f32_kernel launch");
@@ -335,7 +343,7 @@ mg_status_t qr_solve_f32_factors(mg_handle_t h, int n, int nrhs, const float* A,
     take((size_t)QB * n * sizeof(float));
     take((size_t)QB * n * sizeof(float));
     take((size_t)QB * QB * sizeof(float));
-    take((size_t)h->num_sms * (QB + 2) * sizeof(double));
+    take((size_t)2 * h->num_sms * (QB + 2) * sizeof(double));
     double* part = (double*)take((size_t)QT_CTAS * QB * 8 * sizeof(double));
     double* y = (double*)take((size_t)QB * 8 * sizeof(double));
     const cudaStream_t st = h->stream;
