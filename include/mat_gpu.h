@@ -315,21 +315,25 @@ mg_status_t mg_dsposv_ir(mg_handle_t h, int n, int nrhs, const double* A, int ld
  * the FP64 counterpart is Mat's blocked Householder QR,
  * Mat-8.3.1/QR/__Householder_Blocked.h:63-353): n x n A factored by
  * mg_sgeqrf (fp32, the norm / beta / tau of every reflector in FP64, the
- * trailing updates on the split-BF16 tensor cores), then refined in FP64:
- * r = b - A x, d = R^{-1} Q^T r applied in FP64 arithmetic with the fp32
- * reflectors, T factors and R, x += d; GMRES-IR (the same operator as its
- * preconditioner) and the FP64 fallback as in mg_dsgesv_ir.  The report's
+ * trailing updates on the split-BF16 tensor cores), then refined: r = b - A x
+ * in FP64, d = R^{-1} Q^T r with the fp32 reflectors, T factors and R, x += d
+ * in FP64.  Plain refinement solves for d in fp32 as the LU's does (Q^T and
+ * the dataflow upper solve on the scaled residual; in FP64 arithmetic when
+ * the dataflow grid cannot be co-resident); GMRES-IR uses the same operator
+ * in FP64 arithmetic as its preconditioner; then the FP64 fallback as in
+ * mg_dsgesv_ir.  The report's
  * pivot_growth is max |R| / max |A|.  opts.panel is ignored.  Synchronises. */
 mg_status_t mg_dsqrsv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
                          int ldb, double* X, int ldx, const mg_ir_opts* opts, mg_ir_report* report);
 /* The FP32 Householder QR of that solve, for m x n A (m >= n), in place: R on
  * and above the diagonal, the reflectors v below it (v_c = 1 implicit, LAPACK
  * layout as in Mat's blocked panel, QR/__Householder_Blocked.h:63-84).
- * Panels of 128 columns, one cooperative grid each (two bounded grid
- * barriers per column; alpha, beta = -sign(alpha) ||x||, tau = (beta -
- * alpha) / beta and the scaling 1 / (alpha - beta) in FP64), then T (the
- * compact WY factor, fp32) and R2 -= V (T^T (V^T R2)) with the products on the
- * split-BF16 tensor cores.  tau: n doubles (device); T: ceil(n / 128) blocks
+ * Panels of 128 columns, one cooperative grid each (one bounded grid
+ * barrier per column; the column's sum of squares, alpha, beta = -sign(alpha)
+ * ||x||, tau = (beta - alpha) / beta and the scale 1 / (alpha - beta) in
+ * FP64, the reflector's dot products and updates in fp32), then T (the
+ * compact WY factor, fp32, from V^T V formed inside the panel) and
+ * R2 -= V (T^T (V^T R2)) with the products on the split-BF16 tensor cores.  tau: n doubles (device); T: ceil(n / 128) blocks
  * of 128 x 128 floats (device, block b column-major with ld 128).
  * Synchronises. */
 mg_status_t mg_sgeqrf(mg_handle_t h, int m, int n, float* A, int lda, double* tau, float* T);

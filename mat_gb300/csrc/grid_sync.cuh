@@ -18,6 +18,13 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
     return v;
 }
 
+// The arrival: a release-ordered add at GPU scope.  The CTA barrier before it
+// orders the other threads' writes before this thread's, and the release
+// carries them (cumulativity) to whoever acquires the counter.
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
 // Returns false (in every thread of the CTA) if the wait timed out.  `limit`
 // is the poll budget (the self-test lowers it to make a wait run out).
 __device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target, int* err,
@@ -27,8 +34,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target,
     if (threadIdx.x == 0) {
         int ok = 1;
         if (gridDim.x > 1) {
-            __threadfence();
-            atomicAdd(counter, 1u);
+            red_release_add(counter, 1u);
             unsigned spins = 0;
             while (ld_acquire_u32(counter) < target) {
                 if (++spins > limit) {
@@ -50,10 +56,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target,
 // between the two overlaps the other CTAs' arrival.
 __device__ __forceinline__ void grid_arrive(unsigned* counter) {
     __syncthreads();
-    if (threadIdx.x == 0 && gridDim.x > 1) {
-        __threadfence();
-        atomicAdd(counter, 1u);
-    }
+    if (threadIdx.x == 0 && gridDim.x > 1) red_release_add(counter, 1u);
 }
 
 __device__ __forceinline__ bool grid_wait(unsigned* counter, unsigned target, int* err) {

@@ -589,6 +589,24 @@ mg_status_t lu_solve_flow(mg_handle_t h, const float* LU, int n, const float* Li
     return MG_OK;
 }
 
+// The upper solve alone with the dataflow kernel: Out = U^-1 In (the mixed
+// QR's R).  flags: nblk words.
+template <int NR>
+mg_status_t upper_solve_flow(mg_handle_t h, const float* LU, int n, const float* Uinv, float* In, float* Out,
+                             unsigned* flags, int* err) {
+    cudaStream_t st = h->stream;
+    const int nblk = (n + IR_BLOCK - 1) / IR_BLOCK;
+    const size_t smem = (size_t)IR_BLOCK * IR_BLOCK * sizeof(float);
+    MG_CHECK_CUDA(h, cudaMemsetAsync(flags, 0, (size_t)nblk * sizeof(unsigned), st));
+    int lda = n;
+    void* a2[] = {(void*)&LU, &lda, &n, (void*)&Uinv, (void*)&In, (void*)&Out, (void*)&flags, (void*)&err};
+    const cudaError_t e =
+        cudaLaunchCooperativeKernel((const void*)trsv_flow_kernel<false, NR>, dim3(nblk), dim3(256), a2, smem, st);
+    if (e != cudaSuccess) return mg::cuda_fail(h, e, "trsv_flow_kernel<upper> launch");
+    h->launches++;
+    return MG_OK;
+}
+
 // Both triangular solves of one correction: Y (in, destroyed) -> Y = U^-1 L^-1 Y, Z scratch.
 template <int NR>
 mg_status_t lu_solve_blocked(mg_handle_t h, const float* LU, int n, const float* Linv, const float* Uinv, float* Y,
@@ -812,8 +830,11 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
         MG_TRY(mg::chol_to_lu_f32(h, n, w.A32, n, w.Y));
     } else if (qr) {
         // Householder QR of the fp32 copy: R and the reflectors in A32, T blocks
-        // in Linv's area, tau (FP64) in Uinv's
-        MG_TRY(mg::sgeqrf_mixed(h, n, n, w.A32, n, (double*)w.Uinv, w.Linv, w.qws, w.gemm_err + 2));
+        // in Linv's area, tau (FP64) in splitA's (the LU's split area, unused
+        // here); pos = identity for the correction's right-hand-side scaling
+        MG_TRY(mg::sgeqrf_mixed(h, n, n, w.A32, n, (double*)w.splitA, w.Linv, w.qws, w.gemm_err + 2));
+        pos_iota_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.pos, n);
+        MG_TRY(mg::post_launch(h, "pos_iota_kernel"));
     } else {
         s = mg::sgetrf_mixed(h, n, w.A32, n, w.pos, IR_BLOCK, o.nterms, w.xchg, w.splitA, w.splitA2, w.splitB,
                              w.gemm_err, &info, o.panel == 2);
@@ -823,11 +844,27 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
     absmax_upper_kernel<<<n, 256, 0, st>>>(w.A32, n, w.norms + 18);
     MG_TRY(mg::post_launch(h, "absmax_upper_kernel"));
     bool flow = false;
-    if (!qr) {
-        MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
-        MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
+    if (qr) {
+        // inverses of R's diagonal blocks for the correction's dataflow upper
+        // solve; without a co-resident dataflow grid the correction stays on
+        // the FP64 path
+        inv_diag_blocks_kernel<false><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
+                                                                                                      w.Uinv);
+        MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<upper>"));
+        int flow_cap = 0;
+        switch (nrhs) {
+    #define MG_CAP(NRV) \
+        case NRV: flow_cap = trsv_flow_capacity<NRV>(h); break;
+            MG_CAP(1) MG_CAP(2) MG_CAP(3) MG_CAP(4) MG_CAP(5) MG_CAP(6) MG_CAP(7)
+            default: flow_cap = trsv_flow_capacity<8>(h); break;
+    #undef MG_CAP
+        }
+        flow = nblk <= flow_cap;
+    } else {
         // inverses of the diagonal blocks of L and U (the solves' block steps);
         // L's blocks are final once their panel is done (later interchanges only
         // touch rows below them)
@@ -925,11 +962,34 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
         }
         if (it == o.max_iter) break;
         prev_eta = eta;
-        if (qr) {  // correction d = R^{-1} Q^T r in FP64 with the fp32 factors, x += d
+        if (qr && !flow) {  // correction d = R^{-1} Q^T r in FP64 with the fp32 factors, x += d
             mg::ProfScope ps(h, "ir_qr_solve", 4.0 * n * (double)n * nrhs, 6.0 * n * (double)n);
             MG_TRY(mg::qr_solve_f32_factors(h, n, nrhs, w.A32, n, w.Linv, w.R, n, w.gW, n, w.qws));
             add_correction_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(n, nrhs, w.gW, X, ldx);
             MG_TRY(mg::post_launch(h, "add_correction_kernel"));
+            continue;
+        }
+        if (qr) {  // correction in fp32 as the LU's: d = R^{-1} Q^T (r / s), x += s d
+            for (int j = 0; j < nrhs; ++j) hn[24 + j] = hn[j];
+            MG_CHECK_CUDA(h, cudaMemcpyAsync(w.norms + 24, hn + 24, MAX_RHS * sizeof(double), cudaMemcpyHostToDevice,
+                                             st));
+            mg::ProfScope ps(h, "ir_qr_solve", 4.0 * n * (double)n * nrhs, 6.0 * n * (double)n);
+            prep_rhs_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(n, nrhs, w.pos, w.R, w.norms + 24,
+                                                                                 w.Y);
+            MG_TRY(mg::post_launch(h, "prep_rhs_kernel"));
+            MG_TRY(mg::qr_apply_qt_f32(h, n, nrhs, w.A32, n, w.Linv, w.Y, n, w.qws));
+            int* terr = w.gemm_err + 1;
+            switch (nrhs) {
+#define MG_USOLVE(NRV)                                                                         \
+    case NRV:                                                                                  \
+        MG_TRY(upper_solve_flow<NRV>(h, w.A32, n, w.Uinv, w.Y, w.Z, w.flags, terr));           \
+        break;
+                MG_USOLVE(1) MG_USOLVE(2) MG_USOLVE(3) MG_USOLVE(4) MG_USOLVE(5) MG_USOLVE(6) MG_USOLVE(7)
+                default: MG_USOLVE(8)
+#undef MG_USOLVE
+            }
+            update_x_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(n, nrhs, w.Z, w.norms + 24, X, ldx);
+            MG_TRY(mg::post_launch(h, "update_x_kernel"));
             continue;
         }
         // correction: d = U^-1 L^-1 P (r / s), x += s d

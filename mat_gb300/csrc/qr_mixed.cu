@@ -26,6 +26,8 @@ namespace {
 
 constexpr int QB = 128;
 constexpr int QP_THREADS = 256;
+constexpr int QG_ROWS = 32;                                    // rows per chunk of the in-kernel V^T V
+constexpr size_t QG_TILE_BYTES = (size_t)QG_ROWS * (QB + 4) * sizeof(float) + 16;  // + alignment slack
 
 // Sum of one double per thread over the CTA, valid in thread 0 (a shuffle
 // tree per warp, then warp 0 over the warps' sums, in a fixed order).
@@ -61,8 +63,8 @@ __device__ __forceinline__ double block_sum0(double v, double* red) {
 __global__ void __launch_bounds__(QP_THREADS, 1)
     qr_panel_f32_kernel(float* __restrict__ A, int lda, int m, int j0, int w, int rpc, float* __restrict__ V, int ldv,
                         double* __restrict__ tau, double* __restrict__ xp, float* __restrict__ drow, unsigned* bar,
-                        int* err) {
-    extern __shared__ __align__(16) float slab[];  // [w][rpc]
+                        float* __restrict__ gpart, int* err) {
+    extern __shared__ __align__(16) float slab[];  // [w][rpc], then the Gram tile [QG_ROWS][QB + 4]
     __shared__ double red[QP_THREADS / 32];
     __shared__ float s_coef[QB];                   // -tau * (v . a_jj) for the update
     __shared__ double s_tau, s_beta, s_scal;
@@ -134,11 +136,18 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
         }
         __syncthreads();
         const double tc = s_tau, sc = s_scal;
-        // 3. v . a_jj = a_jj(c) + scale (x . a_jj), the CTAs' fp32 partials in a fixed order
-        for (int jj = c + 1 + tid; jj < w; jj += QP_THREADS) {
-            float d = 0.f;
-            for (int u = 0; u < P; ++u) d += __ldcg(reinterpret_cast<const float*>(xpc + (size_t)u * stride + 2) + jj);
-            s_coef[jj] = (float)(-tc * fma(sc, (double)d, (double)__ldcg(&drc[jj])));
+        // 3. v . a_jj = a_jj(c) + scale (x . a_jj), the CTAs' fp32 partials in a
+        //    fixed order (a thread per column, the loads in flight together);
+        //    the update's coefficient -tau (v . a_jj) in fp32
+        {
+            const float tcf = (float)tc, scf0 = (float)sc;
+            for (int jj = c + 1 + tid; jj < w; jj += QP_THREADS) {
+                const float* pc = reinterpret_cast<const float*>(xpc + 2) + jj;
+                float d = 0.f;
+#pragma unroll 8
+                for (int u = 0; u < P; ++u) d += __ldcg(pc + (size_t)u * stride * 2);
+                s_coef[jj] = -tcf * fmaf(scf0, d, __ldcg(&drc[jj]));
+            }
         }
         __syncthreads();
         // 4. v below the diagonal, beta on it; a_jj -= (tau (v . a_jj)) v on my rows
@@ -159,6 +168,45 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
         }
         __syncthreads();
     }
+    // this CTA's part of G = V^T V over its rows (explicit V: 1 on the
+    // diagonal, 0 above): chunks of QG_ROWS rows transposed into a tile, an
+    // 8 x 8 block of G per thread
+    {
+        float* const tile = slab + (((size_t)w * rpc + 3) & ~(size_t)3);  // [QG_ROWS][QB + 4], 16-byte aligned
+        constexpr int LT = QB + 4;
+        const int ta = tid >> 4, tb = tid & 15;      // G rows 8 ta .., columns 8 tb ..
+        float g[8][8];
+#pragma unroll
+        for (int x = 0; x < 8; ++x)
+#pragma unroll
+            for (int y = 0; y < 8; ++y) g[x][y] = 0.f;
+        for (int i0 = 0; i0 < rpc; i0 += QG_ROWS) {
+            __syncthreads();
+            for (int e = tid; e < QG_ROWS * QB; e += QP_THREADS) {
+                const int cc = e / QG_ROWS, ii = e - cc * QG_ROWS, i = i0 + ii, gi = r0 + i;
+                float x = 0.f;
+                if (cc < w && i < rpc && gi < h) x = gi > cc ? slab[(size_t)cc * rpc + i] : (gi == cc ? 1.f : 0.f);
+                tile[ii * LT + cc] = x;
+            }
+            __syncthreads();
+            for (int ii = 0; ii < QG_ROWS; ++ii) {
+                const float4* ra = reinterpret_cast<const float4*>(tile + ii * LT + 8 * ta);
+                const float4* rb = reinterpret_cast<const float4*>(tile + ii * LT + 8 * tb);
+                const float4 a0 = ra[0], a1 = ra[1], b0 = rb[0], b1 = rb[1];
+                const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+                const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+                for (int x = 0; x < 8; ++x)
+#pragma unroll
+                    for (int y = 0; y < 8; ++y) g[x][y] = fmaf(av[x], bv[y], g[x][y]);
+            }
+        }
+        float* const gp = gpart + (size_t)b * QB * QB;
+#pragma unroll
+        for (int x = 0; x < 8; ++x)
+#pragma unroll
+            for (int y = 0; y < 8; ++y) gp[(8 * ta + x) + (size_t)(8 * tb + y) * QB] = g[x][y];
+    }
     // write back: R (upper, diagonal = beta) and v below it; V explicit
     for (int e = tid; e < w * rpc; e += QP_THREADS) {
         const int c = e / rpc, i = e - c * rpc, gi = r0 + i;
@@ -167,6 +215,15 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
             V[gi + (size_t)c * ldv] = gi < c ? 0.f : gi == c ? 1.f : slab[e];
         }
     }
+}
+
+// G (QB x QB, ld QB) = the sum of the panel CTAs' parts, in a fixed order.
+__global__ void qr_gsum_kernel(const float* __restrict__ gpart, int nparts, float* __restrict__ G) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= QB * QB) return;
+    float s = 0.f;
+    for (int u = 0; u < nparts; ++u) s += gpart[(size_t)u * QB * QB + e];
+    G[e] = s;
 }
 
 // T (w x w, upper, fp32, ld QB) of H_0 ... H_{w-1} = I - V T V^T from
@@ -246,6 +303,80 @@ __global__ void qt_update_kernel(const float* __restrict__ A, int lda, int m, in
     }
 }
 
+// ---- the same Q^T in fp32 for the refinement's correction (a scaled
+// residual, as the LU's correction is solved in fp32): X (n x nrhs, ld ldx,
+// nrhs <= 8) := (I - V T^T V^T) X for one panel.  Dots: a warp per reflector,
+// lanes over the rows of the CTA's chunk (coalesced), partials per CTA in a
+// fixed order; the update: a thread per row.
+__global__ void qt32_dots_kernel(const float* __restrict__ A, int lda, int m, int j0, int w, const float* __restrict__ X,
+                                 int ldx, int nrhs, float* __restrict__ part) {
+    const int h = m - j0;
+    const int chunk = (h + gridDim.x - 1) / gridDim.x;
+    const int lo = blockIdx.x * chunk, hi = min(h, lo + chunk);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int c = warp; c < w; c += nw) {
+        const float* v = A + j0 + (size_t)(j0 + c) * lda;
+        float acc[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[j] = 0.f;
+        for (int i = max(lo, c) + lane; i < hi; i += 32) {
+            const float vi = i == c ? 1.f : v[i];
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (j < nrhs) acc[j] = fmaf(vi, X[j0 + i + (size_t)j * ldx], acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], off);
+        }
+        if (lane == 0)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) part[((size_t)blockIdx.x * QB + c) * 8 + j] = acc[j];
+    }
+}
+
+__global__ void qt32_tw_kernel(const float* __restrict__ part, int nparts, const float* __restrict__ T, int w, int nrhs,
+                               float* __restrict__ y) {
+    __shared__ float wv[QB * 8];
+    for (int q = threadIdx.x; q < w * 8; q += blockDim.x) {
+        float d = 0.f;
+#pragma unroll 8
+        for (int u = 0; u < nparts; ++u) d += part[(size_t)u * QB * 8 + q];
+        wv[q] = d;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < w * 8; q += blockDim.x) {
+        const int c = q / 8, j = q % 8;
+        float d = 0.f;
+        if (j < nrhs)
+            for (int k = 0; k <= c; ++k) d = fmaf(T[k + (size_t)c * QB], wv[k * 8 + j], d);  // (T^T w)_c
+        y[q] = d;
+    }
+}
+
+__global__ void qt32_update_kernel(const float* __restrict__ A, int lda, int m, int j0, int w,
+                                   const float* __restrict__ y, int nrhs, float* __restrict__ X, int ldx) {
+    __shared__ float ys[QB * 8];
+    for (int q = threadIdx.x; q < w * 8; q += blockDim.x) ys[q] = y[q];
+    __syncthreads();
+    const int h = m - j0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < h; i += gridDim.x * blockDim.x) {
+        const int cmax = min(w - 1, i);
+        float acc[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[j] = j < nrhs ? X[j0 + i + (size_t)j * ldx] : 0.f;
+        for (int c = 0; c <= cmax; ++c) {
+            const float v = c == i ? 1.f : A[j0 + i + (size_t)(j0 + c) * lda];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[j] = fmaf(-v, ys[c * 8 + j], acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (j < nrhs) X[j0 + i + (size_t)j * ldx] = acc[j];
+    }
+}
+
 __global__ void copy_f64_kernel(int n, int nrhs, const double* __restrict__ B, int ldb, double* __restrict__ X,
                                 int ldx) {
     const size_t total = (size_t)n * nrhs;
@@ -262,6 +393,7 @@ size_t qr_mixed_ws_bytes(int m, int n, int num_sms) {
     return align_up((size_t)m * QB * sizeof(float), 1024)                  // V
            + align_up((size_t)QB * n * sizeof(float), 1024) * 2             // W, W2
            + align_up((size_t)QB * QB * sizeof(float), 1024)                // G
+           + align_up((size_t)P * QB * QB * sizeof(float), 1024)            // the panel CTAs' parts of G
            + align_up((size_t)2 * P * (QB + 2) * sizeof(double), 1024)      // panel partials (by parity)
            + align_up((size_t)QT_CTAS * QB * 8 * sizeof(double), 1024)      // Q^T partials
            + align_up((size_t)QB * 8 * sizeof(double), 1024)                // T^T w
@@ -281,6 +413,7 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
     float* W = (float*)take((size_t)QB * n * sizeof(float));
     float* W2 = (float*)take((size_t)QB * n * sizeof(float));
     float* G = (float*)take((size_t)QB * QB * sizeof(float));
+    float* gpart = (float*)take((size_t)P0max * QB * QB * sizeof(float));
     double* xp = (double*)take((size_t)2 * P0max * (QB + 2) * sizeof(double));
     take((size_t)QT_CTAS * QB * 8 * sizeof(double));
     take((size_t)QB * 8 * sizeof(double));
@@ -297,11 +430,11 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
         int P = (hgt + 255) / 256;
         if (P > P0max) P = P0max;
         int rpc = (hgt + P - 1) / P;
-        while ((size_t)rpc * w * sizeof(float) > (size_t)h->max_smem_optin - 4096 && P < P0max) {
+        while ((size_t)rpc * w * sizeof(float) + QG_TILE_BYTES > (size_t)h->max_smem_optin - 4096 && P < P0max) {
             ++P;
             rpc = (hgt + P - 1) / P;
         }
-        const size_t smem = (size_t)rpc * w * sizeof(float);
+        const size_t smem = (size_t)rpc * w * sizeof(float) + QG_TILE_BYTES;
         if (smem > (size_t)h->max_smem_optin - 4096)
             return fail(h, MG_ERR_UNSUPPORTED, "sgeqrf_mixed: panel of %d rows does not fit the SMs", hgt);
         {
@@ -310,14 +443,15 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
             int lda_ = lda, m_ = m, j0_ = j0, w_ = w, rpc_ = rpc, ldv = hgt;
             float* A_ = A;
             double* tau_ = tau + j0;
-            void* args[] = {&A_, &lda_, &m_, &j0_, &w_, &rpc_, &V, &ldv, &tau_, &xp, &drow, &bar, &err};
+            void* args[] = {&A_, &lda_, &m_, &j0_, &w_, &rpc_, &V, &ldv, &tau_, &xp, &drow, &bar, &gpart, &err};
             const cudaError_t e = cudaLaunchCooperativeKernel((const void*)qr_panel_f32_kernel, dim3(P),
                                                               dim3(QP_THREADS), args, smem, st);
             if (e != cudaSuccess) return cuda_fail(h, e, "qr_panel_f32_kernel launch");
             h->launches++;
         }
         float* Tb = T + (size_t)(j0 / QB) * QB * QB;
-        MG_TRY(sgemm_auto(h, 1, 0, w, w, hgt, 1.f, V, hgt, V, hgt, 0.f, G, QB, 0));
+        qr_gsum_kernel<<<QB * QB / 256, 256, 0, st>>>(gpart, P, G);
+        MG_TRY(post_launch(h, "qr_gsum_kernel"));
         qr_tfactor_kernel<<<1, QB, QB * (QB + 1) * sizeof(float), st>>>(G, QB, tau + j0, w, Tb);
         MG_TRY(post_launch(h, "qr_tfactor_kernel"));
         const int nt = n - j0 - w;
@@ -333,6 +467,37 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
 
 // X := R^{-1} (Q^T B)(0:n) in FP64 for the fp32 factors of sgeqrf_mixed
 // (square use: m = n): Q^T applied panel by panel, then the upper solve.
+// X (fp32, n x nrhs, ld ldx, nrhs <= 8) := Q^T X for the fp32 factors of
+// sgeqrf_mixed (square: m = n), in fp32.
+mg_status_t qr_apply_qt_f32(mg_handle_t h, int n, int nrhs, const float* A, int lda, const float* T, float* X, int ldx,
+                            void* ws) {
+    if (n == 0 || nrhs == 0) return MG_OK;
+    if (nrhs > 8) return fail(h, MG_ERR_ARG, "qr_apply_qt_f32: at most 8 right-hand sides");
+    char* p = (char*)ws;
+    auto take = [&](size_t bytes) { char* q = p; p += align_up(bytes, 1024); return q; };
+    take((size_t)n * QB * sizeof(float));
+    take((size_t)QB * n * sizeof(float));
+    take((size_t)QB * n * sizeof(float));
+    take((size_t)QB * QB * sizeof(float));
+    take((size_t)h->num_sms * QB * QB * sizeof(float));
+    take((size_t)2 * h->num_sms * (QB + 2) * sizeof(double));
+    float* part = (float*)take((size_t)QT_CTAS * QB * 8 * sizeof(double));
+    float* y = (float*)take((size_t)QB * 8 * sizeof(double));
+    const cudaStream_t st = h->stream;
+    const int cap = h->num_sms * 8;
+    for (int j0 = 0; j0 < n; j0 += QB) {
+        const int w = n - j0 < QB ? n - j0 : QB;
+        qt32_dots_kernel<<<QT_CTAS, 256, 0, st>>>(A, lda, n, j0, w, X, ldx, nrhs, part);
+        MG_TRY(post_launch(h, "qt32_dots_kernel"));
+        qt32_tw_kernel<<<1, 256, 0, st>>>(part, QT_CTAS, T + (size_t)(j0 / QB) * QB * QB, w, nrhs, y);
+        MG_TRY(post_launch(h, "qt32_tw_kernel"));
+        int gu = (n - j0 + 255) / 256;
+        qt32_update_kernel<<<gu < cap ? gu : cap, 256, 0, st>>>(A, lda, n, j0, w, y, nrhs, X, ldx);
+        MG_TRY(post_launch(h, "qt32_update_kernel"));
+    }
+    return MG_OK;
+}
+
 mg_status_t qr_solve_f32_factors(mg_handle_t h, int n, int nrhs, const float* A, int lda, const float* T,
                                  const double* B, int ldb, double* X, int ldx, void* ws) {
     if (n == 0 || nrhs == 0) return MG_OK;
@@ -343,6 +508,7 @@ mg_status_t qr_solve_f32_factors(mg_handle_t h, int n, int nrhs, const float* A,
     take((size_t)QB * n * sizeof(float));
     take((size_t)QB * n * sizeof(float));
     take((size_t)QB * QB * sizeof(float));
+    take((size_t)h->num_sms * QB * QB * sizeof(float));
     take((size_t)2 * h->num_sms * (QB + 2) * sizeof(double));
     double* part = (double*)take((size_t)QT_CTAS * QB * 8 * sizeof(double));
     double* y = (double*)take((size_t)QB * 8 * sizeof(double));
