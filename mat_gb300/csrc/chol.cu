@@ -43,9 +43,17 @@ __global__ void llt2_kernel(T* __restrict__ L, int ldl, int k, int col0, int* __
         __syncthreads();  // every thread has read d before row jj is scaled
         if (r >= jj && r < k) s[r + jj * LLT2_MAX] = s[r + jj * LLT2_MAX] * t;
         __syncthreads();
-        if (r > jj && r < k) {
-            const T lrj = s[r + jj * LLT2_MAX];
-            for (int i = jj + 1; i <= r; ++i) s[r + i * LLT2_MAX] = fma(lrj, -s[i + jj * LLT2_MAX], s[r + i * LLT2_MAX]);
+        // the trailing triangle, every element once (the same single fma per
+        // element as a row-at-a-time loop), spread over the CTA as 32 rows x
+        // 4 column groups instead of one thread per row, whose longest row was
+        // the column step's chain
+        {
+            const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5, ncg = blockDim.x >> 5;
+            for (int i = jj + 1 + tc; i < k; i += ncg) {
+                const T lij = s[i + jj * LLT2_MAX];
+                for (int rr = i + tr; rr < k; rr += 32)
+                    s[rr + i * LLT2_MAX] = fma(s[rr + jj * LLT2_MAX], -lij, s[rr + i * LLT2_MAX]);
+            }
         }
         __syncthreads();
     }
@@ -56,32 +64,61 @@ __global__ void llt2_kernel(T* __restrict__ L, int ldl, int k, int col0, int* __
 }
 
 // X (rows x k) := X * Lkk^{-T} (Mat's __Solve_direct_XLT), one thread per row:
-// for j: x_j *= 1/L(j,j); x_kk = fma(x_j, -L(kk,j), x_kk) for kk > j.
+// for j: x_j *= 1/L(j,j); x_kk = fma(x_j, -L(kk,j), x_kk) for kk > j.  The
+// row sits in registers as a rotating window so that the column loop stays
+// rolled at fixed register indices (the fully unrolled k = 96 loop spilled to
+// the stack and was instruction-fetch bound): at step j, position 0 holds x_j
+// and positions 1 .. k-1-j hold x_{j+1} .. x_{k-1}; each step shifts the
+// window by one and parks the finished x_j at the end.
+constexpr int XLT_THREADS = 128;
+template <typename T, int KB>
+constexpr size_t xlt_smem_bytes() { return ((size_t)KB * KB + KB) * sizeof(T); }
+
 template <typename T, int KB = LLT_BS>
-__global__ void xlt_kernel(const T* __restrict__ Ld, int ldl, T* __restrict__ X, int ldx, int rows, int k) {
-    __shared__ T sl[KB * KB];
-    __shared__ T sinv[KB];
-    for (int e = threadIdx.x; e < k * k; e += blockDim.x) sl[e] = Ld[(e % k) + (size_t)(e / k) * ldl];
+__global__ void __launch_bounds__(XLT_THREADS) xlt_kernel(const T* __restrict__ Ld, int ldl, T* __restrict__ X, int ldx,
+                                                         int rows, int k) {
+    extern __shared__ __align__(16) unsigned char xlt_raw[];
+    T* const sl = reinterpret_cast<T*>(xlt_raw);  // [KB][KB]: L(i, j) at i + j * KB
+    T* const sinv = sl + KB * KB;                 // [KB]
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+        const int i = e % k, j = e / k;
+        sl[i + j * KB] = Ld[i + (size_t)j * ldl];
+    }
     __syncthreads();
-    for (int j = threadIdx.x; j < k; j += blockDim.x) sinv[j] = T(1) / sl[j + j * k];
+    for (int j = threadIdx.x; j < k; j += blockDim.x) sinv[j] = T(1) / sl[j + j * KB];
     __syncthreads();
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.x * XLT_THREADS + threadIdx.x;
     if (r >= rows) return;
     T x[KB];
 #pragma unroll
     for (int j = 0; j < KB; ++j) x[j] = j < k ? X[r + (size_t)j * ldx] : T(0);
+#pragma unroll 1
+    for (int j = 0; j < k; ++j) {
+        const T xj = x[0] * sinv[j];
+        const T* lj = sl + j * KB + j;  // lj[d] = L(j + d, j)
+        const int na = k - 1 - j;       // positions 1 .. na still to update
 #pragma unroll
-    for (int j = 0; j < KB; ++j) {
-        if (j < k) {
-            x[j] = x[j] * sinv[j];
+        for (int d = 1; d < KB; ++d) x[d - 1] = d <= na ? fma(xj, -lj[d], x[d]) : x[d];
+        x[KB - 1] = xj;
+    }
+#pragma unroll 1
+    for (int j = k; j < KB; ++j) {  // k < KB: finish the rotation
+        const T x0 = x[0];
 #pragma unroll
-            for (int kk = j + 1; kk < KB; ++kk)
-                if (kk < k) x[kk] = fma(x[j], -sl[kk + j * k], x[kk]);
-        }
+        for (int d = 1; d < KB; ++d) x[d - 1] = x[d];
+        x[KB - 1] = x0;
     }
 #pragma unroll
     for (int j = 0; j < KB; ++j)
         if (j < k) X[r + (size_t)j * ldx] = x[j];
+}
+
+template <typename T, int KB = LLT_BS>
+mg_status_t launch_xlt(mg_handle_t h, cudaStream_t st, const T* Ld, int ldl, T* X, int ldx, int rows, int k) {
+    constexpr size_t smem = xlt_smem_bytes<T, KB>();
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(xlt_kernel<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    xlt_kernel<T, KB><<<(rows + XLT_THREADS - 1) / XLT_THREADS, XLT_THREADS, smem, st>>>(Ld, ldl, X, ldx, rows, k);
+    return mg::post_launch(h, "xlt_kernel");
 }
 
 // Unblocked LDL^T of the k x k block at L (k <= 96), in place, lower part
@@ -281,9 +318,7 @@ mg_status_t potrf_impl(mg_handle_t h, int n, T* L, int ldl, int* info_out) {
             MG_TRY(post_launch(h, "llt2_kernel"));
             if (j + LLT_BS < n) {
                 const int rows = n - (j + LLT_BS);
-                xlt_kernel<T><<<(rows + 127) / 128, 128, 0, h->stream>>>(D, ldl, L + (j + LLT_BS) + (size_t)j * ldl,
-                                                                          ldl, rows, LLT_BS);
-                MG_TRY(post_launch(h, "xlt_kernel"));
+                MG_TRY(launch_xlt<T>(h, h->stream, D, ldl, L + (j + LLT_BS) + (size_t)j * ldl, ldl, rows, LLT_BS));
             }
             return MG_OK;
         };
@@ -357,7 +392,7 @@ mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out)
 // fp32 factorization of an SPD matrix can break down near singularity).
 mg_status_t spotrf_mixed(mg_handle_t h, int n, float* L, int ldl, int nterms, void* split, int* gemm_err,
                          int* info_out) {
-    constexpr int NB = 96;
+    constexpr int NB = 64;
     if (info_out) *info_out = 0;
     if (n == 0) return MG_OK;
     MG_TRY(ensure_hws(h, 64));
@@ -380,8 +415,7 @@ mg_status_t spotrf_mixed(mg_handle_t h, int n, float* L, int ldl, int nterms, vo
         float* C = L + (j + nb) + (size_t)(j + nb) * ldl;
         {
             ProfScope prof(h, "trsm_f32", (double)rows * nb * nb, 8.0 * rows * nb);
-            xlt_kernel<float, NB><<<(rows + 127) / 128, 128, 0, st>>>(D, ldl, P, ldl, rows, nb);
-            MG_TRY(post_launch(h, "xlt_kernel"));
+            MG_TRY((launch_xlt<float, NB>(h, st, D, ldl, P, ldl, rows, nb)));
         }
         {
             ProfScope prof(h, "split", 0.0, 2.0 * rows * nb * (4.0 + 2.0 * nterms));
@@ -434,8 +468,7 @@ mg_status_t dldlt_impl(mg_handle_t h, int n, double* L, int ldl, double* d, int*
             if (j + LLT_BS < n) {
                 const int rows = n - (j + LLT_BS);
                 double* P = L + (j + LLT_BS) + (size_t)j * ldl;
-                xlt_kernel<double><<<(rows + 127) / 128, 128, 0, st>>>(D, ldl, P, ldl, rows, LLT_BS);
-                MG_TRY(post_launch(h, "xlt_kernel"));
+                MG_TRY(launch_xlt<double>(h, st, D, ldl, P, ldl, rows, LLT_BS));
                 int blocks = (int)(((size_t)rows * LLT_BS + 255) / 256);
                 if (blocks > h->num_sms * 8) blocks = h->num_sms * 8;
                 ldlt_scale_kernel<<<blocks, 256, 0, st>>>(P, ldl, rows, LLT_BS, d + j, W, rows);

@@ -17,10 +17,15 @@
 // contiguous runs (the slab in shared memory); per column one bounded grid
 // barrier (the norm's and the dot products' partial sums together), every
 // CTA summing the partials in the same order.
+#include <cooperative_groups.h>
+
 #include <cmath>
 
 #include "grid_sync.cuh"
 #include "mg_internal.cuh"
+#include "tc_common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -46,6 +51,111 @@ __device__ __forceinline__ double block_sum0(double v, double* red) {
     return t;
 }
 
+// The panel slab in shared memory: column c of a CTA's rows at slab + c * lds,
+// lds = rpc | 1 (odd, so that lanes reading one row of consecutive columns hit
+// distinct banks).
+
+// This CTA's part of G = V^T V over its rows of the panel slab (explicit V:
+// 1 on the diagonal, 0 above; rows >= h are zero): chunks of QG_ROWS rows
+// transposed into a tile after the slab, an 8 x 8 block of G per thread,
+// written to gp (QB x QB, ld QB).
+__device__ __forceinline__ void gram_part(const float* slab, int w, int lds, int rpc, int r0, int h, float* gp) {
+    const int tid = threadIdx.x;
+    float* const tile = const_cast<float*>(slab) + (((size_t)w * lds + 3) & ~(size_t)3);  // 16-byte aligned
+    constexpr int LT = QB + 4;
+    const int ta = tid >> 4, tb = tid & 15;  // G rows 8 ta .., columns 8 tb ..
+    float g[8][8];
+#pragma unroll
+    for (int x = 0; x < 8; ++x)
+#pragma unroll
+        for (int y = 0; y < 8; ++y) g[x][y] = 0.f;
+    for (int i0 = 0; i0 < rpc; i0 += QG_ROWS) {
+        __syncthreads();
+        for (int e = tid; e < QG_ROWS * QB; e += QP_THREADS) {
+            const int cc = e / QG_ROWS, ii = e - cc * QG_ROWS, i = i0 + ii, gi = r0 + i;
+            float x = 0.f;
+            if (cc < w && i < rpc && gi < h) x = gi > cc ? slab[(size_t)cc * lds + i] : (gi == cc ? 1.f : 0.f);
+            tile[ii * LT + cc] = x;
+        }
+        __syncthreads();
+        for (int ii = 0; ii < QG_ROWS; ++ii) {
+            const float4* ra = reinterpret_cast<const float4*>(tile + ii * LT + 8 * ta);
+            const float4* rb = reinterpret_cast<const float4*>(tile + ii * LT + 8 * tb);
+            const float4 a0 = ra[0], a1 = ra[1], b0 = rb[0], b1 = rb[1];
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int x = 0; x < 8; ++x)
+#pragma unroll
+                for (int y = 0; y < 8; ++y) g[x][y] = fmaf(av[x], bv[y], g[x][y]);
+        }
+    }
+#pragma unroll
+    for (int x = 0; x < 8; ++x)
+#pragma unroll
+        for (int y = 0; y < 8; ++y) gp[(8 * ta + x) + (size_t)(8 * tb + y) * QB] = g[x][y];
+}
+
+// The dots of column c (the rows below the diagonal) with the panel's later
+// columns jj > c: a thread per (column, half of the rows), four independent
+// accumulators along the rows (a fixed order), the halves added in shared
+// memory (part: 2 x QB floats); then out(jj, dot) for each jj.  Called by
+// every thread of the CTA (it holds a CTA barrier).
+template <class Out>
+__device__ __forceinline__ void panel_dots(const float* slab, int lds, int rpc, int w, int c, int r0, int h,
+                                           float* part, Out out) {
+    const int tid = threadIdx.x, half = tid >> 7, jj = c + 1 + (tid & 127);
+    const int ilo = max(0, c + 1 - r0), ihi = min(rpc, h - r0);  // my rows below the diagonal
+    const int mid = ilo + max(0, ihi - ilo) / 2;
+    if (jj < w) {
+        const float* col = slab + (size_t)c * lds;
+        const float* a = slab + (size_t)jj * lds;
+        const int lo = half ? mid : ilo, hi = half ? max(ihi, mid) : mid;
+        float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;
+        int i = lo;
+        for (; i + 3 < hi; i += 4) {
+            d0 = fmaf(col[i], a[i], d0);
+            d1 = fmaf(col[i + 1], a[i + 1], d1);
+            d2 = fmaf(col[i + 2], a[i + 2], d2);
+            d3 = fmaf(col[i + 3], a[i + 3], d3);
+        }
+        for (; i < hi; ++i) d0 = fmaf(col[i], a[i], d0);
+        part[half * QB + jj] = (d0 + d1) + (d2 + d3);
+    }
+    __syncthreads();
+    if (half == 0 && jj < w) out(jj, part[jj] + part[QB + jj]);
+}
+
+// The reflector and its update on my rows (a thread per row): v = x * scale
+// below the diagonal, beta on it; a_jj += coef_jj v for jj > c (coef = -tau
+// (v . a_jj)), four columns at a time with the loads ahead of the stores.
+__device__ __forceinline__ void panel_apply(float* slab, int lds, int rpc, int w, int c, int r0, int h, float scf,
+                                            float betaf, const float* coef) {
+    for (int i = threadIdx.x; i < rpc; i += QP_THREADS) {
+        const int gi = r0 + i;
+        if (gi < c || gi >= h) continue;
+        float* const p = slab + i;
+        float v = 1.f;
+        if (gi == c) {
+            p[(size_t)c * lds] = betaf;
+        } else {
+            v = p[(size_t)c * lds] * scf;
+            p[(size_t)c * lds] = v;
+        }
+        int jj = c + 1;
+        for (; jj + 3 < w; jj += 4) {
+            float* const q0 = p + (size_t)jj * lds;
+            const float a0 = q0[0], a1 = q0[lds], a2 = q0[2 * (size_t)lds], a3 = q0[3 * (size_t)lds];
+            const float c0 = coef[jj], c1 = coef[jj + 1], c2 = coef[jj + 2], c3 = coef[jj + 3];
+            q0[0] = fmaf(c0, v, a0);
+            q0[lds] = fmaf(c1, v, a1);
+            q0[2 * (size_t)lds] = fmaf(c2, v, a2);
+            q0[3 * (size_t)lds] = fmaf(c3, v, a3);
+        }
+        for (; jj < w; ++jj) p[(size_t)jj * lds] = fmaf(coef[jj], v, p[(size_t)jj * lds]);
+    }
+}
+
 // One grid barrier per column.  Before it every CTA publishes, for the rows
 // below the diagonal, its partial sum of squares of the column x (FP64) and
 // its partial dots of x with the panel's later columns a_j (fp32); the owner
@@ -64,41 +174,36 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
     qr_panel_f32_kernel(float* __restrict__ A, int lda, int m, int j0, int w, int rpc, float* __restrict__ V, int ldv,
                         double* __restrict__ tau, double* __restrict__ xp, float* __restrict__ drow, unsigned* bar,
                         float* __restrict__ gpart, int* err) {
-    extern __shared__ __align__(16) float slab[];  // [w][rpc], then the Gram tile [QG_ROWS][QB + 4]
+    extern __shared__ __align__(16) float slab[];  // [w][lds], then the Gram tile [QG_ROWS][QB + 4]
+    __shared__ float sh_part[2 * QB];              // the dots' halves
     __shared__ double red[QP_THREADS / 32];
     __shared__ float s_coef[QB];                   // -tau * (v . a_jj) for the update
     __shared__ double s_tau, s_beta, s_scal;
     const int P = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int h = m - j0;
     const int r0 = b * rpc, r1 = min(h, r0 + rpc);
+    const int lds = rpc | 1;  // the slab's column stride
     float* const P0 = A + j0 + (size_t)j0 * lda;
     const int stride = QB + 2;
     for (int e = tid; e < w * rpc; e += QP_THREADS) {
         const int c = e / rpc, i = e - c * rpc;
-        slab[e] = r0 + i < h ? P0[r0 + i + (size_t)c * lda] : 0.f;
+        slab[(size_t)c * lds + i] = r0 + i < h ? P0[r0 + i + (size_t)c * lda] : 0.f;
     }
     __syncthreads();
     unsigned target = 0;
     bool ok = true;
     for (int c = 0; c < w && ok; ++c) {
-        float* col = slab + (size_t)c * rpc;
+        float* col = slab + (size_t)c * lds;
         double* const xpc = xp + (size_t)(c & 1) * P * stride;
         float* const drc = drow + (c & 1) * QB;
         // 1. partials below the diagonal: sum of squares (FP64), dots with the
         //    later columns (fp32, a warp per column); the diagonal row (owner)
-        for (int jj = c + 1 + warp; jj < w; jj += QP_THREADS / 32) {
-            const float* a = slab + (size_t)jj * rpc;
-            float d = 0.f;
-            for (int i = lane; i < rpc; i += 32) {
-                const int gi = r0 + i;
-                if (gi > c && gi < h) d = fmaf(col[i], a[i], d);
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xffffffffu, d, off);
-            if (lane == 0) reinterpret_cast<float*>(xpc + (size_t)b * stride + 2)[jj] = d;
+        {
+            float* const xd = reinterpret_cast<float*>(xpc + (size_t)b * stride + 2);
+            panel_dots(slab, lds, rpc, w, c, r0, h, sh_part, [&](int jj, float d) { xd[jj] = d; });
         }
         if (c >= r0 && c < r1)
-            for (int jj = c + tid; jj < w; jj += QP_THREADS) drc[jj] = slab[(size_t)jj * rpc + (c - r0)];
+            for (int jj = c + tid; jj < w; jj += QP_THREADS) drc[jj] = slab[(size_t)jj * lds + (c - r0)];
         double s = 0.0;
         for (int i = tid; i < rpc; i += QP_THREADS) {
             const int gi = r0 + i;
@@ -151,70 +256,163 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
         }
         __syncthreads();
         // 4. v below the diagonal, beta on it; a_jj -= (tau (v . a_jj)) v on my rows
-        const float scf = (float)sc, betaf = (float)s_beta;
-        for (int i = tid; i < rpc; i += QP_THREADS) {
-            const int gi = r0 + i;
-            if (gi > c && gi < h) col[i] = col[i] * scf;
-            else if (gi == c) col[i] = betaf;
-        }
-        __syncthreads();
-        for (int jj = c + 1; jj < w; ++jj) {
-            float* a = slab + (size_t)jj * rpc;
-            const float cf = s_coef[jj];
-            for (int i = tid; i < rpc; i += QP_THREADS) {
-                const int gi = r0 + i;
-                if (gi >= c && gi < h) a[i] = fmaf(cf, gi == c ? 1.f : col[i], a[i]);
-            }
-        }
+        panel_apply(slab, lds, rpc, w, c, r0, h, (float)sc, (float)s_beta, s_coef);
         __syncthreads();
     }
-    // this CTA's part of G = V^T V over its rows (explicit V: 1 on the
-    // diagonal, 0 above): chunks of QG_ROWS rows transposed into a tile, an
-    // 8 x 8 block of G per thread
-    {
-        float* const tile = slab + (((size_t)w * rpc + 3) & ~(size_t)3);  // [QG_ROWS][QB + 4], 16-byte aligned
-        constexpr int LT = QB + 4;
-        const int ta = tid >> 4, tb = tid & 15;      // G rows 8 ta .., columns 8 tb ..
-        float g[8][8];
-#pragma unroll
-        for (int x = 0; x < 8; ++x)
-#pragma unroll
-            for (int y = 0; y < 8; ++y) g[x][y] = 0.f;
-        for (int i0 = 0; i0 < rpc; i0 += QG_ROWS) {
-            __syncthreads();
-            for (int e = tid; e < QG_ROWS * QB; e += QP_THREADS) {
-                const int cc = e / QG_ROWS, ii = e - cc * QG_ROWS, i = i0 + ii, gi = r0 + i;
-                float x = 0.f;
-                if (cc < w && i < rpc && gi < h) x = gi > cc ? slab[(size_t)cc * rpc + i] : (gi == cc ? 1.f : 0.f);
-                tile[ii * LT + cc] = x;
-            }
-            __syncthreads();
-            for (int ii = 0; ii < QG_ROWS; ++ii) {
-                const float4* ra = reinterpret_cast<const float4*>(tile + ii * LT + 8 * ta);
-                const float4* rb = reinterpret_cast<const float4*>(tile + ii * LT + 8 * tb);
-                const float4 a0 = ra[0], a1 = ra[1], b0 = rb[0], b1 = rb[1];
-                const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-                const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-                for (int x = 0; x < 8; ++x)
-#pragma unroll
-                    for (int y = 0; y < 8; ++y) g[x][y] = fmaf(av[x], bv[y], g[x][y]);
-            }
-        }
-        float* const gp = gpart + (size_t)b * QB * QB;
-#pragma unroll
-        for (int x = 0; x < 8; ++x)
-#pragma unroll
-            for (int y = 0; y < 8; ++y) gp[(8 * ta + x) + (size_t)(8 * tb + y) * QB] = g[x][y];
-    }
+    gram_part(slab, w, lds, rpc, r0, h, gpart + (size_t)b * QB * QB);
     // write back: R (upper, diagonal = beta) and v below it; V explicit
     for (int e = tid; e < w * rpc; e += QP_THREADS) {
         const int c = e / rpc, i = e - c * rpc, gi = r0 + i;
         if (gi < h) {
-            P0[gi + (size_t)c * lda] = slab[e];
-            V[gi + (size_t)c * ldv] = gi < c ? 0.f : gi == c ? 1.f : slab[e];
+            const float x = slab[(size_t)c * lds + i];
+            P0[gi + (size_t)c * lda] = x;
+            V[gi + (size_t)c * ldv] = gi < c ? 0.f : gi == c ? 1.f : x;
         }
     }
+}
+
+// ---- the cluster form of the panel: the same column steps on one 16-CTA
+// thread-block cluster, for panels whose slab fits the cluster's shared
+// memory.  The per-column exchange is a push instead of a grid barrier:
+// every CTA stores its record (the sum of squares as a double, then the dot
+// partials) with st.async into its slot of every CTA, the owner of the
+// diagonal row stores that row too, and the bytes complete on each
+// receiver's mbarrier (double-buffered by column parity: a CTA sends column
+// c+2 only after receiving every record of column c+1, which every CTA
+// sends only after its threads have finished reading column c's slots).
+constexpr int QC_CS = 16;
+constexpr int QC_REC = 4 + QB;  // floats per record: the double sum of squares, padding, the dots
+constexpr uint32_t QC_RX_BYTES = QC_CS * QC_REC * sizeof(float) + QB * sizeof(float);
+
+struct QcShared {
+    __align__(16) float recv[2][QC_CS][QC_REC];  // every CTA's record of the column, by parity
+    __align__(16) float recv_diag[2][QB];        // the diagonal row, by parity
+    __align__(8) uint64_t mbar[2];
+    __align__(16) float rec[QC_REC];             // this CTA's record, staged
+    __align__(16) float diag[QB];                // the diagonal row, staged by its owner
+    float coef[QB];
+    double red[QP_THREADS / 32];
+    double tau, beta, scal;
+};
+
+__global__ void __launch_bounds__(QP_THREADS, 1)
+    qr_panel_cluster_kernel(float* __restrict__ A, int lda, int m, int j0, int w, int rpc, float* __restrict__ V,
+                            int ldv, double* __restrict__ tau, float* __restrict__ gpart, int* err) {
+    extern __shared__ __align__(16) float slab[];  // [w][lds], then the Gram tile
+    __shared__ float sh_part[2 * QB];              // the dots' halves
+    __shared__ QcShared qs;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int q = (int)cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int h = m - j0;
+    const int r0 = q * rpc, r1 = min(h, r0 + rpc);
+    const int lds = rpc | 1;  // the slab's column stride
+    float* const P0 = A + j0 + (size_t)j0 * lda;
+    for (int e = tid; e < w * rpc; e += QP_THREADS) {
+        const int c = e / rpc, i = e - c * rpc;
+        slab[(size_t)c * lds + i] = r0 + i < h ? P0[r0 + i + (size_t)c * lda] : 0.f;
+    }
+    if (tid == 0) {
+        tc::mbar_init(&qs.mbar[0], 1);
+        tc::mbar_init(&qs.mbar[1], 1);
+        tc::fence_barrier_init();
+        tc::mbar_arrive_expect_tx(&qs.mbar[0], QC_RX_BYTES);
+        tc::mbar_arrive_expect_tx(&qs.mbar[1], QC_RX_BYTES);
+    }
+    cluster.sync();  // the slab is loaded and every CTA's barriers are armed
+    bool rx_failed = false;  // warp 0: a receive wait gave up (error recorded; later waits skipped)
+    for (int c = 0; c < w; ++c) {
+        const int buf = c & 1;
+        float* col = slab + (size_t)c * lds;
+        const bool owner = c >= r0 && c < r1;
+        // 1. the record: dots of the unscaled column with the later columns
+        //    (fp32, a warp per column), sum of squares (FP64); the diagonal row
+        panel_dots(slab, lds, rpc, w, c, r0, h, sh_part, [&](int jj, float d) { qs.rec[4 + jj] = d; });
+        if (owner)
+            for (int jj = c + tid; jj < w; jj += QP_THREADS) qs.diag[jj] = slab[(size_t)jj * lds + (c - r0)];
+        double s = 0.0;
+        for (int i = tid; i < rpc; i += QP_THREADS) {
+            const int gi = r0 + i;
+            if (gi > c && gi < h) {
+                const double x = col[i];
+                s = fma(x, x, s);
+            }
+        }
+        s = block_sum0(s, qs.red);
+        if (tid == 0) *reinterpret_cast<double*>(&qs.rec[0]) = s;
+        __syncthreads();
+        // 2. warp 0 pushes the record into slot [q] of every CTA (lane l -> CTA
+        //    l), and the owner's warp 0 the diagonal row (lane 16 + l -> CTA l)
+        if (warp == 0) {
+            if (lane < QC_CS) {
+                const uint32_t dst = tc::cluster_addr(&qs.recv[buf][q][0], lane);
+                const uint32_t bar = tc::cluster_addr(&qs.mbar[buf], lane);
+                const float4* r4 = reinterpret_cast<const float4*>(qs.rec);
+#pragma unroll 4
+                for (int u = 0; u < QC_REC / 4; ++u) tc::st_async16(dst + 16u * u, r4[u], bar);
+            } else if (owner) {
+                const uint32_t dst = tc::cluster_addr(&qs.recv_diag[buf][0], lane - QC_CS);
+                const uint32_t bar = tc::cluster_addr(&qs.mbar[buf], lane - QC_CS);
+                const float4* d4 = reinterpret_cast<const float4*>(qs.diag);
+#pragma unroll 4
+                for (int u = 0; u < QB / 4; ++u) tc::st_async16(dst + 16u * u, d4[u], bar);
+            }
+            // 3. wait for the 16 records and the diagonal row; S over the CTAs
+            //    (a shuffle tree, fixed order), then beta, tau and the scale (FP64)
+            int ok = 1;
+            if (lane == 0) {
+                ok = rx_failed ? 0 : (tc::mbar_wait_cluster(&qs.mbar[buf], (uint32_t)((c >> 1) & 1)) ? 1 : 0);
+                if (!ok && !rx_failed) atomicExch(err, 8 /* MG_TIMEOUT */);
+                if (ok) tc::mbar_arrive_expect_tx(&qs.mbar[buf], QC_RX_BYTES);  // column c + 2
+            }
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) rx_failed = true;
+            __syncwarp();
+            double xs = lane < QC_CS ? *reinterpret_cast<const double*>(&qs.recv[buf][lane][0]) : 0.0;
+#pragma unroll
+            for (int off = QC_CS / 2; off > 0; off >>= 1) xs += __shfl_xor_sync(0xffffffffu, xs, off);
+            if (lane == 0) {
+                const double alpha = (double)qs.recv_diag[buf][c];
+                if (xs == 0.0) {  // nothing below the diagonal: H = I
+                    qs.tau = 0.0;
+                    qs.scal = 0.0;
+                    qs.beta = alpha;
+                } else {
+                    const double beta = -copysign(sqrt(fma(alpha, alpha, xs)), alpha);
+                    qs.tau = (beta - alpha) / beta;
+                    qs.scal = 1.0 / (alpha - beta);
+                    qs.beta = beta;
+                }
+                if (q == 0) tau[c] = qs.tau;
+            }
+        }
+        __syncthreads();
+        // 4. v . a_jj = a_jj(c) + scale (x . a_jj) from the 16 records (fixed
+        //    order); the update's coefficient -tau (v . a_jj) in fp32
+        {
+            const float tcf = (float)qs.tau, scf0 = (float)qs.scal;
+            for (int jj = c + 1 + tid; jj < w; jj += QP_THREADS) {
+                float d = 0.f;
+#pragma unroll
+                for (int u = 0; u < QC_CS; ++u) d += qs.recv[buf][u][4 + jj];
+                qs.coef[jj] = -tcf * fmaf(scf0, d, qs.recv_diag[buf][jj]);
+            }
+        }
+        __syncthreads();
+        // 5. v below the diagonal, beta on it; a_jj -= (tau (v . a_jj)) v on my rows
+        panel_apply(slab, lds, rpc, w, c, r0, h, (float)qs.scal, (float)qs.beta, qs.coef);
+        __syncthreads();
+    }
+    gram_part(slab, w, lds, rpc, r0, h, gpart + (size_t)q * QB * QB);
+    for (int e = tid; e < w * rpc; e += QP_THREADS) {
+        const int c = e / rpc, i = e - c * rpc, gi = r0 + i;
+        if (gi < h) {
+            const float x = slab[(size_t)c * lds + i];
+            P0[gi + (size_t)c * lda] = x;
+            V[gi + (size_t)c * ldv] = gi < c ? 0.f : gi == c ? 1.f : x;
+        }
+    }
+    cluster.sync();  // no CTA leaves while another may still store into its shared memory
 }
 
 // G (QB x QB, ld QB) = the sum of the panel CTAs' parts, in a fixed order.
@@ -227,8 +425,10 @@ __global__ void qr_gsum_kernel(const float* __restrict__ gpart, int nparts, floa
 }
 
 // T (w x w, upper, fp32, ld QB) of H_0 ... H_{w-1} = I - V T V^T from
-// G = V^T V: T(c,c) = tau_c, T(0:c, c) = -tau_c T(0:c, 0:c) G(0:c, c), summed
-// in FP64.  One CTA of QB threads; T's columns in dynamic shared memory.
+// G = V^T V: T(c,c) = tau_c, T(0:c, c) = -tau_c T(0:c, 0:c) G(0:c, c), in
+// fp32 (T is an fp32 factor; an FP64 recurrence here cost ~1 ms per panel:
+// up to 127 dependent FP64 FMAs per column at ~70 cycles each).  One CTA of
+// QB threads; T's columns in dynamic shared memory.
 __global__ void qr_tfactor_kernel(const float* __restrict__ G, int ldg, const double* __restrict__ tau, int w,
                                   float* __restrict__ T) {
     extern __shared__ float t[];  // [QB][QB + 1]: t[r * (QB + 1) + c]
@@ -237,11 +437,13 @@ __global__ void qr_tfactor_kernel(const float* __restrict__ G, int ldg, const do
     __syncthreads();
     const int r = threadIdx.x;
     for (int c = 0; c < w; ++c) {
-        double sr = 0.0;
-        if (r < c)
-            for (int k = r; k < c; ++k) sr = fma((double)t[r * LD + k], (double)G[k + (size_t)c * ldg], sr);
-        if (r < c) t[r * LD + c] = (float)(-tau[c] * sr);
-        if (r == c) t[c * LD + c] = (float)tau[c];
+        const float tc = (float)tau[c];
+        if (r < c) {
+            float sr = 0.f;
+            for (int k = r; k < c; ++k) sr = fmaf(t[r * LD + k], G[k + (size_t)c * ldg], sr);
+            t[r * LD + c] = -tc * sr;
+        }
+        if (r == c) t[c * LD + c] = tc;
         __syncthreads();
     }
     for (int e = threadIdx.x; e < QB * QB; e += blockDim.x) {
@@ -254,6 +456,7 @@ __global__ void qr_tfactor_kernel(const float* __restrict__ G, int ldg, const do
 // (A32 below the diagonal of columns j0 .. j0+w, v_c = 1) and its T, in FP64:
 // X(j0:, :) -= V (T^T (V^T X(j0:, :))).
 constexpr int QT_CTAS = 64;
+constexpr int QT32_CTAS = 32;  // the fp32 Q^T's dot CTAs (fewer partials to sum)
 
 __global__ void qt_dots_kernel(const float* __restrict__ A, int lda, int m, int j0, int w, const double* __restrict__ X,
                                int ldx, int nrhs, double* __restrict__ part) {
@@ -355,25 +558,42 @@ __global__ void qt32_tw_kernel(const float* __restrict__ part, int nparts, const
     }
 }
 
-__global__ void qt32_update_kernel(const float* __restrict__ A, int lda, int m, int j0, int w,
-                                   const float* __restrict__ y, int nrhs, float* __restrict__ X, int ldx) {
+// A block of 32 rows x 8 column groups: the thread (row, g) sums the
+// reflectors c = g, g + 8, ... of its row, the 8 partial sums then add up in
+// shared memory in a fixed order.
+__global__ void __launch_bounds__(256) qt32_update_kernel(const float* __restrict__ A, int lda, int m, int j0, int w,
+                                                          const float* __restrict__ y, int nrhs,
+                                                          float* __restrict__ X, int ldx) {
     __shared__ float ys[QB * 8];
+    __shared__ float red[8][8][33];  // [group][rhs][row]
     for (int q = threadIdx.x; q < w * 8; q += blockDim.x) ys[q] = y[q];
     __syncthreads();
     const int h = m - j0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < h; i += gridDim.x * blockDim.x) {
-        const int cmax = min(w - 1, i);
-        float acc[8];
+    const int rl = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const int i = blockIdx.x * 32 + rl;
+    float acc[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) acc[j] = j < nrhs ? X[j0 + i + (size_t)j * ldx] : 0.f;
-        for (int c = 0; c <= cmax; ++c) {
+    for (int j = 0; j < 8; ++j) acc[j] = 0.f;
+    if (i < h) {
+        const int cmax = min(w - 1, i);
+        for (int c = g; c <= cmax; c += 8) {
             const float v = c == i ? 1.f : A[j0 + i + (size_t)(j0 + c) * lda];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) acc[j] = fmaf(-v, ys[c * 8 + j], acc[j]);
+            for (int j = 0; j < 8; ++j) acc[j] = fmaf(v, ys[c * 8 + j], acc[j]);
         }
+    }
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-            if (j < nrhs) X[j0 + i + (size_t)j * ldx] = acc[j];
+    for (int j = 0; j < 8; ++j) red[g][j][rl] = acc[j];
+    __syncthreads();
+    if (g == 0 && i < h) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (j >= nrhs) break;
+            float sum = 0.f;
+#pragma unroll
+            for (int gg = 0; gg < 8; ++gg) sum += red[gg][j][rl];
+            X[j0 + i + (size_t)j * ldx] -= sum;
+        }
     }
 }
 
@@ -424,20 +644,67 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
                                           h->max_smem_optin - 4096));
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(qr_tfactor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)(QB * (QB + 1) * sizeof(float))));
+    // the cluster form when a 16-CTA cluster's shared memory holds the panel
+    const size_t qc_static = sizeof(QcShared) + 2048;  // + the other static shared arrays
+    const size_t qc_max_dyn = (size_t)h->max_smem_optin > qc_static ? (size_t)h->max_smem_optin - qc_static : 0;
+    bool qc_ok = false;
+    {
+        cudaLaunchAttribute at[1];
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(QC_CS);
+        cfg.blockDim = dim3(QP_THREADS);
+        cfg.dynamicSmemBytes = qc_max_dyn;
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = QC_CS;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        qc_ok = cudaFuncSetAttribute(qr_panel_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                    cudaSuccess &&
+                cudaFuncSetAttribute(qr_panel_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)qc_max_dyn) == cudaSuccess &&
+                cudaOccupancyMaxActiveClusters(&nclusters, qr_panel_cluster_kernel, &cfg) == cudaSuccess &&
+                nclusters > 0;
+        if (!qc_ok) cudaGetLastError();
+    }
     for (int j0 = 0; j0 < n; j0 += QB) {
         const int w = n - j0 < QB ? n - j0 : QB;
         const int hgt = m - j0;
-        int P = (hgt + 255) / 256;
-        if (P > P0max) P = P0max;
-        int rpc = (hgt + P - 1) / P;
-        while ((size_t)rpc * w * sizeof(float) + QG_TILE_BYTES > (size_t)h->max_smem_optin - 4096 && P < P0max) {
-            ++P;
-            rpc = (hgt + P - 1) / P;
-        }
-        const size_t smem = (size_t)rpc * w * sizeof(float) + QG_TILE_BYTES;
-        if (smem > (size_t)h->max_smem_optin - 4096)
-            return fail(h, MG_ERR_UNSUPPORTED, "sgeqrf_mixed: panel of %d rows does not fit the SMs", hgt);
-        {
+        const int qc_rpc = (hgt + QC_CS - 1) / QC_CS;
+        const size_t qc_smem = (size_t)(qc_rpc | 1) * w * sizeof(float) + QG_TILE_BYTES;
+        int nparts;  // CTAs of the panel (parts of V^T V)
+        if (qc_ok && qc_smem <= qc_max_dyn) {
+            ProfScope prof(h, "qr_panel_f32", 4.0 * hgt * (double)w * w / 2, 8.0 * hgt * (double)w);
+            cudaLaunchAttribute at[1];
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(QC_CS);
+            cfg.blockDim = dim3(QP_THREADS);
+            cfg.dynamicSmemBytes = qc_smem;
+            cfg.stream = st;
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = QC_CS;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            const cudaError_t e = cudaLaunchKernelEx(&cfg, qr_panel_cluster_kernel, A, lda, m, j0, w, qc_rpc, V, hgt,
+                                                     tau + j0, gpart, err);
+            if (e != cudaSuccess) return cuda_fail(h, e, "qr_panel_cluster_kernel launch");
+            h->launches++;
+            nparts = QC_CS;
+        } else {
+            int P = (hgt + 255) / 256;
+            if (P > P0max) P = P0max;
+            int rpc = (hgt + P - 1) / P;
+            while ((size_t)(rpc | 1) * w * sizeof(float) + QG_TILE_BYTES > (size_t)h->max_smem_optin - 4096 && P < P0max) {
+                ++P;
+                rpc = (hgt + P - 1) / P;
+            }
+            const size_t smem = (size_t)(rpc | 1) * w * sizeof(float) + QG_TILE_BYTES;
+            if (smem > (size_t)h->max_smem_optin - 4096)
+                return fail(h, MG_ERR_UNSUPPORTED, "sgeqrf_mixed: panel of %d rows does not fit the SMs", hgt);
             ProfScope prof(h, "qr_panel_f32", 4.0 * hgt * (double)w * w / 2, 8.0 * hgt * (double)w);
             MG_CHECK_CUDA(h, cudaMemsetAsync(bar, 0, sizeof(unsigned), st));
             int lda_ = lda, m_ = m, j0_ = j0, w_ = w, rpc_ = rpc, ldv = hgt;
@@ -448,9 +715,10 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
                                                               dim3(QP_THREADS), args, smem, st);
             if (e != cudaSuccess) return cuda_fail(h, e, "qr_panel_f32_kernel launch");
             h->launches++;
+            nparts = P;
         }
         float* Tb = T + (size_t)(j0 / QB) * QB * QB;
-        qr_gsum_kernel<<<QB * QB / 256, 256, 0, st>>>(gpart, P, G);
+        qr_gsum_kernel<<<QB * QB / 256, 256, 0, st>>>(gpart, nparts, G);
         MG_TRY(post_launch(h, "qr_gsum_kernel"));
         qr_tfactor_kernel<<<1, QB, QB * (QB + 1) * sizeof(float), st>>>(G, QB, tau + j0, w, Tb);
         MG_TRY(post_launch(h, "qr_tfactor_kernel"));
@@ -465,8 +733,6 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
     return MG_OK;
 }
 
-// X := R^{-1} (Q^T B)(0:n) in FP64 for the fp32 factors of sgeqrf_mixed
-// (square use: m = n): Q^T applied panel by panel, then the upper solve.
 // X (fp32, n x nrhs, ld ldx, nrhs <= 8) := Q^T X for the fp32 factors of
 // sgeqrf_mixed (square: m = n), in fp32.
 mg_status_t qr_apply_qt_f32(mg_handle_t h, int n, int nrhs, const float* A, int lda, const float* T, float* X, int ldx,
@@ -484,20 +750,20 @@ mg_status_t qr_apply_qt_f32(mg_handle_t h, int n, int nrhs, const float* A, int 
     float* part = (float*)take((size_t)QT_CTAS * QB * 8 * sizeof(double));
     float* y = (float*)take((size_t)QB * 8 * sizeof(double));
     const cudaStream_t st = h->stream;
-    const int cap = h->num_sms * 8;
     for (int j0 = 0; j0 < n; j0 += QB) {
         const int w = n - j0 < QB ? n - j0 : QB;
-        qt32_dots_kernel<<<QT_CTAS, 256, 0, st>>>(A, lda, n, j0, w, X, ldx, nrhs, part);
+        qt32_dots_kernel<<<QT32_CTAS, 256, 0, st>>>(A, lda, n, j0, w, X, ldx, nrhs, part);
         MG_TRY(post_launch(h, "qt32_dots_kernel"));
-        qt32_tw_kernel<<<1, 256, 0, st>>>(part, QT_CTAS, T + (size_t)(j0 / QB) * QB * QB, w, nrhs, y);
+        qt32_tw_kernel<<<1, 256, 0, st>>>(part, QT32_CTAS, T + (size_t)(j0 / QB) * QB * QB, w, nrhs, y);
         MG_TRY(post_launch(h, "qt32_tw_kernel"));
-        int gu = (n - j0 + 255) / 256;
-        qt32_update_kernel<<<gu < cap ? gu : cap, 256, 0, st>>>(A, lda, n, j0, w, y, nrhs, X, ldx);
+        qt32_update_kernel<<<(n - j0 + 31) / 32, 256, 0, st>>>(A, lda, n, j0, w, y, nrhs, X, ldx);
         MG_TRY(post_launch(h, "qt32_update_kernel"));
     }
     return MG_OK;
 }
 
+// X := R^{-1} (Q^T B)(0:n) in FP64 for the fp32 factors of sgeqrf_mixed
+// (square use: m = n): Q^T applied panel by panel, then the upper solve.
 mg_status_t qr_solve_f32_factors(mg_handle_t h, int n, int nrhs, const float* A, int lda, const float* T,
                                  const double* B, int ldb, double* X, int ldx, void* ws) {
     if (n == 0 || nrhs == 0) return MG_OK;

@@ -71,6 +71,22 @@ __device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity
     return false;
 }
 
+// Address of the same shared-memory object in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t cluster_addr(const void* local, int rank) {
+    uint32_t out;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(out) : "r"(smem_u32(local)), "r"(rank));
+    return out;
+}
+
+// 16-byte store into another CTA's shared memory (cluster address), its bytes
+// completed on that CTA's mbarrier (cluster address).
+__device__ __forceinline__ void st_async16(uint32_t dst, float4 v, uint32_t mbar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];\n" ::"r"(
+                     dst),
+                 "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "r"(mbar)
+                 : "memory");
+}
+
 // 3-D tiled TMA load into shared memory, completion counted on `bar`.
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y,
                                             int z) {
