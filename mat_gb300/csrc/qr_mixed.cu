@@ -282,7 +282,14 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
 // sends only after its threads have finished reading column c's slots).
 constexpr int QC_CS = 16;
 constexpr int QC_REC = 4 + QB;  // floats per record: the double sum of squares, padding, the dots
-constexpr uint32_t QC_RX_BYTES = QC_CS * QC_REC * sizeof(float) + QB * sizeof(float);
+// 16-byte chunks of a column's record (the double, padding, the w - c - 1
+// dots) and of its diagonal row (w - c entries), and the bytes every CTA
+// receives for the column: 16 records and the row.
+__device__ __forceinline__ int qc_rec16(int w, int c) { return (4 + (w - c - 1) + 3) / 4; }
+__device__ __forceinline__ int qc_diag16(int w, int c) { return (w - c + 3) / 4; }
+__device__ __forceinline__ uint32_t qc_rx_bytes(int w, int c) {
+    return (uint32_t)(16 * (QC_CS * qc_rec16(w, c) + qc_diag16(w, c)));
+}
 
 struct QcShared {
     __align__(16) float recv[2][QC_CS][QC_REC];  // every CTA's record of the column, by parity
@@ -316,8 +323,8 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
         tc::mbar_init(&qs.mbar[0], 1);
         tc::mbar_init(&qs.mbar[1], 1);
         tc::fence_barrier_init();
-        tc::mbar_arrive_expect_tx(&qs.mbar[0], QC_RX_BYTES);
-        tc::mbar_arrive_expect_tx(&qs.mbar[1], QC_RX_BYTES);
+        tc::mbar_arrive_expect_tx(&qs.mbar[0], qc_rx_bytes(w, 0));
+        if (w > 1) tc::mbar_arrive_expect_tx(&qs.mbar[1], qc_rx_bytes(w, 1));
     }
     cluster.sync();  // the slab is loaded and every CTA's barriers are armed
     bool rx_failed = false;  // warp 0: a receive wait gave up (error recorded; later waits skipped)
@@ -327,9 +334,9 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
         const bool owner = c >= r0 && c < r1;
         // 1. the record: dots of the unscaled column with the later columns
         //    (fp32, a warp per column), sum of squares (FP64); the diagonal row
-        panel_dots(slab, lds, rpc, w, c, r0, h, sh_part, [&](int jj, float d) { qs.rec[4 + jj] = d; });
+        panel_dots(slab, lds, rpc, w, c, r0, h, sh_part, [&](int jj, float d) { qs.rec[4 + (jj - c - 1)] = d; });
         if (owner)
-            for (int jj = c + tid; jj < w; jj += QP_THREADS) qs.diag[jj] = slab[(size_t)jj * lds + (c - r0)];
+            for (int jj = c + tid; jj < w; jj += QP_THREADS) qs.diag[jj - c] = slab[(size_t)jj * lds + (c - r0)];
         double s = 0.0;
         for (int i = tid; i < rpc; i += QP_THREADS) {
             const int gi = r0 + i;
@@ -342,20 +349,22 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
         if (tid == 0) *reinterpret_cast<double*>(&qs.rec[0]) = s;
         __syncthreads();
         // 2. warp 0 pushes the record into slot [q] of every CTA (lane l -> CTA
-        //    l), and the owner's warp 0 the diagonal row (lane 16 + l -> CTA l)
+        //    l), and the owner's warp 0 the diagonal row (lane 16 + l -> CTA l);
+        //    only the columns still ahead travel: the record's dots and the
+        //    row's entries are packed from column c + 1 and c on
         if (warp == 0) {
             if (lane < QC_CS) {
                 const uint32_t dst = tc::cluster_addr(&qs.recv[buf][q][0], lane);
                 const uint32_t bar = tc::cluster_addr(&qs.mbar[buf], lane);
                 const float4* r4 = reinterpret_cast<const float4*>(qs.rec);
-#pragma unroll 4
-                for (int u = 0; u < QC_REC / 4; ++u) tc::st_async16(dst + 16u * u, r4[u], bar);
+                const int n16 = qc_rec16(w, c);
+                for (int u = 0; u < n16; ++u) tc::st_async16(dst + 16u * u, r4[u], bar);
             } else if (owner) {
                 const uint32_t dst = tc::cluster_addr(&qs.recv_diag[buf][0], lane - QC_CS);
                 const uint32_t bar = tc::cluster_addr(&qs.mbar[buf], lane - QC_CS);
                 const float4* d4 = reinterpret_cast<const float4*>(qs.diag);
-#pragma unroll 4
-                for (int u = 0; u < QB / 4; ++u) tc::st_async16(dst + 16u * u, d4[u], bar);
+                const int n16 = qc_diag16(w, c);
+                for (int u = 0; u < n16; ++u) tc::st_async16(dst + 16u * u, d4[u], bar);
             }
             // 3. wait for the 16 records and the diagonal row; S over the CTAs
             //    (a shuffle tree, fixed order), then beta, tau and the scale (FP64)
@@ -363,7 +372,7 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
             if (lane == 0) {
                 ok = rx_failed ? 0 : (tc::mbar_wait_cluster(&qs.mbar[buf], (uint32_t)((c >> 1) & 1)) ? 1 : 0);
                 if (!ok && !rx_failed) atomicExch(err, 8 /* MG_TIMEOUT */);
-                if (ok) tc::mbar_arrive_expect_tx(&qs.mbar[buf], QC_RX_BYTES);  // column c + 2
+                if (ok && c + 2 < w) tc::mbar_arrive_expect_tx(&qs.mbar[buf], qc_rx_bytes(w, c + 2));
             }
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) rx_failed = true;
@@ -371,19 +380,20 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
             double xs = lane < QC_CS ? *reinterpret_cast<const double*>(&qs.recv[buf][lane][0]) : 0.0;
 #pragma unroll
             for (int off = QC_CS / 2; off > 0; off >>= 1) xs += __shfl_xor_sync(0xffffffffu, xs, off);
-            if (lane == 0) {
-                const double alpha = (double)qs.recv_diag[buf][c];
-                if (xs == 0.0) {  // nothing below the diagonal: H = I
-                    qs.tau = 0.0;
-                    qs.scal = 0.0;
-                    qs.beta = alpha;
-                } else {
-                    const double beta = -copysign(sqrt(fma(alpha, alpha, xs)), alpha);
-                    qs.tau = (beta - alpha) / beta;
-                    qs.scal = 1.0 / (alpha - beta);
-                    qs.beta = beta;
+            if (lane < 2) {  // tau (lane 0) and the scale (lane 1) in one division sequence
+                const double alpha = (double)qs.recv_diag[buf][0];
+                double qv = 0.0, beta = alpha;  // nothing below the diagonal: H = I
+                if (xs != 0.0) {
+                    beta = -copysign(sqrt(fma(alpha, alpha, xs)), alpha);
+                    qv = (lane == 0 ? beta - alpha : 1.0) / (lane == 0 ? beta : alpha - beta);
                 }
-                if (q == 0) tau[c] = qs.tau;
+                if (lane == 0) {
+                    qs.tau = qv;
+                    qs.beta = beta;
+                    if (q == 0) tau[c] = qv;
+                } else {
+                    qs.scal = qv;
+                }
             }
         }
         __syncthreads();
@@ -394,8 +404,8 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
             for (int jj = c + 1 + tid; jj < w; jj += QP_THREADS) {
                 float d = 0.f;
 #pragma unroll
-                for (int u = 0; u < QC_CS; ++u) d += qs.recv[buf][u][4 + jj];
-                qs.coef[jj] = -tcf * fmaf(scf0, d, qs.recv_diag[buf][jj]);
+                for (int u = 0; u < QC_CS; ++u) d += qs.recv[buf][u][4 + (jj - c - 1)];
+                qs.coef[jj] = -tcf * fmaf(scf0, d, qs.recv_diag[buf][jj - c]);
             }
         }
         __syncthreads();
@@ -431,16 +441,22 @@ __global__ void qr_gsum_kernel(const float* __restrict__ gpart, int nparts, floa
 // QB threads; T's columns in dynamic shared memory.
 __global__ void qr_tfactor_kernel(const float* __restrict__ G, int ldg, const double* __restrict__ tau, int w,
                                   float* __restrict__ T) {
-    extern __shared__ float t[];  // [QB][QB + 1]: t[r * (QB + 1) + c]
+    extern __shared__ float t[];  // [QB][QB + 1]: t[r * (QB + 1) + c], then G's columns [QB][QB + 1]
     constexpr int LD = QB + 1;
+    float* const gs = t + QB * LD;  // G(k, c) at gs[c * LD + k]
     for (int e = threadIdx.x; e < QB * LD; e += blockDim.x) t[e] = 0.f;
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+        const int k = e % w, c = e / w;
+        gs[c * LD + k] = G[k + (size_t)c * ldg];
+    }
     __syncthreads();
     const int r = threadIdx.x;
     for (int c = 0; c < w; ++c) {
         const float tc = (float)tau[c];
         if (r < c) {
+            const float* gc = gs + c * LD;
             float sr = 0.f;
-            for (int k = r; k < c; ++k) sr = fmaf(t[r * LD + k], G[k + (size_t)c * ldg], sr);
+            for (int k = r; k < c; ++k) sr = fmaf(t[r * LD + k], gc[k], sr);
             t[r * LD + c] = -tc * sr;
         }
         if (r == c) t[c * LD + c] = tc;
@@ -643,7 +659,7 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(qr_panel_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           h->max_smem_optin - 4096));
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(qr_tfactor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(QB * (QB + 1) * sizeof(float))));
+                                          (int)(2 * QB * (QB + 1) * sizeof(float))));
     // the cluster form when a 16-CTA cluster's shared memory holds the panel
     const size_t qc_static = sizeof(QcShared) + 2048;  // + the other static shared arrays
     const size_t qc_max_dyn = (size_t)h->max_smem_optin > qc_static ? (size_t)h->max_smem_optin - qc_static : 0;
@@ -720,7 +736,7 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
         float* Tb = T + (size_t)(j0 / QB) * QB * QB;
         qr_gsum_kernel<<<QB * QB / 256, 256, 0, st>>>(gpart, nparts, G);
         MG_TRY(post_launch(h, "qr_gsum_kernel"));
-        qr_tfactor_kernel<<<1, QB, QB * (QB + 1) * sizeof(float), st>>>(G, QB, tau + j0, w, Tb);
+        qr_tfactor_kernel<<<1, QB, 2 * QB * (QB + 1) * sizeof(float), st>>>(G, QB, tau + j0, w, Tb);
         MG_TRY(post_launch(h, "qr_tfactor_kernel"));
         const int nt = n - j0 - w;
         if (nt > 0) {  // R2 -= V (T^T (V^T R2))
