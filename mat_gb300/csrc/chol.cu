@@ -22,6 +22,7 @@ namespace {
 
 constexpr int LLT_BS = 48;        // Mat-8.3.1/Mat.h:73-75 (AVX-512)
 constexpr int LLT2_MAX = 2 * LLT_BS;
+constexpr int LLT2_THREADS = 256;  // lanes over rows, 8 warps over the columns of each column step
 
 // Unblocked Cholesky of the k x k block at L (k <= 96), in place, lower part.
 // Column jj: t = 1/sqrt(L(jj,jj)); L(r,jj) *= t for r >= jj; then for
@@ -35,18 +36,17 @@ __global__ void llt2_kernel(T* __restrict__ L, int ldl, int k, int col0, int* __
         s[r + c * LLT2_MAX] = L[r + (size_t)c * ldl];
     }
     __syncthreads();
-    const int r = threadIdx.x;
     for (int jj = 0; jj < k; ++jj) {
         const T d = s[jj + jj * LLT2_MAX];
         const T t = T(1) / sqrt(d);
-        if (r == 0 && !(d > T(0))) atomicCAS(info, 0, col0 + jj + 1);
+        if (threadIdx.x == 0 && !(d > T(0))) atomicCAS(info, 0, col0 + jj + 1);
         __syncthreads();  // every thread has read d before row jj is scaled
-        if (r >= jj && r < k) s[r + jj * LLT2_MAX] = s[r + jj * LLT2_MAX] * t;
+        for (int r = jj + threadIdx.x; r < k; r += blockDim.x) s[r + jj * LLT2_MAX] = s[r + jj * LLT2_MAX] * t;
         __syncthreads();
         // the trailing triangle, every element once (the same single fma per
-        // element as a row-at-a-time loop), spread over the CTA as 32 rows x
-        // 4 column groups instead of one thread per row, whose longest row was
-        // the column step's chain
+        // element as a row-at-a-time loop), lanes over the rows of a column and
+        // the CTA's warps over the columns; not one thread per row, whose
+        // longest row was the column step's chain (one warp alone: 3.4x slower)
         {
             const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5, ncg = blockDim.x >> 5;
             for (int i = jj + 1 + tc; i < k; i += ncg) {
@@ -301,7 +301,7 @@ mg_status_t potrf_impl(mg_handle_t h, int n, T* L, int ldl, int* info_out) {
     const size_t s2 = (size_t)LLT2_MAX * LLT2_MAX * sizeof(T);
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(llt2_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
     if (n <= 2 * LLT_BS) {
-        llt2_kernel<T><<<1, 128, s2, st>>>(L, ldl, n, 0, dinfo);
+        llt2_kernel<T><<<1, LLT2_THREADS, s2, st>>>(L, ldl, n, 0, dinfo);
         MG_TRY(post_launch(h, "llt2_kernel"));
     } else {
         // Look-ahead of one block column: after step j's panel solve, the next
@@ -314,7 +314,7 @@ mg_status_t potrf_impl(mg_handle_t h, int n, T* L, int ldl, int* info_out) {
         auto diag_and_panel = [&](int j) -> mg_status_t {
             const int nb = n - j < LLT_BS ? n - j : LLT_BS;
             T* D = L + j + (size_t)j * ldl;
-            llt2_kernel<T><<<1, 128, s2, h->stream>>>(D, ldl, nb, j, dinfo);
+            llt2_kernel<T><<<1, LLT2_THREADS, s2, h->stream>>>(D, ldl, nb, j, dinfo);
             MG_TRY(post_launch(h, "llt2_kernel"));
             if (j + LLT_BS < n) {
                 const int rows = n - (j + LLT_BS);
@@ -406,7 +406,7 @@ mg_status_t spotrf_mixed(mg_handle_t h, int n, float* L, int ldl, int nterms, vo
         float* D = L + j + (size_t)j * ldl;
         {
             ProfScope prof(h, "potrf_diag_f32", (double)nb * nb * nb / 3.0, 8.0 * nb * nb);
-            llt2_kernel<float><<<1, 128, s2, st>>>(D, ldl, nb, j, dinfo);
+            llt2_kernel<float><<<1, LLT2_THREADS, s2, st>>>(D, ldl, nb, j, dinfo);
             MG_TRY(post_launch(h, "llt2_kernel"));
         }
         if (j + nb >= n) break;

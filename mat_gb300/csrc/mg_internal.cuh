@@ -113,9 +113,10 @@ mg_status_t upper_solve_f32_factors(mg_handle_t h, int n, int nrhs, const float*
 size_t qr_mixed_ws_bytes(int m, int n, int num_sms);
 mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double* tau, float* T, void* ws, int* err);
 // X (fp32, n x nrhs <= 8, ld ldx) := Q^T X in fp32 with the factors of
-// sgeqrf_mixed (m = n); ws as for qr_solve_f32_factors.
+// sgeqrf_mixed (m = n); ws as for qr_solve_f32_factors; err receives
+// MG_TIMEOUT if a grid barrier of the (cooperative) kernel gave up.
 mg_status_t qr_apply_qt_f32(mg_handle_t h, int n, int nrhs, const float* A, int lda, const float* T, float* X, int ldx,
-                            void* ws);
+                            void* ws, int* err);
 mg_status_t qr_solve_f32_factors(mg_handle_t h, int n, int nrhs, const float* A, int lda, const float* T,
                                  const double* B, int ldb, double* X, int ldx, void* ws);
 // X := (P^T L U)^{-1} B in FP64 for the mixed LU's fp32 in-place factors (lu.cu).

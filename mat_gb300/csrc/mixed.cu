@@ -977,8 +977,8 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
             prep_rhs_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(n, nrhs, w.pos, w.R, w.norms + 24,
                                                                                  w.Y);
             MG_TRY(mg::post_launch(h, "prep_rhs_kernel"));
-            MG_TRY(mg::qr_apply_qt_f32(h, n, nrhs, w.A32, n, w.Linv, w.Y, n, w.qws));
             int* terr = w.gemm_err + 1;
+            MG_TRY(mg::qr_apply_qt_f32(h, n, nrhs, w.A32, n, w.Linv, w.Y, n, w.qws, terr));
             switch (nrhs) {
 #define MG_USOLVE(NRV)                                                                         \
     case NRV:                                                                                  \

@@ -472,7 +472,6 @@ __global__ void qr_tfactor_kernel(const float* __restrict__ G, int ldg, const do
 // (A32 below the diagonal of columns j0 .. j0+w, v_c = 1) and its T, in FP64:
 // X(j0:, :) -= V (T^T (V^T X(j0:, :))).
 constexpr int QT_CTAS = 64;
-constexpr int QT32_CTAS = 32;  // the fp32 Q^T's dot CTAs (fewer partials to sum)
 
 __global__ void qt_dots_kernel(const float* __restrict__ A, int lda, int m, int j0, int w, const double* __restrict__ X,
                                int ldx, int nrhs, double* __restrict__ part) {
@@ -524,91 +523,98 @@ __global__ void qt_update_kernel(const float* __restrict__ A, int lda, int m, in
 
 // ---- the same Q^T in fp32 for the refinement's correction (a scaled
 // residual, as the LU's correction is solved in fp32): X (n x nrhs, ld ldx,
-// nrhs <= 8) := (I - V T^T V^T) X for one panel.  Dots: a warp per reflector,
-// lanes over the rows of the CTA's chunk (coalesced), partials per CTA in a
-// fixed order; the update: a thread per row.
-__global__ void qt32_dots_kernel(const float* __restrict__ A, int lda, int m, int j0, int w, const float* __restrict__ X,
-                                 int ldx, int nrhs, float* __restrict__ part) {
-    const int h = m - j0;
-    const int chunk = (h + gridDim.x - 1) / gridDim.x;
-    const int lo = blockIdx.x * chunk, hi = min(h, lo + chunk);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int c = warp; c < w; c += nw) {
-        const float* v = A + j0 + (size_t)(j0 + c) * lda;
-        float acc[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) acc[j] = 0.f;
-        for (int i = max(lo, c) + lane; i < hi; i += 32) {
-            const float vi = i == c ? 1.f : v[i];
-#pragma unroll
-            for (int j = 0; j < 8; ++j)
-                if (j < nrhs) acc[j] = fmaf(vi, X[j0 + i + (size_t)j * ldx], acc[j]);
-        }
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], off);
-        }
-        if (lane == 0)
-#pragma unroll
-            for (int j = 0; j < 8; ++j) part[((size_t)blockIdx.x * QB + c) * 8 + j] = acc[j];
-    }
-}
-
-__global__ void qt32_tw_kernel(const float* __restrict__ part, int nparts, const float* __restrict__ T, int w, int nrhs,
-                               float* __restrict__ y) {
-    __shared__ float wv[QB * 8];
-    for (int q = threadIdx.x; q < w * 8; q += blockDim.x) {
-        float d = 0.f;
-#pragma unroll 8
-        for (int u = 0; u < nparts; ++u) d += part[(size_t)u * QB * 8 + q];
-        wv[q] = d;
-    }
-    __syncthreads();
-    for (int q = threadIdx.x; q < w * 8; q += blockDim.x) {
-        const int c = q / 8, j = q % 8;
-        float d = 0.f;
-        if (j < nrhs)
-            for (int k = 0; k <= c; ++k) d = fmaf(T[k + (size_t)c * QB], wv[k * 8 + j], d);  // (T^T w)_c
-        y[q] = d;
-    }
-}
-
-// A block of 32 rows x 8 column groups: the thread (row, g) sums the
-// reflectors c = g, g + 8, ... of its row, the 8 partial sums then add up in
-// shared memory in a fixed order.
-__global__ void __launch_bounds__(256) qt32_update_kernel(const float* __restrict__ A, int lda, int m, int j0, int w,
-                                                          const float* __restrict__ y, int nrhs,
-                                                          float* __restrict__ X, int ldx) {
+// nrhs <= 8) := (I - V T^T V^T) X panel after panel, in ONE cooperative grid
+// (per panel a launch of three small kernels cost ~70 us, launch-bound).
+// CTA b owns the rows [b * chunk, (b + 1) * chunk) of X for every panel.  Per
+// panel: (1) partial dots V^T X over my rows (a warp per reflector, lanes over
+// rows), (2) after a grid barrier each CTA adds up a share of the entries of
+// W = V^T X over the CTAs' partials (a fixed order), (3) after another, every
+// CTA forms y = T^T W and updates its rows (32 rows x 8 reflector groups per
+// step, the groups' sums added in shared memory).  Partials and W are
+// double-buffered by panel parity.
+__global__ void __launch_bounds__(256) qt32_fused_kernel(const float* __restrict__ A, int lda, int n,
+                                                         const float* __restrict__ T, float* __restrict__ X, int ldx,
+                                                         int nrhs, float* __restrict__ part, float* __restrict__ W,
+                                                         unsigned* bar, int* err) {
     __shared__ float ys[QB * 8];
     __shared__ float red[8][8][33];  // [group][rhs][row]
-    for (int q = threadIdx.x; q < w * 8; q += blockDim.x) ys[q] = y[q];
-    __syncthreads();
-    const int h = m - j0;
-    const int rl = threadIdx.x & 31, g = threadIdx.x >> 5;
-    const int i = blockIdx.x * 32 + rl;
-    float acc[8];
+    const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int chunk = (n + G - 1) / G, lo = b * chunk, hi = min(n, lo + chunk);
+    unsigned target = 0;
+    for (int j0 = 0, pn = 0; j0 < n; j0 += QB, ++pn) {
+        const int w = min(QB, n - j0);
+        float* const pp = part + (size_t)(pn & 1) * G * QB * 8;
+        float* const wp = W + (size_t)(pn & 1) * QB * 8;
+        // 1. this CTA's partial dots over its rows at or below the panel's diagonal
+        for (int c = warp; c < w; c += 8) {
+            const float* v = A + j0 + (size_t)(j0 + c) * lda;  // v_c at row i: v[i - j0]
+            float acc[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[j] = 0.f;
-    if (i < h) {
-        const int cmax = min(w - 1, i);
-        for (int c = g; c <= cmax; c += 8) {
-            const float v = c == i ? 1.f : A[j0 + i + (size_t)(j0 + c) * lda];
+            for (int j = 0; j < 8; ++j) acc[j] = 0.f;
+            for (int i = max(lo, j0 + c) + lane; i < hi; i += 32) {
+                const float vi = i == j0 + c ? 1.f : v[i - j0];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) acc[j] = fmaf(v, ys[c * 8 + j], acc[j]);
+                for (int j = 0; j < 8; ++j)
+                    if (j < nrhs) acc[j] = fmaf(vi, X[i + (size_t)j * ldx], acc[j]);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], off);
+            }
+            if (lane == 0)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) pp[((size_t)b * QB + c) * 8 + j] = acc[j];
         }
-    }
-#pragma unroll
-    for (int j = 0; j < 8; ++j) red[g][j][rl] = acc[j];
-    __syncthreads();
-    if (g == 0 && i < h) {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            if (j >= nrhs) break;
+        target += G;
+        if (!mg::grid_barrier(bar, target, err)) return;
+        // 2. my share of W's entries, the CTAs' partials in a fixed order
+        for (int e = b * blockDim.x + tid; e < w * 8; e += G * blockDim.x) {
             float sum = 0.f;
+#pragma unroll 8
+            for (int u = 0; u < G; ++u) sum += __ldcg(pp + (size_t)u * QB * 8 + e);
+            wp[e] = sum;
+        }
+        target += G;
+        if (!mg::grid_barrier(bar, target, err)) return;
+        // 3. y = T^T W, then X -= V y on my rows
+        const float* Tb = T + (size_t)(j0 / QB) * QB * QB;
+        for (int q = tid; q < w * 8; q += blockDim.x) {
+            const int c = q / 8, j = q % 8;
+            float d = 0.f;
+            if (j < nrhs)
+                for (int k = 0; k <= c; ++k) d = fmaf(Tb[k + (size_t)c * QB], __ldcg(wp + k * 8 + j), d);
+            ys[q] = d;
+        }
+        __syncthreads();
+        const int rl = tid & 31, g = tid >> 5;
+        for (int i0 = max(lo, j0); i0 < hi; i0 += 32) {
+            const int i = i0 + rl;
+            float acc[8];
 #pragma unroll
-            for (int gg = 0; gg < 8; ++gg) sum += red[gg][j][rl];
-            X[j0 + i + (size_t)j * ldx] -= sum;
+            for (int j = 0; j < 8; ++j) acc[j] = 0.f;
+            if (i < hi) {
+                const int cmax = min(w - 1, i - j0);
+                for (int c = g; c <= cmax; c += 8) {
+                    const float v = c == i - j0 ? 1.f : A[i + (size_t)(j0 + c) * lda];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) acc[j] = fmaf(v, ys[c * 8 + j], acc[j]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) red[g][j][rl] = acc[j];
+            __syncthreads();
+            if (g == 0 && i < hi) {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    if (j >= nrhs) break;
+                    float sum = 0.f;
+#pragma unroll
+                    for (int gg = 0; gg < 8; ++gg) sum += red[gg][j][rl];
+                    X[i + (size_t)j * ldx] -= sum;
+                }
+            }
+            __syncthreads();
         }
     }
 }
@@ -752,7 +758,7 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
 // X (fp32, n x nrhs, ld ldx, nrhs <= 8) := Q^T X for the fp32 factors of
 // sgeqrf_mixed (square: m = n), in fp32.
 mg_status_t qr_apply_qt_f32(mg_handle_t h, int n, int nrhs, const float* A, int lda, const float* T, float* X, int ldx,
-                            void* ws) {
+                            void* ws, int* err) {
     if (n == 0 || nrhs == 0) return MG_OK;
     if (nrhs > 8) return fail(h, MG_ERR_ARG, "qr_apply_qt_f32: at most 8 right-hand sides");
     char* p = (char*)ws;
@@ -761,20 +767,23 @@ mg_status_t qr_apply_qt_f32(mg_handle_t h, int n, int nrhs, const float* A, int 
     take((size_t)QB * n * sizeof(float));
     take((size_t)QB * n * sizeof(float));
     take((size_t)QB * QB * sizeof(float));
-    take((size_t)h->num_sms * QB * QB * sizeof(float));
+    float* part = (float*)take((size_t)h->num_sms * QB * QB * sizeof(float));  // the V^T V parts' area
     take((size_t)2 * h->num_sms * (QB + 2) * sizeof(double));
-    float* part = (float*)take((size_t)QT_CTAS * QB * 8 * sizeof(double));
-    float* y = (float*)take((size_t)QB * 8 * sizeof(double));
+    float* W = (float*)take((size_t)QT_CTAS * QB * 8 * sizeof(double));
+    take((size_t)QB * 8 * sizeof(double));
+    unsigned* bar = (unsigned*)p;  // the workspace tail's barrier word
     const cudaStream_t st = h->stream;
-    for (int j0 = 0; j0 < n; j0 += QB) {
-        const int w = n - j0 < QB ? n - j0 : QB;
-        qt32_dots_kernel<<<QT32_CTAS, 256, 0, st>>>(A, lda, n, j0, w, X, ldx, nrhs, part);
-        MG_TRY(post_launch(h, "qt32_dots_kernel"));
-        qt32_tw_kernel<<<1, 256, 0, st>>>(part, QT32_CTAS, T + (size_t)(j0 / QB) * QB * QB, w, nrhs, y);
-        MG_TRY(post_launch(h, "qt32_tw_kernel"));
-        qt32_update_kernel<<<(n - j0 + 31) / 32, 256, 0, st>>>(A, lda, n, j0, w, y, nrhs, X, ldx);
-        MG_TRY(post_launch(h, "qt32_update_kernel"));
-    }
+    const int G = h->num_sms;        // one CTA per SM (2 x G x QB x 8 partials fit the V^T V parts' area)
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qt32_fused_kernel, 256, 0) != cudaSuccess || per_sm < 1)
+        return fail(h, MG_ERR_UNSUPPORTED, "qr_apply_qt_f32: the cooperative grid does not fit");
+    MG_CHECK_CUDA(h, cudaMemsetAsync(bar, 0, sizeof(unsigned), st));
+    int n_ = n, lda_ = lda, ldx_ = ldx, nrhs_ = nrhs;
+    void* args[] = {(void*)&A, &lda_, &n_, (void*)&T, (void*)&X, &ldx_, &nrhs_, (void*)&part, (void*)&W, (void*)&bar,
+                    (void*)&err};
+    const cudaError_t e = cudaLaunchCooperativeKernel((const void*)qt32_fused_kernel, dim3(G), dim3(256), args, 0, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "qt32_fused_kernel launch");
+    h->launches++;
     return MG_OK;
 }
 
