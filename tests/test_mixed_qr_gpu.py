@@ -33,7 +33,7 @@ def rebuild(Af, tau):
     return X, R, V
 
 
-@pytest.mark.parametrize("m,n", [(300, 200), (1000, 1000), (4096, 1024), (3000, 257)])
+@pytest.mark.parametrize("m,n", [(300, 200), (1000, 1000), (4096, 1024), (3000, 257), (9000, 300)])
 def test_sgeqrf_reconstructs_A(handle, m, n):
     A = colmajor(m, n)
     handle.fill_normal(A, 7)
@@ -71,7 +71,7 @@ def backward_error(a, x, b):
     return (np.abs(r).max(0) / (np.abs(a).sum(1).max() * np.abs(x).max(0) + np.abs(b).max(0))).max()
 
 
-@pytest.mark.parametrize("n,nrhs", [(300, 1), (1024, 4), (2500, 3)])
+@pytest.mark.parametrize("n,nrhs", [(300, 1), (1024, 4), (2500, 3), (7000, 2)])
 def test_mixed_qr_solve(handle, n, nrhs):
     A = colmajor(n, n)
     handle.gen_svd_matrix(A, 3, nrefl=64, sigma_min=1e-6)
