@@ -252,7 +252,8 @@ mg_status_t mg_bf16x_check_error(mg_handle_t h, int* device_err_flag);
  * X = A^{-1} B (n x nrhs, nrhs <= 8) to FP64 normwise backward error:
  * fp32 LU with partial pivoting (fp32 panels, split-BF16 tensor-core
  * trailing updates, fp32 accumulation), then FP64 iterative refinement
- * (r = b - A x in fp64, fp32 correction solves, fp64 update) until every
+ * (r = b - A x to FP64 accuracy or better (opts.residual), fp32 correction
+ * solves, fp64 update) until every
  * column satisfies ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= tol.
  * If refinement stalls (the backward error not halving twice in a row, or
  * max_iter reached), GMRES-IR takes over: refinement steps whose correction
@@ -276,8 +277,25 @@ typedef struct mg_ir_opts {
                       FP64 fallback (default 1; n up to the dataflow solves' size) */
     int panel;     /* FP32 panel pivoting: 0 = default, 1 = partial pivoting,
                       2 = tournament pivoting (one pivot agreement per 16 columns) */
-    int reserved;
+    int residual;  /* arithmetic of r = b - A x: 0 = exact fixed-point integer
+                      (default: every entry of A and x rounded once to 2^-63 of
+                      its row's / column's largest, products and sums exact on
+                      the integer pipe; an A or x with an infinity or NaN takes
+                      FP64), 1 = FP64 FMA */
 } mg_ir_opts;
+
+/* R = B - A X (A n x n, X and B n x nrhs, nrhs <= 8; column-major), the
+ * residual of the mixed solves on its own.  mode 0: exact fixed-point
+ * integer arithmetic: every A(i,k) rounded once to a 63-bit integer in units
+ * of 2^-62 of row i's largest power of two, every X(k,j) likewise per column,
+ * the products and sums exact (int64 on the integer multiply-add pipe), the
+ * sum rounded once to double, then R = B - that in FP64; its error is about
+ * 2^-60 max|A(i,:)| max|X(:,j)| per entry, below FP64's accumulation error.
+ * An A or X holding an infinity or NaN takes mode 1.  mode 1: FP64 FMA
+ * (partial sums over column chunks of 2048, added in a fixed order).
+ * Synchronises (mode 0). */
+mg_status_t mg_dresidual(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* X,
+                         int ldx, const double* B, int ldb, double* R, int ldr, int mode);
 
 typedef struct mg_ir_report {
     int iterations;        /* refinement steps taken (plain and GMRES-IR outer steps) */

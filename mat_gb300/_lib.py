@@ -29,7 +29,7 @@ pf64 = C.POINTER(C.c_double)
 
 class IrOpts(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("nterms", C.c_int), ("fallback", C.c_int),
-                ("gmres", C.c_int), ("panel", C.c_int), ("reserved", C.c_int)]
+                ("gmres", C.c_int), ("panel", C.c_int), ("residual", C.c_int)]
 
 
 class IrReport(C.Structure):
@@ -76,6 +76,7 @@ SIGNATURES: dict[str, tuple] = {
     "mg_sgemm_bf16x": (i32, [vp, i32, i32, i32, i32, f32, vp, i32, vp, i32, f32, vp, i32]),
     "mg_sgemm_bf16x_ex": (i32, [vp, i32, i32, i32, i32, i32, f32, vp, i32, vp, i32, f32, vp, i32]),
     "mg_bf16x_check_error": (i32, [vp, pi32]),
+    "mg_dresidual": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, vp, i32, i32]),
     "mg_dsgesv_ir": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, C.POINTER(IrOpts), C.POINTER(IrReport)]),
     "mg_dsposv_ir": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, C.POINTER(IrOpts), C.POINTER(IrReport)]),
     "mg_dsqrsv_ir": (i32, [vp, i32, i32, vp, i32, vp, i32, vp, i32, C.POINTER(IrOpts), C.POINTER(IrReport)]),

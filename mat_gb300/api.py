@@ -209,16 +209,26 @@ class Handle:
             self.check(st, "mg_sgetrf")
         return pos, info.value
 
+    def dresidual(self, A, X, B, R=None, mode=0):
+        """R = B - A X: mode 0 the exact fixed-point integer residual, 1 FP64 FMA."""
+        n, nrhs = B.shape
+        if R is None:
+            R = colmajor(n, nrhs, device=B.device)
+        self.check(self.lib.mg_dresidual(self.h, n, nrhs, _ptr(A), ld_of(A), _ptr(X), ld_of(X), _ptr(B), ld_of(B),
+                                         _ptr(R), ld_of(R), int(mode)), "mg_dresidual")
+        return R
+
     def dsgesv_ir(self, A, B, X=None, tol=1e-14, max_iter=30, nterms=3, fallback=True, gmres=True, panel=0,
-                  spd=False, qr=False):
+                  residual=0, spd=False, qr=False):
         """Mixed LU (fp32 + split-BF16) + FP64 refinement, GMRES-IR and the FP64
         fallback when refinement stalls; spd=True: the fp32 Cholesky form
-        (mg_dsposv_ir). Returns (X, report dict with the status)."""
+        (mg_dsposv_ir). residual: 0 = the exact fixed-point integer residual,
+        1 = FP64 FMA. Returns (X, report dict with the status)."""
         n = A.shape[0]
         nrhs = B.shape[1]
         if X is None:
             X = colmajor(n, nrhs, device=B.device)
-        o = IrOpts(tol, max_iter, nterms, int(fallback), int(gmres), int(panel), 0)
+        o = IrOpts(tol, max_iter, nterms, int(fallback), int(gmres), int(panel), int(residual))
         r = IrReport()
         name = "mg_dsqrsv_ir" if qr else "mg_dsposv_ir" if spd else "mg_dsgesv_ir"
         st = getattr(self.lib, name)(self.h, n, nrhs, _ptr(A), ld_of(A), _ptr(B), ld_of(B), _ptr(X), ld_of(X),

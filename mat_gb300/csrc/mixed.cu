@@ -67,12 +67,21 @@ __device__ __forceinline__ float d2f_rn(double d) {
     return (float)d;
 }
 
+// The biased exponent field of a double (0 for zeros and subnormals, 0x7ff
+// for infinities and NaNs).
+__device__ __forceinline__ int exp_field(double d) { return (__double2hiint(d) >> 20) & 0x7ff; }
+
+// Also: rexp[i] = the largest exponent field of row i (atomicMax over the
+// column chunks; rexp zeroed by the caller), and *nonfinite = 1 if A holds
+// an infinity or a NaN (the scale of the integer residual below).
 __global__ void __launch_bounds__(256) d2s_absrow_kernel(const double* __restrict__ A, int lda, int n,
                                                          float* __restrict__ S, int lds, double* __restrict__ partial,
-                                                         double* __restrict__ amax) {
+                                                         double* __restrict__ amax, int* __restrict__ rexp,
+                                                         int* __restrict__ nonfinite) {
     const int i0 = blockIdx.x * D2S_ROWS + 4 * threadIdx.x;
     const int k0 = blockIdx.y * D2S_KCHUNK, k1 = min(n, k0 + D2S_KCHUNK);
     float s[4] = {0.f, 0.f, 0.f, 0.f};
+    int em[4] = {0, 0, 0, 0};
     float mx = 0.f;
     if (i0 < n) {  // n is a multiple of 4 here
         int k = k0;
@@ -93,18 +102,28 @@ __global__ void __launch_bounds__(256) d2s_absrow_kernel(const double* __restric
                 s[2] += fabsf(f.z);
                 s[3] += fabsf(f.w);
                 mx = fmaxf(mx, fmaxf(fmaxf(fabsf(f.x), fabsf(f.y)), fmaxf(fabsf(f.z), fabsf(f.w))));
+                em[0] = max(em[0], exp_field(a[u][0].x));
+                em[1] = max(em[1], exp_field(a[u][0].y));
+                em[2] = max(em[2], exp_field(a[u][1].x));
+                em[3] = max(em[3], exp_field(a[u][1].y));
             }
         }
         for (; k < k1; ++k)
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
-                const float f = d2f_rn(A[i0 + r + (size_t)k * lda]);
+                const double d = A[i0 + r + (size_t)k * lda];
+                const float f = d2f_rn(d);
                 S[i0 + r + (size_t)k * lds] = f;
                 s[r] += fabsf(f);
                 mx = fmaxf(mx, fabsf(f));
+                em[r] = max(em[r], exp_field(d));
             }
 #pragma unroll
-        for (int r = 0; r < 4; ++r) partial[(size_t)blockIdx.y * n + i0 + r] = (double)s[r];
+        for (int r = 0; r < 4; ++r) {
+            partial[(size_t)blockIdx.y * n + i0 + r] = (double)s[r];
+            atomicMax(rexp + i0 + r, em[r]);
+            if (em[r] == 0x7ff) atomicExch(nonfinite, 1);
+        }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
@@ -113,18 +132,24 @@ __global__ void __launch_bounds__(256) d2s_absrow_kernel(const double* __restric
 
 // The same for any lda / lds (one row per thread, scalar accesses).
 __global__ void d2s_absrow_scalar_kernel(const double* __restrict__ A, int lda, int n, float* __restrict__ S, int lds,
-                                         double* __restrict__ partial, double* __restrict__ amax) {
+                                         double* __restrict__ partial, double* __restrict__ amax,
+                                         int* __restrict__ rexp, int* __restrict__ nonfinite) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int k0 = blockIdx.y * D2S_KCHUNK, k1 = min(n, k0 + D2S_KCHUNK);
     float s = 0.f, mx = 0.f;
+    int em = 0;
     if (i < n) {
         for (int k = k0; k < k1; ++k) {
-            const float f = d2f_rn(A[i + (size_t)k * lda]);
+            const double d = A[i + (size_t)k * lda];
+            const float f = d2f_rn(d);
             S[i + (size_t)k * lds] = f;
             s += fabsf(f);
             mx = fmaxf(mx, fabsf(f));
+            em = max(em, exp_field(d));
         }
         partial[(size_t)blockIdx.y * n + i] = (double)s;
+        atomicMax(rexp + i, em);
+        if (em == 0x7ff) atomicExch(nonfinite, 1);
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
@@ -191,17 +216,230 @@ __global__ void __launch_bounds__(RES_ROWS) residual_partial_kernel(const double
 // r = b - sum_c partial[c]; rnorm[j] = max |r(:,j)|, xnorm[j] = max |x(:,j)|
 __global__ void residual_reduce_kernel(const double* __restrict__ partial, int nchunks, int n, int nrhs,
                                        const double* __restrict__ B, int ldb, const double* __restrict__ X, int ldx,
-                                       double* __restrict__ R, double* __restrict__ norms) {
+                                       double* __restrict__ R, int ldr, double* __restrict__ norms) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     for (int j = 0; j < nrhs; ++j) {
         double s = 0.0;
         for (int c = 0; c < nchunks; ++c) s += partial[((size_t)c * nrhs + j) * n + i];
         const double r = B[i + (size_t)j * ldb] - s;
-        R[i + (size_t)j * n] = r;
+        R[i + (size_t)j * ldr] = r;
         atomic_max_nonneg(norms + j, fabs(r));
         atomic_max_nonneg(norms + MAX_RHS + j, fabs(X[i + (size_t)j * ldx]));
     }
+}
+
+// ---------------------------------------------------------------- integer residual
+// A X (and r = b - A X) in exact fixed-point integer arithmetic on the
+// integer multiply-add pipe, which on this part issues about 62 lane
+// operations per clock per SM against 2 for FP64 FMA (measured: the FP64
+// kernel above is bound by that pipe).
+//
+// Every A(i,k) becomes a 63-bit integer in units of 2^(ea_i - 1084), ea_i the
+// largest exponent field of row i (the row's largest element maps below
+// 2^62; the others are rounded to the unit, half away from zero), and every
+// X(k,j) likewise with ex_j, the largest exponent field of column j.  Each
+// integer is split into three 21-bit digits (magnitude digits with the
+// value's sign), so that a digit product is below 2^42 and up to 2^20 of
+// them sum exactly in an int64.  The products are kept by weight class
+// c = p + q of their digits (2^(21c)): classes 4 .. 1 (8 products per
+// element and right-hand side); class 0 (the two lowest digits, below
+// 2^-82 of the leading products) is dropped.  Summed exactly over k,
+//   (A X)(i,j) = 2^(ea_i + ex_j - 2147) (acc4 2^63 + acc3 2^42 + acc2 2^21 + acc1),
+// combined once per entry in 128-bit integers and rounded to double.  The
+// error is the rounding of the entries to their units (2^-63 of the row's
+// and the column's largest element), not a rounding per operation.
+constexpr int RI_ROWS = 256;    // rows per CTA (a thread per row)
+constexpr int RI_KSTAGE = 256;  // columns of X staged (as digits) per step
+constexpr int RI_CLASSES = 4;
+constexpr int RI_BATCH = 8;     // loads of A in flight per thread
+
+// The three digits of d in units of 2^(e - 1084), e >= d's exponent field.
+__device__ __forceinline__ void fx_digits(double d, int e, int& d0, int& d1, int& d2) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const int eb = (int)((hi >> 20) & 0x7ffu);
+    const unsigned mh = (hi & 0xfffffu) | (eb ? 0x100000u : 0u);  // the 53-bit significand: mh:lo
+    const int t = 9 + (eb ? eb : 1) - e;                          // its shift to the unit, <= 9
+    unsigned ah, al;
+    if (t >= 0) {
+        ah = __funnelshift_l(lo, mh, t);
+        al = lo << t;
+    } else if (t > -54) {  // right shift by s, adding half a unit first
+        const int s = -t;
+        const unsigned addl = s <= 32 ? 1u << (s - 1) : 0u, addh = s > 32 ? 1u << (s - 33) : 0u;
+        unsigned rl, rh;
+        asm("add.cc.u32 %0, %2, %3;\n\taddc.u32 %1, %4, %5;" : "=r"(rl), "=r"(rh) : "r"(lo), "r"(addl), "r"(mh),
+            "r"(addh));
+        if (s < 32) {
+            al = __funnelshift_r(rl, rh, s);
+            ah = rh >> s;
+        } else {
+            al = rh >> (s - 32);
+            ah = 0u;
+        }
+    } else {
+        ah = al = 0u;
+    }
+    const int sm = (int)hi >> 31;  // 0 or -1: the sign
+    const int u0 = (int)(al & 0x1fffffu), u1 = (int)(__funnelshift_r(al, ah, 21) & 0x1fffffu), u2 = (int)(ah >> 10);
+    d0 = (u0 ^ sm) - sm;
+    d1 = (u1 ^ sm) - sm;
+    d2 = (u2 ^ sm) - sm;
+}
+
+// cexp[j] = the largest exponent field of column j of V (n x nrhs, ld ldv;
+// cexp zeroed by the caller); *nonfinite = 1 if V holds an infinity or NaN.
+__global__ void colexp_kernel(const double* __restrict__ V, int ldv, int n, int nrhs, int* __restrict__ cexp,
+                              int* __restrict__ nonfinite) {
+    const int j = blockIdx.y;
+    int em = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        em = max(em, exp_field(V[i + (size_t)j * ldv]));
+    em = __reduce_max_sync(0xffffffffu, em);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(cexp + j, em);
+        if (em == 0x7ff) atomicExch(nonfinite, 1);
+    }
+}
+
+// rexp[i] = the largest exponent field of row i of A (n x n, ld lda; rexp
+// zeroed by the caller), a thread per row over a chunk of 256 columns;
+// *nonfinite = 1 if A holds an infinity or NaN.
+__global__ void rowexp_kernel(const double* __restrict__ A, int lda, int n, int* __restrict__ rexp,
+                              int* __restrict__ nonfinite) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int k0 = blockIdx.y * 256, k1 = min(n, k0 + 256);
+    int em = 0;
+    for (int k = k0; k < k1; ++k) em = max(em, exp_field(A[i + (size_t)k * lda]));
+    atomicMax(rexp + i, em);
+    if (em == 0x7ff) atomicExch(nonfinite, 1);
+}
+
+// part[((kc * 4 + c) * NR + j) * n + i] = class c + 1 of sum over the column
+// chunk kc (kchunk columns) of A(i,k) V(k,j), exact int64.
+template <int NR>
+__global__ void __launch_bounds__(RI_ROWS, NR <= 4 ? 2 : 1)
+    residual_int_kernel(const double* __restrict__ A, int lda, int n, const double* __restrict__ V, int ldv,
+                        int kchunk, const int* __restrict__ rexp, const int* __restrict__ cexp,
+                        long long* __restrict__ part) {
+    __shared__ __align__(16) int xd[RI_KSTAGE * 3 * NR];  // [k][digit][j]
+    const int tid = threadIdx.x, i = blockIdx.x * RI_ROWS + tid;
+    const int k0 = blockIdx.y * kchunk, k1 = min(n, k0 + kchunk);
+    const int ea = i < n ? rexp[i] : 0;
+    long long acc[NR][RI_CLASSES];
+#pragma unroll
+    for (int j = 0; j < NR; ++j)
+#pragma unroll
+        for (int c = 0; c < RI_CLASSES; ++c) acc[j][c] = 0;
+    for (int kb = k0; kb < k1; kb += RI_KSTAGE) {
+        const int kn = min(RI_KSTAGE, k1 - kb);
+        __syncthreads();
+        for (int q = tid; q < kn * NR; q += RI_ROWS) {
+            const int j = q / kn, kk = q - j * kn;
+            int e0, e1, e2;
+            fx_digits(V[kb + kk + (size_t)j * ldv], cexp[j], e0, e1, e2);
+            int* const x = xd + kk * 3 * NR + j;
+            x[0] = e0;
+            x[NR] = e1;
+            x[2 * NR] = e2;
+        }
+        __syncthreads();
+        if (i < n) {
+            const double* ap = A + i + (size_t)kb * lda;
+            auto mac = [&](double a, int k) {
+                int d0, d1, d2;
+                fx_digits(a, ea, d0, d1, d2);
+                const int* const x = xd + k * 3 * NR;
+#pragma unroll
+                for (int j = 0; j < NR; ++j) {
+                    const int e0 = x[j], e1 = x[NR + j], e2 = x[2 * NR + j];
+                    acc[j][3] += (long long)d2 * e2;
+                    acc[j][2] += (long long)d2 * e1;
+                    acc[j][2] += (long long)d1 * e2;
+                    acc[j][1] += (long long)d2 * e0;
+                    acc[j][1] += (long long)d1 * e1;
+                    acc[j][1] += (long long)d0 * e2;
+                    acc[j][0] += (long long)d1 * e0;
+                    acc[j][0] += (long long)d0 * e1;
+                }
+            };
+            // RI_BATCH loads in flight before the (branching) digit extraction
+            int k = 0;
+            for (; k + RI_BATCH <= kn; k += RI_BATCH) {
+                double av[RI_BATCH];
+#pragma unroll
+                for (int u = 0; u < RI_BATCH; ++u) av[u] = __ldcs(ap + (size_t)(k + u) * lda);
+#pragma unroll
+                for (int u = 0; u < RI_BATCH; ++u) mac(av[u], k + u);
+            }
+            for (; k < kn; ++k) mac(__ldcs(ap + (size_t)k * lda), k);
+        }
+    }
+    if (i < n)
+#pragma unroll
+        for (int j = 0; j < NR; ++j)
+#pragma unroll
+            for (int c = 0; c < RI_CLASSES; ++c)
+                part[(((size_t)blockIdx.y * RI_CLASSES + c) * NR + j) * n + i] = acc[j][c];
+}
+
+// (A V)(i,j) from the int partials of residual_int_kernel (nrhs = its NR).
+__device__ __forceinline__ double int_av(const long long* __restrict__ part, int nchunks, int n, int nrhs, int i, int j,
+                                         int ea, int ex) {
+    long long a[RI_CLASSES] = {0, 0, 0, 0};
+    for (int c = 0; c < nchunks; ++c)
+#pragma unroll
+        for (int q = 0; q < RI_CLASSES; ++q) a[q] += part[(((size_t)c * RI_CLASSES + q) * nrhs + j) * n + i];
+    const __int128 t = ((__int128)a[3] << 63) + ((__int128)a[2] << 42) + ((__int128)a[1] << 21) + (__int128)a[0];
+    const bool neg = t < 0;
+    const unsigned __int128 u = neg ? (unsigned __int128)(-t) : (unsigned __int128)t;
+    const double v = fma((double)(unsigned long long)(u >> 64), 0x1p64, (double)(unsigned long long)u);
+    return ldexp(neg ? -v : v, ea + ex - 2147);
+}
+
+// r = b - A x from the int partials; rnorm / xnorm as residual_reduce_kernel.
+// A non-finite x (flag set by colexp_kernel) gives r = NaN.
+__global__ void residual_int_reduce_kernel(const long long* __restrict__ part, int nchunks, int n, int nrhs,
+                                           const int* __restrict__ rexp, const int* __restrict__ cexp,
+                                           const int* __restrict__ xnonfinite, const double* __restrict__ B, int ldb,
+                                           const double* __restrict__ X, int ldx, double* __restrict__ R, int ldr,
+                                           double* __restrict__ norms) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bool bad = *xnonfinite != 0;
+    for (int j = 0; j < nrhs; ++j) {
+        const double v = int_av(part, nchunks, n, nrhs, i, j, rexp[i], cexp[j]);
+        const double r = bad ? __longlong_as_double(0x7ff8000000000000LL) : B[i + (size_t)j * ldb] - v;
+        R[i + (size_t)j * ldr] = r;
+        atomic_max_nonneg(norms + j, fabs(r));
+        atomic_max_nonneg(norms + MAX_RHS + j, fabs(X[i + (size_t)j * ldx]));
+    }
+}
+
+// Y = A V from the int partials (GMRES-IR's products).
+__global__ void matvec_int_reduce_kernel(const long long* __restrict__ part, int nchunks, int n, int nrhs,
+                                         const int* __restrict__ rexp, const int* __restrict__ cexp,
+                                         const int* __restrict__ vnonfinite, double* __restrict__ Y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bool bad = *vnonfinite != 0;
+    for (int j = 0; j < nrhs; ++j)
+        Y[i + (size_t)j * n] =
+            bad ? __longlong_as_double(0x7ff8000000000000LL) : int_av(part, nchunks, n, nrhs, i, j, rexp[i], cexp[j]);
+}
+
+// Column chunking of the integer residual: the row blocks x column chunks
+// fill whole waves of two resident CTAs per SM (chunks a multiple of 64).
+int resint_kchunk(int n, int num_sms) {
+    const int rb = (n + RI_ROWS - 1) / RI_ROWS;
+    const int slots = 2 * num_sms;
+    const int base = (n + 2047) / 2048;  // chunks of 2048 columns
+    const int waves = (rb * base + slots - 1) / slots;
+    int kch = (waves * slots) / rb;
+    if (kch < 1) kch = 1;
+    const int chunk = (n + kch - 1) / kch;
+    return (chunk + 63) / 64 * 64;
 }
 
 // y[i][j] = float(r[pos[i]][j] / s_j)
@@ -668,7 +906,8 @@ struct IrWs {
     float* Linv;
     float* Uinv;
     double* R;
-    double* partial;
+    double* partial;  // also the integer residual's partials (long long)
+    int* rexp;        // the integer residual's row exponents (n)
     double* norms;  // [0..8) rnorm, [8..16) xnorm, [16] anorm, [24..32) scale
     float* Y;
     float* Z;
@@ -699,7 +938,10 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w, bool qr = f
     const size_t oUi = take((size_t)nblk * IR_BLOCK * IR_BLOCK * sizeof(float));
     const size_t oR = take((size_t)n * nrhs * sizeof(double));
     const int kd2s = (n + D2S_KCHUNK - 1) / D2S_KCHUNK;
-    const size_t oPa = take((size_t)std::max(kch * std::max(nrhs, 1), kd2s) * n * sizeof(double));
+    const int rich = (n + resint_kchunk(n, h->num_sms) - 1) / resint_kchunk(n, h->num_sms);
+    const size_t oPa = take((size_t)std::max({kch * std::max(nrhs, 1), kd2s, RI_CLASSES * rich * std::max(nrhs, 1)}) *
+                            n * sizeof(double));
+    const size_t oRe = take((size_t)n * sizeof(int));
     const size_t oN = take(64 * sizeof(double));
     const size_t oF = take(2 * (size_t)nblk * sizeof(unsigned));
     const size_t oY = take((size_t)n * nrhs * sizeof(float));
@@ -722,6 +964,7 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w, bool qr = f
         w->Uinv = (float*)(b + oUi);
         w->R = (double*)(b + oR);
         w->partial = (double*)(b + oPa);
+        w->rexp = (int*)(b + oRe);
         w->norms = (double*)(b + oN);
         w->flags = (unsigned*)(b + oF);
         w->Y = (float*)(b + oY);
@@ -790,15 +1033,18 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
     setup.emplace(h, "ir_setup", 0.0, 12.0 * n * (double)n);
     MG_CHECK_CUDA(h, cudaMemsetAsync(w.gemm_err, 0, 64, st));
     MG_CHECK_CUDA(h, cudaMemsetAsync(w.norms, 0, 64 * sizeof(double), st));
-    // fp32 copy and the row sums of |A| (one pass), then ||A||_inf
+    MG_CHECK_CUDA(h, cudaMemsetAsync(w.rexp, 0, (size_t)n * sizeof(int), st));
+    // fp32 copy and the row sums of |A| (one pass, also the row exponents of
+    // the integer residual and A's non-finite flag, error word 4), then ||A||_inf
     const int kd2s = (n + D2S_KCHUNK - 1) / D2S_KCHUNK;
     if ((lda & 3) == 0 && (n & 3) == 0 && ((reinterpret_cast<uintptr_t>(A) & 15) == 0)) {
         d2s_absrow_kernel<<<dim3((n + D2S_ROWS - 1) / D2S_ROWS, kd2s), 256, 0, st>>>(A, lda, n, w.A32, n, w.partial,
-                                                                                   w.norms + 17);
+                                                                                   w.norms + 17, w.rexp,
+                                                                                   w.gemm_err + 4);
         MG_TRY(mg::post_launch(h, "d2s_absrow_kernel"));
     } else {
         d2s_absrow_scalar_kernel<<<dim3((n + 255) / 256, kd2s), 256, 0, st>>>(A, lda, n, w.A32, n, w.partial,
-                                                                            w.norms + 17);
+                                                                            w.norms + 17, w.rexp, w.gemm_err + 4);
         MG_TRY(mg::post_launch(h, "d2s_absrow_scalar_kernel"));
     }
     absrow_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kd2s, n, w.norms + 16);
@@ -894,8 +1140,33 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
 
     // refinement --------------------------------------------------------------
     const dim3 rgrid((n + RES_ROWS - 1) / RES_ROWS, kch);
-    // partial sums of A V (V n x nrhs, ld ldv) in w.partial, fp64 FMA
+    // the integer residual unless asked for FP64 or A holds an infinity or NaN
+    // (error word 4, read back with the first residual, before any product)
+    bool int_res = o.residual == 0;
+    const int ri_chunk = resint_kchunk(n, h->num_sms);
+    const int ri_kch = (n + ri_chunk - 1) / ri_chunk;
+    int* const vexp = w.gemm_err + 8;      // the integer residual's column exponents (8)
+    int* const vbad = w.gemm_err + 5;      // ... and V's non-finite flag
+    long long* const ipart = reinterpret_cast<long long*>(w.partial);
+    // partial sums of A V (V n x nrhs, ld ldv) in w.partial: fp64 FMA, or the
+    // integer residual's classes
     auto launch_av = [&](const double* V, int ldv) -> mg_status_t {
+        if (int_res) {
+            MG_CHECK_CUDA(h, cudaMemsetAsync(vbad, 0, 11 * sizeof(int), st));
+            colexp_kernel<<<dim3(std::min(64, (n + 255) / 256), nrhs), 256, 0, st>>>(V, ldv, n, nrhs, vexp, vbad);
+            MG_TRY(mg::post_launch(h, "colexp_kernel"));
+            const dim3 g((n + RI_ROWS - 1) / RI_ROWS, ri_kch);
+            switch (nrhs) {
+#define MG_RES(NRV)                                                                                               \
+    case NRV:                                                                                                     \
+        residual_int_kernel<NRV><<<g, RI_ROWS, 0, st>>>(A, lda, n, V, ldv, ri_chunk, w.rexp, vexp, ipart); break;
+                MG_RES(1) MG_RES(2) MG_RES(3) MG_RES(4) MG_RES(5) MG_RES(6) MG_RES(7)
+                default: residual_int_kernel<8><<<g, RI_ROWS, 0, st>>>(A, lda, n, V, ldv, ri_chunk, w.rexp, vexp, ipart);
+                break;
+#undef MG_RES
+            }
+            return mg::post_launch(h, "residual_int_kernel");
+        }
         switch (nrhs) {
 #define MG_RES(NRV) \
     case NRV: residual_partial_kernel<NRV><<<rgrid, RES_ROWS, 0, st>>>(A, lda, n, V, ldv, w.partial); break;
@@ -905,27 +1176,43 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
         }
         return mg::post_launch(h, "residual_partial_kernel");
     };
+    // Y = A V from the partials of launch_av
+    auto reduce_av = [&](double* Y) -> mg_status_t {
+        if (int_res) {
+            matvec_int_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(ipart, ri_kch, n, nrhs, w.rexp, vexp, vbad, Y);
+            return mg::post_launch(h, "matvec_int_reduce_kernel");
+        }
+        matvec_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kch, n, nrhs, Y);
+        return mg::post_launch(h, "matvec_reduce_kernel");
+    };
     double bnorm[MAX_RHS] = {0};
     int nres = 0;  // residuals evaluated (plain and GMRES-IR steps): the history index
-    // r = b - A x in fp64 (x_zero: x = 0, r = b) and the max-over-columns
-    // normwise backward error; also checks the device error words
+    // r = b - A x (x_zero: x = 0, r = b) and the max-over-columns normwise
+    // backward error; also checks the device error words
     auto residual = [&](bool x_zero, double* eta_out) -> mg_status_t {
         MG_CHECK_CUDA(h, cudaMemsetAsync(w.norms, 0, 16 * sizeof(double), st));
         {
             mg::ProfScope pr(h, "ir_residual", x_zero ? 0.0 : 2.0 * n * (double)n * nrhs,
                              x_zero ? 0.0 : 8.0 * n * (double)n);
             if (!x_zero) MG_TRY(launch_av(X, ldx));
-            residual_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, x_zero ? 0 : kch, n, nrhs, B, ldb, X,
-                                                                   ldx, w.R, w.norms);
-            MG_TRY(mg::post_launch(h, "residual_reduce_kernel"));
+            if (!x_zero && int_res) {
+                residual_int_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(ipart, ri_kch, n, nrhs, w.rexp, vexp, vbad,
+                                                                           B, ldb, X, ldx, w.R, n, w.norms);
+                MG_TRY(mg::post_launch(h, "residual_int_reduce_kernel"));
+            } else {
+                residual_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, x_zero ? 0 : kch, n, nrhs, B, ldb,
+                                                                       X, ldx, w.R, n, w.norms);
+                MG_TRY(mg::post_launch(h, "residual_reduce_kernel"));
+            }
         }
         MG_CHECK_CUDA(h, cudaMemcpyAsync(hn, w.norms, 32 * sizeof(double), cudaMemcpyDeviceToHost, st));
-        int* herr = (int*)(hn + 48);  // device error words: split GEMM, triangular solves, QR panel
-        MG_CHECK_CUDA(h, cudaMemcpyAsync(herr, w.gemm_err, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        int* herr = (int*)(hn + 48);  // device error words: split GEMM, triangular solves, QR panel, -, A non-finite
+        MG_CHECK_CUDA(h, cudaMemcpyAsync(herr, w.gemm_err, 5 * sizeof(int), cudaMemcpyDeviceToHost, st));
         MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
         if (herr[0] || herr[1] || herr[2])
             return mg::fail(h, MG_TIMEOUT, "mixed solve: a bounded device wait timed out (%s)",
                             herr[0] ? "split GEMM" : herr[1] ? "triangular solve" : "QR panel");
+        if (herr[4]) int_res = false;  // A holds an infinity or NaN: FP64 residuals propagate it
         const double anorm = hn[16];
         double eta = 0.0;
         for (int j = 0; j < nrhs; ++j) {
@@ -1090,8 +1377,7 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
                 const double* Vk = w.gV + (size_t)k * nrhs * n;
                 // w = M^{-1} A V_k (A V_k summed into w.R, free until the next residual)
                 MG_TRY(launch_av(Vk, n));
-                matvec_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.partial, kch, n, nrhs, w.R);
-                MG_TRY(mg::post_launch(h, "matvec_reduce_kernel"));
+                MG_TRY(reduce_av(w.R));
                 MG_TRY(precond(w.R, w.gW));
                 // classical Gram-Schmidt, twice
                 for (int pass = 0; pass < 2; ++pass) {
@@ -1165,6 +1451,76 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
     }
     if (rep) *rep = r;
     return result;
+}
+
+// R = B - A X on its own (the residual of the mixed solves): mode 0 the exact
+// fixed-point integer form (FP64 when A or X holds an infinity or NaN),
+// mode 1 FP64 FMA.  Synchronises (to read A's non-finite flag).
+extern "C" mg_status_t mg_dresidual(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* X, int ldx,
+                                    const double* B, int ldb, double* R, int ldr, int mode) {
+    if (!h) return MG_ERR_ARG;
+    if (n < 0 || nrhs < 0 || nrhs > MAX_RHS || lda < std::max(1, n) || ldx < std::max(1, n) ||
+        ldb < std::max(1, n) || ldr < std::max(1, n) || (mode != 0 && mode != 1))
+        return mg::fail(h, MG_ERR_ARG, "mg_dresidual: bad sizes or mode (nrhs <= %d)", MAX_RHS);
+    if (n == 0 || nrhs == 0) return MG_OK;
+    if (!A || !X || !B || !R) return mg::fail(h, MG_ERR_ARG, "mg_dresidual: null pointer");
+    const int kch = (n + RES_KCHUNK - 1) / RES_KCHUNK;
+    const int ri_chunk = resint_kchunk(n, h->num_sms);
+    const int ri_kch = (n + ri_chunk - 1) / ri_chunk;
+    const size_t opart = 0;
+    const size_t orexp = mg::align_up((size_t)std::max(kch, RI_CLASSES * ri_kch) * nrhs * n * sizeof(double), 1024);
+    const size_t oflag = mg::align_up(orexp + (size_t)n * sizeof(int), 1024);
+    const size_t onorm = oflag + 1024;
+    MG_TRY(mg::ensure_ws(h, onorm + 16 * sizeof(double)));
+    MG_TRY(mg::ensure_hws(h, 64));
+    char* b = (char*)h->ws;
+    double* partial = (double*)(b + opart);
+    long long* ipart = (long long*)(b + opart);
+    int* rexp = (int*)(b + orexp);
+    int* flags = (int*)(b + oflag);  // [0] A non-finite, [1] X non-finite, [8..16) column exponents
+    double* norms = (double*)(b + onorm);
+    const cudaStream_t st = h->stream;
+    bool int_res = mode == 0;
+    if (int_res) {
+        MG_CHECK_CUDA(h, cudaMemsetAsync(rexp, 0, (size_t)n * sizeof(int), st));
+        MG_CHECK_CUDA(h, cudaMemsetAsync(flags, 0, 16 * sizeof(int), st));
+        rowexp_kernel<<<dim3((n + 255) / 256, (n + 255) / 256), 256, 0, st>>>(A, lda, n, rexp, flags);
+        MG_TRY(mg::post_launch(h, "rowexp_kernel"));
+        int* hf = (int*)h->hws;
+        MG_CHECK_CUDA(h, cudaMemcpyAsync(hf, flags, sizeof(int), cudaMemcpyDeviceToHost, st));
+        MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
+        int_res = hf[0] == 0;
+    }
+    MG_CHECK_CUDA(h, cudaMemsetAsync(norms, 0, 16 * sizeof(double), st));
+    if (int_res) {
+        colexp_kernel<<<dim3(std::min(64, (n + 255) / 256), nrhs), 256, 0, st>>>(X, ldx, n, nrhs, flags + 8, flags + 1);
+        MG_TRY(mg::post_launch(h, "colexp_kernel"));
+        const dim3 g((n + RI_ROWS - 1) / RI_ROWS, ri_kch);
+        switch (nrhs) {
+#define MG_RES(NRV)                                                                                              \
+    case NRV:                                                                                                    \
+        residual_int_kernel<NRV><<<g, RI_ROWS, 0, st>>>(A, lda, n, X, ldx, ri_chunk, rexp, flags + 8, ipart); break;
+            MG_RES(1) MG_RES(2) MG_RES(3) MG_RES(4) MG_RES(5) MG_RES(6) MG_RES(7)
+            default: residual_int_kernel<8><<<g, RI_ROWS, 0, st>>>(A, lda, n, X, ldx, ri_chunk, rexp, flags + 8, ipart);
+            break;
+#undef MG_RES
+        }
+        MG_TRY(mg::post_launch(h, "residual_int_kernel"));
+        residual_int_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(ipart, ri_kch, n, nrhs, rexp, flags + 8,
+                                                                   flags + 1, B, ldb, X, ldx, R, ldr, norms);
+        return mg::post_launch(h, "residual_int_reduce_kernel");
+    }
+    const dim3 rgrid((n + RES_ROWS - 1) / RES_ROWS, kch);
+    switch (nrhs) {
+#define MG_RES(NRV) \
+    case NRV: residual_partial_kernel<NRV><<<rgrid, RES_ROWS, 0, st>>>(A, lda, n, X, ldx, partial); break;
+        MG_RES(1) MG_RES(2) MG_RES(3) MG_RES(4) MG_RES(5) MG_RES(6) MG_RES(7)
+        default: residual_partial_kernel<8><<<rgrid, RES_ROWS, 0, st>>>(A, lda, n, X, ldx, partial); break;
+#undef MG_RES
+    }
+    MG_TRY(mg::post_launch(h, "residual_partial_kernel"));
+    residual_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(partial, kch, n, nrhs, B, ldb, X, ldx, R, ldr, norms);
+    return mg::post_launch(h, "residual_reduce_kernel");
 }
 
 extern "C" mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double* A, int lda, const double* B,
