@@ -316,11 +316,11 @@ mg_status_t mg_dsgesv_ir(mg_handle_t h, int n, int nrhs, const double* A, int ld
 /* Mixed-precision solve for symmetric positive definite A (no mixed
  * precision in Mat; the FP64 counterpart is Mat's LLT, Mat-8.3.1/LU/__LLT.h:
  * 94-150, with the Cholesky solve): fp32 Cholesky of A's lower triangle in
- * blocks of 96 columns (fp32 diagonal blocks and block-column solves, the
+ * blocks of 64 columns (fp32 diagonal blocks and block-column solves, the
  * trailing updates C -= L21 L21^T on the split-BF16 tensor cores, fp32
  * accumulation), its factor rewritten as the LU of the same matrix
  * (L D^-1)(D L^T), D = diag(L), then the refinement of mg_dsgesv_ir:
- * FP64 residuals with all of A (both triangles: pass the full symmetric
+ * residuals (opts.residual) with all of A (both triangles: pass the full symmetric
  * matrix), GMRES-IR, FP64 fallback (mg_dgesv).  If the fp32 Cholesky breaks
  * down (a non-positive pivot, possible for nearly singular A) the solve
  * goes straight to the FP64 fallback (MG_FALLBACK_USED, path 2), or returns

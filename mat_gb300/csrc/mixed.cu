@@ -20,6 +20,7 @@
 #include <chrono>
 #include <cmath>
 #include <optional>
+#include <type_traits>
 #include <vector>
 
 #include "grid_sync.cuh"
@@ -249,18 +250,15 @@ __global__ void residual_reduce_kernel(const double* __restrict__ partial, int n
 // combined once per entry in 128-bit integers and rounded to double.  The
 // error is the rounding of the entries to their units (2^-63 of the row's
 // and the column's largest element), not a rounding per operation.
-constexpr int RI_ROWS = 256;    // rows per CTA (a thread per row)
-constexpr int RI_KSTAGE = 256;  // columns of X staged (as digits) per step
-constexpr int RI_CLASSES = 4;
-constexpr int RI_BATCH = 8;     // loads of A in flight per thread
+constexpr int RI_CLASSES = 5;
 
-// The three digits of d in units of 2^(e - 1084), e >= d's exponent field.
-__device__ __forceinline__ void fx_digits(double d, int e, int& d0, int& d1, int& d2) {
+// The integer of d in units of 2^(e - 1084), e >= d's exponent field: its
+// magnitude (ah:al, below 2^62) and sign mask sm (0 or -1).
+__device__ __forceinline__ void fx_int(double d, int e, unsigned& ah, unsigned& al, int& sm) {
     const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
     const int eb = (int)((hi >> 20) & 0x7ffu);
     const unsigned mh = (hi & 0xfffffu) | (eb ? 0x100000u : 0u);  // the 53-bit significand: mh:lo
     const int t = 9 + (eb ? eb : 1) - e;                          // its shift to the unit, <= 9
-    unsigned ah, al;
     if (t >= 0) {
         ah = __funnelshift_l(lo, mh, t);
         al = lo << t;
@@ -280,11 +278,31 @@ __device__ __forceinline__ void fx_digits(double d, int e, int& d0, int& d1, int
     } else {
         ah = al = 0u;
     }
-    const int sm = (int)hi >> 31;  // 0 or -1: the sign
+    sm = (int)hi >> 31;
+}
+
+// The three 21-bit digits (magnitude digits carrying the sign) of the
+// magnitude ah:al (below 2^62) with sign mask sm.  32-bit operations only:
+// on this part 64-bit integer shifts issue to the FP64 pipe.
+__device__ __forceinline__ void mag_digits(unsigned ah, unsigned al, int sm, int& d0, int& d1, int& d2) {
     const int u0 = (int)(al & 0x1fffffu), u1 = (int)(__funnelshift_r(al, ah, 21) & 0x1fffffu), u2 = (int)(ah >> 10);
     d0 = (u0 ^ sm) - sm;
     d1 = (u1 ^ sm) - sm;
     d2 = (u2 ^ sm) - sm;
+}
+
+// The digits of d in units of 2^(e - 1084).
+__device__ __forceinline__ void fx_digits(double d, int e, int& d0, int& d1, int& d2) {
+    unsigned ah, al;
+    int sm;
+    fx_int(d, e, ah, al, sm);
+    mag_digits(ah, al, sm, d0, d1, d2);
+}
+
+// The stored form of A's integers: sign and magnitude (the magnitude in bits
+// 0..61, the sign in bit 63), packed and unpacked by register halves.
+__device__ __forceinline__ long long fx_pack(unsigned ah, unsigned al, int sm) {
+    return (long long)(((unsigned long long)(ah | ((unsigned)sm & 0x80000000u)) << 32) | al);
 }
 
 // cexp[j] = the largest exponent field of column j of V (n x nrhs, ld ldv;
@@ -316,82 +334,192 @@ __global__ void rowexp_kernel(const double* __restrict__ A, int lda, int n, int*
     if (em == 0x7ff) atomicExch(nonfinite, 1);
 }
 
-// part[((kc * 4 + c) * NR + j) * n + i] = class c + 1 of sum over the column
-// chunk kc (kchunk columns) of A(i,k) V(k,j), exact int64.
+// xdig[(k * nrhs + j) * 4 + p] = digit p of V(k,j) in units of 2^(cexp[j] -
+// 1084) (p < 3; the fourth int pads the entry to 16 bytes).
+__global__ void xdigits_kernel(const double* __restrict__ V, int ldv, int n, int nrhs, const int* __restrict__ cexp,
+                               int* __restrict__ xdig) {
+    const int total = n * nrhs;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const int k = e / nrhs, j = e - k * nrhs;
+        int d0, d1, d2;
+        fx_digits(V[k + (size_t)j * ldv], cexp[j], d0, d1, d2);
+        reinterpret_cast<int4*>(xdig)[e] = make_int4(d0, d1, d2, 0);
+    }
+}
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)),
+                 "l"(gmem));
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)),
+                 "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+constexpr int RI_ROWS = 256;  // rows per CTA (a thread per row)
+constexpr int RI_KT = 8;      // columns per pipeline stage
+constexpr int RI_NST = 4;     // stages
 template <int NR>
-__global__ void __launch_bounds__(RI_ROWS, NR <= 4 ? 2 : 1)
-    residual_int_kernel(const double* __restrict__ A, int lda, int n, const double* __restrict__ V, int ldv,
-                        int kchunk, const int* __restrict__ rexp, const int* __restrict__ cexp,
+constexpr size_t ri_stage_bytes() {
+    return (size_t)RI_KT * RI_ROWS * 8 + (size_t)RI_KT * NR * 16;
+}
+
+// The two 31-bit digits (carrying the sign) of the magnitude ah:al (below
+// 2^62) with sign mask sm.
+__device__ __forceinline__ void mag_digits31(unsigned ah, unsigned al, int sm, int& a1, int& a0) {
+    const int u0 = (int)(al & 0x7fffffffu), u1 = (int)((ah << 1) | (al >> 31));
+    a0 = (u0 ^ sm) - sm;
+    a1 = (u1 ^ sm) - sm;
+}
+
+// acc += a * b, 32 x 32 -> 64-bit signed (one wide integer multiply-add;
+// written in C++ so that the compiler schedules it: as inline PTX the
+// accumulators spilled).
+__device__ __forceinline__ void imad_wide(long long& acc, int a, int b) { acc += (long long)a * b; }
+
+// part[((kc * RI_CLASSES + c) * n + i) * NR + j] = class c of sum over the
+// column chunk kc (kchunk <= 1024 columns, a multiple of RI_KT) of
+// A(i,k) V(k,j), exact int64.  A's integer in two 31-bit digits a1 a0, V's
+// in three 21-bit digits x2 x1 x0; the five kept products each have a
+// weight of their own (a1 x2: 2^73, a1 x1: 2^52, a0 x2: 2^42, a1 x0: 2^31,
+// a0 x1: 2^21; a0 x0, below 2^-72 of the leading one, is dropped), so every
+// accumulator takes one product per entry, and a product below 2^52 lets
+// 1024 of them sum exactly.  A thread per row with every right-hand side
+// (the row's digits made once; a thread per right-hand side or pair of them
+// repeated that and ran 1.3-1.8x slower).  SRC: A from its FP64 entries (0),
+// the same and its integers stored to Ai (1, for the residuals to come), or
+// from those integers (2: no exponent arithmetic per entry, ld ldi).  Tiles
+// of RI_KT columns x RI_ROWS rows of A (8-byte cp.async, a thread per row)
+// and the matching digits of V (xdig) stream through RI_NST shared-memory
+// stages, so that the loads in flight are bounded by shared memory, not
+// registers.
+template <int NR, int SRC>
+__global__ void __launch_bounds__(RI_ROWS, NR <= 4 ? 3 : 1)
+    residual_int_kernel(const double* __restrict__ A, int lda, long long* __restrict__ Ai, int ldi, int n,
+                        const int* __restrict__ xdig, int kchunk, const int* __restrict__ rexp,
                         long long* __restrict__ part) {
-    __shared__ __align__(16) int xd[RI_KSTAGE * 3 * NR];  // [k][digit][j]
+    extern __shared__ __align__(16) unsigned char ri_smem[];
+    constexpr size_t SB = ri_stage_bytes<NR>();
+    constexpr int XCH = RI_KT * NR;  // 16-byte digit entries of a stage
     const int tid = threadIdx.x, i = blockIdx.x * RI_ROWS + tid;
     const int k0 = blockIdx.y * kchunk, k1 = min(n, k0 + kchunk);
-    const int ea = i < n ? rexp[i] : 0;
+    const int nt = (k1 - k0 + RI_KT - 1) / RI_KT;
+    const bool row_ok = i < n;
+    const int ea = row_ok ? rexp[i] : 0;
+    const char* const src = SRC == 2 ? (const char*)(Ai + i) : (const char*)(A + i);
+    const size_t ldb = (SRC == 2 ? (size_t)ldi : (size_t)lda) * 8;  // bytes between columns
+    auto issue = [&](int t) {  // tile t of the chunk into stage t % RI_NST
+        if (t < nt) {
+            unsigned char* const st = ri_smem + (size_t)(t % RI_NST) * SB;
+            const int kt = k0 + t * RI_KT, kn = min(RI_KT, k1 - kt);
+            if (row_ok)
+                for (int k = 0; k < kn; ++k) cp_async8(st + ((size_t)k * RI_ROWS + tid) * 8, src + (size_t)(kt + k) * ldb);
+            if (tid < XCH && tid < kn * NR)
+                cp_async16(st + (size_t)RI_KT * RI_ROWS * 8 + (size_t)tid * 16, xdig + ((size_t)kt * NR + tid) * 4);
+        }
+        cp_async_commit();
+    };
     long long acc[NR][RI_CLASSES];
 #pragma unroll
     for (int j = 0; j < NR; ++j)
 #pragma unroll
         for (int c = 0; c < RI_CLASSES; ++c) acc[j][c] = 0;
-    for (int kb = k0; kb < k1; kb += RI_KSTAGE) {
-        const int kn = min(RI_KSTAGE, k1 - kb);
-        __syncthreads();
-        for (int q = tid; q < kn * NR; q += RI_ROWS) {
-            const int j = q / kn, kk = q - j * kn;
-            int e0, e1, e2;
-            fx_digits(V[kb + kk + (size_t)j * ldv], cexp[j], e0, e1, e2);
-            int* const x = xd + kk * 3 * NR + j;
-            x[0] = e0;
-            x[NR] = e1;
-            x[2 * NR] = e2;
-        }
-        __syncthreads();
-        if (i < n) {
-            const double* ap = A + i + (size_t)kb * lda;
-            auto mac = [&](double a, int k) {
-                int d0, d1, d2;
-                fx_digits(a, ea, d0, d1, d2);
-                const int* const x = xd + k * 3 * NR;
+#pragma unroll
+    for (int t = 0; t < RI_NST - 1; ++t) issue(t);
+    for (int t = 0; t < nt; ++t) {
+        cp_async_wait<RI_NST - 2>();
+        __syncthreads();  // tile t in every thread's view; stage (t - 1) % RI_NST free
+        issue(t + RI_NST - 1);
+        const unsigned char* const st = ri_smem + (size_t)(t % RI_NST) * SB;
+        const int4* const xs = reinterpret_cast<const int4*>(st + (size_t)RI_KT * RI_ROWS * 8);
+        const int kt = k0 + t * RI_KT, kn = min(RI_KT, k1 - kt);
+        if (row_ok) {
+            auto mac = [&](int k) {
+                const unsigned long long raw = reinterpret_cast<const unsigned long long*>(st)[k * RI_ROWS + tid];
+                unsigned ah, al;
+                int sm;
+                if constexpr (SRC == 2) {
+                    al = (unsigned)raw;
+                    const unsigned hw = (unsigned)(raw >> 32);
+                    ah = hw & 0x7fffffffu;
+                    sm = (int)hw >> 31;
+                } else {
+                    fx_int(__longlong_as_double((long long)raw), ea, ah, al, sm);
+                    if constexpr (SRC == 1) __stcs(Ai + i + (size_t)(kt + k) * ldi, fx_pack(ah, al, sm));
+                }
+                int a1, a0;
+                mag_digits31(ah, al, sm, a1, a0);
 #pragma unroll
                 for (int j = 0; j < NR; ++j) {
-                    const int e0 = x[j], e1 = x[NR + j], e2 = x[2 * NR + j];
-                    acc[j][3] += (long long)d2 * e2;
-                    acc[j][2] += (long long)d2 * e1;
-                    acc[j][2] += (long long)d1 * e2;
-                    acc[j][1] += (long long)d2 * e0;
-                    acc[j][1] += (long long)d1 * e1;
-                    acc[j][1] += (long long)d0 * e2;
-                    acc[j][0] += (long long)d1 * e0;
-                    acc[j][0] += (long long)d0 * e1;
+                    const int4 x = xs[k * NR + j];  // x.x = x0, x.y = x1, x.z = x2
+                    imad_wide(acc[j][4], a1, x.z);
+                    imad_wide(acc[j][3], a1, x.y);
+                    imad_wide(acc[j][2], a0, x.z);
+                    imad_wide(acc[j][1], a1, x.x);
+                    imad_wide(acc[j][0], a0, x.y);
                 }
             };
-            // RI_BATCH loads in flight before the (branching) digit extraction
-            int k = 0;
-            for (; k + RI_BATCH <= kn; k += RI_BATCH) {
-                double av[RI_BATCH];
+            if (kn == RI_KT) {
 #pragma unroll
-                for (int u = 0; u < RI_BATCH; ++u) av[u] = __ldcs(ap + (size_t)(k + u) * lda);
-#pragma unroll
-                for (int u = 0; u < RI_BATCH; ++u) mac(av[u], k + u);
+                for (int k = 0; k < RI_KT; ++k) mac(k);
+            } else {
+                for (int k = 0; k < kn; ++k) mac(k);
             }
-            for (; k < kn; ++k) mac(__ldcs(ap + (size_t)k * lda), k);
         }
     }
-    if (i < n)
+    cp_async_wait<0>();
+    if (row_ok)
 #pragma unroll
-        for (int j = 0; j < NR; ++j)
+        for (int c = 0; c < RI_CLASSES; ++c)
 #pragma unroll
-            for (int c = 0; c < RI_CLASSES; ++c)
-                part[(((size_t)blockIdx.y * RI_CLASSES + c) * NR + j) * n + i] = acc[j][c];
+            for (int j = 0; j < NR; ++j)
+                part[(((size_t)blockIdx.y * RI_CLASSES + c) * n + i) * NR + j] = acc[j][c];
 }
 
-// (A V)(i,j) from the int partials of residual_int_kernel (nrhs = its NR).
+// Launch residual_int_kernel<nrhs, src> (its shared memory set once per variant).
+template <int NR, int S>
+cudaError_t launch_resint_t(dim3 g, cudaStream_t st, const double* A, int lda, long long* Ai, int ldi, int n,
+                            const int* xdig, int kchunk, const int* rexp, long long* part) {
+    static bool attr_set = false;  // benign race: every thread sets the same value
+    const size_t smem = RI_NST * ri_stage_bytes<NR>();
+    if (!attr_set) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(residual_int_kernel<NR, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    residual_int_kernel<NR, S><<<g, RI_ROWS, smem, st>>>(A, lda, Ai, ldi, n, xdig, kchunk, rexp, part);
+    return cudaGetLastError();
+}
+cudaError_t launch_resint(int src, int nrhs, dim3 g, cudaStream_t st, const double* A, int lda, long long* Ai, int ldi,
+                          int n, const int* xdig, int kchunk, const int* rexp, long long* part) {
+#define MG_RI(NRV, S) launch_resint_t<NRV, S>(g, st, A, lda, Ai, ldi, n, xdig, kchunk, rexp, part)
+#define MG_RI3(NRV) \
+    case NRV: return src == 2 ? MG_RI(NRV, 2) : src == 1 ? MG_RI(NRV, 1) : MG_RI(NRV, 0);
+    switch (nrhs) {
+        MG_RI3(1) MG_RI3(2) MG_RI3(3) MG_RI3(4) MG_RI3(5) MG_RI3(6) MG_RI3(7)
+        default: return src == 2 ? MG_RI(8, 2) : src == 1 ? MG_RI(8, 1) : MG_RI(8, 0);
+    }
+#undef MG_RI3
+#undef MG_RI
+}
+
+// (A V)(i,j) from the int partials of residual_int_kernel (nrhs = its NR):
+// the classes summed over the chunks in 128-bit integers, combined as
+// T = s4 2^52 + s3 2^31 + s2 2^21 + s1 2^10 + s0 (the weights over 2^21),
+// rounded to double, scaled by 2^21 and the two units.
 __device__ __forceinline__ double int_av(const long long* __restrict__ part, int nchunks, int n, int nrhs, int i, int j,
                                          int ea, int ex) {
-    long long a[RI_CLASSES] = {0, 0, 0, 0};
+    __int128 a[RI_CLASSES] = {0, 0, 0, 0, 0};
     for (int c = 0; c < nchunks; ++c)
 #pragma unroll
-        for (int q = 0; q < RI_CLASSES; ++q) a[q] += part[(((size_t)c * RI_CLASSES + q) * nrhs + j) * n + i];
-    const __int128 t = ((__int128)a[3] << 63) + ((__int128)a[2] << 42) + ((__int128)a[1] << 21) + (__int128)a[0];
+        for (int q = 0; q < RI_CLASSES; ++q) a[q] += part[(((size_t)c * RI_CLASSES + q) * n + i) * nrhs + j];
+    const __int128 t = (a[4] << 52) + (a[3] << 31) + (a[2] << 21) + (a[1] << 10) + a[0];
     const bool neg = t < 0;
     const unsigned __int128 u = neg ? (unsigned __int128)(-t) : (unsigned __int128)t;
     const double v = fma((double)(unsigned long long)(u >> 64), 0x1p64, (double)(unsigned long long)u);
@@ -431,15 +559,20 @@ __global__ void matvec_int_reduce_kernel(const long long* __restrict__ part, int
 
 // Column chunking of the integer residual: the row blocks x column chunks
 // fill whole waves of two resident CTAs per SM (chunks a multiple of 64).
+// Bytes of the digit array of V (n x nrhs entries of 16 bytes, padded).
+size_t xdig_bytes(int n, int nrhs) { return ((size_t)n * nrhs + (size_t)RI_KT * MAX_RHS) * 16; }
+
+// Column chunks of the integer residual: at most 1024 columns (the exact
+// int64 bound), a multiple of 64, whole waves of three CTAs per SM where the
+// chunk count allows.
 int resint_kchunk(int n, int num_sms) {
     const int rb = (n + RI_ROWS - 1) / RI_ROWS;
-    const int slots = 2 * num_sms;
-    const int base = (n + 2047) / 2048;  // chunks of 2048 columns
-    const int waves = (rb * base + slots - 1) / slots;
-    int kch = (waves * slots) / rb;
-    if (kch < 1) kch = 1;
+    const int slots = 3 * num_sms;
+    int kch = std::max(1, (n + 1023) / 1024);
+    const int waves = (rb * kch + slots - 1) / slots;
+    kch = std::max(kch, (waves * slots) / rb);
     const int chunk = (n + kch - 1) / kch;
-    return (chunk + 63) / 64 * 64;
+    return std::min(1024, (chunk + 63) / 64 * 64);
 }
 
 // y[i][j] = float(r[pos[i]][j] / s_j)
@@ -908,6 +1041,8 @@ struct IrWs {
     double* R;
     double* partial;  // also the integer residual's partials (long long)
     int* rexp;        // the integer residual's row exponents (n)
+    long long* Ai;    // A's integers for the integer residual (n x n, ld n), written by the first
+    int* xdig;        // the digits of the integer residual's right-hand factor (n x 3 x nrhs + padding)
     double* norms;  // [0..8) rnorm, [8..16) xnorm, [16] anorm, [24..32) scale
     float* Y;
     float* Z;
@@ -918,7 +1053,7 @@ struct IrWs {
     void* qws;      // mixed QR: panel reflectors, products, partial sums (QR mode only)
 };
 
-size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w, bool qr = false) {
+size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w, bool qr, bool ai) {
     size_t off = 0;
     auto take = [&](size_t bytes) {
         const size_t o = off;
@@ -942,6 +1077,8 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w, bool qr = f
     const size_t oPa = take((size_t)std::max({kch * std::max(nrhs, 1), kd2s, RI_CLASSES * rich * std::max(nrhs, 1)}) *
                             n * sizeof(double));
     const size_t oRe = take((size_t)n * sizeof(int));
+    const size_t oAi = take(ai ? (size_t)n * n * sizeof(long long) : 0);
+    const size_t oXd = take(xdig_bytes(n, nrhs));
     const size_t oN = take(64 * sizeof(double));
     const size_t oF = take(2 * (size_t)nblk * sizeof(unsigned));
     const size_t oY = take((size_t)n * nrhs * sizeof(float));
@@ -965,6 +1102,8 @@ size_t carve_ir(mg_handle_t h, int n, int nrhs, int nterms, IrWs* w, bool qr = f
         w->R = (double*)(b + oR);
         w->partial = (double*)(b + oPa);
         w->rexp = (int*)(b + oRe);
+        w->Ai = ai ? (long long*)(b + oAi) : nullptr;
+        w->xdig = (int*)(b + oXd);
         w->norms = (double*)(b + oN);
         w->flags = (unsigned*)(b + oF);
         w->Y = (float*)(b + oY);
@@ -1018,10 +1157,10 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
     if (!A || !B || !X) return mg::fail(h, MG_ERR_ARG, "mixed solve: null pointer");
 
     const auto t0 = clk::now();
-    MG_TRY(mg::ensure_ws(h, carve_ir(h, n, nrhs, o.nterms, nullptr, qr)));
+    MG_TRY(mg::ensure_ws(h, carve_ir(h, n, nrhs, o.nterms, nullptr, qr, o.residual == 0)));
     MG_TRY(mg::ensure_hws(h, 512 + sizeof(double) * GM_CTAS * (GM_RESTART + 1) * MAX_RHS));
     IrWs w;
-    carve_ir(h, n, nrhs, o.nterms, &w, qr);
+    carve_ir(h, n, nrhs, o.nterms, &w, qr, o.residual == 0);
     cudaStream_t st = h->stream;
     const int cap = h->num_sms * 8;
     const int kch = (n + RES_KCHUNK - 1) / RES_KCHUNK;
@@ -1143,6 +1282,7 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
     // the integer residual unless asked for FP64 or A holds an infinity or NaN
     // (error word 4, read back with the first residual, before any product)
     bool int_res = o.residual == 0;
+    bool ai_ready = false;  // w.Ai holds A's integers
     const int ri_chunk = resint_kchunk(n, h->num_sms);
     const int ri_kch = (n + ri_chunk - 1) / ri_chunk;
     int* const vexp = w.gemm_err + 8;      // the integer residual's column exponents (8)
@@ -1156,15 +1296,12 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
             colexp_kernel<<<dim3(std::min(64, (n + 255) / 256), nrhs), 256, 0, st>>>(V, ldv, n, nrhs, vexp, vbad);
             MG_TRY(mg::post_launch(h, "colexp_kernel"));
             const dim3 g((n + RI_ROWS - 1) / RI_ROWS, ri_kch);
-            switch (nrhs) {
-#define MG_RES(NRV)                                                                                               \
-    case NRV:                                                                                                     \
-        residual_int_kernel<NRV><<<g, RI_ROWS, 0, st>>>(A, lda, n, V, ldv, ri_chunk, w.rexp, vexp, ipart); break;
-                MG_RES(1) MG_RES(2) MG_RES(3) MG_RES(4) MG_RES(5) MG_RES(6) MG_RES(7)
-                default: residual_int_kernel<8><<<g, RI_ROWS, 0, st>>>(A, lda, n, V, ldv, ri_chunk, w.rexp, vexp, ipart);
-                break;
-#undef MG_RES
-            }
+            // the first product also stores A's integers; the later ones read them
+            xdigits_kernel<<<grid_for((size_t)n * nrhs, 256, cap), 256, 0, st>>>(V, ldv, n, nrhs, vexp, w.xdig);
+            MG_TRY(mg::post_launch(h, "xdigits_kernel"));
+            MG_CHECK_CUDA(h, launch_resint(ai_ready ? 2 : 1, nrhs, g, st, A, lda, w.Ai, n, n, w.xdig, ri_chunk, w.rexp,
+                                           ipart));
+            ai_ready = true;
             return mg::post_launch(h, "residual_int_kernel");
         }
         switch (nrhs) {
@@ -1471,7 +1608,8 @@ extern "C" mg_status_t mg_dresidual(mg_handle_t h, int n, int nrhs, const double
     const size_t orexp = mg::align_up((size_t)std::max(kch, RI_CLASSES * ri_kch) * nrhs * n * sizeof(double), 1024);
     const size_t oflag = mg::align_up(orexp + (size_t)n * sizeof(int), 1024);
     const size_t onorm = oflag + 1024;
-    MG_TRY(mg::ensure_ws(h, onorm + 16 * sizeof(double)));
+    const size_t oxd = onorm + 1024;
+    MG_TRY(mg::ensure_ws(h, oxd + xdig_bytes(n, nrhs)));
     MG_TRY(mg::ensure_hws(h, 64));
     char* b = (char*)h->ws;
     double* partial = (double*)(b + opart);
@@ -1479,6 +1617,7 @@ extern "C" mg_status_t mg_dresidual(mg_handle_t h, int n, int nrhs, const double
     int* rexp = (int*)(b + orexp);
     int* flags = (int*)(b + oflag);  // [0] A non-finite, [1] X non-finite, [8..16) column exponents
     double* norms = (double*)(b + onorm);
+    int* xdig = (int*)(b + oxd);
     const cudaStream_t st = h->stream;
     bool int_res = mode == 0;
     if (int_res) {
@@ -1496,15 +1635,10 @@ extern "C" mg_status_t mg_dresidual(mg_handle_t h, int n, int nrhs, const double
         colexp_kernel<<<dim3(std::min(64, (n + 255) / 256), nrhs), 256, 0, st>>>(X, ldx, n, nrhs, flags + 8, flags + 1);
         MG_TRY(mg::post_launch(h, "colexp_kernel"));
         const dim3 g((n + RI_ROWS - 1) / RI_ROWS, ri_kch);
-        switch (nrhs) {
-#define MG_RES(NRV)                                                                                              \
-    case NRV:                                                                                                    \
-        residual_int_kernel<NRV><<<g, RI_ROWS, 0, st>>>(A, lda, n, X, ldx, ri_chunk, rexp, flags + 8, ipart); break;
-            MG_RES(1) MG_RES(2) MG_RES(3) MG_RES(4) MG_RES(5) MG_RES(6) MG_RES(7)
-            default: residual_int_kernel<8><<<g, RI_ROWS, 0, st>>>(A, lda, n, X, ldx, ri_chunk, rexp, flags + 8, ipart);
-            break;
-#undef MG_RES
-        }
+        xdigits_kernel<<<std::max(1, std::min(h->num_sms * 8, (n * nrhs + 255) / 256)), 256, 0, st>>>(X, ldx, n, nrhs,
+                                                                                                     flags + 8, xdig);
+        MG_TRY(mg::post_launch(h, "xdigits_kernel"));
+        MG_CHECK_CUDA(h, launch_resint(0, nrhs, g, st, A, lda, nullptr, n, n, xdig, ri_chunk, rexp, ipart));
         MG_TRY(mg::post_launch(h, "residual_int_kernel"));
         residual_int_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(ipart, ri_kch, n, nrhs, rexp, flags + 8,
                                                                    flags + 1, B, ldb, X, ldx, R, ldr, norms);
