@@ -775,8 +775,9 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                 const int p = row0 + k * CP_THREADS + tid;
                 act[k] = p < R && p >= cs0 + CP_SW;
             }
-            // columns in groups of 4, the next group's loads in flight during this group's FMAs
-            constexpr int G = 4;
+            // columns in groups of G (G x RPT = 16 loads per thread), the next
+            // group's loads in flight during this group's FMAs
+            constexpr int G = 16 / RPT;
             const size_t ld = (size_t)lda;
             float* const C0 = P0 + (size_t)(cs0 + CP_SW) * ld;
             float cur[G][RPT], nxt[G][RPT];
