@@ -434,7 +434,8 @@ def run_reference(args):
 
 
 def e2e_run(h, A, B, n, nrhs, steps, barrier, warmup=3):
-    """The solve through the C ABI from pinned host buffers, two ways, after
+    """The solve through the C ABI from pinned host buffers (the library's
+    mg_host_malloc_pinned), two ways, after
     `warmup` untimed steps each (wall clock, max over ranks by the barrier):
 
     serial: per step the H2D copy of A and B, the solve, the D2H copy of X
@@ -451,13 +452,25 @@ def e2e_run(h, A, B, n, nrhs, steps, barrier, warmup=3):
 
     import torch
 
+    import numpy as np
+
     from mat_gb300.api import Handle, colmajor
-    hA = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
-    hA.copy_(A.t())  # column-major bytes of A in a row-major (n x n) pinned host buffer
-    hBt = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
-    hBt.copy_(B.t())
-    hXt = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
     lib = h.lib
+    pinned = []
+
+    def host_buffer(rows, cols):
+        # page-locked host memory from the library (mg_host_malloc_pinned), as a CPU tensor
+        p = C.c_void_p()
+        h.check(lib.mg_host_malloc_pinned(C.byref(p), 8 * rows * cols), "mg_host_malloc_pinned")
+        pinned.append(p)
+        arr = np.ctypeslib.as_array((C.c_double * (rows * cols)).from_address(p.value))
+        return torch.from_numpy(arr).view(rows, cols)
+
+    hA = host_buffer(n, n)
+    hA.copy_(A.t())  # column-major bytes of A in a row-major (n x n) pinned host buffer
+    hBt = host_buffer(nrhs, n)
+    hBt.copy_(B.t())
+    hXt = host_buffer(nrhs, n)
     h2d = 8 * n * n + 8 * n * nrhs
     d2h = 8 * n * nrhs
 
@@ -539,6 +552,8 @@ def e2e_run(h, A, B, n, nrhs, steps, barrier, warmup=3):
     hs.close()
     hc.close()
     del dAs, dBs, dXs, hA, hBt, hXt
+    for p in pinned:
+        lib.mg_host_free_pinned(p)
     torch.cuda.empty_cache()
     return {"value": pipe_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "pipelined": True, "step_ms": [round(x, 2) for x in pipe_ms],
