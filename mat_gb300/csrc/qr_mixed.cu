@@ -224,19 +224,20 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
             for (int u = lane; u < P; u += 32) xn2 += __ldcg(&xpc[(size_t)u * stride]);
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) xn2 += __shfl_xor_sync(0xffffffffu, xn2, off);
-            if (lane == 0) {
+            if (lane < 2) {  // tau (lane 0) and the scale (lane 1) in one division sequence
                 const double alpha = (double)__ldcg(&drc[c]);
-                if (xn2 == 0.0) {  // nothing below the diagonal: H = I
-                    s_tau = 0.0;
-                    s_scal = 0.0;
-                    s_beta = alpha;
-                } else {
-                    const double beta = -copysign(sqrt(fma(alpha, alpha, xn2)), alpha);
-                    s_tau = (beta - alpha) / beta;
-                    s_scal = 1.0 / (alpha - beta);
-                    s_beta = beta;
+                double qv = 0.0, beta = alpha;  // nothing below the diagonal: H = I
+                if (xn2 != 0.0) {
+                    beta = -copysign(sqrt(fma(alpha, alpha, xn2)), alpha);
+                    qv = (lane == 0 ? beta - alpha : 1.0) / (lane == 0 ? beta : alpha - beta);
                 }
-                if (b == 0) tau[c] = s_tau;
+                if (lane == 0) {
+                    s_tau = qv;
+                    s_beta = beta;
+                    if (b == 0) tau[c] = qv;
+                } else {
+                    s_scal = qv;
+                }
             }
         }
         __syncthreads();
@@ -249,7 +250,7 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
             for (int jj = c + 1 + tid; jj < w; jj += QP_THREADS) {
                 const float* pc = reinterpret_cast<const float*>(xpc + 2) + jj;
                 float d = 0.f;
-#pragma unroll 8
+#pragma unroll 32
                 for (int u = 0; u < P; ++u) d += __ldcg(pc + (size_t)u * stride * 2);
                 s_coef[jj] = -tcf * fmaf(scf0, d, __ldcg(&drc[jj]));
             }
@@ -348,24 +349,30 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
         s = block_sum0(s, qs.red);
         if (tid == 0) *reinterpret_cast<double*>(&qs.rec[0]) = s;
         __syncthreads();
-        // 2. warp 0 pushes the record into slot [q] of every CTA (lane l -> CTA
-        //    l), and the owner's warp 0 the diagonal row (lane 16 + l -> CTA l);
-        //    only the columns still ahead travel: the record's dots and the
-        //    row's entries are packed from column c + 1 and c on
-        if (warp == 0) {
-            if (lane < QC_CS) {
-                const uint32_t dst = tc::cluster_addr(&qs.recv[buf][q][0], lane);
-                const uint32_t bar = tc::cluster_addr(&qs.mbar[buf], lane);
-                const float4* r4 = reinterpret_cast<const float4*>(qs.rec);
-                const int n16 = qc_rec16(w, c);
-                for (int u = 0; u < n16; ++u) tc::st_async16(dst + 16u * u, r4[u], bar);
-            } else if (owner) {
-                const uint32_t dst = tc::cluster_addr(&qs.recv_diag[buf][0], lane - QC_CS);
-                const uint32_t bar = tc::cluster_addr(&qs.mbar[buf], lane - QC_CS);
-                const float4* d4 = reinterpret_cast<const float4*>(qs.diag);
-                const int n16 = qc_diag16(w, c);
-                for (int u = 0; u < n16; ++u) tc::st_async16(dst + 16u * u, d4[u], bar);
+        // 2. every thread pushes a share of the record into slot [q] of every
+        //    CTA (16-byte chunk u to CTA d for e = u * 16 + d), and the owner's
+        //    threads the diagonal row; only the columns still ahead travel:
+        //    the record's dots and the row's entries are packed from column
+        //    c + 1 and c on
+        {
+            const float4* r4 = reinterpret_cast<const float4*>(qs.rec);
+            const int n16 = qc_rec16(w, c);
+            for (int e = tid; e < n16 * QC_CS; e += QP_THREADS) {
+                const int u = e / QC_CS, d = e - u * QC_CS;
+                tc::st_async16(tc::cluster_addr(&qs.recv[buf][q][0], d) + 16u * u, r4[u],
+                               tc::cluster_addr(&qs.mbar[buf], d));
             }
+            if (owner) {
+                const float4* d4 = reinterpret_cast<const float4*>(qs.diag);
+                const int nd = qc_diag16(w, c);
+                for (int e = tid; e < nd * QC_CS; e += QP_THREADS) {
+                    const int u = e / QC_CS, d = e - u * QC_CS;
+                    tc::st_async16(tc::cluster_addr(&qs.recv_diag[buf][0], d) + 16u * u, d4[u],
+                                   tc::cluster_addr(&qs.mbar[buf], d));
+                }
+            }
+        }
+        if (warp == 0) {
             // 3. wait for the 16 records and the diagonal row; S over the CTAs
             //    (a shuffle tree, fixed order), then beta, tau and the scale (FP64)
             int ok = 1;
