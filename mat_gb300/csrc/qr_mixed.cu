@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
             for (int jj = c + 1 + tid; jj < w; jj += QP_THREADS) {
                 const float* pc = reinterpret_cast<const float*>(xpc + 2) + jj;
                 float d = 0.f;
-#pragma unroll 32
+#pragma unroll 8
                 for (int u = 0; u < P; ++u) d += __ldcg(pc + (size_t)u * stride * 2);
                 s_coef[jj] = -tcf * fmaf(scf0, d, __ldcg(&drc[jj]));
             }
