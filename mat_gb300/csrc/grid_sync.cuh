@@ -25,6 +25,12 @@ __device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
 
+// A flag store with release semantics at GPU scope (after a CTA barrier it
+// publishes the CTA's prior writes to whoever acquires the flag).
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
 // Returns false (in every thread of the CTA) if the wait timed out.  `limit`
 // is the poll budget (the self-test lowers it to make a wait run out).
 __device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target, int* err,

@@ -910,10 +910,7 @@ __global__ void __launch_bounds__(256) trsv_flow_kernel(const float* __restrict_
 #pragma unroll
         for (int j = 0; j < NR; ++j) Xout[r0 + r + (size_t)j * n] = part[0][j][r] + part[1][j][r];
     __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        atomicExch(flags + me, 1u);
-    }
+    if (threadIdx.x == 0) mg::st_release_u32(flags + me, 1u);  // publishes the block's x
 }
 
 // Largest block count the dataflow solve can take as one cooperative grid.

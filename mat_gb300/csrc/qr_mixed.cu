@@ -543,7 +543,9 @@ __global__ void __launch_bounds__(256) qt32_fused_kernel(const float* __restrict
                                                          const float* __restrict__ T, float* __restrict__ X, int ldx,
                                                          int nrhs, float* __restrict__ part, float* __restrict__ W,
                                                          unsigned* bar, int* err) {
+    extern __shared__ float tsm[];   // the panel's T block (QB x QB, column-major)
     __shared__ float ys[QB * 8];
+    __shared__ float wsm[QB * 8];    // W = V^T X of the panel
     __shared__ float red[8][8][33];  // [group][rhs][row]
     const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int chunk = (n + G - 1) / G, lo = b * chunk, hi = min(n, lo + chunk);
@@ -564,33 +566,54 @@ __global__ void __launch_bounds__(256) qt32_fused_kernel(const float* __restrict
                 for (int j = 0; j < 8; ++j)
                     if (j < nrhs) acc[j] = fmaf(vi, X[i + (size_t)j * ldx], acc[j]);
             }
+            // the 8 sums over the warp by halving exchanges (4 + 2 + 1 shuffles
+            // leave lane l with right-hand side (l >> 2) & 7 summed over 8
+            // lanes, two more levels finish it): a fixed order
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
+            for (int h = 4, off = 16; h >= 1; h >>= 1, off >>= 1) {
+                const bool up = (lane & off) != 0;
 #pragma unroll
-                for (int off = 16; off > 0; off >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], off);
+                for (int j = 0; j < h; ++j) {
+                    const float send = up ? acc[j] : acc[j + h];
+                    const float keep = up ? acc[j + h] : acc[j];
+                    acc[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+                }
             }
-            if (lane == 0)
-#pragma unroll
-                for (int j = 0; j < 8; ++j) pp[((size_t)b * QB + c) * 8 + j] = acc[j];
+            acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], 2);
+            acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], 1);
+            if ((lane & 3) == 0) pp[((size_t)b * QB + c) * 8 + ((lane >> 2) & 7)] = acc[0];
         }
         target += G;
         if (!mg::grid_barrier(bar, target, err)) return;
-        // 2. my share of W's entries, the CTAs' partials in a fixed order
-        for (int e = b * blockDim.x + tid; e < w * 8; e += G * blockDim.x) {
+        // 2. W's entries dealt to the grid's warps: lane l sums the partials
+        //    of CTAs l, l + 32, ... (all its loads in flight together), then a
+        //    shuffle tree; a fixed order either way
+        for (int e = b * 8 + warp; e < w * 8; e += G * 8) {
             float sum = 0.f;
-#pragma unroll 8
-            for (int u = 0; u < G; ++u) sum += __ldcg(pp + (size_t)u * QB * 8 + e);
-            wp[e] = sum;
+            for (int u = lane; u < G; u += 32) sum += __ldcg(pp + (size_t)u * QB * 8 + e);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+            if (lane == 0) wp[e] = sum;
         }
         target += G;
         if (!mg::grid_barrier(bar, target, err)) return;
-        // 3. y = T^T W, then X -= V y on my rows
+        // 3. y = T^T W from T and W staged in shared memory, then X -= V y on my rows
         const float* Tb = T + (size_t)(j0 / QB) * QB * QB;
+        {
+            float4 tv[QB * QB / 4 / 256];  // the whole T block, all loads in flight
+            const float4* Tb4 = reinterpret_cast<const float4*>(Tb);
+#pragma unroll
+            for (int u = 0; u < QB * QB / 4 / 256; ++u) tv[u] = __ldg(Tb4 + tid + u * 256);
+#pragma unroll
+            for (int u = 0; u < QB * QB / 4 / 256; ++u) reinterpret_cast<float4*>(tsm)[tid + u * 256] = tv[u];
+        }
+        for (int q = tid; q < w * 8; q += blockDim.x) wsm[q] = __ldcg(wp + q);
+        __syncthreads();
         for (int q = tid; q < w * 8; q += blockDim.x) {
             const int c = q / 8, j = q % 8;
             float d = 0.f;
             if (j < nrhs)
-                for (int k = 0; k <= c; ++k) d = fmaf(Tb[k + (size_t)c * QB], __ldcg(wp + k * 8 + j), d);
+                for (int k = 0; k <= c; ++k) d = fmaf(tsm[k + c * QB], wsm[k * 8 + j], d);
             ys[q] = d;
         }
         __syncthreads();
@@ -782,13 +805,18 @@ mg_status_t qr_apply_qt_f32(mg_handle_t h, int n, int nrhs, const float* A, int 
     const cudaStream_t st = h->stream;
     const int G = h->num_sms;        // one CTA per SM (2 x G x QB x 8 partials fit the V^T V parts' area)
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qt32_fused_kernel, 256, 0) != cudaSuccess || per_sm < 1)
+    const size_t tsm_bytes = (size_t)QB * QB * sizeof(float);
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(qt32_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)tsm_bytes));
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qt32_fused_kernel, 256, tsm_bytes) != cudaSuccess ||
+        per_sm < 1)
         return fail(h, MG_ERR_UNSUPPORTED, "qr_apply_qt_f32: the cooperative grid does not fit");
     MG_CHECK_CUDA(h, cudaMemsetAsync(bar, 0, sizeof(unsigned), st));
     int n_ = n, lda_ = lda, ldx_ = ldx, nrhs_ = nrhs;
     void* args[] = {(void*)&A, &lda_, &n_, (void*)&T, (void*)&X, &ldx_, &nrhs_, (void*)&part, (void*)&W, (void*)&bar,
                     (void*)&err};
-    const cudaError_t e = cudaLaunchCooperativeKernel((const void*)qt32_fused_kernel, dim3(G), dim3(256), args, 0, st);
+    const cudaError_t e =
+        cudaLaunchCooperativeKernel((const void*)qt32_fused_kernel, dim3(G), dim3(256), args, tsm_bytes, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "qt32_fused_kernel launch");
     h->launches++;
     return MG_OK;
