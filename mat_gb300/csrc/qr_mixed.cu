@@ -461,10 +461,20 @@ __global__ void qr_tfactor_kernel(const float* __restrict__ G, int ldg, const do
     for (int c = 0; c < w; ++c) {
         const float tc = (float)tau[c];
         if (r < c) {
+            // four partial sums over k (independent shared-memory loads in
+            // flight), added in a fixed order
             const float* gc = gs + c * LD;
-            float sr = 0.f;
-            for (int k = r; k < c; ++k) sr = fmaf(t[r * LD + k], gc[k], sr);
-            t[r * LD + c] = -tc * sr;
+            const float* tr = t + r * LD;
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+            int k = r;
+            for (; k + 3 < c; k += 4) {
+                s0 = fmaf(tr[k], gc[k], s0);
+                s1 = fmaf(tr[k + 1], gc[k + 1], s1);
+                s2 = fmaf(tr[k + 2], gc[k + 2], s2);
+                s3 = fmaf(tr[k + 3], gc[k + 3], s3);
+            }
+            for (; k < c; ++k) s0 = fmaf(tr[k], gc[k], s0);
+            t[r * LD + c] = -tc * ((s0 + s1) + (s2 + s3));
         }
         if (r == c) t[c * LD + c] = tc;
         __syncthreads();
