@@ -385,7 +385,9 @@ __global__ void split_cols_kernel(const TIN* __restrict__ B, int ldb, int K, int
 // product on the critical path of every step of the mixed LU.
 constexpr int TS_W = 128;  // widest panel
 constexpr int TS_C = 64;   // columns per CTA
-constexpr int TS_THREADS = 4 * TS_C;
+constexpr int TS_TPC = 8;  // threads per column: rows g, g + 8 of every 16-row block
+constexpr int TS_RPB = 16 / TS_TPC;
+constexpr int TS_THREADS = TS_TPC * TS_C;
 constexpr int TS_P = TS_W + 4;  // pitch of both shared arrays (words)
 constexpr size_t TS_SMEM = (size_t)(TS_W * TS_P + TS_C * TS_P) * sizeof(float);
 
@@ -396,8 +398,8 @@ __global__ void __launch_bounds__(TS_THREADS) trsm_split_kernel(const float* __r
     float* const sL = ts_sm;                // [TS_W][TS_P]: L11(i, j) at i * TS_P + j, strict lower part only
     float* const sx = ts_sm + TS_W * TS_P;  // [TS_C][TS_P]: row i of column c at c * TS_P + i
     const int tid = threadIdx.x, lane = tid & 31;
-    const int c = (tid >> 5) * 8 + (lane >> 2);  // my column (of this CTA's TS_C)
-    const int g = lane & 3;                      // my rows g, g+4, g+8, g+12 of each 16-row block
+    const int c = (tid >> 5) * (32 / TS_TPC) + lane / TS_TPC;  // my column (of this CTA's TS_C)
+    const int g = lane & (TS_TPC - 1);                          // my rows g + TS_TPC a of each 16-row block
     const int c0 = blockIdx.x * TS_C;
     const int ncol = min(TS_C, nt - c0);
     float* const xc = sx + c * TS_P;
@@ -431,9 +433,9 @@ __global__ void __launch_bounds__(TS_THREADS) trsm_split_kernel(const float* __r
     }
     __syncthreads();
     for (int I = 0; I < w; I += 16) {
-        float xi[4];  // rows I + g + 4a
+        float xi[TS_RPB];  // rows I + g + TS_TPC a
 #pragma unroll
-        for (int a = 0; a < 4; ++a) xi[a] = xc[I + g + 4 * a];
+        for (int a = 0; a < TS_RPB; ++a) xi[a] = xc[I + g + TS_TPC * a];
         for (int J = 0; J < I; J += 16) {
             float xj[16];
 #pragma unroll
@@ -445,8 +447,8 @@ __global__ void __launch_bounds__(TS_THREADS) trsm_split_kernel(const float* __r
                 xj[4 * b4 + 3] = v.w;
             }
 #pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                const float4* lr = reinterpret_cast<const float4*>(sL + (I + g + 4 * a) * TS_P + J);
+            for (int a = 0; a < TS_RPB; ++a) {
+                const float4* lr = reinterpret_cast<const float4*>(sL + (I + g + TS_TPC * a) * TS_P + J);
 #pragma unroll
                 for (int b4 = 0; b4 < 4; ++b4) {
                     const float4 l = lr[b4];
@@ -460,13 +462,13 @@ __global__ void __launch_bounds__(TS_THREADS) trsm_split_kernel(const float* __r
         // the 16 x 16 diagonal block: x_b final -> the rows below it in the block
 #pragma unroll
         for (int b = 0; b < 16; ++b) {
-            const float xb = __shfl_sync(0xffffffffu, xi[b >> 2], (lane & ~3) | (b & 3));
+            const float xb = __shfl_sync(0xffffffffu, xi[b / TS_TPC], (lane & ~(TS_TPC - 1)) | (b % TS_TPC));
 #pragma unroll
-            for (int a = 0; a < 4; ++a)
-                if (g + 4 * a > b) xi[a] = fmaf(-sL[(I + g + 4 * a) * TS_P + I + b], xb, xi[a]);
+            for (int a = 0; a < TS_RPB; ++a)
+                if (g + TS_TPC * a > b) xi[a] = fmaf(-sL[(I + g + TS_TPC * a) * TS_P + I + b], xb, xi[a]);
         }
 #pragma unroll
-        for (int a = 0; a < 4; ++a) xc[I + g + 4 * a] = xi[a];
+        for (int a = 0; a < TS_RPB; ++a) xc[I + g + TS_TPC * a] = xi[a];
         __syncwarp();  // a column's four threads share one warp
     }
     __syncthreads();
