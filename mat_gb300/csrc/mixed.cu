@@ -702,22 +702,28 @@ __global__ void inv_diag_blocks_kernel(const float* __restrict__ LU, int lda, in
     const int c = threadIdx.x;
     if (c < bs) {
         float* zc = z + c * IR_BLOCK;
+        // each dot in four partial sums (independent shared-memory loads in
+        // flight), added in a fixed order
+        auto dot = [&](int i, int ka, int kb) {  // sum over k in [ka, kb) of blk(i, k) zc[k]
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+            int k = ka;
+            for (; k + 3 < kb; k += 4) {
+                s0 = fmaf(blk[i + k * IR_BLOCK], zc[k], s0);
+                s1 = fmaf(blk[i + (k + 1) * IR_BLOCK], zc[k + 1], s1);
+                s2 = fmaf(blk[i + (k + 2) * IR_BLOCK], zc[k + 2], s2);
+                s3 = fmaf(blk[i + (k + 3) * IR_BLOCK], zc[k + 3], s3);
+            }
+            for (; k < kb; ++k) s0 = fmaf(blk[i + k * IR_BLOCK], zc[k], s0);
+            return (s0 + s1) + (s2 + s3);
+        };
         if (LOWER) {
             for (int i = 0; i < bs; ++i) zc[i] = 0.f;
             zc[c] = 1.f;
-            for (int i = c + 1; i < bs; ++i) {
-                float s = 0.f;
-                for (int k = c; k < i; ++k) s = fmaf(blk[i + k * IR_BLOCK], zc[k], s);
-                zc[i] = -s;
-            }
+            for (int i = c + 1; i < bs; ++i) zc[i] = -dot(i, c, i);
         } else {
             for (int i = 0; i < bs; ++i) zc[i] = 0.f;
             zc[c] = 1.f / blk[c + c * IR_BLOCK];
-            for (int i = c - 1; i >= 0; --i) {
-                float s = 0.f;
-                for (int k = i + 1; k <= c; ++k) s = fmaf(blk[i + k * IR_BLOCK], zc[k], s);
-                zc[i] = -s / blk[i + i * IR_BLOCK];
-            }
+            for (int i = c - 1; i >= 0; --i) zc[i] = -dot(i, i + 1, c + 1) / blk[i + i * IR_BLOCK];
         }
     }
     __syncthreads();
@@ -1223,8 +1229,21 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
         if (s != MG_OK && s != MG_SINGULAR) return s;
     }
     r.info = info;
-    absmax_upper_kernel<<<n, 256, 0, st>>>(w.A32, n, w.norms + 18);
+    // max |U| for the pivot-growth report, on the side stream beside the
+    // refinement (read back at the end of the solve)
+    MG_TRY(mg::ensure_lookahead(h));
+    MG_CHECK_CUDA(h, cudaEventRecord(h->pp_ev[0], st));
+    MG_CHECK_CUDA(h, cudaStreamWaitEvent(h->pp_stream, h->pp_ev[0], 0));
+    absmax_upper_kernel<<<n, 256, 0, h->pp_stream>>>(w.A32, n, w.norms + 18);
     MG_TRY(mg::post_launch(h, "absmax_upper_kernel"));
+    MG_CHECK_CUDA(h, cudaEventRecord(h->pp_ev[1], h->pp_stream));
+    auto read_growth = [&]() -> mg_status_t {
+        MG_CHECK_CUDA(h, cudaStreamWaitEvent(st, h->pp_ev[1], 0));
+        MG_CHECK_CUDA(h, cudaMemcpyAsync(hn + 40, w.norms + 17, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        MG_CHECK_CUDA(h, cudaStreamSynchronize(st));
+        r.pivot_growth = hn[40] > 0 ? hn[41] / hn[40] : 0.0;
+        return MG_OK;
+    };
     bool flow = false;
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(inv_diag_blocks_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           2 * IR_BLOCK * IR_BLOCK * (int)sizeof(float)));
@@ -1250,12 +1269,17 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
         // inverses of the diagonal blocks of L and U (the solves' block steps);
         // L's blocks are final once their panel is done (later interchanges only
         // touch rows below them)
-        inv_diag_blocks_kernel<true><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
-                                                                                                     w.Linv);
+        // L's on the look-ahead stream beside U's
+        MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[0], st));
+        MG_CHECK_CUDA(h, cudaStreamWaitEvent(h->la_stream, h->la_ev[0], 0));
+        inv_diag_blocks_kernel<true><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), h->la_stream>>>(
+            w.A32, n, n, w.Linv);
         MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<lower>"));
+        MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[1], h->la_stream));
         inv_diag_blocks_kernel<false><<<nblk, IR_BLOCK, 2 * IR_BLOCK * IR_BLOCK * sizeof(float), st>>>(w.A32, n, n,
                                                                                                       w.Uinv);
         MG_TRY(mg::post_launch(h, "inv_diag_blocks_kernel<upper>"));
+        MG_CHECK_CUDA(h, cudaStreamWaitEvent(st, h->la_ev[1], 0));
         int flow_cap = 0;
         switch (nrhs) {
     #define MG_CAP(NRV) \
@@ -1356,7 +1380,6 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
             eta = std::max(eta, e);
         }
         r.anorm_inf = anorm;
-        r.pivot_growth = hn[17] > 0 ? hn[18] / hn[17] : 0.0;
         r.backward_error = eta;
         if (nres < 32) r.history[nres] = eta;
         ++nres;
@@ -1583,6 +1606,7 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
             result = mg::fail(h, MG_IR_STALLED, "refinement stalled at backward error %.3e", r.backward_error);
         }
     }
+    MG_TRY(read_growth());
     if (rep) *rep = r;
     return result;
 }
