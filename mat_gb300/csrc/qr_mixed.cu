@@ -446,40 +446,59 @@ __global__ void qr_gsum_kernel(const float* __restrict__ gpart, int nparts, floa
 // fp32 (T is an fp32 factor; an FP64 recurrence here cost ~1 ms per panel:
 // up to 127 dependent FP64 FMAs per column at ~70 cycles each).  One CTA of
 // QB threads; T's columns in dynamic shared memory.
-__global__ void qr_tfactor_kernel(const float* __restrict__ G, int ldg, const double* __restrict__ tau, int w,
-                                  float* __restrict__ T) {
+__global__ void __launch_bounds__(2 * QB) qr_tfactor_kernel(const float* __restrict__ G, int ldg,
+                                                             const double* __restrict__ tau, int w,
+                                                             float* __restrict__ T) {
     extern __shared__ float t[];  // [QB][QB + 1]: t[r * (QB + 1) + c], then G's columns [QB][QB + 1]
+    __shared__ float taus[QB];
     constexpr int LD = QB + 1;
     float* const gs = t + QB * LD;  // G(k, c) at gs[c * LD + k]
-    for (int e = threadIdx.x; e < QB * LD; e += blockDim.x) t[e] = 0.f;
-    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
-        const int k = e % w, c = e / w;
-        gs[c * LD + k] = G[k + (size_t)c * ldg];
+    const int tid = threadIdx.x;
+    for (int e = tid; e < QB * LD; e += blockDim.x) t[e] = 0.f;
+    if (tid < w) taus[tid] = (float)tau[tid];
+    {  // G's w x w block, all loads of a thread in flight together
+        constexpr int PER = QB * QB / (2 * QB);
+        float g[PER];
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int e = tid + u * 2 * QB, k = e % QB, c = e / QB;
+            g[u] = (k < w && c < w) ? G[k + (size_t)c * ldg] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int e = tid + u * 2 * QB, k = e % QB, c = e / QB;
+            gs[c * LD + k] = g[u];
+        }
     }
     __syncthreads();
-    const int r = threadIdx.x;
+    // column c: T(r, c) = -tau_c sum_{k = r}^{c-1} T(r, k) G(k, c) for r < c; two
+    // threads per row (the halves of k), each with four partial sums, added
+    // in a fixed order
+    const int r = tid >> 1, hf = tid & 1;
     for (int c = 0; c < w; ++c) {
-        const float tc = (float)tau[c];
+        float s = 0.f;
         if (r < c) {
-            // four partial sums over k (independent shared-memory loads in
-            // flight), added in a fixed order
             const float* gc = gs + c * LD;
             const float* tr = t + r * LD;
+            const int mid = r + (c - r) / 2;
+            const int ka = hf ? mid : r, kb = hf ? c : mid;
             float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-            int k = r;
-            for (; k + 3 < c; k += 4) {
+            int k = ka;
+            for (; k + 3 < kb; k += 4) {
                 s0 = fmaf(tr[k], gc[k], s0);
                 s1 = fmaf(tr[k + 1], gc[k + 1], s1);
                 s2 = fmaf(tr[k + 2], gc[k + 2], s2);
                 s3 = fmaf(tr[k + 3], gc[k + 3], s3);
             }
-            for (; k < c; ++k) s0 = fmaf(tr[k], gc[k], s0);
-            t[r * LD + c] = -tc * ((s0 + s1) + (s2 + s3));
+            for (; k < kb; ++k) s0 = fmaf(tr[k], gc[k], s0);
+            s = (s0 + s1) + (s2 + s3);
         }
-        if (r == c) t[c * LD + c] = tc;
+        const float other = __shfl_xor_sync(0xffffffffu, s, 1);
+        if (r < c && hf == 0) t[r * LD + c] = -taus[c] * (s + other);
+        if (tid == 2 * c) t[c * LD + c] = taus[c];
         __syncthreads();
     }
-    for (int e = threadIdx.x; e < QB * QB; e += blockDim.x) {
+    for (int e = tid; e < QB * QB; e += blockDim.x) {
         const int rr = e % QB, cc = e / QB;
         T[e] = (rr < w && cc < w) ? t[rr * LD + cc] : 0.f;
     }
@@ -782,7 +801,7 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
         float* Tb = T + (size_t)(j0 / QB) * QB * QB;
         qr_gsum_kernel<<<QB * QB / 256, 256, 0, st>>>(gpart, nparts, G);
         MG_TRY(post_launch(h, "qr_gsum_kernel"));
-        qr_tfactor_kernel<<<1, QB, 2 * QB * (QB + 1) * sizeof(float), st>>>(G, QB, tau + j0, w, Tb);
+        qr_tfactor_kernel<<<1, 2 * QB, 2 * QB * (QB + 1) * sizeof(float), st>>>(G, QB, tau + j0, w, Tb);
         MG_TRY(post_launch(h, "qr_tfactor_kernel"));
         const int nt = n - j0 - w;
         if (nt > 0) {  // R2 -= V (T^T (V^T R2))
