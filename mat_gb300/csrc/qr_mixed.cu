@@ -34,23 +34,6 @@ constexpr int QP_THREADS = 256;
 constexpr int QG_ROWS = 32;                                    // rows per chunk of the in-kernel V^T V
 constexpr size_t QG_TILE_BYTES = (size_t)QG_ROWS * (QB + 4) * sizeof(float) + 16;  // + alignment slack
 
-// Sum of one double per thread over the CTA, valid in thread 0 (a shuffle
-// tree per warp, then warp 0 over the warps' sums, in a fixed order).
-__device__ __forceinline__ double block_sum0(double v, double* red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (warp == 0) {
-        t = lane < QP_THREADS / 32 ? red[lane] : 0.0;
-#pragma unroll
-        for (int off = QP_THREADS / 64; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
-    }
-    return t;
-}
-
 // The panel slab in shared memory: column c of a CTA's rows at slab + c * lds,
 // lds = rpc | 1 (odd, so that lanes reading one row of consecutive columns hit
 // distinct banks).
@@ -99,16 +82,20 @@ __device__ __forceinline__ void gram_part(const float* slab, int w, int lds, int
 // The dots of column c (the rows below the diagonal) with the panel's later
 // columns jj > c: a thread per (column, half of the rows), four independent
 // accumulators along the rows (a fixed order), the halves added in shared
-// memory (part: 2 x QB floats); then out(jj, dot) for each jj.  Called by
-// every thread of the CTA (it holds a CTA barrier).
-template <class Out>
-__device__ __forceinline__ void panel_dots(const float* slab, int lds, int rpc, int w, int c, int r0, int h,
-                                           float* part, Out out) {
-    const int tid = threadIdx.x, half = tid >> 7, jj = c + 1 + (tid & 127);
+// memory (part: 2 x QB floats); then out(jj, dot) for each jj.  With them,
+// under the same CTA barrier, the FP64 sum of squares of those rows: each
+// warp reduces its threads' partial sums by a shuffle tree before the
+// barrier (overlapping the other warps' dots), warp 0 sums the 8 warps'
+// partials after it (a fixed tree) and passes the total to norm_out in
+// lane 0.  Called by every thread of the CTA.
+template <class Out, class NormOut>
+__device__ __forceinline__ void panel_dots_norm(const float* slab, int lds, int rpc, int w, int c, int r0, int h,
+                                                float* part, double* red, Out out, NormOut norm_out) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, half = tid >> 7, jj = c + 1 + (tid & 127);
     const int ilo = max(0, c + 1 - r0), ihi = min(rpc, h - r0);  // my rows below the diagonal
-    const int mid = ilo + max(0, ihi - ilo) / 2;
+    const float* col = slab + (size_t)c * lds;
     if (jj < w) {
-        const float* col = slab + (size_t)c * lds;
+        const int mid = ilo + max(0, ihi - ilo) / 2;
         const float* a = slab + (size_t)jj * lds;
         const int lo = half ? mid : ilo, hi = half ? max(ihi, mid) : mid;
         float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;
@@ -122,8 +109,25 @@ __device__ __forceinline__ void panel_dots(const float* slab, int lds, int rpc, 
         for (; i < hi; ++i) d0 = fmaf(col[i], a[i], d0);
         part[half * QB + jj] = (d0 + d1) + (d2 + d3);
     }
+    double s = 0.0;
+    for (int i = tid; i < rpc; i += QP_THREADS) {
+        const int gi = r0 + i;
+        if (gi > c && gi < h) {
+            const double x = col[i];
+            s = fma(x, x, s);
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0) red[warp] = s;
     __syncthreads();
     if (half == 0 && jj < w) out(jj, part[jj] + part[QB + jj]);
+    if (warp == 0) {
+        double t = lane < QP_THREADS / 32 ? red[lane] : 0.0;
+#pragma unroll
+        for (int off = QP_THREADS / 64; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+        if (lane == 0) norm_out(t);
+    }
 }
 
 // The reflector and its update on my rows (a thread per row): v = x * scale
@@ -193,27 +197,18 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
     unsigned target = 0;
     bool ok = true;
     for (int c = 0; c < w && ok; ++c) {
-        float* col = slab + (size_t)c * lds;
         double* const xpc = xp + (size_t)(c & 1) * P * stride;
         float* const drc = drow + (c & 1) * QB;
         // 1. partials below the diagonal: sum of squares (FP64), dots with the
         //    later columns (fp32, a warp per column); the diagonal row (owner)
         {
             float* const xd = reinterpret_cast<float*>(xpc + (size_t)b * stride + 2);
-            panel_dots(slab, lds, rpc, w, c, r0, h, sh_part, [&](int jj, float d) { xd[jj] = d; });
+            panel_dots_norm(
+                slab, lds, rpc, w, c, r0, h, sh_part, red, [&](int jj, float d) { xd[jj] = d; },
+                [&](double t) { xpc[(size_t)b * stride] = t; });
         }
         if (c >= r0 && c < r1)
             for (int jj = c + tid; jj < w; jj += QP_THREADS) drc[jj] = slab[(size_t)jj * lds + (c - r0)];
-        double s = 0.0;
-        for (int i = tid; i < rpc; i += QP_THREADS) {
-            const int gi = r0 + i;
-            if (gi > c && gi < h) {
-                const double x = col[i];
-                s = fma(x, x, s);
-            }
-        }
-        s = block_sum0(s, red);
-        if (tid == 0) xpc[(size_t)b * stride] = s;
         target += P;
         ok = mg::grid_barrier(bar, target, err);
         if (!ok) break;
@@ -331,23 +326,14 @@ __global__ void __launch_bounds__(QP_THREADS, 1)
     bool rx_failed = false;  // warp 0: a receive wait gave up (error recorded; later waits skipped)
     for (int c = 0; c < w; ++c) {
         const int buf = c & 1;
-        float* col = slab + (size_t)c * lds;
         const bool owner = c >= r0 && c < r1;
         // 1. the record: dots of the unscaled column with the later columns
         //    (fp32, a warp per column), sum of squares (FP64); the diagonal row
-        panel_dots(slab, lds, rpc, w, c, r0, h, sh_part, [&](int jj, float d) { qs.rec[4 + (jj - c - 1)] = d; });
+        panel_dots_norm(
+            slab, lds, rpc, w, c, r0, h, sh_part, qs.red, [&](int jj, float d) { qs.rec[4 + (jj - c - 1)] = d; },
+            [&](double t) { *reinterpret_cast<double*>(&qs.rec[0]) = t; });
         if (owner)
             for (int jj = c + tid; jj < w; jj += QP_THREADS) qs.diag[jj - c] = slab[(size_t)jj * lds + (c - r0)];
-        double s = 0.0;
-        for (int i = tid; i < rpc; i += QP_THREADS) {
-            const int gi = r0 + i;
-            if (gi > c && gi < h) {
-                const double x = col[i];
-                s = fma(x, x, s);
-            }
-        }
-        s = block_sum0(s, qs.red);
-        if (tid == 0) *reinterpret_cast<double*>(&qs.rec[0]) = s;
         __syncthreads();
         // 2. every thread pushes a share of the record into slot [q] of every
         //    CTA (16-byte chunk u to CTA d for e = u * 16 + d), and the owner's
