@@ -286,6 +286,105 @@ __global__ void chol_to_lu_lower_kernel(float* __restrict__ A, int lda, int n, c
     }
 }
 
+// FP32 Cholesky of a diagonal block of the mixed SPD factorization (k <= 64)
+// together with G = L^{-T}, in one sweep with one CTA barrier per column.
+// Right-looking Cholesky is a sequence of column operations on A (column c
+// -= (a_cj / a_jj) column j for every c > j, then column j scaled by
+// 1 / sqrt(a_jj)) that turns A into A L^{-T} = L; the same operations
+// applied to an identity stacked below A turn it into L^{-T}.  The 128 x 64
+// stack [A; I] sits in registers: warp w owns columns w, w+16, w+32, w+48,
+// lane l rows l and l+32 of each half.  Per column j the warp that owns it
+// publishes the column (both halves; A's rows above j as zeros) to shared
+// memory, every thread applies the operation to the columns after j that it
+// owns (a window over its four rotated once per 16 columns, so that register
+// indices stay static in a rolled loop), and the owner scales its copy.  A
+// block narrower than 64 (the last one) is padded with the identity.  info:
+// first non-positive pivot (1-based, from col0).
+constexpr int CI_NB = 64;
+constexpr int CI_THREADS = 512;
+
+__global__ void __launch_bounds__(CI_THREADS) chol_inv64_kernel(float* __restrict__ D, int ldd, int k, int col0,
+                                                              float* __restrict__ G, int* __restrict__ info) {
+    __shared__ float colv[2][2 * CI_NB];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float a[4][4];  // [stacked row lane + 32 q: q < 2 in A, q >= 2 in I][window position]
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int i = lane + 32 * (q & 1);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const int c = w + 16 * m;
+            a[q][m] = i == c ? 1.f : 0.f;
+            if (q < 2 && i < k && c < k && i >= c) a[q][m] = D[i + (size_t)c * ldd];
+        }
+    }
+#pragma unroll 1
+    for (int jm = 0; jm < 4; ++jm) {
+        const int nlive = 3 - jm;  // window positions 1 .. nlive hold columns after this group of 16
+#pragma unroll
+        for (int jj = 0; jj < 16; ++jj) {
+            const int j = 16 * jm + jj;
+            float* const cv = colv[jj & 1];
+            if (w == jj) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) cv[lane + 32 * q] = (q < 2 && lane + 32 * q < j) ? 0.f : a[q][0];
+            }
+            __syncthreads();  // the column is published; the buffer of column j-1 stays readable
+            const float d = cv[j];
+            if (threadIdx.x == 0 && j < k && !(d > 0.f)) atomicCAS(info, 0, col0 + j + 1);
+            const float rd = __frcp_rn(d);
+            float t[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) t[q] = -cv[lane + 32 * q] * rd;
+            if (w > jj) {  // window position 0 is column w + 16 jm, after j
+                const float ck = cv[w + 16 * jm];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) a[q][0] = fmaf(t[q], ck, a[q][0]);
+            }
+#pragma unroll
+            for (int m = 1; m < 4; ++m) {
+                if (m <= nlive) {
+                    const float ck = cv[w + 16 * (jm + m)];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) a[q][m] = fmaf(t[q], ck, a[q][m]);
+                }
+            }
+            if (w == jj) {
+                const float sd = sqrtf(d), rs = __frcp_rn(sd);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int i = lane + 32 * (q & 1);
+                    if (q >= 2 || i > j)
+                        a[q][0] *= rs;
+                    else if (i == j)
+                        a[q][0] = sd;
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {  // rotate the window: the next group's column first
+            const float t0 = a[q][0];
+            a[q][0] = a[q][1];
+            a[q][1] = a[q][2];
+            a[q][2] = a[q][3];
+            a[q][3] = t0;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int i = lane + 32 * (q & 1);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const int c = w + 16 * m;
+            if (q < 2) {
+                if (i < k && c < k && i >= c) D[i + (size_t)c * ldd] = a[q][m];
+            } else {
+                G[i + CI_NB * c] = i <= c ? a[q][m] : 0.f;
+            }
+        }
+    }
+}
+
 }  // namespace
 
 namespace mg {
@@ -381,48 +480,43 @@ mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out)
 }
 
 // FP32 Cholesky for the mixed SPD solve (no counterpart in Mat, whose LLT,
-// LU/__LLT.h:94-150, is FP64): right-looking, blocks of 96 columns; the
-// diagonal block and the block column below it as in the FP32 Cholesky
-// (llt2_kernel, xlt_kernel), the trailing update C -= L21 L21^T on the
-// tensor cores from one split of L21 (split-BF16, `nterms` terms, fp32
-// accumulation, lower-order products first), which serves as both operands
-// (the B operand's rows are L21's rows).  The update covers the whole
-// trailing square; only its lower triangle is read later.  `split` holds
-// bf16x_split_bytes(n, 96, nterms).  info: first non-positive pivot (the
-// fp32 factorization of an SPD matrix can break down near singularity).
-mg_status_t spotrf_mixed(mg_handle_t h, int n, float* L, int ldl, int nterms, void* split, int* gemm_err,
-                         int* info_out) {
-    constexpr int NB = 64;
+// LU/__LLT.h:94-150, is FP64): right-looking, blocks of 64 columns.  Per
+// block: the diagonal block's Cholesky and its inverse transpose G = L^{-T}
+// in one CTA (chol_inv64_kernel); the block column below it as the product
+// X G, fused with the split of X into `nterms` BF16 terms; the trailing
+// update C -= X X^T on the tensor cores from that one split, which serves as
+// both operands (the B operand's rows are X's rows), restricted to the tiles
+// that meet the lower triangle (fp32 accumulation, lower-order products
+// first).  `split` holds bf16x_split_bytes(n, 64, nterms), `gblk` 64 x 64
+// floats.  info: first non-positive pivot (the fp32 factorization of an SPD
+// matrix can break down near singularity).
+mg_status_t spotrf_mixed(mg_handle_t h, int n, float* L, int ldl, int nterms, void* split, float* gblk,
+                         int* gemm_err, int* info_out) {
+    constexpr int NB = CI_NB;
     if (info_out) *info_out = 0;
     if (n == 0) return MG_OK;
     MG_TRY(ensure_hws(h, 64));
     int* dinfo = h->status;
     cudaStream_t st = h->stream;
     MG_CHECK_CUDA(h, cudaMemsetAsync(dinfo, 0, sizeof(int), st));
-    const size_t s2 = (size_t)LLT2_MAX * LLT2_MAX * sizeof(float);
-    MG_CHECK_CUDA(h, cudaFuncSetAttribute(llt2_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
     for (int j = 0; j < n; j += NB) {
         const int nb = n - j < NB ? n - j : NB;
         float* D = L + j + (size_t)j * ldl;
         {
-            ProfScope prof(h, "potrf_diag_f32", (double)nb * nb * nb / 3.0, 8.0 * nb * nb);
-            llt2_kernel<float><<<1, LLT2_THREADS, s2, st>>>(D, ldl, nb, j, dinfo);
-            MG_TRY(post_launch(h, "llt2_kernel"));
+            ProfScope prof(h, "potrf_diag_f32", (double)nb * nb * nb, 8.0 * nb * nb);
+            chol_inv64_kernel<<<1, CI_THREADS, 0, st>>>(D, ldl, nb, j, gblk, dinfo);
+            MG_TRY(post_launch(h, "chol_inv64_kernel"));
         }
         if (j + nb >= n) break;
         const int rows = n - (j + nb);
         float* P = L + (j + nb) + (size_t)j * ldl;
         float* C = L + (j + nb) + (size_t)(j + nb) * ldl;
         {
-            ProfScope prof(h, "trsm_f32", (double)rows * nb * nb, 8.0 * rows * nb);
-            MG_TRY((launch_xlt<float, NB>(h, st, D, ldl, P, ldl, rows, nb)));
-        }
-        {
-            ProfScope prof(h, "split", 0.0, 2.0 * rows * nb * (4.0 + 2.0 * nterms));
-            MG_TRY(bf16x_split<float>(h, true, P, ldl, rows, nb, nterms, split));
+            ProfScope prof(h, "trsm_split_f32", 2.0 * rows * nb * nb, 8.0 * rows * nb + 2.0 * nterms * rows * nb);
+            MG_TRY(bf16x_xlt_split64(h, gblk, P, ldl, rows, nterms, split));
         }
         MG_TRY(bf16x_gemm_presplit(h, nterms, rows, rows, nb, -1.0f, split, split, 1.0f, C, ldl, gemm_err, 0, 0, 0,
-                                   true, true));
+                                   true, true, true));
     }
     int* hw = (int*)h->hws;
     MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -57,6 +57,26 @@ __device__ __constant__ int kProdB[6] = {0, 1, 2, 0, 1, 0};
 __device__ __forceinline__ int prod_a(int np, int p) { return np == 3 ? kProdA[p] : np == 2 ? (p == 0 ? 1 : 0) : 0; }
 __device__ __forceinline__ int prod_b(int np, int p) { return np == 3 ? kProdB[p] : np == 2 ? (p == 1 ? 1 : 0) : 0; }
 
+// Lower mode (a symmetric update of which only the lower triangle is kept):
+// the tiles that meet the triangle row >= column, by column blocks; column
+// block nb (columns nb*BN ..) meets it from m-block nb*BN/BM on.
+static_assert(BN % BM == 0, "lower mode assumes whole m-blocks per column block");
+constexpr int BN_BM = BN / BM;
+__host__ __device__ __forceinline__ int lower_tiles(int num_m, int num_n) {
+    int total = 0;
+    for (int nb = 0; nb < num_n; ++nb) total += num_m > BN_BM * nb ? num_m - BN_BM * nb : 0;
+    return total;
+}
+__device__ __forceinline__ void tile_coords_lower(int t, int num_m, int num_n, int& mb, int& nb) {
+    nb = 0;
+    for (; nb < num_n - 1; ++nb) {
+        const int cnt = num_m > BN_BM * nb ? num_m - BN_BM * nb : 0;
+        if (t < cnt) break;
+        t -= cnt;
+    }
+    mb = BN_BM * nb + t;
+}
+
 __device__ __forceinline__ void tile_coords(int t, int num_m, int num_n, int& mb, int& nb) {
     // grouped raster: 16 m-blocks per group, n fastest inside the group
     constexpr int GM = 16;
@@ -124,7 +144,7 @@ template <int NP>
 __global__ void __launch_bounds__(THREADS, 1)
     bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       float* __restrict__ C, int ldc, int M, int N, int Kp, float alpha, float beta,
-                      int stream_c, int two_pass, int* __restrict__ err) {
+                      int stream_c, int two_pass, int lower, int* __restrict__ err) {
     using CF = Cfg<NP>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -139,7 +159,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int num_m = (M + BM - 1) / BM, num_n = (N + BN - 1) / BN;
-    const int total = num_m * num_n;
+    const int total = lower ? lower_tiles(num_m, num_n) : num_m * num_n;
     const int kblocks = Kp / BK;
     // two_pass (NP >= 2): every k-block's lower-order products first, then
     // a second pass over K for the leading product A_0 B_0 alone, so that
@@ -182,7 +202,10 @@ __global__ void __launch_bounds__(THREADS, 1)
             bool ok = true;
             for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
                 int mb, nb;
-                tile_coords(t, num_m, num_n, mb, nb);
+                if (lower)
+                    tile_coords_lower(t, num_m, num_n, mb, nb);
+                else
+                    tile_coords(t, num_m, num_n, mb, nb);
                 for (int ks = 0; ks < npass * kblocks && ok; ++ks) {
                     const int kb = ks % kblocks;
                     // the leading-product pass needs only the terms A_0, B_0
@@ -286,7 +309,10 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             tc::tc_fence_after();
             int mb, nb;
-            tile_coords(t, num_m, num_n, mb, nb);
+            if (lower)
+                tile_coords_lower(t, num_m, num_n, mb, nb);
+            else
+                tile_coords(t, num_m, num_n, mb, nb);
             const int row = mb * BM + row_in_tile;
             const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN);
             // Software-pipelined by chunks of 32 columns: the C values of chunk
@@ -366,6 +392,83 @@ __global__ void split_cols_kernel(const TIN* __restrict__ B, int ldb, int K, int
         out[e] = h0;
         if (np > 1) out[part_stride + e] = h1;
         if (np > 2) out[2 * part_stride + e] = h2;
+    }
+}
+
+// X (rows x 64, ld ldx) := X G in FP32, G = L^{-T} (64 x 64 upper
+// triangular, column-major, ld 64), and the split terms of the result as a
+// K = 64 operand (parts[p][row][64]), in one pass: one CTA per 64 rows,
+// each thread 4 rows x 4 columns of the product over the X tile and G staged
+// in shared memory (G with a pitch of 65 words: the two column groups of a
+// warp read different banks), then the result staged again (pitch 65) for
+// the coalesced column stores of X and the 16-byte row stores of the terms.
+// This is the block-column solve X := X L^{-T} of the mixed SPD
+// factorization as a product by the diagonal block's inverse.
+constexpr int XS_ROWS = 64;
+constexpr int XS_P = 65;
+
+__global__ void __launch_bounds__(256) xlt_split64_kernel(const float* __restrict__ G, float* __restrict__ X, int ldx,
+                                                          int rows, int np, __nv_bfloat16* __restrict__ out,
+                                                          size_t part_stride) {
+    __shared__ __align__(16) float sm[XS_P * 64 + 64 * XS_ROWS];
+    float* const gs = sm;              // G(k, c) at k + XS_P c
+    float* const xs = sm + XS_P * 64;  // X(r, k) at r + 64 k
+    const int t = threadIdx.x;
+    const int row0 = blockIdx.x * XS_ROWS;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+        const int e = t + 256 * u, r = e & 63, c = e >> 6;
+        gs[r + XS_P * c] = __ldg(G + e);
+        xs[e] = row0 + r < rows ? X[(size_t)(row0 + r) + (size_t)c * ldx] : 0.f;
+    }
+    __syncthreads();
+    const int tx = t & 15, ty = t >> 4;  // rows 4 tx .. 4 tx + 3, columns 4 ty .. 4 ty + 3
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+#pragma unroll 8
+    for (int k = 0; k < 64; ++k) {
+        const float4 xv = *reinterpret_cast<const float4*>(xs + 64 * k + 4 * tx);
+        const float xr[4] = {xv.x, xv.y, xv.z, xv.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float g = gs[k + XS_P * (4 * ty + j)];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[i][j] = fmaf(xr[i], g, acc[i][j]);
+        }
+    }
+    __syncthreads();
+    float* const os = sm;  // result (r, c) at r * XS_P + c
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) os[(4 * tx + i) * XS_P + 4 * ty + j] = acc[i][j];
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+        const int e = t + 256 * u, r = e & 63, c = e >> 6;
+        if (row0 + r < rows) X[(size_t)(row0 + r) + (size_t)c * ldx] = os[r * XS_P + c];
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        const int e = t + 256 * u, r = e >> 3, c8 = (e & 7) * 8;
+        if (row0 + r >= rows) continue;
+        uint32_t w0[4], w1[4], w2[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            __nv_bfloat16 a0, a1, a2, b0, b1, b2;
+            split3(os[r * XS_P + c8 + 2 * v], a0, a1, a2);
+            split3(os[r * XS_P + c8 + 2 * v + 1], b0, b1, b2);
+            w0[v] = (uint32_t)__bfloat16_as_ushort(a0) | ((uint32_t)__bfloat16_as_ushort(b0) << 16);
+            w1[v] = (uint32_t)__bfloat16_as_ushort(a1) | ((uint32_t)__bfloat16_as_ushort(b1) << 16);
+            w2[v] = (uint32_t)__bfloat16_as_ushort(a2) | ((uint32_t)__bfloat16_as_ushort(b2) << 16);
+        }
+        const size_t o = (size_t)(row0 + r) * 64 + c8;
+        *reinterpret_cast<uint4*>(out + o) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+        if (np > 1) *reinterpret_cast<uint4*>(out + part_stride + o) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+        if (np > 2) *reinterpret_cast<uint4*>(out + 2 * part_stride + o) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
     }
 }
 
@@ -519,14 +622,15 @@ bool make_map(CUtensorMap* map, const void* base, int rows, int Kp, int np, size
 template <int NP>
 mg_status_t launch_gemm_np(mg_handle_t h, const CUtensorMap& ma, const CUtensorMap& mb, float* C, int ldc, int M,
                            int N, int Kp, float alpha, float beta, int* err, int max_ctas, int stream_c,
-                           int two_pass) {
+                           int two_pass, int lower) {
     auto kern = bf16x_gemm_kernel<NP>;
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<NP>::SMEM));
-    const int tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+    const int num_m = (M + BM - 1) / BM, num_n = (N + BN - 1) / BN;
+    const int tiles = lower ? lower_tiles(num_m, num_n) : num_m * num_n;
     const int cap = max_ctas > 0 && max_ctas < h->num_sms ? max_ctas : h->num_sms;
     const int grid = tiles < cap ? tiles : cap;
     kern<<<grid, THREADS, Cfg<NP>::SMEM, h->stream>>>(ma, mb, C, ldc, M, N, Kp, alpha, beta, stream_c, two_pass,
-                                                       err);
+                                                       lower, err);
     return mg::post_launch(h, "bf16x_gemm_kernel");
 }
 
@@ -559,6 +663,14 @@ mg_status_t bf16x_split(mg_handle_t h, bool a_side, const TIN* X, int ldx, int r
     return post_launch(h, "split_cols_kernel");
 }
 template mg_status_t bf16x_split<float>(mg_handle_t, bool, const float*, int, int, int, int, void*);
+mg_status_t bf16x_xlt_split64(mg_handle_t h, const float* G, float* X, int ldx, int rows, int np, void* out) {
+    if (rows <= 0) return MG_OK;
+    static_assert(64 % BK == 0, "a 64-column operand needs no K padding");
+    xlt_split64_kernel<<<(rows + XS_ROWS - 1) / XS_ROWS, 256, 0, h->stream>>>(G, X, ldx, rows, np,
+                                                                              (__nv_bfloat16*)out, (size_t)rows * 64);
+    return post_launch(h, "xlt_split64_kernel");
+}
+
 template mg_status_t bf16x_split<double>(mg_handle_t, bool, const double*, int, int, int, int, void*);
 
 mg_status_t bf16x_trsm_split(mg_handle_t h, const float* L11, int lda, float* A12, int nt, int w, int np, void* out) {
@@ -576,8 +688,9 @@ int bf16x_kpad(int K) { return (K + BK - 1) / BK * BK; }
 
 mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, float alpha, const void* Asplit,
                                 const void* Bsplit, float beta, float* C, int ldc, int* err, size_t a_term,
-                                size_t b_term, int max_ctas, bool stream_c, bool two_pass) {
+                                size_t b_term, int max_ctas, bool stream_c, bool two_pass, bool lower) {
     if (M == 0 || N == 0) return MG_OK;
+    if (lower && M != N) return fail(h, MG_ERR_ARG, "split GEMM: lower mode needs a square C (M=%d N=%d)", M, N);
     const int Kp = (K + BK - 1) / BK * BK;
     if (!a_term) a_term = (size_t)M * Kp;
     if (!b_term) b_term = (size_t)N * Kp;
@@ -586,14 +699,17 @@ mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, floa
         return fail(h, MG_ERR_CUDA, "cuTensorMapEncodeTiled failed (M=%d N=%d Kp=%d)", M, N, Kp);
     const int nprod = np == 3 ? 6 : np == 2 ? 3 : 1;
     // flops: every bf16 product the tensor cores execute; bytes: C read+write plus the split operands once
-    ProfScope prof(h, "gemm_bf16x", 2.0 * M * N * (double)Kp * nprod,
-                   (beta == 0.f ? 4.0 : 8.0) * M * N + 2.0 * np * (double)(M + N) * Kp);
+    // lower mode: the tiles meeting the lower triangle, about half of C
+    const double frac = lower ? (lower_tiles((M + BM - 1) / BM, (N + BN - 1) / BN) * (double)BM * BN) / ((double)M * N)
+                              : 1.0;
+    ProfScope prof(h, "gemm_bf16x", frac * 2.0 * M * N * (double)Kp * nprod,
+                   frac * (beta == 0.f ? 4.0 : 8.0) * M * N + 2.0 * np * (double)(M + N) * Kp);
     switch (np) {
-        case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, 0);
+        case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, 0, lower);
         case 2:
-            return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass);
+            return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass, lower);
         default:
-            return launch_gemm_np<3>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass);
+            return launch_gemm_np<3>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass, lower);
     }
 }
 

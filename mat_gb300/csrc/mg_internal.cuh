@@ -174,10 +174,16 @@ mg_status_t bf16x_split(mg_handle_t h, bool a_side, const TIN* X, int ldx, int r
 // read again soon (the next panel's columns).  two_pass: accumulate every
 // lower-order product over K before the leading one (a second pass over K
 // for A_0 B_0; about 6x less accumulation error, one third more operand
-// loads).
+// loads).  lower (M == N): only the tiles that meet C's lower triangle
+// (row >= column) are computed; tiles on the diagonal are computed whole.
 mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, float alpha, const void* Asplit,
                                 const void* Bsplit, float beta, float* C, int ldc, int* err, size_t a_term = 0,
-                                size_t b_term = 0, int max_ctas = 0, bool stream_c = true, bool two_pass = false);
+                                size_t b_term = 0, int max_ctas = 0, bool stream_c = true, bool two_pass = false,
+                                bool lower = false);
+// X (rows x 64, ld ldx) := X G (G: 64 x 64, column-major, ld 64) in FP32,
+// and the np split terms of the result as an operand with K = 64
+// (bf16x_split_bytes(rows, 64, np)).
+mg_status_t bf16x_xlt_split64(mg_handle_t h, const float* G, float* X, int ldx, int rows, int np, void* out);
 // K rounded up to the split GEMM's K step (elements per row of a split term).
 int bf16x_kpad(int K);
 // A12 (w x nt, ld lda) := L11^{-1} A12 with L11 (w x w, ld lda) unit lower,
@@ -202,8 +208,9 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
                          bool tourn = false);
 // FP32 Cholesky with split-BF16 trailing updates for the mixed SPD solve, and
 // the rewrite of its factor as the packed LU of the same matrix (chol.cu).
-mg_status_t spotrf_mixed(mg_handle_t h, int n, float* L, int ldl, int nterms, void* split, int* gemm_err,
-                         int* info_out);
+// split: bf16x_split_bytes(n, 64, nterms); gblk: 64 x 64 floats.
+mg_status_t spotrf_mixed(mg_handle_t h, int n, float* L, int ldl, int nterms, void* split, float* gblk,
+                         int* gemm_err, int* info_out);
 mg_status_t chol_to_lu_f32(mg_handle_t h, int n, float* A, int lda, float* dscratch);
 // Side stream and events of the look-ahead LU (created once per handle).
 mg_status_t ensure_lookahead(mg_handle_t h);

@@ -1200,7 +1200,7 @@ static mg_status_t mixed_solve(mg_handle_t h, int n, int nrhs, const double* A, 
         // Cholesky of the lower triangle, then L L^T as a packed LU with pos = identity
         pos_iota_kernel<<<(n + 255) / 256, 256, 0, st>>>(w.pos, n);
         MG_TRY(mg::post_launch(h, "pos_iota_kernel"));
-        s = mg::spotrf_mixed(h, n, w.A32, n, o.nterms, w.splitA, w.gemm_err, &info);
+        s = mg::spotrf_mixed(h, n, w.A32, n, o.nterms, w.splitA, w.Linv, w.gemm_err, &info);
         if (s != MG_OK && s != MG_NOT_SPD) return s;
         if (s == MG_NOT_SPD) {  // the fp32 Cholesky broke down: straight to the FP64 solve
             r.info = info;
