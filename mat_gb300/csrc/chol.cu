@@ -299,14 +299,29 @@ __global__ void chol_to_lu_lower_kernel(float* __restrict__ A, int lda, int n, c
 // owns (a window over its four rotated once per 16 columns, so that register
 // indices stay static in a rolled loop), and the owner scales its copy.  A
 // block narrower than 64 (the last one) is padded with the identity.  info:
-// first non-positive pivot (1-based, from col0).
+// first non-positive pivot (1-based, from col0).  With ntop > 0 the kernel
+// also forms Xt = P G for the first ntop rows P of the block column below
+// (ld ldd, rows ntop .. 63 of Xt zero), into xtop (64 x 64, ld 64), in the
+// same per-element order as xlt_split64_kernel (fmaf over k from 0), so
+// that Xt equals those rows of the block column's solve bit for bit.
 constexpr int CI_NB = 64;
 constexpr int CI_THREADS = 512;
+constexpr int CI_GP = CI_NB + 1;  // pitch of G in shared memory
 
 __global__ void __launch_bounds__(CI_THREADS) chol_inv64_kernel(float* __restrict__ D, int ldd, int k, int col0,
-                                                              float* __restrict__ G, int* __restrict__ info) {
+                                                              float* __restrict__ G, int* __restrict__ info,
+                                                              int ntop, float* __restrict__ xtop) {
     __shared__ float colv[2][2 * CI_NB];
+    __shared__ float gsm[CI_NB * CI_GP];  // G(k, c) at k + CI_GP c
+    __shared__ float psm[CI_NB * CI_NB];  // P(r, k) at r + 64 k
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (ntop > 0) {
+#pragma unroll
+        for (int u = 0; u < CI_NB * CI_NB / CI_THREADS; ++u) {
+            const int e = threadIdx.x + CI_THREADS * u, r = e & 63, c = e >> 6;
+            psm[e] = r < ntop ? D[CI_NB + r + (size_t)c * ldd] : 0.f;
+        }
+    }
     float a[4][4];  // [stacked row lane + 32 q: q < 2 in A, q >= 2 in I][window position]
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -379,10 +394,27 @@ __global__ void __launch_bounds__(CI_THREADS) chol_inv64_kernel(float* __restric
             if (q < 2) {
                 if (i < k && c < k && i >= c) D[i + (size_t)c * ldd] = a[q][m];
             } else {
-                G[i + CI_NB * c] = i <= c ? a[q][m] : 0.f;
+                const float g = i <= c ? a[q][m] : 0.f;
+                G[i + CI_NB * c] = g;
+                gsm[i + CI_GP * c] = g;
             }
         }
     }
+    if (ntop <= 0) return;
+    __syncthreads();
+    // Xt = P G: thread r = t % 64 and the 8 columns 8 (t / 64) ..
+    const int r = threadIdx.x & 63, c0 = (threadIdx.x >> 6) * 8;
+    float acc[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc[u] = 0.f;
+#pragma unroll 4
+    for (int kk = 0; kk < CI_NB; ++kk) {
+        const float x = psm[r + CI_NB * kk];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc[u] = fmaf(x, gsm[kk + CI_GP * (c0 + u)], acc[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) xtop[r + CI_NB * (c0 + u)] = acc[u];
 }
 
 }  // namespace
@@ -482,42 +514,67 @@ mg_status_t dpotrf_impl(mg_handle_t h, int n, double* L, int ldl, int* info_out)
 // FP32 Cholesky for the mixed SPD solve (no counterpart in Mat, whose LLT,
 // LU/__LLT.h:94-150, is FP64): right-looking, blocks of 64 columns.  Per
 // block: the diagonal block's Cholesky and its inverse transpose G = L^{-T}
-// in one CTA (chol_inv64_kernel); the block column below it as the product
-// X G, fused with the split of X into `nterms` BF16 terms; the trailing
-// update C -= X X^T on the tensor cores from that one split, which serves as
-// both operands (the B operand's rows are X's rows), restricted to the tiles
-// that meet the lower triangle (fp32 accumulation, lower-order products
-// first).  `split` holds bf16x_split_bytes(n, 64, nterms), `gblk` 64 x 64
-// floats.  info: first non-positive pivot (the fp32 factorization of an SPD
-// matrix can break down near singularity).
+// in one CTA, with the product of G and the first 64 rows of the block
+// column below (chol_inv64_kernel); then one kernel for the block column X
+// := X G, the split of X into `nterms` BF16 terms and, in FP32, the update
+// of the next block column by X and those first rows (xlt_split64_kernel);
+// then the rest of the trailing update, C -= X X^T on the tensor cores from
+// the one split, which serves as both operands (the B operand's rows are
+// X's rows; fp32 accumulation, lower-order products first), restricted to
+// the tiles that meet the lower triangle, on the side stream with one SM
+// left free, where the next diagonal block's kernel runs beside it.  The
+// next block column's kernel waits for it (it holds the other SMs and reads
+// the split that kernel rewrites).  `split` holds bf16x_split_bytes(n, 64,
+// nterms), `gblk` 2 x 64 x 64 floats.  info: first non-positive pivot (the
+// fp32 factorization of an SPD matrix can break down near singularity).
 mg_status_t spotrf_mixed(mg_handle_t h, int n, float* L, int ldl, int nterms, void* split, float* gblk,
                          int* gemm_err, int* info_out) {
     constexpr int NB = CI_NB;
     if (info_out) *info_out = 0;
     if (n == 0) return MG_OK;
     MG_TRY(ensure_hws(h, 64));
+    MG_TRY(ensure_lookahead(h));
     int* dinfo = h->status;
     cudaStream_t st = h->stream;
     MG_CHECK_CUDA(h, cudaMemsetAsync(dinfo, 0, sizeof(int), st));
+    float* const xtop = gblk + NB * NB;
+    bool far_pending = false;
     for (int j = 0; j < n; j += NB) {
         const int nb = n - j < NB ? n - j : NB;
+        const int rows = n - (j + nb);
+        const int ntop = rows < NB ? rows : NB;  // the next block column
         float* D = L + j + (size_t)j * ldl;
         {
-            ProfScope prof(h, "potrf_diag_f32", (double)nb * nb * nb, 8.0 * nb * nb);
-            chol_inv64_kernel<<<1, CI_THREADS, 0, st>>>(D, ldl, nb, j, gblk, dinfo);
+            ProfScope prof(h, "potrf_diag_f32", (double)nb * nb * nb + 2.0 * ntop * nb * nb, 8.0 * nb * nb);
+            chol_inv64_kernel<<<1, CI_THREADS, 0, st>>>(D, ldl, nb, j, gblk, dinfo, ntop, xtop);
             MG_TRY(post_launch(h, "chol_inv64_kernel"));
         }
-        if (j + nb >= n) break;
-        const int rows = n - (j + nb);
+        if (rows == 0) break;
         float* P = L + (j + nb) + (size_t)j * ldl;
         float* C = L + (j + nb) + (size_t)(j + nb) * ldl;
+        if (far_pending) MG_CHECK_CUDA(h, cudaStreamWaitEvent(st, h->la_ev[1], 0));
+        far_pending = false;
         {
-            ProfScope prof(h, "trsm_split_f32", 2.0 * rows * nb * nb, 8.0 * rows * nb + 2.0 * nterms * rows * nb);
-            MG_TRY(bf16x_xlt_split64(h, gblk, P, ldl, rows, nterms, split));
+            ProfScope prof(h, "trsm_split_f32", 2.0 * rows * nb * (nb + ntop),
+                           16.0 * rows * nb + 2.0 * nterms * rows * nb);
+            MG_TRY(bf16x_xlt_split64(h, gblk, P, ldl, rows, nterms, split, xtop, ntop, C));
         }
-        MG_TRY(bf16x_gemm_presplit(h, nterms, rows, rows, nb, -1.0f, split, split, 1.0f, C, ldl, gemm_err, 0, 0, 0,
-                                   true, true, true));
+        if (rows > ntop) {
+            MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[0], st));
+            MG_CHECK_CUDA(h, cudaStreamWaitEvent(h->la_stream, h->la_ev[0], 0));
+            {
+                OnStream on(h, h->la_stream);
+                const size_t term = (size_t)rows * NB;  // elements per split term
+                const uint16_t* xs = (const uint16_t*)split + (size_t)ntop * NB;  // rows ntop .. of the split
+                MG_TRY(bf16x_gemm_presplit(h, nterms, rows - ntop, rows - ntop, nb, -1.0f, xs, xs, 1.0f,
+                                           C + ntop + (size_t)ntop * ldl, ldl, gemm_err, term, term, h->num_sms - 1,
+                                           true, true, true));
+                MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[1], h->la_stream));
+            }
+            far_pending = true;
+        }
     }
+    if (far_pending) MG_CHECK_CUDA(h, cudaStreamWaitEvent(st, h->la_ev[1], 0));
     int* hw = (int*)h->hws;
     MG_CHECK_CUDA(h, cudaMemcpyAsync(hw, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
     MG_CHECK_CUDA(h, cudaStreamSynchronize(st));

@@ -396,23 +396,32 @@ __global__ void split_cols_kernel(const TIN* __restrict__ B, int ldb, int K, int
 }
 
 // X (rows x 64, ld ldx) := X G in FP32, G = L^{-T} (64 x 64 upper
-// triangular, column-major, ld 64), and the split terms of the result as a
-// K = 64 operand (parts[p][row][64]), in one pass: one CTA per 64 rows,
-// each thread 4 rows x 4 columns of the product over the X tile and G staged
-// in shared memory (G with a pitch of 65 words: the two column groups of a
-// warp read different banks), then the result staged again (pitch 65) for
-// the coalesced column stores of X and the 16-byte row stores of the terms.
-// This is the block-column solve X := X L^{-T} of the mixed SPD
-// factorization as a product by the diagonal block's inverse.
+// triangular, column-major, ld 64), the split terms of the result as a
+// K = 64 operand (parts[p][row][64]), and, with ntop > 0, the update of the
+// next block column C (rows x ntop, ld ldx) -= X Xt^T in FP32, Xt (64 x 64,
+// ld 64; rows ntop .. zero) being the first ntop rows of the result, formed
+// beforehand by the diagonal block's kernel.  One CTA per 64 rows; each
+// thread 4 rows x 4 columns of both products, over the X tile, G (pitch 65
+// words: the two column groups of a warp read different banks) and Xt
+// staged in shared memory; the result staged again (column-major, pitch 68
+// for 16-byte accesses) for the coalesced column stores of X, the 16-byte
+// row stores of the terms and the second product.  This is the block-column
+// solve X := X L^{-T} of the mixed SPD factorization as a product by the
+// diagonal block's inverse, with the look-ahead part of the trailing update.
 constexpr int XS_ROWS = 64;
 constexpr int XS_P = 65;
+constexpr int XS_OP = 68;
+constexpr size_t XS_SMEM = (size_t)(XS_P * 64 + 64 * XS_ROWS + 64 * 64) * sizeof(float);
 
 __global__ void __launch_bounds__(256) xlt_split64_kernel(const float* __restrict__ G, float* __restrict__ X, int ldx,
                                                           int rows, int np, __nv_bfloat16* __restrict__ out,
-                                                          size_t part_stride) {
-    __shared__ __align__(16) float sm[XS_P * 64 + 64 * XS_ROWS];
-    float* const gs = sm;              // G(k, c) at k + XS_P c
-    float* const xs = sm + XS_P * 64;  // X(r, k) at r + 64 k
+                                                          size_t part_stride, const float* __restrict__ xtop,
+                                                          int ntop, float* __restrict__ C) {
+    extern __shared__ __align__(16) float xs_sm[];
+    float* const gs = xs_sm;                      // G(k, c) at k + XS_P c
+    float* const xs = xs_sm + XS_P * 64;          // X(r, k) at r + 64 k
+    float* const xt = xs + 64 * XS_ROWS;          // Xt(c, k) at c + 64 k
+    float* const os = xs_sm;                      // result (r, c) at r + XS_OP c, after the first product
     const int t = threadIdx.x;
     const int row0 = blockIdx.x * XS_ROWS;
 #pragma unroll
@@ -420,6 +429,7 @@ __global__ void __launch_bounds__(256) xlt_split64_kernel(const float* __restric
         const int e = t + 256 * u, r = e & 63, c = e >> 6;
         gs[r + XS_P * c] = __ldg(G + e);
         xs[e] = row0 + r < rows ? X[(size_t)(row0 + r) + (size_t)c * ldx] : 0.f;
+        if (ntop > 0) xt[e] = __ldg(xtop + e);
     }
     __syncthreads();
     const int tx = t & 15, ty = t >> 4;  // rows 4 tx .. 4 tx + 3, columns 4 ty .. 4 ty + 3
@@ -440,27 +450,26 @@ __global__ void __launch_bounds__(256) xlt_split64_kernel(const float* __restric
         }
     }
     __syncthreads();
-    float* const os = sm;  // result (r, c) at r * XS_P + c
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) os[(4 * tx + i) * XS_P + 4 * ty + j] = acc[i][j];
+    for (int j = 0; j < 4; ++j)
+        *reinterpret_cast<float4*>(os + XS_OP * (4 * ty + j) + 4 * tx) =
+            make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
     __syncthreads();
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
         const int e = t + 256 * u, r = e & 63, c = e >> 6;
-        if (row0 + r < rows) X[(size_t)(row0 + r) + (size_t)c * ldx] = os[r * XS_P + c];
+        if (row0 + r < rows) X[(size_t)(row0 + r) + (size_t)c * ldx] = os[r + XS_OP * c];
     }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
-        const int e = t + 256 * u, r = e >> 3, c8 = (e & 7) * 8;
+        const int e = t + 256 * u, r = e & 63, c8 = (e >> 6) * 8;
         if (row0 + r >= rows) continue;
         uint32_t w0[4], w1[4], w2[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
             __nv_bfloat16 a0, a1, a2, b0, b1, b2;
-            split3(os[r * XS_P + c8 + 2 * v], a0, a1, a2);
-            split3(os[r * XS_P + c8 + 2 * v + 1], b0, b1, b2);
+            split3(os[r + XS_OP * (c8 + 2 * v)], a0, a1, a2);
+            split3(os[r + XS_OP * (c8 + 2 * v + 1)], b0, b1, b2);
             w0[v] = (uint32_t)__bfloat16_as_ushort(a0) | ((uint32_t)__bfloat16_as_ushort(b0) << 16);
             w1[v] = (uint32_t)__bfloat16_as_ushort(a1) | ((uint32_t)__bfloat16_as_ushort(b1) << 16);
             w2[v] = (uint32_t)__bfloat16_as_ushort(a2) | ((uint32_t)__bfloat16_as_ushort(b2) << 16);
@@ -470,6 +479,37 @@ __global__ void __launch_bounds__(256) xlt_split64_kernel(const float* __restric
         if (np > 1) *reinterpret_cast<uint4*>(out + part_stride + o) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
         if (np > 2) *reinterpret_cast<uint4*>(out + 2 * part_stride + o) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
     }
+    if (ntop <= 0) return;
+    // C(r, c) -= sum_k X(r, k) Xt(c, k) for the next block column
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+#pragma unroll 8
+    for (int k = 0; k < 64; ++k) {
+        const float4 xv = *reinterpret_cast<const float4*>(os + XS_OP * k + 4 * tx);
+        const float4 tv = *reinterpret_cast<const float4*>(xt + 64 * k + 4 * ty);
+        const float xr[4] = {xv.x, xv.y, xv.z, xv.w}, tr[4] = {tv.x, tv.y, tv.z, tv.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[i][j] = fmaf(xr[i], tr[j], acc[i][j]);
+    }
+    float cv[4][4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = row0 + 4 * tx + i, c = 4 * ty + j;
+            cv[i][j] = (r < rows && c < ntop) ? C[(size_t)r + (size_t)c * ldx] : 0.f;
+        }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = row0 + 4 * tx + i, c = 4 * ty + j;
+            if (r < rows && c < ntop) C[(size_t)r + (size_t)c * ldx] = cv[i][j] - acc[i][j];
+        }
 }
 
 // U12 := L11^{-1} A12 (FP32, L11 unit lower w x w, w <= 128) and the split
@@ -663,11 +703,14 @@ mg_status_t bf16x_split(mg_handle_t h, bool a_side, const TIN* X, int ldx, int r
     return post_launch(h, "split_cols_kernel");
 }
 template mg_status_t bf16x_split<float>(mg_handle_t, bool, const float*, int, int, int, int, void*);
-mg_status_t bf16x_xlt_split64(mg_handle_t h, const float* G, float* X, int ldx, int rows, int np, void* out) {
+mg_status_t bf16x_xlt_split64(mg_handle_t h, const float* G, float* X, int ldx, int rows, int np, void* out,
+                              const float* xtop, int ntop, float* C) {
     if (rows <= 0) return MG_OK;
     static_assert(64 % BK == 0, "a 64-column operand needs no K padding");
-    xlt_split64_kernel<<<(rows + XS_ROWS - 1) / XS_ROWS, 256, 0, h->stream>>>(G, X, ldx, rows, np,
-                                                                              (__nv_bfloat16*)out, (size_t)rows * 64);
+    MG_CHECK_CUDA(h, cudaFuncSetAttribute(xlt_split64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)XS_SMEM));
+    xlt_split64_kernel<<<(rows + XS_ROWS - 1) / XS_ROWS, 256, XS_SMEM, h->stream>>>(
+        G, X, ldx, rows, np, (__nv_bfloat16*)out, (size_t)rows * 64, xtop, ntop, C);
     return post_launch(h, "xlt_split64_kernel");
 }
 

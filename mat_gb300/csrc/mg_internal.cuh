@@ -181,9 +181,12 @@ mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, floa
                                 size_t b_term = 0, int max_ctas = 0, bool stream_c = true, bool two_pass = false,
                                 bool lower = false);
 // X (rows x 64, ld ldx) := X G (G: 64 x 64, column-major, ld 64) in FP32,
-// and the np split terms of the result as an operand with K = 64
-// (bf16x_split_bytes(rows, 64, np)).
-mg_status_t bf16x_xlt_split64(mg_handle_t h, const float* G, float* X, int ldx, int rows, int np, void* out);
+// the np split terms of the result as an operand with K = 64
+// (bf16x_split_bytes(rows, 64, np)), and with ntop > 0 the FP32 update
+// C (rows x ntop, ld ldx) -= X Xt^T, Xt (64 x 64, ld 64) holding the first
+// ntop rows of the result.
+mg_status_t bf16x_xlt_split64(mg_handle_t h, const float* G, float* X, int ldx, int rows, int np, void* out,
+                              const float* xtop, int ntop, float* C);
 // K rounded up to the split GEMM's K step (elements per row of a split term).
 int bf16x_kpad(int K);
 // A12 (w x nt, ld lda) := L11^{-1} A12 with L11 (w x w, ld lda) unit lower,
@@ -208,7 +211,7 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
                          bool tourn = false);
 // FP32 Cholesky with split-BF16 trailing updates for the mixed SPD solve, and
 // the rewrite of its factor as the packed LU of the same matrix (chol.cu).
-// split: bf16x_split_bytes(n, 64, nterms); gblk: 64 x 64 floats.
+// split: bf16x_split_bytes(n, 64, nterms); gblk: 2 x 64 x 64 floats.
 mg_status_t spotrf_mixed(mg_handle_t h, int n, float* L, int ldl, int nterms, void* split, float* gblk,
                          int* gemm_err, int* info_out);
 mg_status_t chol_to_lu_f32(mg_handle_t h, int n, float* A, int lda, float* dscratch);
