@@ -568,7 +568,7 @@ mg_status_t spotrf_mixed(mg_handle_t h, int n, float* L, int ldl, int nterms, vo
                 const uint16_t* xs = (const uint16_t*)split + (size_t)ntop * NB;  // rows ntop .. of the split
                 MG_TRY(bf16x_gemm_presplit(h, nterms, rows - ntop, rows - ntop, nb, -1.0f, xs, xs, 1.0f,
                                            C + ntop + (size_t)ntop * ldl, ldl, gemm_err, term, term, h->num_sms - 1,
-                                           true, true, true));
+                                           true, true, true, true));
                 MG_CHECK_CUDA(h, cudaEventRecord(h->la_ev[1], h->la_stream));
             }
             far_pending = true;

@@ -41,14 +41,19 @@ constexpr int EPI_WARPS = 8;  // two per TMEM lane quarter, each half of the til
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
 constexpr int TMEM_COLS = 512;
 
-template <int NP>
+// RED: the epilogue adds alpha * (A B) into C with TMA reductions (beta = 1)
+// from two 32 x 32 staging buffers per epilogue warp, which take the shared
+// memory of one or more operand stages.
+template <int NP, bool RED = false>
 struct Cfg {
     static constexpr int A_TILE = BM * BK * 2;                 // bytes per A term tile
     static constexpr int B_TILE = BN * BK * 2;                 // bytes per B term tile
     static constexpr int STAGE = NP * (A_TILE + B_TILE);
-    static constexpr int STAGES = NP == 3 ? 3 : NP == 2 ? 4 : 8;
+    static constexpr int STAGES = RED ? (NP == 3 ? 2 : NP == 2 ? 3 : 6) : (NP == 3 ? 3 : NP == 2 ? 4 : 8);
     static constexpr int NPROD = NP == 3 ? 6 : NP == 2 ? 3 : 1;
-    static constexpr size_t SMEM = (size_t)STAGES * STAGE + 1024 /*align*/ + 256 /*barriers*/;
+    static constexpr int EPI_BUF = 32 * 32 * 4;                // one 32 x 32 fp32 chunk
+    static constexpr int EPI_BYTES = RED ? EPI_WARPS * 2 * EPI_BUF : 0;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE + EPI_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 };
 
 // Products (A term, B term), smallest first.
@@ -140,15 +145,16 @@ __device__ __forceinline__ void epi_store(bool wr, float* crow, int ldc, int col
     }
 }
 
-template <int NP>
+template <int NP, bool RED>
 __global__ void __launch_bounds__(THREADS, 1)
     bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                      float* __restrict__ C, int ldc, int M, int N, int Kp, float alpha, float beta,
-                      int stream_c, int two_pass, int lower, int* __restrict__ err) {
-    using CF = Cfg<NP>;
+                      const __grid_constant__ CUtensorMap tmC, float* __restrict__ C, int ldc, int M, int N, int Kp,
+                      float alpha, float beta, int stream_c, int two_pass, int lower, int* __restrict__ err) {
+    using CF = Cfg<NP, RED>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t* bars = (uint64_t*)(smem + (size_t)CF::STAGES * CF::STAGE);
+    float* const epi_sm = (float*)(smem + (size_t)CF::STAGES * CF::STAGE);  // RED staging
+    uint64_t* bars = (uint64_t*)(smem + (size_t)CF::STAGES * CF::STAGE + CF::EPI_BYTES);
     uint64_t* full = bars;
     uint64_t* empty = bars + CF::STAGES;
     uint64_t* acc_full = bars + 2 * CF::STAGES;
@@ -181,6 +187,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         tc::fence_barrier_init();
         tc::prefetch_tmap(&tmA);
         tc::prefetch_tmap(&tmB);
+        if (RED) tc::prefetch_tmap(&tmC);
     }
     if (warp == 1) {
         tc::tmem_alloc(tmem_slot, TMEM_COLS);
@@ -300,6 +307,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         constexpr int CH_PER = BN / 32 / (EPI_WARPS / 4);  // 32-column chunks per warp
         const int ch0 = ((warp - 2) / 4) * CH_PER;           // this warp's first chunk
         int it = 0;
+        int nred = 0;  // RED: reductions issued by this warp (alternating staging buffers)
         for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
             const int buf = it & 1;
             if (!tc::mbar_wait(&acc_full[buf], (it >> 1) & 1) || *(volatile int*)&s_abort) {
@@ -315,6 +323,34 @@ __global__ void __launch_bounds__(THREADS, 1)
                 tile_coords(t, num_m, num_n, mb, nb);
             const int row = mb * BM + row_in_tile;
             const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN);
+            if constexpr (RED) {
+                // each 32 x 32 chunk: accumulator -> staging buffer (lane = row,
+                // column-major like the tensor map's box) -> one TMA reduction
+                // into C, which clips rows >= M and columns >= N; the buffer's
+                // previous reduction must have read it first
+                float* const wbuf = epi_sm + (size_t)(warp - 2) * 2 * 1024;
+#pragma unroll 1
+                for (int ch = ch0; ch < ch0 + CH_PER; ++ch) {
+                    if (nb * BN + ch * 32 >= N || mb * BM + q * 32 >= M) continue;  // outside C
+                    uint32_t r[32];
+                    tc::tmem_ld_32x32b_x32(taddr + ch * 32, r);
+                    tc::tmem_ld_wait();
+                    float* const sb = wbuf + (nred++ & 1) * 1024;
+                    if (lane == 0) tc::bulk_wait_group_read<1>();
+                    __syncwarp();
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) sb[j * 32 + lane] = alpha * __uint_as_float(r[j]);
+                    tc::fence_proxy_async_shared();
+                    __syncwarp();
+                    if (lane == 0) {
+                        tc::tma_reduce_add_2d(&tmC, sb, mb * BM + q * 32, nb * BN + ch * 32);
+                        tc::bulk_commit_group();
+                    }
+                }
+                tc::tc_fence_before();
+                tc::mbar_arrive(&acc_empty[buf]);
+                continue;
+            }
             // Software-pipelined by chunks of 32 columns: the C values of chunk
             // ch+1 are loaded (32 independent loads per thread in flight) before
             // chunk ch is combined with the accumulator and stored.
@@ -336,6 +372,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
     }
 
+    if (RED && warp >= 2 && lane == 0) tc::bulk_wait_group<0>();  // every reduction complete
     tc::tc_fence_before();
     __syncthreads();
     if (warp == 1) {
@@ -659,18 +696,45 @@ bool make_map(CUtensorMap* map, const void* base, int rows, int Kp, int np, size
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+bool make_cmap(CUtensorMap* map, float* C, int ldc, int M, int N) {
+    EncodeTiledFn enc = get_encode();
+    if (!enc) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)M, (cuuint64_t)N};
+    cuuint64_t strides[1] = {(cuuint64_t)ldc * 4};
+    cuuint32_t box[2] = {32, 32};
+    cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, C, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <int NP>
 mg_status_t launch_gemm_np(mg_handle_t h, const CUtensorMap& ma, const CUtensorMap& mb, float* C, int ldc, int M,
                            int N, int Kp, float alpha, float beta, int* err, int max_ctas, int stream_c,
-                           int two_pass, int lower) {
-    auto kern = bf16x_gemm_kernel<NP>;
-    MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<NP>::SMEM));
+                           int two_pass, int lower, bool red_epi) {
     const int num_m = (M + BM - 1) / BM, num_n = (N + BN - 1) / BN;
     const int tiles = lower ? lower_tiles(num_m, num_n) : num_m * num_n;
     const int cap = max_ctas > 0 && max_ctas < h->num_sms ? max_ctas : h->num_sms;
     const int grid = tiles < cap ? tiles : cap;
-    kern<<<grid, THREADS, Cfg<NP>::SMEM, h->stream>>>(ma, mb, C, ldc, M, N, Kp, alpha, beta, stream_c, two_pass,
-                                                       lower, err);
+    CUtensorMap mc;
+    // the TMA-reduction epilogue when asked for (beta = 1, C 16-byte
+    // aligned, ldc a multiple of 4 floats)
+    const bool red = red_epi && beta == 1.f && ((uintptr_t)C & 15) == 0 && (ldc & 3) == 0 &&
+                     make_cmap(&mc, C, ldc, M, N);
+    if (red) {
+        auto kern = bf16x_gemm_kernel<NP, true>;
+        MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)Cfg<NP, true>::SMEM));
+        kern<<<grid, THREADS, Cfg<NP, true>::SMEM, h->stream>>>(ma, mb, mc, C, ldc, M, N, Kp, alpha, beta, stream_c,
+                                                                two_pass, lower, err);
+    } else {
+        std::memset(&mc, 0, sizeof(mc));
+        auto kern = bf16x_gemm_kernel<NP, false>;
+        MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)Cfg<NP, false>::SMEM));
+        kern<<<grid, THREADS, Cfg<NP, false>::SMEM, h->stream>>>(ma, mb, mc, C, ldc, M, N, Kp, alpha, beta, stream_c,
+                                                                 two_pass, lower, err);
+    }
     return mg::post_launch(h, "bf16x_gemm_kernel");
 }
 
@@ -731,7 +795,8 @@ int bf16x_kpad(int K) { return (K + BK - 1) / BK * BK; }
 
 mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, float alpha, const void* Asplit,
                                 const void* Bsplit, float beta, float* C, int ldc, int* err, size_t a_term,
-                                size_t b_term, int max_ctas, bool stream_c, bool two_pass, bool lower) {
+                                size_t b_term, int max_ctas, bool stream_c, bool two_pass, bool lower,
+                                bool red_epi) {
     if (M == 0 || N == 0) return MG_OK;
     if (lower && M != N) return fail(h, MG_ERR_ARG, "split GEMM: lower mode needs a square C (M=%d N=%d)", M, N);
     const int Kp = (K + BK - 1) / BK * BK;
@@ -748,11 +813,11 @@ mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, floa
     ProfScope prof(h, "gemm_bf16x", frac * 2.0 * M * N * (double)Kp * nprod,
                    frac * (beta == 0.f ? 4.0 : 8.0) * M * N + 2.0 * np * (double)(M + N) * Kp);
     switch (np) {
-        case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, 0, lower);
+        case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, 0, lower, red_epi);
         case 2:
-            return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass, lower);
+            return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass, lower, red_epi);
         default:
-            return launch_gemm_np<3>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass, lower);
+            return launch_gemm_np<3>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass, lower, red_epi);
     }
 }
 

@@ -176,10 +176,15 @@ mg_status_t bf16x_split(mg_handle_t h, bool a_side, const TIN* X, int ldx, int r
 // for A_0 B_0; about 6x less accumulation error, one third more operand
 // loads).  lower (M == N): only the tiles that meet C's lower triangle
 // (row >= column) are computed; tiles on the diagonal are computed whole.
+// red_epi (used when beta == 1, C is 16-byte aligned and ldc a multiple of
+// 4): the epilogue adds alpha * A B into C by TMA reductions from shared
+// memory instead of loading C into registers; faster for a C that streams
+// through HBM, but its L2 traffic slowed a latency-bound kernel running
+// beside it (the LU's panel beside its far update).
 mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, float alpha, const void* Asplit,
                                 const void* Bsplit, float beta, float* C, int ldc, int* err, size_t a_term = 0,
                                 size_t b_term = 0, int max_ctas = 0, bool stream_c = true, bool two_pass = false,
-                                bool lower = false);
+                                bool lower = false, bool red_epi = false);
 // X (rows x 64, ld ldx) := X G (G: 64 x 64, column-major, ld 64) in FP32,
 // the np split terms of the result as an operand with K = 64
 // (bf16x_split_bytes(rows, 64, np)), and with ntop > 0 the FP32 update

@@ -199,7 +199,8 @@ mg_status_t sgemm_auto(mg_handle_t h, int ta, int tb, int m, int n, int k, float
     // op(B) columns as split rows: the columns of B (tb = 0) or its rows (tb = 1)
     MG_TRY(bf16x_split<float>(h, ta == 0, A, lda, m, k, np, base));
     MG_TRY(bf16x_split<float>(h, tb != 0, B, ldb, n, k, np, base + as));
-    return bf16x_gemm_presplit(h, np, m, n, k, alpha, base, base + as, beta, C, ldc, err, 0, 0, 0, true, true);
+    return bf16x_gemm_presplit(h, np, m, n, k, alpha, base, base + as, beta, C, ldc, err, 0, 0, 0, true, true, false,
+                               true);
 }
 
 mg_status_t tc_sgemm_error(mg_handle_t h, int* err_out) {
