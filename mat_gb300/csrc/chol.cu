@@ -297,8 +297,11 @@ __global__ void chol_to_lu_lower_kernel(float* __restrict__ A, int lda, int n, c
 // publishes the column (both halves; A's rows above j as zeros) to shared
 // memory, every thread applies the operation to the columns after j that it
 // owns (a window over its four rotated once per 16 columns, so that register
-// indices stay static in a rolled loop), and the owner scales its copy.  A
-// block narrower than 64 (the last one) is padded with the identity.  info:
+// indices stay static in a rolled loop).  The scaling of each column by
+// 1 / sqrt(a_jj) waits until the sweep is over (a column is the source of
+// the operations of its own step only), which keeps the square root off
+// the chain from one column to the next.  A block narrower than 64 (the
+// last one) is padded with the identity.  info:
 // first non-positive pivot (1-based, from col0).  With ntop > 0 the kernel
 // also forms Xt = P G for the first ntop rows P of the block column below
 // (ld ldd, rows ntop .. 63 of Xt zero), into xtop (64 x 64, ld 64), in the
@@ -306,14 +309,15 @@ __global__ void chol_to_lu_lower_kernel(float* __restrict__ A, int lda, int n, c
 // that Xt equals those rows of the block column's solve bit for bit.
 constexpr int CI_NB = 64;
 constexpr int CI_THREADS = 512;
-constexpr int CI_GP = CI_NB + 1;  // pitch of G in shared memory
+constexpr int CI_GP = CI_NB + 4;  // pitch of G (row-major) in shared memory: 16-byte rows
 
 __global__ void __launch_bounds__(CI_THREADS) chol_inv64_kernel(float* __restrict__ D, int ldd, int k, int col0,
                                                               float* __restrict__ G, int* __restrict__ info,
                                                               int ntop, float* __restrict__ xtop) {
     __shared__ float colv[2][2 * CI_NB];
-    __shared__ float gsm[CI_NB * CI_GP];  // G(k, c) at k + CI_GP c
-    __shared__ float psm[CI_NB * CI_NB];  // P(r, k) at r + 64 k
+    __shared__ float piv[CI_NB];                       // a_jj at step j
+    __shared__ __align__(16) float gsm[CI_NB * CI_GP];  // G(k, c) at k * CI_GP + c
+    __shared__ float psm[CI_NB * CI_NB];               // P(r, k) at r + 64 k
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (ntop > 0) {
 #pragma unroll
@@ -346,7 +350,10 @@ __global__ void __launch_bounds__(CI_THREADS) chol_inv64_kernel(float* __restric
             }
             __syncthreads();  // the column is published; the buffer of column j-1 stays readable
             const float d = cv[j];
-            if (threadIdx.x == 0 && j < k && !(d > 0.f)) atomicCAS(info, 0, col0 + j + 1);
+            if (threadIdx.x == 0) {
+                piv[j] = d;
+                if (j < k && !(d > 0.f)) atomicCAS(info, 0, col0 + j + 1);
+            }
             const float rd = __frcp_rn(d);
             float t[4];
 #pragma unroll
@@ -364,17 +371,6 @@ __global__ void __launch_bounds__(CI_THREADS) chol_inv64_kernel(float* __restric
                     for (int q = 0; q < 4; ++q) a[q][m] = fmaf(t[q], ck, a[q][m]);
                 }
             }
-            if (w == jj) {
-                const float sd = sqrtf(d), rs = __frcp_rn(sd);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int i = lane + 32 * (q & 1);
-                    if (q >= 2 || i > j)
-                        a[q][0] *= rs;
-                    else if (i == j)
-                        a[q][0] = sd;
-                }
-            }
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {  // rotate the window: the next group's column first
@@ -383,6 +379,20 @@ __global__ void __launch_bounds__(CI_THREADS) chol_inv64_kernel(float* __restric
             a[q][1] = a[q][2];
             a[q][2] = a[q][3];
             a[q][3] = t0;
+        }
+    }
+    __syncthreads();  // every pivot recorded
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {  // the deferred scaling of column c by 1 / sqrt(a_cc)
+        const int c = w + 16 * m;
+        const float sd = sqrtf(piv[c]), rs = __frcp_rn(sd);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = lane + 32 * (q & 1);
+            if (q >= 2 || i > c)
+                a[q][m] *= rs;
+            else if (i == c)
+                a[q][m] = sd;
         }
     }
 #pragma unroll
@@ -396,7 +406,7 @@ __global__ void __launch_bounds__(CI_THREADS) chol_inv64_kernel(float* __restric
             } else {
                 const float g = i <= c ? a[q][m] : 0.f;
                 G[i + CI_NB * c] = g;
-                gsm[i + CI_GP * c] = g;
+                gsm[i * CI_GP + c] = g;
             }
         }
     }
@@ -410,8 +420,11 @@ __global__ void __launch_bounds__(CI_THREADS) chol_inv64_kernel(float* __restric
 #pragma unroll 4
     for (int kk = 0; kk < CI_NB; ++kk) {
         const float x = psm[r + CI_NB * kk];
+        const float4 g0 = *reinterpret_cast<const float4*>(gsm + kk * CI_GP + c0);
+        const float4 g1 = *reinterpret_cast<const float4*>(gsm + kk * CI_GP + c0 + 4);
+        const float g[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
 #pragma unroll
-        for (int u = 0; u < 8; ++u) acc[u] = fmaf(x, gsm[kk + CI_GP * (c0 + u)], acc[u]);
+        for (int u = 0; u < 8; ++u) acc[u] = fmaf(x, g[u], acc[u]);
     }
 #pragma unroll
     for (int u = 0; u < 8; ++u) xtop[r + CI_NB * (c0 + u)] = acc[u];
