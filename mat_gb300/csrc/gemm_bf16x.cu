@@ -461,15 +461,35 @@ __global__ void __launch_bounds__(256) xlt_split64_kernel(const float* __restric
     float* const os = xs_sm;                      // result (r, c) at r + XS_OP c, after the first product
     const int t = threadIdx.x;
     const int row0 = blockIdx.x * XS_ROWS;
+    const int tx = t & 15, ty = t >> 4;  // rows 4 tx .. 4 tx + 3, columns 4 ty .. 4 ty + 3
+    // every global load of the kernel issued up front: this thread's part of
+    // G, X and Xt, and the 4 x 4 block of C it updates at the end
+    float cv[4][4];
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
-        const int e = t + 256 * u, r = e & 63, c = e >> 6;
-        gs[r + XS_P * c] = __ldg(G + e);
-        xs[e] = row0 + r < rows ? X[(size_t)(row0 + r) + (size_t)c * ldx] : 0.f;
-        if (ntop > 0) xt[e] = __ldg(xtop + e);
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = row0 + 4 * tx + i, c = 4 * ty + j;
+            cv[i][j] = (r < rows && c < ntop) ? C[(size_t)r + (size_t)c * ldx] : 0.f;
+        }
+    {
+        float gv[16], xv[16], tv[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            const int e = t + 256 * u, r = e & 63, c = e >> 6;
+            gv[u] = __ldg(G + e);
+            xv[u] = row0 + r < rows ? X[(size_t)(row0 + r) + (size_t)c * ldx] : 0.f;
+            tv[u] = ntop > 0 ? __ldg(xtop + e) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            const int e = t + 256 * u, r = e & 63, c = e >> 6;
+            gs[r + XS_P * c] = gv[u];
+            xs[e] = xv[u];
+            xt[e] = tv[u];
+        }
     }
     __syncthreads();
-    const int tx = t & 15, ty = t >> 4;  // rows 4 tx .. 4 tx + 3, columns 4 ty .. 4 ty + 3
     float acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -532,14 +552,6 @@ __global__ void __launch_bounds__(256) xlt_split64_kernel(const float* __restric
 #pragma unroll
             for (int i = 0; i < 4; ++i) acc[i][j] = fmaf(xr[i], tr[j], acc[i][j]);
     }
-    float cv[4][4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int r = row0 + 4 * tx + i, c = 4 * ty + j;
-            cv[i][j] = (r < rows && c < ntop) ? C[(size_t)r + (size_t)c * ldx] : 0.f;
-        }
 #pragma unroll
     for (int j = 0; j < 4; ++j)
 #pragma unroll
