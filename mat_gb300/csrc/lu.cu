@@ -750,7 +750,7 @@ mg_status_t sgetrf_mixed(mg_handle_t h, int n, float* A, int lda, int* pos, int 
         float* A22 = A + (r + w) + (size_t)(r + w) * lda;
         const int w1 = nb < nt ? nb : nt;  // the next panel's columns
         MG_TRY(bf16x_gemm_presplit(h, nterms, nt, w1, w, -1.0f, L21, splitB, 1.0f, A22, lda, gemm_err, 0,
-                                   (size_t)nt * kp, 0, false, true));  // the next panel: kept in L2
+                                   (size_t)nt * kp, 0, false, true, false, true));  // the next panel: kept in L2
         const bool ov = overlappable(k + 1);
         const void* Brest = (const char*)splitB + (size_t)w1 * kp * 2;
         if (nt > w1 && ov) {

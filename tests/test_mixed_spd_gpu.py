@@ -30,7 +30,9 @@ def fp64_chol_solve(handle, S, B):
     return handle.dpotrs(L, B.clone())
 
 
-@pytest.mark.parametrize("n,nrhs", [(300, 1), (1000, 4), (2500, 3), (4096, 4)])
+# 50: one diagonal block only; 65: a one-row block column; 128: two blocks,
+# no far update; 129: a far update of one row; then ragged last blocks
+@pytest.mark.parametrize("n,nrhs", [(50, 2), (65, 1), (128, 1), (129, 3), (300, 1), (1000, 4), (2500, 3), (4096, 4)])
 def test_mixed_spd_gram(handle, n, nrhs):
     S = colmajor(n, n)
     handle.gen_spd_gram(S, 1)
