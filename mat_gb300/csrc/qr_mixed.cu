@@ -428,65 +428,92 @@ __global__ void qr_gsum_kernel(const float* __restrict__ gpart, int nparts, floa
 }
 
 // T (w x w, upper, fp32, ld QB) of H_0 ... H_{w-1} = I - V T V^T from
-// G = V^T V: T(c,c) = tau_c, T(0:c, c) = -tau_c T(0:c, 0:c) G(0:c, c), in
-// fp32 (T is an fp32 factor; an FP64 recurrence here cost ~1 ms per panel:
-// up to 127 dependent FP64 FMAs per column at ~70 cycles each).  One CTA of
-// QB threads; T's columns in dynamic shared memory.
-__global__ void __launch_bounds__(2 * QB) qr_tfactor_kernel(const float* __restrict__ G, int ldg,
-                                                             const double* __restrict__ tau, int w,
-                                                             float* __restrict__ T) {
-    extern __shared__ float t[];  // [QB][QB + 1]: t[r * (QB + 1) + c], then G's columns [QB][QB + 1]
-    __shared__ float taus[QB];
-    constexpr int LD = QB + 1;
-    float* const gs = t + QB * LD;  // G(k, c) at gs[c * LD + k]
-    const int tid = threadIdx.x;
-    for (int e = tid; e < QB * LD; e += blockDim.x) t[e] = 0.f;
-    if (tid < w) taus[tid] = (float)tau[tid];
-    {  // G's w x w block, all loads of a thread in flight together
-        constexpr int PER = QB * QB / (2 * QB);
+// G = V^T V and the taus.  LAPACK's recurrence T(c,c) = tau_c, T(0:c, c) =
+// -tau_c T(0:c, 0:c) G(0:c, c) says that T is the inverse of the upper
+// triangular U = striu(G) + diag(1 / tau) (column c of T U is e_c).  The
+// kernel inverts U right-looking, by the column operations that turn U
+// into I applied to I: with C_j the j-th column before scaling (T_j =
+// tau_j C_j), C_k = e_k - sum_{j<k} tau_j G(j, k) C_j, so once column j is
+// final every later column subtracts tau_j G(j, k) times it; a rank-1 step
+// per column, one CTA barrier each, instead of a dot-product chain per
+// column.  512 threads hold the 128 x 128 C in registers: warp wi the
+// columns wi, wi+16, .., lane l the rows l, l+32, l+64, l+96; the columns
+// sit in a window rotated once per 16 steps (static register indices in a
+// rolled loop), and the owner of column j publishes it to shared memory.
+// The scaling by tau waits until the end.  fp32 throughout (T is an fp32
+// factor; an FP64 recurrence here cost ~1 ms per panel).  Columns and rows
+// from w on are zero.
+constexpr int TF_THREADS = 512;
+
+__global__ void __launch_bounds__(TF_THREADS) qr_tfactor_kernel(const float* __restrict__ G, int ldg,
+                                                                const double* __restrict__ tau, int w,
+                                                                float* __restrict__ T) {
+    extern __shared__ float ms[];  // tau_j G(j, k) at ms[k * QB + j], j < k < w
+    __shared__ float colv[2][QB];
+    const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    {
+        constexpr int PER = QB * QB / TF_THREADS;
         float g[PER];
 #pragma unroll
         for (int u = 0; u < PER; ++u) {
-            const int e = tid + u * 2 * QB, k = e % QB, c = e / QB;
-            g[u] = (k < w && c < w) ? G[k + (size_t)c * ldg] : 0.f;
+            const int e = threadIdx.x + u * TF_THREADS, j = e % QB, k = e / QB;
+            g[u] = (j < k && k < w) ? (float)tau[j] * G[j + (size_t)k * ldg] : 0.f;
         }
 #pragma unroll
-        for (int u = 0; u < PER; ++u) {
-            const int e = tid + u * 2 * QB, k = e % QB, c = e / QB;
-            gs[c * LD + k] = g[u];
-        }
+        for (int u = 0; u < PER; ++u) ms[threadIdx.x + u * TF_THREADS] = g[u];
     }
+    float a[4][8];  // C(lane + 32 q, column of window position p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int p = 0; p < 8; ++p) a[q][p] = (lane + 32 * q == wi + 16 * p) ? 1.f : 0.f;
     __syncthreads();
-    // column c: T(r, c) = -tau_c sum_{k = r}^{c-1} T(r, k) G(k, c) for r < c; two
-    // threads per row (the halves of k), each with four partial sums, added
-    // in a fixed order
-    const int r = tid >> 1, hf = tid & 1;
-    for (int c = 0; c < w; ++c) {
-        float s = 0.f;
-        if (r < c) {
-            const float* gc = gs + c * LD;
-            const float* tr = t + r * LD;
-            const int mid = r + (c - r) / 2;
-            const int ka = hf ? mid : r, kb = hf ? c : mid;
-            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-            int k = ka;
-            for (; k + 3 < kb; k += 4) {
-                s0 = fmaf(tr[k], gc[k], s0);
-                s1 = fmaf(tr[k + 1], gc[k + 1], s1);
-                s2 = fmaf(tr[k + 2], gc[k + 2], s2);
-                s3 = fmaf(tr[k + 3], gc[k + 3], s3);
+#pragma unroll 1
+    for (int jm = 0; jm < 8; ++jm) {
+        const int nlive = 7 - jm;  // window positions 1 .. nlive hold columns after this group of 16
+#pragma unroll
+        for (int jj = 0; jj < 16; ++jj) {
+            const int j = 16 * jm + jj;
+            float* const cv = colv[jj & 1];
+            if (wi == jj) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) cv[lane + 32 * q] = a[q][0];
             }
-            for (; k < kb; ++k) s0 = fmaf(tr[k], gc[k], s0);
-            s = (s0 + s1) + (s2 + s3);
+            __syncthreads();  // column j published; the buffer of column j-1 stays readable
+            float cj[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) cj[q] = cv[lane + 32 * q];
+            if (wi > jj) {  // window position 0 is column wi + 16 jm, after j
+                const float mk = ms[(wi + 16 * jm) * QB + j];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) a[q][0] = fmaf(-mk, cj[q], a[q][0]);
+            }
+#pragma unroll
+            for (int p = 1; p < 8; ++p) {
+                if (p <= nlive) {
+                    const float mk = ms[(wi + 16 * (jm + p)) * QB + j];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) a[q][p] = fmaf(-mk, cj[q], a[q][p]);
+                }
+            }
         }
-        const float other = __shfl_xor_sync(0xffffffffu, s, 1);
-        if (r < c && hf == 0) t[r * LD + c] = -taus[c] * (s + other);
-        if (tid == 2 * c) t[c * LD + c] = taus[c];
-        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {  // rotate the window: the next group's column first
+            const float t0 = a[q][0];
+#pragma unroll
+            for (int p = 0; p < 7; ++p) a[q][p] = a[q][p + 1];
+            a[q][7] = t0;
+        }
     }
-    for (int e = tid; e < QB * QB; e += blockDim.x) {
-        const int rr = e % QB, cc = e / QB;
-        T[e] = (rr < w && cc < w) ? t[rr * LD + cc] : 0.f;
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+        const int c = wi + 16 * p;
+        const float tc = c < w ? (float)tau[c] : 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = lane + 32 * q;
+            T[i + (size_t)QB * c] = (i < w && c < w && i <= c) ? tc * a[q][p] : 0.f;
+        }
     }
 }
 
@@ -710,7 +737,7 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(qr_panel_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           h->max_smem_optin - 4096));
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(qr_tfactor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(2 * QB * (QB + 1) * sizeof(float))));
+                                          (int)(QB * QB * sizeof(float))));
     // the cluster form when a 16-CTA cluster's shared memory holds the panel
     const size_t qc_static = sizeof(QcShared) + 2048;  // + the other static shared arrays
     const size_t qc_max_dyn = (size_t)h->max_smem_optin > qc_static ? (size_t)h->max_smem_optin - qc_static : 0;
@@ -787,7 +814,7 @@ mg_status_t sgeqrf_mixed(mg_handle_t h, int m, int n, float* A, int lda, double*
         float* Tb = T + (size_t)(j0 / QB) * QB * QB;
         qr_gsum_kernel<<<QB * QB / 256, 256, 0, st>>>(gpart, nparts, G);
         MG_TRY(post_launch(h, "qr_gsum_kernel"));
-        qr_tfactor_kernel<<<1, 2 * QB, 2 * QB * (QB + 1) * sizeof(float), st>>>(G, QB, tau + j0, w, Tb);
+        qr_tfactor_kernel<<<1, TF_THREADS, QB * QB * sizeof(float), st>>>(G, QB, tau + j0, w, Tb);
         MG_TRY(post_launch(h, "qr_tfactor_kernel"));
         const int nt = n - j0 - w;
         if (nt > 0) {  // R2 -= V (T^T (V^T R2))
