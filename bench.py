@@ -557,9 +557,18 @@ def e2e_run(h, A, B, n, nrhs, steps, barrier, warmup=3):
     torch.cuda.empty_cache()
     return {"value": pipe_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "pipelined": True, "step_ms": [round(x, 2) for x in pipe_ms],
+            "median_step_ms": round(_median(pipe_ms), 2),
             "serial": {"value": serial_s, "step_ms": [round(x, 2) for x in serial_ms],
+                       "median_step_ms": round(_median(serial_ms), 2),
                        "note": "H2D, solve, D2H back to back per step: the latency of one solve from host memory"},
+            "note": "value is the mean over the timed steps, slow host copies included; median_step_ms beside it",
             "h2d_ms": h2d_ms, "h2d_gbs": 8 * n * n / (h2d_ms * 1e6)}
+
+
+def _median(xs):
+    v = sorted(xs)
+    m = len(v) // 2
+    return v[m] if len(v) % 2 else 0.5 * (v[m - 1] + v[m])
 
 
 def run_ours(args):
