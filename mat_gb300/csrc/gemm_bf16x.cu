@@ -437,31 +437,35 @@ __global__ void split_cols_kernel(const TIN* __restrict__ B, int ldb, int K, int
 // K = 64 operand (parts[p][row][64]), and, with ntop > 0, the update of the
 // next block column C (rows x ntop, ld ldx) -= X Xt^T in FP32, Xt (64 x 64,
 // ld 64; rows ntop .. zero) being the first ntop rows of the result, formed
-// beforehand by the diagonal block's kernel.  One CTA per 64 rows; each
-// thread 4 rows x 4 columns of both products, over the X tile, G (pitch 65
+// beforehand by the diagonal block's kernel.  One CTA of 128 threads per
+// 32 rows (two CTAs per SM at 8128 rows); each thread 4 rows x 4 columns of
+// both products, over the X tile, G (pitch 65
 // words: the two column groups of a warp read different banks) and Xt
 // staged in shared memory; the result staged again (column-major, pitch 68
 // for 16-byte accesses) for the coalesced column stores of X, the 16-byte
 // row stores of the terms and the second product.  This is the block-column
 // solve X := X L^{-T} of the mixed SPD factorization as a product by the
 // diagonal block's inverse, with the look-ahead part of the trailing update.
-constexpr int XS_ROWS = 64;
+constexpr int XS_ROWS = 32;              // rows per CTA
+constexpr int XS_T = XS_ROWS * 4;         // threads: 4 x 4 outputs each over XS_ROWS x 64
+constexpr int XS_TX = XS_ROWS / 4;        // row groups
 constexpr int XS_P = 65;
-constexpr int XS_OP = 68;
+constexpr int XS_OP = XS_ROWS + 4;        // column pitch of the staged result (16-byte aligned)
 constexpr size_t XS_SMEM = (size_t)(XS_P * 64 + 64 * XS_ROWS + 64 * 64) * sizeof(float);
+static_assert(XS_OP * 64 <= XS_P * 64 + 64 * XS_ROWS, "the staged result fits over G and the X tile");
 
-__global__ void __launch_bounds__(256) xlt_split64_kernel(const float* __restrict__ G, float* __restrict__ X, int ldx,
+__global__ void __launch_bounds__(XS_T) xlt_split64_kernel(const float* __restrict__ G, float* __restrict__ X, int ldx,
                                                           int rows, int np, __nv_bfloat16* __restrict__ out,
                                                           size_t part_stride, const float* __restrict__ xtop,
                                                           int ntop, float* __restrict__ C) {
     extern __shared__ __align__(16) float xs_sm[];
     float* const gs = xs_sm;                      // G(k, c) at k + XS_P c
-    float* const xs = xs_sm + XS_P * 64;          // X(r, k) at r + 64 k
+    float* const xs = xs_sm + XS_P * 64;          // X(r, k) at r + XS_ROWS k
     float* const xt = xs + 64 * XS_ROWS;          // Xt(c, k) at c + 64 k
     float* const os = xs_sm;                      // result (r, c) at r + XS_OP c, after the first product
     const int t = threadIdx.x;
     const int row0 = blockIdx.x * XS_ROWS;
-    const int tx = t & 15, ty = t >> 4;  // rows 4 tx .. 4 tx + 3, columns 4 ty .. 4 ty + 3
+    const int tx = t % XS_TX, ty = t / XS_TX;  // rows 4 tx .. 4 tx + 3, columns 4 ty .. 4 ty + 3
     // every global load of the kernel issued up front: this thread's part of
     // G, X and Xt, and the 4 x 4 block of C it updates at the end
     float cv[4][4];
@@ -473,21 +477,27 @@ __global__ void __launch_bounds__(256) xlt_split64_kernel(const float* __restric
             cv[i][j] = (r < rows && c < ntop) ? C[(size_t)r + (size_t)c * ldx] : 0.f;
         }
     {
-        float gv[16], xv[16], tv[16];
+        constexpr int NG = 64 * 64 / XS_T, NX = XS_ROWS * 64 / XS_T;
+        float gv[NG], xv[NX], tv[NG];
 #pragma unroll
-        for (int u = 0; u < 16; ++u) {
-            const int e = t + 256 * u, r = e & 63, c = e >> 6;
+        for (int u = 0; u < NG; ++u) {
+            const int e = t + XS_T * u;
             gv[u] = __ldg(G + e);
-            xv[u] = row0 + r < rows ? X[(size_t)(row0 + r) + (size_t)c * ldx] : 0.f;
             tv[u] = ntop > 0 ? __ldg(xtop + e) : 0.f;
         }
 #pragma unroll
-        for (int u = 0; u < 16; ++u) {
-            const int e = t + 256 * u, r = e & 63, c = e >> 6;
-            gs[r + XS_P * c] = gv[u];
-            xs[e] = xv[u];
+        for (int u = 0; u < NX; ++u) {
+            const int e = t + XS_T * u, r = e % XS_ROWS, c = e / XS_ROWS;
+            xv[u] = row0 + r < rows ? X[(size_t)(row0 + r) + (size_t)c * ldx] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < NG; ++u) {
+            const int e = t + XS_T * u;
+            gs[(e & 63) + XS_P * (e >> 6)] = gv[u];
             xt[e] = tv[u];
         }
+#pragma unroll
+        for (int u = 0; u < NX; ++u) xs[t + XS_T * u] = xv[u];
     }
     __syncthreads();
     float acc[4][4];
@@ -497,7 +507,7 @@ __global__ void __launch_bounds__(256) xlt_split64_kernel(const float* __restric
         for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
 #pragma unroll 8
     for (int k = 0; k < 64; ++k) {
-        const float4 xv = *reinterpret_cast<const float4*>(xs + 64 * k + 4 * tx);
+        const float4 xv = *reinterpret_cast<const float4*>(xs + XS_ROWS * k + 4 * tx);
         const float xr[4] = {xv.x, xv.y, xv.z, xv.w};
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -513,13 +523,13 @@ __global__ void __launch_bounds__(256) xlt_split64_kernel(const float* __restric
             make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
     __syncthreads();
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
-        const int e = t + 256 * u, r = e & 63, c = e >> 6;
+    for (int u = 0; u < XS_ROWS * 64 / XS_T; ++u) {
+        const int e = t + XS_T * u, r = e % XS_ROWS, c = e / XS_ROWS;
         if (row0 + r < rows) X[(size_t)(row0 + r) + (size_t)c * ldx] = os[r + XS_OP * c];
     }
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
-        const int e = t + 256 * u, r = e & 63, c8 = (e >> 6) * 8;
+    for (int u = 0; u < XS_ROWS * 8 / XS_T; ++u) {
+        const int e = t + XS_T * u, r = e % XS_ROWS, c8 = (e / XS_ROWS) * 8;
         if (row0 + r >= rows) continue;
         uint32_t w0[4], w1[4], w2[4];
 #pragma unroll
@@ -785,7 +795,7 @@ mg_status_t bf16x_xlt_split64(mg_handle_t h, const float* G, float* X, int ldx, 
     static_assert(64 % BK == 0, "a 64-column operand needs no K padding");
     MG_CHECK_CUDA(h, cudaFuncSetAttribute(xlt_split64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)XS_SMEM));
-    xlt_split64_kernel<<<(rows + XS_ROWS - 1) / XS_ROWS, 256, XS_SMEM, h->stream>>>(
+    xlt_split64_kernel<<<(rows + XS_ROWS - 1) / XS_ROWS, XS_T, XS_SMEM, h->stream>>>(
         G, X, ldx, rows, np, (__nv_bfloat16*)out, (size_t)rows * 64, xtop, ntop, C);
     return post_launch(h, "xlt_split64_kernel");
 }
