@@ -149,7 +149,8 @@ template <int NP, bool RED>
 __global__ void __launch_bounds__(THREADS, 1)
     bf16x_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       const __grid_constant__ CUtensorMap tmC, float* __restrict__ C, int ldc, int M, int N, int Kp,
-                      float alpha, float beta, int stream_c, int two_pass, int lower, int* __restrict__ err) {
+                      float alpha, float beta, int stream_c, int two_pass, int lower, int ksplit,
+                      int* __restrict__ err) {
     using CF = Cfg<NP, RED>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -165,8 +166,16 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int num_m = (M + BM - 1) / BM, num_n = (N + BN - 1) / BN;
-    const int total = lower ? lower_tiles(num_m, num_n) : num_m * num_n;
+    const int tiles = lower ? lower_tiles(num_m, num_n) : num_m * num_n;
+    // split-K (RED only): work item t is tile t % tiles over the k-blocks of
+    // slice t / tiles, its product added into C like every other slice's
+    const int total = tiles * ksplit;
     const int kblocks = Kp / BK;
+    auto slice_k = [&](int t, int& kb0, int& nk) {
+        const int sl = t / tiles;
+        kb0 = sl * kblocks / ksplit;
+        nk = (sl + 1) * kblocks / ksplit - kb0;
+    };
     // two_pass (NP >= 2): every k-block's lower-order products first, then
     // a second pass over K for the leading product A_0 B_0 alone, so that
     // the tensor cores' accumulation (which rounds relative to the running
@@ -210,13 +219,15 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
                 int mb, nb;
                 if (lower)
-                    tile_coords_lower(t, num_m, num_n, mb, nb);
+                    tile_coords_lower(t % tiles, num_m, num_n, mb, nb);
                 else
-                    tile_coords(t, num_m, num_n, mb, nb);
-                for (int ks = 0; ks < npass * kblocks && ok; ++ks) {
-                    const int kb = ks % kblocks;
+                    tile_coords(t % tiles, num_m, num_n, mb, nb);
+                int kb0, nk;
+                slice_k(t, kb0, nk);
+                for (int ks = 0; ks < npass * nk && ok; ++ks) {
+                    const int kb = kb0 + ks % nk;
                     // the leading-product pass needs only the terms A_0, B_0
-                    const int nterm = (npass == 2 && ks >= kblocks) ? 1 : NP;
+                    const int nterm = (npass == 2 && ks >= nk) ? 1 : NP;
                     if (!tc::mbar_wait(&empty[stage], phase ^ 1)) {
                         ok = false;
                         break;
@@ -261,7 +272,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
                 tc::tc_fence_after();
                 const uint32_t d = tmem_base + (uint32_t)(buf * BN);
-                for (int ks = 0; ks < npass * kblocks; ++ks) {
+                int kb0, nk;
+                slice_k(t, kb0, nk);
+                for (int ks = 0; ks < npass * nk; ++ks) {
                     if (!tc::mbar_wait(&full[stage], phase) || *(volatile int*)&s_abort) {
                         ok = false;
                         break;
@@ -271,8 +284,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                     // products of this k-block: all (one pass), the lower-order
                     // ones (first pass) or the leading one (second pass); the
                     // leading product is the last of the list
-                    const int p_lo = (npass == 2 && ks >= kblocks) ? CF::NPROD - 1 : 0;
-                    const int p_hi = (npass == 2 && ks < kblocks) ? CF::NPROD - 1 : CF::NPROD;
+                    const int p_lo = (npass == 2 && ks >= nk) ? CF::NPROD - 1 : 0;
+                    const int p_hi = (npass == 2 && ks < nk) ? CF::NPROD - 1 : CF::NPROD;
 #pragma unroll
                     for (int p = 0; p < CF::NPROD; ++p) {
                         if (p < p_lo || p >= p_hi) continue;
@@ -318,9 +331,9 @@ __global__ void __launch_bounds__(THREADS, 1)
             tc::tc_fence_after();
             int mb, nb;
             if (lower)
-                tile_coords_lower(t, num_m, num_n, mb, nb);
+                tile_coords_lower(t % tiles, num_m, num_n, mb, nb);
             else
-                tile_coords(t, num_m, num_n, mb, nb);
+                tile_coords(t % tiles, num_m, num_n, mb, nb);
             const int row = mb * BM + row_in_tile;
             const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN);
             if constexpr (RED) {
@@ -733,29 +746,30 @@ bool make_cmap(CUtensorMap* map, float* C, int ldc, int M, int N) {
 template <int NP>
 mg_status_t launch_gemm_np(mg_handle_t h, const CUtensorMap& ma, const CUtensorMap& mb, float* C, int ldc, int M,
                            int N, int Kp, float alpha, float beta, int* err, int max_ctas, int stream_c,
-                           int two_pass, int lower, bool red_epi) {
+                           int two_pass, int lower, bool red_epi, int ksplit) {
     const int num_m = (M + BM - 1) / BM, num_n = (N + BN - 1) / BN;
-    const int tiles = lower ? lower_tiles(num_m, num_n) : num_m * num_n;
+    const int tiles = (lower ? lower_tiles(num_m, num_n) : num_m * num_n) * ksplit;
     const int cap = max_ctas > 0 && max_ctas < h->num_sms ? max_ctas : h->num_sms;
     const int grid = tiles < cap ? tiles : cap;
     CUtensorMap mc;
     // the TMA-reduction epilogue when asked for (beta = 1, C 16-byte
     // aligned, ldc a multiple of 4 floats)
-    const bool red = red_epi && beta == 1.f && ((uintptr_t)C & 15) == 0 && (ldc & 3) == 0 &&
+    const bool red = (red_epi || ksplit > 1) && beta == 1.f && ((uintptr_t)C & 15) == 0 && (ldc & 3) == 0 &&
                      make_cmap(&mc, C, ldc, M, N);
+    if (ksplit > 1 && !red) return mg::fail(h, MG_ERR_ARG, "split GEMM: split-K needs beta = 1 and an aligned C");
     if (red) {
         auto kern = bf16x_gemm_kernel<NP, true>;
         MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)Cfg<NP, true>::SMEM));
         kern<<<grid, THREADS, Cfg<NP, true>::SMEM, h->stream>>>(ma, mb, mc, C, ldc, M, N, Kp, alpha, beta, stream_c,
-                                                                two_pass, lower, err);
+                                                                two_pass, lower, ksplit, err);
     } else {
         std::memset(&mc, 0, sizeof(mc));
         auto kern = bf16x_gemm_kernel<NP, false>;
         MG_CHECK_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)Cfg<NP, false>::SMEM));
         kern<<<grid, THREADS, Cfg<NP, false>::SMEM, h->stream>>>(ma, mb, mc, C, ldc, M, N, Kp, alpha, beta, stream_c,
-                                                                 two_pass, lower, err);
+                                                                 two_pass, lower, 1, err);
     }
     return mg::post_launch(h, "bf16x_gemm_kernel");
 }
@@ -818,9 +832,10 @@ int bf16x_kpad(int K) { return (K + BK - 1) / BK * BK; }
 mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, float alpha, const void* Asplit,
                                 const void* Bsplit, float beta, float* C, int ldc, int* err, size_t a_term,
                                 size_t b_term, int max_ctas, bool stream_c, bool two_pass, bool lower,
-                                bool red_epi) {
+                                bool red_epi, int ksplit) {
     if (M == 0 || N == 0) return MG_OK;
     if (lower && M != N) return fail(h, MG_ERR_ARG, "split GEMM: lower mode needs a square C (M=%d N=%d)", M, N);
+    if (ksplit < 1 || ksplit > (K + BK - 1) / BK) return fail(h, MG_ERR_ARG, "split GEMM: bad split-K %d", ksplit);
     const int Kp = (K + BK - 1) / BK * BK;
     if (!a_term) a_term = (size_t)M * Kp;
     if (!b_term) b_term = (size_t)N * Kp;
@@ -835,11 +850,11 @@ mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, floa
     ProfScope prof(h, "gemm_bf16x", frac * 2.0 * M * N * (double)Kp * nprod,
                    frac * (beta == 0.f ? 4.0 : 8.0) * M * N + 2.0 * np * (double)(M + N) * Kp);
     switch (np) {
-        case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, 0, lower, red_epi);
+        case 1: return launch_gemm_np<1>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, 0, lower, red_epi, ksplit);
         case 2:
-            return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass, lower, red_epi);
+            return launch_gemm_np<2>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass, lower, red_epi, ksplit);
         default:
-            return launch_gemm_np<3>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass, lower, red_epi);
+            return launch_gemm_np<3>(h, ma, mb, C, ldc, M, N, Kp, alpha, beta, err, max_ctas, stream_c, two_pass, lower, red_epi, ksplit);
     }
 }
 

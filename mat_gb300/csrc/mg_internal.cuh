@@ -180,11 +180,13 @@ mg_status_t bf16x_split(mg_handle_t h, bool a_side, const TIN* X, int ldx, int r
 // 4): the epilogue adds alpha * A B into C by TMA reductions from shared
 // memory instead of loading C into registers; faster for a C that streams
 // through HBM, but its L2 traffic slowed a latency-bound kernel running
-// beside it (the LU's panel beside its far update).
+// beside it (the LU's panel beside its far update).  ksplit > 1 (needs
+// beta == 1 and the red_epi conditions): K is cut into ksplit slices, each
+// work item one tile over one slice, every slice's product added into C.
 mg_status_t bf16x_gemm_presplit(mg_handle_t h, int np, int M, int N, int K, float alpha, const void* Asplit,
                                 const void* Bsplit, float beta, float* C, int ldc, int* err, size_t a_term = 0,
                                 size_t b_term = 0, int max_ctas = 0, bool stream_c = true, bool two_pass = false,
-                                bool lower = false, bool red_epi = false);
+                                bool lower = false, bool red_epi = false, int ksplit = 1);
 // X (rows x 64, ld ldx) := X G (G: 64 x 64, column-major, ld 64) in FP32,
 // the np split terms of the result as an operand with K = 64
 // (bf16x_split_bytes(rows, 64, np)), and with ntop > 0 the FP32 update

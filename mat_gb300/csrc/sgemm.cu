@@ -199,6 +199,23 @@ mg_status_t sgemm_auto(mg_handle_t h, int ta, int tb, int m, int n, int k, float
     // op(B) columns as split rows: the columns of B (tb = 0) or its rows (tb = 1)
     MG_TRY(bf16x_split<float>(h, ta == 0, A, lda, m, k, np, base));
     MG_TRY(bf16x_split<float>(h, tb != 0, B, ldb, n, k, np, base + as));
+    // Few output tiles over a long K (the mixed QR's V^T C: 128 rows): split
+    // K so that the whole GPU works, each slice adding into C (cleared first
+    // when beta = 0), with at least 8 k-blocks of 32 per slice
+    const int tiles = ((m + 127) / 128) * ((n + 255) / 256), kblk = (k + 31) / 32;
+    int ksplit = 1;
+    if ((beta == 0.f || beta == 1.f) && ((uintptr_t)C & 15) == 0 && (ldc & 3) == 0 && 2 * tiles <= h->num_sms) {
+        ksplit = h->num_sms / tiles;
+        if (ksplit > kblk / 8) ksplit = kblk / 8;
+        if (ksplit < 2) ksplit = 1;
+    }
+    if (ksplit > 1) {
+        if (beta == 0.f)
+            MG_CHECK_CUDA(h, cudaMemset2DAsync(C, (size_t)ldc * sizeof(float), 0, (size_t)m * sizeof(float), n,
+                                               h->stream));
+        return bf16x_gemm_presplit(h, np, m, n, k, alpha, base, base + as, 1.0f, C, ldc, err, 0, 0, 0, true, true,
+                                   false, true, ksplit);
+    }
     return bf16x_gemm_presplit(h, np, m, n, k, alpha, base, base + as, beta, C, ldc, err, 0, 0, 0, true, true, false,
                                true);
 }
