@@ -187,7 +187,7 @@ mg_status_t ensure_tcws(mg_handle_t h, int slot, size_t bytes) {
 
 mg_status_t sgemm_auto(mg_handle_t h, int ta, int tb, int m, int n, int k, float alpha, const float* A, int lda,
                        const float* B, int ldb, float beta, float* C, int ldc, int tri) {
-    if (k < 32 || (double)m * n * k < (double)(1 << 27) || alpha == 0.f)
+    if (k < 32 || (double)m * n * k < (double)(1 << 24) || alpha == 0.f)
         return sgemm_launch(h, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri);
     constexpr int np = 3;
     const size_t as = align_up(bf16x_split_bytes(m, k, np), 1024), bs = align_up(bf16x_split_bytes(n, k, np), 1024);
